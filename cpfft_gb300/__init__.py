@@ -1,0 +1,211 @@
+"""GB300 finite-strain FFT crystal-plasticity hot path (CPFFT drop-in).
+
+The product is the C-ABI shared library ``_build/libcpfft_gb300.so`` (declared in
+include/cpfft_gpu.h).  This module is a thin ctypes mirror of the reference's routines
+for Python callers and tests: :class:`Solver` exposes ``drive_eps_sig``, ``G_K_dF``,
+``fftPcg``, ``tangent_homo`` and one ``FFT_nr3`` load step with the reference's
+argument meaning and error behaviour (a negative status raises :class:`CpfftError`).
+There is no CPU fallback: loading fails loudly when the library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
+HIST_WORDS = 23
+
+G_REF_SHIFT, G_CENTERED = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+STATUS = {
+    0: "ok", 1: "local mm10 fallback", -1: "CG reached maxIter", -2: "Newton maxIter",
+    -3: "stress BC maxIter", -4: "singular mixed-BC system", -5: "bad argument",
+    -6: "CUDA error", -7: "not initialised", -8: "improper CG tolerance",
+    -9: "out of device memory", -10: "non-finite residual",
+}
+
+
+class CpfftError(RuntimeError):
+    def __init__(self, code, where, detail):
+        super().__init__(f"{where}: {STATUS.get(code, code)} ({code}): {detail}")
+        self.code = code
+
+
+class Crystal(ctypes.Structure):
+    """``cpfft_crystal`` of include/cpfft_gpu.h."""
+
+    _fields_ = [
+        ("slip_type", ctypes.c_int), ("elastic_type", ctypes.c_int),
+        ("e", ctypes.c_double), ("nu", ctypes.c_double), ("mu", ctypes.c_double),
+        ("C11", ctypes.c_double), ("C12", ctypes.c_double), ("C13", ctypes.c_double),
+        ("C33", ctypes.c_double), ("C44", ctypes.c_double), ("C55", ctypes.c_double),
+        ("h_type", ctypes.c_int), ("harden_n", ctypes.c_double),
+        ("tau_y", ctypes.c_double), ("tau_v", ctypes.c_double),
+        ("theta_0", ctypes.c_double), ("voce_m", ctypes.c_double),
+        ("gamma_bar", ctypes.c_double), ("iD_v", ctypes.c_double),
+        ("alter_mode", ctypes.c_int),
+        ("atol", ctypes.c_double), ("atol1", ctypes.c_double),
+        ("rtol", ctypes.c_double), ("rtol1", ctypes.c_double),
+        ("miter", ctypes.c_int), ("exact_j22", ctypes.c_int),
+    ]
+
+
+class Stats(ctypes.Structure):
+    """``cpfft_stats`` of include/cpfft_gpu.h."""
+
+    _fields_ = [
+        ("newton_iters", ctypes.c_int), ("nbc_iters", ctypes.c_int),
+        ("cg_solves", ctypes.c_int), ("cg_iters", ctypes.c_int),
+        ("stress_updates", ctypes.c_int), ("local_fallbacks", ctypes.c_int),
+        ("local_iters", ctypes.c_longlong),
+        ("res_fft", ctypes.c_double), ("res_pbar", ctypes.c_double),
+        ("res_equil", ctypes.c_double),
+        ("t_pcg", ctypes.c_double), ("t_sigeps", ctypes.c_double),
+        ("t_total", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+# every exported symbol and its signature
+_D, _I, _P = ctypes.c_double, ctypes.c_int, ctypes.POINTER
+_DP, _IP = _P(_D), _P(_I)
+SIGNATURES = {
+    "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
+    "cpfft_set_mode": (_I, [_I, _I]),
+    "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
+    "cpfft_green_apply": (_I, [_DP, _DP, _I]),
+    "cpfft_set_K4": (_I, [_DP]),
+    "cpfft_cg": (_I, [_DP, _DP, _D, _IP]),
+    "cpfft_tangent_homo": (_I, [_D, _DP]),
+    "cpfft_nr3_step": (_I, [_I, _DP, _IP, _D, _D, _I, _DP, _P(Stats)]),
+    "cpfft_nr3_begin": (_I, [_D]),
+    "cpfft_sync_to_host": (_I, [_DP, _DP, _DP]),
+    "cpfft_commit_step": (_I, []),
+    "cpfft_set_F": (_I, [_DP, _DP]),
+    "cpfft_finalize": (None, []),
+    "cpfft_last_error": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load the C-ABI library (never a CPU substitute)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; "
+                "g.build()'` (the GPU path has no fallback)")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    if a is None:
+        return None
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(_DP)
+
+
+def _check(code, where):
+    if code < 0:
+        raise CpfftError(code, where, load_library().cpfft_last_error().decode())
+    return code
+
+
+def crystal_struct(crystals):
+    arr = (Crystal * len(crystals))()
+    for k, c in enumerate(crystals):
+        for name, _ in Crystal._fields_:
+            setattr(arr[k], name, c[name])
+    return arr
+
+
+class Solver:
+    """Device-resident RVE.  Fields are numpy arrays shaped (9, N3) / (81, N3), i.e. the
+    memory of the reference's column-major (N3, 9) / (N3, 81) module arrays."""
+
+    def __init__(self, N, mat_list, kocks_deg, crystals, tstep, g_mapping=G_REF_SHIFT,
+                 precision=PREC_FP64):
+        L = load_library()
+        self.N, self.N3 = N, N ** 3
+        self._crys = crystal_struct(crystals)
+        ml = np.ascontiguousarray(mat_list, dtype=np.int32)
+        ka = np.ascontiguousarray(np.asarray(kocks_deg, dtype=np.float64).reshape(3, self.N3))
+        _check(L.cpfft_init(N, ml.ctypes.data_as(_IP), _dp(ka), self._crys, len(crystals),
+                            tstep, g_mapping), "cpfft_init")
+        if precision != PREC_FP64:
+            self.set_mode(precision)
+
+    def close(self):
+        load_library().cpfft_finalize()
+
+    def set_mode(self, precision, warm_start=0):
+        _check(load_library().cpfft_set_mode(precision, warm_start), "cpfft_set_mode")
+
+    # --- mirror of the reference routines ------------------------------------------
+    def drive_eps_sig(self, step, it, Fn=None, Fn1=None, want_P=True, want_K4=False):
+        P = np.zeros((9, self.N3)) if want_P else None
+        K = np.zeros((81, self.N3)) if want_K4 else None
+        rc = _check(load_library().cpfft_stress_update(step, it, _dp(Fn), _dp(Fn1), _dp(P),
+                                                       _dp(K)), "drive_eps_sig")
+        return P, K, rc
+
+    def G_K_dF(self, x, flgK=True):
+        y = np.zeros((9, self.N3))
+        _check(load_library().cpfft_green_apply(_dp(np.ascontiguousarray(x)), _dp(y),
+                                                int(flgK)), "G_K_dF")
+        return y
+
+    def set_K4(self, K4):
+        _check(load_library().cpfft_set_K4(_dp(np.ascontiguousarray(K4))), "set_K4")
+
+    def fftPcg(self, b, tol):
+        x = np.zeros((9, self.N3))
+        its = ctypes.c_int(0)
+        rc = load_library().cpfft_cg(_dp(np.ascontiguousarray(b)), _dp(x), tol,
+                                     ctypes.byref(its))
+        _check(rc, "fftPcg")
+        return x, its.value
+
+    def tangent_homo(self, tol):
+        C = np.zeros(81)
+        _check(load_library().cpfft_tangent_homo(tol, _dp(C)), "tangent_homo")
+        return C.reshape(9, 9).T.copy()  # C[i, j] = C_homo(i, j) of the reference
+
+    def nr3_begin(self, tolPCG):
+        _check(load_library().cpfft_nr3_begin(tolPCG), "FFT_nr3 start")
+
+    def nr3_step(self, step, BC, isNBC, tolNR, tolPCG, maxIter):
+        Pbar = np.zeros(9)
+        st = Stats()
+        bc = np.ascontiguousarray(BC, dtype=np.float64)
+        nb = np.ascontiguousarray(isNBC, dtype=np.int32)
+        rc = _check(load_library().cpfft_nr3_step(step, _dp(bc), nb.ctypes.data_as(_IP), tolNR,
+                                                  tolPCG, maxIter, _dp(Pbar),
+                                                  ctypes.byref(st)), "FFT_nr3 step")
+        return rc, Pbar, st.as_dict()
+
+    def fields(self, history=False):
+        F = np.zeros((9, self.N3))
+        P = np.zeros((9, self.N3))
+        H = np.zeros((HIST_WORDS, self.N3)) if history else None
+        _check(load_library().cpfft_sync_to_host(_dp(F), _dp(P), _dp(H)), "sync_to_host")
+        return (F, P, H) if history else (F, P)
+
+    def commit(self):
+        _check(load_library().cpfft_commit_step(), "commit_step")
+
+    def set_F(self, Fn=None, Fn1=None):
+        _check(load_library().cpfft_set_F(_dp(Fn), _dp(Fn1)), "set_F")

@@ -1,0 +1,866 @@
+// api.cu -- the C-ABI of include/cpfft_gpu.h: device context, material set-up, and the
+// host-side control of the resident Newton-Krylov loop (FFT_nr3 / fftPcg /
+// tangent_homo / NBC_update of src/FFT_nr3.f and src/tangent_homo.f).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_green.cuh"
+#include "krylov.cuh"
+
+static char g_err[512] = "";
+void cpfft_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+namespace {
+
+// ---- host-side material set-up (setup_mm10_rknstr, src/drive_eps_sig.f:537-1002;
+//      finalize_new_crystal, src/mod_crystals.f:414-1931) --------------------------
+const int VI[6] = {0, 1, 2, 0, 1, 0};
+const int VJ[6] = {0, 1, 2, 1, 2, 2};
+
+void fcc_geometry(double b[12][3], double n[12][3]) {
+  const double f = 1.0 / std::sqrt(2.0), g = 1.0 / std::sqrt(3.0);
+  // {111}<110>: direction and normal of each system, in the reference's order
+  const double B[12][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f}, {f, 0, f}, {f, -f, 0},
+                           {0, -f, f}, {-f, 0, -f}, {f, f, 0}, {0, f, f}, {f, 0, -f}, {-f, -f, 0}};
+  const double Nn[12][3] = {{g, g, g},  {g, g, g},  {g, g, g},  {-g, -g, g}, {-g, -g, g}, {-g, -g, g},
+                            {-g, g, g}, {-g, g, g}, {-g, g, g}, {g, -g, g},  {g, -g, g},  {g, -g, g}};
+  memcpy(b, B, sizeof(B));
+  memcpy(n, Nn, sizeof(Nn));
+}
+
+bool invert6(const double a[36], double out[36]) {
+  double m[6][12];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 12; j++) m[i][j] = j < 6 ? a[6 * i + j] : (j - 6 == i ? 1.0 : 0.0);
+  for (int k = 0; k < 6; k++) {
+    int p = k;
+    for (int i = k + 1; i < 6; i++)
+      if (std::fabs(m[i][k]) > std::fabs(m[p][k])) p = i;
+    if (m[p][k] == 0.0) return false;
+    for (int j = 0; j < 12; j++) std::swap(m[k][j], m[p][j]);
+    double inv = 1.0 / m[k][k];
+    for (int j = 0; j < 12; j++) m[k][j] *= inv;
+    for (int i = 0; i < 6; i++)
+      if (i != k) {
+        double f = m[i][k];
+        for (int j = 0; j < 12; j++) m[i][j] -= f * m[k][j];
+      }
+  }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) out[6 * i + j] = m[i][j + 6];
+  return true;
+}
+
+// stiffness in the crystal frame (src/mod_crystals.f:1796-1880)
+bool crystal_stiffness(const cpfft_crystal& p, double C0[36]) {
+  memset(C0, 0, 36 * sizeof(double));
+  if (p.elastic_type == 3) {
+    C0[0] = p.C11; C0[1] = p.C12; C0[2] = p.C13;
+    C0[6] = p.C12; C0[7] = p.C11; C0[8] = p.C13;
+    C0[12] = p.C13; C0[13] = p.C13; C0[14] = p.C33;
+    C0[21] = p.C44; C0[28] = p.C55; C0[35] = p.C55;
+    return true;
+  }
+  if (p.elastic_type != 1 && p.elastic_type != 2) return false;
+  double flex[36] = {0};
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) flex[6 * i + j] = i == j ? 1.0 / p.e : -p.nu / p.e;
+  double sh = p.elastic_type == 1 ? 2.0 * (1.0 + p.nu) / p.e : 1.0 / p.mu;
+  for (int i = 3; i < 6; i++) flex[6 * i + i] = sh;
+  return invert6(flex, C0);
+}
+
+void kocks_rotation(const double ang[3], double r[9]) {  // src/mm10_a.f:1287-1345
+  const double pi = 3.141592653589793;
+  double psi = ang[0] * pi / 180.0, th = ang[1] * pi / 180.0, phi = ang[2] * pi / 180.0;
+  r[0] = -sin(psi) * sin(phi) - cos(psi) * cos(phi) * cos(th);
+  r[1] = cos(psi) * sin(phi) - sin(psi) * cos(phi) * cos(th);
+  r[2] = cos(phi) * sin(th);
+  r[3] = sin(psi) * cos(phi) - cos(psi) * sin(phi) * cos(th);
+  r[4] = -cos(psi) * cos(phi) - sin(psi) * sin(phi) * cos(th);
+  r[5] = sin(phi) * sin(th);
+  r[6] = cos(psi) * sin(th);
+  r[7] = sin(psi) * sin(th);
+  r[8] = cos(th);
+}
+
+void orientation_record(const double C0[36], const double bb[12][3], const double nn[12][3],
+                        const double ang[3], OriRec& o) {
+  double g[9], tr[9];
+  kocks_rotation(ang, g);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) tr[3 * i + j] = g[3 * j + i];
+  for (int s = 0; s < 12; s++) {
+    double bs[3], ns[3];
+    for (int i = 0; i < 3; i++) {
+      bs[i] = tr[3 * i] * bb[s][0] + tr[3 * i + 1] * bb[s][1] + tr[3 * i + 2] * bb[s][2];
+      ns[i] = tr[3 * i] * nn[s][0] + tr[3 * i + 1] * nn[s][1] + tr[3 * i + 2] * nn[s][2];
+    }
+    double A[3][3];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) A[i][j] = bs[i] * ns[j];
+    for (int a = 0; a < 6; a++) {
+      double sym = 0.5 * (A[VI[a]][VJ[a]] + A[VJ[a]][VI[a]]);
+      o.ms[6 * s + a] = a < 3 ? sym : 2.0 * sym;
+    }
+    o.qs[3 * s + 0] = 0.5 * (A[1][2] - A[2][1]);
+    o.qs[3 * s + 1] = 0.5 * (A[0][2] - A[2][0]);
+    o.qs[3 * s + 2] = 0.5 * (A[0][1] - A[1][0]);
+  }
+  double Rs[36], tmp[36];
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) {
+      int ia = VI[a], ja = VJ[a], kb = VI[b], lb = VJ[b];
+      Rs[6 * a + b] = b < 3 ? tr[3 * ia + kb] * tr[3 * ja + kb]
+                            : tr[3 * ia + kb] * tr[3 * ja + lb] + tr[3 * ia + lb] * tr[3 * ja + kb];
+    }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) {
+      double s = 0;
+      for (int k = 0; k < 6; k++) s += C0[6 * i + k] * Rs[6 * j + k];
+      tmp[6 * i + j] = s;
+    }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) {
+      double s = 0;
+      for (int k = 0; k < 6; k++) s += Rs[6 * i + k] * tmp[6 * k + j];
+      o.C[6 * i + j] = s;
+    }
+}
+
+CrysRec crystal_record(const cpfft_crystal& p) {
+  CrysRec c;
+  c.rate_n = p.harden_n;
+  c.tau_y = p.tau_y;
+  c.tau_v = p.tau_v;
+  c.inv_tau_v = 1.0 / p.tau_v;
+  c.theta_0 = p.theta_0;
+  c.voce_m = p.voce_m;
+  c.gamma_bar = p.gamma_bar;
+  c.iD_v = p.iD_v;
+  c.atol = p.atol;
+  c.atol1 = p.atol1;
+  c.rtol = p.rtol;
+  c.rtol1 = p.rtol1;
+  c.miter = p.miter;
+  c.alter_mode = p.alter_mode;
+  c.exact_j22 = p.exact_j22;
+  double r = std::round(p.harden_n);
+  c.n_int = (r == p.harden_n && r >= 2.0 && r <= 64.0) ? (int)r - 1 : -1;
+  c.m_is_one = p.voce_m == 1.0;
+  return c;
+}
+
+// ---- device context -------------------------------------------------------------
+struct Ctx {
+  int N = 0;
+  long long N3 = 0;
+  double dt = 0;
+  int prec = CPFFT_PREC_FP64, warm = 0;
+  cudaStream_t st = nullptr;
+  GridDesc g;
+  double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
+  double *r = nullptr, *p = nullptr, *Ap = nullptr, *w = nullptr, *io = nullptr;
+  double* hist[2] = {nullptr, nullptr};
+  int hn = 0;  // index of the history at n
+  float *K4f = nullptr, *xf = nullptr, *rf = nullptr, *pf = nullptr, *Apf = nullptr;
+  int *ori = nullptr, *crys = nullptr;
+  OriRec* oris = nullptr;
+  CrysRec* cryss = nullptr;
+  double2* S = nullptr;
+  float2* Sf = nullptr;
+  double2* tw = nullptr;
+  float2* twf = nullptr;
+  double *part = nullptr, *sc = nullptr, *h_sc = nullptr;
+  unsigned long long* stats = nullptr;
+  unsigned long long* h_stats = nullptr;
+  bool K4f_valid = false;
+  // FFT_nr3 locals that persist across steps (Fortran DATA => SAVE, src/FFT_nr3.f:29-34)
+  double barF_t[9], P_bar[9], C_homo[81];
+  // counters of the current step
+  long long cg_iters = 0, cg_solves = 0, f64_matvecs = 0, f32_matvecs = 0;
+};
+Ctx* g_ctx = nullptr;
+
+#define TRY(expr)                 \
+  do {                            \
+    int _rc = (expr);             \
+    if (_rc) return _rc;          \
+  } while (0)
+
+template <typename Ptr>
+int dalloc(Ptr& p, size_t bytes) {
+  cudaError_t e = cudaMalloc((void**)&p, bytes);
+  if (e != cudaSuccess) {
+    cpfft_set_error("cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    p = nullptr;
+    return CPFFT_ERR_NO_MEMORY;
+  }
+  return 0;
+}
+
+void free_ctx(Ctx* c) {
+  if (!c) return;
+  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io,
+                  c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
+                  c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (c->h_sc) cudaFreeHost(c->h_sc);
+  if (c->h_stats) cudaFreeHost(c->h_stats);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    cpfft_set_error("%s: %s", what, cudaGetErrorString(e));
+    return CPFFT_ERR_CUDA;
+  }
+  return 0;
+}
+#define CK(expr) TRY(cuda_check((expr), #expr))
+
+int sync(Ctx* c) { return cuda_check(cudaStreamSynchronize(c->st), "stream synchronize"); }
+
+int read_scalar(Ctx* c, int slot, double* out) {
+  CK(cudaMemcpyAsync(c->h_sc + slot, c->sc + slot, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  *out = c->h_sc[slot];
+  return 0;
+}
+
+int dnrm2(Ctx* c, const double* x, double* out) {
+  CK(dev_dot(x, x, 9 * c->N3, c->part, c->sc, SC_TMP, OP_STORE, c->st));
+  double v;
+  TRY(read_scalar(c, SC_TMP, &v));
+  *out = std::sqrt(v);
+  return 0;
+}
+
+// FP64 matvec y = G(K4:x) or G(x)
+int matvec64(Ctx* c, const double* x, double* y, int flgK) {
+  c->f64_matvecs++;
+  return cuda_check(green_apply<double>(x, c->K4, flgK, y, c->S, c->tw, c->g, c->st), "green_apply fp64");
+}
+int matvec32(Ctx* c, const float* x, float* y) {
+  c->f32_matvecs++;
+  return cuda_check(green_apply<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st), "green_apply fp32");
+}
+
+// fftPcg (src/FFT_nr3.f:214-360), plain FP64: CG from x = 0 with the stop test
+// ||r|| <= tol*||b|| .or. ||r|| <= tol and at most 1000 iterations
+int cg64(Ctx* c, const double* b, double* x, double tol, int* iters) {
+  const long long n = 9 * c->N3;
+  const int maxIter = 1000;
+  *iters = 0;
+  CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
+  double n2b;
+  TRY(dnrm2(c, b, &n2b));
+  if (!(tol > 2.220446049250313e-16 && tol < 1.0)) return CPFFT_ERR_CG_TOL;
+  if (!std::isfinite(n2b)) { cpfft_set_error("non-finite CG right-hand side"); return CPFFT_ERR_NONFINITE; }
+  if (n2b <= 2.220446049250313e-16) return 0;
+  const double tolb = tol * n2b;
+  CK(cudaMemcpyAsync(c->r, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaMemcpyAsync(c->p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  CK(dev_dot(c->r, c->r, n, c->part, c->sc, SC_RR, OP_STORE, c->st));
+  int it = 0;
+  for (;;) {
+    TRY(matvec64(c, c->p, c->Ap, 1));
+    CK(dev_dot(c->p, c->Ap, n, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+    CK(dev_cg_xr<double>(x, c->r, c->p, c->Ap, n, c->part, c->sc, c->st));
+    it++;
+    double rr;
+    TRY(read_scalar(c, SC_RRNEW, &rr));
+    double rn = std::sqrt(rr);
+    if (!std::isfinite(rn)) { *iters = it; cpfft_set_error("CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    if (rn <= tolb || rn <= tol || it >= maxIter) break;
+    CK(dev_cg_p<double>(c->p, c->r, n, c->sc, c->st));
+  }
+  *iters = it;
+  c->cg_iters += it;
+  c->cg_solves++;
+  return it >= maxIter ? CPFFT_ERR_CG_MAXIT : 0;
+}
+
+// Mixed precision: FP32 Green/FFT/CG inner solves corrected by an FP64 outer residual
+// (iterative refinement).  Same stop test on the FP64 residual as cg64.
+int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
+  const long long n = 9 * c->N3;
+  const int maxIter = 1000, maxOuter = 40;
+  const double inner_rtol = 1.0e-5;
+  *iters = 0;
+  CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
+  double n2b;
+  TRY(dnrm2(c, b, &n2b));
+  if (!(tol > 2.220446049250313e-16 && tol < 1.0)) return CPFFT_ERR_CG_TOL;
+  if (!std::isfinite(n2b)) { cpfft_set_error("non-finite CG right-hand side"); return CPFFT_ERR_NONFINITE; }
+  if (n2b <= 2.220446049250313e-16) return 0;
+  if (!c->K4f_valid) {
+    cpfft_set_error("mixed precision CG needs the FP32 tangent of a stress update");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const double tolb = tol * n2b;
+  // residual r = b (x = 0)
+  CK(cudaMemcpyAsync(c->w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  double rn = n2b;
+  int total = 0;
+  for (int outer = 0; outer < maxOuter; outer++) {
+    if (rn <= tolb || rn <= tol) break;
+    // inner FP32 CG on A d = r / ||r||
+    CK(dev_to_f32(c->rf, c->w, 1.0 / rn, n, c->st));
+    CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+    CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+    CK(dev_dot_f(c->rf, c->rf, n, c->part, c->sc, SC_RR, OP_STORE, c->st));
+    double rr0;
+    TRY(read_scalar(c, SC_RR, &rr0));
+    const double itol = inner_rtol * std::sqrt(rr0);
+    int it = 0;
+    for (;;) {
+      TRY(matvec32(c, c->pf, c->Apf));
+      CK(dev_dot_f(c->pf, c->Apf, n, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+      CK(dev_cg_xr<float>(c->xf, c->rf, c->pf, c->Apf, n, c->part, c->sc, c->st));
+      it++;
+      double rr;
+      TRY(read_scalar(c, SC_RRNEW, &rr));
+      if (!std::isfinite(rr)) { cpfft_set_error("inner CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
+      if (std::sqrt(rr) <= itol || it >= maxIter || total + it >= maxIter * 4) break;
+      CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+    }
+    total += it;
+    // x += ||r|| d ; r = b - G(K4 : x) in FP64
+    CK(dev_add_f32(x, c->xf, rn, n, c->st));
+    TRY(matvec64(c, x, c->Ap, 1));
+    CK(dev_sub(c->w, b, c->Ap, n, c->st));
+    TRY(dnrm2(c, c->w, &rn));
+    if (!std::isfinite(rn)) { cpfft_set_error("outer residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    if (total >= maxIter * 4) break;
+  }
+  *iters = total;
+  c->cg_iters += total;
+  c->cg_solves++;
+  if (!(rn <= tolb || rn <= tol)) { cpfft_set_error("mixed-precision refinement did not converge"); return CPFFT_ERR_CG_MAXIT; }
+  return 0;
+}
+
+int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
+  return c->prec == CPFFT_PREC_MIXED ? cg_mixed(c, b, x, tol, iters) : cg64(c, b, x, tol, iters);
+}
+
+int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails) {
+  StressArgs a;
+  a.Fn = c->Fn;
+  a.Fn1 = c->Fn1;
+  a.hist_n = c->hist[c->hn];
+  a.hist_np1 = c->hist[1 - c->hn];
+  a.P = c->P;
+  a.K4 = c->K4;
+  a.K4f = c->prec == CPFFT_PREC_MIXED ? c->K4f : nullptr;
+  a.ori = c->ori;
+  a.crys = c->crys;
+  a.oris = c->oris;
+  a.cryss = c->cryss;
+  a.stats = c->stats;
+  a.N3 = c->N3;
+  a.dt = c->dt;
+  a.step = step;
+  a.iter = iter;
+  CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
+  CK(launch_stress(a, c->st));
+  c->K4f_valid = a.K4f != nullptr;
+  CK(cudaMemcpyAsync(c->h_stats, c->stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  if (local_iters) *local_iters = (long long)c->h_stats[0];
+  if (fails) *fails = (int)c->h_stats[1];
+  return 0;
+}
+
+// tangent_homo (src/tangent_homo.f:11-73): 9 CG solves, C_homo(i,j) stored at 9*j+i
+int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
+  const long long N3 = c->N3, n = 9 * N3;
+  *its_total = 0;
+  for (int i = 0; i < 9; i++) {
+    for (int j = 0; j < 9; j++)
+      CK(cudaMemcpyAsync(c->io + j * N3, c->K4 + (9 * j + i) * N3, N3 * sizeof(double),
+                         cudaMemcpyDeviceToDevice, c->st));
+    TRY(matvec64(c, c->io, c->b, 0));
+    CK(dev_scale(c->b, -1.0, n, c->st));
+    int its = 0;
+    TRY(cg(c, c->b, c->io, tolPCG, &its));
+    *its_total += its;
+    CK(dev_add_const(c->io + i * N3, 1.0, N3, c->st));
+    for (int j = 0; j < 9; j++) {
+      double s;
+      CK(dev_dot(c->K4 + 9 * j * N3, c->io, n, c->part, c->sc, SC_TMP, OP_STORE, c->st));
+      TRY(read_scalar(c, SC_TMP, &s));
+      C_homo[9 * j + i] = s / (double)N3;
+    }
+  }
+  return 0;
+}
+
+// NBC_update (src/FFT_nr3.f:375-433): 9x9 LU with partial pivoting
+int nbc_update(const double* C_homo, double* DbarF, const double* P_bar, const double* PBC,
+               const int* isNBC) {
+  double A[81], bb[9];
+  for (int i = 0; i < 9; i++) {
+    if (isNBC[i]) {
+      for (int k = 0; k < 9; k++) A[9 * i + k] = C_homo[k + 9 * i];
+      bb[i] = PBC[i] - P_bar[i];
+    } else {
+      for (int k = 0; k < 9; k++) A[9 * i + k] = 0.0;
+      A[9 * i + i] = 1.0;
+      bb[i] = DbarF[i];
+    }
+  }
+  for (int k = 0; k < 9; k++) {
+    int p = k;
+    for (int i = k + 1; i < 9; i++)
+      if (std::fabs(A[9 * i + k]) > std::fabs(A[9 * p + k])) p = i;
+    if (A[9 * p + k] == 0.0 || !std::isfinite(A[9 * p + k])) {
+      cpfft_set_error("P_bar update failed: singular mixed-BC system");
+      return CPFFT_ERR_NBC_SINGULAR;
+    }
+    if (p != k) {
+      for (int j = 0; j < 9; j++) std::swap(A[9 * k + j], A[9 * p + j]);
+      std::swap(bb[k], bb[p]);
+    }
+    for (int i = k + 1; i < 9; i++) {
+      double l = A[9 * i + k] / A[9 * k + k];
+      for (int j = k; j < 9; j++) A[9 * i + j] -= l * A[9 * k + j];
+      bb[i] -= l * bb[k];
+    }
+  }
+  for (int i = 8; i >= 0; i--) {
+    double s = bb[i];
+    for (int k = i + 1; k < 9; k++) s -= A[9 * i + k] * bb[k];
+    bb[i] = s / A[9 * i + i];
+  }
+  for (int i = 0; i < 9; i++) DbarF[i] = bb[i];
+  return 0;
+}
+
+int need_ctx() {
+  if (!g_ctx) {
+    cpfft_set_error("cpfft_init has not been called");
+    return CPFFT_ERR_NOT_INIT;
+  }
+  return 0;
+}
+
+int alloc_mixed(Ctx* c) {
+  const long long n = 9 * c->N3;
+  if (c->K4f) return 0;
+  TRY(dalloc(c->K4f, 81 * c->N3 * sizeof(float)));
+  TRY(dalloc(c->xf, n * sizeof(float)));
+  TRY(dalloc(c->rf, n * sizeof(float)));
+  TRY(dalloc(c->pf, n * sizeof(float)));
+  TRY(dalloc(c->Apf, n * sizeof(float)));
+  TRY(dalloc(c->Sf, (size_t)9 * c->N * c->N * c->g.H * sizeof(float2)));
+  TRY(dalloc(c->twf, c->N * sizeof(float2)));
+  std::vector<float2> twf(c->N);
+  for (int k = 0; k < c->N; k++) {
+    long double a = -2.0L * 3.14159265358979323846264338327950288L * k / c->N;
+    twf[k] = make_float2((float)cosl(a), (float)sinl(a));
+  }
+  CK(cudaMemcpy(c->twf, twf.data(), c->N * sizeof(float2), cudaMemcpyHostToDevice));
+  CK(green_setup<float>(c->N));
+  return 0;
+}
+
+}  // namespace
+
+// =====================================================================================
+extern "C" {
+
+const char* cpfft_last_error(void) { return g_err; }
+
+void cpfft_finalize(void) {
+  free_ctx(g_ctx);
+  g_ctx = nullptr;
+}
+
+int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_crystal* props,
+               int ncrystals, double tstep, int g_mapping) {
+  cpfft_finalize();
+  if (N < 2 || N > 256 || !matList || !kocks_deg || !props || ncrystals < 1 || !(tstep > 0) ||
+      (g_mapping != CPFFT_G_REF_SHIFT && g_mapping != CPFFT_G_CENTERED)) {
+    cpfft_set_error("cpfft_init: invalid argument (N in [2,256], tstep > 0, mapping 0/1)");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const long long N3 = (long long)N * N * N;
+  std::vector<CrysRec> cr(ncrystals);
+  std::vector<std::vector<double>> C0(ncrystals, std::vector<double>(36));
+  double bb[12][3], nn[12][3];
+  fcc_geometry(bb, nn);
+  for (int k = 0; k < ncrystals; k++) {
+    const cpfft_crystal& p = props[k];
+    if (p.slip_type != 1 || p.h_type != 1 || !(p.tau_v != 0) || !(p.harden_n > 0) ||
+        p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
+      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc + voce only, valid elasticity)", k + 1);
+      return CPFFT_ERR_BAD_ARG;
+    }
+    cr[k] = crystal_record(p);
+  }
+  // distinct (crystal, orientation) records
+  std::vector<int> ori(N3), crys(N3);
+  std::map<std::tuple<int, double, double, double>, int> seen;
+  std::vector<OriRec> oris;
+  for (long long v = 0; v < N3; v++) {
+    int m = matList[v] - 1;
+    if (m < 0 || m >= ncrystals) {
+      cpfft_set_error("cpfft_init: matList[%lld] = %d out of range", v, matList[v]);
+      return CPFFT_ERR_BAD_ARG;
+    }
+    double ang[3] = {kocks_deg[v], kocks_deg[N3 + v], kocks_deg[2 * N3 + v]};
+    auto key = std::make_tuple(m, ang[0], ang[1], ang[2]);
+    auto it = seen.find(key);
+    int id;
+    if (it == seen.end()) {
+      id = (int)oris.size();
+      oris.emplace_back();
+      orientation_record(C0[m].data(), bb, nn, ang, oris.back());
+      seen.emplace(key, id);
+    } else {
+      id = it->second;
+    }
+    ori[v] = id;
+    crys[v] = m;
+  }
+  Ctx* c = new Ctx;
+  c->N = N;
+  c->N3 = N3;
+  c->dt = tstep;
+  c->g.N = N;
+  c->g.H = N / 2 + 1;
+  c->g.N3 = N3;
+  c->g.Nhalf = (N % 2 == 1) ? (N + 1) / 2 : N / 2 + 1;
+  c->g.gmap = g_mapping;
+  c->g.inv_n3 = 1.0 / (double)N3;
+  c->g.tkb = 16;
+  c->g.tkc = 2;
+  c->g.plan = make_plan(N);
+  auto fail = [&](int rc) { free_ctx(c); return rc; };
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+    cpfft_set_error("cudaStreamCreate failed");
+    return fail(CPFFT_ERR_CUDA);
+  }
+  const size_t f9 = 9 * N3 * sizeof(double);
+  int rc = 0;
+  if ((rc = dalloc(c->Fn, f9)) || (rc = dalloc(c->Fn1, f9)) || (rc = dalloc(c->P, f9)) ||
+      (rc = dalloc(c->K4, 81 * N3 * sizeof(double))) || (rc = dalloc(c->b, f9)) ||
+      (rc = dalloc(c->dFm, f9)) || (rc = dalloc(c->r, f9)) || (rc = dalloc(c->p, f9)) ||
+      (rc = dalloc(c->Ap, f9)) || (rc = dalloc(c->w, f9)) || (rc = dalloc(c->io, f9)) ||
+      (rc = dalloc(c->hist[0], H_WORDS * N3 * sizeof(double))) ||
+      (rc = dalloc(c->hist[1], H_WORDS * N3 * sizeof(double))) ||
+      (rc = dalloc(c->ori, N3 * sizeof(int))) || (rc = dalloc(c->crys, N3 * sizeof(int))) ||
+      (rc = dalloc(c->oris, oris.size() * sizeof(OriRec))) ||
+      (rc = dalloc(c->cryss, ncrystals * sizeof(CrysRec))) ||
+      (rc = dalloc(c->S, (size_t)9 * N * N * c->g.H * sizeof(double2))) ||
+      (rc = dalloc(c->tw, N * sizeof(double2))) || (rc = dalloc(c->part, 9 * NPART * sizeof(double))) ||
+      (rc = dalloc(c->sc, SC_COUNT * sizeof(double))) ||
+      (rc = dalloc(c->stats, 4 * sizeof(unsigned long long))))
+    return fail(rc);
+  if (cudaMallocHost((void**)&c->h_sc, SC_COUNT * sizeof(double)) != cudaSuccess ||
+      cudaMallocHost((void**)&c->h_stats, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+    cpfft_set_error("cudaMallocHost failed");
+    return fail(CPFFT_ERR_NO_MEMORY);
+  }
+  std::vector<double2> tw(N);
+  for (int k = 0; k < N; k++) {
+    long double a = -2.0L * 3.14159265358979323846264338327950288L * k / N;
+    tw[k] = make_double2((double)cosl(a), (double)sinl(a));
+  }
+  std::vector<double> F(9 * N3, 0.0);
+  for (int d : {0, 4, 8})
+    for (long long v = 0; v < N3; v++) F[d * N3 + v] = 1.0;
+  // history at n = the state of mm10_init_cc_hist0 (sigma 0, tau_y + 1e-5, Rp = I)
+  std::vector<double> h(H_WORDS * N3, 0.0);
+  for (long long v = 0; v < N3; v++) {
+    h[H_TT * N3 + v] = props[crys[v]].tau_y + 1.0e-5;
+    for (int d : {0, 4, 8}) h[(H_RP + d) * N3 + v] = 1.0;
+  }
+  cudaError_t e;
+  if ((e = cudaMemcpy(c->tw, tw.data(), N * sizeof(double2), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->Fn, F.data(), f9, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->Fn1, F.data(), f9, cudaMemcpyHostToDevice)) ||
+      (e = cudaMemset(c->P, 0, f9)) || (e = cudaMemset(c->K4, 0, 81 * N3 * sizeof(double))) ||
+      (e = cudaMemcpy(c->hist[0], h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->hist[1], h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->ori, ori.data(), N3 * sizeof(int), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->crys, crys.data(), N3 * sizeof(int), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->oris, oris.data(), oris.size() * sizeof(OriRec), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->cryss, cr.data(), ncrystals * sizeof(CrysRec), cudaMemcpyHostToDevice)) ||
+      (e = green_setup<double>(N))) {
+    cpfft_set_error("cpfft_init: %s", cudaGetErrorString(e));
+    return fail(CPFFT_ERR_CUDA);
+  }
+  for (int i = 0; i < 9; i++) {
+    c->barF_t[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    c->P_bar[i] = 0.0;
+  }
+  for (int i = 0; i < 81; i++) c->C_homo[i] = 0.0;
+  g_ctx = c;
+  return 0;
+}
+
+int cpfft_set_mode(int precision, int warm_start) {
+  TRY(need_ctx());
+  if (precision != CPFFT_PREC_FP64 && precision != CPFFT_PREC_MIXED) {
+    cpfft_set_error("cpfft_set_mode: unknown precision %d", precision);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (warm_start) {
+    cpfft_set_error("cpfft_set_mode: the learned warm start is not available in this build");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (precision == CPFFT_PREC_MIXED) TRY(alloc_mixed(g_ctx));
+  if (precision != g_ctx->prec) g_ctx->K4f_valid = false;
+  g_ctx->prec = precision;
+  g_ctx->warm = warm_start;
+  return 0;
+}
+
+int cpfft_set_F(const double* Fn, const double* Fn1) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  const size_t f9 = 9 * c->N3 * sizeof(double);
+  if (Fn) CK(cudaMemcpyAsync(c->Fn, Fn, f9, cudaMemcpyHostToDevice, c->st));
+  if (Fn1) CK(cudaMemcpyAsync(c->Fn1, Fn1, f9, cudaMemcpyHostToDevice, c->st));
+  return sync(c);
+}
+
+int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1, double* Pn1,
+                        double* K4) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (step < 1 || iter < 0) {
+    cpfft_set_error("cpfft_stress_update: step >= 1 and iter >= 0 required");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  TRY(cpfft_set_F(Fn, Fn1));
+  long long li;
+  int fails;
+  TRY(stress(c, step, iter, &li, &fails));
+  if (Pn1) CK(cudaMemcpyAsync(Pn1, c->P, 9 * c->N3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (K4) CK(cudaMemcpyAsync(K4, c->K4, 81 * c->N3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  return fails ? CPFFT_WARN_LOCAL_FALLBACK : 0;
+}
+
+int cpfft_set_K4(const double* K4) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  CK(cudaMemcpyAsync(c->K4, K4, 81 * c->N3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
+  if (c->prec == CPFFT_PREC_MIXED) {
+    // FP32 copy for the inner solves
+    std::vector<float> kf(81 * c->N3);
+    for (long long i = 0; i < 81 * c->N3; i++) kf[i] = (float)K4[i];
+    CK(cudaMemcpyAsync(c->K4f, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    TRY(sync(c));
+    c->K4f_valid = true;
+  }
+  return sync(c);
+}
+
+int cpfft_green_apply(const double* x, double* y, int flgK) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  const size_t f9 = 9 * c->N3 * sizeof(double);
+  CK(cudaMemcpyAsync(c->io, x, f9, cudaMemcpyHostToDevice, c->st));
+  TRY(matvec64(c, c->io, c->b, flgK ? 1 : 0));
+  CK(cudaMemcpyAsync(y, c->b, f9, cudaMemcpyDeviceToHost, c->st));
+  return sync(c);
+}
+
+int cpfft_cg(const double* b, double* x, double tol, int* iters) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  const size_t f9 = 9 * c->N3 * sizeof(double);
+  int its = 0;
+  CK(cudaMemcpyAsync(c->b, b, f9, cudaMemcpyHostToDevice, c->st));
+  int rc = cg(c, c->b, c->io, tol, &its);
+  if (iters) *iters = its;
+  if (rc < 0 && rc != CPFFT_ERR_CG_MAXIT) return rc;
+  CK(cudaMemcpyAsync(x, c->io, f9, cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  return rc;
+}
+
+int cpfft_tangent_homo(double tolPCG, double* C_homo) {
+  TRY(need_ctx());
+  int its;
+  double C[81];
+  TRY(tangent_homo(g_ctx, tolPCG, C, &its));
+  if (C_homo) memcpy(C_homo, C, sizeof(C));
+  return 0;
+}
+
+int cpfft_nr3_begin(double tolPCG) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  long long li;
+  int fails, its;
+  TRY(stress(c, 1, 0, &li, &fails));
+  TRY(tangent_homo(c, tolPCG, c->C_homo, &its));
+  return 0;
+}
+
+int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, double tolPCG,
+                   int maxIter, double* Pbar, cpfft_stats* st) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (!BC || !isNBC || step < 1) {
+    cpfft_set_error("cpfft_nr3_step: invalid argument");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  using clk = std::chrono::steady_clock;
+  auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+  auto t0 = clk::now();
+  cpfft_stats S;
+  memset(&S, 0, sizeof(S));
+  c->cg_iters = c->cg_solves = c->f64_matvecs = c->f32_matvecs = 0;
+  const long long N3 = c->N3, n = 9 * N3;
+  bool existNBC = false;
+  for (int i = 0; i < 9; i++) existNBC |= isNBC[i] != 0;
+  double PBC[9], FBC[9], DbarF[9], barF[9];
+  for (int i = 0; i < 9; i++) {
+    PBC[i] = FBC[i] = DbarF[i] = 0.0;
+    if (isNBC[i]) PBC[i] = BC[i];
+    else { FBC[i] = BC[i]; DbarF[i] = FBC[i] - c->barF_t[i]; }
+  }
+  if (existNBC) TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));
+  for (int i = 0; i < 9; i++) barF[i] = c->barF_t[i] + DbarF[i];
+  int iiter_NBC = 0, rc = 0;
+  double tp = 0, ts = 0;
+  for (;;) {
+    CK(dev_fill9(c->dFm, N3, DbarF, c->st));
+    double Fnorm;
+    TRY(dnrm2(c, c->Fn1, &Fnorm));
+    CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
+    TRY(matvec64(c, c->dFm, c->b, 1));
+    CK(dev_scale(c->b, -1.0, n, c->st));
+    int its;
+    auto a = clk::now();
+    TRY(cg(c, c->b, c->dFm, tolPCG, &its));
+    tp += sec(a);
+    CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
+    double resfft = 1.0;
+    int iiter_EBC = 0;
+    while (resfft > tolNR) {
+      a = clk::now();
+      long long li;
+      int fails;
+      TRY(stress(c, step, iiter_EBC, &li, &fails));
+      ts += sec(a);
+      S.local_iters += li;
+      S.local_fallbacks += fails;
+      S.stress_updates++;
+      TRY(matvec64(c, c->P, c->b, 0));
+      CK(dev_scale(c->b, -1.0, n, c->st));
+      a = clk::now();
+      TRY(cg(c, c->b, c->dFm, tolPCG, &its));
+      tp += sec(a);
+      CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
+      double dn;
+      TRY(dnrm2(c, c->dFm, &dn));
+      resfft = dn / Fnorm;
+      if (!std::isfinite(resfft)) { cpfft_set_error("Newton residual is not finite"); return CPFFT_ERR_NONFINITE; }
+      S.newton_iters++;
+      S.res_fft = resfft;
+      if (iiter_EBC == maxIter) {
+        cpfft_set_error("Newton loop does not converge (step %d)", step);
+        return CPFFT_ERR_NEWTON_MAXIT;
+      }
+      iiter_EBC++;
+    }
+    a = clk::now();
+    long long li;
+    int fails;
+    TRY(stress(c, step, iiter_EBC, &li, &fails));
+    ts += sec(a);
+    S.local_iters += li;
+    S.local_fallbacks += fails;
+    S.stress_updates++;
+    CK(dev_sum9(c->P, N3, c->part, c->sc, SC_SUM9, c->st));
+    CK(cudaMemcpyAsync(c->h_sc + SC_SUM9, c->sc + SC_SUM9, 9 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    TRY(sync(c));
+    double res1 = 0, res2 = 0;
+    for (int i = 0; i < 9; i++) {
+      c->P_bar[i] = c->h_sc[SC_SUM9 + i] / (double)N3;
+      res2 += c->P_bar[i] * c->P_bar[i];
+      if (isNBC[i]) res1 += (c->P_bar[i] - PBC[i]) * (c->P_bar[i] - PBC[i]);
+    }
+    double res3 = res2 < 1.0e-8 ? std::sqrt(res1) : std::sqrt(res1 / res2);
+    S.res_pbar = res3;
+    S.nbc_iters = iiter_NBC + 1;
+    if (res3 <= tolNR) break;
+    if (iiter_NBC > maxIter) {
+      cpfft_set_error("prescribed stress cannot be reached (step %d)", step);
+      return CPFFT_ERR_NBC_MAXIT;
+    }
+    a = clk::now();
+    int th;
+    TRY(tangent_homo(c, tolPCG, c->C_homo, &th));
+    tp += sec(a);
+    for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
+    TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));
+    for (int i = 0; i < 9; i++) barF[i] += DbarF[i];
+    iiter_NBC++;
+  }
+  // roll-over: Fn <- Fn1, history n <- n+1 (src/FFT_nr3.f:173-179, src/update.f)
+  for (int i = 0; i < 9; i++) c->barF_t[i] = barF[i];
+  CK(cudaMemcpyAsync(c->Fn, c->Fn1, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  c->hn = 1 - c->hn;
+  if (Pbar)
+    for (int i = 0; i < 9; i++) Pbar[i] = c->P_bar[i];
+  // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||)
+  TRY(matvec64(c, c->P, c->b, 0));
+  double gp;
+  TRY(dnrm2(c, c->b, &gp));
+  double pb = 0;
+  for (int i = 0; i < 9; i++) pb += c->P_bar[i] * c->P_bar[i];
+  S.res_equil = gp / (std::sqrt((double)N3) * std::sqrt(pb));
+  S.cg_solves = (int)c->cg_solves;
+  S.cg_iters = (int)c->cg_iters;
+  S.t_pcg = tp;
+  S.t_sigeps = ts;
+  S.t_total = sec(t0);
+  if (st) *st = S;
+  (void)rc;
+  return S.local_fallbacks ? CPFFT_WARN_LOCAL_FALLBACK : 0;
+}
+
+int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  const size_t f9 = 9 * c->N3 * sizeof(double);
+  if (Fn1) CK(cudaMemcpyAsync(Fn1, c->Fn1, f9, cudaMemcpyDeviceToHost, c->st));
+  if (Pn1) CK(cudaMemcpyAsync(Pn1, c->P, f9, cudaMemcpyDeviceToHost, c->st));
+  if (history)
+    CK(cudaMemcpyAsync(history, c->hist[c->hn], H_WORDS * c->N3 * sizeof(double),
+                       cudaMemcpyDeviceToHost, c->st));
+  return sync(c);
+}
+
+int cpfft_commit_step(void) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  CK(cudaMemcpyAsync(c->Fn, c->Fn1, 9 * c->N3 * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  c->hn = 1 - c->hn;
+  return sync(c);
+}
+
+}  // extern "C"

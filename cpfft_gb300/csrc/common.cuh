@@ -1,0 +1,69 @@
+// common.cuh -- shared device/host helpers of the GB300 CPFFT hot path.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/cpfft_gpu.h"
+
+#define CPFFT_CUDA_TRY(expr)                                                       \
+  do {                                                                             \
+    cudaError_t _e = (expr);                                                       \
+    if (_e != cudaSuccess) {                                                       \
+      cpfft_set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr,                   \
+                      cudaGetErrorString(_e));                                     \
+      return CPFFT_ERR_CUDA;                                                       \
+    }                                                                              \
+  } while (0)
+
+void cpfft_set_error(const char* fmt, ...);
+
+// ---- per-orientation material data (computed once at init, see api.cu) ------------
+// One record per distinct (crystal, orientation): the rotated stiffness and the slip
+// tensors of setup_mm10_rknstr (src/drive_eps_sig.f:537-1002), which the reference
+// recomputes on every call for every voxel.
+struct OriRec {
+  double C[36];    // stiffness in the sample frame, row-major 6x6
+  double ms[72];   // 12 x 6 sym(b (x) n) Voigt, engineering shear
+  double qs[36];   // 12 x 3 skew(b (x) n) as (w23, w13, w12)
+};
+
+// Scalars of one crystal definition that the Voce path reads.
+struct CrysRec {
+  double rate_n, tau_y, tau_v, inv_tau_v, theta_0, voce_m, gamma_bar, iD_v;
+  double atol, atol1, rtol, rtol1;
+  int miter, alter_mode, exact_j22;
+  int n_int;       // rate_n - 1 when rate_n is integer-valued in [2, 64], else -1
+  int m_is_one;    // voce_m == 1
+};
+
+// Words of the compact per-voxel history (CPFFT_HIST_WORDS)
+enum {
+  H_SIG = 0,      // 6  unrotated Cauchy stress
+  H_TT = 6,       // 1  slip resistance tau_tilde
+  H_RP = 7,       // 9  plastic rotation Rp, column-major
+  H_D = 16,       // 6  unrotated strain increment of the step
+  H_TTR = 22,     // 1  tau_tilde rate
+  H_WORDS = 23
+};
+
+// Stress kernel launch arguments
+struct StressArgs {
+  const double* Fn;      // (9, N3)
+  const double* Fn1;     // (9, N3)
+  const double* hist_n;  // (23, N3)
+  double* hist_np1;      // (23, N3)
+  double* P;             // (9, N3)
+  double* K4;            // (81, N3)
+  float* K4f;            // (81, N3) optional FP32 copy (mixed precision), may be null
+  const int* ori;        // (N3) orientation record id
+  const int* crys;       // (N3) crystal id, 0-based
+  const OriRec* oris;
+  const CrysRec* cryss;
+  unsigned long long* stats;  // [0] local iters, [1] failures, [2] predict iters
+  long long N3;
+  double dt;
+  int step, iter;
+};
+
+cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);

@@ -1,0 +1,450 @@
+// fft_green.cu -- y = G(K : x) or y = G(x) on the GPU: a hand-written real-to-complex
+// 3-D FFT of the 9 tensor components fused with the spectral Green operator.
+//
+// Replaces G_K_dF / fftfem3d / ifftfem3d / ddot42n (src/G_K_dF.f:11-268), which run 18
+// complex 3-D MKL transforms per call on real data and read an 81-wide stored Green
+// table (src/FFT_init.f:272-340).  Here:
+//   pass A  K:x fused into a real-to-complex transform along the fastest axis (two real
+//           lines packed into one complex transform);
+//   pass B  complex transform along the middle axis, tiles of columns in shared memory;
+//   pass C  transform along the slowest axis, Green contraction evaluated from q on the
+//           fly for all 9 components while they sit in shared memory, inverse transform
+//           along the same axis -- the spectrum never round-trips HBM between the
+//           transform and the contraction;
+//   pass D  inverse along the middle axis;
+//   pass E  complex-to-real inverse along the fastest axis, unpacking the line pairs.
+// The reference's result is Re(IDFT(Ghat(q(f)) X(f))); for real input that equals
+// IDFT(Hs(f) X(f)) with Hs(f) = (Ghat(q(f)) + Ghat(q(-f)))/2, which keeps the half
+// spectrum Hermitian and is what pass C applies, for both frequency mappings.
+#include "fft_green.cuh"
+
+namespace {
+
+template <typename T2, typename T>
+__device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+  T2 r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename T2>
+__device__ __forceinline__ T2 conjg(T2 a) { a.y = -a.y; return a; }
+
+// forward radix-2/4/8 butterflies on registers
+template <typename T2, typename T>
+__device__ __forceinline__ void bfly2(T2& a, T2& b) {
+  T2 t = a;
+  a.x = t.x + b.x; a.y = t.y + b.y;
+  b.x = t.x - b.x; b.y = t.y - b.y;
+}
+template <typename T2, typename T>
+__device__ __forceinline__ T2 mul_mi(T2 a) { T2 r; r.x = a.y; r.y = -a.x; return r; }  // * (-i)
+
+template <typename T2, typename T>
+__device__ __forceinline__ void dft4(T2* v) {
+  // X0 = a+b+c+d, X1 = a - i b - c + i d, X2 = a - b + c - d, X3 = a + i b - c - i d
+  bfly2<T2, T>(v[0], v[2]);
+  bfly2<T2, T>(v[1], v[3]);
+  v[3] = mul_mi<T2, T>(v[3]);
+  bfly2<T2, T>(v[0], v[1]);
+  bfly2<T2, T>(v[2], v[3]);
+  T2 t = v[1]; v[1] = v[2]; v[2] = t;
+}
+template <typename T2, typename T>
+__device__ __forceinline__ void dft8(T2* v) {
+  const T h = (T)0.70710678118654752440;
+  T2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<T2, T>(e);
+  dft4<T2, T>(o);
+  // twiddles W8^k for k = 1, 2, 3 (forward)
+  T2 t1; t1.x = h * (o[1].x + o[1].y); t1.y = h * (o[1].y - o[1].x); o[1] = t1;
+  o[2] = mul_mi<T2, T>(o[2]);
+  T2 t3; t3.x = h * (o[3].y - o[3].x); t3.y = -h * (o[3].x + o[3].y); o[3] = t3;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    v[k].x = e[k].x + o[k].x; v[k].y = e[k].y + o[k].y;
+    v[k + 4].x = e[k].x - o[k].x; v[k + 4].y = e[k].y - o[k].y;
+  }
+}
+
+// One forward Stockham stage of radix R on `ncols` columns (column stride cs) from
+// src to dst; tw[k] = exp(-2 pi i k / N).  Radix 2/4/8 run as register butterflies,
+// any other radix evaluates each output as a direct sum (test-only odd sizes).
+template <typename T2, typename T>
+__device__ void stage(const T2* __restrict__ src, T2* __restrict__ dst, int ncols, int cs,
+                      int N, int R, int Ns, const T2* tw) {
+  const int NR = N / R;
+  const int tstride = N / (Ns * R);
+  if (R == 2 || R == 4 || R == 8) {
+    const int total = ncols * NR;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      int col = t / NR, j = t - col * NR;
+      int jm = j % Ns;
+      int ts = jm * tstride;
+      const T2* s = src + col * cs + j;
+      T2 v[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+        if (r < R) {
+          T2 x = s[r * NR];
+          if (r) x = cmul<T2, T>(x, tw[r * ts]);
+          v[r] = x;
+        }
+      if (R == 2) bfly2<T2, T>(v[0], v[1]);
+      else if (R == 4) dft4<T2, T>(v);
+      else dft8<T2, T>(v);
+      T2* d = dst + col * cs + (j / Ns) * Ns * R + jm;
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+        if (r < R) d[r * Ns] = v[r];
+    }
+  } else {
+    const int total = ncols * N;
+    const int NoR = N / R;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      int col = t / N, rem = t - col * N;
+      int j = rem % NR, sidx = rem / NR;  // output s of butterfly j
+      int jm = j % Ns;
+      int ts = jm * tstride;
+      const T2* s = src + col * cs + j;
+      T2 acc; acc.x = 0; acc.y = 0;
+      for (int r = 0; r < R; r++) {
+        int e = (r * ts + ((r * sidx) % R) * NoR) % N;
+        T2 p = cmul<T2, T>(s[r * NR], tw[e]);
+        acc.x += p.x; acc.y += p.y;
+      }
+      dst[col * cs + (j / Ns) * Ns * R + jm + sidx * Ns] = acc;
+    }
+  }
+}
+
+// Forward FFT of ncols columns held in a (ping-pong with b); returns the buffer with
+// the result.  Caller synchronises before (data in a) and this leaves a barrier after.
+template <typename T2, typename T>
+__device__ T2* fft_cols(T2* a, T2* b, int ncols, int cs, const FftPlan& P, const T2* tw) {
+  for (int s = 0; s < P.nst; s++) {
+    stage<T2, T>(a, b, ncols, cs, P.n, P.R[s], P.Ns[s], tw);
+    __syncthreads();
+    T2* t = a; a = b; b = t;
+  }
+  return a;
+}
+
+template <typename T2>
+__device__ void load_tw(T2* tw_s, const T2* tw_g, int N) {
+  for (int k = threadIdx.x; k < N; k += blockDim.x) tw_s[k] = tw_g[k];
+}
+
+__device__ __forceinline__ int qmap(int f, int N, int Nhalf, int gmap) {
+  if (gmap == CPFFT_G_REF_SHIFT) {
+    int k = ((f - Nhalf) % N + N) % N;
+    return k + 1 - Nhalf;
+  }
+  return f <= (N - 1) / 2 ? f : f - N;
+}
+
+// (Ghat(q):A)_ij = q_j (sum_l A_il q_l) / |q|^2, zero when |q|^2 <= 1e-10
+// (formG, src/FFT_init.f:310-335); A is 9 complex, accumulated into out with weight w
+template <typename T2, typename T>
+__device__ __forceinline__ void ghat_acc(const T2* A, int q0, int q1, int q2, T w, T2* out) {
+  int qq = q0 * q0 + q1 * q1 + q2 * q2;
+  if (qq == 0) return;
+  T s = w / (T)qq;
+  T q[3] = {(T)q0, (T)q1, (T)q2};
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    T2 d;
+    d.x = A[3 * i].x * q[0] + A[3 * i + 1].x * q[1] + A[3 * i + 2].x * q[2];
+    d.y = A[3 * i].y * q[0] + A[3 * i + 1].y * q[1] + A[3 * i + 2].y * q[2];
+    d.x *= s; d.y *= s;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      out[3 * i + j].x += q[j] * d.x;
+      out[3 * i + j].y += q[j] * d.y;
+    }
+  }
+}
+
+// ---- pass A: K:x + real-to-complex transform along a --------------------------------
+template <typename T, typename TK>
+__global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK* __restrict__ K4,
+                                              int flgK, typename Vec2<T>::t* __restrict__ S,
+                                              GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = g.N, H = g.H;
+  const long long N3 = g.N3;
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* b0 = tw + N;
+  T2* b1 = b0 + 9 * N;
+  load_tw(tw, twg, N);
+  const int npair = (N + 1) / 2;
+  const int bp = blockIdx.x % npair, c = blockIdx.x / npair;
+  const int bl0 = 2 * bp, bl1 = 2 * bp + 1;
+  for (int t = threadIdx.x; t < 2 * N; t += blockDim.x) {
+    int l = t / N, a = t - l * N;
+    int b = l ? bl1 : bl0;
+    T y[9];
+    if (b < N) {
+      long long v = a + (long long)N * b + (long long)N * N * c;
+      if (flgK) {
+        T xv[9];
+#pragma unroll
+        for (int j = 0; j < 9; j++) xv[j] = x[j * N3 + v];
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+          T s = 0;
+#pragma unroll
+          for (int j = 0; j < 9; j++) s += (T)K4[(9 * i + j) * N3 + v] * xv[j];
+          y[i] = s;
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 9; i++) y[i] = x[i * N3 + v];
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 9; i++) y[i] = 0;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      if (l == 0) b0[i * N + a].x = y[i];
+      else b0[i * N + a].y = y[i];
+    }
+  }
+  __syncthreads();
+  T2* r = fft_cols<T2, T>(b0, b1, 9, N, g.plan, tw);
+  // unpack the two real lines: X0 = (Z + conj Z(-k))/2, X1 = (Z - conj Z(-k))/(2i)
+  for (int t = threadIdx.x; t < 9 * H; t += blockDim.x) {
+    int i = t / H, k = t - i * H;
+    T2 z = r[i * N + k], w = conjg(r[i * N + (N - k) % N]);
+    T2 X0, X1;
+    X0.x = (T)0.5 * (z.x + w.x); X0.y = (T)0.5 * (z.y + w.y);
+    X1.x = (T)0.5 * (z.y - w.y); X1.y = (T)-0.5 * (z.x - w.x);
+    long long base = ((long long)i * N + c) * N;
+    S[(base + bl0) * H + k] = X0;
+    if (bl1 < N) S[(base + bl1) * H + k] = X1;
+  }
+}
+
+// ---- pass B / D: transform along b ---------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pass_b(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+                                              const typename Vec2<T>::t* __restrict__ twg,
+                                              int inverse) {
+  using T2 = typename Vec2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = g.N, H = g.H, TK = g.tkb;
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* b0 = tw + N;
+  T2* b1 = b0 + TK * N;
+  load_tw(tw, twg, N);
+  const int ka0 = blockIdx.x * TK;
+  const int c = blockIdx.y, i = blockIdx.z;
+  T2* plane = S + ((long long)i * N + c) * (long long)N * H;
+  for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
+    int row = t / TK, kk = t - row * TK;
+    int ka = ka0 + kk;
+    T2 v;
+    v.x = 0; v.y = 0;
+    if (ka < H) v = plane[(long long)row * H + ka];
+    if (inverse) v.y = -v.y;
+    b0[kk * N + row] = v;
+  }
+  __syncthreads();
+  T2* r = fft_cols<T2, T>(b0, b1, TK, N, g.plan, tw);
+  for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
+    int row = t / TK, kk = t - row * TK;
+    int ka = ka0 + kk;
+    if (ka < H) {
+      T2 v = r[kk * N + row];
+      if (inverse) v.y = -v.y;
+      plane[(long long)row * H + ka] = v;
+    }
+  }
+}
+
+// ---- pass C: transform along c, Green contraction, inverse along c -------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+                                              const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = g.N, H = g.H, TK = g.tkc;
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* b0 = tw + N;
+  T2* b1 = b0 + 9 * TK * N;
+  load_tw(tw, twg, N);
+  const int ka0 = blockIdx.x * TK;
+  const int kb = blockIdx.y;
+  const long long cstr = (long long)N * H;  // stride between c planes
+  // column (i, kk) holds the N values along c
+  for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
+    int kk = t % TK, rem = t / TK;
+    int c = rem % N, i = rem / N;
+    int ka = ka0 + kk;
+    T2 v;
+    v.x = 0; v.y = 0;
+    if (ka < H) v = S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka];
+    b0[(i * TK + kk) * N + c] = v;
+  }
+  __syncthreads();
+  T2* r = fft_cols<T2, T>(b0, b1, 9 * TK, N, g.plan, tw);
+  T2* o = (r == b0) ? b1 : b0;
+  // Green contraction at every (kc, kb, ka) of the tile, symmetrised over +-f
+  const int Nh = g.Nhalf, gm = g.gmap;
+  const T scale = (T)g.inv_n3;
+  for (int t = threadIdx.x; t < N * TK; t += blockDim.x) {
+    int kc = t / TK, kk = t - kc * TK;
+    int ka = ka0 + kk;
+    T2 A[9], out[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      A[i] = r[(i * TK + kk) * N + kc];
+      out[i].x = 0; out[i].y = 0;
+    }
+    // centered mapping at even N: the Nyquist frequency has no signed partner and
+    // carries no compatible fluctuation (zero Green operator)
+    bool nyq = gm == CPFFT_G_CENTERED && (N & 1) == 0 &&
+               (2 * kc == N || 2 * kb == N || 2 * ka == N);
+    if (ka < H && !nyq) {
+      int p0 = qmap(kc, N, Nh, gm), p1 = qmap(kb, N, Nh, gm), p2 = qmap(ka, N, Nh, gm);
+      int m0 = qmap((N - kc) % N, N, Nh, gm), m1 = qmap((N - kb) % N, N, Nh, gm),
+          m2 = qmap((N - ka) % N, N, Nh, gm);
+      if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
+        ghat_acc<T2, T>(A, p0, p1, p2, scale, out);
+      } else {
+        ghat_acc<T2, T>(A, p0, p1, p2, (T)0.5 * scale, out);
+        ghat_acc<T2, T>(A, m0, m1, m2, (T)0.5 * scale, out);
+      }
+    }
+    // conjugate for the inverse transform
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      out[i].y = -out[i].y;
+      o[(i * TK + kk) * N + kc] = out[i];
+    }
+  }
+  __syncthreads();
+  T2* r2 = fft_cols<T2, T>(o, r, 9 * TK, N, g.plan, tw);
+  for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
+    int kk = t % TK, rem = t / TK;
+    int c = rem % N, i = rem / N;
+    int ka = ka0 + kk;
+    if (ka < H) {
+      T2 v = r2[(i * TK + kk) * N + c];
+      v.y = -v.y;
+      S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka] = v;
+    }
+  }
+}
+
+// ---- pass E: complex-to-real inverse along a, unpacking line pairs -------------------
+template <typename T>
+__global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restrict__ S,
+                                              T* __restrict__ y, GridDesc g,
+                                              const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int N = g.N, H = g.H;
+  const long long N3 = g.N3;
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* b0 = tw + N;
+  T2* b1 = b0 + 9 * N;
+  load_tw(tw, twg, N);
+  const int npair = (N + 1) / 2;
+  const int bp = blockIdx.x % npair, c = blockIdx.x / npair;
+  const int bl0 = 2 * bp, bl1 = 2 * bp + 1;
+  const bool even = (N % 2) == 0;
+  for (int t = threadIdx.x; t < 9 * N; t += blockDim.x) {
+    int i = t / N, k = t - i * N;
+    long long base = ((long long)i * N + c) * N;
+    int kk = k < H ? k : N - k;
+    T2 X0 = S[(base + bl0) * H + kk], X1;
+    if (bl1 < N) X1 = S[(base + bl1) * H + kk];
+    else { X1.x = 0; X1.y = 0; }
+    if (kk == 0 || (even && kk == N / 2)) { X0.y = 0; X1.y = 0; }
+    if (k >= H) { X0.y = -X0.y; X1.y = -X1.y; }
+    // Z = X0 + i X1, load conj(Z) for the inverse
+    T2 z;
+    z.x = X0.x - X1.y;
+    z.y = -(X0.y + X1.x);
+    b0[i * N + k] = z;
+  }
+  __syncthreads();
+  T2* r = fft_cols<T2, T>(b0, b1, 9, N, g.plan, tw);
+  for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
+    int l = t / (9 * N), rem = t - l * 9 * N;
+    int i = rem / N, a = rem - i * N;
+    int b = l ? bl1 : bl0;
+    if (b < N) {
+      T2 z = r[i * N + a];  // conj of the unscaled inverse
+      long long v = a + (long long)N * b + (long long)N * N * c;
+      y[i * N3 + v] = l ? -z.y : z.x;
+    }
+  }
+}
+
+template <typename T>
+size_t smem_a(int N) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * N); }
+template <typename T>
+size_t smem_b(int N, int tk) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * tk * N); }
+template <typename T>
+size_t smem_c(int N, int tk) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * tk * N); }
+
+}  // namespace
+
+FftPlan make_plan(int N) {
+  FftPlan p;
+  p.n = N;
+  p.nst = 0;
+  int m = N, Ns = 1;
+  auto push = [&](int r) {
+    p.R[p.nst] = r;
+    p.Ns[p.nst] = Ns;
+    Ns *= r;
+    p.nst++;
+    m /= r;
+  };
+  while (m % 8 == 0) push(8);
+  while (m % 4 == 0) push(4);
+  while (m % 2 == 0) push(2);
+  for (int f = 3; m > 1; f += 2)
+    while (m % f == 0) push(f);
+  return p;
+}
+
+template <typename T>
+cudaError_t green_setup(int N) {
+  cudaError_t e;
+  size_t a = smem_a<T>(N), b = smem_b<T>(N, 16), c = smem_c<T>(N, 2);
+  if ((e = cudaFuncSetAttribute(pass_a<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
+  if ((e = cudaFuncSetAttribute(pass_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b))) return e;
+  if ((e = cudaFuncSetAttribute(pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c))) return e;
+  if ((e = cudaFuncSetAttribute(pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                        const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
+  const int N = g.N, H = g.H;
+  g.tkb = 16;
+  g.tkc = 2;
+  const int npair = (N + 1) / 2;
+  pass_a<T, T><<<npair * N, 256, smem_a<T>(N), st>>>(x, K4, flgK, S, g, tw);
+  dim3 gb((H + g.tkb - 1) / g.tkb, N, 9);
+  pass_b<T><<<gb, 256, smem_b<T>(N, g.tkb), st>>>(S, g, tw, 0);
+  dim3 gc((H + g.tkc - 1) / g.tkc, N);
+  pass_c<T><<<gc, 256, smem_c<T>(N, g.tkc), st>>>(S, g, tw);
+  pass_b<T><<<gb, 256, smem_b<T>(N, g.tkb), st>>>(S, g, tw, 1);
+  pass_e<T><<<npair * N, 256, smem_a<T>(N), st>>>(S, y, g, tw);
+  return cudaGetLastError();
+}
+
+template cudaError_t green_setup<double>(int);
+template cudaError_t green_setup<float>(int);
+template cudaError_t green_apply<double>(const double*, const double*, int, double*, double2*,
+                                         const double2*, GridDesc, cudaStream_t);
+template cudaError_t green_apply<float>(const float*, const float*, int, float*, float2*,
+                                        const float2*, GridDesc, cudaStream_t);

@@ -1,0 +1,33 @@
+// fft_green.cuh -- declarations of the fused FFT + Green-operator passes.
+#pragma once
+#include "common.cuh"
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { typedef double2 t; };
+template <> struct Vec2<float> { typedef float2 t; };
+
+// Mixed-radix factorisation N = prod R[s]; Ns[s] = prod of the radices before stage s.
+struct FftPlan {
+  int n, nst;
+  int R[16];
+  int Ns[16];
+};
+
+struct GridDesc {
+  int N, H;          // points per axis, half-spectrum length N/2+1
+  long long N3;
+  int Nhalf, gmap;   // reference Nhalf (src/FFT_init.f:146-147) and the q mapping
+  double inv_n3;     // backward scale 1/N^3
+  int tkb, tkc;      // columns per block in passes B and C
+  FftPlan plan;
+};
+
+FftPlan make_plan(int N);
+
+// y = G(K4 : x) (flgK = 1) or y = G(x); S is the spectral scratch (9 * N * N * H complex),
+// tw the length-N forward twiddle table.  All on stream st.
+template <typename T>
+cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                        const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st);
+template <typename T>
+cudaError_t green_setup(int N);

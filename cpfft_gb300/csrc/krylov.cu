@@ -1,0 +1,213 @@
+// krylov.cu -- vector kernels of the device-resident Newton-Krylov loop: CG updates,
+// deterministic two-stage reductions (warp shuffles inside a block, one partial per
+// block, a single-block final pass), field fills and precision casts.
+#include "krylov.cuh"
+
+namespace {
+
+constexpr int RB = 256;  // threads per reduction block
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double ws[RB / 32];
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) ws[w] = v;
+  __syncthreads();
+  v = threadIdx.x < RB / 32 ? ws[threadIdx.x] : 0.0;
+  if (w == 0) v = warp_sum(v);
+  return v;  // valid in thread 0
+}
+
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(RB) k_dot(const TA* __restrict__ a, const TB* __restrict__ b,
+                                            long long n, double* __restrict__ part) {
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB)
+    s += (double)a[i] * (double)b[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// final pass: sc[slot] = sum(part); op-specific scalar follow-ups for CG
+__global__ void __launch_bounds__(1024) k_final(const double* __restrict__ part, int np,
+                                                double* __restrict__ sc, int slot, int op) {
+  __shared__ double ws[32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < np; i += 1024) v += part[i];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = ws[threadIdx.x];
+    v = warp_sum(v);
+    if (threadIdx.x == 0) {
+      sc[slot] = v;
+      if (op == OP_ALPHA) sc[SC_ALPHA] = sc[SC_RR] / v;          // alpha = rr / pAp
+      else if (op == OP_BETA) sc[SC_BETA] = v / sc[SC_RR];       // beta = rr_new / rr
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha Ap ; partial r.r
+template <typename T>
+__global__ void __launch_bounds__(RB) k_cg_xr(T* __restrict__ x, T* __restrict__ r,
+                                              const T* __restrict__ p, const T* __restrict__ Ap,
+                                              long long n, const double* __restrict__ sc,
+                                              double* __restrict__ part) {
+  const double alpha = sc[SC_ALPHA];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
+    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
+    T ri = (T)((double)r[i] - alpha * (double)Ap[i]);
+    r[i] = ri;
+    s += (double)ri * (double)ri;
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// p = r + beta p ; rr <- rr_new
+template <typename T>
+__global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, long long n,
+                       double* __restrict__ sc) {
+  const double beta = sc[SC_BETA];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = (T)((double)r[i] + beta * (double)p[i]);
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc[SC_RR] = sc[SC_RRNEW];
+}
+
+__global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, double a, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void k_scale(double* __restrict__ y, double a, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] *= a;
+}
+__global__ void k_sub(double* __restrict__ y, const double* __restrict__ a,
+                      const double* __restrict__ b, long long n) {  // y = a - b
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = a[i] - b[i];
+}
+// fill component c of a (9, N3) field with v[c]
+__global__ void k_fill9(double* __restrict__ y, long long N3, double v0, double v1, double v2,
+                        double v3, double v4, double v5, double v6, double v7, double v8) {
+  const double v[9] = {v0, v1, v2, v3, v4, v5, v6, v7, v8};
+  long long n = 9 * N3;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = v[i / N3];
+}
+__global__ void k_add_const(double* __restrict__ y, double v, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] += v;
+}
+// y_f = (float)(x * s)
+__global__ void k_to_f32(float* __restrict__ y, const double* __restrict__ x, double s, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = (float)(x[i] * s);
+}
+// y += s * (double)x_f
+__global__ void k_add_f32(double* __restrict__ y, const float* __restrict__ x, double s, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] += s * (double)x[i];
+}
+// sums of each of the 9 components of a (9, N3) field (one partial per block and comp)
+__global__ void __launch_bounds__(RB) k_sum9(const double* __restrict__ x, long long N3,
+                                             double* __restrict__ part) {
+  for (int c = 0; c < 9; c++) {
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < N3; i += (long long)gridDim.x * RB)
+      s += x[c * N3 + i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) part[c * gridDim.x + blockIdx.x] = s;
+    __syncthreads();
+  }
+}
+
+int grid_for(long long n, int bs) {
+  long long b = (n + bs - 1) / bs;
+  return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
+}
+
+}  // namespace
+
+cudaError_t dev_dot(const double* a, const double* b, long long n, double* part, double* sc,
+                    int slot, int op, cudaStream_t st) {
+  k_dot<double, double><<<NPART, RB, 0, st>>>(a, b, n, part);
+  k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
+  return cudaGetLastError();
+}
+cudaError_t dev_dot_f(const float* a, const float* b, long long n, double* part, double* sc,
+                      int slot, int op, cudaStream_t st) {
+  k_dot<float, float><<<NPART, RB, 0, st>>>(a, b, n, part);
+  k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t dev_cg_xr(T* x, T* r, const T* p, const T* Ap, long long n, double* part, double* sc,
+                      cudaStream_t st) {
+  k_cg_xr<T><<<NPART, RB, 0, st>>>(x, r, p, Ap, n, sc, part);
+  k_final<<<1, 1024, 0, st>>>(part, NPART, sc, SC_RRNEW, OP_BETA);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st) {
+  k_cg_p<T><<<grid_for(n, 256), 256, 0, st>>>(p, r, n, sc);
+  return cudaGetLastError();
+}
+template cudaError_t dev_cg_xr<double>(double*, double*, const double*, const double*, long long,
+                                       double*, double*, cudaStream_t);
+template cudaError_t dev_cg_xr<float>(float*, float*, const float*, const float*, long long,
+                                      double*, double*, cudaStream_t);
+template cudaError_t dev_cg_p<double>(double*, const double*, long long, double*, cudaStream_t);
+template cudaError_t dev_cg_p<float>(float*, const float*, long long, double*, cudaStream_t);
+
+cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStream_t st) {
+  k_axpy<<<grid_for(n, 256), 256, 0, st>>>(y, x, a, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st) {
+  k_scale<<<grid_for(n, 256), 256, 0, st>>>(y, a, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st) {
+  k_sub<<<grid_for(n, 256), 256, 0, st>>>(y, a, b, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_fill9(double* y, long long N3, const double* v, cudaStream_t st) {
+  k_fill9<<<grid_for(9 * N3, 256), 256, 0, st>>>(y, N3, v[0], v[1], v[2], v[3], v[4], v[5], v[6],
+                                                  v[7], v[8]);
+  return cudaGetLastError();
+}
+cudaError_t dev_add_const(double* y, double v, long long n, cudaStream_t st) {
+  k_add_const<<<grid_for(n, 256), 256, 0, st>>>(y, v, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_to_f32(float* y, const double* x, double s, long long n, cudaStream_t st) {
+  k_to_f32<<<grid_for(n, 256), 256, 0, st>>>(y, x, s, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_add_f32(double* y, const float* x, double s, long long n, cudaStream_t st) {
+  k_add_f32<<<grid_for(n, 256), 256, 0, st>>>(y, x, s, n);
+  return cudaGetLastError();
+}
+cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, int slot0,
+                     cudaStream_t st) {
+  k_sum9<<<NPART, RB, 0, st>>>(x, N3, part);
+  for (int c = 0; c < 9; c++)
+    k_final<<<1, 1024, 0, st>>>(part + c * NPART, NPART, sc, slot0 + c, OP_STORE);
+  return cudaGetLastError();
+}

@@ -1,0 +1,32 @@
+// krylov.cuh -- device vector operations for the Newton-Krylov loop.
+#pragma once
+#include "common.cuh"
+
+constexpr int NPART = 1024;  // partial sums per reduction (blocks of the first pass)
+
+// device scalar slots
+enum {
+  SC_RR = 0, SC_PAP = 1, SC_RRNEW = 2, SC_ALPHA = 3, SC_BETA = 4, SC_TMP = 5,
+  SC_SUM9 = 8,     // 9 slots: component sums
+  SC_COUNT = 32
+};
+enum { OP_STORE = 0, OP_ALPHA = 1, OP_BETA = 2 };
+
+cudaError_t dev_dot(const double* a, const double* b, long long n, double* part, double* sc,
+                    int slot, int op, cudaStream_t st);
+cudaError_t dev_dot_f(const float* a, const float* b, long long n, double* part, double* sc,
+                      int slot, int op, cudaStream_t st);
+template <typename T>
+cudaError_t dev_cg_xr(T* x, T* r, const T* p, const T* Ap, long long n, double* part, double* sc,
+                      cudaStream_t st);
+template <typename T>
+cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st);
+cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
+cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st);
+cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st);
+cudaError_t dev_fill9(double* y, long long N3, const double* v, cudaStream_t st);
+cudaError_t dev_add_const(double* y, double v, long long n, cudaStream_t st);
+cudaError_t dev_to_f32(float* y, const double* x, double s, long long n, cudaStream_t st);
+cudaError_t dev_add_f32(double* y, const float* x, double s, long long n, cudaStream_t st);
+cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, int slot0,
+                     cudaStream_t st);

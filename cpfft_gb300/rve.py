@@ -1,0 +1,174 @@
+"""Synthetic RVE inputs for the named workloads.
+
+No public dataset is involved: microstructures are periodic Voronoi tessellations of
+seeded uniform points, orientations are Haar-random on SO(3) (Shoemake's subgroup
+algorithm), converted to the Kocks angles the reference's orientation files carry
+(src/mm10_a.f:1287-1345 convention).  Loading follows the reference's `.in` loading
+semantics (src/inlod.f:57-63, src/inlodcase.f): BC_all(:, step) accumulates the
+per-step increments and adds 1 on the diagonal of prescribed F components.
+"""
+from dataclasses import dataclass
+
+import numpy as np
+
+# Material of the named workloads (MPa, s): FCC {111}<110>, anisotropic type-3
+# elasticity C11=C33=168.4, C12=C13=121.4, C44=C55=75.4 GPa, Voce hardening.
+FCC_VOCE = dict(
+    slip_type=1, elastic_type=3, e=0.0, nu=0.0, mu=0.0,
+    C11=168400.0, C12=121400.0, C13=121400.0, C33=168400.0, C44=75400.0, C55=75400.0,
+    h_type=1, harden_n=20.0, tau_y=50.0, tau_v=100.0, theta_0=400.0, voce_m=1.0,
+    gamma_bar=1.0e-3, iD_v=0.0, alter_mode=1,
+    atol=1.0e-10, atol1=1.0e-10, rtol=1.0e-10, rtol1=1.0e-10, miter=30,
+    exact_j22=1,
+)
+
+# component order of 9-vectors: 11,12,13,21,22,23,31,32,33
+COMP = ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]
+
+
+def haar_quaternions(n, rng):
+    """Uniform random unit quaternions (w, x, y, z) by Shoemake's method."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1.0 - u1), np.sqrt(u1)
+    q = np.stack([b * np.cos(2 * np.pi * u3), a * np.sin(2 * np.pi * u2),
+                  a * np.cos(2 * np.pi * u2), b * np.sin(2 * np.pi * u3)], axis=1)
+    return q
+
+
+def quat_to_matrix(q):
+    w, x, y, z = q.T
+    R = np.empty((len(q), 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - w * z)
+    R[:, 0, 2] = 2 * (x * z + w * y)
+    R[:, 1, 0] = 2 * (x * y + w * z)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - w * x)
+    R[:, 2, 0] = 2 * (x * z - w * y)
+    R[:, 2, 1] = 2 * (y * z + w * x)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def kocks_matrix(ang_deg):
+    """Rotation built from Kocks angles (psi, theta, phi) in degrees, the formula of
+    mm10_rotation_matrix (src/mm10_a.f:1287-1345)."""
+    a = np.radians(np.atleast_2d(ang_deg))
+    psi, th, phi = a[:, 0], a[:, 1], a[:, 2]
+    s, c = np.sin, np.cos
+    r = np.empty((len(a), 3, 3))
+    r[:, 0, 0] = -s(psi) * s(phi) - c(psi) * c(phi) * c(th)
+    r[:, 0, 1] = c(psi) * s(phi) - s(psi) * c(phi) * c(th)
+    r[:, 0, 2] = c(phi) * s(th)
+    r[:, 1, 0] = s(psi) * c(phi) - c(psi) * s(phi) * c(th)
+    r[:, 1, 1] = -c(psi) * c(phi) - s(psi) * s(phi) * c(th)
+    r[:, 1, 2] = s(phi) * s(th)
+    r[:, 2, 0] = c(psi) * s(th)
+    r[:, 2, 1] = s(psi) * s(th)
+    r[:, 2, 2] = c(th)
+    return r
+
+
+def matrix_to_kocks(R):
+    """Inverse of kocks_matrix (the extraction of mm10_update_euler_angles,
+    src/mm10_a.f:1171-1222), angles in degrees."""
+    psi = np.arctan2(R[:, 2, 1], R[:, 2, 0])
+    phi = np.arctan2(R[:, 1, 2], R[:, 0, 2])
+    th = np.arccos(np.clip(R[:, 2, 2], -1.0, 1.0))
+    return np.degrees(np.stack([psi, th, phi], axis=1))
+
+
+def quat_to_kocks(q):
+    return matrix_to_kocks(quat_to_matrix(q))
+
+
+def periodic_voronoi(N, ngrains, rng):
+    """Grain id (0-based) per voxel of an N^3 periodic Voronoi tessellation.  Voxel
+    v = a + N*b + N*N*c sits at x = ((c+0.5)/N, (b+0.5)/N, (a+0.5)/N) (tensor index 1
+    pairs with the slowest memory axis, src/FFT_init.f:310-318)."""
+    seeds = rng.random((ngrains, 3))
+    g = (np.arange(N) + 0.5) / N
+    xc, xb, xa = np.meshgrid(g, g, g, indexing="ij")  # c slowest, a fastest
+    pts = np.stack([xc.ravel(), xb.ravel(), xa.ravel()], axis=1)
+    try:
+        from scipy.spatial import cKDTree
+        tree = cKDTree(seeds, boxsize=1.0)
+        _, idx = tree.query(pts)
+        return idx.astype(np.int64)
+    except ImportError:  # pragma: no cover - scipy missing on a host
+        best = np.full(len(pts), np.inf)
+        idx = np.zeros(len(pts), dtype=np.int64)
+        for k, s in enumerate(seeds):
+            d = pts - s
+            d -= np.round(d)
+            r2 = (d * d).sum(1)
+            m = r2 < best
+            best[m] = r2[m]
+            idx[m] = k
+        return idx
+
+
+@dataclass
+class RVE:
+    N: int
+    grains: np.ndarray      # (N3,) 0-based grain id
+    kocks: np.ndarray       # (3, N3) Kocks angles in degrees (column-major (N3,3))
+    mat_list: np.ndarray    # (N3,) 1-based crystal number
+    crystals: list          # crystal dicts
+    quats: np.ndarray       # (ngrains, 4)
+
+
+def make_rve(N, ngrains, seed, crystal=None):
+    rng = np.random.default_rng(seed)
+    grains = periodic_voronoi(N, ngrains, rng)
+    q = haar_quaternions(ngrains, rng)
+    ang = quat_to_kocks(q)                      # (ngrains, 3)
+    kocks = np.ascontiguousarray(ang[grains].T)  # (3, N3)
+    crystal = dict(crystal or FCC_VOCE)
+    return RVE(N=N, grains=grains, kocks=kocks,
+               mat_list=np.ones(N ** 3, dtype=np.int32), crystals=[crystal], quats=q)
+
+
+@dataclass
+class Loading:
+    BC_all: np.ndarray   # (nstep, 9)
+    isNBC: np.ndarray    # (9,) int
+    name: str
+
+
+def _accumulate(incr, isNBC, nstep):
+    """BC_all as inlod builds it (src/inlod.f:57-63) for constant per-step increments."""
+    mults = np.ones(nstep)
+    bc = np.cumsum(np.outer(mults, incr), axis=0)
+    for d in (0, 4, 8):
+        if not isNBC[d]:
+            bc[:, d] += 1.0
+    return bc
+
+
+def uniaxial_tension(total_strain, nstep):
+    """F_xx prescribed; F_xy = F_xz = F_yz = 0 prescribed to suppress the rigid rotation
+    about the load axis; the other five P components held at zero."""
+    isNBC = np.array([0, 0, 0, 1, 1, 0, 1, 1, 1], dtype=np.int32)
+    incr = np.zeros(9)
+    incr[0] = total_strain / nstep
+    return Loading(_accumulate(incr, isNBC, nstep), isNBC, "uniaxial_tension")
+
+
+def plane_strain_compression(total_strain, nstep):
+    """F_zz decreasing, F_yy = 1, F_xy = F_xz = F_yz = 0 prescribed; P_xx, P_yx, P_zx,
+    P_zy held at zero."""
+    isNBC = np.array([1, 0, 0, 1, 0, 0, 1, 1, 0], dtype=np.int32)
+    incr = np.zeros(9)
+    incr[8] = -total_strain / nstep
+    return Loading(_accumulate(incr, isNBC, nstep), isNBC, "plane_strain_compression")
+
+
+def uniaxial_strain(direction, total_strain, nstep):
+    """Fully prescribed F = I + eps n (x) n (a random tensile direction cannot be
+    written with the deck's per-component keywords, src/inlodcase.f)."""
+    n = np.asarray(direction, dtype=np.float64)
+    n = n / np.linalg.norm(n)
+    isNBC = np.zeros(9, dtype=np.int32)
+    incr = (total_strain / nstep) * np.outer(n, n).ravel()
+    return Loading(_accumulate(incr, isNBC, nstep), isNBC, "uniaxial_strain")

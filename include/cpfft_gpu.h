@@ -1,0 +1,192 @@
+/*
+ * cpfft_gpu.h -- C-ABI of the GB300 finite-strain FFT crystal-plasticity hot path.
+ *
+ * This is the drop-in boundary for the Fortran driver of CPFFT (maranGit/CPFFT).  The
+ * host keeps its .in parser, material/crystal blocks and result writers; the bodies of
+ * the routines listed below become thin ISO_C_BINDING calls into this library.  All
+ * arguments are plain pointers and sizes; fields use the reference's column-major
+ * layouts:
+ *   - a 9-component field is (N3, 9), component order 11,12,13,21,22,23,31,32,33
+ *     (src/drive_eps_sig.f:205-226), voxel index v = a + N*b + N*N*c with `a` the
+ *     fastest memory axis (src/FFT_init.f:310-318);
+ *   - a 4th-order field is (N3, 81), column (ij)(kl) = 9*(3*(i-1)+j-1) + 3*(k-1)+l
+ *     (src/G_K_dF.f:258-264, src/cep2A.f:133-154).
+ * Everything is FP64 at the boundary.
+ *
+ * Threading: every call must come from one host thread; the library owns one CUDA
+ * stream and one global context (the reference keeps its state in module arrays,
+ * src/mod_fft.f).  Calls are not re-entrant.
+ *
+ * Return codes: 0 = success, > 0 = warning, < 0 = error (see CPFFT_* below).  The
+ * reference aborts (`die_abort`, src/mpi_code.f:35-53) on every error; a Fortran caller
+ * maps negative codes to `die_abort` to keep that behaviour.
+ */
+#ifndef CPFFT_GPU_H
+#define CPFFT_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define CPFFT_OK                     0
+#define CPFFT_WARN_LOCAL_FALLBACK    1   /* >= 1 voxel's local mm10 solve failed        */
+#define CPFFT_ERR_CG_MAXIT          -1   /* fftPcg hit maxIter (src/FFT_nr3.f:335-339)   */
+#define CPFFT_ERR_NEWTON_MAXIT      -2   /* Newton loop (src/FFT_nr3.f:116-119)          */
+#define CPFFT_ERR_NBC_MAXIT         -3   /* P_bar loop (src/FFT_nr3.f:153-156)           */
+#define CPFFT_ERR_NBC_SINGULAR      -4   /* dgesv info /= 0 (src/FFT_nr3.f:417-421)      */
+#define CPFFT_ERR_BAD_ARG           -5
+#define CPFFT_ERR_CUDA              -6
+#define CPFFT_ERR_NOT_INIT          -7
+#define CPFFT_ERR_CG_TOL            -8   /* improper CG tolerance (src/FFT_nr3.f:248-251)*/
+#define CPFFT_ERR_NO_MEMORY         -9
+#define CPFFT_ERR_NONFINITE        -10   /* NaN/Inf reached a global residual            */
+
+/* Green-operator frequency mapping (src/FFT_init.f:146-147, 310-318, 354-385). */
+#define CPFFT_G_REF_SHIFT  0   /* bit-faithful to the reference: q = ((k-Nhalf) mod N)+1-Nhalf */
+#define CPFFT_G_CENTERED   1   /* signed wavenumber (identical to REF_SHIFT for odd N)         */
+
+/* Krylov / Green precision (north-star "precision" pattern). */
+#define CPFFT_PREC_FP64    0   /* plain: every operator in FP64                                */
+#define CPFFT_PREC_MIXED   1   /* FP32 Green/FFT/CG inner iterations, FP64 outer refinement    */
+
+/*
+ * One crystal definition: the fields of the reference's `crystal` block that the
+ * FCC + Voce path reads (src/mod_crystals.f:231-410 defaults, 1796-1880 elasticity;
+ * keyword parser src/incrystal.f).  Units are the deck's (MPa, s).
+ */
+typedef struct cpfft_crystal {
+    int    slip_type;      /* 1 = fcc {111}<110>, 12 systems (only value accepted)        */
+    int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
+    double e, nu, mu;
+    double C11, C12, C13, C33, C44, C55;
+    int    h_type;         /* 1 = voce (only value accepted)                              */
+    double harden_n;       /* rate exponent                                               */
+    double tau_y, tau_v, theta_0, voce_m;
+    double gamma_bar;      /* eps_dot_0_y                                                 */
+    double iD_v;           /* diffusion slip term                                         */
+    int    alter_mode;     /* 1: dg = gamma_bar * dt (src/mm10_a.f:2075-2076)             */
+    double atol, atol1, rtol, rtol1;   /* local Newton tolerances                          */
+    int    miter;          /* local Newton iteration cap                                  */
+    int    exact_j22;      /* 0: the reference's d(R2)/d(tau_tilde) (src/mm10_b.f:1942-1968),
+                              which carries an extra sign(1,slip increment) factor and so
+                              converges only linearly once slip reverses on any system;
+                              1: the exact derivative (no such factor). Not a deck keyword. */
+} cpfft_crystal;
+
+/* Per load-step statistics (mirrors the thyme buckets of src/thyme.f:15-47). */
+typedef struct cpfft_stats {
+    int       newton_iters;     /* global Newton iterations, summed over P_bar passes      */
+    int       nbc_iters;        /* P_bar (natural BC) passes                               */
+    int       cg_solves;        /* fftPcg calls                                            */
+    int       cg_iters;         /* total CG iterations                                     */
+    int       stress_updates;   /* full-grid drive_eps_sig passes                          */
+    int       local_fallbacks;  /* voxel updates whose local solve failed                  */
+    long long local_iters;      /* sum over voxel updates of local Newton iterations       */
+    double    res_fft;          /* last ||dF|| / ||F|| (src/FFT_nr3.f:114)                 */
+    double    res_pbar;         /* last relative P_bar residual (src/FFT_nr3.f:143-147)    */
+    double    res_equil;        /* ||G(P)|| / (sqrt(N3) * ||P_bar||) after the step        */
+    double    t_pcg;            /* seconds in CG (bucket 1)                                */
+    double    t_sigeps;         /* seconds in stress updates (bucket 2)                    */
+    double    t_total;          /* seconds in the whole call                               */
+} cpfft_stats;
+
+/*
+ * Set up the grid, the material point data and the device state.
+ * Replaces FFT_init (src/FFT_init.f:16-177: Ghat4/coeffs tables are not stored, the
+ * Green operator is evaluated from q on the fly), fftAllocate(1/3) (:191-234) and the
+ * per-call orientation setup of setup_mm10_rknstr (src/drive_eps_sig.f:537-1002),
+ * which is done once here.
+ *   N          grid points per axis (N3 = N^3 voxels)
+ *   matList    (N3) 1-based crystal number per voxel (src/mod_fft.f:550)
+ *   kocks_deg  (N3, 3) column-major Kocks angles in degrees (psi, theta, phi)
+ *   props      (ncrystals) crystal definitions
+ *   tstep      time step of every load step (src/indypm.f: "time step")
+ *   g_mapping  CPFFT_G_REF_SHIFT or CPFFT_G_CENTERED
+ * Fn = Fn1 = I, Pn = Pn1 = 0 afterwards (src/FFT_init.f:157-161).
+ */
+int cpfft_init(int N, const int* matList, const double* kocks_deg,
+               const cpfft_crystal* props, int ncrystals, double tstep, int g_mapping);
+
+/* Select the Krylov precision (CPFFT_PREC_*) and the learned warm start (0/1).
+ * No counterpart in the reference (spec precision and learned patterns). */
+int cpfft_set_mode(int precision, int warm_start);
+
+/*
+ * Stress update of every voxel: replaces drive_eps_sig(step, iter)
+ * (src/drive_eps_sig.f:16-45, do_nleps_block :57-340, rstgp1/mm10 below it).
+ * Fn, Fn1 (N3,9) host arrays; writes Pn1 (N3,9) and K4 (N3,81) host arrays (either
+ * may be NULL to leave the result on the device only).  Uses and advances the
+ * device-resident history at n+1; the history at n changes only in cpfft_commit_step.
+ * iter == 0 selects the explicit predictor with the elastic tangent
+ * (src/rstgp1.f:870-877).  Returns CPFFT_WARN_LOCAL_FALLBACK if a local solve failed.
+ */
+int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1,
+                        double* Pn1, double* K4);
+
+/*
+ * y = G(K4 : x) (flgK = 1) or y = G(x) (flgK = 0): replaces G_K_dF (src/G_K_dF.f:11-87).
+ * K4 is the device copy written by the last cpfft_stress_update (or cpfft_set_K4).
+ * x, y (N3,9) host arrays.
+ */
+int cpfft_green_apply(const double* x, double* y, int flgK);
+
+/* Upload a tangent field K4 (N3,81) from the host (for callers that own K4). */
+int cpfft_set_K4(const double* K4);
+
+/*
+ * Unpreconditioned CG on G(K4 : x) = b from x = 0: replaces fftPcg
+ * (src/FFT_nr3.f:214-360; MKL RCI dcg with the user stop test ||r|| <= tol*||b||
+ * or ||r|| <= tol, at most 1000 iterations).  b, x (N3,9) host arrays.
+ * *iters receives the iteration count.
+ */
+int cpfft_cg(const double* b, double* x, double tol, int* iters);
+
+/*
+ * Homogenised tangent C_homo (81, column-major (9,9)): replaces tangent_homo
+ * (src/tangent_homo.f:11-73), 9 CG solves with the device K4.
+ */
+int cpfft_tangent_homo(double tolPCG, double* C_homo);
+
+/*
+ * One whole load step resident on the device: replaces the body of the step loop of
+ * FFT_nr3 (src/FFT_nr3.f:51-185) up to and including the state roll-over
+ * (Fn <- Fn1, Pn <- Pn1, update).  The homogenised tangent used by the first
+ * NBC_update of the step is the one left by the previous step (or by
+ * cpfft_nr3_begin for step 1), exactly as the reference keeps C_homo across steps.
+ *   BC      (9) this step's column of BC_all (src/inlod.f:57-63)
+ *   isNBC   (9) 1 where P is prescribed, 0 where F is prescribed
+ *   Pbar    (9) out: volume-averaged P after the step
+ *   st      out: statistics (may be NULL)
+ */
+int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR,
+                   double tolPCG, int maxIter, double* Pbar, cpfft_stats* st);
+
+/*
+ * Start of FFT_nr3 (src/FFT_nr3.f:36-47): the initial drive_eps_sig(1,0) of the
+ * `compute` command (src/FFT_finite_3d.f:145) and the first tangent_homo.
+ */
+int cpfft_nr3_begin(double tolPCG);
+
+/* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
+ * compact history at n (N3, CPFFT_HIST_WORDS) used by the result writers. */
+#define CPFFT_HIST_WORDS 23   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) */
+int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history);
+
+/* State roll-over Fn <- Fn1, Pn <- Pn1, history n <- n+1: replaces update
+ * (src/update.f:16-193) and FFT_nr3.f:173-179 in mirror mode. */
+int cpfft_commit_step(void);
+
+/* Overwrite the device Fn / Fn1 fields (N3,9) from the host (mirror mode). */
+int cpfft_set_F(const double* Fn, const double* Fn1);
+
+/* Release every device allocation. */
+void cpfft_finalize(void);
+
+/* Human-readable text of the last error (static storage). */
+const char* cpfft_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPFFT_GPU_H */

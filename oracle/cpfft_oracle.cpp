@@ -1,0 +1,1516 @@
+// cpfft_oracle.cpp -- CPU restatement of the CPFFT finite-strain FFT crystal-plasticity
+// hot path (TEST INFRASTRUCTURE ONLY; the product never links it).
+//
+// Each routine cites the reference routine (path:line, relative to the reference
+// project) it restates.  Parity is unpinned: the reference has no tests or golden
+// data and cannot be built here; the oracle is checked against analytic known answers
+// (tests/test_oracle_*.py).  Third-party arithmetic the reference takes from Intel MKL
+// (no version pinned, src/makefile:9-13) is restated from the published algorithms:
+// DFTI -> an exact mixed-radix DFT, RCI dcg -> textbook Hestenes-Stiefel CG,
+// dgesv -> LU with partial pivoting, dsytrf/dsytri -> Gauss-Jordan inverse.
+// The eigenvalues of C = F^T F use the trigonometric closed form of the cubic
+// (O. K. Smith, Comm. ACM 4(4) 168, 1961).
+#include "cpfft_oracle.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+typedef double M3[3][3];
+typedef double M6[6][6];
+const double PI = 3.141592653589793;  // mm10_constants pi (src/mod_crystals.f:121)
+
+inline double sgn1(double x) { return x < 0.0 ? -1.0 : 1.0; }  // Fortran sign(1,x)
+
+// Voigt pairs in the reference order xx,yy,zz,xy,yz,xz
+const int VI[6] = {0, 1, 2, 0, 1, 0};
+const int VJ[6] = {0, 1, 2, 1, 2, 2};
+
+void mm33(const M3 a, const M3 b, M3 c) {  // c = a b
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      c[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j];
+}
+void tr33(const M3 a, M3 b) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) b[i][j] = a[j][i];
+}
+double det33(const M3 a) {  // cep2A_det33 order (src/cep2A.f:341-360)
+  double d = a[0][0] * a[1][1] * a[2][2];
+  d = d + a[0][1] * a[1][2] * a[2][0];
+  d = d + a[0][2] * a[1][0] * a[2][1];
+  d = d - a[0][0] * a[1][2] * a[2][1];
+  d = d - a[0][1] * a[1][0] * a[2][2];
+  d = d - a[0][2] * a[1][1] * a[2][0];
+  return d;
+}
+
+// inv33 (src/drive_eps_sig.f:1017-1100): cofactor inverse and determinant
+double inv33(const M3 a, M3 g) {
+  double j1 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  double j2 = a[1][0] * a[2][2] - a[1][2] * a[2][0];
+  double j3 = a[1][0] * a[2][1] - a[1][1] * a[2][0];
+  double dj = a[0][0] * j1 - a[0][1] * j2 + a[0][2] * j3;
+  g[0][0] = j1 / dj;
+  g[1][0] = -j2 / dj;
+  g[2][0] = j3 / dj;
+  g[0][1] = (a[2][1] * a[0][2] - a[0][1] * a[2][2]) / dj;
+  g[1][1] = (a[0][0] * a[2][2] - a[2][0] * a[0][2]) / dj;
+  g[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / dj;
+  g[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / dj;
+  g[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / dj;
+  g[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / dj;
+  return dj;
+}
+
+// LU with partial pivoting, solve a x = b for nrhs right-hand sides (dgesv).
+// a is n x n row-major (destroyed), b is n x nrhs row-major.  Returns 0 or k+1 for a
+// zero pivot at step k (LAPACK's info convention).
+int lu_solve(int n, double* a, int nrhs, double* b) {
+  int info = 0;
+  for (int k = 0; k < n; k++) {
+    int p = k;
+    double best = std::fabs(a[k * n + k]);
+    for (int i = k + 1; i < n; i++) {
+      double v = std::fabs(a[i * n + k]);
+      if (v > best) { best = v; p = i; }
+    }
+    if (a[p * n + k] == 0.0) { if (!info) info = k + 1; continue; }
+    if (p != k) {
+      for (int j = 0; j < n; j++) std::swap(a[k * n + j], a[p * n + j]);
+      for (int j = 0; j < nrhs; j++) std::swap(b[k * nrhs + j], b[p * nrhs + j]);
+    }
+    double inv = 1.0 / a[k * n + k];
+    for (int i = k + 1; i < n; i++) {
+      double l = a[i * n + k] * inv;
+      a[i * n + k] = l;
+      for (int j = k + 1; j < n; j++) a[i * n + j] -= l * a[k * n + j];
+      for (int j = 0; j < nrhs; j++) b[i * nrhs + j] -= l * b[k * nrhs + j];
+    }
+  }
+  if (info) return info;
+  for (int j = 0; j < nrhs; j++)
+    for (int i = n - 1; i >= 0; i--) {
+      double s = b[i * nrhs + j];
+      for (int k = i + 1; k < n; k++) s -= a[i * n + k] * b[k * nrhs + j];
+      b[i * nrhs + j] = s / a[i * n + i];
+    }
+  return 0;
+}
+
+// Gauss-Jordan inverse of a 6x6 (mm10_invsym's role, src/mm10_a.f:1370-1395)
+void inv66(const M6 a, M6 out) {
+  double m[6][12];
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 12; j++) m[i][j] = j < 6 ? a[i][j] : (j - 6 == i ? 1.0 : 0.0);
+  for (int k = 0; k < 6; k++) {
+    int p = k;
+    for (int i = k + 1; i < 6; i++)
+      if (std::fabs(m[i][k]) > std::fabs(m[p][k])) p = i;
+    for (int j = 0; j < 12; j++) std::swap(m[k][j], m[p][j]);
+    double inv = 1.0 / m[k][k];
+    for (int j = 0; j < 12; j++) m[k][j] *= inv;
+    for (int i = 0; i < 6; i++)
+      if (i != k) {
+        double f = m[i][k];
+        for (int j = 0; j < 12; j++) m[i][j] -= f * m[k][j];
+      }
+  }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) out[i][j] = m[i][j + 6];
+}
+
+// ---- rotation helpers (src/mm10_a.f:1287-1520) -------------------------------------
+// Kocks angles in degrees -> crystal rotation g (mm10_rotation_matrix, :1287-1345)
+void kocks_g(const double ang[3], M3 r) {
+  double psi = ang[0] * PI / 180.0, th = ang[1] * PI / 180.0, phi = ang[2] * PI / 180.0;
+  r[0][0] = -std::sin(psi) * std::sin(phi) - std::cos(psi) * std::cos(phi) * std::cos(th);
+  r[0][1] = std::cos(psi) * std::sin(phi) - std::sin(psi) * std::cos(phi) * std::cos(th);
+  r[0][2] = std::cos(phi) * std::sin(th);
+  r[1][0] = std::sin(psi) * std::cos(phi) - std::cos(psi) * std::sin(phi) * std::cos(th);
+  r[1][1] = -std::cos(psi) * std::cos(phi) - std::sin(psi) * std::sin(phi) * std::cos(th);
+  r[1][2] = std::sin(phi) * std::sin(th);
+  r[2][0] = std::cos(psi) * std::sin(th);
+  r[2][1] = std::sin(psi) * std::sin(th);
+  r[2][2] = std::cos(th);
+}
+// 6x6 rotation of a tensor-shear Voigt vector: rv = R (.) R^T (mm10_rt2rve :1400-1447,
+// also getrm1 option 2, src/polar.f:729-780)
+void rt2rve(const M3 r, M6 rv) {
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) {
+      int ia = VI[a], ja = VJ[a], kb = VI[b], lb = VJ[b];
+      rv[a][b] = b < 3 ? r[ia][kb] * r[ja][kb]
+                       : r[ia][kb] * r[ja][lb] + r[ia][lb] * r[ja][kb];
+    }
+}
+// unsigned minors, the reference's 3x3 rotation of its (w23,w13,w12) skew vectors
+// (mm10_rt2rvw :1460-1475)
+void rt2rvw(const M3 t, M3 rv) {
+  rv[0][0] = t[1][1] * t[2][2] - t[1][2] * t[2][1];
+  rv[0][1] = t[1][0] * t[2][2] - t[1][2] * t[2][0];
+  rv[0][2] = t[1][0] * t[2][1] - t[1][1] * t[2][0];
+  rv[1][0] = t[0][1] * t[2][2] - t[0][2] * t[2][1];
+  rv[1][1] = t[0][0] * t[2][2] - t[0][2] * t[2][0];
+  rv[1][2] = t[0][0] * t[2][1] - t[0][1] * t[2][0];
+  rv[2][0] = t[0][1] * t[1][2] - t[0][2] * t[1][1];
+  rv[2][1] = t[0][0] * t[1][2] - t[0][2] * t[1][0];
+  rv[2][2] = t[0][0] * t[1][1] - t[0][1] * t[1][0];
+}
+// rotation of an engineering-shear Voigt strain: d = R^T D R (getrm1 option 1,
+// src/polar.f:680-728)
+void getrm1_opt1(const M3 r, M6 q) {
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) {
+      int ia = VI[a], ja = VJ[a], kb = VI[b], lb = VJ[b];
+      double v = b < 3 ? r[kb][ia] * r[kb][ja]
+                       : 0.5 * (r[kb][ia] * r[lb][ja] + r[lb][ia] * r[kb][ja]);
+      q[a][b] = a < 3 ? v : 2.0 * v;
+    }
+}
+void mv6(const M6 a, const double* x, double* y) {  // mm10_a_mult_type_2 order
+  for (int i = 0; i < 6; i++) y[i] = a[i][0] * x[0];
+  for (int j = 1; j < 6; j++)
+    for (int i = 0; i < 6; i++) y[i] = y[i] + a[i][j] * x[j];
+}
+
+// ---- polar decomposition (rtcmp1/irscp1/ivcmp1, src/polar.f:18-224) ----------------
+void sym3_eigs(const double c[6], double ev[3]) {
+  // c in the reference's packed order c11,c12,c22,c13,c23,c33
+  double a11 = c[0], a12 = c[1], a22 = c[2], a13 = c[3], a23 = c[4], a33 = c[5];
+  double p1 = a12 * a12 + a13 * a13 + a23 * a23;
+  double q = (a11 + a22 + a33) / 3.0;
+  double b11 = a11 - q, b22 = a22 - q, b33 = a33 - q;
+  double p2 = b11 * b11 + b22 * b22 + b33 * b33 + 2.0 * p1;
+  if (p2 <= 0.0) { ev[0] = ev[1] = ev[2] = q; return; }
+  double p = std::sqrt(p2 / 6.0);
+  double ip = 1.0 / p;
+  double B11 = b11 * ip, B22 = b22 * ip, B33 = b33 * ip;
+  double B12 = a12 * ip, B13 = a13 * ip, B23 = a23 * ip;
+  double detB = B11 * (B22 * B33 - B23 * B23) - B12 * (B12 * B33 - B23 * B13) +
+                B13 * (B12 * B23 - B22 * B13);
+  double r = 0.5 * detB;
+  double phi = r <= -1.0 ? PI / 3.0 : (r >= 1.0 ? 0.0 : std::acos(r) / 3.0);
+  double e1 = q + 2.0 * p * std::cos(phi);
+  double e3 = q + 2.0 * p * std::cos(phi + 2.0 * PI / 3.0);
+  double e2 = 3.0 * q - e1 - e3;
+  ev[0] = e3; ev[1] = e2; ev[2] = e1;
+}
+void polar_R(const M3 f, M3 r) {
+  double c[6], cc[6];
+  c[0] = f[0][0] * f[0][0] + f[1][0] * f[1][0] + f[2][0] * f[2][0];
+  c[1] = f[0][0] * f[0][1] + f[1][0] * f[1][1] + f[2][0] * f[2][1];
+  c[2] = f[0][1] * f[0][1] + f[1][1] * f[1][1] + f[2][1] * f[2][1];
+  c[3] = f[0][0] * f[0][2] + f[1][0] * f[1][2] + f[2][0] * f[2][2];
+  c[4] = f[0][1] * f[0][2] + f[1][1] * f[1][2] + f[2][1] * f[2][2];
+  c[5] = f[0][2] * f[0][2] + f[1][2] * f[1][2] + f[2][2] * f[2][2];
+  cc[0] = c[0] * c[0] + c[1] * c[1] + c[3] * c[3];
+  cc[1] = c[0] * c[1] + c[1] * c[2] + c[3] * c[4];
+  cc[2] = c[1] * c[1] + c[2] * c[2] + c[4] * c[4];
+  cc[3] = c[0] * c[3] + c[1] * c[4] + c[3] * c[5];
+  cc[4] = c[1] * c[3] + c[2] * c[4] + c[4] * c[5];
+  cc[5] = c[3] * c[3] + c[4] * c[4] + c[5] * c[5];
+  double ev[3];
+  sym3_eigs(c, ev);
+  for (int i = 0; i < 3; i++) ev[i] = std::sqrt(ev[i]);
+  double iu = ev[0] + ev[1] + ev[2];
+  double iiu = ev[0] * ev[1] + ev[1] * ev[2] + ev[0] * ev[2];
+  double iiiu = ev[0] * ev[1] * ev[2];
+  // inverse right stretch from the invariants (Hoger & Carlson closed form)
+  double a2 = 1.0 / (iiiu * (iu * iiu - iiiu));
+  double b2 = iu * iiu * iiu - iiiu * (iu * iu + iiu);
+  double c2 = -iiiu - iu * (iu * iu - 2.0 * iiu);
+  double d2 = iu;
+  double ui[6];
+  ui[0] = a2 * (b2 + c2 * c[0] + d2 * cc[0]);
+  ui[1] = a2 * (c2 * c[1] + d2 * cc[1]);
+  ui[2] = a2 * (b2 + c2 * c[2] + d2 * cc[2]);
+  ui[3] = a2 * (c2 * c[3] + d2 * cc[3]);
+  ui[4] = a2 * (c2 * c[4] + d2 * cc[4]);
+  ui[5] = a2 * (b2 + c2 * c[5] + d2 * cc[5]);
+  for (int i = 0; i < 3; i++) {
+    r[i][0] = f[i][0] * ui[0] + f[i][1] * ui[1] + f[i][2] * ui[3];
+    r[i][1] = f[i][0] * ui[1] + f[i][1] * ui[2] + f[i][2] * ui[4];
+    r[i][2] = f[i][0] * ui[3] + f[i][1] * ui[4] + f[i][2] * ui[5];
+  }
+}
+
+// ---- crystal data (src/mod_crystals.f:438-515, 1796-1880) --------------------------
+struct Crys {
+  cpfft_crystal p;
+  M6 C0;                 // stiffness in the crystal frame
+  double b[12][3], n[12][3];
+};
+void fcc_systems(double b[12][3], double n[12][3]) {
+  // FCC {111}<110>: slip directions and plane normals, in the reference's order.
+  const double f = 1.0 / std::sqrt(2.0), g = 1.0 / std::sqrt(3.0);
+  const double B[12][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f},
+                           {f, 0, f},  {f, -f, 0}, {0, -f, f}, {-f, 0, -f},
+                           {f, f, 0},  {0, f, f},  {f, 0, -f}, {-f, -f, 0}};
+  const double Nn[12][3] = {{g, g, g},  {g, g, g},  {g, g, g},  {-g, -g, g},
+                            {-g, -g, g}, {-g, -g, g}, {-g, g, g}, {-g, g, g},
+                            {-g, g, g}, {g, -g, g},  {g, -g, g}, {g, -g, g}};
+  for (int s = 0; s < 12; s++)
+    for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
+}
+void crystal_finalize(const cpfft_crystal& p, Crys& c) {
+  c.p = p;
+  fcc_systems(c.b, c.n);
+  std::memset(c.C0, 0, sizeof(c.C0));
+  if (p.elastic_type == 3) {
+    double C22 = p.C11, C23 = p.C13, C66 = p.C55;
+    c.C0[0][0] = p.C11; c.C0[0][1] = p.C12; c.C0[0][2] = p.C13;
+    c.C0[1][0] = p.C12; c.C0[1][1] = C22;   c.C0[1][2] = C23;
+    c.C0[2][0] = p.C13; c.C0[2][1] = C23;   c.C0[2][2] = p.C33;
+    c.C0[3][3] = p.C44; c.C0[4][4] = p.C55; c.C0[5][5] = C66;
+  } else {
+    M6 flex;
+    std::memset(flex, 0, sizeof(flex));
+    double e = p.e, v = p.nu;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) flex[i][j] = i == j ? 1.0 / e : -v / e;
+    double sh = p.elastic_type == 1 ? 2.0 * (1.0 + v) / e : 1.0 / p.mu;
+    for (int i = 3; i < 6; i++) flex[i][i] = sh;
+    inv66(flex, c.C0);
+  }
+}
+
+// Per-voxel orientation data: setup_mm10_rknstr (src/drive_eps_sig.f:537-1002)
+struct VoxProps {
+  M6 C;            // stiffness rotated to the sample frame
+  double ms[12][6], qs[12][3];
+  M3 g;
+};
+void voxel_props(const Crys& cr, const double ang[3], VoxProps& vp) {
+  kocks_g(ang, vp.g);
+  M3 tr;
+  tr33(vp.g, tr);  // trans_rot
+  for (int s = 0; s < 12; s++) {
+    double bs[3], ns[3];
+    for (int i = 0; i < 3; i++) {
+      bs[i] = tr[i][0] * cr.b[s][0] + tr[i][1] * cr.b[s][1] + tr[i][2] * cr.b[s][2];
+      ns[i] = tr[i][0] * cr.n[s][0] + tr[i][1] * cr.n[s][1] + tr[i][2] * cr.n[s][2];
+    }
+    M3 A, As, Aa;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) A[i][j] = bs[i] * ns[j];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        As[i][j] = 0.5 * (A[i][j] + A[j][i]);
+        Aa[i][j] = 0.5 * (A[i][j] - A[j][i]);
+      }
+    // mm10_et2ev / mm10_wt2wv (src/mm10_a.f:1487-1520)
+    vp.ms[s][0] = As[0][0]; vp.ms[s][1] = As[1][1]; vp.ms[s][2] = As[2][2];
+    vp.ms[s][3] = 2.0 * As[0][1]; vp.ms[s][4] = 2.0 * As[1][2]; vp.ms[s][5] = 2.0 * As[0][2];
+    vp.qs[s][0] = Aa[1][2]; vp.qs[s][1] = Aa[0][2]; vp.qs[s][2] = Aa[0][1];
+  }
+  M6 Rs, tmp;
+  rt2rve(tr, Rs);
+  for (int i = 0; i < 6; i++)       // temp66 = C0 * Rs^T
+    for (int j = 0; j < 6; j++) {
+      double s = 0;
+      for (int k = 0; k < 6; k++) s += cr.C0[i][k] * Rs[j][k];
+      tmp[i][j] = s;
+    }
+  for (int i = 0; i < 6; i++)
+    for (int j = 0; j < 6; j++) {
+      double s = 0;
+      for (int k = 0; k < 6; k++) s += Rs[i][k] * tmp[k][j];
+      vp.C[i][j] = s;
+    }
+}
+
+// ---- mm10 (Voce, one crystal) -------------------------------------------------------
+struct State {          // compact history (CPFFT_HIST_WORDS order)
+  double sig[6];
+  double tt;
+  M3 Rp;
+  double D[6];
+  double tt_rate;
+};
+void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f:473-571)
+  std::memset(&s, 0, sizeof(s));
+  for (int i = 0; i < 3; i++) s.Rp[i][i] = 1.0;
+  s.tt = cr.p.tau_y + 1.0e-5;                // mm10_init_voche (:2046-2056)
+}
+void state_pack(const State& s, double* h) {
+  for (int i = 0; i < 6; i++) h[i] = s.sig[i];
+  h[6] = s.tt;
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) h[7 + 3 * j + i] = s.Rp[i][j];  // column-major
+  for (int i = 0; i < 6; i++) h[16 + i] = s.D[i];
+  h[22] = s.tt_rate;
+}
+void state_unpack(const double* h, State& s) {
+  for (int i = 0; i < 6; i++) s.sig[i] = h[i];
+  s.tt = h[6];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) s.Rp[i][j] = h[7 + 3 * j + i];
+  for (int i = 0; i < 6; i++) s.D[i] = h[16 + i];
+  s.tt_rate = h[22];
+}
+
+// the np1 / curr "crystal_state" pieces the Voce routines read
+struct Np1 {
+  double D[6];
+  double tinc, dg;
+  double ms[12][6], qs[12][3], qc[12][3];
+  double tt_rate;
+};
+
+struct Mm10 {
+  const cpfft_crystal* p;
+  const VoxProps* vp;
+  const State* n;
+
+  // mm10_setup (src/mm10_a.f:830-975) + mm10_setup_voche (:2058-2080)
+  void setup(Np1& s, const double D[6], double tinc, const M3 R) const {
+    for (int i = 0; i < 6; i++) s.D[i] = D[i];
+    s.tinc = tinc;
+    double t1 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    double t2 = D[3] * D[3] + D[4] * D[4] + D[5] * D[5];
+    s.dg = std::sqrt((2.0 / 3.0) * (t1 + 0.5 * t2));
+    M3 tnRp, RW, work, RWC;
+    tr33(n->Rp, tnRp);
+    M6 RE;
+    rt2rve(tnRp, RE);
+    rt2rvw(tnRp, RW);
+    mm33(R, tnRp, work);
+    rt2rvw(work, RWC);
+    for (int i = 0; i < 12; i++) {
+      mv6(RE, vp->ms[i], s.ms[i]);
+      for (int a = 0; a < 3; a++) {
+        s.qs[i][a] = RW[a][0] * vp->qs[i][0] + RW[a][1] * vp->qs[i][1] + RW[a][2] * vp->qs[i][2];
+        s.qc[i][a] = RWC[a][0] * vp->qs[i][0] + RWC[a][1] * vp->qs[i][1] + RWC[a][2] * vp->qs[i][2];
+      }
+    }
+    if (p->alter_mode) s.dg = p->gamma_bar * s.tinc;
+    s.tt_rate = 0.0;
+  }
+  double rs(const Np1& s, const double* st, int i) const {  // mm10_rs (src/mm10_b.f:1831)
+    return st[0] * s.ms[i][0] + st[1] * s.ms[i][1] + st[2] * s.ms[i][2] +
+           st[3] * s.ms[i][3] + st[4] * s.ms[i][4] + st[5] * s.ms[i][5];
+  }
+  double slipinc(const Np1& s, const double* st, double tt, int i) const {  // :1805-1820
+    double r = rs(s, st, i);
+    return s.dg / tt * std::pow(std::fabs(r / tt), p->harden_n - 1.0) * r;
+  }
+  double hterm(double tt) const {  // Voce h_term with tau_l = 0 (gradFeinv is zeroed)
+    return 1.0 - (tt - p->tau_y) / p->tau_v + 0.0 / (tt - p->tau_y);
+  }
+  // symmetric part of S*W in the reference's vector forms (mm10_symsw :1505-1525)
+  static void symsw(const double* s, const double* w, double* sw) {
+    sw[0] = s[3] * w[2] - s[5] * w[1];
+    sw[1] = s[3] * w[2] - s[4] * w[0];
+    sw[2] = s[5] * w[1] + s[4] * w[0];
+    sw[3] = 0.5 * (w[2] * (s[0] - s[1]) + w[0] * s[5] - w[1] * s[4]);
+    sw[4] = 0.5 * (w[0] * (s[1] - s[2]) + w[1] * s[3] + w[2] * s[5]);
+    sw[5] = 0.5 * (w[1] * (s[0] - s[2]) + w[0] * s[3] - w[2] * s[4]);
+  }
+  void form_wp(const Np1& s, const double* st, double tt, double w[3]) const {
+    w[0] = w[1] = w[2] = 0.0;
+    for (int i = 0; i < 12; i++) {  // mm10_form_wp (src/mm10_b.f:1304-1381)
+      double si = slipinc(s, st, tt, i);
+      for (int a = 0; a < 3; a++) w[a] = w[a] + si * s.qc[i][a];
+      double r = rs(s, st, i);
+      for (int a = 0; a < 3; a++) w[a] = w[a] + r * s.tinc * p->iD_v * s.qc[i][a];
+    }
+  }
+  // mm10_formR1 (src/mm10_b.f:1061-1101)
+  void formR1(const Np1& s, const double* st, double tt, double R1[6]) const {
+    double dbar[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 12; i++) {  // mm10_form_dbarp voce (:1161-1190)
+      double si = slipinc(s, st, tt, i);
+      double r = rs(s, st, i);
+      double f = r * s.tinc * p->iD_v + si;
+      for (int a = 0; a < 6; a++) dbar[a] = dbar[a] + f * s.ms[i][a];
+    }
+    double w[3], sw[6], wv1[6], wv2[6];
+    form_wp(s, st, tt, w);
+    symsw(st, w, sw);
+    for (int a = 0; a < 6; a++) wv1[a] = s.D[a] - dbar[a];
+    mv6(vp->C, wv1, wv2);
+    for (int a = 0; a < 6; a++) R1[a] = st[a] - n->sig[a] - wv2[a] + 2.0 * sw[a];
+  }
+  // mm10_h_voche (src/mm10_b.f:1888-1912)
+  double h_voce(const Np1& s, const double* st, double tt) const {
+    double h = 0.0;
+    for (int i = 0; i < 12; i++) {
+      double si = slipinc(s, st, tt, i);
+      double ht = hterm(tt);
+      h = h + std::pow(std::fabs(ht), p->voce_m) * sgn1(ht) * std::fabs(si);
+    }
+    return n->tt + p->theta_0 * h;
+  }
+  // mm10_formR (src/mm10_b.f:1029-1047) with mm10_formR2 (:63-113)
+  void formR(Np1& s, const double* x, double R[7]) const {
+    formR1(s, x, x[6], R);
+    double h = h_voce(s, x, x[6]);
+    R[6] = x[6] - h;
+    s.tt_rate = (h - n->tt) / s.tinc;
+  }
+  // mm10_formJ11 (src/mm10_b.f:177-257)
+  void formJ11(const Np1& s, const double* st, double tt, double J[6][6]) const {
+    double sq[12][6];
+    for (int i = 0; i < 12; i++) symsw(st, s.qc[i], sq[i]);
+    std::memset(J, 0, 36 * sizeof(double));
+    for (int i = 0; i < 12; i++) {
+      double r = rs(s, st, i);
+      double dgdt = std::pow(std::fabs(r), p->harden_n - 1.0);
+      dgdt = s.dg * p->harden_n / std::pow(tt, p->harden_n) * dgdt;
+      dgdt = dgdt + s.tinc * p->iD_v;
+      double wv[6];
+      for (int a = 0; a < 6; a++) wv[a] = 2.0 * sq[i][a];
+      for (int j = 0; j < 6; j++)
+        for (int a = 0; a < 6; a++) wv[a] = wv[a] + vp->C[a][j] * s.ms[i][j];
+      for (int c = 0; c < 6; c++) {
+        double t = dgdt * s.ms[i][c];
+        for (int a = 0; a < 6; a++) J[a][c] += wv[a] * t;
+      }
+    }
+    double w[3];
+    form_wp(s, st, tt, w);
+    double iw[6][6];
+    std::memset(iw, 0, sizeof(iw));  // mm10_iw (src/mm10_b.f:1590-1634)
+    iw[0][3] = 2.0 * w[2];  iw[0][5] = -2.0 * w[1];
+    iw[1][3] = 2.0 * w[2];  iw[1][4] = -2.0 * w[0];
+    iw[2][4] = 2.0 * w[0];  iw[2][5] = 2.0 * w[1];
+    iw[3][0] = w[2];  iw[3][1] = -w[2]; iw[3][4] = -w[1]; iw[3][5] = w[0];
+    iw[4][1] = w[0];  iw[4][2] = -w[0]; iw[4][3] = w[1];  iw[4][5] = w[2];
+    iw[5][0] = w[1];  iw[5][2] = -w[1]; iw[5][3] = w[0];  iw[5][4] = -w[2];
+    for (int a = 0; a < 6; a++)
+      for (int c = 0; c < 6; c++) J[a][c] = J[a][c] + iw[a][c];
+    for (int a = 0; a < 6; a++) J[a][a] = J[a][a] + 1.0;
+  }
+  // mm10_formJ (src/mm10_b.f:901-954): J11 | J12 ; J21 | J22
+  void formJ(const Np1& s, const double* x, double J[7][7]) const {
+    const double* st = x;
+    double tt = x[6];
+    double J11[6][6];
+    formJ11(s, st, tt, J11);
+    double sq[12][6];
+    for (int i = 0; i < 12; i++) symsw(st, s.qc[i], sq[i]);
+    double J12[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < 12; i++) {  // mm10_formJ12 + mm10_dgdh_voche (:271-353, 2012-2030)
+      double dgam = slipinc(s, st, tt, i);
+      double dgdtt = -p->harden_n / tt * dgam;
+      double tm[6];
+      for (int a = 0; a < 6; a++) tm[a] = 2.0 * sq[i][a];
+      for (int j = 0; j < 6; j++)
+        for (int a = 0; a < 6; a++) tm[a] = tm[a] + vp->C[a][j] * s.ms[i][j];
+      for (int a = 0; a < 6; a++) J12[a] += tm[a] * dgdtt;
+    }
+    double et[6] = {0, 0, 0, 0, 0, 0};  // mm10_estress_voche (:1914-1940)
+    for (int i = 0; i < 12; i++) {
+      double r = rs(s, st, i);
+      double ht = hterm(tt);
+      double f = std::pow(std::fabs(ht), p->voce_m) * sgn1(ht) *
+                 std::pow(std::fabs(r), p->harden_n - 2.0) * r;
+      for (int a = 0; a < 6; a++) et[a] = et[a] + f * s.ms[i][a];
+    }
+    double fac = p->theta_0 * s.dg * p->harden_n / std::pow(tt, p->harden_n);
+    double etau = 0.0;  // mm10_ehard_voche (:1942-1968)
+    for (int i = 0; i < 12; i++) {
+      double si = slipinc(s, st, tt, i);
+      double ht = hterm(tt);
+      double a = p->voce_m * (-1.0 / p->tau_v - 0.0 / ((tt - p->tau_y) * (tt - p->tau_y))) *
+                 std::fabs(si) / std::fabs(ht);
+      double b = std::fabs(si) * p->harden_n / tt * sgn1(ht);
+      if (!p->exact_j22) b = b * sgn1(si);  // the reference's extra factor
+      etau = etau + (a - b) * std::pow(std::fabs(ht), p->voce_m);
+    }
+    etau = p->theta_0 * etau;
+    etau = 1.0 - etau;
+    for (int a = 0; a < 6; a++) {
+      for (int c = 0; c < 6; c++) J[a][c] = J11[a][c];
+      J[a][6] = J12[a];
+      J[6][a] = -(fac * et[a]);
+    }
+    J[6][6] = etau;
+  }
+
+  struct Result {
+    double sig[6], tt, tt_rate;
+    double J[7][7];   // last Jacobian formed by the update phase
+    bool have_J;
+    int iters;        // update-phase Newton iterations (summed over sub-steps)
+  };
+
+  // mm10_solve (src/mm10_a.f:2860-3295); returns false on failure
+  bool solve(Np1& cu, double dtinc, double stress[6], double& tt, Result& res) const {
+    const double c = 1.0e-4, red = 0.5;
+    const int mls = 10, mmin = 1;
+    double x[7];
+    for (int i = 0; i < 6; i++) x[i] = stress[i];
+    x[6] = tt;
+    // ---- predict (:2975-3156)
+    double inR1;
+    {
+      int iter = 0;
+      double x1[6], x2;
+      for (int i = 0; i < 6; i++) x1[i] = x[i];
+      double d1[6], d2[6];
+      for (int i = 0; i < 6; i++) { d1[i] = cu.D[i]; d2[i] = n->D[i]; }
+      for (double* d : {d1, d2}) {
+        double dtr = (d[0] + d[1] + d[2]) / 3.0;
+        d[0] -= dtr; d[1] -= dtr; d[2] -= dtr;
+        double t1 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double t2 = d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
+        if (t1 + t2 == 0.0) for (int i = 0; i < 6; i++) d[i] = 0.0;
+        else { double nn = std::sqrt(t1 + t2); for (int i = 0; i < 6; i++) d[i] = d[i] / nn; }
+      }
+      double t1 = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2];
+      double t2 = d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5];
+      double cos_ang = std::max(t1 + t2, 0.0);
+      x2 = x[6] + cos_ang * n->tt_rate * dtinc;
+      double R1[6];
+      formR1(cu, x1, x2, R1);
+      double nR1 = std::sqrt(R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] +
+                             R1[4] * R1[4] + R1[5] * R1[5]);
+      inR1 = nR1;
+#ifdef ORC_DEBUG
+      fprintf(stderr, "  predict start nR1 %.3e x2 %.6f\n", nR1, x2);
+#endif
+      while (nR1 > p->atol1 && nR1 / inR1 > p->rtol1) {
+        double J11[6][6];
+        formJ11(cu, x1, x2, J11);
+        double mJ[36], dx1[6];
+        for (int a = 0; a < 6; a++)
+          for (int b = 0; b < 6; b++) mJ[a * 6 + b] = -J11[a][b];
+        for (int a = 0; a < 6; a++) dx1[a] = R1[a];
+        lu_solve(6, mJ, 1, dx1);
+        double alpha = 1.0;
+        double dotR1 = R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] +
+                       R1[4] * R1[4] + R1[5] * R1[5];
+        double ls1 = 0.5 * dotR1;
+        double wv[6];
+        for (int a = 0; a < 6; a++) {
+          wv[a] = 0.0;
+          for (int b = 0; b < 6; b++) wv[a] += J11[b][a] * R1[b];
+        }
+        double ls2 = c * (dx1[0] * wv[0] + dx1[1] * wv[1] + dx1[2] * wv[2] + dx1[3] * wv[3] +
+                          dx1[4] * wv[4] + dx1[5] * wv[5]);
+        int ls = 0;
+        for (;;) {
+          double nlsx = ls1 + ls2 * alpha;
+          double xn[6];
+          for (int a = 0; a < 6; a++) xn[a] = x1[a] + alpha * dx1[a];
+          formR1(cu, xn, x2, R1);
+          dotR1 = R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] +
+                  R1[4] * R1[4] + R1[5] * R1[5];
+          nR1 = std::sqrt(dotR1);
+          double nRs = 0.5 * dotR1;
+          if (nRs <= nlsx || ls > mls) {
+            for (int a = 0; a < 6; a++) x1[a] = xn[a];
+            break;
+          }
+          alpha = red * alpha;
+          ls++;
+        }
+        iter++;
+#ifdef ORC_DEBUG
+        fprintf(stderr, "  predict it %d nR1 %.3e ls %d\n", iter, nR1, ls);
+#endif
+        bool nan = false;
+        for (int a = 0; a < 6; a++) nan |= std::isnan(x1[a]);
+        if (iter > p->miter || nan) return false;
+      }
+      for (int i = 0; i < 6; i++) x[i] = x1[i];
+      x[6] = x2;
+    }
+    // ---- update (:3162-3293)
+    int iter = 0;
+    double R[7];
+    formR(cu, x, R);
+    double dotR = 0;
+    for (int a = 0; a < 7; a++) dotR += R[a] * R[a];
+    double nR = std::sqrt(dotR), inR = nR;
+    if (inR == 0.0) inR = inR1;
+    while ((nR > p->atol && nR / inR > p->rtol) || iter < mmin) {
+      formJ(cu, x, res.J);
+      res.have_J = true;
+      double mJ[49], dx[7];
+      for (int a = 0; a < 7; a++)
+        for (int b = 0; b < 7; b++) mJ[a * 7 + b] = -res.J[a][b];
+      for (int a = 0; a < 7; a++) dx[a] = R[a];
+      lu_solve(7, mJ, 1, dx);
+      double alpha = 1.0;
+      dotR = 0;
+      for (int a = 0; a < 7; a++) dotR += R[a] * R[a];
+      double ls1 = 0.5 * dotR;
+      double wv[7];
+      for (int a = 0; a < 7; a++) {
+        wv[a] = 0.0;
+        for (int b = 0; b < 7; b++) wv[a] += res.J[b][a] * R[b];
+      }
+      double ls2 = 0;
+      for (int a = 0; a < 7; a++) ls2 += dx[a] * wv[a];
+      ls2 = c * ls2;
+      int ls = 0;
+      for (;;) {
+        double nlsx = ls1 + ls2 * alpha;
+        double xn[7];
+        for (int a = 0; a < 7; a++) xn[a] = x[a] + alpha * dx[a];
+        formR(cu, xn, R);
+        dotR = 0;
+        for (int a = 0; a < 7; a++) dotR += R[a] * R[a];
+        nR = std::sqrt(dotR);
+        double nRs = 0.5 * dotR;
+        if (nRs <= nlsx || ls > mls) {
+          for (int a = 0; a < 7; a++) x[a] = xn[a];
+          break;
+        }
+        alpha = red * alpha;
+        ls++;
+      }
+      iter++;
+#ifdef ORC_DEBUG
+      fprintf(stderr, "  update it %d nR %.3e inR %.3e ls %d tt %.6f\n", iter, nR, inR, ls, x[6]);
+#endif
+      bool nan = false;
+      for (int a = 0; a < 7; a++) nan |= std::isnan(x[a]);
+      if (iter > p->miter || nan) { res.iters += iter; return false; }
+    }
+    res.iters += iter;
+    for (int i = 0; i < 6; i++) stress[i] = x[i];
+    tt = x[6];
+    return true;
+  }
+
+  // mm10_solve_strup + mm10_solve_crystal (src/mm10_a.f:2628-2845, 1080-1157).
+  // Returns false when the local solve failed (the reference then keeps sigma_n).
+  bool update(const double D[6], double dt, const M3 R, bool iter0, State& out,
+              double cep[6][6], int* local_iters) const {
+    Np1 np1;
+    setup(np1, D, dt, R);
+    double stress[6], ostress[6], tt = n->tt, ott = n->tt;
+    for (int i = 0; i < 6; i++) stress[i] = ostress[i] = n->sig[i];
+    double temp1 = 0, temp2 = 0;
+    for (int i = 0; i < 6; i++) { temp1 += D[i] * D[i]; temp2 += stress[i] * stress[i]; }
+    bool no_load = temp2 == 0.0 && temp1 == 0.0;
+    Result res;
+    res.have_J = false;
+    res.iters = 0;
+    double tt_rate_out = 0.0;
+    bool ok = true;
+    if (iter0 || no_load) {  // mm10_solve_strup_a (:2721-2743)
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) cep[a][b] = vp->C[a][b];
+      if (!no_load) {
+        double R1[6];
+        formR1(np1, stress, tt, R1);
+        for (int a = 0; a < 6; a++) stress[a] = stress[a] - R1[a];
+      }
+      tt_rate_out = 0.0;
+    } else {  // mm10_solve_strup_iterate (:2747-2843)
+      double frac = 0.0, step = 1.0;
+      int cuts = 0;
+      const int mcuts = 4;
+      Np1 curr;
+      bool fail = false;
+      while (frac < 1.0) {
+        double Dw[6];
+        for (int i = 0; i < 6; i++) Dw[i] = np1.D[i] * (step + frac);
+        setup(curr, Dw, np1.tinc * (step + frac), R);
+        tt = n->tt;
+        fail = !solve(curr, np1.tinc * step, stress, tt, res);
+        if (fail) {
+          for (int i = 0; i < 6; i++) stress[i] = ostress[i];
+          tt = ott;
+          step = step * 0.5;
+          cuts++;
+          if (cuts > mcuts) break;
+          fail = false;
+        } else {
+          for (int i = 0; i < 6; i++) ostress[i] = stress[i];
+          ott = tt;
+          frac = frac + step;
+        }
+      }
+      bool nan = std::isnan(tt);
+      for (int i = 0; i < 6; i++) nan |= std::isnan(stress[i]);
+      if (fail || nan) ok = false;
+      tt_rate_out = curr.tt_rate;
+    }
+    if (local_iters) *local_iters = res.iters;
+    if (!ok) {
+      // Reference: material_cut_step is raised and never checked by the FFT driver
+      // (src/mm10_a.f:2806-2841).  Keep sigma_n / tau_n and the elastic tangent.
+      for (int i = 0; i < 6; i++) out.sig[i] = n->sig[i];
+      out.tt = n->tt;
+      out.tt_rate = 0.0;
+      for (int i = 0; i < 6; i++) out.D[i] = D[i];
+      std::memcpy(out.Rp, n->Rp, sizeof(M3));
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) cep[a][b] = vp->C[a][b];
+      return false;
+    }
+    for (int i = 0; i < 6; i++) out.sig[i] = stress[i];
+    out.tt = tt;
+    out.tt_rate = tt_rate_out;
+    for (int i = 0; i < 6; i++) out.D[i] = D[i];
+    if (iter0 || no_load) {
+      // early return of mm10_solve_crystal: np1%Rp keeps the zero of mm10_setup_np1
+      std::memset(out.Rp, 0, sizeof(M3));
+      return true;
+    }
+    // mm10_tangent (src/mm10_a.f:658-815) for Voce: JA = JB = 0, JR = C
+    {
+      double J22 = res.J[6][6];
+      double JJ[36], JR[36];
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) {
+          double beta = res.J[6][b] / J22;
+          JJ[a * 6 + b] = res.J[a][b] - res.J[a][6] * beta;
+          JR[a * 6 + b] = vp->C[a][b];
+        }
+      lu_solve(6, JJ, 6, JR);
+      for (int a = 0; a < 6; a++)  // mm10_a_make_symm_1
+        for (int b = 0; b < 6; b++) cep[a][b] = (JR[a * 6 + b] + JR[b * 6 + a]) * 0.5;
+    }
+    // mm10_update_rotation (src/mm10_a.f:3310-3327) with np1 at the converged x
+    {
+      double wb[3] = {0, 0, 0};
+      for (int i = 0; i < 12; i++) {  // mm10_form_wbarp (src/mm10_b.f:1231-1290)
+        double si = slipinc(np1, out.sig, out.tt, i);
+        for (int a = 0; a < 3; a++) wb[a] = wb[a] + si * np1.qs[i][a];
+        double r = rs(np1, out.sig, i);
+        for (int a = 0; a < 3; a++) wb[a] = wb[a] + r * np1.tinc * p->iD_v * np1.qs[i][a];
+      }
+      M3 W = {{0.0, wb[2], wb[1]}, {-wb[2], 0.0, wb[0]}, {-wb[1], -wb[0], 0.0}};
+      M3 ex;  // mm10_expmw3x3 (:3360-3385)
+      double alpha = std::sqrt(W[1][2] * W[1][2] + W[0][2] * W[0][2] + W[0][1] * W[0][1]);
+      if (alpha < 1.0e-16) {
+        std::memset(ex, 0, sizeof(ex));
+      } else {
+        M3 WW;
+        mm33(W, W, WW);
+        double ca = (1.0 - std::cos(alpha)) / (alpha * alpha), sa = std::sin(alpha) / alpha;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) ex[i][j] = ca * WW[i][j] + sa * W[i][j];
+      }
+      for (int i = 0; i < 3; i++) ex[i][i] += 1.0;
+      mm33(ex, n->Rp, out.Rp);
+    }
+    return true;
+  }
+};
+
+// ---- cep2A (src/cep2A.f:86-284) ------------------------------------------------------
+inline int I4(int i, int j, int k, int l) { return i * 27 + j * 9 + k * 3 + l; }
+void cep2A(const M3 Fn, const M3 t, const double C[6][6], const M3 Rh, const M3 fnhinv,
+           const M3 R, const M3 Fn1, const M3 finv, double detFn1, double dPdF[81]) {
+  M3 transR, U, Y, temp, sigma, Uinv, t_Uinv, R_t, RY, RYR, RtRF, dJdF;
+  tr33(R, transR);
+  mm33(transR, Fn1, U);
+  double trU = U[0][0] + U[1][1] + U[2][2];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) Y[i][j] = (i == j ? trU : 0.0) - U[i][j];
+  mm33(R, t, temp);
+  mm33(temp, transR, sigma);
+  mm33(finv, R, Uinv);
+  mm33(t, Uinv, t_Uinv);
+  mm33(R, t, R_t);
+  mm33(R, Y, RY);
+  mm33(RY, transR, RYR);
+  double detY_1 = 1.0 / det33(Y);
+  mm33(R_t, Uinv, RtRF);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) dJdF[i][j] = finv[j][i] * detFn1;
+  M3 dFn, Fnh, transRh, Uh, Yh, RYRh, RYh, FpFinv, L33, D2;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      dFn[i][j] = Fn1[i][j] - Fn[i][j];
+      Fnh[i][j] = 0.5 * (Fn1[i][j] + Fn[i][j]);
+    }
+  tr33(Rh, transRh);
+  mm33(transRh, Fnh, Uh);
+  double trUh = Uh[0][0] + Uh[1][1] + Uh[2][2];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) Yh[i][j] = (i == j ? trUh : 0.0) - Uh[i][j];
+  mm33(Rh, Yh, temp);
+  mm33(temp, transRh, RYRh);
+  double detYh_1 = 1.0 / det33(Yh);
+  mm33(Rh, Yh, RYh);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) FpFinv[i][j] = 0.5 * fnhinv[i][j];
+  mm33(dFn, FpFinv, L33);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) D2[i][j] = L33[i][j] + L33[j][i];
+  const int iv[9] = {0, 3, 5, 3, 1, 4, 5, 4, 2};
+  double cep99[9][9];
+  for (int a = 0; a < 9; a++)
+    for (int b = 0; b < 9; b++) cep99[a][b] = C[iv[a]][iv[b]];
+  double dRdF[81], dRhdF[81], dLdF[81];
+  for (int m = 0; m < 81; m++) {
+    int i = m / 27, j = (m / 9) % 3, k = (m / 3) % 3, l = m % 3;
+    dRdF[m] = detY_1 * (RYR[i][k] * Y[l][j] - RY[i][l] * RY[k][j]);
+    dRhdF[m] = detYh_1 * (RYRh[i][k] * Yh[l][j] - RYh[i][l] * RYh[k][j]);
+    dRhdF[m] = dRhdF[m] * 0.5;
+    dLdF[m] = -L33[i][k] * FpFinv[l][j];
+    if (i == k) dLdF[m] = dLdF[m] + FpFinv[l][j];
+  }
+  double dtdF[81], d1[81], d2[81], d3[81];
+  for (int a = 0; a < 81; a++) {
+    int i = a / 27, j = (a / 9) % 3, p = (a / 3) % 3, q = a % 3;
+    double s1 = 0, s2 = 0, s3 = 0;
+    for (int m = 0; m < 3; m++)
+      for (int n = 0; n < 3; n++) {
+        s1 = s1 + dRhdF[I4(m, i, p, q)] * D2[m][n] * Rh[n][j];
+        s2 = s2 + Rh[m][i] * dLdF[I4(m, n, p, q)] * Rh[n][j];
+        s2 = s2 + Rh[m][i] * dLdF[I4(n, m, p, q)] * Rh[n][j];
+        s3 = s3 + Rh[m][i] * D2[m][n] * dRhdF[I4(n, j, p, q)];
+      }
+    d1[a] = s1; d2[a] = s2; d3[a] = s3;
+  }
+  double dt1[81];
+  for (int a = 0; a < 81; a++) dt1[a] = d1[a] + d2[a] + d3[a];
+  // cep2A_ddot44 (src/cep2A.f:319-339): column-major walk of the 9x9 cep99
+  const int off[9] = {0, 27, 54, 9, 36, 63, 18, 45, 72};
+  for (int ii = 0; ii < 9; ii++)
+    for (int jj = 0; jj < 9; jj++) {
+      double s = 0;
+      for (int r = 0; r < 9; r++) s += cep99[r][ii] * dt1[off[r] + jj];
+      dtdF[ii * 9 + jj] = s;
+    }
+  for (int pp = 0; pp < 81; pp++) {
+    int i = pp / 27, j = (pp / 9) % 3, k = (pp / 3) % 3, l = pp % 3;
+    double P0 = RtRF[i][j] * dJdF[k][l], P1 = 0, P2 = 0, P3 = 0, P4 = 0;
+    for (int m = 0; m < 3; m++) {
+      P1 = P1 - detFn1 * sigma[i][m] * finv[j][k] * finv[l][m];
+      P2 = P2 + detFn1 * dRdF[I4(i, m, k, l)] * t_Uinv[m][j];
+      for (int n = 0; n < 3; n++) {
+        P3 = P3 + detFn1 * R[i][m] * dtdF[I4(m, n, k, l)] * Uinv[n][j];
+        P4 = P4 + detFn1 * R_t[i][m] * dRdF[I4(n, m, k, l)] * finv[j][n];
+      }
+    }
+    dPdF[pp] = P0 + P1 + P2 + P3 + P4;
+  }
+}
+
+// ---- one material point: do_nleps_block body (src/drive_eps_sig.f:200-325) ----------
+struct PointOut {
+  double P[9], A[81], sig[6], cep[6][6];
+  int iters;
+  bool ok;
+};
+void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int iter,
+                    const M3 Fn, const M3 Fn1, const State& n_in, State& np1, PointOut& o) {
+  State n = n_in;
+  if (step == 1) state_init(cr, n);  // mm10 re-initialises history at step 1 (:78-83)
+  M3 fnh, dfn, rnh, rn1, fnhinv, fn1inv;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      fnh[i][j] = 0.5 * (Fn[i][j] + Fn1[i][j]);
+      dfn[i][j] = Fn1[i][j] - Fn[i][j];
+    }
+  polar_R(fnh, rnh);
+  polar_R(Fn1, rn1);
+  inv33(fnh, fnhinv);
+  // mul33 (src/drive_eps_sig.f:1110-1170): ddt = sym(dfn * fnhinv), engineering shear
+  double ddt[6];
+  {
+    const M3& A = dfn;
+    const M3& B = fnhinv;
+    ddt[0] = A[0][0] * B[0][0] + A[0][1] * B[1][0] + A[0][2] * B[2][0];
+    ddt[3] = A[1][0] * B[0][0] + A[1][1] * B[1][0] + A[1][2] * B[2][0] + A[0][0] * B[0][1] +
+             A[0][1] * B[1][1] + A[0][2] * B[2][1];
+    ddt[5] = A[2][0] * B[0][0] + A[2][1] * B[1][0] + A[2][2] * B[2][0] + A[0][0] * B[0][2] +
+             A[0][1] * B[1][2] + A[0][2] * B[2][2];
+    ddt[1] = A[1][0] * B[0][1] + A[1][1] * B[1][1] + A[1][2] * B[2][1];
+    ddt[4] = A[2][0] * B[0][1] + A[2][1] * B[1][1] + A[2][2] * B[2][1] + A[1][0] * B[0][2] +
+             A[1][1] * B[1][2] + A[1][2] * B[2][2];
+    ddt[2] = A[2][0] * B[0][2] + A[2][1] * B[1][2] + A[2][2] * B[2][2];
+  }
+  M6 qnh;
+  getrm1_opt1(rnh, qnh);
+  double uddt[6];
+  for (int j = 0; j < 6; j++)  // qmply1 (src/qmply1.f:15-49)
+    uddt[j] = qnh[j][0] * ddt[0] + qnh[j][1] * ddt[1] + qnh[j][2] * ddt[2] +
+              qnh[j][3] * ddt[3] + qnh[j][4] * ddt[4] + qnh[j][5] * ddt[5];
+  Mm10 mm{&cr.p, &vp, &n};
+  int it = 0;
+  o.ok = mm.update(uddt, dt, rn1, iter == 0, np1, o.cep, &it);
+  o.iters = it;
+  for (int i = 0; i < 6; i++) o.sig[i] = np1.sig[i];
+  // Cauchy stress T = R t R^T (getrm1 opt 2 + qmply1), P = J T F^-T (cs2p :1182-1224)
+  M6 qt;
+  rt2rve(rn1, qt);
+  double cs[6];
+  for (int j = 0; j < 6; j++)
+    cs[j] = qt[j][0] * np1.sig[0] + qt[j][1] * np1.sig[1] + qt[j][2] * np1.sig[2] +
+            qt[j][3] * np1.sig[3] + qt[j][4] * np1.sig[4] + qt[j][5] * np1.sig[5];
+  double detF = inv33(Fn1, fn1inv);
+  const M3& fi = fn1inv;
+  o.P[0] = detF * (cs[0] * fi[0][0] + cs[3] * fi[0][1] + cs[5] * fi[0][2]);
+  o.P[1] = detF * (cs[0] * fi[1][0] + cs[3] * fi[1][1] + cs[5] * fi[1][2]);
+  o.P[2] = detF * (cs[0] * fi[2][0] + cs[3] * fi[2][1] + cs[5] * fi[2][2]);
+  o.P[3] = detF * (cs[3] * fi[0][0] + cs[1] * fi[0][1] + cs[4] * fi[0][2]);
+  o.P[4] = detF * (cs[3] * fi[1][0] + cs[1] * fi[1][1] + cs[4] * fi[1][2]);
+  o.P[5] = detF * (cs[3] * fi[2][0] + cs[1] * fi[2][1] + cs[4] * fi[2][2]);
+  o.P[6] = detF * (cs[5] * fi[0][0] + cs[4] * fi[0][1] + cs[2] * fi[0][2]);
+  o.P[7] = detF * (cs[5] * fi[1][0] + cs[4] * fi[1][1] + cs[2] * fi[1][2]);
+  o.P[8] = detF * (cs[5] * fi[2][0] + cs[4] * fi[2][1] + cs[2] * fi[2][2]);
+  M3 t33 = {{np1.sig[0], np1.sig[3], np1.sig[5]},
+            {np1.sig[3], np1.sig[1], np1.sig[4]},
+            {np1.sig[5], np1.sig[4], np1.sig[2]}};
+  cep2A(Fn, t33, o.cep, rnh, fnhinv, rn1, Fn1, fn1inv, detF, o.A);
+}
+
+// ---- FFT (restated DFTI role: exact complex DFT) --------------------------------------
+struct FFT1 {
+  int n;
+  std::vector<int> fac;
+  std::vector<std::complex<double>> tw;  // exp(-2 pi i k / n)
+  explicit FFT1(int n_) : n(n_) {
+    int m = n;
+    for (int f : {4, 2, 3, 5, 7})
+      while (m % f == 0) { fac.push_back(f); m /= f; }
+    for (int f = 11; m > 1; f += 2)
+      while (m % f == 0) { fac.push_back(f); m /= f; }
+    tw.resize(n);
+    for (int k = 0; k < n; k++)
+      tw[k] = std::complex<double>(std::cos(2.0 * PI * k / n), -std::sin(2.0 * PI * k / n));
+  }
+  // recursive mixed-radix decimation in time; sign -1 forward, +1 backward (unscaled)
+  void rec(const std::complex<double>* in, std::complex<double>* out, int len, int stride,
+           int fi, int sign, std::complex<double>* scratch) const {
+    if (len == 1) { out[0] = in[0]; return; }
+    int r = fac[fi], m = len / r;
+    for (int q = 0; q < r; q++) rec(in + q * stride, out + q * m, m, stride * r, fi + 1, sign, scratch);
+    int step = n / len;
+    for (int k = 0; k < m; k++) {
+      std::complex<double> v[16];
+      std::complex<double>* vv = r <= 16 ? v : scratch;
+      for (int q = 0; q < r; q++) {
+        std::complex<double> w = tw[(q * k * step) % n];
+        if (sign > 0) w = std::conj(w);
+        vv[q] = out[q * m + k] * w;
+      }
+      for (int s = 0; s < r; s++) {
+        std::complex<double> acc = 0.0;
+        for (int q = 0; q < r; q++) {
+          std::complex<double> w = tw[((q * s) % r) * (n / r)];
+          if (sign > 0) w = std::conj(w);
+          acc += vv[q] * w;
+        }
+        scratch[r + s] = acc;
+      }
+      for (int s = 0; s < r; s++) out[s * m + k] = scratch[r + s];
+    }
+  }
+  void run(std::complex<double>* data, int sign, std::vector<std::complex<double>>& buf) const {
+    if ((int)buf.size() < 2 * n + 64) buf.resize(2 * n + 64);
+    std::complex<double>* in = buf.data();
+    std::complex<double>* scratch = buf.data() + n;
+    for (int i = 0; i < n; i++) in[i] = data[i];
+    rec(in, data, n, 1, 0, sign, scratch);
+  }
+};
+
+void fft3(const FFT1& f, double* re, double* im, int sign) {
+  int N = f.n;
+  std::vector<std::complex<double>> line(N), buf;
+  for (int axis = 0; axis < 3; axis++) {
+    long s = axis == 0 ? 1 : (axis == 1 ? N : (long)N * N);
+    for (int u = 0; u < N; u++)
+      for (int w = 0; w < N; w++) {
+        long base;
+        if (axis == 0) base = (long)u * N + (long)w * N * N;
+        else if (axis == 1) base = u + (long)w * N * N;
+        else base = u + (long)w * N;
+        for (int k = 0; k < N; k++) line[k] = std::complex<double>(re[base + k * s], im[base + k * s]);
+        f.run(line.data(), sign, buf);
+        for (int k = 0; k < N; k++) { re[base + k * s] = line[k].real(); im[base + k * s] = line[k].imag(); }
+      }
+  }
+  if (sign > 0) {
+    double sc = 1.0 / ((double)N * N * N);
+    long N3 = (long)N * N * N;
+    for (long v = 0; v < N3; v++) { re[v] *= sc; im[v] *= sc; }
+  }
+}
+
+}  // namespace
+
+// ======================================================================================
+struct orc_ctx {
+  int N;
+  long N3;
+  double dt;
+  int gmap, nthreads;
+  std::vector<Crys> crys;
+  std::vector<int> mat;            // 0-based crystal per voxel
+  std::vector<VoxProps> vprops;
+  std::vector<State> hn, hn1;
+  std::vector<double> Fn, Fn1, Pn, Pn1, K4, b, dFm;
+  // G_K_dF tables: Ghat "centered" q per axis and the fftshift phase
+  std::vector<double> qax;         // per axis value of q for memory index k
+  std::vector<char> nyq;           // per axis: memory index k holds the Nyquist frequency
+  std::vector<double> coef_c, coef_s;
+  FFT1* fft;
+  // FFT_nr3 persistent locals (Fortran DATA => SAVE'd, src/FFT_nr3.f:29-34)
+  double barF_t[9], P_bar[9], C_homo[81];
+};
+
+static void ghat_apply(const orc_ctx* c, long v, const double* in9, double* out9,
+                       const double q[3]) {
+  (void)c; (void)v;
+  double qq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+  if (std::fabs(qq) <= 1.0e-10) { for (int i = 0; i < 9; i++) out9[i] = 0.0; return; }
+  // (G:A)_ij = sum_kl delta_ik q_j q_l / |q|^2 A_kl  (formG, src/FFT_init.f:272-340)
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double s = 0;
+      for (int l = 0; l < 3; l++) s += (q[j] * q[l] / qq) * in9[3 * i + l];
+      out9[3 * i + j] = s;
+    }
+}
+
+extern "C" {
+
+orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
+                    const cpfft_crystal* props, int ncrystals, double tstep, int g_mapping,
+                    int nthreads) {
+  orc_ctx* c = new orc_ctx;
+  c->N = N;
+  c->N3 = (long)N * N * N;
+  c->dt = tstep;
+  c->gmap = g_mapping;
+  c->nthreads = nthreads > 0 ? nthreads : 1;
+  c->crys.resize(ncrystals);
+  for (int i = 0; i < ncrystals; i++) crystal_finalize(props[i], c->crys[i]);
+  long N3 = c->N3;
+  c->mat.resize(N3);
+  c->vprops.resize(N3);
+  for (long v = 0; v < N3; v++) {
+    c->mat[v] = matList[v] - 1;
+    double ang[3] = {kocks_deg[v], kocks_deg[N3 + v], kocks_deg[2 * N3 + v]};
+    voxel_props(c->crys[c->mat[v]], ang, c->vprops[v]);
+  }
+  c->hn.resize(N3);
+  c->hn1.resize(N3);
+  for (long v = 0; v < N3; v++) { state_init(c->crys[c->mat[v]], c->hn[v]); c->hn1[v] = c->hn[v]; }
+  c->Fn.assign(9 * N3, 0.0);
+  for (int d : {0, 4, 8})
+    for (long v = 0; v < N3; v++) c->Fn[d * N3 + v] = 1.0;
+  c->Fn1 = c->Fn;
+  c->Pn.assign(9 * N3, 0.0);
+  c->Pn1.assign(9 * N3, 0.0);
+  c->K4.assign(81 * N3, 0.0);
+  c->b.assign(9 * N3, 0.0);
+  c->dFm.assign(9 * N3, 0.0);
+  int Nhalf = (N % 2 == 1) ? (N + 1) / 2 : N / 2 + 1;  // src/FFT_init.f:146-147
+  c->qax.resize(N);
+  c->nyq.assign(N, 0);
+  for (int k = 0; k < N; k++) {
+    // memory index k of the phase-shifted transform holds true frequency (k+Nhalf) mod N
+    int f = (k + Nhalf) % N;
+    if (g_mapping == CPFFT_G_REF_SHIFT) {
+      c->qax[k] = (double)(k + 1 - Nhalf);
+    } else {
+      c->qax[k] = (double)(f <= (N - 1) / 2 ? f : f - N);  // signed wavenumber
+      // even N: the Nyquist frequency has no signed partner; its Green operator is zero
+      c->nyq[k] = (N % 2 == 0 && 2 * f == N) ? 1 : 0;
+    }
+  }
+  c->coef_c.resize(N3);
+  c->coef_s.resize(N3);
+  double NhN = (double)Nhalf * 2.0 * PI / (double)N;  // formfftshift (:354-385)
+  for (int k = 0; k < N; k++)
+    for (int j = 0; j < N; j++)
+      for (int i = 0; i < N; i++) {
+        double temp = NhN * (double)(i + j + k);
+        long v = i + (long)N * j + (long)N * N * k;
+        c->coef_c[v] = std::cos(temp);
+        c->coef_s[v] = -std::sin(temp);
+      }
+  c->fft = new FFT1(N);
+  for (int i = 0; i < 9; i++) c->barF_t[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int i = 0; i < 9; i++) c->P_bar[i] = 0.0;
+  for (int i = 0; i < 81; i++) c->C_homo[i] = 0.0;
+  return c;
+}
+
+void orc_destroy(orc_ctx* c) {
+  if (!c) return;
+  delete c->fft;
+  delete c;
+}
+
+static void load33(const double* f, long N3, long v, M3 m) {
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) m[i][j] = f[(3 * i + j) * N3 + v];
+}
+
+int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn, const double* Fn1,
+                      double* Pn1, double* K4, long long* local_iters) {
+  long N3 = c->N3;
+  if (Fn) std::copy(Fn, Fn + 9 * N3, c->Fn.begin());
+  if (Fn1) std::copy(Fn1, Fn1 + 9 * N3, c->Fn1.begin());
+  int fails = 0;
+  long long its = 0;
+#pragma omp parallel for schedule(dynamic, 128) reduction(+ : fails, its) num_threads(c->nthreads)
+  for (long v = 0; v < N3; v++) {
+    M3 fn, fn1;
+    load33(c->Fn.data(), N3, v, fn);
+    load33(c->Fn1.data(), N3, v, fn1);
+    PointOut o;
+    material_point(c->crys[c->mat[v]], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v],
+                   c->hn1[v], o);
+    if (!o.ok) fails++;
+    its += o.iters;
+    for (int i = 0; i < 9; i++) c->Pn1[i * N3 + v] = o.P[i];
+    for (int m = 0; m < 81; m++) c->K4[m * N3 + v] = o.A[m];
+  }
+  if (Pn1) std::copy(c->Pn1.begin(), c->Pn1.end(), Pn1);
+  if (K4) std::copy(c->K4.begin(), c->K4.end(), K4);
+  if (local_iters) *local_iters = its;
+  return fails;
+}
+
+void orc_commit(orc_ctx* c) {  // update (src/update.f) + FFT_nr3.f:173-179
+  c->hn = c->hn1;
+  c->Fn = c->Fn1;
+  c->Pn = c->Pn1;
+}
+
+// G_K_dF (src/G_K_dF.f:11-87), restated with an explicit complex DFT
+void orc_green_apply(orc_ctx* c, const double* x, double* y, int flgK, const double* K4) {
+  long N3 = c->N3;
+  int N = c->N;
+  const double* K = K4 ? K4 : c->K4.data();
+  std::vector<double> r1(9 * N3), r2(9 * N3), r3(9 * N3);
+  if (flgK) {
+    // ddot42n (src/G_K_dF.f:241-268), its summation order kept
+#pragma omp parallel for num_threads(c->nthreads)
+    for (long v = 0; v < N3; v++)
+      for (int i = 0; i < 9; i++) {
+        double t[9];
+        for (int j = 0; j < 9; j++) t[j] = K[(9 * i + j) * N3 + v] * x[j * N3 + v];
+        double s1 = t[1] + t[5], s2 = t[2] + t[6], s3 = t[3] + t[7], s4 = t[4] + t[8];
+        s1 = s1 + s3; s2 = s2 + s4;
+        s1 = s1 + s2;
+        r1[i * N3 + v] = t[0] + s1;
+      }
+  } else {
+    std::copy(x, x + 9 * N3, r1.begin());
+  }
+#pragma omp parallel for num_threads(std::min(c->nthreads, 9))
+  for (int i = 0; i < 9; i++) {  // fftfem3d (:101-157)
+    double* re = &r2[i * N3];
+    double* im = &r3[i * N3];
+    for (long v = 0; v < N3; v++) {
+      re[v] = r1[i * N3 + v] * c->coef_c[v];
+      im[v] = r1[i * N3 + v] * c->coef_s[v];
+    }
+    fft3(*c->fft, re, im, -1);
+  }
+  // Ghat multiply of the real and imaginary parts (:64-65); memory index (a,b,cc)
+  // with a fastest carries q = (q[cc], q[b], q[a]) (formG, src/FFT_init.f:310-318)
+#pragma omp parallel for num_threads(c->nthreads)
+  for (long v = 0; v < N3; v++) {
+    int a = (int)(v % N), bb = (int)((v / N) % N), cc = (int)(v / ((long)N * N));
+    double q[3] = {c->qax[cc], c->qax[bb], c->qax[a]};
+    double in_re[9], in_im[9], o_re[9], o_im[9];
+    for (int i = 0; i < 9; i++) { in_re[i] = r2[i * N3 + v]; in_im[i] = r3[i * N3 + v]; }
+    if (c->nyq[cc] || c->nyq[bb] || c->nyq[a]) q[0] = q[1] = q[2] = 0.0;
+    ghat_apply(c, v, in_re, o_re, q);
+    ghat_apply(c, v, in_im, o_im, q);
+    for (int i = 0; i < 9; i++) { r1[i * N3 + v] = o_re[i]; r2[i * N3 + v] = o_im[i]; }
+  }
+#pragma omp parallel for num_threads(std::min(c->nthreads, 9))
+  for (int i = 0; i < 9; i++) {  // ifftfem3d (:171-227)
+    double* re = &r1[i * N3];
+    double* im = &r2[i * N3];
+    fft3(*c->fft, re, im, +1);
+    for (long v = 0; v < N3; v++) y[i * N3 + v] = re[v] * c->coef_c[v] + im[v] * c->coef_s[v];
+  }
+}
+
+static double nrm2(const double* x, long n) {
+  double s = 0;
+  for (long i = 0; i < n; i++) s += x[i] * x[i];
+  return std::sqrt(s);
+}
+static double dotp(const double* x, const double* y, long n) {
+  double s = 0;
+  for (long i = 0; i < n; i++) s += x[i] * y[i];
+  return s;
+}
+
+// fftPcg (src/FFT_nr3.f:214-360): unpreconditioned CG from x = 0 with the reference's
+// stop test ||r|| <= tol*||b|| .or. ||r|| <= tol, maxIter 1000
+int orc_cg(orc_ctx* c, const double* b, double* x, double tol, int* iters) {
+  long n = 9 * c->N3;
+  const int maxIter = 1000;
+  std::fill(x, x + n, 0.0);
+  *iters = 0;
+  double n2b = nrm2(b, n);
+  double tolb = tol * n2b;
+  if (tol <= 2.220446049250313e-16 || tol >= 1.0) return CPFFT_ERR_CG_TOL;
+  if (n2b <= 2.220446049250313e-16) return 0;
+  std::vector<double> r(b, b + n), p(b, b + n), Ap(n);
+  double rr = dotp(r.data(), r.data(), n);
+  int it = 0;
+  while (true) {
+    orc_green_apply(c, p.data(), Ap.data(), 1, nullptr);
+    double pAp = dotp(p.data(), Ap.data(), n);
+    double alpha = rr / pAp;
+    for (long i = 0; i < n; i++) { x[i] += alpha * p[i]; r[i] -= alpha * Ap[i]; }
+    it++;
+    double rn = nrm2(r.data(), n);
+    if (rn <= tolb || rn <= tol) break;
+    if (it >= maxIter) break;
+    double rr_new = rn * rn;
+    double beta = rr_new / rr;
+    rr = rr_new;
+    for (long i = 0; i < n; i++) p[i] = r[i] + beta * p[i];
+  }
+  *iters = it;
+  return it >= maxIter ? CPFFT_ERR_CG_MAXIT : 0;  // src/FFT_nr3.f:335-339
+}
+
+// tangent_homo (src/tangent_homo.f:11-73)
+int orc_tangent_homo(orc_ctx* c, double tolPCG, double* C_homo) {
+  long N3 = c->N3;
+  std::vector<double> Cij(9 * N3);
+  int total = 0;
+  for (int i = 0; i < 9; i++) {
+    for (int j = 0; j < 9; j++)
+      std::copy(&c->K4[(9 * j + i) * N3], &c->K4[(9 * j + i) * N3] + N3, &Cij[j * N3]);
+    orc_green_apply(c, Cij.data(), c->b.data(), 0, nullptr);
+    for (long k = 0; k < 9 * N3; k++) c->b[k] = -c->b[k];
+    int its = 0;
+    int rc = orc_cg(c, c->b.data(), Cij.data(), tolPCG, &its);
+    total += its;
+    if (rc) return rc;
+    for (long v = 0; v < N3; v++) Cij[i * N3 + v] += 1.0;
+    for (int j = 0; j < 9; j++) {
+      double s = dotp(&c->K4[(9 * j) * N3], Cij.data(), 9 * N3);
+      C_homo[9 * j + i] = s / (double)N3;
+    }
+  }
+  return total;
+}
+
+// NBC_update (src/FFT_nr3.f:375-433)
+static int nbc_update(const double* C_homo, double* DbarF, const double* P_bar,
+                      const double* PBC, const int* isNBC) {
+  double A[81], bb[9];
+  for (int i = 0; i < 9; i++) {
+    if (isNBC[i]) {
+      for (int k = 0; k < 9; k++) A[i * 9 + k] = C_homo[k + 9 * i];  // C_homo(1:9, i)
+      bb[i] = PBC[i] - P_bar[i];
+    } else {
+      for (int k = 0; k < 9; k++) A[i * 9 + k] = 0.0;
+      A[i * 9 + i] = 1.0;
+      bb[i] = DbarF[i];
+    }
+  }
+  int info = lu_solve(9, A, 1, bb);
+  if (info) return CPFFT_ERR_NBC_SINGULAR;
+  for (int i = 0; i < 9; i++) DbarF[i] = bb[i];
+  return 0;
+}
+
+int orc_nr3_begin(orc_ctx* c, double tolPCG) {
+  orc_stress_update(c, 1, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
+  int rc = orc_tangent_homo(c, tolPCG, c->C_homo);
+  return rc < 0 ? rc : 0;
+}
+
+// one load step of FFT_nr3 (src/FFT_nr3.f:51-185)
+int orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC, double tolNR,
+                 double tolPCG, int maxIter, double* Pbar, cpfft_stats* st) {
+  using clk = std::chrono::steady_clock;
+  auto t0 = clk::now();
+  cpfft_stats S;
+  std::memset(&S, 0, sizeof(S));
+  long N3 = c->N3, n = 9 * N3;
+  bool existNBC = false;
+  for (int i = 0; i < 9; i++) existNBC |= isNBC[i] != 0;
+  double PBC[9], FBC[9], DbarF[9], barF[9];
+  for (int i = 0; i < 9; i++) {
+    PBC[i] = FBC[i] = DbarF[i] = 0.0;
+    if (isNBC[i]) PBC[i] = BC[i];
+    else { FBC[i] = BC[i]; DbarF[i] = FBC[i] - c->barF_t[i]; }
+  }
+  int rc = 0;
+  if (existNBC && (rc = nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC))) return rc;
+  for (int i = 0; i < 9; i++) barF[i] = c->barF_t[i] + DbarF[i];
+  int iiter_NBC = 0;
+  double tp = 0, ts = 0;
+  auto tic = [] { return clk::now(); };
+  auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+  while (true) {
+    for (int i = 0; i < 9; i++)
+      for (long v = 0; v < N3; v++) c->dFm[i * N3 + v] = DbarF[i];
+    double Fnorm = nrm2(c->Fn1.data(), n);
+    for (long k = 0; k < n; k++) c->Fn1[k] += c->dFm[k];
+    orc_green_apply(c, c->dFm.data(), c->b.data(), 1, nullptr);
+    for (long k = 0; k < n; k++) c->b[k] = -c->b[k];
+    int its = 0;
+    auto a = tic();
+    rc = orc_cg(c, c->b.data(), c->dFm.data(), tolPCG, &its);
+    tp += sec(a);
+    S.cg_solves++; S.cg_iters += its;
+    if (rc) return rc;
+    for (long k = 0; k < n; k++) c->Fn1[k] += c->dFm[k];
+    double resfft = 1.0;
+    int iiter_EBC = 0;
+    while (resfft > tolNR) {
+      a = tic();
+      long long li = 0;
+      S.local_fallbacks += orc_stress_update(c, step, iiter_EBC, nullptr, nullptr, nullptr, nullptr, &li);
+      ts += sec(a);
+      S.local_iters += li;
+      S.stress_updates++;
+      orc_green_apply(c, c->Pn1.data(), c->b.data(), 0, nullptr);
+      for (long k = 0; k < n; k++) c->b[k] = -c->b[k];
+      a = tic();
+      rc = orc_cg(c, c->b.data(), c->dFm.data(), tolPCG, &its);
+      tp += sec(a);
+      S.cg_solves++; S.cg_iters += its;
+      if (rc) return rc;
+      for (long k = 0; k < n; k++) c->Fn1[k] += c->dFm[k];
+      resfft = nrm2(c->dFm.data(), n) / Fnorm;
+      S.newton_iters++;
+      S.res_fft = resfft;
+      if (iiter_EBC == maxIter) return CPFFT_ERR_NEWTON_MAXIT;
+      iiter_EBC++;
+    }
+    a = tic();
+    long long li = 0;
+    S.local_fallbacks += orc_stress_update(c, step, iiter_EBC, nullptr, nullptr, nullptr, nullptr, &li);
+    ts += sec(a);
+    S.local_iters += li;
+    S.stress_updates++;
+    double res1 = 0, res2 = 0;
+    for (int i = 0; i < 9; i++) {
+      double s = 0;
+      for (long v = 0; v < N3; v++) s += c->Pn1[i * N3 + v];
+      c->P_bar[i] = s / (double)N3;
+      res2 += c->P_bar[i] * c->P_bar[i];
+      if (isNBC[i]) res1 += (c->P_bar[i] - PBC[i]) * (c->P_bar[i] - PBC[i]);
+    }
+    double res3 = res2 < 1.0e-8 ? std::sqrt(res1) : std::sqrt(res1 / res2);
+    S.res_pbar = res3;
+    S.nbc_iters = iiter_NBC + 1;
+    if (res3 <= tolNR) break;
+    if (iiter_NBC > maxIter) return CPFFT_ERR_NBC_MAXIT;
+    a = tic();
+    int th = orc_tangent_homo(c, tolPCG, c->C_homo);
+    tp += sec(a);
+    if (th < 0) return th;
+    S.cg_solves += 9; S.cg_iters += th;
+    for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
+    if ((rc = nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC))) return rc;
+    for (int i = 0; i < 9; i++) barF[i] += DbarF[i];
+    iiter_NBC++;
+  }
+  for (int i = 0; i < 9; i++) c->barF_t[i] = barF[i];
+  orc_commit(c);
+  if (Pbar) for (int i = 0; i < 9; i++) Pbar[i] = c->P_bar[i];
+  // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||)
+  orc_green_apply(c, c->Pn1.data(), c->b.data(), 0, nullptr);
+  double pb = 0;
+  for (int i = 0; i < 9; i++) pb += c->P_bar[i] * c->P_bar[i];
+  S.res_equil = nrm2(c->b.data(), n) / (std::sqrt((double)N3) * std::sqrt(pb));
+  S.t_pcg = tp;
+  S.t_sigeps = ts;
+  S.t_total = sec(t0);
+  if (st) *st = S;
+  return S.local_fallbacks ? CPFFT_WARN_LOCAL_FALLBACK : 0;
+}
+
+void orc_get_fields(orc_ctx* c, double* Fn, double* Fn1, double* Pn, double* Pn1, double* K4) {
+  if (Fn) std::copy(c->Fn.begin(), c->Fn.end(), Fn);
+  if (Fn1) std::copy(c->Fn1.begin(), c->Fn1.end(), Fn1);
+  if (Pn) std::copy(c->Pn.begin(), c->Pn.end(), Pn);
+  if (Pn1) std::copy(c->Pn1.begin(), c->Pn1.end(), Pn1);
+  if (K4) std::copy(c->K4.begin(), c->K4.end(), K4);
+}
+void orc_set_fields(orc_ctx* c, const double* Fn, const double* Fn1) {
+  if (Fn) std::copy(Fn, Fn + 9 * c->N3, c->Fn.begin());
+  if (Fn1) std::copy(Fn1, Fn1 + 9 * c->N3, c->Fn1.begin());
+}
+void orc_get_history(orc_ctx* c, double* hist_n, double* hist_np1) {
+  long N3 = c->N3;
+  double h[ORC_HIST];
+  for (long v = 0; v < N3; v++) {
+    if (hist_n) { state_pack(c->hn[v], h); for (int w = 0; w < ORC_HIST; w++) hist_n[w * N3 + v] = h[w]; }
+    if (hist_np1) { state_pack(c->hn1[v], h); for (int w = 0; w < ORC_HIST; w++) hist_np1[w * N3 + v] = h[w]; }
+  }
+}
+void orc_set_history_n(orc_ctx* c, const double* hist_n) {
+  long N3 = c->N3;
+  double h[ORC_HIST];
+  for (long v = 0; v < N3; v++) {
+    for (int w = 0; w < ORC_HIST; w++) h[w] = hist_n[w * N3 + v];
+    state_unpack(h, c->hn[v]);
+  }
+}
+
+int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3], double tstep,
+                     int step, int iter, const double Fn[9], const double Fn1[9],
+                     const double* hist_n, double* hist_np1, double P[9], double A[81],
+                     double out_sig6[6], double out_cep36[36]) {
+  Crys cr;
+  crystal_finalize(*props, cr);
+  VoxProps vp;
+  voxel_props(cr, kocks_deg, vp);
+  State n, np1;
+  if (hist_n) state_unpack(hist_n, n);
+  else state_init(cr, n);
+  M3 fn, fn1;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { fn[i][j] = Fn[3 * i + j]; fn1[i][j] = Fn1[3 * i + j]; }
+  PointOut o;
+  material_point(cr, vp, tstep, step, iter, fn, fn1, n, np1, o);
+  if (hist_np1) state_pack(np1, hist_np1);
+  if (P) for (int i = 0; i < 9; i++) P[i] = o.P[i];
+  if (A) for (int i = 0; i < 81; i++) A[i] = o.A[i];
+  if (out_sig6) for (int i = 0; i < 6; i++) out_sig6[i] = o.sig[i];
+  if (out_cep36) for (int a = 0; a < 6; a++) for (int b = 0; b < 6; b++) out_cep36[a * 6 + b] = o.cep[a][b];
+  return o.ok ? o.iters : -1;
+}
+
+void orc_polar(const double F[9], double R[9]) {
+  M3 f, r;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) f[i][j] = F[3 * i + j];
+  polar_R(f, r);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[3 * i + j] = r[i][j];
+}
+
+void orc_crystal_setup(const cpfft_crystal* props, const double kocks_deg[3], double C66[36],
+                       double ms[72], double qs[36]) {
+  Crys cr;
+  crystal_finalize(*props, cr);
+  VoxProps vp;
+  voxel_props(cr, kocks_deg, vp);
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) C66[a * 6 + b] = vp.C[a][b];
+  for (int s = 0; s < 12; s++) {
+    for (int a = 0; a < 6; a++) ms[s * 6 + a] = vp.ms[s][a];
+    for (int a = 0; a < 3; a++) qs[s * 3 + a] = vp.qs[s][a];
+  }
+}
+
+void orc_fft3(int N, double* re, double* im, int sign) {
+  FFT1 f(N);
+  fft3(f, re, im, sign);
+}
+
+}  // extern "C"

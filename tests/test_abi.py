@@ -1,0 +1,78 @@
+"""The C-ABI library builds, loads and exports every entry point include/cpfft_gpu.h
+declares; argument checks that run before any device work behave as documented.
+No GPU is needed (no call here reaches CUDA)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "cpfft_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cpfft_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("cpfft_init", "cpfft_stress_update", "cpfft_green_apply", "cpfft_cg",
+                     "cpfft_nr3_step", "cpfft_sync_to_host", "cpfft_commit_step",
+                     "cpfft_finalize", "cpfft_tangent_homo"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(gpulib):
+    lib = gpulib.LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r" T (cpfft_[a-z0-9_]+)", out))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    L = gpulib.load_library()
+    for n in declared_functions():
+        assert hasattr(L, n)
+        assert n in gpulib.SIGNATURES
+
+
+def test_calls_before_init_fail_cleanly(gpulib):
+    L = gpulib.load_library()
+    L.cpfft_finalize()
+    x = np.zeros(9)
+    assert L.cpfft_stress_update(1, 0, None, None, None, None) == -7
+    assert L.cpfft_commit_step() == -7
+    assert L.cpfft_nr3_step(1, x.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                            np.zeros(9, dtype=np.int32).ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                            1e-6, 1e-10, 10, None, None) == -7
+    assert b"cpfft_init" in L.cpfft_last_error()
+
+
+def test_init_rejects_bad_arguments(gpulib):
+    from cpfft_gb300 import rve
+    L = gpulib.load_library()
+    cr = gpulib.crystal_struct([dict(rve.FCC_VOCE)])
+    ml = np.ones(8, dtype=np.int32)
+    ka = np.zeros(24)
+    P = ctypes.POINTER
+    mlp = ml.ctypes.data_as(P(ctypes.c_int))
+    kap = ka.ctypes.data_as(P(ctypes.c_double))
+    assert L.cpfft_init(1, mlp, kap, cr, 1, 1.0, 0) == -5       # N too small
+    assert L.cpfft_init(2, mlp, kap, cr, 1, -1.0, 0) == -5      # tstep
+    assert L.cpfft_init(2, mlp, kap, cr, 1, 1.0, 7) == -5       # mapping
+    bad = dict(rve.FCC_VOCE)
+    bad["slip_type"] = 2
+    assert L.cpfft_init(2, mlp, kap, gpulib.crystal_struct([bad]), 1, 1.0, 0) == -5
+    ml2 = ml.copy()
+    ml2[3] = 5
+    assert L.cpfft_init(2, ml2.ctypes.data_as(P(ctypes.c_int)), kap, cr, 1, 1.0, 0) == -5
+
+
+def test_product_path_does_not_reference_the_oracle():
+    for dirpath, _, files in os.walk(os.path.join(ROOT, "cpfft_gb300")):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                text = open(os.path.join(dirpath, f)).read()
+                assert "pyoracle" not in text and "cpfft_oracle" not in text, f

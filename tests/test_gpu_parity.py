@@ -1,0 +1,157 @@
+"""GPU parity: every entry point of the C-ABI against the CPU oracle on the same seeded
+inputs.  Tolerances: per-voxel P, dP/dF and history within 1e-8 relative (FP64 stress
+update); the Green operator within 1e-11 relative; CG solutions within the CG
+tolerance; load-step P_bar within 1e-9 relative of the oracle."""
+import numpy as np
+import pytest
+
+from cpfft_gb300 import rve
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def per_voxel_rel(a, b):
+    """max over voxels of |a - b|_inf / max(|b|_inf, floor) per voxel."""
+    scale = np.maximum(np.abs(b).max(axis=0), 1e-6 * np.abs(b).max())
+    return (np.abs(a - b).max(axis=0) / scale).max()
+
+
+def make_pair(gpulib, oracle, N, ngr=4, seed=11, gmap=0, crystal=None, precision=0):
+    r = rve.make_rve(N, ngr, seed, crystal)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gmap, precision)
+    o = oracle.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, gmap, nthreads=8)
+    return r, s, o
+
+
+def random_F(N, amp, seed):
+    rng = np.random.default_rng(seed)
+    Fn = np.zeros((9, N ** 3))
+    Fn[[0, 4, 8]] = 1.0
+    Fn1 = Fn + amp * rng.standard_normal((9, N ** 3))
+    return Fn, Fn1
+
+
+@pytest.mark.parametrize("exact", [1, 0])
+def test_stress_update_parity(gpulib, oracle, exact):
+    cr = dict(rve.FCC_VOCE)
+    cr["exact_j22"] = exact
+    N = 8
+    r, s, o = make_pair(gpulib, oracle, N, crystal=cr)
+    try:
+        Fn, Fn1 = random_F(N, 4e-4, 1)
+        for it in (0, 1, 2):
+            P, K, _ = s.drive_eps_sig(1, it, Fn, Fn1, want_K4=True)
+            Po, Ko, fails, _ = o.stress_update(1, it, Fn, Fn1)
+            assert fails == 0
+            assert per_voxel_rel(P, Po) < 1e-8
+            assert per_voxel_rel(K, Ko) < 1e-8
+        # a second step on top of the committed history
+        s.commit()
+        o.commit()
+        Fn2 = Fn1 + (Fn1 - Fn)
+        for it in (0, 1):
+            P, K, _ = s.drive_eps_sig(2, it, Fn1, Fn2, want_K4=True)
+            Po, Ko, fails, _ = o.stress_update(2, it, Fn1, Fn2)
+            assert per_voxel_rel(P, Po) < 1e-8
+            assert per_voxel_rel(K, Ko) < 1e-8
+        _, _, H = s.fields(history=True)
+        Ho, Ho1 = o.history()
+        assert per_voxel_rel(H, Ho) < 1e-8
+    finally:
+        s.close()
+        o.close()
+
+
+@pytest.mark.parametrize("N,gmap", [(5, 0), (7, 0), (8, 1), (9, 0), (12, 1), (15, 0), (16, 1),
+                                    (16, 0), (32, 1)])
+def test_green_parity(gpulib, oracle, N, gmap):
+    r, s, o = make_pair(gpulib, oracle, N, gmap=gmap)
+    try:
+        Fn, Fn1 = random_F(N, 1e-3, 2)
+        _, K, _ = s.drive_eps_sig(1, 0, Fn, Fn1, want_P=False, want_K4=True)
+        rng = np.random.default_rng(N)
+        x = rng.standard_normal((9, N ** 3))
+        for flgK in (True, False):
+            y = s.G_K_dF(x, flgK)
+            yo = o.green(x, flgK, K4=K)
+            assert rel(y, yo) < 1e-11, (flgK, rel(y, yo))
+    finally:
+        s.close()
+        o.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cg_parity(gpulib, oracle, precision):
+    N = 9
+    r, s, o = make_pair(gpulib, oracle, N, precision=precision)
+    try:
+        Fn, Fn1 = random_F(N, 1e-3, 3)
+        _, K, _ = s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False, want_K4=True)
+        o.stress_update(1, 1, Fn, Fn1)
+        b = -o.green(np.ones((9, N ** 3)) * 1e-3, True)
+        x, its = s.fftPcg(b, 1e-10)
+        xo, itso, rc = o.cg(b, 1e-10)
+        assert rc == 0
+        # both meet ||r|| <= 1e-10 ||b||; the solutions agree to that tolerance times
+        # the operator's conditioning
+        assert rel(x, xo) < 1e-7
+        res = o.green(x, True) - b
+        assert np.linalg.norm(res) <= 1.5e-10 * np.linalg.norm(b)
+        if precision == 0:
+            assert abs(its - itso) <= 2
+    finally:
+        s.close()
+        o.close()
+
+
+def test_tangent_homo_parity(gpulib, oracle):
+    N = 7
+    r, s, o = make_pair(gpulib, oracle, N)
+    try:
+        s.nr3_begin(1e-10)
+        o.nr3_begin(1e-10)
+        C = s.tangent_homo(1e-10)
+        Co, rc = o.tangent_homo(1e-10)
+        assert rc >= 0
+        assert rel(C, Co) < 1e-9
+    finally:
+        s.close()
+        o.close()
+
+
+@pytest.mark.parametrize("case", ["fcc_voce_odd", "faithful_j22", "even_centered", "mixed"])
+def test_load_step_parity(gpulib, oracle, case):
+    cr = dict(rve.FCC_VOCE)
+    N, gmap, inc, nsteps, precision, tolP = 9, 0, 1e-3, 3, 0, 1e-9
+    if case == "faithful_j22":
+        cr["exact_j22"] = 0
+        inc = 2.5e-4
+    elif case == "even_centered":
+        N, gmap, nsteps = 8, 1, 2
+    elif case == "mixed":
+        precision, tolP = 1, 1e-6
+    r, s, o = make_pair(gpulib, oracle, N, ngr=4, seed=21, gmap=gmap, crystal=cr,
+                        precision=precision)
+    load = rve.uniaxial_tension(inc * 20, 20)
+    try:
+        s.nr3_begin(1e-10)
+        o.nr3_begin(1e-10)
+        for step in range(1, nsteps + 1):
+            rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+            rco, Pbo, sto = o.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+            assert rc == 0 and rco == 0
+            assert rel(Pbar, Pbo) < tolP, (step, rel(Pbar, Pbo))
+            if precision == 0:
+                assert st["newton_iters"] == sto["newton_iters"]
+                assert st["nbc_iters"] == sto["nbc_iters"]
+        F, P = s.fields()
+        fo = o.fields()
+        assert per_voxel_rel(P, fo["Pn1"]) < (1e-8 if precision == 0 else 1e-5)
+        assert rel(F, fo["Fn1"]) < (1e-9 if precision == 0 else 1e-6)
+    finally:
+        s.close()
+        o.close()
