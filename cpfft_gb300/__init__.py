@@ -88,7 +88,15 @@ SIGNATURES = {
     "cpfft_set_F": (_I, [_DP, _DP]),
     "cpfft_finalize": (None, []),
     "cpfft_last_error": (ctypes.c_char_p, []),
+    "cpfft_measure_fp64_peak": (_I, [_DP]),
 }
+
+
+def measure_fp64_peak():
+    """FP64 FMA rate of the current GPU in TFLOP/s."""
+    v = ctypes.c_double(0.0)
+    _check(load_library().cpfft_measure_fp64_peak(ctypes.byref(v)), "fp64 peak")
+    return v.value
 
 _lib = None
 

@@ -173,6 +173,7 @@ struct Ctx {
   GridDesc g;
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
   double *r = nullptr, *p = nullptr, *Ap = nullptr, *w = nullptr, *io = nullptr;
+  double* w2 = nullptr;  // mixed precision: FP64 copy of an inner correction
   double* hist[2] = {nullptr, nullptr};
   int hn = 0;  // index of the history at n
   float *K4f = nullptr, *xf = nullptr, *rf = nullptr, *pf = nullptr, *Apf = nullptr;
@@ -213,7 +214,7 @@ int dalloc(Ptr& p, size_t bytes) {
 
 void free_ctx(Ctx* c) {
   if (!c) return;
-  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io,
+  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats};
   for (void* q : ptrs)
@@ -340,8 +341,13 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
       CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
     }
     total += it;
-    // x += ||r|| d ; r = b - G(K4 : x) in FP64
-    CK(dev_add_f32(x, c->xf, rn, n, c->st));
+    // x += G(||r|| d) ; r = b - G(K4 : x) in FP64.  The FP64 projection keeps x in the
+    // range of G (compatible, zero-mean fields), where every FP64 CG iterate lives:
+    // FP32 rounding leaks into the kernel of G, which the residual cannot see.
+    CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
+    CK(dev_add_f32(c->w2, c->xf, rn, n, c->st));
+    TRY(matvec64(c, c->w2, c->Ap, 0));
+    CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
     TRY(matvec64(c, x, c->Ap, 1));
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
@@ -463,6 +469,7 @@ int need_ctx() {
 int alloc_mixed(Ctx* c) {
   const long long n = 9 * c->N3;
   if (c->K4f) return 0;
+  TRY(dalloc(c->w2, n * sizeof(double)));
   TRY(dalloc(c->K4f, 81 * c->N3 * sizeof(float)));
   TRY(dalloc(c->xf, n * sizeof(float)));
   TRY(dalloc(c->rf, n * sizeof(float)));

@@ -186,6 +186,10 @@ void cpfft_finalize(void);
 /* Human-readable text of the last error (static storage). */
 const char* cpfft_last_error(void);
 
+/* Diagnostic, no counterpart in the reference: measured FP64 FMA rate of the current
+ * GPU in TFLOP/s (the roofline denominator of the FP64-bound kernels). */
+int cpfft_measure_fp64_peak(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -44,9 +44,13 @@ def test_stress_update_parity(gpulib, oracle, exact):
     try:
         Fn, Fn1 = random_F(N, 4e-4, 1)
         for it in (0, 1, 2):
-            P, K, _ = s.drive_eps_sig(1, it, Fn, Fn1, want_K4=True)
+            P, K, rc = s.drive_eps_sig(1, it, Fn, Fn1, want_K4=True)
             Po, Ko, fails, _ = o.stress_update(1, it, Fn, Fn1)
-            assert fails == 0
+            # with the reference's d(R2)/d(tau) a few random-shear voxels exhaust miter;
+            # both sides then keep sigma_n and the elastic tangent and report it
+            assert rc == (1 if fails else 0)
+            if exact:
+                assert fails == 0
             assert per_voxel_rel(P, Po) < 1e-8
             assert per_voxel_rel(K, Ko) < 1e-8
         # a second step on top of the committed history
@@ -54,8 +58,9 @@ def test_stress_update_parity(gpulib, oracle, exact):
         o.commit()
         Fn2 = Fn1 + (Fn1 - Fn)
         for it in (0, 1):
-            P, K, _ = s.drive_eps_sig(2, it, Fn1, Fn2, want_K4=True)
+            P, K, rc = s.drive_eps_sig(2, it, Fn1, Fn2, want_K4=True)
             Po, Ko, fails, _ = o.stress_update(2, it, Fn1, Fn2)
+            assert rc == (1 if fails else 0)
             assert per_voxel_rel(P, Po) < 1e-8
             assert per_voxel_rel(K, Ko) < 1e-8
         _, _, H = s.fields(history=True)
@@ -96,9 +101,9 @@ def test_cg_parity(gpulib, oracle, precision):
         x, its = s.fftPcg(b, 1e-10)
         xo, itso, rc = o.cg(b, 1e-10)
         assert rc == 0
-        # both meet ||r|| <= 1e-10 ||b||; the solutions agree to that tolerance times
-        # the operator's conditioning
-        assert rel(x, xo) < 1e-7
+        # both meet ||r|| <= 1e-10 ||b|| and stay in the range of G; the solutions agree
+        # to that tolerance times the operator's conditioning
+        assert rel(x, xo) < 1e-7, rel(x, xo)
         res = o.green(x, True) - b
         assert np.linalg.norm(res) <= 1.5e-10 * np.linalg.norm(b)
         if precision == 0:
