@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Headline benchmark: voxel stress-updates/s and s/load-step of the finite-strain FFT
+crystal-plasticity hot path at 128^3 (the workload the metric is quoted on).
+
+Workload: 128^3 voxels, 256 periodic-Voronoi grains (seed 3) with Haar-random
+orientations, FCC mm10 Voce material, plane-strain compression at 1e-3 per load step
+(F_zz prescribed, F_yy = 1, shear F held at zero, other P zero), local Newton 1e-10,
+global NR 1e-6, CG 1e-10.  Synthetic inputs (no dataset).  A "step" is one whole load
+step of FFT_nr3 (Newton-Krylov to convergence, the P_bar loop with its homogenised
+tangents, and the state roll-over) through the C-ABI's resident entry point.
+
+value  = N^3 x (stress-update passes in the timed steps) / device time of those steps
+         (CUDA events on the library's stream), whole job over ranks (replicas).
+e2e    = the same units over host wall time of each step plus copying the step's
+         result fields Fn1, Pn1 back to pinned host buffers.
+Inputs larger than L2: every field is >= 150 MB (9 x 128^3 FP64), K4 is 1.4 GB.
+
+`--impl reference` times the CPU stand-in of the reference (the C++ oracle, OpenMP on
+all host cores) on bounded samples of the same workload (see cpu_sample()).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+# per-voxel algorithmic work (the design doc roofline section)
+BYTES_GREEN32 = 540.0          # FP32 Krylov matvec: x 36 + K4 324 + y 36 + 2 half-spectrum trips 144
+BYTES_GREEN64 = 1080.0         # FP64 matvec
+BYTES_STRESS = 1264.0          # stress update: F, F1, state n, P, A, state n+1
+
+
+def fft_flops_per_voxel(N):
+    """Real 3-D transforms: 2.5 log2(N^3) flops per voxel per transform (half of the
+    5 N log2 N complex count), 18 transforms, plus K:x (162) per matvec."""
+    import math
+    return 18 * 2.5 * math.log2(N ** 3) + 162.0
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.idx = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.idx), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, p[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM traffic from the committed ncu summaries (bytes per voxel)."""
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic_per_voxel.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def workload(N, grains, seed):
+    from cpfft_gb300 import rve
+    r = rve.make_rve(N, grains, seed)
+    load = rve.plane_strain_compression(0.10, 100)
+    return r, load
+
+
+def cpu_sample(r, load, steps_hint, nthreads, n_stress_sample, n_green):
+    """CPU stand-in of the reference on a bounded sample of the same workload: the oracle
+    stress update on `n_stress_sample` voxels of the 128^3 RVE (after the first load
+    increment, Newton iteration 1) and `n_green` full-grid FP64 G(K:x) applies; a load
+    step is extrapolated with the per-step pass counts `steps_hint`
+    (stress-update passes, matvecs)."""
+    from oracle import pyoracle as po
+    N = r.N
+    N3 = N ** 3
+    o = po.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 1, nthreads=nthreads)
+    try:
+        # homogeneous first increment of the loading as the sample's F field
+        Fn = np.zeros((9, N3))
+        Fn[[0, 4, 8]] = 1.0
+        Fn1 = np.repeat(load.BC_all[0][:, None], N3, axis=1)
+        o.set_fields(Fn, Fn1)
+        t0 = time.perf_counter()
+        o.stress_sample(1, 1, 0, n_stress_sample)
+        t_su = (time.perf_counter() - t0) * N3 / n_stress_sample
+        x = np.random.default_rng(0).standard_normal((9, N3))
+        t0 = time.perf_counter()
+        for _ in range(n_green):
+            o.green(x, True)
+        t_mv = (time.perf_counter() - t0) / n_green
+    finally:
+        o.close()
+    su, mv = steps_hint
+    t_step = su * t_su + mv * t_mv
+    return {"t_stress_full_grid": t_su, "t_matvec": t_mv, "t_load_step": t_step,
+            "value": N3 * su / t_step}
+
+
+def reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    N = args.N
+    r, load = workload(N, args.grains, args.seed)
+    hint = workload_counts()
+    nthreads = os.cpu_count()
+    vals = []
+    t_total = 0.0
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        res = cpu_sample(r, load, hint, nthreads, n_stress_sample=max(4096, N ** 3 // 64),
+                         n_green=1)
+        t_total += time.perf_counter() - t0
+        if s >= args.warmup:
+            vals.append(res)
+    v = statistics.median([x["value"] for x in vals])
+    tstep = statistics.median([x["t_load_step"] for x in vals])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "voxel stress-updates/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tstep, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(args, "reference"),
+        "cpu_baseline": {"value": v, "unit": "voxel stress-updates/s", "cores": nthreads,
+                         "kind": "port",
+                         "sample": (f"C++ oracle (restatement of the Fortran+MKL path, OpenMP "
+                                    f"{nthreads} threads): stress update on N^3/64 voxels and one "
+                                    f"full-grid FP64 G(K:x) at {N}^3, extrapolated to a load step "
+                                    f"with {hint[0]} stress passes and {hint[1]} matvecs per step")},
+        "e2e": {"value": v, "unit": "voxel stress-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "s_per_load_step": tstep,
+        "wall_s": t_total,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+METRIC = "voxel stress-updates/s and s/load-step at 128^3: learned+mixed vs plain FP64 on GPU"
+
+
+def workload_counts():
+    """Stress-update passes and FP64-equivalent matvecs of one load step of this
+    workload, as measured by the GPU run (profiles/workload_counts.json), else the
+    values of the first measurement."""
+    try:
+        with open(os.path.join(HERE, "profiles", "workload_counts.json")) as f:
+            d = json.load(f)
+            return d["stress_updates_per_step"], d["matvecs_per_step"]
+    except OSError:
+        return 17, 5700
+
+
+def config_dict(args, impl):
+    return {"workload": f"plane-strain compression 10%/100 steps, {args.N}^3 voxels, "
+                        f"{args.grains} Voronoi grains (seed {args.seed}), FCC mm10 Voce",
+            "N": args.N, "grains": args.grains, "seed": args.seed,
+            "mode": args.mode if impl != "reference" else "fp64",
+            "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
+            "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10},
+            "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def gb300_arm(args):
+    import torch
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    else:
+        torch.cuda.set_device(0)
+    import cpfft_gb300 as cp
+    cp.load_library()
+    fp64_peak = cp.measure_fp64_peak()
+    peaks, peak_kind = load_peaks()
+    N = args.N
+    N3 = N ** 3
+    r, load = workload(N, args.grains, args.seed)
+    prec = cp.PREC_MIXED if args.mode == "mixed" else cp.PREC_FP64
+    solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
+    tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
+    solver.nr3_begin(tolPCG)
+    step = 0
+    for _ in range(args.warmup):
+        step += 1
+        rc, _, _ = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
+    # pinned host buffers for the e2e copies of each step's result fields
+    Fh = torch.empty((9, N3), dtype=torch.float64).pin_memory()
+    Ph = torch.empty((9, N3), dtype=torch.float64).pin_memory()
+    Fp = ctypes.cast(Fh.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    Pp = ctypes.cast(Ph.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    L = cp.load_library()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    stats = []
+    t_e2e = 0.0
+    for _ in range(args.steps):
+        step += 1
+        t0 = time.perf_counter()
+        rc, Pbar, st = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG,
+                                       maxIter)
+        if L.cpfft_sync_to_host(Fp, Pp, None) != 0:
+            raise RuntimeError("sync_to_host failed")
+        t_e2e += time.perf_counter() - t0
+        stats.append(st)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t_dev = sum(s["t_device"] for s in stats)
+    su = sum(s["stress_updates"] for s in stats)
+    units = float(N3 * su)
+    tmax, temax = t_dev, t_e2e
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_dev, t_e2e, units], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        tot = t.clone()
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        tmax, temax, units_all = mx[0].item(), mx[1].item(), tot[2].item()
+    else:
+        units_all = units
+    if rank != 0:
+        solver.close()
+        return 0
+    # roofline of the dominant kernel (largest summed event time in the timed steps)
+    tg32 = sum(s["t_green32"] for s in stats)
+    tg64 = sum(s["t_green64"] for s in stats)
+    tsk = sum(s["t_stress_kernel"] for s in stats)
+    ng32 = sum(s["n_green32"] for s in stats)
+    ng64 = sum(s["n_green64"] for s in stats)
+    traffic = load_traffic()
+    kern = max([("green32", tg32), ("green64", tg64), ("stress", tsk)], key=lambda kv: kv[1])[0]
+    if kern == "green32":
+        per = tg32 / ng32
+        ach = BYTES_GREEN32 * N3 / per / 1e9
+        roof = {"kernel": "fp32 G(K:x) (5 passes)", "bound": "hbm", "achieved": ach,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": traffic.get("green32", None) and traffic["green32"] * N3,
+                "algorithmic_bytes_per_launch": BYTES_GREEN32 * N3, "avg_launch_ms": per * 1e3}
+    elif kern == "green64":
+        per = tg64 / ng64
+        ach = fft_flops_per_voxel(N) * N3 / per / 1e12
+        roof = {"kernel": "fp64 G(K:x) (5 passes)", "bound": "fp64", "achieved": ach,
+                "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "peak_source": "measured DFMA rate on this GPU (cpfft_measure_fp64_peak)",
+                "traffic": traffic.get("green64", None) and traffic["green64"] * N3,
+                "algorithmic_flops_per_launch": fft_flops_per_voxel(N) * N3,
+                "avg_launch_ms": per * 1e3}
+    else:
+        per = tsk / su
+        ach = BYTES_STRESS * N3 / per / 1e9
+        roof = {"kernel": "stress update (mm10 + cep2A)", "bound": "hbm", "achieved": ach,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+                "peak_source": f"{peak_kind} hbm_gbs; the kernel is FP64-pipe bound",
+                "traffic": traffic.get("stress", None) and traffic["stress"] * N3,
+                "algorithmic_bytes_per_launch": BYTES_STRESS * N3, "avg_launch_ms": per * 1e3}
+    kernel_split = {"stress_s": tsk, "green64_s": tg64, "green32_s": tg32,
+                    "n_green64": ng64, "n_green32": ng32, "stress_passes": su}
+    cg_iters = sum(s["cg_iters"] for s in stats)
+    hint = (su / len(stats), (cg_iters + ng64) / len(stats))
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        res = cpu_sample(r, load, workload_counts(), os.cpu_count(),
+                         n_stress_sample=max(4096, N3 // 64), n_green=1)
+        cpu = {"value": res["value"], "unit": "voxel stress-updates/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": (f"C++ oracle, OpenMP {os.cpu_count()} threads: stress update of "
+                          f"N^3/64 voxels + one full-grid FP64 G(K:x) at {N}^3, extrapolated "
+                          f"to a load step ({workload_counts()[0]} passes, "
+                          f"{workload_counts()[1]} matvecs)"),
+               "s_per_load_step": res["t_load_step"]}
+    line = {
+        "metric": METRIC,
+        "value": units_all / tmax,
+        "unit": "voxel stress-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tmax / args.steps,
+        "s_per_load_step": tmax / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == cp.PREC_FP64 else "f64+f32",
+        "data": "synthetic",
+        "config": config_dict(args, "gb300"),
+        "e2e": {"value": units_all / temax, "unit": "voxel stress-updates/s",
+                "h2d_bytes_per_step": 9 * 8 + 9 * 4,
+                "d2h_bytes_per_step": 2 * 9 * N3 * 8 + 9 * 8},
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "roofline": roof,
+        "kernel_time_split": kernel_split,
+        "per_step_counts": {"stress_passes": hint[0], "fp64_equiv_matvecs": hint[1],
+                            "newton": [s["newton_iters"] for s in stats],
+                            "nbc": [s["nbc_iters"] for s in stats],
+                            "cg_iters": [s["cg_iters"] for s in stats],
+                            "res_equil": [s["res_equil"] for s in stats],
+                            "res_fft": [s["res_fft"] for s in stats],
+                            "local_iters_per_voxel_pass": sum(s["local_iters"] for s in stats) / (N3 * su)},
+        "fp64_peak_tflops": fp64_peak,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    solver.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--N", type=int, default=128)
+    ap.add_argument("--grains", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
+    # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
+    # the benchmark uses the reference example deck's value 1e-5; the equilibrium
+    # residual ||G(P)||/||P_bar|| is reported per step.
+    ap.add_argument("--tol-nr", type=float, default=1e-5)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gb300_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

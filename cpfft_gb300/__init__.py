@@ -63,7 +63,10 @@ class Stats(ctypes.Structure):
         ("res_fft", ctypes.c_double), ("res_pbar", ctypes.c_double),
         ("res_equil", ctypes.c_double),
         ("t_pcg", ctypes.c_double), ("t_sigeps", ctypes.c_double),
-        ("t_total", ctypes.c_double),
+        ("t_total", ctypes.c_double), ("t_device", ctypes.c_double),
+        ("t_stress_kernel", ctypes.c_double), ("t_green64", ctypes.c_double),
+        ("t_green32", ctypes.c_double), ("n_green64", ctypes.c_longlong),
+        ("n_green32", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
     ]
 
     def as_dict(self):

@@ -15,6 +15,7 @@
 #include "krylov.cuh"
 
 static char g_err[512] = "";
+long long g_kernel_launches = 0;
 void cpfft_set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -174,6 +175,7 @@ struct Ctx {
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
   double *r = nullptr, *p = nullptr, *Ap = nullptr, *w = nullptr, *io = nullptr;
   double* w2 = nullptr;  // mixed precision: FP64 copy of an inner correction
+  bool log = false;      // CPFFT_LOG=1: the reference's residual reports on stderr
   double* hist[2] = {nullptr, nullptr};
   int hn = 0;  // index of the history at n
   float *K4f = nullptr, *xf = nullptr, *rf = nullptr, *pf = nullptr, *Apf = nullptr;
@@ -192,7 +194,48 @@ struct Ctx {
   double barF_t[9], P_bar[9], C_homo[81];
   // counters of the current step
   long long cg_iters = 0, cg_solves = 0, f64_matvecs = 0, f32_matvecs = 0;
+  // CUDA-event timing of every stress / Green launch on the library stream
+  static const int KT_CAP = 512;
+  cudaEvent_t kt_ev[2 * KT_CAP];
+  int kt_kind[KT_CAP];
+  int kt_used = 0;
+  bool kt_ready = false;
+  double kt_acc[3] = {0, 0, 0};
+  long long kt_cnt[3] = {0, 0, 0};
+  cudaEvent_t step_ev[2];
 };
+
+enum { KT_STRESS = 0, KT_G64 = 1, KT_G32 = 2 };
+
+int kt_drain(Ctx* c) {
+  if (!c->kt_used) return 0;
+  if (cudaStreamSynchronize(c->st) != cudaSuccess) {
+    cpfft_set_error("stream synchronize failed");
+    return CPFFT_ERR_CUDA;
+  }
+  for (int i = 0; i < c->kt_used; i++) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->kt_ev[2 * i], c->kt_ev[2 * i + 1]);
+    c->kt_acc[c->kt_kind[i]] += 1e-3 * ms;
+    c->kt_cnt[c->kt_kind[i]]++;
+  }
+  c->kt_used = 0;
+  return 0;
+}
+void kt_start(Ctx* c, int kind) {
+  if (!c->kt_ready) return;
+  c->kt_kind[c->kt_used] = kind;
+  cudaEventRecord(c->kt_ev[2 * c->kt_used], c->st);
+}
+int kt_stop(Ctx* c) {
+  if (!c->kt_ready) return 0;
+  cudaEventRecord(c->kt_ev[2 * c->kt_used + 1], c->st);
+  if (++c->kt_used == Ctx::KT_CAP) return kt_drain(c);
+  return 0;
+}
+void kt_reset(Ctx* c) {
+  for (int k = 0; k < 3; k++) { c->kt_acc[k] = 0; c->kt_cnt[k] = 0; }
+}
 Ctx* g_ctx = nullptr;
 
 #define TRY(expr)                 \
@@ -221,6 +264,11 @@ void free_ctx(Ctx* c) {
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->h_stats) cudaFreeHost(c->h_stats);
+  if (c->kt_ready) {
+    for (int i = 0; i < 2 * Ctx::KT_CAP; i++) cudaEventDestroy(c->kt_ev[i]);
+    cudaEventDestroy(c->step_ev[0]);
+    cudaEventDestroy(c->step_ev[1]);
+  }
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -254,11 +302,15 @@ int dnrm2(Ctx* c, const double* x, double* out) {
 // FP64 matvec y = G(K4:x) or G(x)
 int matvec64(Ctx* c, const double* x, double* y, int flgK) {
   c->f64_matvecs++;
-  return cuda_check(green_apply<double>(x, c->K4, flgK, y, c->S, c->tw, c->g, c->st), "green_apply fp64");
+  kt_start(c, KT_G64);
+  TRY(cuda_check(green_apply<double>(x, c->K4, flgK, y, c->S, c->tw, c->g, c->st), "green_apply fp64"));
+  return kt_stop(c);
 }
 int matvec32(Ctx* c, const float* x, float* y) {
   c->f32_matvecs++;
-  return cuda_check(green_apply<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st), "green_apply fp32");
+  kt_start(c, KT_G32);
+  TRY(cuda_check(green_apply<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st), "green_apply fp32"));
+  return kt_stop(c);
 }
 
 // fftPcg (src/FFT_nr3.f:214-360), plain FP64: CG from x = 0 with the stop test
@@ -384,7 +436,9 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails) {
   a.step = step;
   a.iter = iter;
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
+  kt_start(c, KT_STRESS);
   CK(launch_stress(a, c->st));
+  TRY(kt_stop(c));
   c->K4f_valid = a.K4f != nullptr;
   CK(cudaMemcpyAsync(c->h_stats, c->stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
   TRY(sync(c));
@@ -559,10 +613,25 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   c->g.tkb = 16;
   c->g.tkc = 2;
   c->g.plan = make_plan(N);
+  {
+    const char* lg = getenv("CPFFT_LOG");
+    c->log = lg && lg[0] == '1';
+  }
   auto fail = [&](int rc) { free_ctx(c); return rc; };
   if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
     cpfft_set_error("cudaStreamCreate failed");
     return fail(CPFFT_ERR_CUDA);
+  }
+  {
+    bool ok = true;
+    for (int i = 0; i < 2 * Ctx::KT_CAP; i++) ok &= cudaEventCreate(&c->kt_ev[i]) == cudaSuccess;
+    ok &= cudaEventCreate(&c->step_ev[0]) == cudaSuccess;
+    ok &= cudaEventCreate(&c->step_ev[1]) == cudaSuccess;
+    if (!ok) {
+      cpfft_set_error("cudaEventCreate failed");
+      return fail(CPFFT_ERR_CUDA);
+    }
+    c->kt_ready = true;
   }
   const size_t f9 = 9 * N3 * sizeof(double);
   int rc = 0;
@@ -739,6 +808,10 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   cpfft_stats S;
   memset(&S, 0, sizeof(S));
   c->cg_iters = c->cg_solves = c->f64_matvecs = c->f32_matvecs = 0;
+  TRY(kt_drain(c));
+  kt_reset(c);
+  const long long launches0 = g_kernel_launches;
+  CK(cudaEventRecord(c->step_ev[0], c->st));
   const long long N3 = c->N3, n = 9 * N3;
   bool existNBC = false;
   for (int i = 0; i < 9; i++) existNBC |= isNBC[i] != 0;
@@ -787,6 +860,9 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       if (!std::isfinite(resfft)) { cpfft_set_error("Newton residual is not finite"); return CPFFT_ERR_NONFINITE; }
       S.newton_iters++;
       S.res_fft = resfft;
+      if (c->log)  // the reference's per-iteration report (src/FFT_nr3.f:115, format 1001)
+        fprintf(stderr, "       Iteration %5d  residual %10.3e  (cg %d, local fallbacks %d)\n",
+                iiter_EBC, resfft, its, fails);
       if (iiter_EBC == maxIter) {
         cpfft_set_error("Newton loop does not converge (step %d)", step);
         return CPFFT_ERR_NEWTON_MAXIT;
@@ -812,6 +888,8 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     }
     double res3 = res2 < 1.0e-8 ? std::sqrt(res1) : std::sqrt(res1 / res2);
     S.res_pbar = res3;
+    if (c->log)  // src/FFT_nr3.f:148, format 1002
+      fprintf(stderr, "       Stress iteration %5d  residual %10.3e\n", iiter_NBC, res3);
     S.nbc_iters = iiter_NBC + 1;
     if (res3 <= tolNR) break;
     if (iiter_NBC > maxIter) {
@@ -844,6 +922,19 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   S.cg_iters = (int)c->cg_iters;
   S.t_pcg = tp;
   S.t_sigeps = ts;
+  CK(cudaEventRecord(c->step_ev[1], c->st));
+  TRY(kt_drain(c));
+  {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->step_ev[0], c->step_ev[1]));
+    S.t_device = 1e-3 * ms;
+  }
+  S.t_stress_kernel = c->kt_acc[KT_STRESS];
+  S.t_green64 = c->kt_acc[KT_G64];
+  S.t_green32 = c->kt_acc[KT_G32];
+  S.n_green64 = c->kt_cnt[KT_G64];
+  S.n_green32 = c->kt_cnt[KT_G32];
+  S.kernel_launches = g_kernel_launches - launches0;
   S.t_total = sec(t0);
   if (st) *st = S;
   (void)rc;

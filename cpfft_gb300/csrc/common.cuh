@@ -18,6 +18,10 @@
 
 void cpfft_set_error(const char* fmt, ...);
 
+// Kernels launched by this library since load (the library is single-threaded by
+// contract, see the header); every launch wrapper adds its launches here.
+extern long long g_kernel_launches;
+
 // ---- per-orientation material data (computed once at init, see api.cu) ------------
 // One record per distinct (crystal, orientation): the rotated stiffness and the slip
 // tensors of setup_mm10_rknstr (src/drive_eps_sig.f:537-1002), which the reference

@@ -439,6 +439,7 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
   pass_c<T><<<gc, 256, smem_c<T>(N, g.tkc), st>>>(S, g, tw);
   pass_b<T><<<gb, 256, smem_b<T>(N, g.tkb), st>>>(S, g, tw, 1);
   pass_e<T><<<npair * N, 256, smem_a<T>(N), st>>>(S, y, g, tw);
+  g_kernel_launches += 5;
   return cudaGetLastError();
 }
 

@@ -144,29 +144,34 @@ int grid_for(long long n, int bs) {
 
 }  // namespace
 
+static cudaError_t counted(int k) {
+  g_kernel_launches += k;
+  return cudaGetLastError();
+}
+
 cudaError_t dev_dot(const double* a, const double* b, long long n, double* part, double* sc,
                     int slot, int op, cudaStream_t st) {
   k_dot<double, double><<<NPART, RB, 0, st>>>(a, b, n, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
-  return cudaGetLastError();
+  return counted(2);
 }
 cudaError_t dev_dot_f(const float* a, const float* b, long long n, double* part, double* sc,
                       int slot, int op, cudaStream_t st) {
   k_dot<float, float><<<NPART, RB, 0, st>>>(a, b, n, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
-  return cudaGetLastError();
+  return counted(2);
 }
 template <typename T>
 cudaError_t dev_cg_xr(T* x, T* r, const T* p, const T* Ap, long long n, double* part, double* sc,
                       cudaStream_t st) {
   k_cg_xr<T><<<NPART, RB, 0, st>>>(x, r, p, Ap, n, sc, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, SC_RRNEW, OP_BETA);
-  return cudaGetLastError();
+  return counted(2);
 }
 template <typename T>
 cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st) {
   k_cg_p<T><<<grid_for(n, 256), 256, 0, st>>>(p, r, n, sc);
-  return cudaGetLastError();
+  return counted(1);
 }
 template cudaError_t dev_cg_xr<double>(double*, double*, const double*, const double*, long long,
                                        double*, double*, cudaStream_t);
@@ -177,37 +182,37 @@ template cudaError_t dev_cg_p<float>(float*, const float*, long long, double*, c
 
 cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStream_t st) {
   k_axpy<<<grid_for(n, 256), 256, 0, st>>>(y, x, a, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st) {
   k_scale<<<grid_for(n, 256), 256, 0, st>>>(y, a, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st) {
   k_sub<<<grid_for(n, 256), 256, 0, st>>>(y, a, b, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_fill9(double* y, long long N3, const double* v, cudaStream_t st) {
   k_fill9<<<grid_for(9 * N3, 256), 256, 0, st>>>(y, N3, v[0], v[1], v[2], v[3], v[4], v[5], v[6],
                                                   v[7], v[8]);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_add_const(double* y, double v, long long n, cudaStream_t st) {
   k_add_const<<<grid_for(n, 256), 256, 0, st>>>(y, v, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_to_f32(float* y, const double* x, double s, long long n, cudaStream_t st) {
   k_to_f32<<<grid_for(n, 256), 256, 0, st>>>(y, x, s, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_add_f32(double* y, const float* x, double s, long long n, cudaStream_t st) {
   k_add_f32<<<grid_for(n, 256), 256, 0, st>>>(y, x, s, n);
-  return cudaGetLastError();
+  return counted(1);
 }
 cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, int slot0,
                      cudaStream_t st) {
   k_sum9<<<NPART, RB, 0, st>>>(x, N3, part);
   for (int c = 0; c < 9; c++)
     k_final<<<1, 1024, 0, st>>>(part + c * NPART, NPART, sc, slot0 + c, OP_STORE);
-  return cudaGetLastError();
+  return counted(10);
 }

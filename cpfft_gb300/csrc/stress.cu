@@ -852,5 +852,6 @@ cudaError_t launch_stress(const StressArgs& a, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;
   unsigned blocks = (unsigned)((a.N3 + 127) / 128);
   stress_kernel<<<blocks, 128, 0, s>>>(a);
+  g_kernel_launches += 1;
   return cudaGetLastError();
 }

@@ -88,7 +88,14 @@ typedef struct cpfft_stats {
     double    res_equil;        /* ||G(P)|| / (sqrt(N3) * ||P_bar||) after the step        */
     double    t_pcg;            /* seconds in CG (bucket 1)                                */
     double    t_sigeps;         /* seconds in stress updates (bucket 2)                    */
-    double    t_total;          /* seconds in the whole call                               */
+    double    t_total;          /* seconds in the whole call (host clock)                  */
+    double    t_device;         /* seconds between CUDA events at the call's start and end */
+    double    t_stress_kernel;  /* summed CUDA-event time of the stress-update kernel      */
+    double    t_green64;        /* summed CUDA-event time of FP64 Green applies            */
+    double    t_green32;        /* summed CUDA-event time of FP32 Green applies            */
+    long long n_green64;        /* FP64 Green applies                                      */
+    long long n_green32;        /* FP32 Green applies                                      */
+    long long kernel_launches;  /* kernels this call launched                              */
 } cpfft_stats;
 
 /*

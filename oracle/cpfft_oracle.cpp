@@ -1178,6 +1178,25 @@ int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn, const do
   return fails;
 }
 
+// stress update of voxels [v0, v1) only (bounded CPU-baseline samples); no outputs
+int orc_stress_sample(orc_ctx* c, int step, int iter, long v0, long v1) {
+  long N3 = c->N3;
+  int fails = 0;
+#pragma omp parallel for schedule(dynamic, 128) reduction(+ : fails) num_threads(c->nthreads)
+  for (long v = v0; v < v1; v++) {
+    M3 fn, fn1;
+    load33(c->Fn.data(), N3, v, fn);
+    load33(c->Fn1.data(), N3, v, fn1);
+    PointOut o;
+    material_point(c->crys[c->mat[v]], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v],
+                   c->hn1[v], o);
+    if (!o.ok) fails++;
+    for (int i = 0; i < 9; i++) c->Pn1[i * N3 + v] = o.P[i];
+    for (int m = 0; m < 81; m++) c->K4[m * N3 + v] = o.A[m];
+  }
+  return fails;
+}
+
 void orc_commit(orc_ctx* c) {  // update (src/update.f) + FFT_nr3.f:173-179
   c->hn = c->hn1;
   c->Fn = c->Fn1;
@@ -1386,6 +1405,8 @@ int orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC, doubl
       resfft = nrm2(c->dFm.data(), n) / Fnorm;
       S.newton_iters++;
       S.res_fft = resfft;
+      if (getenv("ORC_LOG"))
+        fprintf(stderr, "  nbc %d newton %d resfft %.3e cg %d\n", iiter_NBC, iiter_EBC, resfft, its);
       if (iiter_EBC == maxIter) return CPFFT_ERR_NEWTON_MAXIT;
       iiter_EBC++;
     }

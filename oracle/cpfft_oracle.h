@@ -30,6 +30,8 @@ void     orc_destroy(orc_ctx* c);
 int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn,
                       const double* Fn1, double* Pn1, double* K4,
                       long long* local_iters);
+/* the same on voxels [v0, v1) only (bounded CPU-baseline samples) */
+int orc_stress_sample(orc_ctx* c, int step, int iter, long v0, long v1);
 /* update(): history n <- n+1, Fn <- Fn1, Pn <- Pn1 */
 void orc_commit(orc_ctx* c);
 

@@ -51,7 +51,10 @@ class Stats(ctypes.Structure):
         ("res_fft", ctypes.c_double), ("res_pbar", ctypes.c_double),
         ("res_equil", ctypes.c_double),
         ("t_pcg", ctypes.c_double), ("t_sigeps", ctypes.c_double),
-        ("t_total", ctypes.c_double),
+        ("t_total", ctypes.c_double), ("t_device", ctypes.c_double),
+        ("t_stress_kernel", ctypes.c_double), ("t_green64", ctypes.c_double),
+        ("t_green32", ctypes.c_double), ("n_green64", ctypes.c_longlong),
+        ("n_green32", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -79,6 +82,8 @@ def lib():
         L.orc_stress_update.restype = i
         L.orc_stress_update.argtypes = [vp, i, i, dp, dp, dp, dp, P(ctypes.c_longlong)]
         L.orc_commit.argtypes = [vp]
+        L.orc_stress_sample.restype = i
+        L.orc_stress_sample.argtypes = [vp, i, i, ctypes.c_long, ctypes.c_long]
         L.orc_green_apply.argtypes = [vp, dp, dp, i, dp]
         L.orc_cg.restype = i
         L.orc_cg.argtypes = [vp, dp, dp, d, ip]
@@ -150,6 +155,9 @@ class Oracle:
         fails = lib().orc_stress_update(self.h, step, it, _p(Fn), _p(Fn1), _p(P), _p(K),
                                         ctypes.byref(li))
         return P, K, fails, li.value
+
+    def stress_sample(self, step, it, v0, v1):
+        return lib().orc_stress_sample(self.h, step, it, v0, v1)
 
     def commit(self):
         lib().orc_commit(self.h)
