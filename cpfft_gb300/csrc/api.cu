@@ -924,6 +924,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   S.t_sigeps = ts;
   CK(cudaEventRecord(c->step_ev[1], c->st));
   TRY(kt_drain(c));
+  CK(cudaEventSynchronize(c->step_ev[1]));
   {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->step_ev[0], c->step_ev[1]));
