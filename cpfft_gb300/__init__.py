@@ -92,6 +92,8 @@ SIGNATURES = {
     "cpfft_finalize": (None, []),
     "cpfft_last_error": (ctypes.c_char_p, []),
     "cpfft_measure_fp64_peak": (_I, [_DP]),
+    "cpfft_green_apply_noalloc": (_I, [_I, _I, ctypes.c_void_p, ctypes.c_void_p, _I,
+                                       ctypes.c_void_p, ctypes.c_void_p]),
 }
 
 

@@ -138,6 +138,21 @@ int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1,
  */
 int cpfft_green_apply(const double* x, double* y, int flgK);
 
+/*
+ * y = G(K4 : x) (flgK = 1) or y = G(x) without any device allocation.  No counterpart in
+ * the reference: it is for callers that cannot call cudaMalloc (host programs that give
+ * all device memory to their own pool allocator at start-up or run under a fixed
+ * device-memory budget).  x, K4, y are the CALLER's device buffers ((N3,9), (N3,81),
+ * (N3,9); K4 may be NULL when flgK = 0); no cpfft_init is needed.  The scratch is one
+ * static device array sized for N <= 32 (2.5 MB, kept by every GPU that loads the
+ * library until exit); larger N returns CPFFT_ERR_BAD_ARG.  The first call on a device
+ * looks up that array's address with the device current -- make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race.  `stream` is
+ * a cudaStream_t (NULL = the legacy default stream); the call returns after enqueueing.
+ */
+int cpfft_green_apply_noalloc(int N, int g_mapping, const double* x, const double* K4,
+                              int flgK, double* y, void* stream);
+
 /* Upload a tangent field K4 (N3,81) from the host (for callers that own K4). */
 int cpfft_set_K4(const double* K4);
 
