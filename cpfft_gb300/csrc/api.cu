@@ -352,8 +352,8 @@ int cg64(Ctx* c, const double* b, double* x, double tol, int* iters) {
 // (iterative refinement).  Same stop test on the FP64 residual as cg64.
 int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
   const long long n = 9 * c->N3;
-  const int maxIter = 1000, maxOuter = 40;
-  const double inner_rtol = 1.0e-5;
+  const int maxIter = 2000;     // FP32 iterations (the FP64 path's cap is 1000)
+  const double delta = 1.0e-2;  // reliable-update threshold
   *iters = 0;
   CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
   double n2b;
@@ -366,50 +366,65 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
     return CPFFT_ERR_BAD_ARG;
   }
   const double tolb = tol * n2b;
-  // residual r = b (x = 0)
+  // FP32 CG on scaled vectors (rf = r / ||r_true||) with reliable updates: whenever the
+  // recursive FP32 residual has dropped by `delta` since the last true residual, the
+  // FP32 increment is projected and added to x in FP64, the true residual
+  // b - G(K4 : x) is recomputed in FP64, and the recursion continues from it with the
+  // same search direction (rescaled).  The stop test is the reference's, on the FP64
+  // residual.  The FP64 projection G keeps x in the range of G (compatible, zero-mean
+  // fields) where every FP64 CG iterate lives: FP32 rounding leaks into the kernel of G,
+  // which the residual cannot see.
   CK(cudaMemcpyAsync(c->w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-  double rn = n2b;
-  int total = 0;
-  for (int outer = 0; outer < maxOuter; outer++) {
-    if (rn <= tolb || rn <= tol) break;
-    // inner FP32 CG on A d = r / ||r||
-    CK(dev_to_f32(c->rf, c->w, 1.0 / rn, n, c->st));
-    CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
-    CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
-    CK(dev_dot_f(c->rf, c->rf, n, c->part, c->sc, SC_RR, OP_STORE, c->st));
-    double rr0;
-    TRY(read_scalar(c, SC_RR, &rr0));
-    const double itol = inner_rtol * std::sqrt(rr0);
-    int it = 0;
-    for (;;) {
-      TRY(matvec32(c, c->pf, c->Apf));
-      CK(dev_dot_f(c->pf, c->Apf, n, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
-      CK(dev_cg_xr<float>(c->xf, c->rf, c->pf, c->Apf, n, c->part, c->sc, c->st));
-      it++;
-      double rr;
+  double rn = n2b, scale = 1.0 / n2b, maxr = n2b;
+  CK(dev_to_f32(c->rf, c->w, scale, n, c->st));
+  CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+  CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+  CK(dev_dot_f(c->rf, c->rf, n, c->part, c->sc, SC_RR, OP_STORE, c->st));
+  double rr_prev;
+  TRY(read_scalar(c, SC_RR, &rr_prev));
+  int it = 0;
+  bool converged = false;
+  for (;;) {
+    TRY(matvec32(c, c->pf, c->Apf));
+    CK(dev_dot_f(c->pf, c->Apf, n, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+    CK(dev_cg_xr<float>(c->xf, c->rf, c->pf, c->Apf, n, c->part, c->sc, c->st));
+    it++;
+    double rr;
+    TRY(read_scalar(c, SC_RRNEW, &rr));
+    if (!std::isfinite(rr)) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    const double rest = std::sqrt(rr) / scale;
+    if (rest < delta * maxr || rest <= tolb || rest <= tol || it >= maxIter) {
+      // reliable update
+      CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
+      CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
+      TRY(matvec64(c, c->w2, c->Ap, 0));
+      CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
+      TRY(matvec64(c, x, c->Ap, 1));
+      CK(dev_sub(c->w, b, c->Ap, n, c->st));
+      TRY(dnrm2(c, c->w, &rn));
+      if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
+      if (rn <= tolb || rn <= tol) { converged = true; break; }
+      if (it >= maxIter) break;
+      const double nscale = 1.0 / rn, k = nscale / scale;
+      CK(dev_to_f32(c->rf, c->w, nscale, n, c->st));
+      CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+      CK(dev_scale_f(c->pf, (float)k, n, c->st));
+      CK(dev_dot_f(c->rf, c->rf, n, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
       TRY(read_scalar(c, SC_RRNEW, &rr));
-      if (!std::isfinite(rr)) { cpfft_set_error("inner CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
-      if (std::sqrt(rr) <= itol || it >= maxIter || total + it >= maxIter * 4) break;
-      CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+      // beta = |r_true|^2 / |r_prev|^2 with both in the new scaling
+      c->h_sc[SC_BETA] = rr / (rr_prev * k * k);
+      CK(cudaMemcpyAsync(c->sc + SC_BETA, c->h_sc + SC_BETA, sizeof(double),
+                         cudaMemcpyHostToDevice, c->st));
+      scale = nscale;
+      maxr = rn;
     }
-    total += it;
-    // x += G(||r|| d) ; r = b - G(K4 : x) in FP64.  The FP64 projection keeps x in the
-    // range of G (compatible, zero-mean fields), where every FP64 CG iterate lives:
-    // FP32 rounding leaks into the kernel of G, which the residual cannot see.
-    CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
-    CK(dev_add_f32(c->w2, c->xf, rn, n, c->st));
-    TRY(matvec64(c, c->w2, c->Ap, 0));
-    CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
-    TRY(matvec64(c, x, c->Ap, 1));
-    CK(dev_sub(c->w, b, c->Ap, n, c->st));
-    TRY(dnrm2(c, c->w, &rn));
-    if (!std::isfinite(rn)) { cpfft_set_error("outer residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    if (total >= maxIter * 4) break;
+    CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+    rr_prev = rr;
   }
-  *iters = total;
-  c->cg_iters += total;
+  *iters = it;
+  c->cg_iters += it;
   c->cg_solves++;
-  if (!(rn <= tolb || rn <= tol)) { cpfft_set_error("mixed-precision refinement did not converge"); return CPFFT_ERR_CG_MAXIT; }
+  if (!converged) { cpfft_set_error("mixed-precision CG did not converge"); return CPFFT_ERR_CG_MAXIT; }
   return 0;
 }
 

@@ -67,6 +67,12 @@ __device__ __forceinline__ void dft8(T2* v) {
   }
 }
 
+// Shared-memory columns are padded: element k of a column sits at pidx(k) = k + k/8 and
+// columns are padlen(N) apart.  The Stockham stages write with strides of R and Ns
+// elements; the padding breaks those power-of-two strides across the 32 banks.
+__host__ __device__ __forceinline__ int pidx(int k) { return k + (k >> 3); }
+__host__ __device__ __forceinline__ int padlen(int N) { return N + (N >> 3) + 1; }
+
 // One forward Stockham stage of radix R on `ncols` columns (column stride cs) from
 // src to dst; tw[k] = exp(-2 pi i k / N).  Radix 2/4/8 run as register butterflies,
 // any other radix evaluates each output as a direct sum (test-only odd sizes).
@@ -81,22 +87,23 @@ __device__ void stage(const T2* __restrict__ src, T2* __restrict__ dst, int ncol
       int col = t / NR, j = t - col * NR;
       int jm = j % Ns;
       int ts = jm * tstride;
-      const T2* s = src + col * cs + j;
+      const T2* s = src + col * cs;
       T2 v[8];
 #pragma unroll
       for (int r = 0; r < 8; r++)
         if (r < R) {
-          T2 x = s[r * NR];
+          T2 x = s[pidx(j + r * NR)];
           if (r) x = cmul<T2, T>(x, tw[r * ts]);
           v[r] = x;
         }
       if (R == 2) bfly2<T2, T>(v[0], v[1]);
       else if (R == 4) dft4<T2, T>(v);
       else dft8<T2, T>(v);
-      T2* d = dst + col * cs + (j / Ns) * Ns * R + jm;
+      T2* d = dst + col * cs;
+      const int base = (j / Ns) * Ns * R + jm;
 #pragma unroll
       for (int r = 0; r < 8; r++)
-        if (r < R) d[r * Ns] = v[r];
+        if (r < R) d[pidx(base + r * Ns)] = v[r];
     }
   } else {
     const int total = ncols * N;
@@ -106,14 +113,14 @@ __device__ void stage(const T2* __restrict__ src, T2* __restrict__ dst, int ncol
       int j = rem % NR, sidx = rem / NR;  // output s of butterfly j
       int jm = j % Ns;
       int ts = jm * tstride;
-      const T2* s = src + col * cs + j;
+      const T2* s = src + col * cs;
       T2 acc; acc.x = 0; acc.y = 0;
       for (int r = 0; r < R; r++) {
         int e = (r * ts + ((r * sidx) % R) * NoR) % N;
-        T2 p = cmul<T2, T>(s[r * NR], tw[e]);
+        T2 p = cmul<T2, T>(s[pidx(j + r * NR)], tw[e]);
         acc.x += p.x; acc.y += p.y;
       }
-      dst[col * cs + (j / Ns) * Ns * R + jm + sidx * Ns] = acc;
+      dst[col * cs + pidx((j / Ns) * Ns * R + jm + sidx * Ns)] = acc;
     }
   }
 }
@@ -172,11 +179,11 @@ __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK*
                                               GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
   using T2 = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = g.N, H = g.H;
+  const int N = g.N, H = g.H, Lp = padlen(N);
   const long long N3 = g.N3;
   T2* tw = reinterpret_cast<T2*>(smem_raw);
   T2* b0 = tw + N;
-  T2* b1 = b0 + 9 * N;
+  T2* b1 = b0 + 9 * Lp;
   load_tw(tw, twg, N);
   const int npair = (N + 1) / 2;
   const int bp = blockIdx.x % npair, c = blockIdx.x / npair;
@@ -208,16 +215,16 @@ __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK*
     }
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-      if (l == 0) b0[i * N + a].x = y[i];
-      else b0[i * N + a].y = y[i];
+      if (l == 0) b0[i * Lp + pidx(a)].x = y[i];
+      else b0[i * Lp + pidx(a)].y = y[i];
     }
   }
   __syncthreads();
-  T2* r = fft_cols<T2, T>(b0, b1, 9, N, g.plan, tw);
+  T2* r = fft_cols<T2, T>(b0, b1, 9, Lp, g.plan, tw);
   // unpack the two real lines: X0 = (Z + conj Z(-k))/2, X1 = (Z - conj Z(-k))/(2i)
   for (int t = threadIdx.x; t < 9 * H; t += blockDim.x) {
     int i = t / H, k = t - i * H;
-    T2 z = r[i * N + k], w = conjg(r[i * N + (N - k) % N]);
+    T2 z = r[i * Lp + pidx(k)], w = conjg(r[i * Lp + pidx((N - k) % N)]);
     T2 X0, X1;
     X0.x = (T)0.5 * (z.x + w.x); X0.y = (T)0.5 * (z.y + w.y);
     X1.x = (T)0.5 * (z.y - w.y); X1.y = (T)-0.5 * (z.x - w.x);
@@ -234,10 +241,10 @@ __global__ void __launch_bounds__(256) pass_b(typename Vec2<T>::t* __restrict__ 
                                               int inverse) {
   using T2 = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = g.N, H = g.H, TK = g.tkb;
+  const int N = g.N, H = g.H, TK = g.tkb, Lp = padlen(N);
   T2* tw = reinterpret_cast<T2*>(smem_raw);
   T2* b0 = tw + N;
-  T2* b1 = b0 + TK * N;
+  T2* b1 = b0 + TK * Lp;
   load_tw(tw, twg, N);
   const int ka0 = blockIdx.x * TK;
   const int c = blockIdx.y, i = blockIdx.z;
@@ -249,15 +256,15 @@ __global__ void __launch_bounds__(256) pass_b(typename Vec2<T>::t* __restrict__ 
     v.x = 0; v.y = 0;
     if (ka < H) v = plane[(long long)row * H + ka];
     if (inverse) v.y = -v.y;
-    b0[kk * N + row] = v;
+    b0[kk * Lp + pidx(row)] = v;
   }
   __syncthreads();
-  T2* r = fft_cols<T2, T>(b0, b1, TK, N, g.plan, tw);
+  T2* r = fft_cols<T2, T>(b0, b1, TK, Lp, g.plan, tw);
   for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
     int row = t / TK, kk = t - row * TK;
     int ka = ka0 + kk;
     if (ka < H) {
-      T2 v = r[kk * N + row];
+      T2 v = r[kk * Lp + pidx(row)];
       if (inverse) v.y = -v.y;
       plane[(long long)row * H + ka] = v;
     }
@@ -270,10 +277,10 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
                                               const typename Vec2<T>::t* __restrict__ twg) {
   using T2 = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = g.N, H = g.H, TK = g.tkc;
+  const int N = g.N, H = g.H, TK = g.tkc, Lp = padlen(N);
   T2* tw = reinterpret_cast<T2*>(smem_raw);
   T2* b0 = tw + N;
-  T2* b1 = b0 + 9 * TK * N;
+  T2* b1 = b0 + 9 * TK * Lp;
   load_tw(tw, twg, N);
   const int ka0 = blockIdx.x * TK;
   const int kb = blockIdx.y;
@@ -286,10 +293,10 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
     T2 v;
     v.x = 0; v.y = 0;
     if (ka < H) v = S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka];
-    b0[(i * TK + kk) * N + c] = v;
+    b0[(i * TK + kk) * Lp + pidx(c)] = v;
   }
   __syncthreads();
-  T2* r = fft_cols<T2, T>(b0, b1, 9 * TK, N, g.plan, tw);
+  T2* r = fft_cols<T2, T>(b0, b1, 9 * TK, Lp, g.plan, tw);
   T2* o = (r == b0) ? b1 : b0;
   // Green contraction at every (kc, kb, ka) of the tile, symmetrised over +-f
   const int Nh = g.Nhalf, gm = g.gmap;
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
     T2 A[9], out[9];
 #pragma unroll
     for (int i = 0; i < 9; i++) {
-      A[i] = r[(i * TK + kk) * N + kc];
+      A[i] = r[(i * TK + kk) * Lp + pidx(kc)];
       out[i].x = 0; out[i].y = 0;
     }
     // centered mapping at even N: the Nyquist frequency has no signed partner and
@@ -322,17 +329,17 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
 #pragma unroll
     for (int i = 0; i < 9; i++) {
       out[i].y = -out[i].y;
-      o[(i * TK + kk) * N + kc] = out[i];
+      o[(i * TK + kk) * Lp + pidx(kc)] = out[i];
     }
   }
   __syncthreads();
-  T2* r2 = fft_cols<T2, T>(o, r, 9 * TK, N, g.plan, tw);
+  T2* r2 = fft_cols<T2, T>(o, r, 9 * TK, Lp, g.plan, tw);
   for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
     int kk = t % TK, rem = t / TK;
     int c = rem % N, i = rem / N;
     int ka = ka0 + kk;
     if (ka < H) {
-      T2 v = r2[(i * TK + kk) * N + c];
+      T2 v = r2[(i * TK + kk) * Lp + pidx(c)];
       v.y = -v.y;
       S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka] = v;
     }
@@ -346,11 +353,11 @@ __global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restr
                                               const typename Vec2<T>::t* __restrict__ twg) {
   using T2 = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int N = g.N, H = g.H;
+  const int N = g.N, H = g.H, Lp = padlen(N);
   const long long N3 = g.N3;
   T2* tw = reinterpret_cast<T2*>(smem_raw);
   T2* b0 = tw + N;
-  T2* b1 = b0 + 9 * N;
+  T2* b1 = b0 + 9 * Lp;
   load_tw(tw, twg, N);
   const int npair = (N + 1) / 2;
   const int bp = blockIdx.x % npair, c = blockIdx.x / npair;
@@ -369,16 +376,16 @@ __global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restr
     T2 z;
     z.x = X0.x - X1.y;
     z.y = -(X0.y + X1.x);
-    b0[i * N + k] = z;
+    b0[i * Lp + pidx(k)] = z;
   }
   __syncthreads();
-  T2* r = fft_cols<T2, T>(b0, b1, 9, N, g.plan, tw);
+  T2* r = fft_cols<T2, T>(b0, b1, 9, Lp, g.plan, tw);
   for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
     int l = t / (9 * N), rem = t - l * 9 * N;
     int i = rem / N, a = rem - i * N;
     int b = l ? bl1 : bl0;
     if (b < N) {
-      T2 z = r[i * N + a];  // conj of the unscaled inverse
+      T2 z = r[i * Lp + pidx(a)];  // conj of the unscaled inverse
       long long v = a + (long long)N * b + (long long)N * N * c;
       y[i * N3 + v] = l ? -z.y : z.x;
     }
@@ -386,11 +393,16 @@ __global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restr
 }
 
 template <typename T>
-size_t smem_a(int N) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * N); }
+size_t smem_a(int N) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * padlen(N)); }
 template <typename T>
-size_t smem_b(int N, int tk) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * tk * N); }
+size_t smem_b(int N, int tk) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * tk * padlen(N)); }
 template <typename T>
-size_t smem_c(int N, int tk) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * tk * N); }
+size_t smem_c(int N, int tk) {
+  return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * tk * padlen(N));
+}
+// columns per block of pass C: 32-byte rows of the half spectrum per (component, c)
+template <typename T>
+constexpr int tile_c() { return sizeof(T) == 4 ? 4 : 2; }
 
 }  // namespace
 
@@ -417,7 +429,7 @@ FftPlan make_plan(int N) {
 template <typename T>
 cudaError_t green_setup(int N) {
   cudaError_t e;
-  size_t a = smem_a<T>(N), b = smem_b<T>(N, 16), c = smem_c<T>(N, 2);
+  size_t a = smem_a<T>(N), b = smem_b<T>(N, 16), c = smem_c<T>(N, tile_c<T>());
   if ((e = cudaFuncSetAttribute(pass_a<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
   if ((e = cudaFuncSetAttribute(pass_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b))) return e;
   if ((e = cudaFuncSetAttribute(pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c))) return e;
@@ -430,7 +442,7 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
   const int N = g.N, H = g.H;
   g.tkb = 16;
-  g.tkc = 2;
+  g.tkc = tile_c<T>();
   const int npair = (N + 1) / 2;
   pass_a<T, T><<<npair * N, 256, smem_a<T>(N), st>>>(x, K4, flgK, S, g, tw);
   dim3 gb((H + g.tkb - 1) / g.tkb, N, 9);

@@ -25,11 +25,11 @@ __device__ __forceinline__ double block_sum(double v) {
 template <typename TA, typename TB>
 __global__ void __launch_bounds__(RB) k_dot(const TA* __restrict__ a, const TB* __restrict__ b,
                                             long long n, double* __restrict__ part) {
-  double s = 0.0;
+  TA s = 0;
   for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB)
-    s += (double)a[i] * (double)b[i];
-  s = block_sum(s);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
+    s += a[i] * (TA)b[i];
+  double sb = block_sum((double)s);
+  if (threadIdx.x == 0) part[blockIdx.x] = sb;
 }
 
 // final pass: sc[slot] = sum(part); op-specific scalar follow-ups for CG
@@ -58,26 +58,28 @@ __global__ void __launch_bounds__(RB) k_cg_xr(T* __restrict__ x, T* __restrict__
                                               const T* __restrict__ p, const T* __restrict__ Ap,
                                               long long n, const double* __restrict__ sc,
                                               double* __restrict__ part) {
-  const double alpha = sc[SC_ALPHA];
-  double s = 0.0;
+  // arithmetic in T: on GB300 an FP64 instruction costs ~64 FP32 ones, so the FP32
+  // vectors stay in FP32; per-thread partial sums are promoted only for the block sum
+  const T alpha = (T)sc[SC_ALPHA];
+  T s = 0;
   for (long long i = (long long)blockIdx.x * RB + threadIdx.x; i < n; i += (long long)gridDim.x * RB) {
-    x[i] = (T)((double)x[i] + alpha * (double)p[i]);
-    T ri = (T)((double)r[i] - alpha * (double)Ap[i]);
+    x[i] = x[i] + alpha * p[i];
+    T ri = r[i] - alpha * Ap[i];
     r[i] = ri;
-    s += (double)ri * (double)ri;
+    s += ri * ri;
   }
-  s = block_sum(s);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  double sb = block_sum((double)s);
+  if (threadIdx.x == 0) part[blockIdx.x] = sb;
 }
 
 // p = r + beta p ; rr <- rr_new
 template <typename T>
 __global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, long long n,
                        double* __restrict__ sc) {
-  const double beta = sc[SC_BETA];
+  const T beta = (T)sc[SC_BETA];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    p[i] = (T)((double)r[i] + beta * (double)p[i]);
+    p[i] = r[i] + beta * p[i];
   __syncthreads();
   if (blockIdx.x == 0 && threadIdx.x == 0) sc[SC_RR] = sc[SC_RRNEW];
 }
@@ -88,6 +90,11 @@ __global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, dou
     y[i] += a * x[i];
 }
 __global__ void k_scale(double* __restrict__ y, double a, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] *= a;
+}
+__global__ void k_scale_f(float* __restrict__ y, float a, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] *= a;
@@ -186,6 +193,10 @@ cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStre
 }
 cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st) {
   k_scale<<<grid_for(n, 256), 256, 0, st>>>(y, a, n);
+  return counted(1);
+}
+cudaError_t dev_scale_f(float* y, float a, long long n, cudaStream_t st) {
+  k_scale_f<<<grid_for(n, 256), 256, 0, st>>>(y, a, n);
   return counted(1);
 }
 cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st) {

@@ -24,6 +24,7 @@ cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st)
 cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
 cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st);
 cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st);
+cudaError_t dev_scale_f(float* y, float a, long long n, cudaStream_t st);
 cudaError_t dev_fill9(double* y, long long N3, const double* v, cudaStream_t st);
 cudaError_t dev_add_const(double* y, double v, long long n, cudaStream_t st);
 cudaError_t dev_to_f32(float* y, const double* x, double s, long long n, cudaStream_t st);
