@@ -17,6 +17,7 @@
 // IDFT(Hs(f) X(f)) with Hs(f) = (Ghat(q(f)) + Ghat(q(-f)))/2, which keeps the half
 // spectrum Hermitian and is what pass C applies, for both frequency mappings.
 #include "fft_green.cuh"
+#include "fft_warp.cuh"
 
 namespace {
 
@@ -392,6 +393,260 @@ __global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restr
   }
 }
 
+// ---- warp-FFT passes for power-of-two N = 32 M ------------------------------------
+// Same data flow and HBM layout as the passes above; each column transform runs in the
+// registers of one warp (fft_warp.cuh), shared memory only stages coalesced tiles.
+
+// load a column held at col[pidx(k)], transform (inverse through conjugation), store back
+template <int M, typename T, bool INV>
+__device__ __forceinline__ void warp_column(typename Vec2<T>::t* col,
+                                            const typename Vec2<T>::t* tw) {
+  using T2 = typename Vec2<T>::t;
+  const int lane = threadIdx.x & 31;
+  T2 v[M];
+#pragma unroll
+  for (int j = 0; j < M; j++) {
+    v[j] = col[pidx(32 * j + lane)];
+    if (INV) v[j].y = -v[j].y;
+  }
+  warpfft::fft<M, T2, T>(v, tw);
+  const int kb = M * warpfft::brev5(lane);
+  __syncwarp();
+#pragma unroll
+  for (int k1 = 0; k1 < M; k1++) {
+    T2 o = v[k1];
+    if (INV) o.y = -o.y;
+    col[pidx(k1 + kb)] = o;
+  }
+}
+
+template <int M, typename T, typename TK>
+__global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK* __restrict__ K4,
+                                               int flgK, typename Vec2<T>::t* __restrict__ S,
+                                               GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  const int Lp = padlen(N);
+  const long long N3 = g.N3;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* col = tw + N;
+  load_tw(tw, twg, N);
+  const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
+  const int bl0 = 2 * bp;
+  for (int t = threadIdx.x; t < 2 * N; t += blockDim.x) {
+    int l = t / N, a = t - l * N;
+    long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
+    T y[9];
+    if (flgK) {
+      T xv[9];
+#pragma unroll
+      for (int j = 0; j < 9; j++) xv[j] = x[j * N3 + v];
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        T s = 0;
+#pragma unroll
+        for (int j = 0; j < 9; j++) s += (T)K4[(9 * i + j) * N3 + v] * xv[j];
+        y[i] = s;
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 9; i++) y[i] = x[i * N3 + v];
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      if (l == 0) col[i * Lp + pidx(a)].x = y[i];
+      else col[i * Lp + pidx(a)].y = y[i];
+    }
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  if (w < 9) warp_column<M, T, false>(col + w * Lp, tw);
+  __syncthreads();
+  for (int t = threadIdx.x; t < 9 * H; t += blockDim.x) {
+    int i = t / H, k = t - i * H;
+    T2 z = col[i * Lp + pidx(k)], wv = conjg(col[i * Lp + pidx((N - k) & (N - 1))]);
+    T2 X0, X1;
+    X0.x = (T)0.5 * (z.x + wv.x); X0.y = (T)0.5 * (z.y + wv.y);
+    X1.x = (T)0.5 * (z.y - wv.y); X1.y = (T)-0.5 * (z.x - wv.x);
+    long long base = ((long long)i * N + c) * N;
+    S[(base + bl0) * H + k] = X0;
+    S[(base + bl0 + 1) * H + k] = X1;
+  }
+}
+
+// TK columns of one (component, c) plane per block, one warp per column
+template <int M, typename T, int TK>
+__global__ void __launch_bounds__(32 * TK) wpass_b(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+                                                   const typename Vec2<T>::t* __restrict__ twg,
+                                                   int inverse) {
+  using T2 = typename Vec2<T>::t;
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  const int Lp = padlen(N);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* col = tw + N;
+  load_tw(tw, twg, N);
+  const int ka0 = blockIdx.x * TK;
+  const int c = blockIdx.y, i = blockIdx.z;
+  T2* plane = S + ((long long)i * N + c) * (long long)N * H;
+  for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
+    int row = t / TK, kk = t - row * TK;
+    int ka = ka0 + kk;
+    T2 v;
+    v.x = 0; v.y = 0;
+    if (ka < H) v = plane[(long long)row * H + ka];
+    col[kk * Lp + pidx(row)] = v;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  if (inverse) warp_column<M, T, true>(col + w * Lp, tw);
+  else warp_column<M, T, false>(col + w * Lp, tw);
+  __syncthreads();
+  for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
+    int row = t / TK, kk = t - row * TK;
+    int ka = ka0 + kk;
+    if (ka < H) plane[(long long)row * H + ka] = col[kk * Lp + pidx(row)];
+  }
+}
+
+template <int M, typename T, int TK>
+__global__ void __launch_bounds__(256) wpass_c(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+                                               const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  const int Lp = padlen(N);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* col = tw + N;
+  load_tw(tw, twg, N);
+  const int ka0 = blockIdx.x * TK;
+  const int kb = blockIdx.y;
+  const long long cstr = (long long)N * H;
+  for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
+    int kk = t % TK, rem = t / TK;
+    int c = rem % N, i = rem / N;
+    int ka = ka0 + kk;
+    T2 v;
+    v.x = 0; v.y = 0;
+    if (ka < H) v = S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka];
+    col[(i * TK + kk) * Lp + pidx(c)] = v;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int cc = w; cc < 9 * TK; cc += nw) warp_column<M, T, false>(col + cc * Lp, tw);
+  __syncthreads();
+  const int Nh = g.Nhalf, gm = g.gmap;
+  const T scale = (T)g.inv_n3;
+  for (int t = threadIdx.x; t < N * TK; t += blockDim.x) {
+    int kc = t / TK, kk = t - kc * TK;
+    int ka = ka0 + kk;
+    T2 A[9], out[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+      A[i] = col[(i * TK + kk) * Lp + pidx(kc)];
+      out[i].x = 0; out[i].y = 0;
+    }
+    bool nyq = gm == CPFFT_G_CENTERED && (2 * kc == N || 2 * kb == N || 2 * ka == N);
+    if (ka < H && !nyq) {
+      int p0 = qmap(kc, N, Nh, gm), p1 = qmap(kb, N, Nh, gm), p2 = qmap(ka, N, Nh, gm);
+      int m0 = qmap((N - kc) & (N - 1), N, Nh, gm), m1 = qmap((N - kb) & (N - 1), N, Nh, gm),
+          m2 = qmap((N - ka) & (N - 1), N, Nh, gm);
+      if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
+        ghat_acc<T2, T>(A, p0, p1, p2, scale, out);
+      } else {
+        ghat_acc<T2, T>(A, p0, p1, p2, (T)0.5 * scale, out);
+        ghat_acc<T2, T>(A, m0, m1, m2, (T)0.5 * scale, out);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; i++) col[(i * TK + kk) * Lp + pidx(kc)] = out[i];
+  }
+  __syncthreads();
+  for (int cc = w; cc < 9 * TK; cc += nw) warp_column<M, T, true>(col + cc * Lp, tw);
+  __syncthreads();
+  for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
+    int kk = t % TK, rem = t / TK;
+    int c = rem % N, i = rem / N;
+    int ka = ka0 + kk;
+    if (ka < H)
+      S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka] = col[(i * TK + kk) * Lp + pidx(c)];
+  }
+}
+
+template <int M, typename T>
+__global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __restrict__ S,
+                                               T* __restrict__ y, GridDesc g,
+                                               const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  const int Lp = padlen(N);
+  const long long N3 = g.N3;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* col = tw + N;
+  load_tw(tw, twg, N);
+  const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
+  const int bl0 = 2 * bp;
+  for (int t = threadIdx.x; t < 9 * N; t += blockDim.x) {
+    int i = t / N, k = t - i * N;
+    long long base = ((long long)i * N + c) * N;
+    int kk = k < H ? k : N - k;
+    T2 X0 = S[(base + bl0) * H + kk], X1 = S[(base + bl0 + 1) * H + kk];
+    if (kk == 0 || kk == N / 2) { X0.y = 0; X1.y = 0; }
+    if (k >= H) { X0.y = -X0.y; X1.y = -X1.y; }
+    T2 z;  // Z = X0 + i X1 (the inverse is taken as conj(FFT(conj Z)))
+    z.x = X0.x - X1.y;
+    z.y = X0.y + X1.x;
+    col[i * Lp + pidx(k)] = z;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  if (w < 9) warp_column<M, T, true>(col + w * Lp, tw);
+  __syncthreads();
+  for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
+    int l = t / (9 * N), rem = t - l * 9 * N;
+    int i = rem / N, a = rem - i * N;
+    T2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
+    long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
+    y[i * N3 + v] = l ? z.y : z.x;
+  }
+}
+
+template <typename T>
+size_t smem_w(int N, int ncols) { return sizeof(typename Vec2<T>::t) * (size_t)(N + ncols * padlen(N)); }
+template <typename T>
+constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
+constexpr int WTILE_B = 8;
+
+template <int M, typename T>
+cudaError_t wgreen_setup() {
+  constexpr int N = 32 * M;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(wpass_a<M, T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_w<T>(N, 9)))) return e;
+  if ((e = cudaFuncSetAttribute(wpass_b<M, T, WTILE_B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_w<T>(N, WTILE_B)))) return e;
+  if ((e = cudaFuncSetAttribute(wpass_c<M, T, wtile_c<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_w<T>(N, 9 * wtile_c<T>())))) return e;
+  if ((e = cudaFuncSetAttribute(wpass_e<M, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_w<T>(N, 9)))) return e;
+  return cudaSuccess;
+}
+
+template <int M, typename T>
+void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                  const typename Vec2<T>::t* tw, const GridDesc& g, cudaStream_t st) {
+  constexpr int N = 32 * M, H = N / 2 + 1, TC = wtile_c<T>();
+  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(x, K4, flgK, S, g, tw);
+  dim3 gb((H + WTILE_B - 1) / WTILE_B, N, 9);
+  wpass_b<M, T, WTILE_B><<<gb, 32 * WTILE_B, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 0);
+  dim3 gc((H + TC - 1) / TC, N);
+  wpass_c<M, T, TC><<<gc, 256, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
+  wpass_b<M, T, WTILE_B><<<gb, 32 * WTILE_B, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
+  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(S, y, g, tw);
+}
+
 template <typename T>
 size_t smem_a(int N) { return sizeof(typename Vec2<T>::t) * (size_t)(N + 2 * 9 * padlen(N)); }
 template <typename T>
@@ -429,6 +684,15 @@ FftPlan make_plan(int N) {
 template <typename T>
 cudaError_t green_setup(int N) {
   cudaError_t e;
+  // FP32 power-of-two grids take the warp-FFT passes; FP64 keeps the shared-memory
+  // Stockham passes (the shuffle stages would execute redundant FP64 products)
+  switch (sizeof(T) == 4 ? N : 0) {
+    case 32: return wgreen_setup<1, T>();
+    case 64: return wgreen_setup<2, T>();
+    case 128: return wgreen_setup<4, T>();
+    case 256: return wgreen_setup<8, T>();
+    default: break;
+  }
   size_t a = smem_a<T>(N), b = smem_b<T>(N, 16), c = smem_c<T>(N, tile_c<T>());
   if ((e = cudaFuncSetAttribute(pass_a<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
   if ((e = cudaFuncSetAttribute(pass_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b))) return e;
@@ -441,6 +705,18 @@ template <typename T>
 cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
   const int N = g.N, H = g.H;
+  bool warp_path = true;
+  switch (sizeof(T) == 4 ? N : 0) {
+    case 32: wgreen_apply<1, T>(x, K4, flgK, y, S, tw, g, st); break;
+    case 64: wgreen_apply<2, T>(x, K4, flgK, y, S, tw, g, st); break;
+    case 128: wgreen_apply<4, T>(x, K4, flgK, y, S, tw, g, st); break;
+    case 256: wgreen_apply<8, T>(x, K4, flgK, y, S, tw, g, st); break;
+    default: warp_path = false;
+  }
+  if (warp_path) {
+    g_kernel_launches += 5;
+    return cudaGetLastError();
+  }
   g.tkb = 16;
   g.tkc = tile_c<T>();
   const int npair = (N + 1) / 2;

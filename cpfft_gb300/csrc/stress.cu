@@ -209,6 +209,7 @@ struct Crystal {
   double tinc, dg;
   double ms[12][6];
   double qc[12][3];
+  double Cms[12][6];  // C ms_i, constant while ms is (the reference forms it per call)
 };
 
 __device__ __forceinline__ double Cv(const double* C, int a, int b) { return __ldg(C + 6 * a + b); }
@@ -243,20 +244,29 @@ __device__ void setup_np1(Crystal& s, const OriRec* rec, const double* D, double
     }
     for (int a = 0; a < 3; a++)
       s.qc[i][a] = RWC[3 * a] * q0[0] + RWC[3 * a + 1] * q0[1] + RWC[3 * a + 2] * q0[2];
+    for (int a = 0; a < 6; a++) {
+      double v = 0.0;
+      for (int j = 0; j < 6; j++) v += Cv(s.C, a, j) * s.ms[i][j];
+      s.Cms[i][a] = v;
+    }
   }
 }
 
-// resolved shear and slip increment of every system (mm10_rs, mm10_slipinc)
+// resolved shear and slip increment of every system (mm10_rs, mm10_slipinc):
+//   si = dg/tt |rs/tt|^(n-1) rs = dg |rs|^(n-1) rs / tt^n,
+// keeping pw = |rs|^(n-1), which the Jacobian reuses (d si / d rs, d si / d tt)
 __device__ __forceinline__ void slips(const Crystal& s, const double* st, double tt, double* rs,
-                                      double* si) {
+                                      double* si, double* pw) {
   const CrysRec& c = *s.cr;
   double itt = 1.0 / tt;
-  double dgt = s.dg * itt;
+  double dgn = s.dg * (c.n_int >= 0 ? ipow(itt, c.n_int + 1) : pow(itt, c.rate_n));
   for (int i = 0; i < 12; i++) {
     double r = st[0] * s.ms[i][0] + st[1] * s.ms[i][1] + st[2] * s.ms[i][2] +
                st[3] * s.ms[i][3] + st[4] * s.ms[i][4] + st[5] * s.ms[i][5];
     rs[i] = r;
-    si[i] = dgt * powabs(r * itt, c.n_int, c.rate_n - 1.0) * r;
+    double p = powabs(r, c.n_int, c.rate_n - 1.0);
+    pw[i] = p;
+    si[i] = dgn * p * r;
   }
 }
 
@@ -292,9 +302,10 @@ __device__ void formR1(const Crystal& s, const double* st, const double* rs, con
 }
 
 // full residual (mm10_formR + mm10_formR2 / mm10_h_voche); returns tau_tilde rate
-__device__ double formR(const Crystal& s, const double* x, double* R, double* rs, double* si) {
+__device__ double formR(const Crystal& s, const double* x, double* R, double* rs, double* si,
+                        double* pw) {
   const CrysRec& c = *s.cr;
-  slips(s, x, x[6], rs, si);
+  slips(s, x, x[6], rs, si, pw);
   formR1(s, x, rs, si, R);
   double ht = hterm(c, x[6]);
   double hp = hpow(c, ht) * sgn1(ht);
@@ -306,27 +317,29 @@ __device__ double formR(const Crystal& s, const double* x, double* R, double* rs
 }
 
 // J11 (mm10_formJ11, src/mm10_b.f:177-257); J is 6x6 row-major inside a 7x7 when ld=7
-template <int ld>
+template <int ld, bool WITH12>
 __device__ void formJ11(const Crystal& s, const double* st, double tt, const double* rs,
-                        const double* si, double* J) {
+                        const double* si, const double* pw, double* J, double* J12,
+                        double itt) {
   const CrysRec& c = *s.cr;
   for (int a = 0; a < 6; a++)
     for (int b = 0; b < 6; b++) J[ld * a + b] = 0.0;
+  // d si / d rs = dg n |rs|^(n-1) / tt^n (mm10_dgdt_voche)
   double fac = s.dg * c.rate_n / (c.n_int >= 0 ? ipow(tt, c.n_int + 1) : pow(tt, c.rate_n));
   double tid = s.tinc * c.iD_v;
   double w[3] = {0, 0, 0};
   for (int i = 0; i < 12; i++) {
-    double dgdt = fac * powabs(rs[i], c.n_int, c.rate_n - 1.0) + tid;
+    double dgdt = fac * pw[i] + tid;
     double sq[6], wv[6];
     symsw(st, s.qc[i], sq);
-    for (int a = 0; a < 6; a++) {
-      double v = 2.0 * sq[a];
-      for (int j = 0; j < 6; j++) v += Cv(s.C, a, j) * s.ms[i][j];
-      wv[a] = v;
-    }
+    for (int a = 0; a < 6; a++) wv[a] = s.Cms[i][a] + 2.0 * sq[a];
     for (int b = 0; b < 6; b++) {
       double t = dgdt * s.ms[i][b];
       for (int a = 0; a < 6; a++) J[ld * a + b] += wv[a] * t;
+    }
+    if (WITH12) {  // the same (C ms + 2 symTW) vector drives J12 (mm10_formJ12)
+      double dgdtt = -c.rate_n * itt * si[i];  // mm10_dgdh_voche
+      for (int a = 0; a < 6; a++) J12[a] += wv[a] * dgdtt;
     }
     double f = rs[i] * tid + si[i];
     for (int a = 0; a < 3; a++) w[a] += f * s.qc[i][a];
@@ -343,28 +356,21 @@ __device__ void formJ11(const Crystal& s, const double* st, double tt, const dou
 
 // full 7x7 Jacobian (mm10_formJ, src/mm10_b.f:901-954)
 __device__ void formJ(const Crystal& s, const double* x, const double* rs, const double* si,
-                      double* J) {
+                      const double* pw, double* J) {
   const CrysRec& c = *s.cr;
   double tt = x[6];
-  formJ11<7>(s, x, tt, rs, si, J);
   double itt = 1.0 / tt;
+  double J12[6] = {0, 0, 0, 0, 0, 0}, et[6] = {0, 0, 0, 0, 0, 0};
+  formJ11<7, true>(s, x, tt, rs, si, pw, J, J12, itt);
   double ht = hterm(c, tt);
   double hp = hpow(c, ht);
   double sh = sgn1(ht);
-  double J12[6] = {0, 0, 0, 0, 0, 0}, et[6] = {0, 0, 0, 0, 0, 0};
   double etau = 0.0;
-  double n_1 = c.rate_n - 2.0;
-  int n2 = c.n_int >= 0 ? c.n_int - 1 : -1;
   for (int i = 0; i < 12; i++) {
-    double sq[6];
-    symsw(x, s.qc[i], sq);
-    double dgdtt = -c.rate_n * itt * si[i];           // mm10_dgdh_voche
-    for (int a = 0; a < 6; a++) {
-      double v = 2.0 * sq[a];
-      for (int j = 0; j < 6; j++) v += Cv(s.C, a, j) * s.ms[i][j];
-      J12[a] += v * dgdtt;
-    }
-    double f = hp * sh * powabs(rs[i], n2, n_1) * rs[i];  // mm10_estress_voche
+    // mm10_estress_voche: |rs|^(n-2) rs = |rs|^(n-1) sign(rs)
+    double r2 = c.n_int >= 0 ? (rs[i] < 0.0 ? -pw[i] : (rs[i] > 0.0 ? pw[i] : 0.0))
+                             : pow(fabs(rs[i]), c.rate_n - 2.0) * rs[i];
+    double f = hp * sh * r2;
     for (int a = 0; a < 6; a++) et[a] += f * s.ms[i][a];
     double asi = fabs(si[i]);                          // mm10_ehard_voche
     double ta = c.voce_m * (-c.inv_tau_v) * asi / fabs(ht);
@@ -392,7 +398,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
                       bool& haveJ, int& iters, int& piters, double& ttrate) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
-  double x[7], rs[12], si[12];
+  double x[7], rs[12], si[12], pw[12];
   for (int i = 0; i < 6; i++) x[i] = stress[i];
   x[6] = tt;
   double inR1;
@@ -412,7 +418,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     double x2 = x[6] + cs * cu.nttr * dtinc;
     double x1[6], R1[6];
     for (int i = 0; i < 6; i++) x1[i] = x[i];
-    slips(cu, x1, x2, rs, si);
+    slips(cu, x1, x2, rs, si, pw);
     formR1(cu, x1, rs, si, R1);
     double dot = 0;
     for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
@@ -421,7 +427,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     int it = 0;
     while (nR1 > c.atol1 && nR1 / inR1 > c.rtol1) {
       double J[36], mJ[36], dx[6];
-      formJ11<6>(cu, x1, x2, rs, si, J);
+      formJ11<6, false>(cu, x1, x2, rs, si, pw, J, nullptr, 0.0);
       for (int a = 0; a < 36; a++) mJ[a] = -J[a];
       for (int a = 0; a < 6; a++) dx[a] = R1[a];
       lu_solve1<6>(mJ, dx);
@@ -436,7 +442,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
       for (int ls = 0;; ls++) {
         double xn[6];
         for (int a = 0; a < 6; a++) xn[a] = x1[a] + alpha * dx[a];
-        slips(cu, xn, x2, rs, si);
+        slips(cu, xn, x2, rs, si, pw);
         formR1(cu, xn, rs, si, R1);
         dot = 0;
         for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
@@ -457,13 +463,13 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
   // ---- update
   int it = 0;
   double R[7];
-  ttrate = formR(cu, x, R, rs, si);
+  ttrate = formR(cu, x, R, rs, si, pw);
   double dot = 0;
   for (int a = 0; a < 7; a++) dot += R[a] * R[a];
   double nR = sqrt(dot), inR = nR;
   if (inR == 0.0) inR = inR1;
   while ((nR > c.atol && nR / inR > c.rtol) || it < 1) {
-    formJ(cu, x, rs, si, Jlast);
+    formJ(cu, x, rs, si, pw, Jlast);
     haveJ = true;
     double mJ[49], dx[7];
     for (int a = 0; a < 49; a++) mJ[a] = -Jlast[a];
@@ -480,7 +486,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     for (int ls = 0;; ls++) {
       double xn[7];
       for (int a = 0; a < 7; a++) xn[a] = x[a] + alpha * dx[a];
-      ttrate = formR(cu, xn, R, rs, si);
+      ttrate = formR(cu, xn, R, rs, si, pw);
       dot = 0;
       for (int a = 0; a < 7; a++) dot += R[a] * R[a];
       nR = sqrt(dot);
@@ -688,8 +694,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
   if (iter0 || no_load) {
     for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
     if (!no_load) {
-      double rs[12], si[12], R1[6];
-      slips(s, stress, tt, rs, si);
+      double rs[12], si[12], pw[12], R1[6];
+      slips(s, stress, tt, rs, si, pw);
       formR1(s, stress, rs, si, R1);
       for (int i = 0; i < 6; i++) stress[i] -= R1[i];
     }
@@ -797,8 +803,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) tr[3 * i + j] = nRp[3 * j + i];
     rt2rvw(tr, RW);
-    double rs[12], si[12], wb[3] = {0, 0, 0};
-    slips(s, stress, tt, rs, si);
+    double rs[12], si[12], pw[12], wb[3] = {0, 0, 0};
+    slips(s, stress, tt, rs, si, pw);
     double tid = s.tinc * cr->iD_v;
     for (int i = 0; i < 12; i++) {
       double q0[3], qs[3];

@@ -72,8 +72,10 @@ def test_stress_update_parity(gpulib, oracle, exact):
 
 
 @pytest.mark.parametrize("N,gmap", [(5, 0), (7, 0), (8, 1), (9, 0), (12, 1), (15, 0), (16, 1),
-                                    (16, 0), (32, 1)])
+                                    (16, 0), (32, 1), (32, 0), (64, 1), (128, 1)])
 def test_green_parity(gpulib, oracle, N, gmap):
+    """Sizes 32-256 that are powers of two run the warp-FFT passes, the others the
+    shared-memory Stockham passes."""
     r, s, o = make_pair(gpulib, oracle, N, gmap=gmap)
     try:
         Fn, Fn1 = random_F(N, 1e-3, 2)
