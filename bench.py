@@ -5,7 +5,7 @@ crystal-plasticity hot path at 128^3 (the workload the metric is quoted on).
 Workload: 128^3 voxels, 256 periodic-Voronoi grains (seed 3) with Haar-random
 orientations, FCC mm10 Voce material, plane-strain compression at 1e-3 per load step
 (F_zz prescribed, F_yy = 1, shear F held at zero, other P zero), local Newton 1e-10,
-global NR 1e-6, CG 1e-10.  Synthetic inputs (no dataset).  A "step" is one whole load
+global NR 1e-5 (--tol-nr), CG 1e-10.  Synthetic inputs (no dataset).  A "step" is one whole load
 step of FFT_nr3 (Newton-Krylov to convergence, the P_bar loop with its homogenised
 tangents, and the state roll-over) through the C-ABI's resident entry point.
 
@@ -32,7 +32,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
-# per-voxel algorithmic work (the design doc roofline section)
+# per-voxel algorithmic work: minimal HBM bytes of one launch per voxel
 BYTES_GREEN32 = 540.0          # FP32 Krylov matvec: x 36 + K4 324 + y 36 + 2 half-spectrum trips 144
 BYTES_GREEN64 = 1080.0         # FP64 matvec
 BYTES_STRESS = 1264.0          # stress update: F, F1, state n, P, A, state n+1
@@ -254,6 +254,8 @@ def gb300_arm(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    # marks the timed region for `ncu --profile-from-start off`; no effect otherwise
+    torch.cuda.profiler.start()
     stats = []
     t_e2e = 0.0
     for _ in range(args.steps):
@@ -266,6 +268,7 @@ def gb300_arm(args):
         t_e2e += time.perf_counter() - t0
         stats.append(st)
     torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (test infrastructure only).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
-module, and only as the checker or the timed CPU stand-in.  The product path never
+module, and only as the parity reference or the timed CPU stand-in.  The product path never
 touches it.
 """
 import ctypes
