@@ -275,17 +275,8 @@ def gb300_arm(args):
     t_dev = sum(s["t_device"] for s in stats)
     su = sum(s["stress_updates"] for s in stats)
     units = float(N3 * su)
-    tmax, temax = t_dev, t_e2e
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_dev, t_e2e, units], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        tot = t.clone()
-        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-        tmax, temax, units_all = mx[0].item(), mx[1].item(), tot[2].item()
-    else:
-        units_all = units
+    from cpfft_gb300 import replicas
+    tmax, temax, units_all = replicas.reduce_timings(t_dev, t_e2e, units, device="cuda")
     if rank != 0:
         solver.close()
         return 0
