@@ -315,8 +315,8 @@ def gb300_arm(args):
                 "algorithmic_bytes_per_launch": BYTES_STRESS * N3, "avg_launch_ms": per * 1e3}
     kernel_split = {"stress_s": tsk, "green64_s": tg64, "green32_s": tg32,
                     "n_green64": ng64, "n_green32": ng32, "stress_passes": su}
-    cg_iters = sum(s["cg_iters"] for s in stats)
-    hint = (su / len(stats), (cg_iters + ng64) / len(stats))
+    # G(K:x) applies per step, FP32 and FP64 together (each FP32 CG iteration is one)
+    hint = (su / len(stats), (ng32 + ng64) / len(stats))
     cpu = None
     if world == 1 and not args.no_cpu:
         res = cpu_sample(r, load, workload_counts(), os.cpu_count(),
@@ -345,13 +345,14 @@ def gb300_arm(args):
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "roofline": roof,
         "kernel_time_split": kernel_split,
-        "per_step_counts": {"stress_passes": hint[0], "fp64_equiv_matvecs": hint[1],
+        "per_step_counts": {"stress_passes": hint[0], "matvecs": hint[1],
                             "newton": [s["newton_iters"] for s in stats],
                             "nbc": [s["nbc_iters"] for s in stats],
                             "cg_iters": [s["cg_iters"] for s in stats],
                             "res_equil": [s["res_equil"] for s in stats],
                             "res_fft": [s["res_fft"] for s in stats],
-                            "local_iters_per_voxel_pass": sum(s["local_iters"] for s in stats) / (N3 * su)},
+                            "local_iters_per_voxel_pass": sum(s["local_iters"] for s in stats) / (N3 * su),
+                            "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in stats) / (N3 * su)},
         "fp64_peak_tflops": fp64_peak,
         "clocks": clk,
         "cpu_baseline": cpu,

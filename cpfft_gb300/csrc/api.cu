@@ -175,6 +175,8 @@ struct Ctx {
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
   double *r = nullptr, *p = nullptr, *Ap = nullptr, *w = nullptr, *io = nullptr;
   double* w2 = nullptr;  // mixed precision: FP64 copy of an inner correction
+  double* th_x = nullptr;  // mixed precision: tangent_homo's 9 solutions of the last call
+  bool th_valid = false;
   bool log = false;      // CPFFT_LOG=1: the reference's residual reports on stderr
   double* hist[2] = {nullptr, nullptr};
   int hn = 0;  // index of the history at n
@@ -257,7 +259,7 @@ int dalloc(Ptr& p, size_t bytes) {
 
 void free_ctx(Ctx* c) {
   if (!c) return;
-  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2,
+  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats};
   for (void* q : ptrs)
@@ -312,6 +314,19 @@ int matvec32(Ctx* c, const float* x, float* y) {
   TRY(cuda_check(green_apply<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st), "green_apply fp32"));
   return kt_stop(c);
 }
+// y = G(K4f : x) and sc[SC_PAP] = x . y with alpha = rr / (x . y): the product is summed
+// inside the last FFT pass where that pass supports it, else by a separate reduction
+int matvec32_alpha(Ctx* c, const float* x, float* y) {
+  c->f32_matvecs++;
+  kt_start(c, KT_G32);
+  int np = 0;
+  TRY(cuda_check(green_apply_dot<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st, c->part, &np),
+                 "green_apply fp32"));
+  TRY(kt_stop(c));
+  if (np) CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
+  else CK(dev_dot_f(x, y, 9 * c->N3, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+  return 0;
+}
 
 // fftPcg (src/FFT_nr3.f:214-360), plain FP64: CG from x = 0 with the stop test
 // ||r|| <= tol*||b|| .or. ||r|| <= tol and at most 1000 iterations
@@ -350,12 +365,12 @@ int cg64(Ctx* c, const double* b, double* x, double tol, int* iters) {
 
 // Mixed precision: FP32 Green/FFT/CG inner solves corrected by an FP64 outer residual
 // (iterative refinement).  Same stop test on the FP64 residual as cg64.
-int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
+int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
   const long long n = 9 * c->N3;
   const int maxIter = 2000;     // FP32 iterations (the FP64 path's cap is 1000)
   const double delta = 1.0e-2;  // reliable-update threshold
   *iters = 0;
-  CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
+  if (!use_x0) CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
   double n2b;
   TRY(dnrm2(c, b, &n2b));
   if (!(tol > 2.220446049250313e-16 && tol < 1.0)) return CPFFT_ERR_CG_TOL;
@@ -374,8 +389,21 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
   // residual.  The FP64 projection G keeps x in the range of G (compatible, zero-mean
   // fields) where every FP64 CG iterate lives: FP32 rounding leaks into the kernel of G,
   // which the residual cannot see.
-  CK(cudaMemcpyAsync(c->w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-  double rn = n2b, scale = 1.0 / n2b, maxr = n2b;
+  double rn = n2b;
+  if (use_x0) {
+    // start from the caller's x (kept in the range of G): r = b - G(K4 : x) in FP64
+    TRY(matvec64(c, x, c->Ap, 1));
+    CK(dev_sub(c->w, b, c->Ap, n, c->st));
+    TRY(dnrm2(c, c->w, &rn));
+    if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    if (rn <= tolb || rn <= tol) {
+      c->cg_solves++;
+      return 0;
+    }
+  } else {
+    CK(cudaMemcpyAsync(c->w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  }
+  double scale = 1.0 / rn, maxr = rn;
   CK(dev_to_f32(c->rf, c->w, scale, n, c->st));
   CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
   CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
@@ -385,8 +413,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
   int it = 0;
   bool converged = false;
   for (;;) {
-    TRY(matvec32(c, c->pf, c->Apf));
-    CK(dev_dot_f(c->pf, c->Apf, n, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+    TRY(matvec32_alpha(c, c->pf, c->Apf));
     CK(dev_cg_xr<float>(c->xf, c->rf, c->pf, c->Apf, n, c->part, c->sc, c->st));
     it++;
     double rr;
@@ -429,10 +456,12 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters) {
 }
 
 int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
-  return c->prec == CPFFT_PREC_MIXED ? cg_mixed(c, b, x, tol, iters) : cg64(c, b, x, tol, iters);
+  return c->prec == CPFFT_PREC_MIXED ? cg_mixed(c, b, x, tol, iters, false)
+                                     : cg64(c, b, x, tol, iters);
 }
 
-int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails) {
+int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
+           long long* predict_iters = nullptr) {
   StressArgs a;
   a.Fn = c->Fn;
   a.Fn1 = c->Fn1;
@@ -459,13 +488,20 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails) {
   TRY(sync(c));
   if (local_iters) *local_iters = (long long)c->h_stats[0];
   if (fails) *fails = (int)c->h_stats[1];
+  if (predict_iters) *predict_iters = (long long)c->h_stats[2];
   return 0;
 }
 
-// tangent_homo (src/tangent_homo.f:11-73): 9 CG solves, C_homo(i,j) stored at 9*j+i
+// tangent_homo (src/tangent_homo.f:11-73): 9 CG solves, C_homo(i,j) stored at 9*j+i.
+// In mixed precision each solve starts from the fluctuation field the same column
+// converged to in the previous call (the tangent changes little between calls); the
+// stop test, ||r|| <= tol ||b||, is unchanged.  The plain FP64 path starts from zero as
+// the reference does.
 int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
   const long long N3 = c->N3, n = 9 * N3;
   *its_total = 0;
+  const bool warm = c->prec == CPFFT_PREC_MIXED;
+  if (warm && !c->th_x) TRY(dalloc(c->th_x, 9 * n * sizeof(double)));
   for (int i = 0; i < 9; i++) {
     for (int j = 0; j < 9; j++)
       CK(cudaMemcpyAsync(c->io + j * N3, c->K4 + (9 * j + i) * N3, N3 * sizeof(double),
@@ -473,7 +509,14 @@ int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
     TRY(matvec64(c, c->io, c->b, 0));
     CK(dev_scale(c->b, -1.0, n, c->st));
     int its = 0;
-    TRY(cg(c, c->b, c->io, tolPCG, &its));
+    if (warm) {
+      if (c->th_valid)
+        CK(cudaMemcpyAsync(c->io, c->th_x + i * n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+      TRY(cg_mixed(c, c->b, c->io, tolPCG, &its, c->th_valid));
+      CK(cudaMemcpyAsync(c->th_x + i * n, c->io, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+    } else {
+      TRY(cg(c, c->b, c->io, tolPCG, &its));
+    }
     *its_total += its;
     CK(dev_add_const(c->io + i * N3, 1.0, N3, c->st));
     for (int j = 0; j < 9; j++) {
@@ -483,6 +526,7 @@ int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
       C_homo[9 * j + i] = s / (double)N3;
     }
   }
+  if (warm) c->th_valid = true;
   return 0;
 }
 
@@ -660,7 +704,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
       (rc = dalloc(c->oris, oris.size() * sizeof(OriRec))) ||
       (rc = dalloc(c->cryss, ncrystals * sizeof(CrysRec))) ||
       (rc = dalloc(c->S, (size_t)9 * N * N * c->g.H * sizeof(double2))) ||
-      (rc = dalloc(c->tw, N * sizeof(double2))) || (rc = dalloc(c->part, 9 * NPART * sizeof(double))) ||
+      (rc = dalloc(c->tw, N * sizeof(double2))) || (rc = dalloc(c->part, (size_t)std::max<long long>(9 * NPART, (long long)N * N) * sizeof(double))) ||
       (rc = dalloc(c->sc, SC_COUNT * sizeof(double))) ||
       (rc = dalloc(c->stats, 4 * sizeof(unsigned long long))))
     return fail(rc);
@@ -858,8 +902,10 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       a = clk::now();
       long long li;
       int fails;
-      TRY(stress(c, step, iiter_EBC, &li, &fails));
+      long long pi = 0;
+      TRY(stress(c, step, iiter_EBC, &li, &fails, &pi));
       ts += sec(a);
+      S.predict_iters += pi;
       S.local_iters += li;
       S.local_fallbacks += fails;
       S.stress_updates++;
@@ -887,8 +933,10 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     a = clk::now();
     long long li;
     int fails;
-    TRY(stress(c, step, iiter_EBC, &li, &fails));
+    long long pi = 0;
+    TRY(stress(c, step, iiter_EBC, &li, &fails, &pi));
     ts += sec(a);
+    S.predict_iters += pi;
     S.local_iters += li;
     S.local_fallbacks += fails;
     S.stress_updates++;

@@ -574,10 +574,14 @@ __global__ void __launch_bounds__(256) wpass_c(typename Vec2<T>::t* __restrict__
   }
 }
 
+// dotx != nullptr: also one partial sum per block of dotx . y over the voxels the block
+// writes (the CG product p . Ap without re-reading Ap), into part[blockIdx.x]
 template <int M, typename T>
 __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __restrict__ S,
                                                T* __restrict__ y, GridDesc g,
-                                               const typename Vec2<T>::t* __restrict__ twg) {
+                                               const typename Vec2<T>::t* __restrict__ twg,
+                                               const T* __restrict__ dotx,
+                                               double* __restrict__ part) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
   const int Lp = padlen(N);
@@ -604,12 +608,27 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
   const int w = threadIdx.x >> 5;
   if (w < 9) warp_column<M, T, true>(col + w * Lp, tw);
   __syncthreads();
+  T dsum = 0;
   for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
     int l = t / (9 * N), rem = t - l * 9 * N;
     int i = rem / N, a = rem - i * N;
     T2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
     long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
-    y[i * N3 + v] = l ? z.y : z.x;
+    const T yv = l ? z.y : z.x;
+    y[i * N3 + v] = yv;
+    if (dotx) dsum += dotx[i * N3 + v] * yv;
+  }
+  if (dotx) {  // block sum (9 warps), fixed order
+    __shared__ double wsum[9];
+    double d = (double)dsum;
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = 0.0;
+      for (int k = 0; k < 9; k++) b += wsum[k];
+      part[blockIdx.x] = b;
+    }
   }
 }
 
@@ -636,7 +655,8 @@ cudaError_t wgreen_setup() {
 
 template <int M, typename T>
 void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
-                  const typename Vec2<T>::t* tw, const GridDesc& g, cudaStream_t st) {
+                  const typename Vec2<T>::t* tw, const GridDesc& g, cudaStream_t st,
+                  double* part) {
   constexpr int N = 32 * M, H = N / 2 + 1, TC = wtile_c<T>();
   wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(x, K4, flgK, S, g, tw);
   dim3 gb((H + WTILE_B - 1) / WTILE_B, N, 9);
@@ -644,7 +664,8 @@ void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* 
   dim3 gc((H + TC - 1) / TC, N);
   wpass_c<M, T, TC><<<gc, 256, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
   wpass_b<M, T, WTILE_B><<<gb, 32 * WTILE_B, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
-  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(S, y, g, tw);
+  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(S, y, g, tw, part ? x : nullptr,
+                                                           part);
 }
 
 template <typename T>
@@ -702,18 +723,21 @@ cudaError_t green_setup(int N) {
 }
 
 template <typename T>
-cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
-                        const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
+cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                            const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st,
+                            double* part, int* nparts) {
   const int N = g.N, H = g.H;
   bool warp_path = true;
+  if (nparts) *nparts = 0;
   switch (sizeof(T) == 4 ? N : 0) {
-    case 32: wgreen_apply<1, T>(x, K4, flgK, y, S, tw, g, st); break;
-    case 64: wgreen_apply<2, T>(x, K4, flgK, y, S, tw, g, st); break;
-    case 128: wgreen_apply<4, T>(x, K4, flgK, y, S, tw, g, st); break;
-    case 256: wgreen_apply<8, T>(x, K4, flgK, y, S, tw, g, st); break;
+    case 32: wgreen_apply<1, T>(x, K4, flgK, y, S, tw, g, st, part); break;
+    case 64: wgreen_apply<2, T>(x, K4, flgK, y, S, tw, g, st, part); break;
+    case 128: wgreen_apply<4, T>(x, K4, flgK, y, S, tw, g, st, part); break;
+    case 256: wgreen_apply<8, T>(x, K4, flgK, y, S, tw, g, st, part); break;
     default: warp_path = false;
   }
   if (warp_path) {
+    if (part && nparts) *nparts = (N / 2) * N;
     g_kernel_launches += 5;
     return cudaGetLastError();
   }
@@ -731,9 +755,17 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                        const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
+  return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr);
+}
+
 template cudaError_t green_setup<double>(int);
 template cudaError_t green_setup<float>(int);
 template cudaError_t green_apply<double>(const double*, const double*, int, double*, double2*,
                                          const double2*, GridDesc, cudaStream_t);
 template cudaError_t green_apply<float>(const float*, const float*, int, float*, float2*,
                                         const float2*, GridDesc, cudaStream_t);
+template cudaError_t green_apply_dot<float>(const float*, const float*, int, float*, float2*,
+                                            const float2*, GridDesc, cudaStream_t, double*, int*);

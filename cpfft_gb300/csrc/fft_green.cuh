@@ -29,5 +29,12 @@ FftPlan make_plan(int N);
 template <typename T>
 cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st);
+// the same, and with part != nullptr also the partial sums of x . y: *nparts partials
+// in part (the warp-FFT sizes), or *nparts = 0 when this size does not fuse the product
+// (the caller then reduces x . y itself)
+template <typename T>
+cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
+                            const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st,
+                            double* part, int* nparts);
 template <typename T>
 cudaError_t green_setup(int N);

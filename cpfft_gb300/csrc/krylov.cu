@@ -72,6 +72,56 @@ __global__ void __launch_bounds__(RB) k_cg_xr(T* __restrict__ x, T* __restrict__
   if (threadIdx.x == 0) part[blockIdx.x] = sb;
 }
 
+// FP32 form with 16-byte vector accesses (n % 4 elements handled by a scalar tail)
+__global__ void __launch_bounds__(RB) k_cg_xr4(float* __restrict__ x, float* __restrict__ r,
+                                               const float* __restrict__ p,
+                                               const float* __restrict__ Ap, long long n,
+                                               const double* __restrict__ sc,
+                                               double* __restrict__ part) {
+  const float alpha = (float)sc[SC_ALPHA];
+  const long long n4 = n >> 2, stride = (long long)gridDim.x * RB;
+  float4* x4 = reinterpret_cast<float4*>(x);
+  float4* r4 = reinterpret_cast<float4*>(r);
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  const float4* a4 = reinterpret_cast<const float4*>(Ap);
+  float s = 0.f;
+  const long long t0 = (long long)blockIdx.x * RB + threadIdx.x;
+  for (long long i = t0; i < n4; i += stride) {
+    float4 xv = x4[i], pv = p4[i], rv = r4[i], av = a4[i];
+    xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+    rv.x -= alpha * av.x; rv.y -= alpha * av.y; rv.z -= alpha * av.z; rv.w -= alpha * av.w;
+    x4[i] = xv;
+    r4[i] = rv;
+    s += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+  }
+  for (long long i = 4 * n4 + t0; i < n; i += stride) {
+    x[i] = x[i] + alpha * p[i];
+    float ri = r[i] - alpha * Ap[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  double sb = block_sum((double)s);
+  if (threadIdx.x == 0) part[blockIdx.x] = sb;
+}
+
+__global__ void k_cg_p4(float* __restrict__ p, const float* __restrict__ r, long long n,
+                        double* __restrict__ sc) {
+  const float beta = (float)sc[SC_BETA];
+  const long long n4 = n >> 2, stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float4* p4 = reinterpret_cast<float4*>(p);
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+  for (long long i = t0; i < n4; i += stride) {
+    float4 pv = p4[i], rv = r4[i];
+    pv.x = rv.x + beta * pv.x; pv.y = rv.y + beta * pv.y;
+    pv.z = rv.z + beta * pv.z; pv.w = rv.w + beta * pv.w;
+    p4[i] = pv;
+  }
+  for (long long i = 4 * n4 + t0; i < n; i += stride) p[i] = r[i] + beta * p[i];
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc[SC_RR] = sc[SC_RRNEW];
+}
+
 // p = r + beta p ; rr <- rr_new
 template <typename T>
 __global__ void k_cg_p(T* __restrict__ p, const T* __restrict__ r, long long n,
@@ -171,13 +221,24 @@ cudaError_t dev_dot_f(const float* a, const float* b, long long n, double* part,
 template <typename T>
 cudaError_t dev_cg_xr(T* x, T* r, const T* p, const T* Ap, long long n, double* part, double* sc,
                       cudaStream_t st) {
-  k_cg_xr<T><<<NPART, RB, 0, st>>>(x, r, p, Ap, n, sc, part);
+  if (sizeof(T) == 4)
+    k_cg_xr4<<<NPART, RB, 0, st>>>((float*)x, (float*)r, (const float*)p, (const float*)Ap, n,
+                                   sc, part);
+  else
+    k_cg_xr<T><<<NPART, RB, 0, st>>>(x, r, p, Ap, n, sc, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, SC_RRNEW, OP_BETA);
   return counted(2);
 }
 template <typename T>
 cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st) {
-  k_cg_p<T><<<grid_for(n, 256), 256, 0, st>>>(p, r, n, sc);
+  if (sizeof(T) == 4)
+    k_cg_p4<<<grid_for(n / 4 + 1, 256), 256, 0, st>>>((float*)p, (const float*)r, n, sc);
+  else
+    k_cg_p<T><<<grid_for(n, 256), 256, 0, st>>>(p, r, n, sc);
+  return counted(1);
+}
+cudaError_t dev_final(double* part, int np, double* sc, int slot, int op, cudaStream_t st) {
+  k_final<<<1, 1024, 0, st>>>(part, np, sc, slot, op);
   return counted(1);
 }
 template cudaError_t dev_cg_xr<double>(double*, double*, const double*, const double*, long long,

@@ -21,6 +21,8 @@ cudaError_t dev_cg_xr(T* x, T* r, const T* p, const T* Ap, long long n, double* 
                       cudaStream_t st);
 template <typename T>
 cudaError_t dev_cg_p(T* p, const T* r, long long n, double* sc, cudaStream_t st);
+// sc[slot] = sum of np partials (with the op's CG follow-up)
+cudaError_t dev_final(double* part, int np, double* sc, int slot, int op, cudaStream_t st);
 cudaError_t dev_axpy(double* y, const double* x, double a, long long n, cudaStream_t st);
 cudaError_t dev_scale(double* y, double a, long long n, cudaStream_t st);
 cudaError_t dev_sub(double* y, const double* a, const double* b, long long n, cudaStream_t st);

@@ -96,6 +96,7 @@ typedef struct cpfft_stats {
     long long n_green64;        /* FP64 Green applies                                      */
     long long n_green32;        /* FP32 Green applies                                      */
     long long kernel_launches;  /* kernels this call launched                              */
+    long long predict_iters;    /* local predictor (6x6) Newton iterations, summed         */
 } cpfft_stats;
 
 /*
