@@ -77,6 +77,7 @@ class Stats(ctypes.Structure):
 # every exported symbol and its signature
 _D, _I, _P = ctypes.c_double, ctypes.c_int, ctypes.POINTER
 _DP, _IP = _P(_D), _P(_I)
+_FP, _LL = _P(ctypes.c_float), ctypes.c_longlong
 SIGNATURES = {
     "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
     "cpfft_set_mode": (_I, [_I, _I]),
@@ -95,7 +96,65 @@ SIGNATURES = {
     "cpfft_measure_fp64_peak": (_I, [_DP]),
     "cpfft_green_apply_noalloc": (_I, [_I, _I, ctypes.c_void_p, ctypes.c_void_p, _I,
                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "cpfft_mlp_init": (_I, [_I]),
+    "cpfft_mlp_set_params": (_I, [_FP, _FP]),
+    "cpfft_mlp_get_params": (_I, [_FP, _FP]),
+    "cpfft_mlp_forward": (_I, [_FP, _LL, _FP]),
+    "cpfft_mlp_loss_grad": (_I, [_FP, _FP, _LL, _FP, _FP]),
+    "cpfft_mlp_train": (_I, [_FP, _FP, _LL, _I, _I, ctypes.c_float, _I, _FP]),
 }
+
+MLP_NIN, MLP_NOUT, MLP_PARAMS, MLP_NORM = 20, 7, 22800, 54
+
+
+def _fp(a):
+    if a is None:
+        return None
+    if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("expected a C-contiguous float32 array")
+    return a.ctypes.data_as(_FP)
+
+
+class Mlp:
+    """The learned initial guess's network on the GPU (one per process)."""
+
+    def __init__(self, seed=0):
+        _check(load_library().cpfft_mlp_init(int(seed)), "mlp_init")
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        n = np.zeros(MLP_NORM, np.float32)
+        _check(load_library().cpfft_mlp_get_params(_fp(p), _fp(n)), "mlp_get_params")
+        return p, n
+
+    def set_params(self, params=None, norm=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        _check(load_library().cpfft_mlp_set_params(_fp(p), _fp(n)), "mlp_set_params")
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], MLP_NOUT), np.float32)
+        _check(load_library().cpfft_mlp_forward(_fp(X), X.shape[0], _fp(Y)), "mlp_forward")
+        return Y
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = ctypes.c_float(0.0)
+        _check(load_library().cpfft_mlp_loss_grad(_fp(X), _fp(T), X.shape[0], _fp(g),
+                                                   ctypes.byref(loss)), "mlp_loss_grad")
+        return loss.value, g
+
+    def train(self, X, T, epochs, batch_tiles=16, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        loss = ctypes.c_float(0.0)
+        _check(load_library().cpfft_mlp_train(_fp(X), _fp(T), X.shape[0], int(epochs),
+                                               int(batch_tiles), float(lr), int(seed),
+                                               ctypes.byref(loss)), "mlp_train")
+        return loss.value
 
 
 def measure_fp64_peak():

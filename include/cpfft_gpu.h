@@ -46,7 +46,7 @@ extern "C" {
 #define CPFFT_G_REF_SHIFT  0   /* bit-faithful to the reference: q = ((k-Nhalf) mod N)+1-Nhalf */
 #define CPFFT_G_CENTERED   1   /* signed wavenumber (identical to REF_SHIFT for odd N)         */
 
-/* Krylov / Green precision (north-star "precision" pattern). */
+/* Krylov / Green precision: plain FP64, or FP32 inner iterations under an FP64 residual. */
 #define CPFFT_PREC_FP64    0   /* plain: every operator in FP64                                */
 #define CPFFT_PREC_MIXED   1   /* FP32 Green/FFT/CG inner iterations, FP64 outer refinement    */
 
@@ -116,8 +116,8 @@ typedef struct cpfft_stats {
 int cpfft_init(int N, const int* matList, const double* kocks_deg,
                const cpfft_crystal* props, int ncrystals, double tstep, int g_mapping);
 
-/* Select the Krylov precision (CPFFT_PREC_*) and the learned warm start (0/1).
- * No counterpart in the reference (spec precision and learned patterns). */
+/* Select the Krylov precision (CPFFT_PREC_*) and the learned initial guess of the local
+ * solve (0/1).  Extensions with no counterpart in the reference. */
 int cpfft_set_mode(int precision, int warm_start);
 
 /*
@@ -212,6 +212,30 @@ const char* cpfft_last_error(void);
 /* Diagnostic, no counterpart in the reference: measured FP64 FMA rate of the current
  * GPU in TFLOP/s (the roofline denominator of the FP64-bound kernels). */
 int cpfft_measure_fp64_peak(double* tflops);
+
+/* ---- Learned initial guess of the local mm10 solve (extension; no reference
+ * counterpart).  A 20-128-128-7 SiLU network (BF16 weights, FP32 accumulation, tcgen05
+ * tensor cores) maps a voxel's features -- lattice quaternion (4), rotated strain
+ * increment D (6), sigma_n (6), tau_n, tau rate_n, cos(D, D_n), |D| -- to the converged
+ * increments sigma - sigma_n (6) and tau - tau_n.  Parameters: CPFFT_MLP_PARAMS floats
+ * (W1 [128][32], b1, W2 [128][128], b2, W3 [16][128], b3; padded rows and columns zero);
+ * normalisation: CPFFT_MLP_NORM floats (feature means, inverse deviations, target means,
+ * target deviations).  X is (n, 20) and Y, T are (n, 7), row-major FP32 host arrays. */
+#define CPFFT_MLP_NIN 20
+#define CPFFT_MLP_NOUT 7
+#define CPFFT_MLP_PARAMS 22800
+#define CPFFT_MLP_NORM 54
+
+int cpfft_mlp_init(int seed);                                  /* Glorot init, identity norm */
+int cpfft_mlp_set_params(const float* params, const float* norm);  /* either may be NULL */
+int cpfft_mlp_get_params(float* params, float* norm);
+int cpfft_mlp_forward(const float* X, long long n, float* Y);
+/* mean squared error (normalised outputs) of one batch and its gradient, no update */
+int cpfft_mlp_loss_grad(const float* X, const float* T, long long n, float* grad, float* loss);
+/* Adam over (X, T): `epochs` shuffled passes, minibatches of batch_tiles x 128 samples;
+ * sets the normalisation from the data; *loss = mean loss of the last epoch */
+int cpfft_mlp_train(const float* X, const float* T, long long n, int epochs, int batch_tiles,
+                    float lr, int seed, float* loss);
 
 #ifdef __cplusplus
 }
