@@ -67,7 +67,7 @@ class Stats(ctypes.Structure):
         ("t_stress_kernel", ctypes.c_double), ("t_green64", ctypes.c_double),
         ("t_green32", ctypes.c_double), ("n_green64", ctypes.c_longlong),
         ("n_green32", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
-        ("predict_iters", ctypes.c_longlong),
+        ("predict_iters", ctypes.c_longlong), ("guess_rejected", ctypes.c_longlong),
     ]
 
     def as_dict(self):
@@ -102,6 +102,8 @@ SIGNATURES = {
     "cpfft_mlp_forward": (_I, [_FP, _LL, _FP]),
     "cpfft_mlp_loss_grad": (_I, [_FP, _FP, _LL, _FP, _FP]),
     "cpfft_mlp_train": (_I, [_FP, _FP, _LL, _I, _I, ctypes.c_float, _I, _FP]),
+    "cpfft_learn_log": (_I, [_LL, _I, _I]),
+    "cpfft_learn_fetch": (_I, [_FP, _FP, _P(_LL)]),
 }
 
 MLP_NIN, MLP_NOUT, MLP_PARAMS, MLP_NORM = 20, 7, 22800, 54
@@ -225,7 +227,24 @@ class Solver:
         load_library().cpfft_finalize()
 
     def set_mode(self, precision, warm_start=0):
-        _check(load_library().cpfft_set_mode(precision, warm_start), "cpfft_set_mode")
+        _check(load_library().cpfft_set_mode(precision, int(warm_start)), "cpfft_set_mode")
+
+    # --- learned initial guess of the local solve --------------------------------------
+    def learn_log(self, capacity, stride=1, phase=0):
+        """Log (features, converged increments) of the plain local solves of every
+        stride-th voxel into device buffers of `capacity` pairs (0 stops logging)."""
+        _check(load_library().cpfft_learn_log(int(capacity), int(stride), int(phase)),
+               "cpfft_learn_log")
+        self._log_cap = int(capacity)
+
+    def learn_fetch(self):
+        cap = getattr(self, "_log_cap", 0)
+        X = np.zeros((cap, MLP_NIN), np.float32)
+        T = np.zeros((cap, MLP_NOUT), np.float32)
+        n = ctypes.c_longlong(0)
+        _check(load_library().cpfft_learn_fetch(_fp(X), _fp(T), ctypes.byref(n)),
+               "cpfft_learn_fetch")
+        return X[:n.value], T[:n.value]
 
     # --- mirror of the reference routines ------------------------------------------
     def drive_eps_sig(self, step, it, Fn=None, Fn1=None, want_P=True, want_K4=False):

@@ -12,6 +12,11 @@
 
 #include "common.cuh"
 #include "fft_green.cuh"
+#include "mlp.cuh"
+
+// the learned initial guess's device weights and error check (mlp.cu)
+bool mlp_device_weights(mlp::Weights* w, int** err);
+int mlp_check_error();
 #include "krylov.cuh"
 
 static char g_err[512] = "";
@@ -120,6 +125,7 @@ void orientation_record(const double C0[36], const double bb[12][3], const doubl
     o.qs[3 * s + 1] = 0.5 * (A[0][2] - A[2][0]);
     o.qs[3 * s + 2] = 0.5 * (A[0][1] - A[1][0]);
   }
+  for (int i = 0; i < 9; i++) o.g[i] = tr[i];
   double Rs[36], tmp[36];
   for (int a = 0; a < 6; a++)
     for (int b = 0; b < 6; b++) {
@@ -177,6 +183,11 @@ struct Ctx {
   double* w2 = nullptr;  // mixed precision: FP64 copy of an inner correction
   double* th_x = nullptr;  // mixed precision: tangent_homo's 9 solutions of the last call
   bool th_valid = false;
+  // logging of (features, converged increments) pairs for the learned initial guess
+  float *log_X = nullptr, *log_T = nullptr;
+  unsigned long long* log_n = nullptr;
+  long long log_cap = 0;
+  int log_stride = 1, log_phase = 0;
   bool log = false;      // CPFFT_LOG=1: the reference's residual reports on stderr
   double* hist[2] = {nullptr, nullptr};
   int hn = 0;  // index of the history at n
@@ -259,7 +270,8 @@ int dalloc(Ptr& p, size_t bytes) {
 
 void free_ctx(Ctx* c) {
   if (!c) return;
-  void* ptrs[] = {c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
+  void* ptrs[] = {c->log_X, c->log_T, c->log_n,
+                  c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats};
   for (void* q : ptrs)
@@ -461,7 +473,7 @@ int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
 }
 
 int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
-           long long* predict_iters = nullptr) {
+           long long* predict_iters = nullptr, long long* rejected = nullptr) {
   StressArgs a;
   a.Fn = c->Fn;
   a.Fn1 = c->Fn1;
@@ -479,9 +491,30 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.dt = c->dt;
   a.step = step;
   a.iter = iter;
+  a.mlp_packed = nullptr;
+  a.mlp_params = a.mlp_norm = nullptr;
+  a.mlp_err = nullptr;
+  bool warm = false;
+  if (c->warm && iter > 0) {
+    mlp::Weights w;
+    if (!mlp_device_weights(&w, &a.mlp_err)) {
+      cpfft_set_error("learned initial guess selected but the network is not initialised");
+      return CPFFT_ERR_NOT_INIT;
+    }
+    a.mlp_packed = w.packed;
+    a.mlp_params = w.params;
+    a.mlp_norm = w.norm;
+    warm = true;
+  }
+  a.log_X = c->log_cap > 0 ? c->log_X : nullptr;
+  a.log_T = c->log_T;
+  a.log_n = c->log_n;
+  a.log_cap = c->log_cap;
+  a.log_stride = c->log_stride;
+  a.log_phase = c->log_phase;
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
-  CK(launch_stress(a, c->st));
+  CK(launch_stress(a, warm, c->st));
   TRY(kt_stop(c));
   c->K4f_valid = a.K4f != nullptr;
   CK(cudaMemcpyAsync(c->h_stats, c->stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
@@ -489,6 +522,8 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   if (local_iters) *local_iters = (long long)c->h_stats[0];
   if (fails) *fails = (int)c->h_stats[1];
   if (predict_iters) *predict_iters = (long long)c->h_stats[2];
+  if (rejected) *rejected = (long long)c->h_stats[3];
+  if (warm) TRY(mlp_check_error());
   return 0;
 }
 
@@ -758,13 +793,61 @@ int cpfft_set_mode(int precision, int warm_start) {
     return CPFFT_ERR_BAD_ARG;
   }
   if (warm_start) {
-    cpfft_set_error("cpfft_set_mode: the learned warm start is not available in this build");
-    return CPFFT_ERR_BAD_ARG;
+    mlp::Weights w;
+    int* err;
+    if (!mlp_device_weights(&w, &err)) {
+      cpfft_set_error("cpfft_set_mode: the learned initial guess needs cpfft_mlp_init (and "
+                      "trained parameters)");
+      return CPFFT_ERR_NOT_INIT;
+    }
   }
   if (precision == CPFFT_PREC_MIXED) TRY(alloc_mixed(g_ctx));
   if (precision != g_ctx->prec) g_ctx->K4f_valid = false;
   g_ctx->prec = precision;
   g_ctx->warm = warm_start;
+  return 0;
+}
+
+int cpfft_learn_log(long long capacity, int stride, int phase) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (capacity < 0 || stride < 1 || phase < 0 || phase >= stride) {
+    cpfft_set_error("cpfft_learn_log: bad arguments");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  for (void* q : {(void*)c->log_X, (void*)c->log_T, (void*)c->log_n})
+    if (q) cudaFree(q);
+  c->log_X = c->log_T = nullptr;
+  c->log_n = nullptr;
+  c->log_cap = 0;
+  if (capacity == 0) return 0;
+  TRY(dalloc(c->log_X, (size_t)capacity * mlp::NIN * sizeof(float)));
+  TRY(dalloc(c->log_T, (size_t)capacity * mlp::NOUT * sizeof(float)));
+  TRY(dalloc(c->log_n, sizeof(unsigned long long)));
+  CK(cudaMemset(c->log_n, 0, sizeof(unsigned long long)));
+  c->log_cap = capacity;
+  c->log_stride = stride;
+  c->log_phase = phase;
+  return 0;
+}
+
+int cpfft_learn_fetch(float* X, float* T, long long* n) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (!n) {
+    cpfft_set_error("cpfft_learn_fetch: n is NULL");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  *n = 0;
+  if (!c->log_cap) return 0;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, c->log_n, sizeof(cnt), cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  const long long m = std::min<long long>((long long)cnt, c->log_cap);
+  if (X) CK(cudaMemcpyAsync(X, c->log_X, (size_t)m * mlp::NIN * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  if (T) CK(cudaMemcpyAsync(T, c->log_T, (size_t)m * mlp::NOUT * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  *n = m;
   return 0;
 }
 
@@ -902,10 +985,11 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       a = clk::now();
       long long li;
       int fails;
-      long long pi = 0;
-      TRY(stress(c, step, iiter_EBC, &li, &fails, &pi));
+      long long pi = 0, rj = 0;
+      TRY(stress(c, step, iiter_EBC, &li, &fails, &pi, &rj));
       ts += sec(a);
       S.predict_iters += pi;
+      S.guess_rejected += rj;
       S.local_iters += li;
       S.local_fallbacks += fails;
       S.stress_updates++;
@@ -933,10 +1017,11 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     a = clk::now();
     long long li;
     int fails;
-    long long pi = 0;
-    TRY(stress(c, step, iiter_EBC, &li, &fails, &pi));
+    long long pi = 0, rj = 0;
+    TRY(stress(c, step, iiter_EBC, &li, &fails, &pi, &rj));
     ts += sec(a);
     S.predict_iters += pi;
+    S.guess_rejected += rj;
     S.local_iters += li;
     S.local_fallbacks += fails;
     S.stress_updates++;

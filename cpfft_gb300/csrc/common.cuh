@@ -30,6 +30,7 @@ struct OriRec {
   double C[36];    // stiffness in the sample frame, row-major 6x6
   double ms[72];   // 12 x 6 sym(b (x) n) Voigt, engineering shear
   double qs[36];   // 12 x 3 skew(b (x) n) as (w23, w13, w12)
+  double g[9];     // lattice -> sample rotation applied to b and n, row-major
 };
 
 // Scalars of one crystal definition that the Voce path reads.
@@ -64,10 +65,23 @@ struct StressArgs {
   const int* crys;       // (N3) crystal id, 0-based
   const OriRec* oris;
   const CrysRec* cryss;
-  unsigned long long* stats;  // [0] local iters, [1] failures, [2] predict iters
+  unsigned long long* stats;  // [0] local iters, [1] failures, [2] predict iters,
+                              // [3] learned guesses the Newton solve rejected
   long long N3;
   double dt;
   int step, iter;
+  // learned initial guess (mlp.cuh): BF16 operand copies, FP32 parameters, normalisation
+  const void* mlp_packed;
+  const float* mlp_params;
+  const float* mlp_norm;
+  int* mlp_err;               // set when a tensor-core wait gave up
+  // logging of (features, converged increments) pairs from the plain solve
+  float* log_X;               // [cap][20], null: no logging
+  float* log_T;               // [cap][7]
+  unsigned long long* log_n;  // pairs written (may exceed cap: extra pairs are dropped)
+  long long log_cap;
+  int log_stride, log_phase;  // voxels v with v % stride == phase are logged
 };
 
-cudaError_t launch_stress(const StressArgs& a, cudaStream_t s);
+// warm = true: the learned initial guess starts the local Newton solve
+cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);

@@ -432,12 +432,15 @@ int step(long long first, long long n, int ntiles, float lr, float* gout, float*
 
 }  // namespace
 
-// the device weights of the learned initial guess, for the stress-update kernel
-bool mlp_device_weights(Weights* w) {
+// the device weights of the learned initial guess and the tensor-core error flag, for
+// the stress-update kernel
+bool mlp_device_weights(Weights* w, int** err) {
   if (!g_mlp.ready) return false;
   *w = weights();
+  *err = g_mlp.err;
   return true;
 }
+int mlp_check_error() { return g_mlp.ready ? check_err() : 0; }
 
 extern "C" {
 

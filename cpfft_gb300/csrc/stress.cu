@@ -10,6 +10,7 @@
 // through 3x3 intermediates (about 1.6 kflop instead of ~20 kflop).  Every local loop
 // is bounded by miter and the line-search cap, so no thread can spin.
 #include "common.cuh"
+#include "mlp.cuh"
 
 namespace {
 
@@ -392,6 +393,9 @@ __device__ __forceinline__ bool anynan(const double* x, int n) {
   return r;
 }
 
+__device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jlast, bool& haveJ,
+                              int& iters, double& ttrate);
+
 // mm10_solve (src/mm10_a.f:2860-3295): predict on R1 with tau_tilde extrapolated, then
 // the coupled Newton; Armijo line search c = 1e-4, halving, at most 11 trials.
 __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, double* Jlast,
@@ -461,13 +465,27 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     x[6] = x2;
   }
   // ---- update
+  if (!newton_update(cu, x, inR1, Jlast, haveJ, iters, ttrate)) return false;
+  for (int i = 0; i < 6; i++) stress[i] = x[i];
+  tt = x[6];
+  return true;
+}
+
+// The coupled 7x7 Newton of mm10_solve (src/mm10_a.f:3105-3295) from x = (sigma, tau):
+// Armijo line search, converged when ||R|| <= atol or ||R|| / ||R_0|| <= rtol after at
+// least one iteration; inR_alt replaces ||R_0|| when the start is an exact root.
+__device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jlast, bool& haveJ,
+                              int& iters, double& ttrate) {
+  const CrysRec& c = *cu.cr;
+  const double cls = 1.0e-4;
+  double rs[12], si[12], pw[12];
   int it = 0;
   double R[7];
   ttrate = formR(cu, x, R, rs, si, pw);
   double dot = 0;
   for (int a = 0; a < 7; a++) dot += R[a] * R[a];
   double nR = sqrt(dot), inR = nR;
-  if (inR == 0.0) inR = inR1;
+  if (inR == 0.0) inR = inR_alt;
   while ((nR > c.atol && nR / inR > c.rtol) || it < 1) {
     formJ(cu, x, rs, si, pw, Jlast);
     haveJ = true;
@@ -500,8 +518,6 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     if (it > c.miter || anynan(x, 7)) { iters += it; return false; }
   }
   iters += it;
-  for (int i = 0; i < 6; i++) stress[i] = x[i];
-  tt = x[6];
   return true;
 }
 
@@ -601,30 +617,107 @@ __device__ void cep2A(const double* Fn, const double* Fn1, const double* t, cons
     }
 }
 
-__device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& piters,
-                             bool& ok);
+// block state of the learned initial guess inside the stress kernel
+struct GuessBlock {
+  unsigned char* smem;  // mlp::FWD_SMEM bytes
+  uint32_t tmem;        // 256 TMEM columns
+  uint64_t* bar;
+  uint32_t phase;
+};
 
+// Features of the learned initial guess (mlp::NIN, raw units): the quaternion of the
+// lattice rotation the local solve sees (Rp_n^T g; sign with w >= 0), the unrotated strain
+// increment D (6), sigma_n (6), tau_n, the tau rate of step n, cos(dev D, dev D_n) (the
+// predictor's extrapolation factor) and |D|.  FP32: only an initial guess depends on them.
+__device__ void guess_features(const double* g, const double* nRp, const double* D,
+                               const double* nsig, double ntt, double nttr, const double* nD,
+                               float* f) {
+  float M[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      M[3 * i + j] = (float)(nRp[i] * g[j] + nRp[3 + i] * g[3 + j] + nRp[6 + i] * g[6 + j]);
+  float w, x, y, z;  // Shepperd's branch choice keeps the square root away from zero
+  const float t = M[0] + M[4] + M[8];
+  if (t > 0.0f) {
+    float q = 2.0f * sqrtf(1.0f + t);
+    w = 0.25f * q; x = (M[7] - M[5]) / q; y = (M[2] - M[6]) / q; z = (M[3] - M[1]) / q;
+  } else if (M[0] > M[4] && M[0] > M[8]) {
+    float q = 2.0f * sqrtf(fmaxf(1.0f + M[0] - M[4] - M[8], 1e-20f));
+    w = (M[7] - M[5]) / q; x = 0.25f * q; y = (M[1] + M[3]) / q; z = (M[2] + M[6]) / q;
+  } else if (M[4] > M[8]) {
+    float q = 2.0f * sqrtf(fmaxf(1.0f + M[4] - M[0] - M[8], 1e-20f));
+    w = (M[2] - M[6]) / q; x = (M[1] + M[3]) / q; y = 0.25f * q; z = (M[5] + M[7]) / q;
+  } else {
+    float q = 2.0f * sqrtf(fmaxf(1.0f + M[8] - M[0] - M[4], 1e-20f));
+    w = (M[3] - M[1]) / q; x = (M[2] + M[6]) / q; y = (M[5] + M[7]) / q; z = 0.25f * q;
+  }
+  const float sg = w < 0.0f ? -1.0f : 1.0f;
+  f[0] = sg * w; f[1] = sg * x; f[2] = sg * y; f[3] = sg * z;
+  for (int i = 0; i < 6; i++) { f[4 + i] = (float)D[i]; f[10 + i] = (float)nsig[i]; }
+  f[16] = (float)ntt;
+  f[17] = (float)nttr;
+  float d1[6], d2[6], n1 = 0.0f, n2 = 0.0f, dd = 0.0f;
+  const float tr1 = (float)(D[0] + D[1] + D[2]) / 3.0f, tr2 = (float)(nD[0] + nD[1] + nD[2]) / 3.0f;
+  for (int i = 0; i < 6; i++) {
+    d1[i] = (float)D[i] - (i < 3 ? tr1 : 0.0f);
+    d2[i] = (float)nD[i] - (i < 3 ? tr2 : 0.0f);
+    n1 += d1[i] * d1[i];
+    n2 += d2[i] * d2[i];
+    dd += d1[i] * d2[i];
+  }
+  f[18] = (n1 > 0.0f && n2 > 0.0f) ? dd * rsqrtf(n1 * n2) : 0.0f;
+  float dn = 0.0f;
+  for (int i = 0; i < 6; i++) dn += (float)(D[i] * D[i]);
+  f[19] = sqrtf(dn);
+}
+
+template <bool WARM>
+__device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& iters,
+                             int& piters, bool& ok, int& rejected, GuessBlock* gb);
+
+// WARM: the learned initial guess starts each local Newton solve (launches with iter > 0
+// only); every thread of the block takes part in the block-level network evaluation, so
+// the tail block's surplus threads evaluate a copy of the last voxel and store nothing.
+template <bool WARM>
 __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
   long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  int iters = 0, piters = 0;
+  const bool valid = v < a.N3;
+  int iters = 0, piters = 0, rej = 0;
   bool ok = true;
-  if (v < a.N3) voxel_update(a, v, iters, piters, ok);
+  if (WARM) {
+    extern __shared__ __align__(128) unsigned char guess_smem[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tslot;
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&bar, 1);
+      tc::fence_mbar_init();
+    }
+    GuessBlock gb{guess_smem, mlp::tmem_block_alloc(&tslot, 256), &bar, 0u};
+    voxel_update<true>(a, valid ? v : a.N3 - 1, valid, iters, piters, ok, rej, &gb);
+    mlp::tmem_block_free(gb.tmem, 256);
+    if (!valid) { iters = 0; piters = 0; ok = true; rej = 0; }
+  } else if (valid) {
+    voxel_update<false>(a, v, true, iters, piters, ok, rej, nullptr);
+  }
   // statistics, warp-aggregated (every lane of the warp reaches this point)
-  unsigned long long li = iters, pi = piters, fl = ok ? 0 : 1;
+  unsigned long long li = iters, pi = piters, fl = ok ? 0 : 1, rj = rej;
   for (int o = 16; o > 0; o >>= 1) {
     li += __shfl_down_sync(0xffffffffu, li, o);
     pi += __shfl_down_sync(0xffffffffu, pi, o);
     fl += __shfl_down_sync(0xffffffffu, fl, o);
+    rj += __shfl_down_sync(0xffffffffu, rj, o);
   }
   if ((threadIdx.x & 31) == 0 && a.stats) {
     atomicAdd(a.stats + 0, li);
     atomicAdd(a.stats + 1, fl);
     atomicAdd(a.stats + 2, pi);
+    atomicAdd(a.stats + 3, rj);
   }
 }
 
-__device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& piters,
-                             bool& ok) {
+template <bool WARM>
+__device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& iters,
+                             int& piters, bool& ok, int& rejected, GuessBlock* gb) {
   const long long N3 = a.N3;
   double Fn[9], Fn1[9];
   for (int i = 0; i < 9; i++) {
@@ -691,6 +784,25 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
   double Jl[49];
   bool haveJ = false;
   ok = true;
+  // ---- learned initial guess / logging features
+  float feat[mlp::NIN];
+  const bool logit = !WARM && a.log_X && valid && !iter0 && !no_load &&
+                     (v % a.log_stride) == a.log_phase;
+  if (WARM || logit) guess_features(rec->g, nRp, uddt, nsig, ntt, nttr, nD, feat);
+  double guess[7];
+  bool have_guess = false;
+  if (WARM) {
+    float out[mlp::NOUT];
+    const mlp::Weights w{reinterpret_cast<const __nv_bfloat16*>(a.mlp_packed), a.mlp_params,
+                         a.mlp_norm};
+    const bool mok = mlp::forward_tile(w, gb->smem, gb->tmem, gb->bar, &gb->phase, feat, out);
+    if (!mok && threadIdx.x == 0) atomicExch(a.mlp_err, 1);
+    if (mok) {
+      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + (double)out[i];
+      guess[6] = ntt + (double)out[6];
+      have_guess = !anynan(guess, 7) && guess[6] > 0.0 && !iter0 && !no_load;
+    }
+  }
   if (iter0 || no_load) {
     for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
     if (!no_load) {
@@ -706,6 +818,21 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
     for (int i = 0; i < 6; i++) ostress[i] = stress[i];
     int cuts = 0;
     bool fail = false;
+    if (WARM && have_guess) {
+      // the full step from the network's guess; a guess the Newton solve cannot finish
+      // from is dropped and the plain predictor path below runs instead
+      double x[7], trw = 0.0;
+      for (int i = 0; i < 7; i++) x[i] = guess[i];
+      if (newton_update(s, x, 1.0, Jl, haveJ, iters, trw) && !anynan(x, 7)) {
+        for (int i = 0; i < 6; i++) stress[i] = x[i];
+        tt = x[6];
+        ttrate = trw;
+        frac = 1.0;
+      } else {
+        rejected = 1;
+        haveJ = false;
+      }
+    }
     while (frac < 1.0) {
       double Dw[6];
       for (int i = 0; i < 6; i++) Dw[i] = uddt[i] * (stp + frac);
@@ -791,6 +918,14 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
       ttrate = 0.0;
       for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
     }
+    if (logit && ok) {  // (features, converged increments) for training the guess
+      const unsigned long long slot = atomicAdd(a.log_n, 1ull);
+      if ((long long)slot < a.log_cap) {
+        for (int i = 0; i < mlp::NIN; i++) a.log_X[slot * mlp::NIN + i] = feat[i];
+        for (int i = 0; i < 6; i++) a.log_T[slot * mlp::NOUT + i] = (float)(stress[i] - nsig[i]);
+        a.log_T[slot * mlp::NOUT + 6] = (float)(tt - ntt);
+      }
+    }
   }
   // ---- plastic rotation (mm10_update_rotation, src/mm10_a.f:3310-3327)
   double Rp[9];
@@ -827,6 +962,7 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
     ex[0] += 1.0; ex[4] += 1.0; ex[8] += 1.0;
     mm3(ex, nRp, Rp);
   }
+  if (!valid) return;
   // ---- store history n+1
   for (int i = 0; i < 6; i++) a.hist_np1[(H_SIG + i) * N3 + v] = stress[i];
   a.hist_np1[H_TT * N3 + v] = tt;
@@ -854,10 +990,22 @@ __device__ void voxel_update(const StressArgs& a, long long v, int& iters, int& 
 
 }  // namespace
 
-cudaError_t launch_stress(const StressArgs& a, cudaStream_t s) {
+cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;
   unsigned blocks = (unsigned)((a.N3 + 127) / 128);
-  stress_kernel<<<blocks, 128, 0, s>>>(a);
+  if (warm) {
+    static bool attr = false;
+    if (!attr) {
+      cudaError_t e = cudaFuncSetAttribute(stress_kernel<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           mlp::FWD_SMEM);
+      if (e != cudaSuccess) return e;
+      attr = true;
+    }
+    stress_kernel<true><<<blocks, 128, mlp::FWD_SMEM, s>>>(a);
+  } else {
+    stress_kernel<false><<<blocks, 128, 0, s>>>(a);
+  }
   g_kernel_launches += 1;
   return cudaGetLastError();
 }

@@ -97,6 +97,7 @@ typedef struct cpfft_stats {
     long long n_green32;        /* FP32 Green applies                                      */
     long long kernel_launches;  /* kernels this call launched                              */
     long long predict_iters;    /* local predictor (6x6) Newton iterations, summed         */
+    long long guess_rejected;   /* learned initial guesses the Newton solve dropped        */
 } cpfft_stats;
 
 /*
@@ -236,6 +237,11 @@ int cpfft_mlp_loss_grad(const float* X, const float* T, long long n, float* grad
  * sets the normalisation from the data; *loss = mean loss of the last epoch */
 int cpfft_mlp_train(const float* X, const float* T, long long n, int epochs, int batch_tiles,
                     float lr, int seed, float* loss);
+/* Log (features, converged increments) pairs of the plain local solves of voxels with
+ * v % stride == phase into device buffers of `capacity` pairs (0 stops logging). */
+int cpfft_learn_log(long long capacity, int stride, int phase);
+/* Copy the logged pairs to host arrays X (n, 20) and T (n, 7); *n = pairs copied. */
+int cpfft_learn_fetch(float* X, float* T, long long* n);
 
 #ifdef __cplusplus
 }

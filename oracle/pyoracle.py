@@ -55,7 +55,7 @@ class Stats(ctypes.Structure):
         ("t_stress_kernel", ctypes.c_double), ("t_green64", ctypes.c_double),
         ("t_green32", ctypes.c_double), ("n_green64", ctypes.c_longlong),
         ("n_green32", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
-        ("predict_iters", ctypes.c_longlong),
+        ("predict_iters", ctypes.c_longlong), ("guess_rejected", ctypes.c_longlong),
     ]
 
     def as_dict(self):

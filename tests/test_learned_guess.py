@@ -1,0 +1,54 @@
+"""The learned initial guess of the local mm10 Newton solve, end to end on the GPU:
+log (features, converged increments) from the plain solver on one RVE, train the
+network with the tcgen05 kernels, then solve a different RVE (other seed) with and
+without the guess.  The guess only changes where each local Newton solve starts: the
+volume-averaged stress must agree with the plain run to the solver tolerances, and the
+local iterations (predictor + coupled Newton) must drop."""
+import numpy as np
+import pytest
+
+from cpfft_gb300 import rve
+
+pytestmark = pytest.mark.gpu
+
+
+def run(gpulib, N, seed, nsteps, warm=False, log=0):
+    r = rve.make_rve(N, 8, seed)
+    load = rve.uniaxial_tension(0.02, 20)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                      gpulib.PREC_FP64)
+    try:
+        if warm:
+            s.set_mode(gpulib.PREC_FP64, 1)
+        if log:
+            s.learn_log(log)
+        s.nr3_begin(1e-10)
+        pbar, it_local, it_pred, rej = [], 0, 0, 0
+        for step in range(1, nsteps + 1):
+            rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+            assert rc == 0
+            pbar.append(Pbar)
+            it_local += st["local_iters"]
+            it_pred += st["predict_iters"]
+            rej += st["guess_rejected"]
+        data = s.learn_fetch() if log else None
+        return np.array(pbar), it_local, it_pred, rej, data
+    finally:
+        s.close()
+
+
+def test_learned_guess_cuts_local_iterations(gpulib):
+    N, nsteps = 16, 8
+    _, _, _, _, (X, T) = run(gpulib, N, 31, nsteps, log=2_000_000)
+    assert X.shape[0] > 50_000 and np.isfinite(X).all() and np.isfinite(T).all()
+    m = gpulib.Mlp(5)
+    loss = m.train(X, T, epochs=30, batch_tiles=16, lr=2e-3, seed=3)
+    assert loss < 0.05, loss
+    pb0, li0, pi0, rj0, _ = run(gpulib, N, 32, nsteps)
+    pb1, li1, pi1, rj1, _ = run(gpulib, N, 32, nsteps, warm=True)
+    print(f"plain: update {li0} + predictor {pi0} = {li0 + pi0}; "
+          f"learned: update {li1} + predictor {pi1} = {li1 + pi1}, rejected guesses {rj1}")
+    assert rj0 == 0
+    # same equilibrium to the Newton/NBC tolerances of the run (1e-6)
+    assert np.abs(pb1 - pb0).max() <= 1e-5 * np.abs(pb0).max()
+    assert li1 + pi1 < 0.8 * (li0 + pi0)

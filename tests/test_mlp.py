@@ -25,11 +25,11 @@ def random_params(seed):
     return p.astype(np.float32), norm.astype(np.float32)
 
 
-def data(n, seed):
+def data(n, seed, fseed=0):
     rng = np.random.default_rng(seed)
     X = rng.standard_normal((n, ref.NIN)).astype(np.float32)
-    # a smooth target the network can learn
-    A = rng.standard_normal((ref.NIN, ref.NOUT)) / np.sqrt(ref.NIN)
+    # a smooth target the network can learn (the function is fixed by fseed)
+    A = np.random.default_rng(1000 + fseed).standard_normal((ref.NIN, ref.NOUT)) / np.sqrt(ref.NIN)
     T = (np.tanh(X @ A) + 0.1 * np.sin(3 * X[:, :ref.NOUT])).astype(np.float32)
     return X, T
 
