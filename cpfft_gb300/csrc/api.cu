@@ -494,6 +494,13 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.mlp_packed = nullptr;
   a.mlp_params = a.mlp_norm = nullptr;
   a.mlp_err = nullptr;
+  // learned start: the predicted stress increment, pulled back 2 % inside the rate
+  // surface; tau from the reference's extrapolation (measured: the network's tau guess
+  // costs coupled-Newton iterations, and a stress start outside the surface costs
+  // predictor iterations)
+  a.guess_ls = 1.0;
+  a.guess_lt = 0.0;
+  a.guess_eps = 0.02;
   bool warm = false;
   if (c->warm && iter > 0) {
     mlp::Weights w;

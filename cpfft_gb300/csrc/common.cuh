@@ -75,6 +75,8 @@ struct StressArgs {
   const float* mlp_params;
   const float* mlp_norm;
   int* mlp_err;               // set when a tensor-core wait gave up
+  double guess_ls, guess_lt;  // fractions of the predicted stress / tau increments used
+  double guess_eps;           // margin below the rate surface for the learned start
   // logging of (features, converged increments) pairs from the plain solve
   float* log_X;               // [cap][20], null: no logging
   float* log_T;               // [cap][7]

@@ -211,6 +211,8 @@ struct Crystal {
   double ms[12][6];
   double qc[12][3];
   double Cms[12][6];  // C ms_i, constant while ms is (the reference forms it per call)
+  double guess_eps;   // learned start: margin below the rate surface
+  int guess_tau;      // learned start: take tau from the guess (else the extrapolation)
 };
 
 __device__ __forceinline__ double Cv(const double* C, int a, int b) { return __ldg(C + 6 * a + b); }
@@ -398,8 +400,13 @@ __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jl
 
 // mm10_solve (src/mm10_a.f:2860-3295): predict on R1 with tau_tilde extrapolated, then
 // the coupled Newton; Armijo line search c = 1e-4, halving, at most 11 trials.
+//
+// x0 (7, or null): a learned starting point (sigma, tau) for the predictor in place of
+// (sigma_n, extrapolated tau).  The relative stop test keeps the residual of the plain
+// start as its scale, so both starts iterate to the same absolute tolerance.
 __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, double* Jlast,
-                      bool& haveJ, int& iters, int& piters, double& ttrate) {
+                      bool& haveJ, int& iters, int& piters, double& ttrate,
+                      const double* x0 = nullptr) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
   double x[7], rs[12], si[12], pw[12];
@@ -428,6 +435,30 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
     double nR1 = sqrt(dot);
     inR1 = nR1;
+    if (x0) {
+      // stress start from the guess, pulled back along the predicted increment until no
+      // slip system's resolved shear exceeds (1 - eps) tau: the power-law Newton
+      // converges fast from inside the rate surface and slowly from outside it
+      double smax = 1.0;
+      const double lim = (1.0 - cu.guess_eps) * x2;
+      for (int i = 0; i < 12; i++) {
+        double r0 = 0.0, dr = 0.0;
+        for (int k = 0; k < 6; k++) {
+          r0 += x[k] * cu.ms[i][k];
+          dr += (x0[k] - x[k]) * cu.ms[i][k];
+        }
+        if (dr > 0.0 && r0 + dr > lim) smax = fmin(smax, fmax(0.0, (lim - r0) / dr));
+        if (dr < 0.0 && r0 + dr < -lim) smax = fmin(smax, fmax(0.0, (-lim - r0) / dr));
+      }
+      for (int i = 0; i < 6; i++) x1[i] = x[i] + smax * (x0[i] - x[i]);
+      if (cu.guess_tau) x2 = x0[6];
+      slips(cu, x1, x2, rs, si, pw);
+      formR1(cu, x1, rs, si, R1);
+      dot = 0;
+      for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
+      nR1 = sqrt(dot);
+      if (inR1 == 0.0) inR1 = nR1;
+    }
     int it = 0;
     while (nR1 > c.atol1 && nR1 / inR1 > c.rtol1) {
       double J[36], mJ[36], dx[6];
@@ -774,6 +805,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   s.nttr = nttr;
   for (int i = 0; i < 6; i++) s.nD[i] = nD[i];
   setup_np1(s, rec, uddt, a.dt, rn1, nRp);
+  s.guess_eps = a.guess_eps;
+  s.guess_tau = a.guess_lt > 0.0;
   double stress[6], tt = ntt, ttrate = 0.0;
   for (int i = 0; i < 6; i++) stress[i] = nsig[i];
   double t1 = 0, t2 = 0;
@@ -798,8 +831,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     const bool mok = mlp::forward_tile(w, gb->smem, gb->tmem, gb->bar, &gb->phase, feat, out);
     if (!mok && threadIdx.x == 0) atomicExch(a.mlp_err, 1);
     if (mok) {
-      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + (double)out[i];
-      guess[6] = ntt + (double)out[6];
+      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + a.guess_ls * (double)out[i];
+      guess[6] = ntt + a.guess_lt * (double)out[6];
       have_guess = !anynan(guess, 7) && guess[6] > 0.0 && !iter0 && !no_load;
     }
   }
@@ -819,13 +852,14 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     int cuts = 0;
     bool fail = false;
     if (WARM && have_guess) {
-      // the full step from the network's guess; a guess the Newton solve cannot finish
-      // from is dropped and the plain predictor path below runs instead
-      double x[7], trw = 0.0;
-      for (int i = 0; i < 7; i++) x[i] = guess[i];
-      if (newton_update(s, x, 1.0, Jl, haveJ, iters, trw) && !anynan(x, 7)) {
-        for (int i = 0; i < 6; i++) stress[i] = x[i];
-        tt = x[6];
+      // the full step with the predictor started from the network's guess; a solve that
+      // fails from there is dropped and the plain path below runs instead
+      double st[6], ttw = ntt, trw = 0.0;
+      for (int i = 0; i < 6; i++) st[i] = stress[i];
+      if (solve(s, a.dt, st, ttw, Jl, haveJ, iters, piters, trw, guess) && !anynan(st, 6) &&
+          !isnan(ttw)) {
+        for (int i = 0; i < 6; i++) stress[i] = st[i];
+        tt = ttw;
         ttrate = trw;
         frac = 1.0;
       } else {
