@@ -15,6 +15,11 @@ e2e    = the same units over host wall time of each step plus copying the step's
          result fields Fn1, Pn1 back to pinned host buffers.
 Inputs larger than L2: every field is >= 150 MB (9 x 128^3 FP64), K4 is 1.4 GB.
 
+Modes (--mode): learned (default; the workload's configuration) = FP32 Krylov under the
+FP64 residual plus the learned initial guess of the local solves, whose network is
+trained before the timed steps on pairs logged from a 64^3 RVE of another seed
+(train_guess); mixed = the same without the learned guess; fp64 = the plain form.
+
 `--impl reference` times the CPU stand-in of the reference (the C++ oracle, OpenMP on
 all host cores) on bounded samples of the same workload (see cpu_sample()).
 """
@@ -112,6 +117,39 @@ def load_traffic():
             return json.load(f)
     except OSError:
         return {}
+
+
+def train_guess(cp, N=64, grains=64, seed=100, steps=5, stride=3, epochs=4):
+    """The learned initial guess: log (features, converged increments) of the plain local
+    solves on a 64^3 RVE with another seed (every `stride`-th voxel, `steps` load steps of
+    the same loading, mixed precision), then train the network with the tcgen05 kernels.
+    Outside the timed region."""
+    from cpfft_gb300 import rve
+    t0 = time.perf_counter()
+    r = rve.make_rve(N, grains, seed)
+    load = rve.plane_strain_compression(0.10, 100)
+    s = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, cp.PREC_MIXED)
+    try:
+        s.learn_log(N ** 3 * 10 * steps // stride, stride)
+        s.nr3_begin(1e-10)
+        done = 0
+        for step in range(1, steps + 1):
+            try:
+                # every local solve of every pass is a valid pair; a looser global
+                # tolerance only shortens the run
+                s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-4, 1e-10, 20)
+            except cp.CpfftError:
+                break  # a global Newton limit cycle ends the logging run; keep its pairs
+            done = step
+        X, T = s.learn_fetch()
+    finally:
+        s.close()
+    t1 = time.perf_counter()
+    m = cp.Mlp(seed)
+    loss = m.train(X, T, epochs=epochs, batch_tiles=32, lr=2e-3, seed=seed)
+    return {"pairs": int(X.shape[0]), "rve": f"{N}^3, {grains} grains, seed {seed}, {done} steps",
+            "epochs": epochs, "loss": loss, "t_log_s": t1 - t0,
+            "t_train_s": time.perf_counter() - t1}
 
 
 def workload(N, grains, seed):
@@ -235,8 +273,11 @@ def gb300_arm(args):
     N = args.N
     N3 = N ** 3
     r, load = workload(N, args.grains, args.seed)
-    prec = cp.PREC_MIXED if args.mode == "mixed" else cp.PREC_FP64
+    learned = train_guess(cp) if args.mode == "learned" else None
+    prec = cp.PREC_FP64 if args.mode == "fp64" else cp.PREC_MIXED
     solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
+    if learned:
+        solver.set_mode(prec, 1)
     tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
     solver.nr3_begin(tolPCG)
     step = 0
@@ -336,7 +377,7 @@ def gb300_arm(args):
         "ms_per_step": 1e3 * tmax / args.steps,
         "s_per_load_step": tmax / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == cp.PREC_FP64 else "f64+f32",
+        "dtype": {"fp64": "f64", "mixed": "f64+f32", "learned": "f64+f32+bf16"}[args.mode],
         "data": "synthetic",
         "config": config_dict(args, "gb300"),
         "e2e": {"value": units_all / temax, "unit": "voxel stress-updates/s",
@@ -352,7 +393,9 @@ def gb300_arm(args):
                             "res_equil": [s["res_equil"] for s in stats],
                             "res_fft": [s["res_fft"] for s in stats],
                             "local_iters_per_voxel_pass": sum(s["local_iters"] for s in stats) / (N3 * su),
-                            "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in stats) / (N3 * su)},
+                            "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in stats) / (N3 * su),
+                            "guess_rejected": [s["guess_rejected"] for s in stats]},
+        "learned": learned,
         "fp64_peak_tflops": fp64_peak,
         "clocks": clk,
         "cpu_baseline": cpu,
@@ -371,7 +414,9 @@ def main():
     ap.add_argument("--N", type=int, default=128)
     ap.add_argument("--grains", type=int, default=256)
     ap.add_argument("--seed", type=int, default=3)
-    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
+    # mixed: FP32 Krylov under the FP64 residual; learned: the same with the learned
+    # initial guess of the local solves (trained before the timed steps); fp64: plain
+    ap.add_argument("--mode", default="learned", choices=["learned", "mixed", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
     # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
