@@ -910,6 +910,23 @@ int cpfft_green_apply(const double* x, double* y, int flgK) {
   return sync(c);
 }
 
+int cpfft_green_apply_f32(const float* x, float* y, int flgK) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (c->prec != CPFFT_PREC_MIXED || (flgK && !c->K4f_valid)) {
+    cpfft_set_error("cpfft_green_apply_f32: needs mixed precision and, with K, the FP32 "
+                    "tangent of a stress update");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const size_t f9 = 9 * c->N3 * sizeof(float);
+  CK(cudaMemcpyAsync(c->rf, x, f9, cudaMemcpyHostToDevice, c->st));
+  c->f32_matvecs++;
+  TRY(cuda_check(green_apply<float>(c->rf, c->K4f, flgK ? 1 : 0, c->Apf, c->Sf, c->twf, c->g, c->st),
+                 "green_apply fp32"));
+  CK(cudaMemcpyAsync(y, c->Apf, f9, cudaMemcpyDeviceToHost, c->st));
+  return sync(c);
+}
+
 int cpfft_cg(const double* b, double* x, double tol, int* iters) {
   TRY(need_ctx());
   Ctx* c = g_ctx;

@@ -68,11 +68,6 @@ __device__ __forceinline__ void dft8(T2* v) {
   }
 }
 
-// Shared-memory columns are padded: element k of a column sits at pidx(k) = k + k/8 and
-// columns are padlen(N) apart.  The Stockham stages write with strides of R and Ns
-// elements; the padding breaks those power-of-two strides across the 32 banks.
-__host__ __device__ __forceinline__ int pidx(int k) { return k + (k >> 3); }
-__host__ __device__ __forceinline__ int padlen(int N) { return N + (N >> 3) + 1; }
 
 // One forward Stockham stage of radix R on `ncols` columns (column stride cs) from
 // src to dst; tw[k] = exp(-2 pi i k / N).  Radix 2/4/8 run as register butterflies,
@@ -397,27 +392,22 @@ __global__ void __launch_bounds__(256) pass_e(const typename Vec2<T>::t* __restr
 // Same data flow and HBM layout as the passes above; each column transform runs in the
 // registers of one warp (fft_warp.cuh), shared memory only stages coalesced tiles.
 
-// load a column held at col[pidx(k)], transform (inverse through conjugation), store back
-template <int M, typename T, bool INV>
-__device__ __forceinline__ void warp_column(typename Vec2<T>::t* col,
-                                            const typename Vec2<T>::t* tw) {
+// columns per warp of the register transform and 9 component columns rounded up to it
+template <int N>
+constexpr int cpw() { return 32 / regfft::Shape<N>::P; }
+template <int N>
+constexpr int ncols9() { return ((9 + cpw<N>() - 1) / cpw<N>()) * cpw<N>(); }
+
+// Transform ncols columns (stride Lp; ncols a multiple of cpw<N>()) with every warp of
+// the block; inverse through conjugation.  Columns past the data are scratch.
+template <int N, typename T, bool INV>
+__device__ __forceinline__ void block_columns(typename Vec2<T>::t* base, int ncols, int Lp,
+                                              const typename Vec2<T>::t* tw) {
   using T2 = typename Vec2<T>::t;
-  const int lane = threadIdx.x & 31;
-  T2 v[M];
-#pragma unroll
-  for (int j = 0; j < M; j++) {
-    v[j] = col[pidx(32 * j + lane)];
-    if (INV) v[j].y = -v[j].y;
-  }
-  warpfft::fft<M, T2, T>(v, tw);
-  const int kb = M * warpfft::brev5(lane);
-  __syncwarp();
-#pragma unroll
-  for (int k1 = 0; k1 < M; k1++) {
-    T2 o = v[k1];
-    if (INV) o.y = -o.y;
-    col[pidx(k1 + kb)] = o;
-  }
+  constexpr int P = regfft::Shape<N>::P, CPW = cpw<N>();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int g = w; g * CPW < ncols; g += nw)
+    regfft::column<N, T2, T, INV>(base + (g * CPW + lane / P) * Lp, tw, lane % P);
 }
 
 template <int M, typename T, typename TK>
@@ -460,8 +450,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
     }
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5;
-  if (w < 9) warp_column<M, T, false>(col + w * Lp, tw);
+  block_columns<N, T, false>(col, ncols9<N>(), Lp, tw);
   __syncthreads();
   for (int t = threadIdx.x; t < 9 * H; t += blockDim.x) {
     int i = t / H, k = t - i * H;
@@ -477,7 +466,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
 
 // TK columns of one (component, c) plane per block, one warp per column
 template <int M, typename T, int TK>
-__global__ void __launch_bounds__(32 * TK) wpass_b(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+__global__ void __launch_bounds__(32 * TK / cpw<32 * M>()) wpass_b(typename Vec2<T>::t* __restrict__ S, GridDesc g,
                                                    const typename Vec2<T>::t* __restrict__ twg,
                                                    int inverse) {
   using T2 = typename Vec2<T>::t;
@@ -499,9 +488,8 @@ __global__ void __launch_bounds__(32 * TK) wpass_b(typename Vec2<T>::t* __restri
     col[kk * Lp + pidx(row)] = v;
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5;
-  if (inverse) warp_column<M, T, true>(col + w * Lp, tw);
-  else warp_column<M, T, false>(col + w * Lp, tw);
+  if (inverse) block_columns<N, T, true>(col, TK, Lp, tw);
+  else block_columns<N, T, false>(col, TK, Lp, tw);
   __syncthreads();
   for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
     int row = t / TK, kk = t - row * TK;
@@ -511,7 +499,7 @@ __global__ void __launch_bounds__(32 * TK) wpass_b(typename Vec2<T>::t* __restri
 }
 
 template <int M, typename T, int TK>
-__global__ void __launch_bounds__(256) wpass_c(typename Vec2<T>::t* __restrict__ S, GridDesc g,
+__global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__ S, GridDesc g,
                                                const typename Vec2<T>::t* __restrict__ twg) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
@@ -533,8 +521,7 @@ __global__ void __launch_bounds__(256) wpass_c(typename Vec2<T>::t* __restrict__
     col[(i * TK + kk) * Lp + pidx(c)] = v;
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int cc = w; cc < 9 * TK; cc += nw) warp_column<M, T, false>(col + cc * Lp, tw);
+  block_columns<N, T, false>(col, 9 * TK, Lp, tw);
   __syncthreads();
   const int Nh = g.Nhalf, gm = g.gmap;
   const T scale = (T)g.inv_n3;
@@ -563,7 +550,7 @@ __global__ void __launch_bounds__(256) wpass_c(typename Vec2<T>::t* __restrict__
     for (int i = 0; i < 9; i++) col[(i * TK + kk) * Lp + pidx(kc)] = out[i];
   }
   __syncthreads();
-  for (int cc = w; cc < 9 * TK; cc += nw) warp_column<M, T, true>(col + cc * Lp, tw);
+  block_columns<N, T, true>(col, 9 * TK, Lp, tw);
   __syncthreads();
   for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
     int kk = t % TK, rem = t / TK;
@@ -605,8 +592,7 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
     col[i * Lp + pidx(k)] = z;
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5;
-  if (w < 9) warp_column<M, T, true>(col + w * Lp, tw);
+  block_columns<N, T, true>(col, ncols9<N>(), Lp, tw);
   __syncthreads();
   T dsum = 0;
   for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
@@ -636,20 +622,20 @@ template <typename T>
 size_t smem_w(int N, int ncols) { return sizeof(typename Vec2<T>::t) * (size_t)(N + ncols * padlen(N)); }
 template <typename T>
 constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
-constexpr int WTILE_B = 8;
+constexpr int WTILE_B = 16;  // columns of pass B / D per block: 128-byte rows
 
 template <int M, typename T>
 cudaError_t wgreen_setup() {
   constexpr int N = 32 * M;
   cudaError_t e;
   if ((e = cudaFuncSetAttribute(wpass_a<M, T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_w<T>(N, 9)))) return e;
+                                (int)smem_w<T>(N, ncols9<N>())))) return e;
   if ((e = cudaFuncSetAttribute(wpass_b<M, T, WTILE_B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, WTILE_B)))) return e;
   if ((e = cudaFuncSetAttribute(wpass_c<M, T, wtile_c<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, 9 * wtile_c<T>())))) return e;
   if ((e = cudaFuncSetAttribute(wpass_e<M, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_w<T>(N, 9)))) return e;
+                                (int)smem_w<T>(N, ncols9<N>())))) return e;
   return cudaSuccess;
 }
 
@@ -658,14 +644,15 @@ void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* 
                   const typename Vec2<T>::t* tw, const GridDesc& g, cudaStream_t st,
                   double* part) {
   constexpr int N = 32 * M, H = N / 2 + 1, TC = wtile_c<T>();
-  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(x, K4, flgK, S, g, tw);
+  constexpr int NA = ncols9<N>(), TB = 32 * WTILE_B / cpw<N>();
+  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, flgK, S, g, tw);
   dim3 gb((H + WTILE_B - 1) / WTILE_B, N, 9);
-  wpass_b<M, T, WTILE_B><<<gb, 32 * WTILE_B, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 0);
+  wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 0);
   dim3 gc((H + TC - 1) / TC, N);
-  wpass_c<M, T, TC><<<gc, 256, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
-  wpass_b<M, T, WTILE_B><<<gb, 32 * WTILE_B, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
-  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, 9), st>>>(S, y, g, tw, part ? x : nullptr,
-                                                           part);
+  wpass_c<M, T, TC><<<gc, 288, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
+  wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
+  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw, part ? x : nullptr,
+                                                            part);
 }
 
 template <typename T>

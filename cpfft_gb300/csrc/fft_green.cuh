@@ -24,6 +24,12 @@ struct GridDesc {
 
 FftPlan make_plan(int N);
 
+// Shared-memory columns are padded: element k of a column sits at pidx(k) = k + k/8 and
+// columns are padlen(N) apart.  The transforms access columns with power-of-two strides;
+// the padding spreads those strides across the 32 banks.
+__host__ __device__ __forceinline__ int pidx(int k) { return k + (k >> 3); }
+__host__ __device__ __forceinline__ int padlen(int N) { return N + (N >> 3) + 1; }
+
 // y = G(K4 : x) (flgK = 1) or y = G(x); S is the spectral scratch (9 * N * N * H complex),
 // tw the length-N forward twiddle table.  All on stream st.
 template <typename T>

@@ -1,16 +1,21 @@
-// fft_warp.cuh -- register-resident column FFTs for power-of-two N = 32 M (M = 1..8).
+// fft_warp.cuh -- register column FFTs for power-of-two N in {32, 64, 128, 256}.
 //
-// One warp transforms one column.  Four-step factorisation N = M x 32 with
-// n = 32 j + l (l = lane) and k = k1 + M k2:
-//   X[k1 + M k2] = sum_l W_32^{l k2} W_N^{l k1} ( sum_j x[32 j + l] W_M^{j k1} ).
-// Each lane does the M-point DFT of its own elements, applies W_N^{l k1}, then the
-// 32-point DFT across lanes runs as five radix-2 decimation-in-frequency stages over
-// warp shuffles, which leaves lane l holding X[k1 + M brev5(l)].  No shared memory and
-// no block barrier inside the transform.
+// A column of N points in shared memory is transformed by P threads of one warp (a warp
+// holds 32 / P columns), each thread holding R = N / P points in registers:
+//   N = 32: P = 8,  R = 4      N = 64: P = 8, R = 8
+//   N = 128: P = 16, R = 8     N = 256: P = 16, R = 16
+// Four-step factorisation with n = t + P j and k = k1 + R k2 (t < P, j, k1 < R, k2 < P):
+//   Y[k1][t]    = W_N^{t k1} DFT_R(x[t + P j])[k1]                        (step 1)
+//   X[k1 + R k2] = DFT_P(Y[k1][.])[k2]                                     (step 2)
+// Step 2 runs as one P-point DFT per thread when P == R; when P == 2R two neighbouring
+// threads split it into even / odd halves (R-point DFTs) joined by one radix-2 stage
+// over a lane shuffle.  The only data exchange is one pass through the column's own
+// shared memory between the steps (warp-synchronous: no block barrier).  Output in
+// natural order.  Inverse transforms conjugate on the way in and out.
 #pragma once
 #include "fft_green.cuh"
 
-namespace warpfft {
+namespace regfft {
 
 template <typename T2>
 __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
@@ -25,69 +30,120 @@ __device__ __forceinline__ T2 shfl_xor2(T2 v, int m) {
   v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
   return v;
 }
-// forward M-point DFT in registers (M = 1, 2, 4, 8)
-template <int M, typename T2, typename T>
-__device__ __forceinline__ void dft_m(T2* v) {
-  if (M == 2) {
-    T2 a = v[0], b = v[1];
-    v[0].x = a.x + b.x; v[0].y = a.y + b.y;
-    v[1].x = a.x - b.x; v[1].y = a.y - b.y;
-  } else if (M == 4) {
+template <typename T2>
+__device__ __forceinline__ void bfly(T2& a, T2& b) {
+  T2 t = a;
+  a.x = t.x + b.x; a.y = t.y + b.y;
+  b.x = t.x - b.x; b.y = t.y - b.y;
+}
+
+// forward R-point DFT in registers, natural order in and out (R = 2, 4, 8, 16)
+template <int R, typename T2, typename T>
+__device__ __forceinline__ void dft(T2* v) {
+  if (R == 2) {
+    bfly(v[0], v[1]);
+  } else if (R == 4) {
     T2 a = v[0], b = v[1], c = v[2], d = v[3];
-    T2 s0, s1, d0, d1;
-    s0.x = a.x + c.x; s0.y = a.y + c.y; d0.x = a.x - c.x; d0.y = a.y - c.y;
-    s1.x = b.x + d.x; s1.y = b.y + d.y; d1.x = b.x - d.x; d1.y = b.y - d.y;
-    v[0].x = s0.x + s1.x; v[0].y = s0.y + s1.y;
-    v[2].x = s0.x - s1.x; v[2].y = s0.y - s1.y;
-    v[1].x = d0.x + d1.y; v[1].y = d0.y - d1.x;   // d0 - i d1
-    v[3].x = d0.x - d1.y; v[3].y = d0.y + d1.x;   // d0 + i d1
-  } else if (M == 8) {
+    bfly(a, c);  // a = a + c, c = a - c
+    bfly(b, d);  // b = b + d, d = b - d
+    v[0].x = a.x + b.x; v[0].y = a.y + b.y;
+    v[2].x = a.x - b.x; v[2].y = a.y - b.y;
+    v[1].x = c.x + d.y; v[1].y = c.y - d.x;  // c - i d
+    v[3].x = c.x - d.y; v[3].y = c.y + d.x;  // c + i d
+  } else if (R == 8) {
     const T h = (T)0.70710678118654752440;
     T2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
-    dft_m<4, T2, T>(e);
-    dft_m<4, T2, T>(o);
-    T2 t1; t1.x = h * (o[1].x + o[1].y); t1.y = h * (o[1].y - o[1].x); o[1] = t1;
-    T2 t2; t2.x = o[2].y; t2.y = -o[2].x; o[2] = t2;
-    T2 t3; t3.x = h * (o[3].y - o[3].x); t3.y = -h * (o[3].x + o[3].y); o[3] = t3;
+    dft<4, T2, T>(e);
+    dft<4, T2, T>(o);
+    T2 t1; t1.x = h * (o[1].x + o[1].y); t1.y = h * (o[1].y - o[1].x); o[1] = t1;  // W8^1
+    T2 t2; t2.x = o[2].y; t2.y = -o[2].x; o[2] = t2;                               // W8^2
+    T2 t3; t3.x = h * (o[3].y - o[3].x); t3.y = -h * (o[3].x + o[3].y); o[3] = t3;  // W8^3
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       v[k].x = e[k].x + o[k].x; v[k].y = e[k].y + o[k].y;
       v[k + 4].x = e[k].x - o[k].x; v[k + 4].y = e[k].y - o[k].y;
     }
-  }
-}
-
-// Forward DFT of one column of N = 32 M points held as v[j] = x[32 j + lane].
-// On return v[k1] = X[k1 + M brev5(lane)].  tw[k] = exp(-2 pi i k / N).
-template <int M, typename T2, typename T>
-__device__ __forceinline__ void fft(T2* v, const T2* __restrict__ tw) {
-  constexpr int N = 32 * M;
-  const int lane = threadIdx.x & 31;
-  dft_m<M, T2, T>(v);
+  } else if (R == 16) {
+    // W16^k = cos(k pi / 8) - i sin(k pi / 8)
+    const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173;
+    const T h = (T)0.70710678118654752440;
+    T2 e[8], o[8];
 #pragma unroll
-  for (int k1 = 1; k1 < M; k1++) v[k1] = cmul(v[k1], tw[lane * k1]);
+    for (int k = 0; k < 8; k++) { e[k] = v[2 * k]; o[k] = v[2 * k + 1]; }
+    dft<8, T2, T>(e);
+    dft<8, T2, T>(o);
+    const T wr[8] = {(T)1, c1, h, s1, (T)0, -s1, -h, -c1};
+    const T wi[8] = {(T)0, -s1, -h, -c1, (T)-1, -c1, -h, -s1};
 #pragma unroll
-  for (int d = 16; d >= 1; d >>= 1) {
-    const bool upper = (lane & d) != 0;
-    const T2 w = tw[(lane & (d - 1)) * (N / (2 * d))];
+    for (int k = 1; k < 8; k++) {
+      T2 t;
+      t.x = o[k].x * wr[k] - o[k].y * wi[k];
+      t.y = o[k].x * wi[k] + o[k].y * wr[k];
+      o[k] = t;
+    }
 #pragma unroll
-    for (int k1 = 0; k1 < M; k1++) {
-      T2 p = shfl_xor2(v[k1], d);
-      T2 r;
-      if (upper) {
-        T2 diff;
-        diff.x = p.x - v[k1].x;
-        diff.y = p.y - v[k1].y;
-        r = cmul(diff, w);
-      } else {
-        r.x = v[k1].x + p.x;
-        r.y = v[k1].y + p.y;
-      }
-      v[k1] = r;
+    for (int k = 0; k < 8; k++) {
+      v[k].x = e[k].x + o[k].x; v[k].y = e[k].y + o[k].y;
+      v[k + 8].x = e[k].x - o[k].x; v[k + 8].y = e[k].y - o[k].y;
     }
   }
 }
 
-__device__ __forceinline__ int brev5(int l) { return (int)(__brev((unsigned)l) >> 27); }
+template <int N> struct Shape;
+template <> struct Shape<32> { static constexpr int P = 8, R = 4; };
+template <> struct Shape<64> { static constexpr int P = 8, R = 8; };
+template <> struct Shape<128> { static constexpr int P = 16, R = 8; };
+template <> struct Shape<256> { static constexpr int P = 16, R = 16; };
 
-}  // namespace warpfft
+// Transform the column at col (element k at col[pidx(k)]) with thread t of its P threads;
+// tw[k] = exp(-2 pi i k / N) in shared memory.  Every lane of the warp must call this
+// (warp-synchronous shuffles and __syncwarp), each on its own column.
+template <int N, typename T2, typename T, bool INV>
+__device__ __forceinline__ void column(T2* col, const T2* tw, int t) {
+  constexpr int P = Shape<N>::P, R = Shape<N>::R;
+  T2 v[R > P ? R : P];
+#pragma unroll
+  for (int j = 0; j < R; j++) {
+    v[j] = col[pidx(t + P * j)];
+    if (INV) v[j].y = -v[j].y;
+  }
+  dft<R, T2, T>(v);
+#pragma unroll
+  for (int k1 = 1; k1 < R; k1++) v[k1] = cmul(v[k1], tw[t * k1]);
+  __syncwarp();
+#pragma unroll
+  for (int k1 = 0; k1 < R; k1++) col[pidx(k1 * P + t)] = v[k1];
+  __syncwarp();
+  if (P == R) {
+#pragma unroll
+    for (int m = 0; m < P; m++) v[m] = col[pidx(t * P + m)];
+    dft<P, T2, T>(v);
+    __syncwarp();
+#pragma unroll
+    for (int k2 = 0; k2 < P; k2++) {
+      T2 o = v[k2];
+      if (INV) o.y = -o.y;
+      col[pidx(t + R * k2)] = o;
+    }
+  } else {  // P == 2R: threads (k1, h) hold the even (h = 0) / odd (h = 1) half
+    const int k1 = t >> 1, hh = t & 1;
+#pragma unroll
+    for (int m = 0; m < R; m++) v[m] = col[pidx(k1 * P + 2 * m + hh)];
+    dft<R, T2, T>(v);
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+      T2 p = shfl_xor2(v[i], 1);
+      T2 e = hh ? p : v[i], od = hh ? v[i] : p;
+      T2 w = cmul(od, tw[i * R]);  // W_P^i = W_N^{i R}
+      T2 o;
+      o.x = hh ? e.x - w.x : e.x + w.x;
+      o.y = hh ? e.y - w.y : e.y + w.y;
+      if (INV) o.y = -o.y;
+      col[pidx(k1 + R * (hh * R + i))] = o;
+    }
+  }
+  __syncwarp();
+}
+
+}  // namespace regfft

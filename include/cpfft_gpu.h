@@ -140,6 +140,10 @@ int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1,
  */
 int cpfft_green_apply(const double* x, double* y, int flgK);
 
+/* The FP32 form of the same operator (the mixed-precision inner Krylov matvec) on FP32
+ * host arrays; needs CPFFT_PREC_MIXED and, for flgK = 1, a stress update since. */
+int cpfft_green_apply_f32(const float* x, float* y, int flgK);
+
 /*
  * y = G(K4 : x) (flgK = 1) or y = G(x) without any device allocation.  No counterpart in
  * the reference: it is for callers that cannot call cudaMalloc (host programs that give

@@ -162,3 +162,22 @@ def test_load_step_parity(gpulib, oracle, case):
     finally:
         s.close()
         o.close()
+
+
+@pytest.mark.parametrize("N", [32, 64, 128, 256])
+def test_green_fp32_warp_path(gpulib, N):
+    """The FP32 register-FFT passes (powers of two 32-256) against the FP64 operator on the
+    same tangent: agreement to FP32 rounding of an N^3 transform."""
+    r = rve.make_rve(N, 8, 13)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                      gpulib.PREC_MIXED)
+    try:
+        Fn, Fn1 = random_F(N, 1e-3, 4)
+        s.drive_eps_sig(1, 0, Fn, Fn1, want_P=False)
+        x = np.random.default_rng(N).standard_normal((9, N ** 3))
+        for flgK in (True, False):
+            y64 = s.G_K_dF(x, flgK)
+            y32 = s.G_K_dF_f32(x.astype(np.float32), flgK)
+            assert rel(y32, y64) < 1e-5, (flgK, rel(y32, y64))
+    finally:
+        s.close()
