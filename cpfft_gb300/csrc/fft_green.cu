@@ -479,13 +479,22 @@ __global__ void __launch_bounds__(32 * TK / cpw<32 * M>()) wpass_b(typename Vec2
   const int ka0 = blockIdx.x * TK;
   const int c = blockIdx.y, i = blockIdx.z;
   T2* plane = S + ((long long)i * N + c) * (long long)N * H;
-  for (int t = threadIdx.x; t < TK * N; t += blockDim.x) {
-    int row = t / TK, kk = t - row * TK;
-    int ka = ka0 + kk;
-    T2 v;
-    v.x = 0; v.y = 0;
-    if (ka < H) v = plane[(long long)row * H + ka];
-    col[kk * Lp + pidx(row)] = v;
+  // every load of the tile in flight before the first shared-memory store
+  constexpr int NT = 32 * TK / cpw<N>(), E = TK * N / NT;
+  static_assert(E * NT == TK * N, "tile must divide evenly over the block");
+  {
+    T2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, row = t / TK, ka = ka0 + t % TK;
+      v[e].x = 0; v[e].y = 0;
+      if (ka < H) v[e] = plane[(long long)row * H + ka];
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, row = t / TK, kk = t % TK;
+      col[kk * Lp + pidx(row)] = v[e];
+    }
   }
   __syncthreads();
   if (inverse) block_columns<N, T, true>(col, TK, Lp, tw);
@@ -511,14 +520,23 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
   const int ka0 = blockIdx.x * TK;
   const int kb = blockIdx.y;
   const long long cstr = (long long)N * H;
-  for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
-    int kk = t % TK, rem = t / TK;
-    int c = rem % N, i = rem / N;
-    int ka = ka0 + kk;
-    T2 v;
-    v.x = 0; v.y = 0;
-    if (ka < H) v = S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka];
-    col[(i * TK + kk) * Lp + pidx(c)] = v;
+  constexpr int NT = 288, E = 9 * N * TK / NT;
+  static_assert(E * NT == 9 * N * TK, "tile must divide evenly over the block");
+  {
+    T2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, kk = t % TK, rem = t / TK;
+      const int c = rem % N, i = rem / N, ka = ka0 + kk;
+      v[e].x = 0; v[e].y = 0;
+      if (ka < H) v[e] = S[((long long)i * N) * cstr + c * cstr + (long long)kb * H + ka];
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, kk = t % TK, rem = t / TK;
+      const int c = rem % N, i = rem / N;
+      col[(i * TK + kk) * Lp + pidx(c)] = v[e];
+    }
   }
   __syncthreads();
   block_columns<N, T, false>(col, 9 * TK, Lp, tw);
@@ -579,30 +597,55 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
   load_tw(tw, twg, N);
   const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
   const int bl0 = 2 * bp;
-  for (int t = threadIdx.x; t < 9 * N; t += blockDim.x) {
-    int i = t / N, k = t - i * N;
-    long long base = ((long long)i * N + c) * N;
-    int kk = k < H ? k : N - k;
-    T2 X0 = S[(base + bl0) * H + kk], X1 = S[(base + bl0 + 1) * H + kk];
-    if (kk == 0 || kk == N / 2) { X0.y = 0; X1.y = 0; }
-    if (k >= H) { X0.y = -X0.y; X1.y = -X1.y; }
-    T2 z;  // Z = X0 + i X1 (the inverse is taken as conj(FFT(conj Z)))
-    z.x = X0.x - X1.y;
-    z.y = X0.y + X1.x;
-    col[i * Lp + pidx(k)] = z;
+  constexpr int NT = 288, E = 9 * N / NT;
+  static_assert(E * NT == 9 * N, "lines must divide evenly over the block");
+  {
+    T2 X0[E], X1[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
+      const long long base = ((long long)i * N + c) * N;
+      const int kk = k < H ? k : N - k;
+      X0[e] = S[(base + bl0) * H + kk];
+      X1[e] = S[(base + bl0 + 1) * H + kk];
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
+      const int kk = k < H ? k : N - k;
+      T2 a = X0[e], b = X1[e];
+      if (kk == 0 || kk == N / 2) { a.y = 0; b.y = 0; }
+      if (k >= H) { a.y = -a.y; b.y = -b.y; }
+      T2 z;  // Z = X0 + i X1 (the inverse is taken as conj(FFT(conj Z)))
+      z.x = a.x - b.y;
+      z.y = a.y + b.x;
+      col[i * Lp + pidx(k)] = z;
+    }
+  }
+  // the other factor of the fused product, loaded before the transform hides its latency
+  constexpr int EO = 2 * 9 * N / NT;
+  T px[EO];
+  if (dotx) {
+#pragma unroll
+    for (int e = 0; e < EO; e++) {
+      const int t = threadIdx.x + e * NT, l = t / (9 * N), rem = t - l * 9 * N;
+      const int i = rem / N, a = rem - i * N;
+      px[e] = dotx[i * N3 + a + (long long)N * (bl0 + l) + (long long)N * N * c];
+    }
   }
   __syncthreads();
   block_columns<N, T, true>(col, ncols9<N>(), Lp, tw);
   __syncthreads();
   T dsum = 0;
-  for (int t = threadIdx.x; t < 2 * 9 * N; t += blockDim.x) {
-    int l = t / (9 * N), rem = t - l * 9 * N;
-    int i = rem / N, a = rem - i * N;
+#pragma unroll
+  for (int e = 0; e < EO; e++) {
+    const int t = threadIdx.x + e * NT, l = t / (9 * N), rem = t - l * 9 * N;
+    const int i = rem / N, a = rem - i * N;
     T2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
     long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
     const T yv = l ? z.y : z.x;
     y[i * N3 + v] = yv;
-    if (dotx) dsum += dotx[i * N3 + v] * yv;
+    if (dotx) dsum += px[e] * yv;
   }
   if (dotx) {  // block sum (9 warps), fixed order
     __shared__ double wsum[9];
