@@ -530,6 +530,10 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   if (fails) *fails = (int)c->h_stats[1];
   if (predict_iters) *predict_iters = (long long)c->h_stats[2];
   if (rejected) *rejected = (long long)c->h_stats[3];
+  if (c->log)  // per-pass local work (CPFFT_LOG=1)
+    fprintf(stderr, "       stress pass step %d iter %d: update %.4f predictor %.4f per voxel%s\n",
+            step, iter, (double)c->h_stats[0] / (double)c->N3,
+            (double)c->h_stats[2] / (double)c->N3, warm ? " (learned start)" : "");
   if (warm) TRY(mlp_check_error());
   return 0;
 }
