@@ -251,6 +251,8 @@ def config_dict(args, impl):
                         f"{args.grains} Voronoi grains (seed {args.seed}), FCC mm10 Voce",
             "N": args.N, "grains": args.grains, "seed": args.seed,
             "mode": args.mode if impl != "reference" else "fp64",
+            "precond": (args.precond if impl != "reference" and args.mode != "fp64"
+                        else "none (the reference's fftPcg)"),
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
             "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
@@ -278,6 +280,8 @@ def gb300_arm(args):
     solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
     if learned:
         solver.set_mode(prec, 1)
+    if prec == cp.PREC_MIXED and args.precond == "reference":
+        solver.set_precond(cp.PRECOND_REFERENCE)
     tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
     solver.nr3_begin(tolPCG)
     step = 0
@@ -418,6 +422,9 @@ def main():
     # initial guess of the local solves (trained before the timed steps); fp64: plain
     ap.add_argument("--mode", default="learned", choices=["learned", "mixed", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    # preconditioner of the FP32 inner Krylov iterations (mixed / learned): the Green
+    # operator of the mean-tangent reference medium, or none (the reference's plain CG)
+    ap.add_argument("--precond", default="reference", choices=["reference", "none"])
     # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
     # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
     # the benchmark uses the reference example deck's value 1e-5; the equilibrium

@@ -18,6 +18,7 @@ HIST_WORDS = 23
 
 G_REF_SHIFT, G_CENTERED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_NONE, PRECOND_REFERENCE = 0, 1
 
 STATUS = {
     0: "ok", 1: "local mm10 fallback", -1: "CG reached maxIter", -2: "Newton maxIter",
@@ -81,6 +82,7 @@ _FP, _LL = _P(ctypes.c_float), ctypes.c_longlong
 SIGNATURES = {
     "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
     "cpfft_set_mode": (_I, [_I, _I]),
+    "cpfft_set_precond": (_I, [_I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
@@ -229,6 +231,10 @@ class Solver:
 
     def set_mode(self, precision, warm_start=0):
         _check(load_library().cpfft_set_mode(precision, int(warm_start)), "cpfft_set_mode")
+
+    def set_precond(self, precond=PRECOND_REFERENCE):
+        """Reference-medium preconditioner of the mixed-precision inner iterations."""
+        _check(load_library().cpfft_set_precond(int(precond)), "cpfft_set_precond")
 
     # --- learned initial guess of the local solve --------------------------------------
     def learn_log(self, capacity, stride=1, phase=0):

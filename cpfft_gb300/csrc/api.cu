@@ -203,6 +203,12 @@ struct Ctx {
   unsigned long long* stats = nullptr;
   unsigned long long* h_stats = nullptr;
   bool K4f_valid = false;
+  // reference-medium preconditioner of the FP32 inner iterations (cpfft_set_precond)
+  int precond = 0;
+  bool pre_ok = false;     // the current reference medium is usable
+  double* k0sum = nullptr; // (81) component sums of K4f
+  double* h_k0 = nullptr;  // pinned (81) copy
+  float* h_pre = nullptr;  // pinned: 36 acoustic coefficients + 81 entries of K0
   // FFT_nr3 locals that persist across steps (Fortran DATA => SAVE, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
   // counters of the current step
@@ -273,11 +279,14 @@ void free_ctx(Ctx* c) {
   void* ptrs[] = {c->log_X, c->log_T, c->log_n,
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
-                  c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats};
+                  c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
+                  c->k0sum};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->h_stats) cudaFreeHost(c->h_stats);
+  if (c->h_k0) cudaFreeHost(c->h_k0);
+  if (c->h_pre) cudaFreeHost(c->h_pre);
   if (c->kt_ready) {
     for (int i = 0; i < 2 * Ctx::KT_CAP; i++) cudaEventDestroy(c->kt_ev[i]);
     cudaEventDestroy(c->step_ev[0]);
@@ -337,6 +346,114 @@ int matvec32_alpha(Ctx* c, const float* x, float* y) {
   TRY(kt_stop(c));
   if (np) CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
   else CK(dev_dot_f(x, y, 9 * c->N3, c->part, c->sc, SC_PAP, OP_ALPHA, c->st));
+  return 0;
+}
+
+// ---- reference-medium preconditioning of the FP32 inner iterations -------------------
+// The inner system G(K : x) = b is solved as G0(K : x) = G0(b), G0 the Green operator of a
+// homogeneous reference medium K0 (the symmetrised volume average of the current tangent).
+// Both have the same solutions on compatible fields (G0 o G = G0, and G0 annihilates
+// exactly the divergence-free fields), and G0(K : .) is self-adjoint in the inner product
+// <a, b>_K0 on compatible fields, where CG on it is CG preconditioned by G(K0 : .).  Its
+// iteration count follows the contrast of K against K0 instead of against the identity.
+
+// Sums of K4f (after a stress update or an uploaded tangent), read back with the stream's
+// next synchronisation; reference_build then forms the medium.
+int reference_reduce(Ctx* c) {
+  if (!c->k0sum) {
+    TRY(dalloc(c->k0sum, 81 * sizeof(double)));
+    if (cudaMallocHost((void**)&c->h_k0, 81 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost((void**)&c->h_pre, (36 + 81) * sizeof(float)) != cudaSuccess) {
+      cpfft_set_error("cudaMallocHost failed");
+      return CPFFT_ERR_NO_MEMORY;
+    }
+  }
+  CK(dev_mean81(c->K4f, c->N3, c->part, c->k0sum, c->st));
+  CK(cudaMemcpyAsync(c->h_k0, c->k0sum, 81 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  return 0;
+}
+
+// K0 = sym(mean K4) / its largest entry; usable when the acoustic tensor
+// A0(n)_ik = K0_ijkl n_j n_l is positive definite on a dense set of directions n.
+int reference_build(Ctx* c) {
+  double K0[81], mx = 0.0;
+  for (int I = 0; I < 9; I++)
+    for (int J = 0; J < 9; J++) {
+      K0[9 * I + J] = 0.5 * (c->h_k0[9 * I + J] + c->h_k0[9 * J + I]) / (double)c->N3;
+      mx = std::max(mx, std::fabs(K0[9 * I + J]));
+    }
+  c->pre_ok = false;
+  if (!(mx > 0.0) || !std::isfinite(mx)) return 0;
+  for (double& k : K0) k /= mx;
+  static const int RI[6] = {0, 1, 2, 0, 1, 0}, RK[6] = {0, 1, 2, 1, 2, 2};
+  static const int PJ[6] = {0, 1, 2, 0, 1, 0}, PL[6] = {0, 1, 2, 1, 2, 2};
+  double coef[36];
+  for (int r = 0; r < 6; r++)
+    for (int m = 0; m < 6; m++) {
+      const int i = RI[r], k = RK[r], j = PJ[m], l = PL[m];
+      double v = K0[9 * (3 * i + j) + 3 * k + l];
+      if (j != l) v += K0[9 * (3 * i + l) + 3 * k + j];
+      coef[6 * r + m] = v;
+    }
+  // positive definiteness (Sylvester) with a margin, on 64 x 128 directions of the sphere
+  const double pi = 3.14159265358979323846;
+  double lo = 1e300, hi = 0.0;
+  for (int it = 0; it <= 64; it++)
+    for (int ip = 0; ip < 128; ip++) {
+      const double th = pi * it / 64.0, ph = 2.0 * pi * ip / 128.0;
+      const double n[3] = {std::sin(th) * std::cos(ph), std::sin(th) * std::sin(ph), std::cos(th)};
+      const double pr[6] = {n[0] * n[0], n[1] * n[1], n[2] * n[2], n[0] * n[1], n[1] * n[2], n[0] * n[2]};
+      double a[6];
+      for (int r = 0; r < 6; r++) {
+        a[r] = 0.0;
+        for (int m = 0; m < 6; m++) a[r] += coef[6 * r + m] * pr[m];
+      }
+      const double m2 = a[0] * a[1] - a[3] * a[3];
+      const double det = a[0] * (a[1] * a[2] - a[4] * a[4]) - a[3] * (a[3] * a[2] - a[4] * a[5]) +
+                         a[5] * (a[3] * a[4] - a[1] * a[5]);
+      const double tr = a[0] + a[1] + a[2];
+      if (!(a[0] > 0.0 && m2 > 0.0 && det > 0.0 && tr > 0.0)) return 0;
+      // det / tr^3 bounds the smallest eigenvalue's share from below
+      lo = std::min(lo, det / (tr * tr * tr));
+      hi = std::max(hi, tr);
+    }
+  if (c->log)
+    fprintf(stderr, "         reference medium: min det/tr^3 of the acoustic tensor %.3e%s\n", lo,
+            lo > 1.0e-9 ? "" : " (not used)");
+  if (!(lo > 1.0e-9)) return 0;
+  for (int k = 0; k < 36; k++) c->h_pre[k] = (float)coef[k];
+  for (int k = 0; k < 81; k++) c->h_pre[36 + k] = (float)K0[k];
+  CK(green_set_reference(c->h_pre, c->st));
+  CK(dev_set_k0(c->h_pre + 36, c->st));
+  c->pre_ok = true;
+  return 0;
+}
+
+// the preconditioned operator is a projection for odd N or the centered mapping
+bool pre_applies(const Ctx* c) {
+  return c->precond && c->prec == CPFFT_PREC_MIXED &&
+         (c->g.gmap == CPFFT_G_CENTERED || (c->N & 1));
+}
+
+// y = G0(K4f : x) (flgK = 1) or G0(x); with want_alpha also sc[SC_PAP] = <K4f : x, x>
+// (= <x, y>_K0) and alpha = rr / pAp
+int matvec32_pre(Ctx* c, const float* x, float* y, int flgK, bool want_alpha) {
+  c->f32_matvecs++;
+  GridDesc g = c->g;
+  g.pre = 1;
+  int np = 0;
+  kt_start(c, KT_G32);
+  TRY(cuda_check(green_apply_dot<float>(x, c->K4f, flgK, y, c->Sf, c->twf, g, c->st,
+                                        want_alpha ? c->part : nullptr, &np),
+                 "green_apply fp32 (reference medium)"));
+  TRY(kt_stop(c));
+  if (want_alpha) {
+    if (!np) {
+      cpfft_set_error("internal: the preconditioned product was not fused");
+      return CPFFT_ERR_CUDA;
+    }
+    CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
+  }
   return 0;
 }
 
@@ -424,6 +541,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
   TRY(read_scalar(c, SC_RR, &rr_prev));
   int it = 0;
   bool converged = false;
+  int restarts = 0;
   for (;;) {
     TRY(matvec32_alpha(c, c->pf, c->Apf));
     CK(dev_cg_xr<float>(c->xf, c->rf, c->pf, c->Apf, n, c->part, c->sc, c->st));
@@ -434,6 +552,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
     const double rest = std::sqrt(rr) / scale;
     if (rest < delta * maxr || rest <= tolb || rest <= tol || it >= maxIter) {
       // reliable update
+      restarts++;
       CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
       CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
       TRY(matvec64(c, c->w2, c->Ap, 0));
@@ -463,12 +582,115 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
   *iters = it;
   c->cg_iters += it;
   c->cg_solves++;
+  if (c->log)
+    fprintf(stderr, "         cg (mixed): %d iterations, %d restarts, |r|/|b| %.2e\n", it, restarts,
+            rn / n2b);
   if (!converged) { cpfft_set_error("mixed-precision CG did not converge"); return CPFFT_ERR_CG_MAXIT; }
   return 0;
 }
 
+// Mixed precision with the reference-medium preconditioner: FP32 CG on G0(K : x) = G0(r)
+// in the K0 inner product, with the same reliable updates, FP64 residual b - G(K4 : x),
+// FP64 projection of each correction and the reference's stop test as cg_mixed.  After a
+// reliable update the recursion restarts from G0 of the true residual.
+int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
+  const long long n = 9 * c->N3;
+  const int maxIter = 2000;
+  const double delta = 1.0e-2;
+  *iters = 0;
+  if (!use_x0) CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
+  double n2b;
+  TRY(dnrm2(c, b, &n2b));
+  if (!(tol > 2.220446049250313e-16 && tol < 1.0)) return CPFFT_ERR_CG_TOL;
+  if (!std::isfinite(n2b)) { cpfft_set_error("non-finite CG right-hand side"); return CPFFT_ERR_NONFINITE; }
+  if (n2b <= 2.220446049250313e-16) return 0;
+  if (!c->K4f_valid) {
+    cpfft_set_error("mixed precision CG needs the FP32 tangent of a stress update");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const double tolb = tol * n2b;
+  double rn = n2b;
+  if (use_x0) {
+    TRY(matvec64(c, x, c->Ap, 1));
+    CK(dev_sub(c->w, b, c->Ap, n, c->st));
+    TRY(dnrm2(c, c->w, &rn));
+    if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    if (rn <= tolb || rn <= tol) {
+      c->cg_solves++;
+      return 0;
+    }
+  } else {
+    CK(cudaMemcpyAsync(c->w, b, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+  }
+  // preconditioned residual rf = G0(w / ||w||)
+  double scale = 1.0 / rn;
+  CK(dev_to_f32(c->Apf, c->w, scale, n, c->st));
+  TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
+  CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+  CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RR, OP_STORE, c->st));
+  double rr_prev;
+  TRY(read_scalar(c, SC_RR, &rr_prev));
+  double rr0 = rr_prev;  // <r, r>_K0 at the last restart
+  int it = 0;
+  bool converged = false;
+  int restarts = 0;
+  for (;;) {
+    TRY(matvec32_pre(c, c->pf, c->Apf, 1, true));
+    CK(dev_cg_xr_k0(c->xf, c->rf, c->pf, c->Apf, c->N3, c->part, c->sc, c->st));
+    it++;
+    double rr;
+    TRY(read_scalar(c, SC_RRNEW, &rr));
+    if (!std::isfinite(rr)) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    // the preconditioned residual's reduction since the restart, and the true residual
+    // it predicts
+    const double red = std::sqrt(std::max(rr, 0.0) / rr0), est = rn * red;
+    if (red < delta || est <= tolb || est <= tol || it >= maxIter) {
+      // reliable update: x += G(xf / scale) in FP64, true residual, restart
+      restarts++;
+      CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
+      CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
+      TRY(matvec64(c, c->w2, c->Ap, 0));
+      CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
+      TRY(matvec64(c, x, c->Ap, 1));
+      CK(dev_sub(c->w, b, c->Ap, n, c->st));
+      TRY(dnrm2(c, c->w, &rn));
+      if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
+      if (rn <= tolb || rn <= tol) { converged = true; break; }
+      if (it >= maxIter) break;
+      const double nscale = 1.0 / rn, k = nscale / scale;
+      CK(dev_to_f32(c->Apf, c->w, nscale, n, c->st));
+      TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
+      CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+      CK(dev_scale_f(c->pf, (float)k, n, c->st));
+      CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+      TRY(read_scalar(c, SC_RRNEW, &rr));
+      c->h_sc[SC_BETA] = rr / (rr_prev * k * k);
+      CK(cudaMemcpyAsync(c->sc + SC_BETA, c->h_sc + SC_BETA, sizeof(double),
+                         cudaMemcpyHostToDevice, c->st));
+      scale = nscale;
+      rr0 = rr;
+    }
+    CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+    rr_prev = rr;
+  }
+  *iters = it;
+  c->cg_iters += it;
+  c->cg_solves++;
+  if (c->log)
+    fprintf(stderr, "         cg (mixed, reference medium): %d iterations, %d restarts, |r|/|b| %.2e\n", it, restarts,
+            rn / n2b);
+  if (!converged) { cpfft_set_error("mixed-precision CG did not converge"); return CPFFT_ERR_CG_MAXIT; }
+  return 0;
+}
+
+int cg_mixed_any(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
+  if (pre_applies(c) && c->pre_ok) return cg_mixed_pre(c, b, x, tol, iters, use_x0);
+  return cg_mixed(c, b, x, tol, iters, use_x0);
+}
+
 int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
-  return c->prec == CPFFT_PREC_MIXED ? cg_mixed(c, b, x, tol, iters, false)
+  return c->prec == CPFFT_PREC_MIXED ? cg_mixed_any(c, b, x, tol, iters, false)
                                      : cg64(c, b, x, tol, iters);
 }
 
@@ -524,8 +746,11 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   CK(launch_stress(a, warm, c->st));
   TRY(kt_stop(c));
   c->K4f_valid = a.K4f != nullptr;
+  const bool reduce = c->K4f_valid && pre_applies(c);
+  if (reduce) TRY(reference_reduce(c));
   CK(cudaMemcpyAsync(c->h_stats, c->stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
   TRY(sync(c));
+  if (reduce) TRY(reference_build(c));
   if (local_iters) *local_iters = (long long)c->h_stats[0];
   if (fails) *fails = (int)c->h_stats[1];
   if (predict_iters) *predict_iters = (long long)c->h_stats[2];
@@ -558,7 +783,7 @@ int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
     if (warm) {
       if (c->th_valid)
         CK(cudaMemcpyAsync(c->io, c->th_x + i * n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
-      TRY(cg_mixed(c, c->b, c->io, tolPCG, &its, c->th_valid));
+      TRY(cg_mixed_any(c, c->b, c->io, tolPCG, &its, c->th_valid));
       CK(cudaMemcpyAsync(c->th_x + i * n, c->io, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
     } else {
       TRY(cg(c, c->b, c->io, tolPCG, &its));
@@ -819,6 +1044,24 @@ int cpfft_set_mode(int precision, int warm_start) {
   return 0;
 }
 
+int cpfft_set_precond(int precond) {
+  TRY(need_ctx());
+  if (precond != CPFFT_PRECOND_NONE && precond != CPFFT_PRECOND_REFERENCE) {
+    cpfft_set_error("cpfft_set_precond: unknown preconditioner %d", precond);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  Ctx* c = g_ctx;
+  c->precond = precond;
+  c->pre_ok = false;
+  // the medium of the current FP32 tangent, if there is one
+  if (c->K4f_valid && pre_applies(c)) {
+    TRY(reference_reduce(c));
+    TRY(sync(c));
+    TRY(reference_build(c));
+  }
+  return 0;
+}
+
 int cpfft_learn_log(long long capacity, int stride, int phase) {
   TRY(need_ctx());
   Ctx* c = g_ctx;
@@ -900,6 +1143,11 @@ int cpfft_set_K4(const double* K4) {
     CK(cudaMemcpyAsync(c->K4f, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
     TRY(sync(c));
     c->K4f_valid = true;
+    if (pre_applies(c)) {
+      TRY(reference_reduce(c));
+      TRY(sync(c));
+      TRY(reference_build(c));
+    }
   }
   return sync(c);
 }

@@ -168,11 +168,85 @@ __device__ __forceinline__ void ghat_acc(const T2* A, int q0, int q1, int q2, T 
   }
 }
 
+// Acoustic-tensor coefficients of the reference medium K0 (green_set_reference).
+__constant__ float c_acoef[36];
+
+// Reference-medium Green operator: (Ghat0(q):X)_ij = (A0(q)^-1 X q)_i q_j with
+// A0(q)_ik = sum_jl K0_ijkl q_j q_l (Moulinec-Suquet's Gamma0 for the stiffness K0),
+// accumulated into out with weight w.  A0 is symmetric (K0 has the major symmetry) and
+// inverted through its cofactors; a direction where it is not positive definite
+// contributes nothing.
+template <typename T2, typename T>
+__device__ __forceinline__ void ghat0_acc(const T2* A, int q0, int q1, int q2, T w, T2* out) {
+  if (q0 == 0 && q1 == 0 && q2 == 0) return;
+  const T q[3] = {(T)q0, (T)q1, (T)q2};
+  const T pr[6] = {q[0] * q[0], q[1] * q[1], q[2] * q[2], q[0] * q[1], q[1] * q[2], q[0] * q[2]};
+  T a[6];
+#pragma unroll
+  for (int r = 0; r < 6; r++) {
+    T s = 0;
+#pragma unroll
+    for (int m = 0; m < 6; m++) s += (T)c_acoef[6 * r + m] * pr[m];
+    a[r] = s;
+  }
+  // a = (a00, a11, a22, a01, a12, a02)
+  const T c00 = a[1] * a[2] - a[4] * a[4], c01 = a[5] * a[4] - a[3] * a[2];
+  const T c02 = a[3] * a[4] - a[5] * a[1], c11 = a[0] * a[2] - a[5] * a[5];
+  const T c12 = a[3] * a[5] - a[0] * a[4], c22 = a[0] * a[1] - a[3] * a[3];
+  const T det = a[0] * c00 + a[3] * c01 + a[5] * c02;
+  if (!(det > (T)0)) return;
+  const T s = w / det;
+  T2 d[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    d[i].x = A[3 * i].x * q[0] + A[3 * i + 1].x * q[1] + A[3 * i + 2].x * q[2];
+    d[i].y = A[3 * i].y * q[0] + A[3 * i + 1].y * q[1] + A[3 * i + 2].y * q[2];
+  }
+  T2 e[3];
+  e[0].x = (c00 * d[0].x + c01 * d[1].x + c02 * d[2].x) * s;
+  e[0].y = (c00 * d[0].y + c01 * d[1].y + c02 * d[2].y) * s;
+  e[1].x = (c01 * d[0].x + c11 * d[1].x + c12 * d[2].x) * s;
+  e[1].y = (c01 * d[0].y + c11 * d[1].y + c12 * d[2].y) * s;
+  e[2].x = (c02 * d[0].x + c12 * d[1].x + c22 * d[2].x) * s;
+  e[2].y = (c02 * d[0].y + c12 * d[1].y + c22 * d[2].y) * s;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      out[3 * i + j].x += e[i].x * q[j];
+      out[3 * i + j].y += e[i].y * q[j];
+    }
+}
+
+// the spectral operator of pass C: the reference medium when selected (FP32 only)
+template <typename T2, typename T>
+__device__ __forceinline__ void green_acc(bool pre, const T2* A, int q0, int q1, int q2, T w,
+                                          T2* out) {
+  if (sizeof(T) == 4 && pre) ghat0_acc<T2, T>(A, q0, q1, q2, w, out);
+  else ghat_acc<T2, T>(A, q0, q1, q2, w, out);
+}
+
+// one partial sum per block of the per-thread values d (fixed order), into *dst
+template <int NT>
+__device__ __forceinline__ void block_partial(double d, double* dst) {
+  __shared__ double wsum[NT / 32];
+  for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0;
+    for (int k = 0; k < NT / 32; k++) b += wsum[k];
+    *dst = b;
+  }
+}
+
 // ---- pass A: K:x + real-to-complex transform along a --------------------------------
+// part != nullptr (with flgK): one partial sum per block of <K : x, x> over its voxels
 template <typename T, typename TK>
 __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK* __restrict__ K4,
                                               int flgK, typename Vec2<T>::t* __restrict__ S,
-                                              GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
+                                              GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
+                                              double* __restrict__ part) {
   using T2 = typename Vec2<T>::t;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int N = g.N, H = g.H, Lp = padlen(N);
@@ -184,6 +258,7 @@ __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK*
   const int npair = (N + 1) / 2;
   const int bp = blockIdx.x % npair, c = blockIdx.x / npair;
   const int bl0 = 2 * bp, bl1 = 2 * bp + 1;
+  T dsum = 0;
   for (int t = threadIdx.x; t < 2 * N; t += blockDim.x) {
     int l = t / N, a = t - l * N;
     int b = l ? bl1 : bl0;
@@ -200,6 +275,7 @@ __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK*
 #pragma unroll
           for (int j = 0; j < 9; j++) s += (T)K4[(9 * i + j) * N3 + v] * xv[j];
           y[i] = s;
+          dsum += s * xv[i];
         }
       } else {
 #pragma unroll
@@ -215,6 +291,7 @@ __global__ void __launch_bounds__(256) pass_a(const T* __restrict__ x, const TK*
       else b0[i * Lp + pidx(a)].y = y[i];
     }
   }
+  if (part) block_partial<256>((double)dsum, part + blockIdx.x);
   __syncthreads();
   T2* r = fft_cols<T2, T>(b0, b1, 9, Lp, g.plan, tw);
   // unpack the two real lines: X0 = (Z + conj Z(-k))/2, X1 = (Z - conj Z(-k))/(2i)
@@ -315,10 +392,10 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
       int m0 = qmap((N - kc) % N, N, Nh, gm), m1 = qmap((N - kb) % N, N, Nh, gm),
           m2 = qmap((N - ka) % N, N, Nh, gm);
       if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
-        ghat_acc<T2, T>(A, p0, p1, p2, scale, out);
+        green_acc<T2, T>(g.pre, A, p0, p1, p2, scale, out);
       } else {
-        ghat_acc<T2, T>(A, p0, p1, p2, (T)0.5 * scale, out);
-        ghat_acc<T2, T>(A, m0, m1, m2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, A, p0, p1, p2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, A, m0, m1, m2, (T)0.5 * scale, out);
       }
     }
     // conjugate for the inverse transform
@@ -410,10 +487,12 @@ __device__ __forceinline__ void block_columns(typename Vec2<T>::t* base, int nco
     regfft::column<N, T2, T, INV>(base + (g * CPW + lane / P) * Lp, tw, lane % P);
 }
 
+// part != nullptr (with flgK): one partial sum per block of <K : x, x> over its voxels
 template <int M, typename T, typename TK>
 __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK* __restrict__ K4,
                                                int flgK, typename Vec2<T>::t* __restrict__ S,
-                                               GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
+                                               GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
+                                               double* __restrict__ part) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
   const int Lp = padlen(N);
@@ -424,6 +503,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
   load_tw(tw, twg, N);
   const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
   const int bl0 = 2 * bp;
+  T dsum = 0;
   for (int t = threadIdx.x; t < 2 * N; t += blockDim.x) {
     int l = t / N, a = t - l * N;
     long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
@@ -438,6 +518,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
 #pragma unroll
         for (int j = 0; j < 9; j++) s += (T)K4[(9 * i + j) * N3 + v] * xv[j];
         y[i] = s;
+        dsum += s * xv[i];
       }
     } else {
 #pragma unroll
@@ -449,6 +530,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
       else col[i * Lp + pidx(a)].y = y[i];
     }
   }
+  if (part) block_partial<288>((double)dsum, part + blockIdx.x);
   __syncthreads();
   block_columns<N, T, false>(col, ncols9<N>(), Lp, tw);
   __syncthreads();
@@ -558,10 +640,10 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
       int m0 = qmap((N - kc) & (N - 1), N, Nh, gm), m1 = qmap((N - kb) & (N - 1), N, Nh, gm),
           m2 = qmap((N - ka) & (N - 1), N, Nh, gm);
       if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
-        ghat_acc<T2, T>(A, p0, p1, p2, scale, out);
+        green_acc<T2, T>(g.pre, A, p0, p1, p2, scale, out);
       } else {
-        ghat_acc<T2, T>(A, p0, p1, p2, (T)0.5 * scale, out);
-        ghat_acc<T2, T>(A, m0, m1, m2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, A, p0, p1, p2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, A, m0, m1, m2, (T)0.5 * scale, out);
       }
     }
 #pragma unroll
@@ -688,14 +770,18 @@ void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* 
                   double* part) {
   constexpr int N = 32 * M, H = N / 2 + 1, TC = wtile_c<T>();
   constexpr int NA = ncols9<N>(), TB = 32 * WTILE_B / cpw<N>();
-  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, flgK, S, g, tw);
+  // the fused product: <K : x, x> in pass A for the reference-medium operator (where it
+  // equals <x, y> in the K0 inner product), else <x, y> in pass E
+  double* part_a = g.pre ? part : nullptr;
+  double* part_e = g.pre ? nullptr : part;
+  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, flgK, S, g, tw, part_a);
   dim3 gb((H + WTILE_B - 1) / WTILE_B, N, 9);
   wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 0);
   dim3 gc((H + TC - 1) / TC, N);
   wpass_c<M, T, TC><<<gc, 288, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
   wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
-  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw, part ? x : nullptr,
-                                                            part);
+  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw, part_e ? x : nullptr,
+                                                            part_e);
 }
 
 template <typename T>
@@ -774,7 +860,11 @@ cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Ve
   g.tkb = 16;
   g.tkc = tile_c<T>();
   const int npair = (N + 1) / 2;
-  pass_a<T, T><<<npair * N, 256, smem_a<T>(N), st>>>(x, K4, flgK, S, g, tw);
+  // the reference-medium operator's product <K : x, x> is summed in pass A; the plain
+  // operator's <x, y> is left to the caller on this path
+  double* part_a = (g.pre && part && flgK) ? part : nullptr;
+  if (part_a && nparts) *nparts = npair * N;
+  pass_a<T, T><<<npair * N, 256, smem_a<T>(N), st>>>(x, K4, flgK, S, g, tw, part_a);
   dim3 gb((H + g.tkb - 1) / g.tkb, N, 9);
   pass_b<T><<<gb, 256, smem_b<T>(N, g.tkb), st>>>(S, g, tw, 0);
   dim3 gc((H + g.tkc - 1) / g.tkc, N);
@@ -789,6 +879,10 @@ template <typename T>
 cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
   return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr);
+}
+
+cudaError_t green_set_reference(const float* coef36, cudaStream_t st) {
+  return cudaMemcpyToSymbolAsync(c_acoef, coef36, 36 * sizeof(float), 0, cudaMemcpyHostToDevice, st);
 }
 
 template cudaError_t green_setup<double>(int);

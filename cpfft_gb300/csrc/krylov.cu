@@ -194,6 +194,106 @@ __global__ void __launch_bounds__(RB) k_sum9(const double* __restrict__ x, long 
   }
 }
 
+// ---- K0-weighted forms of the reference-medium preconditioned FP32 CG ----------------
+// The CG of the preconditioned operator G0(K : .) runs in the inner product
+// <a, b>_K0 = sum_v a_v . (K0 b_v), K0 the (normalised, symmetrised) 9x9 reference stiffness.
+__constant__ float c_k0[81];
+
+__device__ __forceinline__ float k0_form(const float* a, const float* b) {
+  float s = 0.f;
+#pragma unroll
+  for (int i = 0; i < 9; i++) {
+    float t = 0.f;
+#pragma unroll
+    for (int j = 0; j < 9; j++) t += c_k0[9 * i + j] * b[j];
+    s += a[i] * t;
+  }
+  return s;
+}
+
+// x += alpha p ; r -= alpha Ap ; partial <r, r>_K0 -- one voxel's 9 components per thread
+// (component-major fields), four voxels at a time with 16-byte accesses when N3 % 4 == 0
+__global__ void __launch_bounds__(RB) k_cg_xr_k0(float* __restrict__ x, float* __restrict__ r,
+                                                 const float* __restrict__ p,
+                                                 const float* __restrict__ Ap, long long N3,
+                                                 const double* __restrict__ sc,
+                                                 double* __restrict__ part) {
+  const float alpha = (float)sc[SC_ALPHA];
+  const long long stride = (long long)gridDim.x * RB, t0 = (long long)blockIdx.x * RB + threadIdx.x;
+  float s = 0.f;
+  if ((N3 & 3) == 0) {
+    const long long n4 = N3 >> 2;
+    for (long long v = t0; v < n4; v += stride) {
+      float rv[4][9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        const long long k = i * n4 + v;
+        float4 xv = reinterpret_cast<float4*>(x)[k];
+        const float4 pv = reinterpret_cast<const float4*>(p)[k];
+        float4 qv = reinterpret_cast<float4*>(r)[k];
+        const float4 av = reinterpret_cast<const float4*>(Ap)[k];
+        xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+        qv.x -= alpha * av.x; qv.y -= alpha * av.y; qv.z -= alpha * av.z; qv.w -= alpha * av.w;
+        reinterpret_cast<float4*>(x)[k] = xv;
+        reinterpret_cast<float4*>(r)[k] = qv;
+        rv[0][i] = qv.x; rv[1][i] = qv.y; rv[2][i] = qv.z; rv[3][i] = qv.w;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) s += k0_form(rv[u], rv[u]);
+    }
+  } else {
+    for (long long v = t0; v < N3; v += stride) {
+      float rv[9];
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        const long long k = i * N3 + v;
+        x[k] += alpha * p[k];
+        rv[i] = r[k] - alpha * Ap[k];
+        r[k] = rv[i];
+      }
+      s += k0_form(rv, rv);
+    }
+  }
+  double sb = block_sum((double)s);
+  if (threadIdx.x == 0) part[blockIdx.x] = sb;
+}
+
+// partial <a, b>_K0
+__global__ void __launch_bounds__(RB) k_dot_k0(const float* __restrict__ a, const float* __restrict__ b,
+                                               long long N3, double* __restrict__ part) {
+  float s = 0.f;
+  for (long long v = (long long)blockIdx.x * RB + threadIdx.x; v < N3; v += (long long)gridDim.x * RB) {
+    float av[9], bv[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) { av[i] = a[i * N3 + v]; bv[i] = b[i * N3 + v]; }
+    s += k0_form(av, bv);
+  }
+  double sb = block_sum((double)s);
+  if (threadIdx.x == 0) part[blockIdx.x] = sb;
+}
+
+// component sums of an (81, N3) FP32 field: part[m * gridDim.x + blockIdx.x]
+__global__ void __launch_bounds__(RB) k_sum81(const float* __restrict__ K, long long N3,
+                                              double* __restrict__ part) {
+  const int m = blockIdx.y;
+  double s = 0.0;
+  for (long long v = (long long)blockIdx.x * RB + threadIdx.x; v < N3; v += (long long)gridDim.x * RB)
+    s += (double)K[m * N3 + v];
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[m * gridDim.x + blockIdx.x] = s;
+}
+
+// out[m] = sum of the np partials of row m (one block of 64 threads per row, np <= 64)
+__global__ void __launch_bounds__(64) k_final_rows(const double* __restrict__ part, int np,
+                                                   double* __restrict__ out) {
+  __shared__ double ws[2];
+  double v = threadIdx.x < np ? part[blockIdx.x * np + threadIdx.x] : 0.0;
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) out[blockIdx.x] = ws[0] + ws[1];
+}
+
 int grid_for(long long n, int bs) {
   long long b = (n + bs - 1) / bs;
   return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
@@ -287,4 +387,26 @@ cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, in
   for (int c = 0; c < 9; c++)
     k_final<<<1, 1024, 0, st>>>(part + c * NPART, NPART, sc, slot0 + c, OP_STORE);
   return counted(10);
+}
+
+cudaError_t dev_set_k0(const float* k0, cudaStream_t st) {
+  return cudaMemcpyToSymbolAsync(c_k0, k0, 81 * sizeof(float), 0, cudaMemcpyHostToDevice, st);
+}
+cudaError_t dev_cg_xr_k0(float* x, float* r, const float* p, const float* Ap, long long N3,
+                         double* part, double* sc, cudaStream_t st) {
+  k_cg_xr_k0<<<NPART, RB, 0, st>>>(x, r, p, Ap, N3, sc, part);
+  k_final<<<1, 1024, 0, st>>>(part, NPART, sc, SC_RRNEW, OP_BETA);
+  return counted(2);
+}
+cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, double* part, double* sc,
+                       int slot, int op, cudaStream_t st) {
+  k_dot_k0<<<NPART, RB, 0, st>>>(a, b, N3, part);
+  k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
+  return counted(2);
+}
+cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81, cudaStream_t st) {
+  constexpr int NB = 64;
+  k_sum81<<<dim3(NB, 81), RB, 0, st>>>(K, N3, part);
+  k_final_rows<<<81, 64, 0, st>>>(part, NB, sc81);
+  return counted(2);
 }

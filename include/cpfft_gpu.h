@@ -121,6 +121,19 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg,
  * solve (0/1).  Extensions with no counterpart in the reference. */
 int cpfft_set_mode(int precision, int warm_start);
 
+/* Preconditioner of the FP32 inner iterations of CPFFT_PREC_MIXED (extension; the
+ * reference's fftPcg, src/FFT_nr3.f:214-360, is unpreconditioned, and so is the FP64
+ * path here).  CPFFT_PRECOND_REFERENCE solves G0(K : x) = G0(b) instead of
+ * G(K : x) = b, G0 the Green operator of a homogeneous reference medium K0 = the
+ * symmetrised volume average of the current tangent, recomputed after every stress
+ * update.  Same solutions (both equations say K : x - b' is divergence free), the same
+ * FP64 residual b - G(K : x) and stop test; fewer iterations.  It applies to odd N and to
+ * CPFFT_G_CENTERED (where the Green operator is a projection); elsewhere, or when the
+ * averaged tangent is not strongly elliptic, the plain inner iteration runs. */
+#define CPFFT_PRECOND_NONE       0
+#define CPFFT_PRECOND_REFERENCE  1
+int cpfft_set_precond(int precond);
+
 /*
  * Stress update of every voxel: replaces drive_eps_sig(step, iter)
  * (src/drive_eps_sig.f:16-45, do_nleps_block :57-340, rstgp1/mm10 below it).

@@ -91,10 +91,12 @@ def test_green_parity(gpulib, oracle, N, gmap):
         o.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_cg_parity(gpulib, oracle, precision):
+@pytest.mark.parametrize("precision,precond", [(0, 0), (1, 0), (1, 1)])
+def test_cg_parity(gpulib, oracle, precision, precond):
     N = 9
     r, s, o = make_pair(gpulib, oracle, N, precision=precision)
+    if precond:
+        s.set_precond(gpulib.PRECOND_REFERENCE)
     try:
         Fn, Fn1 = random_F(N, 1e-3, 3)
         _, K, _ = s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False, want_K4=True)
@@ -130,7 +132,8 @@ def test_tangent_homo_parity(gpulib, oracle):
         o.close()
 
 
-@pytest.mark.parametrize("case", ["fcc_voce_odd", "faithful_j22", "even_centered", "mixed"])
+@pytest.mark.parametrize("case", ["fcc_voce_odd", "faithful_j22", "even_centered", "mixed",
+                                  "mixed_precond"])
 def test_load_step_parity(gpulib, oracle, case):
     cr = dict(rve.FCC_VOCE)
     N, gmap, inc, nsteps, precision, tolP = 9, 0, 1e-3, 3, 0, 1e-9
@@ -139,10 +142,12 @@ def test_load_step_parity(gpulib, oracle, case):
         inc = 2.5e-4
     elif case == "even_centered":
         N, gmap, nsteps = 8, 1, 2
-    elif case == "mixed":
+    elif case in ("mixed", "mixed_precond"):
         precision, tolP = 1, 1e-6
     r, s, o = make_pair(gpulib, oracle, N, ngr=4, seed=21, gmap=gmap, crystal=cr,
                         precision=precision)
+    if case == "mixed_precond":
+        s.set_precond(gpulib.PRECOND_REFERENCE)
     load = rve.uniaxial_tension(inc * 20, 20)
     try:
         s.nr3_begin(1e-10)
@@ -179,5 +184,32 @@ def test_green_fp32_warp_path(gpulib, N):
             y64 = s.G_K_dF(x, flgK)
             y32 = s.G_K_dF_f32(x.astype(np.float32), flgK)
             assert rel(y32, y64) < 1e-5, (flgK, rel(y32, y64))
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_precond_cg_warp_path(gpulib, N):
+    """Reference-medium preconditioned mixed CG on the warp-FFT sizes: the solution of the
+    plain FP64 CG (itself checked against the oracle above) to the CG tolerance, the
+    reference's stop test met on the FP64 residual, in fewer FP32 iterations than the
+    unpreconditioned mixed CG on the same system."""
+    r = rve.make_rve(N, 8, 17)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED)
+    try:
+        Fn, Fn1 = random_F(N, 2e-3, 5)
+        s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False)
+        b = -s.G_K_dF(np.ones((9, N ** 3)) * 1e-3, True)
+        x64, it64 = s.fftPcg(b, 1e-10)
+        s.set_mode(gpulib.PREC_MIXED)
+        s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False)  # the FP32 tangent
+        xm, itm = s.fftPcg(b, 1e-10)
+        s.set_precond(gpulib.PRECOND_REFERENCE)
+        xp, itp = s.fftPcg(b, 1e-10)
+        for x in (xm, xp):
+            assert rel(x, x64) < 1e-7, rel(x, x64)
+            res = s.G_K_dF(x, True) - b
+            assert np.linalg.norm(res) <= 1.5e-10 * np.linalg.norm(b)
+        assert itp < itm, (itp, itm, it64)
     finally:
         s.close()
