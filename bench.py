@@ -152,6 +152,16 @@ def train_guess(cp, N=64, grains=64, seed=100, steps=5, stride=3, epochs=4):
             "t_train_s": time.perf_counter() - t1}
 
 
+def start_flags(cp, args):
+    """Start of the local solves: the reference's predictor in the plain FP64 form; the
+    previous global iterate where there is one, else the learned guess (learned) or the
+    return-mapped elastic trial (mixed), in the fast forms."""
+    if args.mode == "fp64":
+        return cp.START_PLAIN
+    first = cp.START_LEARNED if args.mode == "learned" else cp.START_TRIAL
+    return first | (cp.START_ITERATE if args.start_iterate else 0)
+
+
 def workload(N, grains, seed):
     from cpfft_gb300 import rve
     r = rve.make_rve(N, grains, seed)
@@ -253,6 +263,11 @@ def config_dict(args, impl):
             "mode": args.mode if impl != "reference" else "fp64",
             "precond": (args.precond if impl != "reference" and args.mode != "fp64"
                         else "none (the reference's fftPcg)"),
+            "local_start": ({"fp64": "reference predictor", "mixed": "return-mapped elastic trial",
+                             "learned": "return-mapped learned guess"}[args.mode if impl != "reference" else "fp64"]
+                            + (", previous global iterate where available"
+                               if impl != "reference" and args.mode != "fp64" and args.start_iterate
+                               else "")),
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
             "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
@@ -278,8 +293,7 @@ def gb300_arm(args):
     learned = train_guess(cp) if args.mode == "learned" else None
     prec = cp.PREC_FP64 if args.mode == "fp64" else cp.PREC_MIXED
     solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
-    if learned:
-        solver.set_mode(prec, 1)
+    solver.set_mode(prec, start_flags(cp, args))
     if prec == cp.PREC_MIXED and args.precond == "reference":
         solver.set_precond(cp.PRECOND_REFERENCE)
     tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
@@ -425,6 +439,8 @@ def main():
     # preconditioner of the FP32 inner Krylov iterations (mixed / learned): the Green
     # operator of the mean-tangent reference medium, or none (the reference's plain CG)
     ap.add_argument("--precond", default="reference", choices=["reference", "none"])
+    # fast forms: start a pass's local solves at the previous global iterate of the step
+    ap.add_argument("--no-start-iterate", dest="start_iterate", action="store_false")
     # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
     # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
     # the benchmark uses the reference example deck's value 1e-5; the equilibrium

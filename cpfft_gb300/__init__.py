@@ -19,6 +19,7 @@ HIST_WORDS = 23
 G_REF_SHIFT, G_CENTERED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_REFERENCE = 0, 1
+START_PLAIN, START_LEARNED, START_ITERATE, START_TRIAL = 0, 1, 2, 4
 
 STATUS = {
     0: "ok", 1: "local mm10 fallback", -1: "CG reached maxIter", -2: "Newton maxIter",
@@ -229,7 +230,8 @@ class Solver:
     def close(self):
         load_library().cpfft_finalize()
 
-    def set_mode(self, precision, warm_start=0):
+    def set_mode(self, precision, warm_start=START_PLAIN):
+        """warm_start: START_PLAIN or an OR of START_LEARNED / START_ITERATE / START_TRIAL."""
         _check(load_library().cpfft_set_mode(precision, int(warm_start)), "cpfft_set_mode")
 
     def set_precond(self, precond=PRECOND_REFERENCE):

@@ -176,6 +176,7 @@ struct Ctx {
   long long N3 = 0;
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
+  int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
   cudaStream_t st = nullptr;
   GridDesc g;
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
@@ -716,15 +717,18 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.mlp_packed = nullptr;
   a.mlp_params = a.mlp_norm = nullptr;
   a.mlp_err = nullptr;
-  // learned start: the predicted stress increment, pulled back 2 % inside the rate
-  // surface; tau from the reference's extrapolation (measured: the network's tau guess
-  // costs coupled-Newton iterations, and a stress start outside the surface costs
-  // predictor iterations)
-  a.guess_ls = 1.0;
-  a.guess_lt = 0.0;
-  a.guess_eps = 0.02;
+  // start of the local solves.  Plain: the reference's (predictor from sigma_n).
+  // CPFFT_START_ITERATE: a pass that follows an implicit pass of the same step starts the
+  // coupled Newton from that pass's converged state.  On the other implicit passes,
+  // CPFFT_START_LEARNED starts it from the network's guess and CPFFT_START_TRIAL from the
+  // elastic trial, both returned inside the rate surface.
+  const bool have_iterate = c->pass_step == step && c->pass_iter >= 1 && iter == c->pass_iter + 1;
+  a.start_iterate = (c->warm & CPFFT_START_ITERATE) && iter >= 2 && have_iterate;
+  a.start_trial = (c->warm & CPFFT_START_TRIAL) && !(c->warm & CPFFT_START_LEARNED) &&
+                  !a.start_iterate;
+  a.start_cap = 8;
   bool warm = false;
-  if (c->warm && iter > 0) {
+  if ((c->warm & CPFFT_START_LEARNED) && iter > 0 && !a.start_iterate) {
     mlp::Weights w;
     if (!mlp_device_weights(&w, &a.mlp_err)) {
       cpfft_set_error("learned initial guess selected but the network is not initialised");
@@ -745,6 +749,8 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   kt_start(c, KT_STRESS);
   CK(launch_stress(a, warm, c->st));
   TRY(kt_stop(c));
+  c->pass_step = step;
+  c->pass_iter = iter;
   c->K4f_valid = a.K4f != nullptr;
   const bool reduce = c->K4f_valid && pre_applies(c);
   if (reduce) TRY(reference_reduce(c));
@@ -756,9 +762,12 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   if (predict_iters) *predict_iters = (long long)c->h_stats[2];
   if (rejected) *rejected = (long long)c->h_stats[3];
   if (c->log)  // per-pass local work (CPFFT_LOG=1)
-    fprintf(stderr, "       stress pass step %d iter %d: update %.4f predictor %.4f per voxel%s\n",
-            step, iter, (double)c->h_stats[0] / (double)c->N3,
-            (double)c->h_stats[2] / (double)c->N3, warm ? " (learned start)" : "");
+    fprintf(stderr, "       stress pass step %d iter %d: update %.4f predictor %.4f per voxel%s, "
+            "%.4f starts dropped\n", step, iter, (double)c->h_stats[0] / (double)c->N3,
+            (double)c->h_stats[2] / (double)c->N3,
+            warm ? " (learned start)" : a.start_iterate ? " (iterate start)" :
+            a.start_trial && iter > 0 ? " (trial start)" : "",
+            (double)c->h_stats[3] / (double)c->N3);
   if (warm) TRY(mlp_check_error());
   return 0;
 }
@@ -1028,7 +1037,11 @@ int cpfft_set_mode(int precision, int warm_start) {
     cpfft_set_error("cpfft_set_mode: unknown precision %d", precision);
     return CPFFT_ERR_BAD_ARG;
   }
-  if (warm_start) {
+  if (warm_start & ~(CPFFT_START_LEARNED | CPFFT_START_ITERATE | CPFFT_START_TRIAL)) {
+    cpfft_set_error("cpfft_set_mode: unknown start flags %d", warm_start);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (warm_start & CPFFT_START_LEARNED) {
     mlp::Weights w;
     int* err;
     if (!mlp_device_weights(&w, &err)) {
@@ -1333,6 +1346,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   for (int i = 0; i < 9; i++) c->barF_t[i] = barF[i];
   CK(cudaMemcpyAsync(c->Fn, c->Fn1, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
   c->hn = 1 - c->hn;
+  c->pass_step = 0;
   if (Pbar)
     for (int i = 0; i < 9; i++) Pbar[i] = c->P_bar[i];
   // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||)
@@ -1383,6 +1397,7 @@ int cpfft_commit_step(void) {
   Ctx* c = g_ctx;
   CK(cudaMemcpyAsync(c->Fn, c->Fn1, 9 * c->N3 * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
   c->hn = 1 - c->hn;
+  c->pass_step = 0;
   return sync(c);
 }
 

@@ -57,7 +57,7 @@ struct StressArgs {
   const double* Fn;      // (9, N3)
   const double* Fn1;     // (9, N3)
   const double* hist_n;  // (23, N3)
-  double* hist_np1;      // (23, N3)
+  double* hist_np1;      // (23, N3): written; read as the previous iterate's local state
   double* P;             // (9, N3)
   double* K4;            // (81, N3)
   float* K4f;            // (81, N3) optional FP32 copy (mixed precision), may be null
@@ -75,8 +75,15 @@ struct StressArgs {
   const float* mlp_params;
   const float* mlp_norm;
   int* mlp_err;               // set when a tensor-core wait gave up
-  double guess_ls, guess_lt;  // fractions of the predicted stress / tau increments used
-  double guess_eps;           // margin below the rate surface for the learned start
+  // start of the local solves (fast modes), each in place of the reference's predictor:
+  // start_iterate = 1: the coupled Newton starts from the state left in hist_np1 by the
+  // previous global iteration of this step; start_trial = 1: from the elastic trial
+  // returned inside the rate surface; warm launches: from the learned guess returned
+  // inside the surface.  start_cap bounds the iterations from such a start before the
+  // plain solve takes over.
+  int start_iterate;
+  int start_trial;
+  int start_cap;
   // logging of (features, converged increments) pairs from the plain solve
   float* log_X;               // [cap][20], null: no logging
   float* log_T;               // [cap][7]

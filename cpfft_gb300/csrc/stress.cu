@@ -211,8 +211,6 @@ struct Crystal {
   double ms[12][6];
   double qc[12][3];
   double Cms[12][6];  // C ms_i, constant while ms is (the reference forms it per call)
-  double guess_eps;   // learned start: margin below the rate surface
-  int guess_tau;      // learned start: take tau from the guess (else the extrapolation)
 };
 
 __device__ __forceinline__ double Cv(const double* C, int a, int b) { return __ldg(C + 6 * a + b); }
@@ -396,17 +394,31 @@ __device__ __forceinline__ bool anynan(const double* x, int n) {
 }
 
 __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jlast, bool& haveJ,
-                              int& iters, double& ttrate);
+                              int& iters, double& ttrate, bool fixed_scale = false,
+                              int cap = 1 << 30);
+
+// tau_tilde extrapolated along the previous step's rate (mm10_solve, src/mm10_a.f:2900-2935):
+// tau_n + max(cos(dev D, dev D_n), 0) * tau_rate_n * dt
+__device__ double tau_extrapolated(const Crystal& cu, double tt, double dtinc) {
+  double d1[6], d2[6];
+  for (int i = 0; i < 6; i++) { d1[i] = cu.D[i]; d2[i] = cu.nD[i]; }
+  for (int k = 0; k < 2; k++) {
+    double* d = k ? d2 : d1;
+    double dtr = (d[0] + d[1] + d[2]) / 3.0;
+    d[0] -= dtr; d[1] -= dtr; d[2] -= dtr;
+    double t = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
+    double sc = t == 0.0 ? 0.0 : 1.0 / sqrt(t);
+    for (int i = 0; i < 6; i++) d[i] = t == 0.0 ? 0.0 : d[i] * sc;
+  }
+  double cs = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2] + d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5];
+  cs = fmax(cs, 0.0);
+  return tt + cs * cu.nttr * dtinc;
+}
 
 // mm10_solve (src/mm10_a.f:2860-3295): predict on R1 with tau_tilde extrapolated, then
 // the coupled Newton; Armijo line search c = 1e-4, halving, at most 11 trials.
-//
-// x0 (7, or null): a learned starting point (sigma, tau) for the predictor in place of
-// (sigma_n, extrapolated tau).  The relative stop test keeps the residual of the plain
-// start as its scale, so both starts iterate to the same absolute tolerance.
 __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, double* Jlast,
-                      bool& haveJ, int& iters, int& piters, double& ttrate,
-                      const double* x0 = nullptr) {
+                      bool& haveJ, int& iters, int& piters, double& ttrate) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
   double x[7], rs[12], si[12], pw[12];
@@ -414,19 +426,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
   x[6] = tt;
   double inR1;
   {  // ---- predict
-    double d1[6], d2[6];
-    for (int i = 0; i < 6; i++) { d1[i] = cu.D[i]; d2[i] = cu.nD[i]; }
-    for (int k = 0; k < 2; k++) {
-      double* d = k ? d2 : d1;
-      double dtr = (d[0] + d[1] + d[2]) / 3.0;
-      d[0] -= dtr; d[1] -= dtr; d[2] -= dtr;
-      double t = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
-      double sc = t == 0.0 ? 0.0 : 1.0 / sqrt(t);
-      for (int i = 0; i < 6; i++) d[i] = t == 0.0 ? 0.0 : d[i] * sc;
-    }
-    double cs = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2] + d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5];
-    cs = fmax(cs, 0.0);
-    double x2 = x[6] + cs * cu.nttr * dtinc;
+    double x2 = tau_extrapolated(cu, x[6], dtinc);
     double x1[6], R1[6];
     for (int i = 0; i < 6; i++) x1[i] = x[i];
     slips(cu, x1, x2, rs, si, pw);
@@ -435,30 +435,6 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
     for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
     double nR1 = sqrt(dot);
     inR1 = nR1;
-    if (x0) {
-      // stress start from the guess, pulled back along the predicted increment until no
-      // slip system's resolved shear exceeds (1 - eps) tau: the power-law Newton
-      // converges fast from inside the rate surface and slowly from outside it
-      double smax = 1.0;
-      const double lim = (1.0 - cu.guess_eps) * x2;
-      for (int i = 0; i < 12; i++) {
-        double r0 = 0.0, dr = 0.0;
-        for (int k = 0; k < 6; k++) {
-          r0 += x[k] * cu.ms[i][k];
-          dr += (x0[k] - x[k]) * cu.ms[i][k];
-        }
-        if (dr > 0.0 && r0 + dr > lim) smax = fmin(smax, fmax(0.0, (lim - r0) / dr));
-        if (dr < 0.0 && r0 + dr < -lim) smax = fmin(smax, fmax(0.0, (-lim - r0) / dr));
-      }
-      for (int i = 0; i < 6; i++) x1[i] = x[i] + smax * (x0[i] - x[i]);
-      if (cu.guess_tau) x2 = x0[6];
-      slips(cu, x1, x2, rs, si, pw);
-      formR1(cu, x1, rs, si, R1);
-      dot = 0;
-      for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
-      nR1 = sqrt(dot);
-      if (inR1 == 0.0) inR1 = nR1;
-    }
     int it = 0;
     while (nR1 > c.atol1 && nR1 / inR1 > c.rtol1) {
       double J[36], mJ[36], dx[6];
@@ -502,11 +478,54 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
   return true;
 }
 
+// Pull a start (sigma, tau) back along the segment from sigma_n until no slip system's
+// resolved shear exceeds frac * tau: the power-law Newton converges from inside the rate
+// surface and diverges from far outside it.
+__device__ void pull_inside(const Crystal& cu, const double* nsig, double* x, double frac) {
+  double smax = 1.0;
+  const double lim = frac * x[6];
+  for (int i = 0; i < 12; i++) {
+    double r0 = 0.0, dr = 0.0;
+    for (int k = 0; k < 6; k++) {
+      r0 += nsig[k] * cu.ms[i][k];
+      dr += (x[k] - nsig[k]) * cu.ms[i][k];
+    }
+    if (dr > 0.0 && r0 + dr > lim) smax = fmin(smax, fmax(0.0, (lim - r0) / dr));
+    if (dr < 0.0 && r0 + dr < -lim) smax = fmin(smax, fmax(0.0, (-lim - r0) / dr));
+  }
+  for (int k = 0; k < 6; k++) x[k] = nsig[k] + smax * (x[k] - nsig[k]);
+}
+
+// The full step's coupled Newton started at x0 = (sigma, tau) -- the previous global
+// iteration's converged local state, the return-mapped elastic trial or the learned
+// guess -- in place of the predictor's result: no predictor.  The stop test is the coupled Newton's, scaled by the residual of
+// the reference's start (sigma_n, extrapolated tau), so both starts iterate to the same
+// tolerance; at most `cap` iterations, after which the caller runs the plain solve.
+__device__ bool solve_from(Crystal& cu, double dtinc, const double* x0, double* stress,
+                           double& tt, double* Jlast, bool& haveJ, int& iters, double& ttrate,
+                           int cap) {
+  double x[7], R[7], rs[12], si[12], pw[12];
+  for (int i = 0; i < 6; i++) x[i] = stress[i];
+  x[6] = tau_extrapolated(cu, tt, dtinc);
+  formR(cu, x, R, rs, si, pw);
+  double dot = 0;
+  for (int a = 0; a < 7; a++) dot += R[a] * R[a];
+  const double scale = sqrt(dot);
+  for (int i = 0; i < 7; i++) x[i] = x0[i];
+  if (!(x[6] > 0.0) || anynan(x, 7)) return false;
+  if (!newton_update(cu, x, scale, Jlast, haveJ, iters, ttrate, true, cap)) return false;
+  for (int i = 0; i < 6; i++) stress[i] = x[i];
+  tt = x[6];
+  return true;
+}
+
 // The coupled 7x7 Newton of mm10_solve (src/mm10_a.f:3105-3295) from x = (sigma, tau):
 // Armijo line search, converged when ||R|| <= atol or ||R|| / ||R_0|| <= rtol after at
 // least one iteration; inR_alt replaces ||R_0|| when the start is an exact root.
+// fixed_scale: inR_alt is the relative test's scale (a start other than the predictor's);
+// cap: an iteration limit below miter (that start is then abandoned)
 __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jlast, bool& haveJ,
-                              int& iters, double& ttrate) {
+                              int& iters, double& ttrate, bool fixed_scale, int cap) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
   double rs[12], si[12], pw[12];
@@ -516,7 +535,8 @@ __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jl
   double dot = 0;
   for (int a = 0; a < 7; a++) dot += R[a] * R[a];
   double nR = sqrt(dot), inR = nR;
-  if (inR == 0.0) inR = inR_alt;
+  if (inR == 0.0 || fixed_scale) inR = inR_alt;
+  const int mit = min(c.miter, cap);
   while ((nR > c.atol && nR / inR > c.rtol) || it < 1) {
     formJ(cu, x, rs, si, pw, Jlast);
     haveJ = true;
@@ -546,7 +566,7 @@ __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jl
       alpha *= 0.5;
     }
     it++;
-    if (it > c.miter || anynan(x, 7)) { iters += it; return false; }
+    if (it > mit || anynan(x, 7)) { iters += it; return false; }
   }
   iters += it;
   return true;
@@ -647,6 +667,9 @@ __device__ void cep2A(const double* Fn, const double* Fn1, const double* t, cons
         }
     }
 }
+
+// margin of the returned starts below the rate surface: |tau_i| <= START_SURFACE tau
+constexpr double START_SURFACE = 0.98;
 
 // block state of the learned initial guess inside the stress kernel
 struct GuessBlock {
@@ -805,8 +828,6 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   s.nttr = nttr;
   for (int i = 0; i < 6; i++) s.nD[i] = nD[i];
   setup_np1(s, rec, uddt, a.dt, rn1, nRp);
-  s.guess_eps = a.guess_eps;
-  s.guess_tau = a.guess_lt > 0.0;
   double stress[6], tt = ntt, ttrate = 0.0;
   for (int i = 0; i < 6; i++) stress[i] = nsig[i];
   double t1 = 0, t2 = 0;
@@ -831,10 +852,26 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     const bool mok = mlp::forward_tile(w, gb->smem, gb->tmem, gb->bar, &gb->phase, feat, out);
     if (!mok && threadIdx.x == 0) atomicExch(a.mlp_err, 1);
     if (mok) {
-      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + a.guess_ls * (double)out[i];
-      guess[6] = ntt + a.guess_lt * (double)out[6];
+      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + (double)out[i];
+      guess[6] = ntt + (double)out[6];
       have_guess = !anynan(guess, 7) && guess[6] > 0.0 && !iter0 && !no_load;
     }
+    if (have_guess) pull_inside(s, nsig, guess, START_SURFACE);
+  } else if (a.start_iterate && !iter0 && !no_load && valid) {
+    // the previous global iteration's converged local state of this step (history n+1)
+    for (int i = 0; i < 6; i++) guess[i] = a.hist_np1[(H_SIG + i) * N3 + v];
+    guess[6] = a.hist_np1[H_TT * N3 + v];
+    have_guess = !anynan(guess, 7) && guess[6] > 0.0;
+  } else if (a.start_trial && !iter0 && !no_load) {
+    // the elastic trial sigma_n + C D with tau extrapolated, returned inside the surface
+    for (int i = 0; i < 6; i++) {
+      double t = 0.0;
+      for (int j = 0; j < 6; j++) t += Cv(s.C, i, j) * uddt[j];
+      guess[i] = nsig[i] + t;
+    }
+    guess[6] = tau_extrapolated(s, ntt, a.dt);
+    have_guess = !anynan(guess, 7) && guess[6] > 0.0;
+    if (have_guess) pull_inside(s, nsig, guess, START_SURFACE);
   }
   if (iter0 || no_load) {
     for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
@@ -851,13 +888,13 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int i = 0; i < 6; i++) ostress[i] = stress[i];
     int cuts = 0;
     bool fail = false;
-    if (WARM && have_guess) {
-      // the full step with the predictor started from the network's guess; a solve that
-      // fails from there is dropped and the plain path below runs instead
+    if (have_guess) {
+      // the full step's coupled Newton from the start (learned guess or previous
+      // iterate); a solve that fails from there is dropped and the plain path below runs
       double st[6], ttw = ntt, trw = 0.0;
       for (int i = 0; i < 6; i++) st[i] = stress[i];
-      if (solve(s, a.dt, st, ttw, Jl, haveJ, iters, piters, trw, guess) && !anynan(st, 6) &&
-          !isnan(ttw)) {
+      const bool okg = solve_from(s, a.dt, guess, st, ttw, Jl, haveJ, iters, trw, a.start_cap);
+      if (okg && !anynan(st, 6) && !isnan(ttw)) {
         for (int i = 0; i < 6; i++) stress[i] = st[i];
         tt = ttw;
         ttrate = trw;

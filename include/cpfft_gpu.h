@@ -117,8 +117,24 @@ typedef struct cpfft_stats {
 int cpfft_init(int N, const int* matList, const double* kocks_deg,
                const cpfft_crystal* props, int ncrystals, double tstep, int g_mapping);
 
-/* Select the Krylov precision (CPFFT_PREC_*) and the learned initial guess of the local
- * solve (0/1).  Extensions with no counterpart in the reference. */
+/* Select the Krylov precision (CPFFT_PREC_*) and the start of the local mm10 solves
+ * (warm_start: 0 = the reference's predictor from sigma_n, or an OR of the flags below).
+ * Extensions with no counterpart in the reference.  A start replaces the predictor: the
+ * coupled Newton of mm10_solve runs from it to the reference's local tolerance (its test
+ * scaled by the residual of the reference's start), and a start that has not converged
+ * within 8 iterations falls back to the reference's solve; only the number of local
+ * iterations changes.
+ *   CPFFT_START_LEARNED  the learned network's guess, returned along the segment from
+ *                        sigma_n to 98 % of the rate surface (needs cpfft_mlp_init and
+ *                        trained parameters)
+ *   CPFFT_START_ITERATE  on a stress pass that follows an implicit pass of the same
+ *                        load step: that pass's converged local state (precedence over
+ *                        the other two on those passes)
+ *   CPFFT_START_TRIAL    the elastic trial sigma_n + C D, tau extrapolated, returned to
+ *                        98 % of the rate surface (ignored with CPFFT_START_LEARNED) */
+#define CPFFT_START_LEARNED  1
+#define CPFFT_START_ITERATE  2
+#define CPFFT_START_TRIAL    4
 int cpfft_set_mode(int precision, int warm_start);
 
 /* Preconditioner of the FP32 inner iterations of CPFFT_PREC_MIXED (extension; the

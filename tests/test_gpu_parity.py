@@ -133,7 +133,7 @@ def test_tangent_homo_parity(gpulib, oracle):
 
 
 @pytest.mark.parametrize("case", ["fcc_voce_odd", "faithful_j22", "even_centered", "mixed",
-                                  "mixed_precond"])
+                                  "mixed_precond", "mixed_fast"])
 def test_load_step_parity(gpulib, oracle, case):
     cr = dict(rve.FCC_VOCE)
     N, gmap, inc, nsteps, precision, tolP = 9, 0, 1e-3, 3, 0, 1e-9
@@ -142,12 +142,14 @@ def test_load_step_parity(gpulib, oracle, case):
         inc = 2.5e-4
     elif case == "even_centered":
         N, gmap, nsteps = 8, 1, 2
-    elif case in ("mixed", "mixed_precond"):
+    elif case in ("mixed", "mixed_precond", "mixed_fast"):
         precision, tolP = 1, 1e-6
     r, s, o = make_pair(gpulib, oracle, N, ngr=4, seed=21, gmap=gmap, crystal=cr,
                         precision=precision)
-    if case == "mixed_precond":
+    if case in ("mixed_precond", "mixed_fast"):
         s.set_precond(gpulib.PRECOND_REFERENCE)
+    if case == "mixed_fast":  # the fast local starts too (local solves to the same tolerance)
+        s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL)
     load = rve.uniaxial_tension(inc * 20, 20)
     try:
         s.nr3_begin(1e-10)

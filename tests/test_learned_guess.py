@@ -1,13 +1,15 @@
-"""The learned initial guess of the local mm10 Newton solve, end to end on the GPU:
-log (features, converged increments) from the plain solver on one RVE, train the
-network with the tcgen05 kernels, then solve a different RVE (other seed) with and
-without the guess.  The guess only changes where each local Newton solve starts: the
-volume-averaged stress and the global iteration counts must agree with the plain run,
-and the test reports the local iterations (predictor + coupled Newton) of both runs.
-Measured on this material: the learned start saves no local iterations over the
-reference's elastic-side predictor (the power-law Newton's iteration count is set by
-the nonlinearity, not by the distance of an inside start), so the bound checked is that
-it costs at most 5 % more."""
+"""Starts of the local mm10 Newton solves, end to end on the GPU: log (features,
+converged increments) from the plain solver on one RVE, train the learned guess's
+network with the tcgen05 kernels, then solve a different RVE (other seed) from each
+start.  A start only changes where each local Newton solve begins (it replaces the
+reference's predictor and iterates to the same tolerance), so the volume-averaged stress
+and the global iteration counts must agree with the reference's start, and the local
+iterations (predictor + coupled Newton) must drop.
+
+Measured on this material (reported by the test): the learned guess, returned inside the
+rate surface, saves about a third of the local iterations over the reference's start;
+the return-mapped elastic trial, which needs no network, saves slightly more; the
+previous global iterate saves the most on the passes where it exists."""
 import numpy as np
 import pytest
 
@@ -16,14 +18,13 @@ from cpfft_gb300 import rve
 pytestmark = pytest.mark.gpu
 
 
-def run(gpulib, N, seed, nsteps, warm=False, log=0):
+def run(gpulib, N, seed, nsteps, start=0, log=0):
     r = rve.make_rve(N, 8, seed)
     load = rve.uniaxial_tension(0.02, 20)
     s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
                       gpulib.PREC_FP64)
     try:
-        if warm:
-            s.set_mode(gpulib.PREC_FP64, 1)
+        s.set_mode(gpulib.PREC_FP64, start)
         if log:
             s.learn_log(log)
         s.nr3_begin(1e-10)
@@ -37,24 +38,32 @@ def run(gpulib, N, seed, nsteps, warm=False, log=0):
             it_pred += st["predict_iters"]
             rej += st["guess_rejected"]
         data = s.learn_fetch() if log else None
-        return np.array(pbar), it_local, it_pred, rej, data, newton
+        return np.array(pbar), it_local + it_pred, rej, data, newton
     finally:
         s.close()
 
 
-def test_learned_guess_parity_and_local_iterations(gpulib):
+def test_local_starts_parity_and_iterations(gpulib):
     N, nsteps = 16, 8
-    _, _, _, _, (X, T), _ = run(gpulib, N, 31, nsteps, log=2_000_000)
+    _, _, _, (X, T), _ = run(gpulib, N, 31, nsteps, log=2_000_000)
     assert X.shape[0] > 50_000 and np.isfinite(X).all() and np.isfinite(T).all()
     m = gpulib.Mlp(5)
     loss = m.train(X, T, epochs=15, batch_tiles=16, lr=2e-3, seed=3)
     assert loss < 0.02, loss
-    pb0, li0, pi0, rj0, _, nw0 = run(gpulib, N, 32, nsteps)
-    pb1, li1, pi1, rj1, _, nw1 = run(gpulib, N, 32, nsteps, warm=True)
-    print(f"plain: update {li0} + predictor {pi0} = {li0 + pi0}; "
-          f"learned: update {li1} + predictor {pi1} = {li1 + pi1}, rejected guesses {rj1}")
+    starts = {"reference": 0, "learned": gpulib.START_LEARNED, "trial": gpulib.START_TRIAL,
+              "iterate+learned": gpulib.START_ITERATE | gpulib.START_LEARNED,
+              "iterate+trial": gpulib.START_ITERATE | gpulib.START_TRIAL}
+    res = {k: run(gpulib, N, 32, nsteps, start=v) for k, v in starts.items()}
+    pb0, it0, rj0, _, nw0 = res["reference"]
     assert rj0 == 0
-    assert nw1 == nw0
-    # same equilibrium: the local solves converge to the same tolerance
-    assert np.abs(pb1 - pb0).max() <= 1e-9 * np.abs(pb0).max()
-    assert li1 + pi1 <= 1.05 * (li0 + pi0)
+    for k, (pb, it, rj, _, nw) in res.items():
+        print(f"{k:16s} local iterations {it:9d} ({it / it0:.3f} of the reference start), "
+              f"starts dropped {rj}")
+        assert nw == nw0, k
+        # same equilibrium: the local solves converge to the same tolerance
+        assert np.abs(pb - pb0).max() <= 1e-8 * np.abs(pb0).max(), k
+    # what the trained network gains over the reference's start, and the iterate start
+    assert res["learned"][1] <= 0.85 * it0
+    assert res["trial"][1] <= 0.85 * it0
+    assert res["iterate+trial"][1] <= 0.65 * it0
+    assert res["iterate+learned"][1] <= 0.65 * it0
