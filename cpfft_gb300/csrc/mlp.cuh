@@ -9,9 +9,9 @@
 
 namespace mlp {
 
-constexpr int NIN = 20;    // features: lattice quaternion 4, D 6, sigma_n 6, tau_n, tau rate,
-                           // cos(D, D_n), |D|
-constexpr int NOUT = 7;    // targets: sigma - sigma_n (6), tau - tau_n
+constexpr int NIN = 20;    // features: lattice quaternion 4, D 6, return-mapped trial stress 6,
+                           // tau_n, extrapolated tau, cos(D, D_n), |D|
+constexpr int NOUT = 7;    // targets: sigma - sigma_trial (6), tau - tau_extrapolated
 constexpr int KIN = 32;    // NIN padded to the MMA K granularity
 constexpr int NH = 128;    // hidden width
 constexpr int NO = 16;     // NOUT padded to the smallest MMA N

@@ -681,8 +681,9 @@ struct GuessBlock {
 
 // Features of the learned initial guess (mlp::NIN, raw units): the quaternion of the
 // lattice rotation the local solve sees (Rp_n^T g; sign with w >= 0), the unrotated strain
-// increment D (6), sigma_n (6), tau_n, the tau rate of step n, cos(dev D, dev D_n) (the
-// predictor's extrapolation factor) and |D|.  FP32: only an initial guess depends on them.
+// increment D (6), the return-mapped elastic trial stress (6), tau_n, the extrapolated tau,
+// cos(dev D, dev D_n) (the extrapolation factor) and |D|.  The network's outputs correct
+// the return-mapped trial (stress and tau).  FP32: only an initial guess depends on them.
 __device__ void guess_features(const double* g, const double* nRp, const double* D,
                                const double* nsig, double ntt, double nttr, const double* nD,
                                float* f) {
@@ -838,11 +839,26 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   double Jl[49];
   bool haveJ = false;
   ok = true;
+  // ---- the return-mapped elastic trial: sigma_n + C D with tau extrapolated, returned
+  //      inside the rate surface -- the trial start, and the base the learned guess corrects
+  const bool implicit_load = !iter0 && !no_load;
+  const bool logit = !WARM && a.log_X && valid && implicit_load &&
+                     (v % a.log_stride) == a.log_phase;
+  double trial[7];
+  for (int i = 0; i < 6; i++) trial[i] = nsig[i];
+  trial[6] = ntt;
+  if (implicit_load && (WARM || logit || a.start_trial)) {
+    for (int i = 0; i < 6; i++) {
+      double t = 0.0;
+      for (int j = 0; j < 6; j++) t += Cv(s.C, i, j) * uddt[j];
+      trial[i] = nsig[i] + t;
+    }
+    trial[6] = tau_extrapolated(s, ntt, a.dt);
+    pull_inside(s, nsig, trial, START_SURFACE);
+  }
   // ---- learned initial guess / logging features
   float feat[mlp::NIN];
-  const bool logit = !WARM && a.log_X && valid && !iter0 && !no_load &&
-                     (v % a.log_stride) == a.log_phase;
-  if (WARM || logit) guess_features(rec->g, nRp, uddt, nsig, ntt, nttr, nD, feat);
+  if (WARM || logit) guess_features(rec->g, nRp, uddt, trial, ntt, trial[6], nD, feat);
   double guess[7];
   bool have_guess = false;
   if (WARM) {
@@ -851,10 +867,9 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
                          a.mlp_norm};
     const bool mok = mlp::forward_tile(w, gb->smem, gb->tmem, gb->bar, &gb->phase, feat, out);
     if (!mok && threadIdx.x == 0) atomicExch(a.mlp_err, 1);
-    if (mok) {
-      for (int i = 0; i < 6; i++) guess[i] = nsig[i] + (double)out[i];
-      guess[6] = ntt + (double)out[6];
-      have_guess = !anynan(guess, 7) && guess[6] > 0.0 && !iter0 && !no_load;
+    if (mok) {  // the network's correction of the return-mapped trial
+      for (int i = 0; i < 7; i++) guess[i] = trial[i] + (double)out[i];
+      have_guess = !anynan(guess, 7) && guess[6] > 0.0 && implicit_load;
     }
     if (have_guess) pull_inside(s, nsig, guess, START_SURFACE);
   } else if (a.start_iterate && !iter0 && !no_load && valid) {
@@ -862,16 +877,9 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int i = 0; i < 6; i++) guess[i] = a.hist_np1[(H_SIG + i) * N3 + v];
     guess[6] = a.hist_np1[H_TT * N3 + v];
     have_guess = !anynan(guess, 7) && guess[6] > 0.0;
-  } else if (a.start_trial && !iter0 && !no_load) {
-    // the elastic trial sigma_n + C D with tau extrapolated, returned inside the surface
-    for (int i = 0; i < 6; i++) {
-      double t = 0.0;
-      for (int j = 0; j < 6; j++) t += Cv(s.C, i, j) * uddt[j];
-      guess[i] = nsig[i] + t;
-    }
-    guess[6] = tau_extrapolated(s, ntt, a.dt);
+  } else if (a.start_trial && implicit_load) {
+    for (int i = 0; i < 7; i++) guess[i] = trial[i];
     have_guess = !anynan(guess, 7) && guess[6] > 0.0;
-    if (have_guess) pull_inside(s, nsig, guess, START_SURFACE);
   }
   if (iter0 || no_load) {
     for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
@@ -993,8 +1001,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
       const unsigned long long slot = atomicAdd(a.log_n, 1ull);
       if ((long long)slot < a.log_cap) {
         for (int i = 0; i < mlp::NIN; i++) a.log_X[slot * mlp::NIN + i] = feat[i];
-        for (int i = 0; i < 6; i++) a.log_T[slot * mlp::NOUT + i] = (float)(stress[i] - nsig[i]);
-        a.log_T[slot * mlp::NOUT + 6] = (float)(tt - ntt);
+        for (int i = 0; i < 6; i++) a.log_T[slot * mlp::NOUT + i] = (float)(stress[i] - trial[i]);
+        a.log_T[slot * mlp::NOUT + 6] = (float)(tt - trial[6]);
       }
     }
   }

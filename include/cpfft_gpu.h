@@ -124,9 +124,9 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg,
  * scaled by the residual of the reference's start), and a start that has not converged
  * within 8 iterations falls back to the reference's solve; only the number of local
  * iterations changes.
- *   CPFFT_START_LEARNED  the learned network's guess, returned along the segment from
- *                        sigma_n to 98 % of the rate surface (needs cpfft_mlp_init and
- *                        trained parameters)
+ *   CPFFT_START_LEARNED  the return-mapped elastic trial (below) corrected by the learned
+ *                        network, returned along the segment from sigma_n to 98 % of the
+ *                        rate surface (needs cpfft_mlp_init and trained parameters)
  *   CPFFT_START_ITERATE  on a stress pass that follows an implicit pass of the same
  *                        load step: that pass's converged local state (precedence over
  *                        the other two on those passes)
@@ -250,8 +250,9 @@ int cpfft_measure_fp64_peak(double* tflops);
 /* ---- Learned initial guess of the local mm10 solve (extension; no reference
  * counterpart).  A 20-128-128-7 SiLU network (BF16 weights, FP32 accumulation, tcgen05
  * tensor cores) maps a voxel's features -- lattice quaternion (4), rotated strain
- * increment D (6), sigma_n (6), tau_n, tau rate_n, cos(D, D_n), |D| -- to the converged
- * increments sigma - sigma_n (6) and tau - tau_n.  Parameters: CPFFT_MLP_PARAMS floats
+ * increment D (6), the return-mapped elastic trial stress (6), tau_n, the extrapolated
+ * tau, cos(D, D_n), |D| -- to the converged state's offset from the return-mapped trial:
+ * sigma - sigma_trial (6) and tau - tau_extrapolated.  Parameters: CPFFT_MLP_PARAMS floats
  * (W1 [128][32], b1, W2 [128][128], b2, W3 [16][128], b3; padded rows and columns zero);
  * normalisation: CPFFT_MLP_NORM floats (feature means, inverse deviations, target means,
  * target deviations).  X is (n, 20) and Y, T are (n, 7), row-major FP32 host arrays. */
@@ -270,7 +271,7 @@ int cpfft_mlp_loss_grad(const float* X, const float* T, long long n, float* grad
  * sets the normalisation from the data; *loss = mean loss of the last epoch */
 int cpfft_mlp_train(const float* X, const float* T, long long n, int epochs, int batch_tiles,
                     float lr, int seed, float* loss);
-/* Log (features, converged increments) pairs of the plain local solves of voxels with
+/* Log (features, converged offsets) pairs of the plain local solves of voxels with
  * v % stride == phase into device buffers of `capacity` pairs (0 stops logging). */
 int cpfft_learn_log(long long capacity, int stride, int phase);
 /* Copy the logged pairs to host arrays X (n, 20) and T (n, 7); *n = pairs copied. */

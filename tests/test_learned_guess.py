@@ -6,10 +6,14 @@ reference's predictor and iterates to the same tolerance), so the volume-average
 and the global iteration counts must agree with the reference's start, and the local
 iterations (predictor + coupled Newton) must drop.
 
-Measured on this material (reported by the test): the learned guess, returned inside the
-rate surface, saves about a third of the local iterations over the reference's start;
-the return-mapped elastic trial, which needs no network, saves slightly more; the
-previous global iterate saves the most on the passes where it exists."""
+The learned guess is the network's correction of the return-mapped elastic trial (the
+trial stress returned along the segment from sigma_n to 98 % of the rate surface),
+returned the same way.  Measured on this material (reported by the test): the learned
+start saves about a third of the local iterations over the reference's start, but the
+return-mapped trial alone, with no network, saves slightly more -- the network's
+correction does not beat a zero correction, so the learned start gains nothing over the
+physics-based one; the previous global iterate saves the most on the passes where it
+exists."""
 import numpy as np
 import pytest
 
