@@ -87,6 +87,7 @@ SIGNATURES = {
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
+    "cpfft_green_apply_df": (_I, [_DP, _DP, _I]),
     "cpfft_set_K4": (_I, [_DP]),
     "cpfft_cg": (_I, [_DP, _DP, _D, _IP]),
     "cpfft_tangent_homo": (_I, [_D, _DP]),
@@ -274,6 +275,13 @@ class Solver:
         x = np.ascontiguousarray(x, np.float32)
         y = np.zeros((9, self.N3), np.float32)
         _check(load_library().cpfft_green_apply_f32(_fp(x), _fp(y), int(flgK)), "G_K_dF_f32")
+        return y
+
+    def G_K_dF_df(self, x, flgK=True):
+        """The double-float FP64-accurate operator of the mixed-precision solver."""
+        y = np.zeros((9, self.N3))
+        _check(load_library().cpfft_green_apply_df(_dp(np.ascontiguousarray(x)), _dp(y),
+                                                   int(flgK)), "G_K_dF_df")
         return y
 
     def set_K4(self, K4):

@@ -193,6 +193,11 @@ struct Ctx {
   double* hist[2] = {nullptr, nullptr};
   int hn = 0;  // index of the history at n
   float *K4f = nullptr, *xf = nullptr, *rf = nullptr, *pf = nullptr, *Apf = nullptr;
+  // mixed precision: FP64-accurate operator in double-float (power-of-two N 32..256):
+  // K4 = K4f + K4lo to 48 bits, double-float twiddles
+  float* K4lo = nullptr;
+  dfl2* twdf = nullptr;
+  bool df_ok = false;
   int *ori = nullptr, *crys = nullptr;
   OriRec* oris = nullptr;
   CrysRec* cryss = nullptr;
@@ -281,7 +286,7 @@ void free_ctx(Ctx* c) {
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
-                  c->k0sum};
+                  c->k0sum, c->K4lo, c->twdf};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -328,6 +333,20 @@ int matvec64(Ctx* c, const double* x, double* y, int flgK) {
   c->f64_matvecs++;
   kt_start(c, KT_G64);
   TRY(cuda_check(green_apply<double>(x, c->K4, flgK, y, c->S, c->tw, c->g, c->st), "green_apply fp64"));
+  return kt_stop(c);
+}
+
+// The FP64-accurate operator of the solver: mixed precision evaluates it in double-float
+// on the FP32 pipes where the grid allows (about 1e-13 relative to the FP64 operator, far
+// inside the 1e-10 CG tolerance it serves), the plain form in native FP64.
+int matvec_acc(Ctx* c, const double* x, double* y, int flgK) {
+  if (!(c->prec == CPFFT_PREC_MIXED && c->df_ok && (c->K4f_valid || !flgK)))
+    return matvec64(c, x, y, flgK);
+  c->f64_matvecs++;
+  kt_start(c, KT_G64);
+  TRY(cuda_check(green_apply_df(x, c->K4f, c->K4lo, flgK, y, reinterpret_cast<dfl2*>(c->S),
+                                c->twdf, c->g, c->st),
+                 "green_apply double-float"));
   return kt_stop(c);
 }
 int matvec32(Ctx* c, const float* x, float* y) {
@@ -522,7 +541,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
   double rn = n2b;
   if (use_x0) {
     // start from the caller's x (kept in the range of G): r = b - G(K4 : x) in FP64
-    TRY(matvec64(c, x, c->Ap, 1));
+    TRY(matvec_acc(c, x, c->Ap, 1));
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
     if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
@@ -556,9 +575,9 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
       restarts++;
       CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
       CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
-      TRY(matvec64(c, c->w2, c->Ap, 0));
+      TRY(matvec_acc(c, c->w2, c->Ap, 0));
       CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
-      TRY(matvec64(c, x, c->Ap, 1));
+      TRY(matvec_acc(c, x, c->Ap, 1));
       CK(dev_sub(c->w, b, c->Ap, n, c->st));
       TRY(dnrm2(c, c->w, &rn));
       if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
@@ -612,7 +631,7 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
   const double tolb = tol * n2b;
   double rn = n2b;
   if (use_x0) {
-    TRY(matvec64(c, x, c->Ap, 1));
+    TRY(matvec_acc(c, x, c->Ap, 1));
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
     if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
@@ -651,9 +670,9 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
       restarts++;
       CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
       CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
-      TRY(matvec64(c, c->w2, c->Ap, 0));
+      TRY(matvec_acc(c, c->w2, c->Ap, 0));
       CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
-      TRY(matvec64(c, x, c->Ap, 1));
+      TRY(matvec_acc(c, x, c->Ap, 1));
       CK(dev_sub(c->w, b, c->Ap, n, c->st));
       TRY(dnrm2(c, c->w, &rn));
       if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
@@ -705,6 +724,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.P = c->P;
   a.K4 = c->K4;
   a.K4f = c->prec == CPFFT_PREC_MIXED ? c->K4f : nullptr;
+  a.K4lo = c->prec == CPFFT_PREC_MIXED && c->df_ok ? c->K4lo : nullptr;
   a.ori = c->ori;
   a.crys = c->crys;
   a.oris = c->oris;
@@ -786,7 +806,7 @@ int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
     for (int j = 0; j < 9; j++)
       CK(cudaMemcpyAsync(c->io + j * N3, c->K4 + (9 * j + i) * N3, N3 * sizeof(double),
                          cudaMemcpyDeviceToDevice, c->st));
-    TRY(matvec64(c, c->io, c->b, 0));
+    TRY(matvec_acc(c, c->io, c->b, 0));
     CK(dev_scale(c->b, -1.0, n, c->st));
     int its = 0;
     if (warm) {
@@ -877,6 +897,21 @@ int alloc_mixed(Ctx* c) {
   }
   CK(cudaMemcpy(c->twf, twf.data(), c->N * sizeof(float2), cudaMemcpyHostToDevice));
   CK(green_setup<float>(c->N));
+  if (green_df_supported(c->N)) {
+    TRY(dalloc(c->K4lo, 81 * c->N3 * sizeof(float)));
+    TRY(dalloc(c->twdf, c->N * sizeof(dfl2)));
+    std::vector<dfl2> tw(c->N);
+    for (int k = 0; k < c->N; k++) {
+      long double a = -2.0L * 3.14159265358979323846264338327950288L * k / c->N;
+      long double cr = cosl(a), ci = sinl(a);
+      const float hr = (float)cr, hi = (float)ci;
+      tw[k].x = dfl(hr, (float)(cr - (long double)hr));
+      tw[k].y = dfl(hi, (float)(ci - (long double)hi));
+    }
+    CK(cudaMemcpy(c->twdf, tw.data(), c->N * sizeof(dfl2), cudaMemcpyHostToDevice));
+    CK(green_setup_df(c->N));
+    c->df_ok = true;
+  }
   return 0;
 }
 
@@ -1150,11 +1185,16 @@ int cpfft_set_K4(const double* K4) {
   Ctx* c = g_ctx;
   CK(cudaMemcpyAsync(c->K4, K4, 81 * c->N3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
   if (c->prec == CPFFT_PREC_MIXED) {
-    // FP32 copy for the inner solves
+    // FP32 copy for the inner solves (and its FP32 remainder for the double-float operator)
     std::vector<float> kf(81 * c->N3);
     for (long long i = 0; i < 81 * c->N3; i++) kf[i] = (float)K4[i];
     CK(cudaMemcpyAsync(c->K4f, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
     TRY(sync(c));
+    if (c->df_ok) {
+      for (long long i = 0; i < 81 * c->N3; i++) kf[i] = (float)(K4[i] - (double)(float)K4[i]);
+      CK(cudaMemcpyAsync(c->K4lo, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+      TRY(sync(c));
+    }
     c->K4f_valid = true;
     if (pre_applies(c)) {
       TRY(reference_reduce(c));
@@ -1189,6 +1229,21 @@ int cpfft_green_apply_f32(const float* x, float* y, int flgK) {
   TRY(cuda_check(green_apply<float>(c->rf, c->K4f, flgK ? 1 : 0, c->Apf, c->Sf, c->twf, c->g, c->st),
                  "green_apply fp32"));
   CK(cudaMemcpyAsync(y, c->Apf, f9, cudaMemcpyDeviceToHost, c->st));
+  return sync(c);
+}
+
+int cpfft_green_apply_df(const double* x, double* y, int flgK) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (c->prec != CPFFT_PREC_MIXED || !c->df_ok || (flgK && !c->K4f_valid)) {
+    cpfft_set_error("cpfft_green_apply_df: needs mixed precision, N in {32, 64, 128, 256} "
+                    "and, with K, the tangent of a stress update");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const size_t f9 = 9 * c->N3 * sizeof(double);
+  CK(cudaMemcpyAsync(c->io, x, f9, cudaMemcpyHostToDevice, c->st));
+  TRY(matvec_acc(c, c->io, c->b, flgK ? 1 : 0));
+  CK(cudaMemcpyAsync(y, c->b, f9, cudaMemcpyDeviceToHost, c->st));
   return sync(c);
 }
 
@@ -1261,7 +1316,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     double Fnorm;
     TRY(dnrm2(c, c->Fn1, &Fnorm));
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
-    TRY(matvec64(c, c->dFm, c->b, 1));
+    TRY(matvec_acc(c, c->dFm, c->b, 1));
     CK(dev_scale(c->b, -1.0, n, c->st));
     int its;
     auto a = clk::now();
@@ -1282,7 +1337,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       S.local_iters += li;
       S.local_fallbacks += fails;
       S.stress_updates++;
-      TRY(matvec64(c, c->P, c->b, 0));
+      TRY(matvec_acc(c, c->P, c->b, 0));
       CK(dev_scale(c->b, -1.0, n, c->st));
       a = clk::now();
       TRY(cg(c, c->b, c->dFm, tolPCG, &its));
@@ -1350,7 +1405,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   if (Pbar)
     for (int i = 0; i < 9; i++) Pbar[i] = c->P_bar[i];
   // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||)
-  TRY(matvec64(c, c->P, c->b, 0));
+  TRY(matvec_acc(c, c->P, c->b, 0));
   double gp;
   TRY(dnrm2(c, c->b, &gp));
   double pb = 0;

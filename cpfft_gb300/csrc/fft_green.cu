@@ -222,8 +222,26 @@ __device__ __forceinline__ void ghat0_acc(const T2* A, int q0, int q1, int q2, T
 template <typename T2, typename T>
 __device__ __forceinline__ void green_acc(bool pre, const T2* A, int q0, int q1, int q2, T w,
                                           T2* out) {
-  if (sizeof(T) == 4 && pre) ghat0_acc<T2, T>(A, q0, q1, q2, w, out);
-  else ghat_acc<T2, T>(A, q0, q1, q2, w, out);
+  if constexpr (sizeof(T) == 4) {
+    if (pre) {
+      ghat0_acc<T2, T>(A, q0, q1, q2, w, out);
+      return;
+    }
+  }
+  ghat_acc<T2, T>(A, q0, q1, q2, w, out);
+}
+
+// an entry of the tangent in the transform's arithmetic type: FP32 / FP64 as stored, or
+// the double-float pair (hi, lo) of the FP64 tangent
+template <typename T, typename TK>
+__device__ __forceinline__ T kval(const TK* __restrict__ K, const float* __restrict__ Klo,
+                                  long long i) {
+  return (T)K[i];
+}
+template <>
+__device__ __forceinline__ dfl kval<dfl, float>(const float* __restrict__ K,
+                                                const float* __restrict__ Klo, long long i) {
+  return dfl(K[i], Klo[i]);
 }
 
 // one partial sum per block of the per-thread values d (fixed order), into *dst
@@ -474,6 +492,10 @@ template <int N>
 constexpr int cpw() { return 32 / regfft::Shape<N>::P; }
 template <int N>
 constexpr int ncols9() { return ((9 + cpw<N>() - 1) / cpw<N>()) * cpw<N>(); }
+// columns of pass C's tile: 9 components x TK, rounded up to whole warps of the register
+// transform (the extra columns are scratch)
+template <int N, int TK>
+constexpr int ncols_c() { return ((9 * TK + cpw<N>() - 1) / cpw<N>()) * cpw<N>(); }
 
 // Transform ncols columns (stride Lp; ncols a multiple of cpw<N>()) with every warp of
 // the block; inverse through conjugation.  Columns past the data are scratch.
@@ -487,9 +509,12 @@ __device__ __forceinline__ void block_columns(typename Vec2<T>::t* base, int nco
     regfft::column<N, T2, T, INV>(base + (g * CPW + lane / P) * Lp, tw, lane % P);
 }
 
-// part != nullptr (with flgK): one partial sum per block of <K : x, x> over its voxels
-template <int M, typename T, typename TK>
-__global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK* __restrict__ K4,
+// part != nullptr (with flgK): one partial sum per block of <K : x, x> over its voxels.
+// TIO: the field type of x (float, or double for the double-float transform T = dfl,
+// whose tangent is the pair K4, K4lo)
+template <int M, typename T, typename TK, typename TIO>
+__global__ void __launch_bounds__(288) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
+                                               const float* __restrict__ K4lo,
                                                int flgK, typename Vec2<T>::t* __restrict__ S,
                                                GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
                                                double* __restrict__ part) {
@@ -511,18 +536,18 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
     if (flgK) {
       T xv[9];
 #pragma unroll
-      for (int j = 0; j < 9; j++) xv[j] = x[j * N3 + v];
+      for (int j = 0; j < 9; j++) xv[j] = from_io<T, TIO>(x[j * N3 + v]);
 #pragma unroll
       for (int i = 0; i < 9; i++) {
         T s = 0;
 #pragma unroll
-        for (int j = 0; j < 9; j++) s += (T)K4[(9 * i + j) * N3 + v] * xv[j];
+        for (int j = 0; j < 9; j++) s += kval<T, TK>(K4, K4lo, (9 * i + j) * N3 + v) * xv[j];
         y[i] = s;
-        dsum += s * xv[i];
+        if (part) dsum += s * xv[i];
       }
     } else {
 #pragma unroll
-      for (int i = 0; i < 9; i++) y[i] = x[i * N3 + v];
+      for (int i = 0; i < 9; i++) y[i] = from_io<T, TIO>(x[i * N3 + v]);
     }
 #pragma unroll
     for (int i = 0; i < 9; i++) {
@@ -530,7 +555,7 @@ __global__ void __launch_bounds__(288) wpass_a(const T* __restrict__ x, const TK
       else col[i * Lp + pidx(a)].y = y[i];
     }
   }
-  if (part) block_partial<288>((double)dsum, part + blockIdx.x);
+  if (part) block_partial<288>(to_io<double, T>(dsum), part + blockIdx.x);
   __syncthreads();
   block_columns<N, T, false>(col, ncols9<N>(), Lp, tw);
   __syncthreads();
@@ -621,7 +646,7 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
     }
   }
   __syncthreads();
-  block_columns<N, T, false>(col, 9 * TK, Lp, tw);
+  block_columns<N, T, false>(col, ncols_c<N, TK>(), Lp, tw);
   __syncthreads();
   const int Nh = g.Nhalf, gm = g.gmap;
   const T scale = (T)g.inv_n3;
@@ -650,7 +675,7 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
     for (int i = 0; i < 9; i++) col[(i * TK + kk) * Lp + pidx(kc)] = out[i];
   }
   __syncthreads();
-  block_columns<N, T, true>(col, 9 * TK, Lp, tw);
+  block_columns<N, T, true>(col, ncols_c<N, TK>(), Lp, tw);
   __syncthreads();
   for (int t = threadIdx.x; t < 9 * N * TK; t += blockDim.x) {
     int kk = t % TK, rem = t / TK;
@@ -663,11 +688,11 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
 
 // dotx != nullptr: also one partial sum per block of dotx . y over the voxels the block
 // writes (the CG product p . Ap without re-reading Ap), into part[blockIdx.x]
-template <int M, typename T>
+template <int M, typename T, typename TIO>
 __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __restrict__ S,
-                                               T* __restrict__ y, GridDesc g,
+                                               TIO* __restrict__ y, GridDesc g,
                                                const typename Vec2<T>::t* __restrict__ twg,
-                                               const T* __restrict__ dotx,
+                                               const TIO* __restrict__ dotx,
                                                double* __restrict__ part) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
@@ -712,7 +737,7 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
     for (int e = 0; e < EO; e++) {
       const int t = threadIdx.x + e * NT, l = t / (9 * N), rem = t - l * 9 * N;
       const int i = rem / N, a = rem - i * N;
-      px[e] = dotx[i * N3 + a + (long long)N * (bl0 + l) + (long long)N * N * c];
+      px[e] = from_io<T, TIO>(dotx[i * N3 + a + (long long)N * (bl0 + l) + (long long)N * N * c]);
     }
   }
   __syncthreads();
@@ -726,12 +751,12 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
     T2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
     long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
     const T yv = l ? z.y : z.x;
-    y[i * N3 + v] = yv;
+    y[i * N3 + v] = to_io<TIO, T>(yv);
     if (dotx) dsum += px[e] * yv;
   }
   if (dotx) {  // block sum (9 warps), fixed order
     __shared__ double wsum[9];
-    double d = (double)dsum;
+    double d = to_io<double, T>(dsum);
     for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = d;
     __syncthreads();
@@ -749,39 +774,40 @@ template <typename T>
 constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
 constexpr int WTILE_B = 16;  // columns of pass B / D per block: 128-byte rows
 
-template <int M, typename T>
+template <int M, typename T, typename TK = T, typename TIO = T>
 cudaError_t wgreen_setup() {
   constexpr int N = 32 * M;
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(wpass_a<M, T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if ((e = cudaFuncSetAttribute(wpass_a<M, T, TK, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   if ((e = cudaFuncSetAttribute(wpass_b<M, T, WTILE_B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, WTILE_B)))) return e;
   if ((e = cudaFuncSetAttribute(wpass_c<M, T, wtile_c<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem_w<T>(N, 9 * wtile_c<T>())))) return e;
-  if ((e = cudaFuncSetAttribute(wpass_e<M, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem_w<T>(N, ncols_c<N, wtile_c<T>()>())))) return e;
+  if ((e = cudaFuncSetAttribute(wpass_e<M, T, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   return cudaSuccess;
 }
 
-template <int M, typename T>
-void wgreen_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
-                  const typename Vec2<T>::t* tw, const GridDesc& g, cudaStream_t st,
-                  double* part) {
+template <int M, typename T, typename TK = T, typename TIO = T>
+void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* y,
+                  typename Vec2<T>::t* S, const typename Vec2<T>::t* tw, const GridDesc& g,
+                  cudaStream_t st, double* part) {
   constexpr int N = 32 * M, H = N / 2 + 1, TC = wtile_c<T>();
   constexpr int NA = ncols9<N>(), TB = 32 * WTILE_B / cpw<N>();
   // the fused product: <K : x, x> in pass A for the reference-medium operator (where it
   // equals <x, y> in the K0 inner product), else <x, y> in pass E
   double* part_a = g.pre ? part : nullptr;
   double* part_e = g.pre ? nullptr : part;
-  wpass_a<M, T, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, flgK, S, g, tw, part_a);
+  wpass_a<M, T, TK, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, K4lo, flgK, S, g, tw,
+                                                                    part_a);
   dim3 gb((H + WTILE_B - 1) / WTILE_B, N, 9);
   wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 0);
   dim3 gc((H + TC - 1) / TC, N);
-  wpass_c<M, T, TC><<<gc, 288, smem_w<T>(N, 9 * TC), st>>>(S, g, tw);
+  wpass_c<M, T, TC><<<gc, 288, smem_w<T>(N, ncols_c<N, TC>()), st>>>(S, g, tw);
   wpass_b<M, T, WTILE_B><<<gb, TB, smem_w<T>(N, WTILE_B), st>>>(S, g, tw, 1);
-  wpass_e<M, T><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw, part_e ? x : nullptr,
-                                                            part_e);
+  wpass_e<M, T, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw,
+                                                                 part_e ? x : nullptr, part_e);
 }
 
 template <typename T>
@@ -846,10 +872,10 @@ cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Ve
   bool warp_path = true;
   if (nparts) *nparts = 0;
   switch (sizeof(T) == 4 ? N : 0) {
-    case 32: wgreen_apply<1, T>(x, K4, flgK, y, S, tw, g, st, part); break;
-    case 64: wgreen_apply<2, T>(x, K4, flgK, y, S, tw, g, st, part); break;
-    case 128: wgreen_apply<4, T>(x, K4, flgK, y, S, tw, g, st, part); break;
-    case 256: wgreen_apply<8, T>(x, K4, flgK, y, S, tw, g, st, part); break;
+    case 32: wgreen_apply<1, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
+    case 64: wgreen_apply<2, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
+    case 128: wgreen_apply<4, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
+    case 256: wgreen_apply<8, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
     default: warp_path = false;
   }
   if (warp_path) {
@@ -879,6 +905,32 @@ template <typename T>
 cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
   return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr);
+}
+
+bool green_df_supported(int N) { return N == 32 || N == 64 || N == 128 || N == 256; }
+
+cudaError_t green_setup_df(int N) {
+  switch (N) {
+    case 32: return wgreen_setup<1, dfl, float, double>();
+    case 64: return wgreen_setup<2, dfl, float, double>();
+    case 128: return wgreen_setup<4, dfl, float, double>();
+    case 256: return wgreen_setup<8, dfl, float, double>();
+    default: return cudaErrorNotSupported;
+  }
+}
+
+cudaError_t green_apply_df(const double* x, const float* K4hi, const float* K4lo, int flgK,
+                           double* y, dfl2* S, const dfl2* tw, GridDesc g, cudaStream_t st) {
+  g.pre = 0;
+  switch (g.N) {
+    case 32: wgreen_apply<1, dfl, float, double>(x, K4hi, K4lo, flgK, y, S, tw, g, st, nullptr); break;
+    case 64: wgreen_apply<2, dfl, float, double>(x, K4hi, K4lo, flgK, y, S, tw, g, st, nullptr); break;
+    case 128: wgreen_apply<4, dfl, float, double>(x, K4hi, K4lo, flgK, y, S, tw, g, st, nullptr); break;
+    case 256: wgreen_apply<8, dfl, float, double>(x, K4hi, K4lo, flgK, y, S, tw, g, st, nullptr); break;
+    default: return cudaErrorNotSupported;
+  }
+  g_kernel_launches += 5;
+  return cudaGetLastError();
 }
 
 cudaError_t green_set_reference(const float* coef36, cudaStream_t st) {

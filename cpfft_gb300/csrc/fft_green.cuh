@@ -1,10 +1,12 @@
 // fft_green.cuh -- declarations of the fused FFT + Green-operator passes.
 #pragma once
 #include "common.cuh"
+#include "dfloat.cuh"
 
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { typedef double2 t; };
 template <> struct Vec2<float> { typedef float2 t; };
+template <> struct Vec2<dfl> { typedef dfl2 t; };
 
 // Mixed-radix factorisation N = prod R[s]; Ns[s] = prod of the radices before stage s.
 struct FftPlan {
@@ -53,3 +55,14 @@ cudaError_t green_setup(int N);
 // (X q) (x) q / |q|^2, and the fused product of green_apply_dot is <K : x, x>, summed in
 // pass A, in place of <x, y>.
 cudaError_t green_set_reference(const float* coef36, cudaStream_t st);
+
+// FP64-accurate y = G(K : x) (flgK = 1) or G(x) in double-float arithmetic on the FP32
+// pipes, for the power-of-two grids 32..256 of the warp-FFT passes (green_df_supported).
+// x, y are FP64 fields; K is given as the float pair K4hi + K4lo (the FP64 tangent to 48
+// bits); S is the FP64 spectral scratch (double-float complex values are 16 bytes too);
+// tw the double-float twiddle table.  Relative error about 1e-13 against the FP64
+// operator, from about a fifth of its time.
+bool green_df_supported(int N);
+cudaError_t green_setup_df(int N);
+cudaError_t green_apply_df(const double* x, const float* K4hi, const float* K4lo, int flgK,
+                           double* y, dfl2* S, const dfl2* tw, GridDesc g, cudaStream_t st);

@@ -11,7 +11,8 @@
 // threads split it into even / odd halves (R-point DFTs) joined by one radix-2 stage
 // over a lane shuffle.  The only data exchange is one pass through the column's own
 // shared memory between the steps (warp-synchronous: no block barrier).  Output in
-// natural order.  Inverse transforms conjugate on the way in and out.
+// natural order.  Inverse transforms conjugate on the way in and out.  T is float, or the
+// double-float type of dfloat.cuh for FP64-accurate transforms on the FP32 pipes.
 #pragma once
 #include "fft_green.cuh"
 
@@ -26,8 +27,8 @@ __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
 }
 template <typename T2>
 __device__ __forceinline__ T2 shfl_xor2(T2 v, int m) {
-  v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
-  v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+  v.x = shfl_xor_val(v.x, m);
+  v.y = shfl_xor_val(v.y, m);
   return v;
 }
 template <typename T2>

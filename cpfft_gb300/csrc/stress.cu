@@ -1065,6 +1065,11 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   for (int m = 0; m < 81; m++) a.K4[m * N3 + v] = A[m];
   if (a.K4f)
     for (int m = 0; m < 81; m++) a.K4f[m * N3 + v] = (float)A[m];
+  if (a.K4lo)
+    for (int m = 0; m < 81; m++) {
+      const float h = (float)A[m];
+      a.K4lo[m * N3 + v] = (float)(A[m] - (double)h);
+    }
 }
 
 }  // namespace

@@ -173,6 +173,12 @@ int cpfft_green_apply(const double* x, double* y, int flgK);
  * host arrays; needs CPFFT_PREC_MIXED and, for flgK = 1, a stress update since. */
 int cpfft_green_apply_f32(const float* x, float* y, int flgK);
 
+/* The FP64-accurate operator of CPFFT_PREC_MIXED in double-float arithmetic (each value
+ * a pair of floats, about 48 bits, on the FP32 pipes): the outer residuals and
+ * projections of the mixed-precision CG use it where N is 32, 64, 128 or 256, in place of
+ * the native FP64 G_K_dF.  x, y (N3,9) FP64 host arrays. */
+int cpfft_green_apply_df(const double* x, double* y, int flgK);
+
 /*
  * y = G(K4 : x) (flgK = 1) or y = G(x) without any device allocation.  No counterpart in
  * the reference: it is for callers that cannot call cudaMalloc (host programs that give

@@ -215,3 +215,55 @@ def test_precond_cg_warp_path(gpulib, N):
         assert itp < itm, (itp, itm, it64)
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("N", [32, 64, 128])
+def test_green_double_float(gpulib, N):
+    """The double-float operator of mixed precision against the native FP64 operator on the
+    same tangent: FP64 accuracy (well inside the 1e-10 CG tolerance it serves)."""
+    r = rve.make_rve(N, 8, 13)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                      gpulib.PREC_MIXED)
+    try:
+        Fn, Fn1 = random_F(N, 1e-3, 4)
+        s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False)
+        x = np.random.default_rng(N).standard_normal((9, N ** 3))
+        for flgK in (True, False):
+            y64 = s.G_K_dF(x, flgK)
+            ydf = s.G_K_dF_df(x, flgK)
+            assert rel(ydf, y64) < 1e-12, (flgK, rel(ydf, y64))
+    finally:
+        s.close()
+
+
+def test_mixed_fast_vs_fp64_32(gpulib):
+    """The fast form at a warp-FFT size (FP32 inner CG with the reference-medium
+    preconditioner, double-float outer residuals, iterate + trial local starts) against the
+    plain FP64 form (itself checked against the oracle above) on the same 32^3 RVE: P_bar
+    within 1e-6 relative, per-voxel P within 1e-5, the same global iteration counts."""
+    N = 32
+    r = rve.make_rve(N, 8, 23)
+    load = rve.uniaxial_tension(0.02, 20)
+    out = []
+    for fast in (False, True):
+        s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                          gpulib.PREC_MIXED if fast else gpulib.PREC_FP64)
+        try:
+            if fast:
+                s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL)
+                s.set_precond(gpulib.PRECOND_REFERENCE)
+            s.nr3_begin(1e-10)
+            pb, its = [], []
+            for step in range(1, 4):
+                rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+                assert rc == 0
+                pb.append(Pbar)
+                its.append((st["newton_iters"], st["nbc_iters"]))
+            F, P = s.fields()
+            out.append((np.array(pb), its, P))
+        finally:
+            s.close()
+    (pb0, it0, P0), (pb1, it1, P1) = out
+    assert rel(pb1, pb0) < 1e-6, rel(pb1, pb0)
+    assert per_voxel_rel(P1, P0) < 1e-5
+    assert it1 == it0
