@@ -70,6 +70,7 @@ class Stats(ctypes.Structure):
         ("t_green32", ctypes.c_double), ("n_green64", ctypes.c_longlong),
         ("n_green32", ctypes.c_longlong), ("kernel_launches", ctypes.c_longlong),
         ("predict_iters", ctypes.c_longlong), ("guess_rejected", ctypes.c_longlong),
+        ("t_cg_graph", ctypes.c_double), ("n_green32_timed", ctypes.c_longlong),
     ]
 
     def as_dict(self):

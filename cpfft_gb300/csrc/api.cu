@@ -209,6 +209,13 @@ struct Ctx {
   unsigned long long* stats = nullptr;
   unsigned long long* h_stats = nullptr;
   bool K4f_valid = false;
+  // the preconditioned FP32 CG iteration as a graph: a WHILE node around one iteration
+  // (p update, G0(K:p) with alpha, x/r update with beta, stop test)
+  cudaGraph_t cg_graph = nullptr;
+  cudaGraphExec_t cg_exec = nullptr;
+  cudaGraphConditionalHandle cg_handle = 0;
+  int cg_graph_state = 0;         // 0 not built, 1 built, -1 unavailable (eager iterations)
+  long long cg_body_launches = 0; // kernels of one iteration
   // reference-medium preconditioner of the FP32 inner iterations (cpfft_set_precond)
   int precond = 0;
   bool pre_ok = false;     // the current reference medium is usable
@@ -225,12 +232,12 @@ struct Ctx {
   int kt_kind[KT_CAP];
   int kt_used = 0;
   bool kt_ready = false;
-  double kt_acc[3] = {0, 0, 0};
-  long long kt_cnt[3] = {0, 0, 0};
+  double kt_acc[4] = {0, 0, 0, 0};
+  long long kt_cnt[4] = {0, 0, 0, 0};
   cudaEvent_t step_ev[2];
 };
 
-enum { KT_STRESS = 0, KT_G64 = 1, KT_G32 = 2 };
+enum { KT_STRESS = 0, KT_G64 = 1, KT_G32 = 2, KT_CGGRAPH = 3 };
 
 int kt_drain(Ctx* c) {
   if (!c->kt_used) return 0;
@@ -259,7 +266,7 @@ int kt_stop(Ctx* c) {
   return 0;
 }
 void kt_reset(Ctx* c) {
-  for (int k = 0; k < 3; k++) { c->kt_acc[k] = 0; c->kt_cnt[k] = 0; }
+  for (int k = 0; k < 4; k++) { c->kt_acc[k] = 0; c->kt_cnt[k] = 0; }
 }
 Ctx* g_ctx = nullptr;
 
@@ -298,6 +305,8 @@ void free_ctx(Ctx* c) {
     cudaEventDestroy(c->step_ev[0]);
     cudaEventDestroy(c->step_ev[1]);
   }
+  if (c->cg_exec) cudaGraphExecDestroy(c->cg_exec);
+  if (c->cg_graph) cudaGraphDestroy(c->cg_graph);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -609,6 +618,122 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
   return 0;
 }
 
+// One preconditioned FP32 CG iteration on the device: p = r + beta p (and rr <- rr_new),
+// Ap = G0(K4f : p) with pAp = <K4f : p, p> and alpha = rr / pAp, x += alpha p, r -= alpha Ap
+// with rr_new = <r, r>_K0 and beta, then the stop test (k_cg_cond).  `timed` brackets the
+// Green apply with the per-launch CUDA events (never inside a capture).
+int cg_pre_body(Ctx* c, bool use_handle, bool timed) {
+  const long long n = 9 * c->N3;
+  GridDesc g = c->g;
+  g.pre = 1;
+  int np = 0;
+  CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+  if (timed) kt_start(c, KT_G32);
+  CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np));
+  if (timed) TRY(kt_stop(c));
+  if (!np) {
+    cpfft_set_error("internal: the preconditioned product was not fused");
+    return CPFFT_ERR_CUDA;
+  }
+  CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
+  CK(dev_cg_xr_k0(c->xf, c->rf, c->pf, c->Apf, c->N3, c->part, c->sc, c->st));
+  CK(dev_cg_cond(c->sc, c->cg_handle, use_handle, c->st));
+  return 0;
+}
+
+// Capture the iteration once into a graph whose WHILE node repeats it while k_cg_cond
+// says so (the node's default value runs the body at least once per launch).  Every
+// buffer and launch shape is fixed for the context; alpha, beta and the stop test's
+// inputs live in device memory.  If anything fails, the iterations run eagerly instead.
+void build_cg_graph(Ctx* c) {
+  if (c->cg_graph_state) return;
+  c->cg_graph_state = -1;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) { cudaGetLastError(); return; }
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams prm = {};
+  cudaGraphNode_t node;
+  bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (ok) {
+    prm.type = cudaGraphNodeTypeConditional;
+    prm.conditional.handle = h;
+    prm.conditional.type = cudaGraphCondTypeWhile;
+    prm.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &prm) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = prm.conditional.phGraph_out[0];
+    ok = cudaStreamBeginCaptureToGraph(c->st, body, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const long long l0 = g_kernel_launches;
+      c->cg_handle = h;
+      const int rc = cg_pre_body(c, true, false);
+      cudaGraph_t out = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(c->st, &out);
+      c->cg_body_launches = g_kernel_launches - l0;
+      g_kernel_launches = l0;
+      ok = rc == 0 && e == cudaSuccess;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    c->cg_handle = 0;
+    return;
+  }
+  c->cg_graph = g;
+  c->cg_exec = ex;
+  c->cg_graph_state = 1;
+}
+
+// Run iterations from the current (rf, pf, xf) until k_cg_cond stops them: the first one
+// eagerly with the Green apply timed (the per-launch figure of the FP32 operator), the
+// rest as one launch of the iteration graph.  rr (in) is <r,r>_K0 now; *rr_out the value
+// at the end; *it_out the iteration count after the segment; *stop the reason.
+int cg_segment(Ctx* c, double rr, double rn, double tolb, double tol, double delta, int it,
+               int maxIter, double beta, double* rr_out, double* rr_prev_out, int* it_out,
+               int* stop) {
+  double* h = c->h_sc;
+  h[SC_BETA] = beta;
+  h[SC_RRNEW] = rr;
+  CK(cudaMemcpyAsync(c->sc + SC_BETA, h + SC_BETA, sizeof(double), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->sc + SC_RRNEW, h + SC_RRNEW, sizeof(double), cudaMemcpyHostToDevice, c->st));
+  h[SC_RR0] = rr; h[SC_RN] = rn; h[SC_TOLB] = tolb; h[SC_TOL] = tol; h[SC_DELTA] = delta;
+  h[SC_CNT] = (double)it; h[SC_MAXIT] = (double)maxIter; h[SC_STOP] = 0.0;
+  CK(cudaMemcpyAsync(c->sc + SC_RR0, h + SC_RR0, (SC_STOP - SC_RR0 + 1) * sizeof(double),
+                     cudaMemcpyHostToDevice, c->st));
+  build_cg_graph(c);
+  int done = 0;
+  for (;;) {
+    TRY(cg_pre_body(c, false, done == 0));
+    done++;
+    double st;
+    TRY(read_scalar(c, SC_STOP, &st));
+    if (st != 0.0) break;
+    if (c->cg_graph_state == 1) {
+      kt_start(c, KT_CGGRAPH);
+      CK(cudaGraphLaunch(c->cg_exec, c->st));
+      TRY(kt_stop(c));
+      break;
+    }
+  }
+  CK(cudaMemcpyAsync(h + SC_CNT, c->sc + SC_CNT, (SC_STOP - SC_CNT + 1) * sizeof(double),
+                     cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(h + SC_RR, c->sc + SC_RR, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  TRY(read_scalar(c, SC_RRNEW, rr_out));
+  *rr_prev_out = h[SC_RR];  // <r,r>_K0 before the last iteration (its beta's denominator)
+  const int it_end = (int)h[SC_CNT];
+  const long long its = it_end - it;
+  c->f32_matvecs += its;
+  if (c->cg_graph_state == 1) g_kernel_launches += (its - done) * c->cg_body_launches;
+  *it_out = it_end;
+  *stop = (int)h[SC_STOP];
+  return 0;
+}
+
 // Mixed precision with the reference-medium preconditioner: FP32 CG on G0(K : x) = G0(r)
 // in the K0 inner product, with the same reliable updates, FP64 residual b - G(K4 : x),
 // FP64 projection of each correction and the reference's stop test as cg_mixed.  After a
@@ -648,58 +773,52 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
   TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
   CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
   CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
-  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RR, OP_STORE, c->st));
-  double rr_prev;
-  TRY(read_scalar(c, SC_RR, &rr_prev));
-  double rr0 = rr_prev;  // <r, r>_K0 at the last restart
-  int it = 0;
+  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+  double rr;
+  TRY(read_scalar(c, SC_RRNEW, &rr));
+  double beta = 0.0;  // the first iteration's p = r + 0 p = r
+  int it = 0, restarts = 0;
   bool converged = false;
-  int restarts = 0;
   for (;;) {
-    TRY(matvec32_pre(c, c->pf, c->Apf, 1, true));
-    CK(dev_cg_xr_k0(c->xf, c->rf, c->pf, c->Apf, c->N3, c->part, c->sc, c->st));
-    it++;
-    double rr;
-    TRY(read_scalar(c, SC_RRNEW, &rr));
-    if (!std::isfinite(rr)) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    // the preconditioned residual's reduction since the restart, and the true residual
-    // it predicts
-    const double red = std::sqrt(std::max(rr, 0.0) / rr0), est = rn * red;
-    if (red < delta || est <= tolb || est <= tol || it >= maxIter) {
-      // reliable update: x += G(xf / scale) in FP64, true residual, restart
-      restarts++;
-      CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
-      CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
-      TRY(matvec_acc(c, c->w2, c->Ap, 0));
-      CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
-      TRY(matvec_acc(c, x, c->Ap, 1));
-      CK(dev_sub(c->w, b, c->Ap, n, c->st));
-      TRY(dnrm2(c, c->w, &rn));
-      if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
-      if (rn <= tolb || rn <= tol) { converged = true; break; }
-      if (it >= maxIter) break;
-      const double nscale = 1.0 / rn, k = nscale / scale;
-      CK(dev_to_f32(c->Apf, c->w, nscale, n, c->st));
-      TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
-      CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
-      CK(dev_scale_f(c->pf, (float)k, n, c->st));
-      CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
-      TRY(read_scalar(c, SC_RRNEW, &rr));
-      c->h_sc[SC_BETA] = rr / (rr_prev * k * k);
-      CK(cudaMemcpyAsync(c->sc + SC_BETA, c->h_sc + SC_BETA, sizeof(double),
-                         cudaMemcpyHostToDevice, c->st));
-      scale = nscale;
-      rr0 = rr;
-    }
-    CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
-    rr_prev = rr;
+    // one segment of iterations on the device: until <r,r>_K0 has dropped by delta, the
+    // true residual it predicts meets the stop test, or maxIter
+    int stop = 0;
+    double rr_prev = rr;
+    TRY(cg_segment(c, rr, rn, tolb, tol, delta, it, maxIter, beta, &rr, &rr_prev, &it, &stop));
+    if (stop == STOP_NONFINITE) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    // reliable update: x += G(xf / scale) in FP64-accurate arithmetic, true residual
+    restarts++;
+    CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
+    CK(dev_add_f32(c->w2, c->xf, 1.0 / scale, n, c->st));
+    TRY(matvec_acc(c, c->w2, c->Ap, 0));
+    CK(dev_axpy(x, c->Ap, 1.0, n, c->st));
+    TRY(matvec_acc(c, x, c->Ap, 1));
+    CK(dev_sub(c->w, b, c->Ap, n, c->st));
+    TRY(dnrm2(c, c->w, &rn));
+    if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    if (rn <= tolb || rn <= tol) { converged = true; break; }
+    if (it >= maxIter) break;
+    // restart from G0 of the true residual, keeping the search direction (rescaled)
+    const double nscale = 1.0 / rn, k = nscale / scale;
+    CK(dev_to_f32(c->Apf, c->w, nscale, n, c->st));
+    TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
+    CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+    CK(dev_scale_f(c->pf, (float)k, n, c->st));
+    CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+    double rr_new;
+    TRY(read_scalar(c, SC_RRNEW, &rr_new));
+    // beta = |r_true|^2 / |r_prev|^2 with both in the new scaling (the iteration's beta
+    // with the recomputed residual in place of the recursive one)
+    beta = rr_new / (rr_prev * k * k);
+    rr = rr_new;
+    scale = nscale;
   }
   *iters = it;
   c->cg_iters += it;
   c->cg_solves++;
   if (c->log)
-    fprintf(stderr, "         cg (mixed, reference medium): %d iterations, %d restarts, |r|/|b| %.2e\n", it, restarts,
-            rn / n2b);
+    fprintf(stderr, "         cg (mixed, reference medium): %d iterations, %d restarts, |r|/|b| %.2e%s\n",
+            it, restarts, rn / n2b, c->cg_graph_state == 1 ? " (graph)" : "");
   if (!converged) { cpfft_set_error("mixed-precision CG did not converge"); return CPFFT_ERR_CG_MAXIT; }
   return 0;
 }
@@ -1427,7 +1546,9 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   S.t_green64 = c->kt_acc[KT_G64];
   S.t_green32 = c->kt_acc[KT_G32];
   S.n_green64 = c->kt_cnt[KT_G64];
-  S.n_green32 = c->kt_cnt[KT_G32];
+  S.n_green32 = c->f32_matvecs;
+  S.n_green32_timed = c->kt_cnt[KT_G32];
+  S.t_cg_graph = c->kt_acc[KT_CGGRAPH];
   S.kernel_launches = g_kernel_launches - launches0;
   S.t_total = sec(t0);
   if (st) *st = S;

@@ -294,6 +294,24 @@ __global__ void __launch_bounds__(64) k_final_rows(const double* __restrict__ pa
   if (threadIdx.x == 0) out[blockIdx.x] = ws[0] + ws[1];
 }
 
+__global__ void k_cg_cond(double* __restrict__ sc, cudaGraphConditionalHandle h, int use_handle) {
+  const double rr = sc[SC_RRNEW];
+  const double cnt = sc[SC_CNT] + 1.0;
+  sc[SC_CNT] = cnt;
+  int stop = STOP_NONE;
+  if (!isfinite(rr)) {
+    stop = STOP_NONFINITE;
+  } else if (!(sc[SC_RR0] > 0.0)) {
+    stop = STOP_TEST;  // nothing to reduce: let the caller's true residual decide
+  } else {
+    const double red = sqrt(fmax(rr, 0.0) / sc[SC_RR0]), est = sc[SC_RN] * red;
+    if (red < sc[SC_DELTA] || est <= sc[SC_TOLB] || est <= sc[SC_TOL]) stop = STOP_TEST;
+    else if (cnt >= sc[SC_MAXIT]) stop = STOP_MAXIT;
+  }
+  sc[SC_STOP] = (double)stop;
+  if (use_handle) cudaGraphSetConditional(h, stop == STOP_NONE ? 1u : 0u);
+}
+
 int grid_for(long long n, int bs) {
   long long b = (n + bs - 1) / bs;
   return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
@@ -409,4 +427,9 @@ cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81,
   k_sum81<<<dim3(NB, 81), RB, 0, st>>>(K, N3, part);
   k_final_rows<<<81, 64, 0, st>>>(part, NB, sc81);
   return counted(2);
+}
+cudaError_t dev_cg_cond(double* sc, cudaGraphConditionalHandle h, bool use_handle,
+                        cudaStream_t st) {
+  k_cg_cond<<<1, 1, 0, st>>>(sc, h, use_handle ? 1 : 0);
+  return counted(1);
 }

@@ -8,8 +8,15 @@ constexpr int NPART = 1024;  // partial sums per reduction (blocks of the first 
 enum {
   SC_RR = 0, SC_PAP = 1, SC_RRNEW = 2, SC_ALPHA = 3, SC_BETA = 4, SC_TMP = 5,
   SC_SUM9 = 8,     // 9 slots: component sums
+  // stop test of a device-driven CG segment (k_cg_cond): <r,r> at the segment start,
+  // the true residual norm there, the reference's absolute thresholds, the segment's
+  // reduction target, the iteration counter and cap, and the reason the segment ended
+  SC_RR0 = 17, SC_RN = 18, SC_TOLB = 19, SC_TOL = 20, SC_DELTA = 21,
+  SC_CNT = 22, SC_MAXIT = 23, SC_STOP = 24,
   SC_COUNT = 32
 };
+// SC_STOP values
+enum { STOP_NONE = 0, STOP_TEST = 1, STOP_MAXIT = 2, STOP_NONFINITE = 3 };
 enum { OP_STORE = 0, OP_ALPHA = 1, OP_BETA = 2 };
 
 cudaError_t dev_dot(const double* a, const double* b, long long n, double* part, double* sc,
@@ -44,3 +51,11 @@ cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, double* par
                        int slot, int op, cudaStream_t st);
 // sc81[m] = sum over voxels of component m of an (81, N3) FP32 field (part: 81 x 64)
 cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81, cudaStream_t st);
+
+// End-of-iteration test of a preconditioned FP32 CG segment (one thread): counts the
+// iteration and stops when the K0 norm of the residual has dropped by SC_DELTA since the
+// segment began, when the true residual it predicts meets the reference's test, at the
+// cap SC_MAXIT, or on a non-finite value.  With use_handle it drives the WHILE node of
+// the captured iteration graph (cudaGraphSetConditional); the counter bounds that loop.
+cudaError_t dev_cg_cond(double* sc, cudaGraphConditionalHandle h, bool use_handle,
+                        cudaStream_t st);

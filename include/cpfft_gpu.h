@@ -91,13 +91,16 @@ typedef struct cpfft_stats {
     double    t_total;          /* seconds in the whole call (host clock)                  */
     double    t_device;         /* seconds between CUDA events at the call's start and end */
     double    t_stress_kernel;  /* summed CUDA-event time of the stress-update kernel      */
-    double    t_green64;        /* summed CUDA-event time of FP64 Green applies            */
-    double    t_green32;        /* summed CUDA-event time of FP32 Green applies            */
-    long long n_green64;        /* FP64 Green applies                                      */
+    double    t_green64;        /* summed CUDA-event time of FP64-accurate Green applies   */
+    double    t_green32;        /* summed CUDA-event time of the timed FP32 Green applies  */
+    long long n_green64;        /* FP64-accurate Green applies (FP64 or double-float)      */
     long long n_green32;        /* FP32 Green applies                                      */
     long long kernel_launches;  /* kernels this call launched                              */
     long long predict_iters;    /* local predictor (6x6) Newton iterations, summed         */
     long long guess_rejected;   /* learned initial guesses the Newton solve dropped        */
+    double    t_cg_graph;       /* CUDA-event time of the graph-launched CG iterations     */
+    long long n_green32_timed;  /* FP32 Green applies timed one by one (t_green32 covers
+                                   these; the others run inside the iteration graph)       */
 } cpfft_stats;
 
 /*

@@ -76,3 +76,18 @@ def test_product_path_does_not_reference_the_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert "pyoracle" not in text and "cpfft_oracle" not in text, f
+
+
+def test_stats_mirrors_match_the_header():
+    """cpfft_stats is filled by both the library and the oracle: the ctypes mirrors must
+    have the header's fields in order (a shorter mirror would be overrun)."""
+    import cpfft_gb300
+    from oracle import pyoracle
+    src = open(os.path.join(ROOT, "include", "cpfft_gpu.h")).read()
+    body = re.search(r"typedef struct cpfft_stats \{(.*?)\} cpfft_stats;", src, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    ctype = {"int": ctypes.c_int, "double": ctypes.c_double, "long long": ctypes.c_longlong}
+    fields = [(m.group(2), ctype[m.group(1)])
+              for m in re.finditer(r"(long long|int|double)\s+(\w+);", body)]
+    for mirror in (cpfft_gb300.Stats, pyoracle.Stats):
+        assert [(n, t) for n, t in mirror._fields_] == fields
