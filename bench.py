@@ -159,7 +159,8 @@ def start_flags(cp, args):
     if args.mode == "fp64":
         return cp.START_PLAIN
     first = cp.START_LEARNED if args.mode == "learned" else cp.START_TRIAL
-    return first | (cp.START_ITERATE if args.start_iterate else 0)
+    return (first | (cp.START_ITERATE if args.start_iterate else 0) |
+            (cp.TANGENT_F32 if args.tangent == "f32" else 0))
 
 
 def workload(N, grains, seed):
@@ -271,6 +272,8 @@ def config_dict(args, impl):
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
             "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
+            "stress_schedule": args.schedule if impl != "reference" and args.mode != "fp64" else "blocks",
+            "tangent": args.tangent if impl != "reference" and args.mode != "fp64" else "f64",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -294,6 +297,8 @@ def gb300_arm(args):
     prec = cp.PREC_FP64 if args.mode == "fp64" else cp.PREC_MIXED
     solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
     solver.set_mode(prec, start_flags(cp, args))
+    if args.schedule == "queue" and args.mode != "fp64":
+        solver.set_schedule(cp.SCHED_QUEUE)
     if prec == cp.PREC_MIXED and args.precond == "reference":
         solver.set_precond(cp.PRECOND_REFERENCE)
     tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
@@ -452,6 +457,11 @@ def main():
     ap.add_argument("--precond", default="reference", choices=["reference", "none"])
     # fast forms: start a pass's local solves at the previous global iterate of the step
     ap.add_argument("--no-start-iterate", dest="start_iterate", action="store_false")
+    # voxel order of the implicit stress passes: 128-voxel blocks in order, or the
+    # persistent kernel's cost-sorted work queue
+    ap.add_argument("--schedule", default="queue", choices=["blocks", "queue"])
+    # fast forms: the consistent tangent (it steers Newton only) in FP32 or FP64
+    ap.add_argument("--tangent", default="f32", choices=["f32", "f64"])
     # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
     # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
     # the benchmark uses the reference example deck's value 1e-5; the equilibrium

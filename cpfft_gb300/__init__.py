@@ -20,6 +20,8 @@ G_REF_SHIFT, G_CENTERED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_REFERENCE = 0, 1
 START_PLAIN, START_LEARNED, START_ITERATE, START_TRIAL = 0, 1, 2, 4
+SCHED_BLOCKS, SCHED_QUEUE = 0, 1
+TANGENT_F32 = 8  # set_mode option of the mixed form
 
 STATUS = {
     0: "ok", 1: "local mm10 fallback", -1: "CG reached maxIter", -2: "Newton maxIter",
@@ -85,6 +87,7 @@ SIGNATURES = {
     "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
     "cpfft_set_mode": (_I, [_I, _I]),
     "cpfft_set_precond": (_I, [_I]),
+    "cpfft_set_schedule": (_I, [_I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
@@ -233,8 +236,13 @@ class Solver:
         load_library().cpfft_finalize()
 
     def set_mode(self, precision, warm_start=START_PLAIN):
-        """warm_start: START_PLAIN or an OR of START_LEARNED / START_ITERATE / START_TRIAL."""
+        """warm_start: START_PLAIN or an OR of START_LEARNED / START_ITERATE / START_TRIAL,
+        and TANGENT_F32 (mixed precision)."""
         _check(load_library().cpfft_set_mode(precision, int(warm_start)), "cpfft_set_mode")
+
+    def set_schedule(self, schedule=SCHED_QUEUE):
+        """Voxel order of the implicit stress passes: blocks in order, or the work queue."""
+        _check(load_library().cpfft_set_schedule(int(schedule)), "cpfft_set_schedule")
 
     def set_precond(self, precond=PRECOND_REFERENCE):
         """Reference-medium preconditioner of the mixed-precision inner iterations."""

@@ -177,6 +177,12 @@ struct Ctx {
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
+  // voxel work queue of the implicit stress passes (cpfft_set_schedule)
+  int sched = CPFFT_SCHED_BLOCKS;
+  int tangent_f32 = 0;  // mixed precision: the consistent tangent in FP32 (CPFFT_TANGENT_F32)
+  unsigned char* vcost = nullptr;  // (N3) local iterations of each voxel's last implicit pass
+  int* vperm = nullptr;            // (N3) queue order
+  unsigned int* vq = nullptr;      // 2 x 64 bin counters / offsets + the queue head
   cudaStream_t st = nullptr;
   GridDesc g;
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
@@ -293,7 +299,7 @@ void free_ctx(Ctx* c) {
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
-                  c->k0sum, c->K4lo, c->twdf};
+                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -844,6 +850,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.K4 = c->K4;
   a.K4f = c->prec == CPFFT_PREC_MIXED ? c->K4f : nullptr;
   a.K4lo = c->prec == CPFFT_PREC_MIXED && c->df_ok ? c->K4lo : nullptr;
+  a.tangent_f32 = c->prec == CPFFT_PREC_MIXED && c->tangent_f32;
   a.ori = c->ori;
   a.crys = c->crys;
   a.oris = c->oris;
@@ -884,6 +891,15 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.log_cap = c->log_cap;
   a.log_stride = c->log_stride;
   a.log_phase = c->log_phase;
+  a.perm = nullptr;
+  a.queue = nullptr;
+  a.cost = nullptr;
+  if (c->sched == CPFFT_SCHED_QUEUE && iter > 0) {
+    CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
+    a.perm = c->vperm;
+    a.queue = c->vq + 128;
+    a.cost = c->vcost;
+  }
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
   CK(launch_stress(a, warm, c->st));
@@ -1191,7 +1207,8 @@ int cpfft_set_mode(int precision, int warm_start) {
     cpfft_set_error("cpfft_set_mode: unknown precision %d", precision);
     return CPFFT_ERR_BAD_ARG;
   }
-  if (warm_start & ~(CPFFT_START_LEARNED | CPFFT_START_ITERATE | CPFFT_START_TRIAL)) {
+  if (warm_start & ~(CPFFT_START_LEARNED | CPFFT_START_ITERATE | CPFFT_START_TRIAL |
+                     CPFFT_TANGENT_F32)) {
     cpfft_set_error("cpfft_set_mode: unknown start flags %d", warm_start);
     return CPFFT_ERR_BAD_ARG;
   }
@@ -1207,7 +1224,8 @@ int cpfft_set_mode(int precision, int warm_start) {
   if (precision == CPFFT_PREC_MIXED) TRY(alloc_mixed(g_ctx));
   if (precision != g_ctx->prec) g_ctx->K4f_valid = false;
   g_ctx->prec = precision;
-  g_ctx->warm = warm_start;
+  g_ctx->warm = warm_start & (CPFFT_START_LEARNED | CPFFT_START_ITERATE | CPFFT_START_TRIAL);
+  g_ctx->tangent_f32 = (warm_start & CPFFT_TANGENT_F32) != 0;
   return 0;
 }
 
@@ -1226,6 +1244,23 @@ int cpfft_set_precond(int precond) {
     TRY(sync(c));
     TRY(reference_build(c));
   }
+  return 0;
+}
+
+int cpfft_set_schedule(int schedule) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (schedule != CPFFT_SCHED_BLOCKS && schedule != CPFFT_SCHED_QUEUE) {
+    cpfft_set_error("cpfft_set_schedule: unknown schedule %d", schedule);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (schedule == CPFFT_SCHED_QUEUE && !c->vcost) {
+    TRY(dalloc(c->vcost, c->N3));
+    TRY(dalloc(c->vperm, c->N3 * sizeof(int)));
+    TRY(dalloc(c->vq, 129 * sizeof(unsigned int)));
+    CK(cudaMemset(c->vcost, 0, c->N3));
+  }
+  c->sched = schedule;
   return 0;
 }
 

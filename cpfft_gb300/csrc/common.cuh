@@ -85,6 +85,11 @@ struct StressArgs {
   int start_iterate;
   int start_trial;
   int start_cap;
+  // voxel work queue (null perm: one block per 128 consecutive voxels)
+  const int* perm;            // (N3) voxel ids, heaviest previous-pass cost first
+  unsigned int* queue;        // next queue slot (zeroed by launch_voxel_queue)
+  unsigned char* cost;        // (N3) out: local iterations of this pass (null: not kept)
+  int tangent_f32;            // 1: dP/dF (cep2A) in FP32 (the fast form; it steers Newton only)
   // logging of (features, converged increments) pairs from the plain solve
   float* log_X;               // [cap][20], null: no logging
   float* log_T;               // [cap][7]
@@ -95,3 +100,7 @@ struct StressArgs {
 
 // warm = true: the learned initial guess starts the local Newton solve
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
+// Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost
+// bin, queue head zeroed.  scratch: 128 unsigned ints.
+cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,
+                               int* perm, unsigned int* queue, cudaStream_t s);

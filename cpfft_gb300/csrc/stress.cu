@@ -9,6 +9,8 @@
 // reciprocals hoisted out of the 12-slip loops, and cep2A's 81-term loops contracted
 // through 3x3 intermediates (about 1.6 kflop instead of ~20 kflop).  Every local loop
 // is bounded by miter and the line-search cap, so no thread can spin.
+#include <algorithm>
+
 #include "common.cuh"
 #include "mlp.cuh"
 
@@ -30,29 +32,33 @@ __device__ __forceinline__ double powabs(double x, int n_int, double e) {
   return n_int >= 0 ? ipow(fabs(x), n_int) : pow(fabs(x), e);
 }
 
-// ---- 3x3 helpers (row-major double[9]) ---------------------------------------------
-__device__ __forceinline__ void mm3(const double* a, const double* b, double* c) {
+// ---- 3x3 helpers (row-major [9]; FP64, or FP32 for the fast form's tangent) ------------
+template <typename R>
+__device__ __forceinline__ void mm3(const R* a, const R* b, R* c) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       c[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
 }
-__device__ __forceinline__ void mtm3(const double* a, const double* b, double* c) {  // a^T b
+template <typename R>
+__device__ __forceinline__ void mtm3(const R* a, const R* b, R* c) {  // a^T b
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       c[3 * i + j] = a[i] * b[j] + a[3 + i] * b[3 + j] + a[6 + i] * b[6 + j];
 }
-__device__ __forceinline__ void mmt3(const double* a, const double* b, double* c) {  // a b^T
+template <typename R>
+__device__ __forceinline__ void mmt3(const R* a, const R* b, R* c) {  // a b^T
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++)
       c[3 * i + j] = a[3 * i] * b[3 * j] + a[3 * i + 1] * b[3 * j + 1] + a[3 * i + 2] * b[3 * j + 2];
 }
-__device__ __forceinline__ double det3(const double* a) {
+template <typename R>
+__device__ __forceinline__ R det3(const R* a) {
   return a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
          a[2] * (a[3] * a[7] - a[4] * a[6]);
 }
@@ -572,16 +578,17 @@ __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jl
   return true;
 }
 
-// cep2A (src/cep2A.f:86-284), contracted through 3x3 intermediates.
+// cep2A (src/cep2A.f:86-284), contracted through 3x3 intermediates.  T = double (the
+// reference's arithmetic) or float (the fast form: the tangent only steers the global
+// Newton iteration, whose residual and stresses stay FP64).
 //   Fn, Fn1, Rh, R, fnhinv, finv: row-major 3x3;  t: unrotated Cauchy stress 3x3;
 //   C: 6x6 tangent (row-major, local);  J = det Fn1.  Writes A[81] (ij)(kl).
-__device__ void cep2A(const double* Fn, const double* Fn1, const double* t, const double* C,
-                      const double* Rh, const double* R, const double* fnhinv,
-                      const double* finv, double J, double* A, long long N3, double* K4,
-                      float* K4f) {
-  double U[9], Y[9], tmp[9], sigma[9], Uinv[9], tU[9], Rt[9], RY[9], RYR[9], RtRF[9];
+template <typename T>
+__device__ void cep2A(const T* Fn, const T* Fn1, const T* t, const T* C, const T* Rh, const T* R,
+                      const T* fnhinv, const T* finv, T J, T* A) {
+  T U[9], Y[9], tmp[9], sigma[9], Uinv[9], tU[9], Rt[9], RY[9], RYR[9], RtRF[9];
   mtm3(R, Fn1, U);
-  double trU = U[0] + U[4] + U[8];
+  T trU = U[0] + U[4] + U[8];
   for (int i = 0; i < 9; i++) Y[i] = -U[i];
   Y[0] += trU; Y[4] += trU; Y[8] += trU;
   mm3(R, t, Rt);
@@ -590,45 +597,45 @@ __device__ void cep2A(const double* Fn, const double* Fn1, const double* t, cons
   mm3(t, Uinv, tU);
   mm3(R, Y, RY);
   mmt3(RY, R, RYR);
-  double dY = 1.0 / det3(Y);
+  T dY = T(1) / det3(Y);
   mm3(Rt, Uinv, RtRF);
-  double Fnh[9], Uh[9], Yh[9], RYh[9], RYRh[9], Fp[9], L[9], D2[9];
-  for (int i = 0; i < 9; i++) { Fnh[i] = 0.5 * (Fn1[i] + Fn[i]); Fp[i] = 0.5 * fnhinv[i]; tmp[i] = Fn1[i] - Fn[i]; }
+  T Fnh[9], Uh[9], Yh[9], RYh[9], RYRh[9], Fp[9], L[9], D2[9];
+  for (int i = 0; i < 9; i++) { Fnh[i] = T(0.5) * (Fn1[i] + Fn[i]); Fp[i] = T(0.5) * fnhinv[i]; tmp[i] = Fn1[i] - Fn[i]; }
   mtm3(Rh, Fnh, Uh);
-  double trUh = Uh[0] + Uh[4] + Uh[8];
+  T trUh = Uh[0] + Uh[4] + Uh[8];
   for (int i = 0; i < 9; i++) Yh[i] = -Uh[i];
   Yh[0] += trUh; Yh[4] += trUh; Yh[8] += trUh;
   mm3(Rh, Yh, RYh);
   mmt3(RYh, Rh, RYRh);
-  double hY = 0.5 / det3(Yh);
+  T hY = T(0.5) / det3(Yh);
   mm3(tmp, Fp, L);
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) D2[3 * i + j] = L[3 * i + j] + L[3 * j + i];
   // dt/dF pieces: E = D2 Rh, A1 = RYRh^T E, B1 = RYh^T E, a = Rh^T (I - L), b = Fp Rh
-  double E[9], A1[9], B1[9], M[9], am[9], bm[9];
+  T E[9], A1[9], B1[9], M[9], am[9], bm[9];
   mm3(D2, Rh, E);
   mtm3(RYRh, E, A1);
   mtm3(RYh, E, B1);
   for (int i = 0; i < 9; i++) M[i] = -L[i];
-  M[0] += 1.0; M[4] += 1.0; M[8] += 1.0;
+  M[0] += T(1); M[4] += T(1); M[8] += T(1);
   mtm3(Rh, M, am);
   mm3(Fp, Rh, bm);
   // dt1[(i,j),(p,q)] is symmetric in (i,j); keep its 6 Voigt rows, shear rows doubled
-  double w[6][9];
+  T w[6][9];
   for (int v = 0; v < 6; v++) {
     int i = c_vi[v], j = c_vj[v];
     for (int p = 0; p < 3; p++)
       for (int q = 0; q < 3; q++) {
-        double d13 = hY * (A1[3 * p + j] * Yh[3 * q + i] - B1[3 * q + j] * RYh[3 * p + i]) +
+        T d13 = hY * (A1[3 * p + j] * Yh[3 * q + i] - B1[3 * q + j] * RYh[3 * p + i]) +
                      hY * (A1[3 * p + i] * Yh[3 * q + j] - B1[3 * q + i] * RYh[3 * p + j]);
-        double d2 = am[3 * i + p] * bm[3 * q + j] + bm[3 * q + i] * am[3 * j + p];
-        double s = d13 + d2;
-        w[v][3 * p + q] = v < 3 ? s : 2.0 * s;
+        T d2 = am[3 * i + p] * bm[3 * q + j] + bm[3 * q + i] * am[3 * j + p];
+        T s = d13 + d2;
+        w[v][3 * p + q] = v < 3 ? s : T(2) * s;
       }
   }
   // T_pq[m][n] = sum_v C[v][vm(mn)] w[v][pq] (cep2A_ddot44 with the row index summed)
   // P-terms: P0 + P1 + P2 + P4 from 3x3 products, P3 = J R T_kl Uinv
-  double S1[9], YtU[9], RYtU[9], RtYt[9], fRYR[9], RtRYt[9], fRY[9], dJ[9];
+  T S1[9], YtU[9], RYtU[9], RtYt[9], fRYR[9], RtRYt[9], fRY[9], dJ[9];
   mmt3(sigma, finv, S1);
   mm3(Y, tU, YtU);
   mm3(RY, tU, RYtU);
@@ -638,32 +645,31 @@ __device__ void cep2A(const double* Fn, const double* Fn1, const double* t, cons
   mm3(finv, RY, fRY);
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) dJ[3 * i + j] = finv[3 * j + i] * J;
-  const double JdY = J * dY;
+  const T JdY = J * dY;
   for (int k = 0; k < 3; k++)
     for (int l = 0; l < 3; l++) {
       int pq = 3 * k + l;
-      double T[9];
+      T Tk[9];
       for (int u = 0; u < 6; u++) {  // distinct (m,n) Voigt column u
-        double s = 0.0;
+        T s = T(0);
         for (int v = 0; v < 6; v++) s += C[6 * v + u] * w[v][pq];
         int m = c_vi[u], n = c_vj[u];
-        T[3 * m + n] = s;
-        T[3 * n + m] = s;
+        Tk[3 * m + n] = s;
+        Tk[3 * n + m] = s;
       }
-      double RT[9], RTU[9];
-      mm3(R, T, RT);
+      T RT[9], RTU[9];
+      mm3(R, Tk, RT);
       mm3(RT, Uinv, RTU);
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
-          double P0 = RtRF[3 * i + j] * dJ[3 * k + l];
-          double P1 = -J * S1[3 * i + l] * finv[3 * j + k];
-          double P2 = JdY * (RYR[3 * i + k] * YtU[3 * l + j] - RY[3 * i + l] * RYtU[3 * k + j]);
-          double P3 = J * RTU[3 * i + j];
-          double P4 = JdY * (RtYt[3 * i + l] * fRYR[3 * j + k] - RtRYt[3 * i + k] * fRY[3 * j + l]);
-          double a = P0 + P1 + P2 + P3 + P4;
+          T P0 = RtRF[3 * i + j] * dJ[3 * k + l];
+          T P1 = -J * S1[3 * i + l] * finv[3 * j + k];
+          T P2 = JdY * (RYR[3 * i + k] * YtU[3 * l + j] - RY[3 * i + l] * RYtU[3 * k + j]);
+          T P3 = J * RTU[3 * i + j];
+          T P4 = JdY * (RtYt[3 * i + l] * fRYR[3 * j + k] - RtRYt[3 * i + k] * fRY[3 * j + l]);
+          T a = P0 + P1 + P2 + P3 + P4;
           long long col = 9 * (3 * i + j) + pq;
           A[col] = a;
-          (void)N3; (void)K4; (void)K4f;
         }
     }
 }
@@ -732,13 +738,16 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
 
 // WARM: the learned initial guess starts each local Newton solve (launches with iter > 0
 // only); every thread of the block takes part in the block-level network evaluation, so
-// the tail block's surplus threads evaluate a copy of the last voxel and store nothing.
+// the tail chunk's surplus threads evaluate a copy of the last voxel and store nothing.
+//
+// Voxel order: one block per 128 consecutive voxels, or (a.perm != null) the voxel work
+// queue: persistent blocks take 128-voxel chunks of a.perm -- voxels sorted by the local
+// cost of their previous pass, heaviest first -- from the atomic head a.queue, so a warp
+// holds voxels of similar iteration counts and the SMs even out at the tail.
 template <bool WARM>
 __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
-  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = v < a.N3;
-  int iters = 0, piters = 0, rej = 0;
-  bool ok = true;
+  int iters = 0, piters = 0, rej = 0, fails = 0;
+  GuessBlock gb{nullptr, 0u, nullptr, 0u};
   if (WARM) {
     extern __shared__ __align__(128) unsigned char guess_smem[];
     __shared__ __align__(8) uint64_t bar;
@@ -747,15 +756,42 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
       tc::mbar_init(&bar, 1);
       tc::fence_mbar_init();
     }
-    GuessBlock gb{guess_smem, mlp::tmem_block_alloc(&tslot, 256), &bar, 0u};
-    voxel_update<true>(a, valid ? v : a.N3 - 1, valid, iters, piters, ok, rej, &gb);
-    mlp::tmem_block_free(gb.tmem, 256);
-    if (!valid) { iters = 0; piters = 0; ok = true; rej = 0; }
-  } else if (valid) {
-    voxel_update<false>(a, v, true, iters, piters, ok, rej, nullptr);
+    gb = GuessBlock{guess_smem, mlp::tmem_block_alloc(&tslot, 256), &bar, 0u};
   }
+  __shared__ long long chunk;
+  for (long long round = 0;; round++) {
+    long long base;
+    if (a.perm) {
+      if (threadIdx.x == 0) chunk = (long long)atomicAdd(a.queue, 128u);
+      __syncthreads();
+      base = chunk;
+      __syncthreads();
+    } else {
+      base = (long long)blockIdx.x * 128;
+    }
+    if (base >= a.N3 || (!a.perm && round > 0)) break;
+    const long long idx = base + threadIdx.x;
+    const bool valid = idx < a.N3;
+    const long long last = a.N3 - 1;
+    const long long v = a.perm ? (long long)a.perm[valid ? idx : last] : (valid ? idx : last);
+    int it = 0, pit = 0, rj = 0;
+    bool ok = true;
+    if (WARM) {
+      voxel_update<true>(a, v, valid, it, pit, ok, rj, &gb);
+    } else if (valid) {
+      voxel_update<false>(a, v, true, it, pit, ok, rj, nullptr);
+    }
+    if (valid) {
+      iters += it;
+      piters += pit;
+      rej += rj;
+      fails += ok ? 0 : 1;
+      if (a.cost) a.cost[v] = (unsigned char)min(it + pit, 255);
+    }
+  }
+  if (WARM) mlp::tmem_block_free(gb.tmem, 256);
   // statistics, warp-aggregated (every lane of the warp reaches this point)
-  unsigned long long li = iters, pi = piters, fl = ok ? 0 : 1, rj = rej;
+  unsigned long long li = iters, pi = piters, fl = fails, rj = rej;
   for (int o = 16; o > 0; o >>= 1) {
     li += __shfl_down_sync(0xffffffffu, li, o);
     pi += __shfl_down_sync(0xffffffffu, pi, o);
@@ -767,6 +803,65 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
     atomicAdd(a.stats + 1, fl);
     atomicAdd(a.stats + 2, pi);
     atomicAdd(a.stats + 3, rj);
+  }
+}
+
+// ---- the voxel work queue: voxels sorted by the cost of their previous pass -----------
+constexpr int QBINS = 64;  // costs 0 .. 62 and >= 63 (iterations of the local solve)
+
+// per-bin voxel counts (hist zeroed before)
+__global__ void __launch_bounds__(256) k_cost_hist(const unsigned char* __restrict__ cost,
+                                                   long long N3, unsigned int* __restrict__ hist) {
+  __shared__ unsigned int h[QBINS];
+  for (int b = threadIdx.x; b < QBINS; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N3;
+       v += (long long)gridDim.x * blockDim.x)
+    atomicAdd(&h[min((int)cost[v], QBINS - 1)], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < QBINS; b += blockDim.x)
+    if (h[b]) atomicAdd(&hist[b], h[b]);
+}
+
+// first queue slot of every bin, heaviest bin first (one block of QBINS threads); also
+// resets the queue head
+__global__ void k_cost_offsets(const unsigned int* __restrict__ hist, unsigned int* __restrict__ offs,
+                               unsigned int* __restrict__ queue) {
+  __shared__ unsigned int h[QBINS];
+  h[threadIdx.x] = hist[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int run = 0;
+    for (int b = QBINS - 1; b >= 0; b--) {
+      offs[b] = run;
+      run += h[b];
+    }
+    *queue = 0u;
+  }
+}
+
+// scatter voxel ids into their bins' ranges: each block reserves its bins' slots with one
+// atomic per bin, then fills them (order inside a bin is arbitrary)
+__global__ void __launch_bounds__(256) k_cost_scatter(const unsigned char* __restrict__ cost,
+                                                      long long N3, long long per_block,
+                                                      unsigned int* __restrict__ offs,
+                                                      int* __restrict__ perm) {
+  __shared__ unsigned int cnt[QBINS], start[QBINS];
+  for (int b = threadIdx.x; b < QBINS; b += blockDim.x) cnt[b] = 0;
+  __syncthreads();
+  const long long v0 = (long long)blockIdx.x * per_block;
+  const long long v1 = min(v0 + per_block, N3);
+  for (long long v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+    atomicAdd(&cnt[min((int)cost[v], QBINS - 1)], 1u);
+  __syncthreads();
+  for (int b = threadIdx.x; b < QBINS; b += blockDim.x) {
+    start[b] = cnt[b] ? atomicAdd(&offs[b], cnt[b]) : 0u;
+    cnt[b] = 0;
+  }
+  __syncthreads();
+  for (long long v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+    const int b = min((int)cost[v], QBINS - 1);
+    perm[start[b] + atomicAdd(&cnt[b], 1u)] = (int)v;
   }
 }
 
@@ -1060,8 +1155,24 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     mmt3(T, fn1inv, P);  // T F^-T
     for (int i = 0; i < 9; i++) a.P[i * N3 + v] = detF * P[i];
   }
+  if (a.tangent_f32) {
+    // the fast form's tangent in FP32 (K4 = K4f exactly, K4lo = 0)
+    float f[9], f1[9], tf[9], rh[9], r1[9], fhi[9], f1i[9], cf[36], Af[81];
+    for (int i = 0; i < 9; i++) {
+      f[i] = (float)Fn[i]; f1[i] = (float)Fn1[i]; tf[i] = (float)tm[i]; rh[i] = (float)rnh[i];
+      r1[i] = (float)rn1[i]; fhi[i] = (float)fnhinv[i]; f1i[i] = (float)fn1inv[i];
+    }
+    for (int i = 0; i < 36; i++) cf[i] = (float)cep[i];
+    cep2A<float>(f, f1, tf, cf, rh, r1, fhi, f1i, (float)detF, Af);
+    for (int m = 0; m < 81; m++) a.K4[m * N3 + v] = (double)Af[m];
+    if (a.K4f)
+      for (int m = 0; m < 81; m++) a.K4f[m * N3 + v] = Af[m];
+    if (a.K4lo)
+      for (int m = 0; m < 81; m++) a.K4lo[m * N3 + v] = 0.0f;
+    return;
+  }
   double A[81];
-  cep2A(Fn, Fn1, tm, cep, rnh, rn1, fnhinv, fn1inv, detF, A, N3, a.K4, a.K4f);
+  cep2A<double>(Fn, Fn1, tm, cep, rnh, rn1, fnhinv, fn1inv, detF, A);
   for (int m = 0; m < 81; m++) a.K4[m * N3 + v] = A[m];
   if (a.K4f)
     for (int m = 0; m < 81; m++) a.K4f[m * N3 + v] = (float)A[m];
@@ -1076,20 +1187,49 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
 
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;
-  unsigned blocks = (unsigned)((a.N3 + 127) / 128);
-  if (warm) {
-    static bool attr = false;
-    if (!attr) {
-      cudaError_t e = cudaFuncSetAttribute(stress_kernel<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           mlp::FWD_SMEM);
-      if (e != cudaSuccess) return e;
-      attr = true;
-    }
-    stress_kernel<true><<<blocks, 128, mlp::FWD_SMEM, s>>>(a);
-  } else {
-    stress_kernel<false><<<blocks, 128, 0, s>>>(a);
+  static bool attr = false;
+  if (warm && !attr) {
+    cudaError_t e = cudaFuncSetAttribute(stress_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         mlp::FWD_SMEM);
+    if (e != cudaSuccess) return e;
+    attr = true;
   }
+  unsigned blocks = (unsigned)((a.N3 + 127) / 128);
+  if (a.perm) {
+    // persistent: as many blocks as fit on the GPU at once
+    static int resident[2] = {0, 0};
+    int& r = resident[warm ? 1 : 0];
+    if (!r) {
+      int dev = 0, sms = 0, per = 0;
+      cudaError_t e;
+      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+      e = warm ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<true>, 128, mlp::FWD_SMEM)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<false>, 128, 0);
+      if (e != cudaSuccess) return e;
+      r = sms * (per > 0 ? per : 1);
+    }
+    blocks = (unsigned)std::min<long long>((long long)r, (long long)blocks);
+  }
+  if (warm) stress_kernel<true><<<blocks, 128, mlp::FWD_SMEM, s>>>(a);
+  else stress_kernel<false><<<blocks, 128, 0, s>>>(a);
   g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,
+                               int* perm, unsigned int* queue, cudaStream_t s) {
+  unsigned int* hist = scratch;
+  unsigned int* offs = scratch + QBINS;
+  cudaError_t e = cudaMemsetAsync(hist, 0, QBINS * sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  const int hb = (int)std::min<long long>((N3 + 255) / 256, 1024);
+  k_cost_hist<<<hb, 256, 0, s>>>(cost, N3, hist);
+  k_cost_offsets<<<1, QBINS, 0, s>>>(hist, offs, queue);
+  const long long per_block = 8192;
+  k_cost_scatter<<<(unsigned)((N3 + per_block - 1) / per_block), 256, 0, s>>>(cost, N3, per_block,
+                                                                             offs, perm);
+  g_kernel_launches += 3;
   return cudaGetLastError();
 }

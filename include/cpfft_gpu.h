@@ -134,10 +134,15 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg,
  *                        load step: that pass's converged local state (precedence over
  *                        the other two on those passes)
  *   CPFFT_START_TRIAL    the elastic trial sigma_n + C D, tau extrapolated, returned to
- *                        98 % of the rate surface (ignored with CPFFT_START_LEARNED) */
+ *                        98 % of the rate surface (ignored with CPFFT_START_LEARNED)
+ * and, with CPFFT_PREC_MIXED,
+ *   CPFFT_TANGENT_F32    the consistent tangent dP/dF (cep2A) evaluated in FP32: it only
+ *                        steers the global Newton iteration (stresses, local solves and
+ *                        every residual stay FP64); K4 then holds the FP32 values */
 #define CPFFT_START_LEARNED  1
 #define CPFFT_START_ITERATE  2
 #define CPFFT_START_TRIAL    4
+#define CPFFT_TANGENT_F32    8
 int cpfft_set_mode(int precision, int warm_start);
 
 /* Preconditioner of the FP32 inner iterations of CPFFT_PREC_MIXED (extension; the
@@ -152,6 +157,16 @@ int cpfft_set_mode(int precision, int warm_start);
 #define CPFFT_PRECOND_NONE       0
 #define CPFFT_PRECOND_REFERENCE  1
 int cpfft_set_precond(int precond);
+
+/* Voxel order of the implicit stress passes (extension; the reference runs OpenMP over
+ * 128-voxel blocks in order, src/drive_eps_sig.f:31-39).  CPFFT_SCHED_BLOCKS: one thread
+ * block per 128 consecutive voxels.  CPFFT_SCHED_QUEUE: a persistent kernel whose blocks
+ * take 128-voxel chunks from a device work queue ordered by each voxel's local iteration
+ * count in its previous implicit pass, heaviest first, so the threads of a warp iterate
+ * alike and the SMs finish together.  Results are identical; only the timing changes. */
+#define CPFFT_SCHED_BLOCKS  0
+#define CPFFT_SCHED_QUEUE   1
+int cpfft_set_schedule(int schedule);
 
 /*
  * Stress update of every voxel: replaces drive_eps_sig(step, iter)

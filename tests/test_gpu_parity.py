@@ -148,8 +148,10 @@ def test_load_step_parity(gpulib, oracle, case):
                         precision=precision)
     if case in ("mixed_precond", "mixed_fast"):
         s.set_precond(gpulib.PRECOND_REFERENCE)
-    if case == "mixed_fast":  # the fast local starts too (local solves to the same tolerance)
-        s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL)
+    if case == "mixed_fast":  # the fast local starts and FP32 tangent too
+        s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL |
+                   gpulib.TANGENT_F32)
+        s.set_schedule(gpulib.SCHED_QUEUE)
     load = rve.uniaxial_tension(inc * 20, 20)
     try:
         s.nr3_begin(1e-10)
@@ -238,7 +240,8 @@ def test_green_double_float(gpulib, N):
 
 def test_mixed_fast_vs_fp64_32(gpulib):
     """The fast form at a warp-FFT size (FP32 inner CG with the reference-medium
-    preconditioner, double-float outer residuals, iterate + trial local starts) against the
+    preconditioner, double-float outer residuals, iterate + trial local starts, FP32
+    tangent, voxel-queue stress passes) against the
     plain FP64 form (itself checked against the oracle above) on the same 32^3 RVE: P_bar
     within 1e-6 relative, per-voxel P within 1e-5, the same global iteration counts."""
     N = 32
@@ -250,8 +253,10 @@ def test_mixed_fast_vs_fp64_32(gpulib):
                           gpulib.PREC_MIXED if fast else gpulib.PREC_FP64)
         try:
             if fast:
-                s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL)
+                s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL |
+                           gpulib.TANGENT_F32)
                 s.set_precond(gpulib.PRECOND_REFERENCE)
+                s.set_schedule(gpulib.SCHED_QUEUE)
             s.nr3_begin(1e-10)
             pb, its = [], []
             for step in range(1, 4):
@@ -267,3 +272,32 @@ def test_mixed_fast_vs_fp64_32(gpulib):
     assert rel(pb1, pb0) < 1e-6, rel(pb1, pb0)
     assert per_voxel_rel(P1, P0) < 1e-5
     assert it1 == it0
+
+
+def test_voxel_queue_schedule_is_exact(gpulib):
+    """The persistent kernel's cost-sorted voxel queue computes every voxel exactly as the
+    in-order blocks do: identical fields and iteration counts after load steps."""
+    N = 16
+    r = rve.make_rve(N, 8, 29)
+    load = rve.uniaxial_tension(0.02, 20)
+    out = []
+    for sched in (gpulib.SCHED_BLOCKS, gpulib.SCHED_QUEUE):
+        s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                          gpulib.PREC_MIXED)
+        try:
+            s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL)
+            s.set_precond(gpulib.PRECOND_REFERENCE)
+            s.set_schedule(sched)
+            s.nr3_begin(1e-10)
+            its = []
+            for step in range(1, 4):
+                rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+                assert rc == 0
+                its.append((st["newton_iters"], st["cg_iters"], st["local_iters"]))
+            F, P, H = s.fields(history=True)
+            out.append((F, P, H, its))
+        finally:
+            s.close()
+    (F0, P0, H0, i0), (F1, P1, H1, i1) = out
+    assert i0 == i1
+    assert np.array_equal(P0, P1) and np.array_equal(F0, F1) and np.array_equal(H0, H1)
