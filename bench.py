@@ -430,6 +430,7 @@ def gb300_arm(args):
                             "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in stats) / (N3 * su),
                             "guess_rejected": [s["guess_rejected"] for s in stats]},
         "learned": learned,
+        "autotuned_tiles": solver.tuning() if prec == cp.PREC_MIXED else None,
         "fp64_peak_tflops": fp64_peak,
         "clocks": clk,
         "cpu_baseline": cpu,

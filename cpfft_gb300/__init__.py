@@ -88,6 +88,7 @@ SIGNATURES = {
     "cpfft_set_mode": (_I, [_I, _I]),
     "cpfft_set_precond": (_I, [_I]),
     "cpfft_set_schedule": (_I, [_I]),
+    "cpfft_tuning": (_I, [_IP, _DP]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
@@ -243,6 +244,14 @@ class Solver:
     def set_schedule(self, schedule=SCHED_QUEUE):
         """Voxel order of the implicit stress passes: blocks in order, or the work queue."""
         _check(load_library().cpfft_set_schedule(int(schedule)), "cpfft_set_schedule")
+
+    def tuning(self):
+        """Autotuned tile shapes {fp32: (B/D, C), double_float: (B/D, C)} and ms/apply."""
+        t = np.zeros(4, np.int32)
+        ms = np.zeros(2)
+        _check(load_library().cpfft_tuning(t.ctypes.data_as(_IP), _dp(ms)), "cpfft_tuning")
+        return {"fp32_tiles": t[:2].tolist(), "double_float_tiles": t[2:].tolist(),
+                "fp32_ms": float(ms[0]), "double_float_ms": float(ms[1])}
 
     def set_precond(self, precond=PRECOND_REFERENCE):
         """Reference-medium preconditioner of the mixed-precision inner iterations."""

@@ -204,6 +204,8 @@ struct Ctx {
   float* K4lo = nullptr;
   dfl2* twdf = nullptr;
   bool df_ok = false;
+  GridDesc gdf;            // the double-float operator's tile shapes (autotuned)
+  float tune_ms[2] = {0.f, 0.f};  // autotuned time per apply: FP32, double-float
   int *ori = nullptr, *crys = nullptr;
   OriRec* oris = nullptr;
   CrysRec* cryss = nullptr;
@@ -360,7 +362,7 @@ int matvec_acc(Ctx* c, const double* x, double* y, int flgK) {
   c->f64_matvecs++;
   kt_start(c, KT_G64);
   TRY(cuda_check(green_apply_df(x, c->K4f, c->K4lo, flgK, y, reinterpret_cast<dfl2*>(c->S),
-                                c->twdf, c->g, c->st),
+                                c->twdf, c->gdf, c->st),
                  "green_apply double-float"));
   return kt_stop(c);
 }
@@ -1017,6 +1019,7 @@ int need_ctx() {
 int alloc_mixed(Ctx* c) {
   const long long n = 9 * c->N3;
   if (c->K4f) return 0;
+  const long long launches0 = g_kernel_launches;
   TRY(dalloc(c->w2, n * sizeof(double)));
   TRY(dalloc(c->K4f, 81 * c->N3 * sizeof(float)));
   TRY(dalloc(c->xf, n * sizeof(float)));
@@ -1046,6 +1049,21 @@ int alloc_mixed(Ctx* c) {
     CK(cudaMemcpy(c->twdf, tw.data(), c->N * sizeof(dfl2), cudaMemcpyHostToDevice));
     CK(green_setup_df(c->N));
     c->df_ok = true;
+    // tile shapes of both operators, timed on this GPU with this grid's buffers
+    CK(cudaMemsetAsync(c->K4f, 0, 81 * c->N3 * sizeof(float), c->st));
+    CK(cudaMemsetAsync(c->K4lo, 0, 81 * c->N3 * sizeof(float), c->st));
+    CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+    CK(cudaMemsetAsync(c->io, 0, n * sizeof(double), c->st));
+    CK(green_autotune_f32(c->xf, c->K4f, c->Apf, c->Sf, c->twf, &c->g, c->st, &c->tune_ms[0]));
+    c->gdf = c->g;
+    c->gdf.wtc = 0;
+    CK(green_autotune_df(c->io, c->K4f, c->K4lo, c->b, reinterpret_cast<dfl2*>(c->S), c->twdf,
+                         &c->gdf, c->st, &c->tune_ms[1]));
+    g_kernel_launches = launches0;  // tuning launches are not the caller's work
+    if (c->log)
+      fprintf(stderr, "       autotuned tiles: FP32 B/D %d C %d (%.3f ms), double-float B/D %d C %d "
+              "(%.3f ms)\n", c->g.wtb, c->g.wtc, c->tune_ms[0], c->gdf.wtb, c->gdf.wtc,
+              c->tune_ms[1]);
   }
   return 0;
 }
@@ -1243,6 +1261,22 @@ int cpfft_set_precond(int precond) {
     TRY(reference_reduce(c));
     TRY(sync(c));
     TRY(reference_build(c));
+  }
+  return 0;
+}
+
+int cpfft_tuning(int* tiles, double* ms) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (tiles) {
+    tiles[0] = c->g.wtb;
+    tiles[1] = c->g.wtc;
+    tiles[2] = c->gdf.wtb;
+    tiles[3] = c->gdf.wtc;
+  }
+  if (ms) {
+    ms[0] = c->tune_ms[0];
+    ms[1] = c->tune_ms[1];
   }
   return 0;
 }

@@ -22,6 +22,8 @@ struct GridDesc {
   double inv_n3;     // backward scale 1/N^3
   int tkb, tkc;      // columns per block in passes B and C
   int pre = 0;       // FP32 passes: 1 = reference-medium operator (green_set_reference)
+  int wtb = 16, wtc = 0;  // warp passes: columns per block of passes B/D and of pass C (0: 4 for
+                          // FP32, 2 for double-float)
   FftPlan plan;
 };
 
@@ -66,3 +68,12 @@ bool green_df_supported(int N);
 cudaError_t green_setup_df(int N);
 cudaError_t green_apply_df(const double* x, const float* K4hi, const float* K4lo, int flgK,
                            double* y, dfl2* S, const dfl2* tw, GridDesc g, cudaStream_t st);
+
+// Autotuner of the warp passes' tile shapes: times every candidate (columns per block of
+// passes B/D in {8, 16, 32} x of pass C in {2, 4}) on the given buffers with CUDA events
+// and stores the fastest in g->wtb / g->wtc (best_ms: its time per apply).  The buffers'
+// contents are overwritten (y, S).  No-op for sizes without warp passes.
+cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2* S,
+                               const float2* tw, GridDesc* g, cudaStream_t st, float* best_ms);
+cudaError_t green_autotune_df(const double* x, const float* K4hi, const float* K4lo, double* y,
+                              dfl2* S, const dfl2* tw, GridDesc* g, cudaStream_t st, float* best_ms);

@@ -168,6 +168,14 @@ int cpfft_set_precond(int precond);
 #define CPFFT_SCHED_QUEUE   1
 int cpfft_set_schedule(int schedule);
 
+/* Tile shapes the autotuner chose for this grid when CPFFT_PREC_MIXED was first selected
+ * (extension): columns per block of the transform passes along the middle axis (both
+ * directions) and along the slowest axis (with the Green contraction), for the FP32
+ * operator (tiles[0], tiles[1]) and the double-float operator (tiles[2], tiles[3]); ms:
+ * the measured time per apply of each.  Zeros before the mixed form is selected or for
+ * grids the register passes do not cover (N other than 32, 64, 128, 256). */
+int cpfft_tuning(int* tiles, double* ms);
+
 /*
  * Stress update of every voxel: replaces drive_eps_sig(step, iter)
  * (src/drive_eps_sig.f:16-45, do_nleps_block :57-340, rstgp1/mm10 below it).
