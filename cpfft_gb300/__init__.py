@@ -79,6 +79,23 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Rve(ctypes.Structure):
+    """``cpfft_rve`` of include/cpfft_gpu.h (one RVE of cpfft_batch_solve)."""
+
+    _fields_ = [
+        ("N", ctypes.c_int), ("matList", ctypes.POINTER(ctypes.c_int)),
+        ("kocks_deg", ctypes.POINTER(ctypes.c_double)), ("props", ctypes.POINTER(Crystal)),
+        ("ncrystals", ctypes.c_int), ("tstep", ctypes.c_double), ("g_mapping", ctypes.c_int),
+        ("nsteps", ctypes.c_int), ("BC_all", ctypes.POINTER(ctypes.c_double)),
+        ("isNBC", ctypes.POINTER(ctypes.c_int)),
+        ("Pbar", ctypes.POINTER(ctypes.c_double)), ("Fn1", ctypes.POINTER(ctypes.c_double)),
+        ("Pn1", ctypes.POINTER(ctypes.c_double)), ("status", ctypes.c_int),
+        ("steps_done", ctypes.c_int), ("voxel_updates", ctypes.c_longlong),
+        ("cg_iters", ctypes.c_longlong), ("seconds", ctypes.c_double),
+        ("error", ctypes.c_char * 160),
+    ]
+
+
 # every exported symbol and its signature
 _D, _I, _P = ctypes.c_double, ctypes.c_int, ctypes.POINTER
 _DP, _IP = _P(_D), _P(_I)
@@ -89,6 +106,7 @@ SIGNATURES = {
     "cpfft_set_precond": (_I, [_I]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
+    "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
@@ -343,3 +361,44 @@ class Solver:
 
     def set_F(self, Fn=None, Fn1=None):
         _check(load_library().cpfft_set_F(_dp(Fn), _dp(Fn1)), "set_F")
+
+
+def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE,
+                schedule=SCHED_QUEUE, tolNR=1e-5, tolPCG=1e-10, maxIter=20, nthreads=4,
+                want_fields=False):
+    """Solve many RVEs at once (cpfft_batch_solve).  rves: dicts with N, mat_list, kocks,
+    crystals, tstep, g_mapping and a loading (rve.Loading: BC_all, isNBC, nsteps used).
+    Returns one dict per RVE: Pbar (nsteps, 9), status, voxel_updates, cg_iters, seconds,
+    and (want_fields) F, P (9, N3)."""
+    L = load_library()
+    arr = (Rve * len(rves))()
+    keep, out = [], []
+    for k, d in enumerate(rves):
+        N, N3 = d["N"], d["N"] ** 3
+        ml = np.ascontiguousarray(d["mat_list"], dtype=np.int32)
+        ka = np.ascontiguousarray(np.asarray(d["kocks"], dtype=np.float64).reshape(3, N3))
+        cr = crystal_struct(d["crystals"])
+        nsteps = int(d["nsteps"])
+        bc = np.ascontiguousarray(np.asarray(d["BC_all"], dtype=np.float64)[:nsteps])
+        nb = np.ascontiguousarray(d["isNBC"], dtype=np.int32)
+        pb = np.zeros((nsteps, 9))
+        F = np.zeros((9, N3)) if want_fields else None
+        P = np.zeros((9, N3)) if want_fields else None
+        keep += [ml, ka, cr, bc, nb, pb, F, P]
+        r = arr[k]
+        r.N, r.ncrystals, r.tstep, r.g_mapping, r.nsteps = N, len(d["crystals"]), d["tstep"], \
+            d.get("g_mapping", G_CENTERED), nsteps
+        r.matList = ml.ctypes.data_as(_IP)
+        r.kocks_deg, r.BC_all, r.Pbar = _dp(ka), _dp(bc), _dp(pb)
+        r.props = ctypes.cast(cr, ctypes.POINTER(Crystal))
+        r.isNBC = nb.ctypes.data_as(_IP)
+        r.Fn1, r.Pn1 = _dp(F), _dp(P)
+        out.append({"Pbar": pb, "F": F, "P": P})
+    rc = L.cpfft_batch_solve(arr, len(rves), precision, options, precond, schedule, tolNR,
+                             tolPCG, maxIter, nthreads)
+    for k, o in enumerate(out):
+        r = arr[k]
+        o.update(status=r.status, steps_done=r.steps_done, voxel_updates=r.voxel_updates,
+                 cg_iters=r.cg_iters, seconds=r.seconds, error=r.error.decode())
+    _check(rc, "cpfft_batch_solve")
+    return out

@@ -2,11 +2,15 @@
 // host-side control of the resident Newton-Krylov loop (FFT_nr3 / fftPcg /
 // tangent_homo / NBC_update of src/FFT_nr3.f and src/tangent_homo.f).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <numeric>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -19,13 +23,25 @@ bool mlp_device_weights(mlp::Weights* w, int** err);
 int mlp_check_error();
 #include "krylov.cuh"
 
-static char g_err[512] = "";
-long long g_kernel_launches = 0;
+// per host thread: a thread drives one context (cpfft_batch_solve runs several at once)
+static thread_local char g_err[512] = "";
+thread_local long long g_kernel_launches = 0;
 void cpfft_set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(g_err, sizeof(g_err), fmt, ap);
   va_end(ap);
+}
+
+cudaError_t raise_max_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<const void*, size_t> set;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[func];
+  if (bytes <= cur) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
 }
 
 namespace {
@@ -230,6 +246,7 @@ struct Ctx {
   double* k0sum = nullptr; // (81) component sums of K4f
   double* h_k0 = nullptr;  // pinned (81) copy
   float* h_pre = nullptr;  // pinned: 36 acoustic coefficients + 81 entries of K0
+  float* pre_dev = nullptr;  // the same on the device (read by the preconditioned kernels)
   // FFT_nr3 locals that persist across steps (Fortran DATA => SAVE, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
   // counters of the current step
@@ -276,7 +293,7 @@ int kt_stop(Ctx* c) {
 void kt_reset(Ctx* c) {
   for (int k = 0; k < 4; k++) { c->kt_acc[k] = 0; c->kt_cnt[k] = 0; }
 }
-Ctx* g_ctx = nullptr;
+thread_local Ctx* g_ctx = nullptr;
 
 #define TRY(expr)                 \
   do {                            \
@@ -301,7 +318,7 @@ void free_ctx(Ctx* c) {
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
-                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq};
+                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq, c->pre_dev};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -399,6 +416,8 @@ int matvec32_alpha(Ctx* c, const float* x, float* y) {
 int reference_reduce(Ctx* c) {
   if (!c->k0sum) {
     TRY(dalloc(c->k0sum, 81 * sizeof(double)));
+    TRY(dalloc(c->pre_dev, (36 + 81) * sizeof(float)));
+    c->g.acoef = c->pre_dev;
     if (cudaMallocHost((void**)&c->h_k0, 81 * sizeof(double)) != cudaSuccess ||
         cudaMallocHost((void**)&c->h_pre, (36 + 81) * sizeof(float)) != cudaSuccess) {
       cpfft_set_error("cudaMallocHost failed");
@@ -460,8 +479,8 @@ int reference_build(Ctx* c) {
   if (!(lo > 1.0e-9)) return 0;
   for (int k = 0; k < 36; k++) c->h_pre[k] = (float)coef[k];
   for (int k = 0; k < 81; k++) c->h_pre[36 + k] = (float)K0[k];
-  CK(green_set_reference(c->h_pre, c->st));
-  CK(dev_set_k0(c->h_pre + 36, c->st));
+  CK(cudaMemcpyAsync(c->pre_dev, c->h_pre, (36 + 81) * sizeof(float), cudaMemcpyHostToDevice,
+                     c->st));
   c->pre_ok = true;
   return 0;
 }
@@ -644,7 +663,7 @@ int cg_pre_body(Ctx* c, bool use_handle, bool timed) {
     return CPFFT_ERR_CUDA;
   }
   CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
-  CK(dev_cg_xr_k0(c->xf, c->rf, c->pf, c->Apf, c->N3, c->part, c->sc, c->st));
+  CK(dev_cg_xr_k0(c->xf, c->rf, c->pf, c->Apf, c->N3, c->pre_dev + 36, c->part, c->sc, c->st));
   CK(dev_cg_cond(c->sc, c->cg_handle, use_handle, c->st));
   return 0;
 }
@@ -781,7 +800,7 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
   TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
   CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
   CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
-  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->pre_dev + 36, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
   double rr;
   TRY(read_scalar(c, SC_RRNEW, &rr));
   double beta = 0.0;  // the first iteration's p = r + 0 p = r
@@ -812,7 +831,7 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
     TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
     CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
     CK(dev_scale_f(c->pf, (float)k, n, c->st));
-    CK(dev_dot_k0(c->rf, c->rf, c->N3, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+    CK(dev_dot_k0(c->rf, c->rf, c->N3, c->pre_dev + 36, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
     double rr_new;
     TRY(read_scalar(c, SC_RRNEW, &rr_new));
     // beta = |r_true|^2 / |r_prev|^2 with both in the new scaling (the iteration's beta
@@ -1644,6 +1663,86 @@ int cpfft_commit_step(void) {
   c->hn = 1 - c->hn;
   c->pass_step = 0;
   return sync(c);
+}
+
+// ---- many RVEs: one context per RVE, worker threads over a largest-first queue --------
+static void batch_one(cpfft_rve& r, int precision, int options, int precond, int schedule,
+                      double tolNR, double tolPCG, int maxIter) {
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
+  r.status = 0;
+  r.steps_done = 0;
+  r.voxel_updates = 0;
+  r.cg_iters = 0;
+  r.error[0] = 0;
+  auto fail = [&](int rc) {
+    r.status = rc;
+    snprintf(r.error, sizeof(r.error), "%s", cpfft_last_error());
+  };
+  int rc = cpfft_init(r.N, r.matList, r.kocks_deg, r.props, r.ncrystals, r.tstep, r.g_mapping);
+  if (rc < 0) { fail(rc); r.seconds = std::chrono::duration<double>(clk::now() - t0).count(); return; }
+  if ((rc = cpfft_set_mode(precision, options)) < 0 ||
+      (precision == CPFFT_PREC_MIXED && (rc = cpfft_set_precond(precond)) < 0) ||
+      (precision == CPFFT_PREC_MIXED && (rc = cpfft_set_schedule(schedule)) < 0) ||
+      (rc = cpfft_nr3_begin(tolPCG)) < 0) {
+    fail(rc);
+  } else {
+    const long long N3 = (long long)r.N * r.N * r.N;
+    for (int s = 1; s <= r.nsteps; s++) {
+      cpfft_stats st;
+      double pb[9];
+      rc = cpfft_nr3_step(s, r.BC_all + 9 * (s - 1), r.isNBC, tolNR, tolPCG, maxIter, pb, &st);
+      if (rc < 0) { fail(rc); break; }
+      if (rc > r.status) r.status = rc;
+      if (r.Pbar) memcpy(r.Pbar + 9 * (s - 1), pb, sizeof(pb));
+      r.steps_done = s;
+      r.voxel_updates += N3 * st.stress_updates;
+      r.cg_iters += st.cg_iters;
+    }
+    if (r.status >= 0 && (r.Fn1 || r.Pn1) && (rc = cpfft_sync_to_host(r.Fn1, r.Pn1, nullptr)) < 0)
+      fail(rc);
+  }
+  cpfft_finalize();
+  r.seconds = std::chrono::duration<double>(clk::now() - t0).count();
+}
+
+int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int precond,
+                      int schedule, double tolNR, double tolPCG, int maxIter, int nthreads) {
+  if (nrve < 0 || (nrve > 0 && !rves) || nthreads < 1) {
+    cpfft_set_error("cpfft_batch_solve: invalid argument");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  for (int k = 0; k < nrve; k++)
+    if (rves[k].nsteps < 0 || (rves[k].nsteps > 0 && (!rves[k].BC_all || !rves[k].isNBC))) {
+      cpfft_set_error("cpfft_batch_solve: RVE %d has no loading", k);
+      return CPFFT_ERR_BAD_ARG;
+    }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cpfft_set_error("cpfft_batch_solve: no CUDA device");
+    return CPFFT_ERR_CUDA;
+  }
+  std::vector<int> order(nrve);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rves[a].N > rves[b].N; });
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    for (;;) {
+      const int k = next.fetch_add(1);
+      if (k >= nrve) break;
+      batch_one(rves[order[k]], precision, options, precond, schedule, tolNR, tolPCG, maxIter);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 0; i < std::min(nthreads, nrve); i++) pool.emplace_back(worker);
+  for (auto& t : pool) t.join();
+  for (int k = 0; k < nrve; k++)
+    if (rves[k].status < 0) {
+      cpfft_set_error("RVE %d: %s", k, rves[k].error);
+      return rves[k].status;
+    }
+  return 0;
 }
 
 }  // extern "C"

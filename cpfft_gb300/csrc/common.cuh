@@ -18,9 +18,13 @@
 
 void cpfft_set_error(const char* fmt, ...);
 
-// Kernels launched by this library since load (the library is single-threaded by
-// contract, see the header); every launch wrapper adds its launches here.
-extern long long g_kernel_launches;
+// Raise a kernel's maximum dynamic shared memory to at least `bytes` (never lowers it;
+// thread-safe), for kernels whose launches need different sizes per grid.
+cudaError_t raise_max_dynamic_smem(const void* func, size_t bytes);
+
+// Kernels launched by the calling host thread through this library (each thread drives
+// its own context); every launch wrapper adds its launches here.
+extern thread_local long long g_kernel_launches;
 
 // ---- per-orientation material data (computed once at init, see api.cu) ------------
 // One record per distinct (crystal, orientation): the rotated stiffness and the slip

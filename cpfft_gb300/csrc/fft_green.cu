@@ -54,10 +54,12 @@ cudaError_t green_setup(int N) {
     }
   }
   size_t a = smem_a<T>(N), b = smem_b<T>(N, 16), c = smem_c<T>(N, tile_c<T>());
-  if ((e = cudaFuncSetAttribute(pass_a<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
-  if ((e = cudaFuncSetAttribute(pass_b<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b))) return e;
-  if ((e = cudaFuncSetAttribute(pass_c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c))) return e;
-  if ((e = cudaFuncSetAttribute(pass_e<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)a))) return e;
+  // the shared-memory passes serve every N: the attribute only ever grows, so contexts of
+  // different grids (concurrent ones included) never lower it under each other
+  if ((e = raise_max_dynamic_smem((const void*)pass_a<T, T>, a))) return e;
+  if ((e = raise_max_dynamic_smem((const void*)pass_b<T>, b))) return e;
+  if ((e = raise_max_dynamic_smem((const void*)pass_c<T>, c))) return e;
+  if ((e = raise_max_dynamic_smem((const void*)pass_e<T>, a))) return e;
   return cudaSuccess;
 }
 
@@ -118,9 +120,6 @@ cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2
   return e;
 }
 
-cudaError_t green_set_reference(const float* coef36, cudaStream_t st) {
-  return cudaMemcpyToSymbolAsync(c_acoef, coef36, 36 * sizeof(float), 0, cudaMemcpyHostToDevice, st);
-}
 
 template cudaError_t green_setup<double>(int);
 template cudaError_t green_setup<float>(int);

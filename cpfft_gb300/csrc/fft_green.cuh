@@ -21,7 +21,8 @@ struct GridDesc {
   int Nhalf, gmap;   // reference Nhalf (src/FFT_init.f:146-147) and the q mapping
   double inv_n3;     // backward scale 1/N^3
   int tkb, tkc;      // columns per block in passes B and C
-  int pre = 0;       // FP32 passes: 1 = reference-medium operator (green_set_reference)
+  int pre = 0;       // FP32 passes: 1 = reference-medium operator with coefficients acoef
+  const float* acoef = nullptr;  // (36, device) acoustic-tensor coefficients of the medium
   int wtb = 16, wtc = 0;  // warp passes: columns per block of passes B/D and of pass C (0: 4 for
                           // FP32, 2 for double-float)
   FftPlan plan;
@@ -50,13 +51,12 @@ cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Ve
 template <typename T>
 cudaError_t green_setup(int N);
 
-// Reference medium of the preconditioned FP32 operator (GridDesc::pre = 1): the 36
+// Reference medium of the preconditioned FP32 operator (GridDesc::pre = 1, acoef): the 36
 // coefficients of the acoustic tensor A0(q)_ik = sum_jl K0_ijkl q_j q_l, six unique
 // (i <= k) rows over the six products q_0q_0, q_1q_1, q_2q_2, q_0q_1, q_1q_2, q_0q_2.
 // With pre = 1 pass C applies Ghat0(q) X = (A0(q)^-1 X q) (x) q in place of
 // (X q) (x) q / |q|^2, and the fused product of green_apply_dot is <K : x, x>, summed in
 // pass A, in place of <x, y>.
-cudaError_t green_set_reference(const float* coef36, cudaStream_t st);
 
 // FP64-accurate y = G(K : x) (flgK = 1) or G(x) in double-float arithmetic on the FP32
 // pipes, for the power-of-two grids 32..256 of the warp-FFT passes (green_df_supported).

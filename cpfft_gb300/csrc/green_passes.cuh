@@ -155,8 +155,6 @@ __device__ __forceinline__ void ghat_acc(const T2* A, int q0, int q1, int q2, T 
   }
 }
 
-// Acoustic-tensor coefficients of the reference medium K0 (green_set_reference).
-__constant__ float c_acoef[36];
 
 // Reference-medium Green operator: (Ghat0(q):X)_ij = (A0(q)^-1 X q)_i q_j with
 // A0(q)_ik = sum_jl K0_ijkl q_j q_l (Moulinec-Suquet's Gamma0 for the stiffness K0),
@@ -164,7 +162,8 @@ __constant__ float c_acoef[36];
 // inverted through its cofactors; a direction where it is not positive definite
 // contributes nothing.
 template <typename T2, typename T>
-__device__ __forceinline__ void ghat0_acc(const T2* A, int q0, int q1, int q2, T w, T2* out) {
+__device__ __forceinline__ void ghat0_acc(const float* coef, const T2* A, int q0, int q1, int q2,
+                                          T w, T2* out) {
   if (q0 == 0 && q1 == 0 && q2 == 0) return;
   const T q[3] = {(T)q0, (T)q1, (T)q2};
   const T pr[6] = {q[0] * q[0], q[1] * q[1], q[2] * q[2], q[0] * q[1], q[1] * q[2], q[0] * q[2]};
@@ -173,7 +172,7 @@ __device__ __forceinline__ void ghat0_acc(const T2* A, int q0, int q1, int q2, T
   for (int r = 0; r < 6; r++) {
     T s = 0;
 #pragma unroll
-    for (int m = 0; m < 6; m++) s += (T)c_acoef[6 * r + m] * pr[m];
+    for (int m = 0; m < 6; m++) s += (T)coef[6 * r + m] * pr[m];
     a[r] = s;
   }
   // a = (a00, a11, a22, a01, a12, a02)
@@ -207,15 +206,21 @@ __device__ __forceinline__ void ghat0_acc(const T2* A, int q0, int q1, int q2, T
 
 // the spectral operator of pass C: the reference medium when selected (FP32 only)
 template <typename T2, typename T>
-__device__ __forceinline__ void green_acc(bool pre, const T2* A, int q0, int q1, int q2, T w,
-                                          T2* out) {
+__device__ __forceinline__ void green_acc(bool pre, const float* coef, const T2* A, int q0, int q1,
+                                          int q2, T w, T2* out) {
   if constexpr (sizeof(T) == 4) {
     if (pre) {
-      ghat0_acc<T2, T>(A, q0, q1, q2, w, out);
+      ghat0_acc<T2, T>(coef, A, q0, q1, q2, w, out);
       return;
     }
   }
   ghat_acc<T2, T>(A, q0, q1, q2, w, out);
+}
+
+// the reference medium's coefficients in shared memory (block-wide; pre only)
+__device__ __forceinline__ void load_acoef(const GridDesc& g, float* s_coef) {
+  if (g.pre)
+    for (int i = threadIdx.x; i < 36; i += blockDim.x) s_coef[i] = g.acoef[i];
 }
 
 // an entry of the tangent in the transform's arithmetic type: FP32 / FP64 as stored, or
@@ -360,6 +365,8 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
   T2* b0 = tw + N;
   T2* b1 = b0 + 9 * TK * Lp;
   load_tw(tw, twg, N);
+  __shared__ float s_coef[36];
+  load_acoef(g, s_coef);
   const int ka0 = blockIdx.x * TK;
   const int kb = blockIdx.y;
   const long long cstr = (long long)N * H;  // stride between c planes
@@ -397,10 +404,10 @@ __global__ void __launch_bounds__(256) pass_c(typename Vec2<T>::t* __restrict__ 
       int m0 = qmap((N - kc) % N, N, Nh, gm), m1 = qmap((N - kb) % N, N, Nh, gm),
           m2 = qmap((N - ka) % N, N, Nh, gm);
       if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
-        green_acc<T2, T>(g.pre, A, p0, p1, p2, scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, p0, p1, p2, scale, out);
       } else {
-        green_acc<T2, T>(g.pre, A, p0, p1, p2, (T)0.5 * scale, out);
-        green_acc<T2, T>(g.pre, A, m0, m1, m2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, p0, p1, p2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, m0, m1, m2, (T)0.5 * scale, out);
       }
     }
     // conjugate for the inverse transform
@@ -611,6 +618,8 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
   T2* tw = reinterpret_cast<T2*>(smem_raw);
   T2* col = tw + N;
   load_tw(tw, twg, N);
+  __shared__ float s_coef[36];
+  load_acoef(g, s_coef);
   const int ka0 = blockIdx.x * TK;
   const int kb = blockIdx.y;
   const long long cstr = (long long)N * H;
@@ -652,10 +661,10 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
       int m0 = qmap((N - kc) & (N - 1), N, Nh, gm), m1 = qmap((N - kb) & (N - 1), N, Nh, gm),
           m2 = qmap((N - ka) & (N - 1), N, Nh, gm);
       if (m0 == -p0 && m1 == -p1 && m2 == -p2) {
-        green_acc<T2, T>(g.pre, A, p0, p1, p2, scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, p0, p1, p2, scale, out);
       } else {
-        green_acc<T2, T>(g.pre, A, p0, p1, p2, (T)0.5 * scale, out);
-        green_acc<T2, T>(g.pre, A, m0, m1, m2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, p0, p1, p2, (T)0.5 * scale, out);
+        green_acc<T2, T>(g.pre, s_coef, A, m0, m1, m2, (T)0.5 * scale, out);
       }
     }
 #pragma unroll

@@ -196,16 +196,19 @@ __global__ void __launch_bounds__(RB) k_sum9(const double* __restrict__ x, long 
 
 // ---- K0-weighted forms of the reference-medium preconditioned FP32 CG ----------------
 // The CG of the preconditioned operator G0(K : .) runs in the inner product
-// <a, b>_K0 = sum_v a_v . (K0 b_v), K0 the (normalised, symmetrised) 9x9 reference stiffness.
-__constant__ float c_k0[81];
-
-__device__ __forceinline__ float k0_form(const float* a, const float* b) {
+// <a, b>_K0 = sum_v a_v . (K0 b_v), K0 the (normalised, symmetrised) 9x9 reference stiffness
+// of the calling context (device memory, staged in shared memory per block).
+__device__ __forceinline__ void load_k0(const float* __restrict__ k0, float* s_k0) {
+  for (int i = threadIdx.x; i < 81; i += blockDim.x) s_k0[i] = k0[i];
+  __syncthreads();
+}
+__device__ __forceinline__ float k0_form(const float* s_k0, const float* a, const float* b) {
   float s = 0.f;
 #pragma unroll
   for (int i = 0; i < 9; i++) {
     float t = 0.f;
 #pragma unroll
-    for (int j = 0; j < 9; j++) t += c_k0[9 * i + j] * b[j];
+    for (int j = 0; j < 9; j++) t += s_k0[9 * i + j] * b[j];
     s += a[i] * t;
   }
   return s;
@@ -216,8 +219,11 @@ __device__ __forceinline__ float k0_form(const float* a, const float* b) {
 __global__ void __launch_bounds__(RB) k_cg_xr_k0(float* __restrict__ x, float* __restrict__ r,
                                                  const float* __restrict__ p,
                                                  const float* __restrict__ Ap, long long N3,
+                                                 const float* __restrict__ k0,
                                                  const double* __restrict__ sc,
                                                  double* __restrict__ part) {
+  __shared__ float s_k0[81];
+  load_k0(k0, s_k0);
   const float alpha = (float)sc[SC_ALPHA];
   const long long stride = (long long)gridDim.x * RB, t0 = (long long)blockIdx.x * RB + threadIdx.x;
   float s = 0.f;
@@ -239,7 +245,7 @@ __global__ void __launch_bounds__(RB) k_cg_xr_k0(float* __restrict__ x, float* _
         rv[0][i] = qv.x; rv[1][i] = qv.y; rv[2][i] = qv.z; rv[3][i] = qv.w;
       }
 #pragma unroll
-      for (int u = 0; u < 4; u++) s += k0_form(rv[u], rv[u]);
+      for (int u = 0; u < 4; u++) s += k0_form(s_k0, rv[u], rv[u]);
     }
   } else {
     for (long long v = t0; v < N3; v += stride) {
@@ -251,7 +257,7 @@ __global__ void __launch_bounds__(RB) k_cg_xr_k0(float* __restrict__ x, float* _
         rv[i] = r[k] - alpha * Ap[k];
         r[k] = rv[i];
       }
-      s += k0_form(rv, rv);
+      s += k0_form(s_k0, rv, rv);
     }
   }
   double sb = block_sum((double)s);
@@ -260,13 +266,16 @@ __global__ void __launch_bounds__(RB) k_cg_xr_k0(float* __restrict__ x, float* _
 
 // partial <a, b>_K0
 __global__ void __launch_bounds__(RB) k_dot_k0(const float* __restrict__ a, const float* __restrict__ b,
-                                               long long N3, double* __restrict__ part) {
+                                               long long N3, const float* __restrict__ k0,
+                                               double* __restrict__ part) {
+  __shared__ float s_k0[81];
+  load_k0(k0, s_k0);
   float s = 0.f;
   for (long long v = (long long)blockIdx.x * RB + threadIdx.x; v < N3; v += (long long)gridDim.x * RB) {
     float av[9], bv[9];
 #pragma unroll
     for (int i = 0; i < 9; i++) { av[i] = a[i * N3 + v]; bv[i] = b[i * N3 + v]; }
-    s += k0_form(av, bv);
+    s += k0_form(s_k0, av, bv);
   }
   double sb = block_sum((double)s);
   if (threadIdx.x == 0) part[blockIdx.x] = sb;
@@ -407,18 +416,15 @@ cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, in
   return counted(10);
 }
 
-cudaError_t dev_set_k0(const float* k0, cudaStream_t st) {
-  return cudaMemcpyToSymbolAsync(c_k0, k0, 81 * sizeof(float), 0, cudaMemcpyHostToDevice, st);
-}
 cudaError_t dev_cg_xr_k0(float* x, float* r, const float* p, const float* Ap, long long N3,
-                         double* part, double* sc, cudaStream_t st) {
-  k_cg_xr_k0<<<NPART, RB, 0, st>>>(x, r, p, Ap, N3, sc, part);
+                         const float* k0, double* part, double* sc, cudaStream_t st) {
+  k_cg_xr_k0<<<NPART, RB, 0, st>>>(x, r, p, Ap, N3, k0, sc, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, SC_RRNEW, OP_BETA);
   return counted(2);
 }
-cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, double* part, double* sc,
-                       int slot, int op, cudaStream_t st) {
-  k_dot_k0<<<NPART, RB, 0, st>>>(a, b, N3, part);
+cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, const float* k0,
+                       double* part, double* sc, int slot, int op, cudaStream_t st) {
+  k_dot_k0<<<NPART, RB, 0, st>>>(a, b, N3, k0, part);
   k_final<<<1, 1024, 0, st>>>(part, NPART, sc, slot, op);
   return counted(2);
 }

@@ -42,13 +42,12 @@ cudaError_t dev_sum9(const double* x, long long N3, double* part, double* sc, in
                      cudaStream_t st);
 
 // Reference-medium preconditioned FP32 CG: the inner product <a, b>_K0 uses the 9x9
-// matrix set by dev_set_k0 (row-major, (ij) index 3i+j).
-cudaError_t dev_set_k0(const float* k0, cudaStream_t st);
+// matrix k0 (device memory, row-major, (ij) index 3i+j).
 // x += alpha p, r -= alpha Ap, sc[SC_RRNEW] = <r, r>_K0 and beta (fields (9, N3) FP32)
 cudaError_t dev_cg_xr_k0(float* x, float* r, const float* p, const float* Ap, long long N3,
-                         double* part, double* sc, cudaStream_t st);
-cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, double* part, double* sc,
-                       int slot, int op, cudaStream_t st);
+                         const float* k0, double* part, double* sc, cudaStream_t st);
+cudaError_t dev_dot_k0(const float* a, const float* b, long long N3, const float* k0,
+                       double* part, double* sc, int slot, int op, cudaStream_t st);
 // sc81[m] = sum over voxels of component m of an (81, N3) FP32 field (part: 81 x 64)
 cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81, cudaStream_t st);
 

@@ -13,9 +13,10 @@
  *     (src/G_K_dF.f:258-264, src/cep2A.f:133-154).
  * Everything is FP64 at the boundary.
  *
- * Threading: every call must come from one host thread; the library owns one CUDA
- * stream and one global context (the reference keeps its state in module arrays,
- * src/mod_fft.f).  Calls are not re-entrant.
+ * Threading: a context (one RVE, one CUDA stream; the reference keeps this state in module
+ * arrays, src/mod_fft.f) belongs to the host thread that called cpfft_init, and every
+ * call acts on the calling thread's context; cpfft_batch_solve runs several contexts at
+ * once from its own threads.  Calls on one context are not re-entrant.
  *
  * Return codes: 0 = success, > 0 = warning, < 0 = error (see CPFFT_* below).  The
  * reference aborts (`die_abort`, src/mpi_code.f:35-53) on every error; a Fortran caller
@@ -256,6 +257,44 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR,
  * `compute` command (src/FFT_finite_3d.f:145) and the first tangent_homo.
  */
 int cpfft_nr3_begin(double tolPCG);
+
+/*
+ * Many RVEs at once (extension; the reference solves one RVE per run).  Each RVE runs the
+ * whole `compute` sequence -- cpfft_init, the selected mode, cpfft_nr3_begin, nsteps x
+ * cpfft_nr3_step -- in its own library context and CUDA stream, driven by one of
+ * `nthreads` host threads that take RVEs from a shared queue, largest grid first; the
+ * RVEs' kernels therefore run concurrently on the GPU.  Per-RVE results are identical to
+ * solving the RVEs one after another.  The calling thread's own context is untouched.
+ */
+typedef struct cpfft_rve {
+    /* in */
+    int N;                        /* grid points per axis                                  */
+    const int* matList;           /* (N3) as cpfft_init                                    */
+    const double* kocks_deg;      /* (N3, 3)                                               */
+    const cpfft_crystal* props;
+    int ncrystals;
+    double tstep;
+    int g_mapping;
+    int nsteps;
+    const double* BC_all;         /* (9, nsteps): column s-1 = the BC of load step s       */
+    const int* isNBC;             /* (9)                                                   */
+    /* out */
+    double* Pbar;                 /* (9, nsteps) volume-averaged P after each step         */
+    double* Fn1;                  /* (N3, 9) final F, or NULL                              */
+    double* Pn1;                  /* (N3, 9) final P, or NULL                              */
+    int status;                   /* first error, else the largest warning, else 0         */
+    int steps_done;
+    long long voxel_updates;      /* N3 x stress-update passes                             */
+    long long cg_iters;
+    double seconds;               /* host wall time of this RVE                            */
+    char error[160];              /* cpfft_last_error() of the failing call                */
+} cpfft_rve;
+
+/* precision / options / precond / schedule as cpfft_set_mode, cpfft_set_precond and
+ * cpfft_set_schedule (precond and schedule apply to CPFFT_PREC_MIXED); tolerances as
+ * cpfft_nr3_step.  Returns 0, or the first RVE error in queue order. */
+int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int precond,
+                      int schedule, double tolNR, double tolPCG, int maxIter, int nthreads);
 
 /* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
  * compact history at n (N3, CPFFT_HIST_WORDS) used by the result writers. */
