@@ -768,6 +768,8 @@ int cg_segment(Ctx* c, double rr, double rn, double tolb, double tol, double del
 int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
   const long long n = 9 * c->N3;
   const int maxIter = 2000;
+  // reduction of <r,r>_K0 per segment before a reliable update; 1e-3 lets the FP32
+  // recursion drift until the solve stagnates (measured at 128^3)
   const double delta = 1.0e-2;
   *iters = 0;
   if (!use_x0) CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
