@@ -14,7 +14,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
-HIST_WORDS = 23
+HIST_WORDS = 29
 
 G_REF_SHIFT, G_CENTERED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -106,6 +106,9 @@ SIGNATURES = {
     "cpfft_set_precond": (_I, [_I]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
+    "cpfft_format_flat": (_I, [_I, ctypes.c_char_p, _LL, _P(_LL)]),
+    "cpfft_write_flat": (_I, [_I, _I, ctypes.c_char_p, ctypes.c_char_p]),
+    "cpfft_format_e15": (_I, [_DP, _LL, ctypes.c_char_p]),
     "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
@@ -356,6 +359,21 @@ class Solver:
         _check(load_library().cpfft_sync_to_host(_dp(F), _dp(P), _dp(H)), "sync_to_host")
         return (F, P, H) if history else (F, P)
 
+    # --- element result files (ouelestr) ---------------------------------------------
+    def format_flat(self, quantity):
+        """The data lines of wesNNNNN_text (quantity 2) / weeNNNNN_text (1) as bytes."""
+        L = load_library()
+        n = ctypes.c_longlong(0)
+        L.cpfft_format_flat(int(quantity), None, 0, ctypes.byref(n))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(L.cpfft_format_flat(int(quantity), buf, n.value, ctypes.byref(n)), "format_flat")
+        return buf.raw[:n.value]
+
+    def write_flat(self, quantity, step, structure_name="cpfft", directory=""):
+        _check(load_library().cpfft_write_flat(int(quantity), int(step),
+                                               structure_name.encode(), directory.encode()),
+               "write_flat")
+
     def commit(self):
         _check(load_library().cpfft_commit_step(), "commit_step")
 
@@ -402,3 +420,12 @@ def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE
                  cg_iters=r.cg_iters, seconds=r.seconds, error=r.error.decode())
     _check(rc, "cpfft_batch_solve")
     return out
+
+
+def format_e15(values):
+    """Fortran E15.6 of each value (the GPU formatter of the result files)."""
+    x = np.ascontiguousarray(values, dtype=np.float64).ravel()
+    buf = ctypes.create_string_buffer(15 * len(x) + 1)
+    _check(load_library().cpfft_format_e15(_dp(x), len(x), buf), "format_e15")
+    raw = buf.raw[:15 * len(x)].decode()
+    return [raw[15 * i:15 * i + 15] for i in range(len(x))]

@@ -7,9 +7,11 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <ctime>
 #include <map>
 #include <mutex>
 #include <numeric>
+#include <string>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -17,6 +19,13 @@
 #include "common.cuh"
 #include "fft_green.cuh"
 #include "mlp.cuh"
+
+// element result text (results.cu)
+void host_e15(double v, char* out);
+cudaError_t launch_format_flat(const double* hist, long long N3, int word0, int nvals, char* text,
+                               unsigned char* flags, cudaStream_t st);
+cudaError_t launch_format_values(const double* x, long long n, char* out, unsigned char* flags,
+                                 cudaStream_t st);
 
 // the learned initial guess's device weights and error check (mlp.cu)
 bool mlp_device_weights(mlp::Weights* w, int** err);
@@ -1744,6 +1753,127 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
       cpfft_set_error("RVE %d: %s", k, rves[k].error);
       return rves[k].status;
     }
+  return 0;
+}
+
+// ---- element result files (ouelestr / oupestr / ouddpa_flat_header) -----------------
+int cpfft_format_e15(const double* x, long long n, char* out) {
+  if (n < 0 || (n > 0 && (!x || !out))) {
+    cpfft_set_error("cpfft_format_e15: invalid argument");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (n == 0) return 0;
+  double* dx = nullptr;
+  char* dout = nullptr;
+  unsigned char* dfl = nullptr;
+  int rc = 0;
+  if ((rc = dalloc(dx, n * sizeof(double))) || (rc = dalloc(dout, n * 15)) ||
+      (rc = dalloc(dfl, n))) {
+    cudaFree(dx); cudaFree(dout); cudaFree(dfl);
+    return rc;
+  }
+  std::vector<unsigned char> fl(n);
+  cudaError_t e;
+  if ((e = cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice)) ||
+      (e = launch_format_values(dx, n, dout, dfl, 0)) ||
+      (e = cudaMemcpy(out, dout, n * 15, cudaMemcpyDeviceToHost)) ||
+      (e = cudaMemcpy(fl.data(), dfl, n, cudaMemcpyDeviceToHost)))
+    rc = cuda_check(e, "cpfft_format_e15");
+  cudaFree(dx); cudaFree(dout); cudaFree(dfl);
+  if (rc) return rc;
+  for (long long i = 0; i < n; i++)
+    if (fl[i]) host_e15(x[i], out + 15 * i);
+  return 0;
+}
+
+int cpfft_format_flat(int quantity, char* text, long long capacity, long long* length) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (quantity != 1 && quantity != 2) {
+    cpfft_set_error("cpfft_format_flat: quantity must be 1 (strains) or 2 (stresses)");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const int nvals = quantity == 2 ? 26 : 22;  // num_short_stress / num_short_strain + 15
+  const int word0 = quantity == 2 ? H_SIG : H_EPS;
+  const long long L = nvals * 15LL + 1, total = c->N3 * L;
+  if (length) *length = total;
+  if (!text || capacity < total) {
+    cpfft_set_error("cpfft_format_flat: buffer of %lld bytes needed", total);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  char* dt = nullptr;
+  unsigned char* dfl = nullptr;
+  int rc = 0;
+  if ((rc = dalloc(dt, total)) || (rc = dalloc(dfl, 6 * c->N3))) {
+    cudaFree(dt);
+    cudaFree(dfl);
+    return rc;
+  }
+  std::vector<unsigned char> fl(6 * c->N3);
+  cudaError_t e;
+  if ((e = launch_format_flat(c->hist[c->hn], c->N3, word0, nvals, dt, dfl, c->st)) ||
+      (e = cudaMemcpyAsync(text, dt, total, cudaMemcpyDeviceToHost, c->st)) ||
+      (e = cudaMemcpyAsync(fl.data(), dfl, 6 * c->N3, cudaMemcpyDeviceToHost, c->st)) ||
+      (e = cudaStreamSynchronize(c->st)))
+    rc = cuda_check(e, "cpfft_format_flat");
+  cudaFree(dt);
+  cudaFree(dfl);
+  if (rc) return rc;
+  // the fields the device could not round exactly: formatted here from the same values
+  std::vector<double> hv;
+  for (long long v = 0; v < c->N3; v++)
+    for (int j = 0; j < 6; j++)
+      if (fl[6 * v + j]) {
+        if (hv.empty()) {
+          hv.resize(6 * c->N3);
+          std::vector<double> w(c->N3);
+          for (int jj = 0; jj < 6; jj++) {
+            CK(cudaMemcpy(w.data(), c->hist[c->hn] + (word0 + jj) * c->N3, c->N3 * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+            for (long long u = 0; u < c->N3; u++) hv[6 * u + jj] = w[u];
+          }
+        }
+        double x = hv[6 * v + j];
+        if (std::fabs(x) < 1.0e-30) x = 0.0;
+        host_e15(x, text + v * L + 15 * j);
+      }
+  return 0;
+}
+
+int cpfft_write_flat(int quantity, int step, const char* structure_name, const char* directory) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  long long total = 0;
+  cpfft_format_flat(quantity, nullptr, 0, &total);
+  if (quantity != 1 && quantity != 2) return CPFFT_ERR_BAD_ARG;
+  std::vector<char> text(total);
+  TRY(cpfft_format_flat(quantity, text.data(), total, &total));
+  // wes / wee + step (i5.5) + _text (ouocst_elem, src/ouresult.f:700-712)
+  int stepno = step > 99999 ? step - 99999 : step;
+  char name[64];
+  snprintf(name, sizeof(name), "%s%05d_text", quantity == 2 ? "wes" : "wee", stepno);
+  std::string path = directory && directory[0] ? std::string(directory) + "/" + name : name;
+  FILE* f = fopen(path.c_str(), "w");
+  if (!f) {
+    cpfft_set_error("cpfft_write_flat: cannot open %s", path.c_str());
+    return CPFFT_ERR_BAD_ARG;
+  }
+  // header (ouddpa_flat_header, src/ouresult.f:335-396)
+  char sname[9];
+  snprintf(sname, sizeof(sname), "%-8.8s", structure_name ? structure_name : "");
+  time_t now = time(nullptr);
+  char date[32];
+  strftime(date, sizeof(date), "%a %b %e %H:%M:%S %Y", localtime(&now));  // fdate's layout
+  const long long nonode = (long long)(c->N + 1) * (c->N + 1) * (c->N + 1);
+  fprintf(f, "#\n#  WARP3D element results: %-15s\n#  Structure name: %s\n"
+             "#  Model nodes, elements: %8lld%8lld\n#  %-24s\n#  Load(time) step: %8d\n#\n",
+          quantity == 2 ? "stresses" : "strains", sname, nonode, c->N3, date, step);
+  const size_t w = fwrite(text.data(), 1, text.size(), f);
+  fclose(f);
+  if (w != text.size()) {
+    cpfft_set_error("cpfft_write_flat: short write to %s", path.c_str());
+    return CPFFT_ERR_BAD_ARG;
+  }
   return 0;
 }
 

@@ -53,7 +53,8 @@ enum {
   H_RP = 7,       // 9  plastic rotation Rp, column-major
   H_D = 16,       // 6  unrotated strain increment of the step
   H_TTR = 22,     // 1  tau_tilde rate
-  H_WORDS = 23
+  H_EPS = 23,     // 6  unrotated strain (sum of the step increments, rstgp1_update_strains)
+  H_WORDS = 29
 };
 
 // Stress kernel launch arguments

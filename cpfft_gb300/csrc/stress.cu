@@ -1144,6 +1144,10 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int j = 0; j < 3; j++) a.hist_np1[(H_RP + 3 * j + i) * N3 + v] = Rp[3 * i + j];
   for (int i = 0; i < 6; i++) a.hist_np1[(H_D + i) * N3 + v] = uddt[i];
   a.hist_np1[H_TTR * N3 + v] = ttrate;
+  // strains at n+1 = strains at n + the unrotated increment (rstgp1_update_strains,
+  // src/drive_eps_sig.f:264-265, src/rstgp1.f:1378-1394); zero at n for step 1
+  for (int i = 0; i < 6; i++)
+    a.hist_np1[(H_EPS + i) * N3 + v] = (a.step == 1 ? 0.0 : a.hist_n[(H_EPS + i) * N3 + v]) + uddt[i];
   // ---- Cauchy stress and P = J T F^-T (cs2p, src/drive_eps_sig.f:1182-1224)
   double tm[9] = {stress[0], stress[3], stress[5], stress[3], stress[1], stress[4],
                   stress[5], stress[4], stress[2]};

@@ -298,8 +298,24 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
 
 /* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
  * compact history at n (N3, CPFFT_HIST_WORDS) used by the result writers. */
-#define CPFFT_HIST_WORDS 23   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) */
+#define CPFFT_HIST_WORDS 29   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6) */
 int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history);
+
+/* ---- element result files (ouelestr, src/ouresult.f:140-300) --------------------------
+ * The per-voxel lines of the flat text files wesNNNNN_text (quantity 2: the unrotated
+ * Cauchy stress, 26 values a line) and weeNNNNN_text (quantity 1: the unrotated strain,
+ * 22 values a line), from the history after the last roll-over (where ouresult is
+ * called, src/FFT_nr3.f:173-183).  Every value is written as the Fortran E15.6 of
+ * oupestr's `(30e15.6)`, rounded to nearest (ties to even), values below 1e-30 as zero,
+ * the columns past the six components zero as in the reference; formatted on the GPU.
+ * cpfft_format_flat fills `text` (capacity >= *length = N3 x (values x 15 + 1) bytes; with
+ * text NULL it only reports the size).  cpfft_write_flat writes the whole file, header
+ * included (ouddpa_flat_header: structure name, node and element counts, date, step),
+ * named as ouocst_elem names it, into `directory` (NULL or "" = the working directory). */
+int cpfft_format_flat(int quantity, char* text, long long capacity, long long* length);
+int cpfft_write_flat(int quantity, int step, const char* structure_name, const char* directory);
+/* E15.6 of n values (15 characters each, no separators) into out: the formatter above. */
+int cpfft_format_e15(const double* x, long long n, char* out);
 
 /* State roll-over Fn <- Fn1, Pn <- Pn1, history n <- n+1: replaces update
  * (src/update.f:16-193) and FFT_nr3.f:173-179 in mirror mode. */

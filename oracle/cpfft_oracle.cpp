@@ -336,6 +336,7 @@ struct State {          // compact history (CPFFT_HIST_WORDS order)
   M3 Rp;
   double D[6];
   double tt_rate;
+  double eps[6];        // unrotated strain (rstgp1_update_strains, src/rstgp1.f:1378-1394)
 };
 void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f:473-571)
   std::memset(&s, 0, sizeof(s));
@@ -349,6 +350,7 @@ void state_pack(const State& s, double* h) {
     for (int i = 0; i < 3; i++) h[7 + 3 * j + i] = s.Rp[i][j];  // column-major
   for (int i = 0; i < 6; i++) h[16 + i] = s.D[i];
   h[22] = s.tt_rate;
+  for (int i = 0; i < 6; i++) h[23 + i] = s.eps[i];
 }
 void state_unpack(const double* h, State& s) {
   for (int i = 0; i < 6; i++) s.sig[i] = h[i];
@@ -357,6 +359,7 @@ void state_unpack(const double* h, State& s) {
     for (int i = 0; i < 3; i++) s.Rp[i][j] = h[7 + 3 * j + i];
   for (int i = 0; i < 6; i++) s.D[i] = h[16 + i];
   s.tt_rate = h[22];
+  for (int i = 0; i < 6; i++) s.eps[i] = h[23 + i];
 }
 
 // the np1 / curr "crystal_state" pieces the Voce routines read
@@ -941,6 +944,8 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
   int it = 0;
   o.ok = mm.update(uddt, dt, rn1, iter == 0, np1, o.cep, &it);
   o.iters = it;
+  // strains at n+1 = strains at n + uddt (src/drive_eps_sig.f:264-265)
+  for (int i = 0; i < 6; i++) np1.eps[i] = n.eps[i] + uddt[i];
   for (int i = 0; i < 6; i++) o.sig[i] = np1.sig[i];
   // Cauchy stress T = R t R^T (getrm1 opt 2 + qmply1), P = J T F^-T (cs2p :1182-1224)
   M6 qt;

@@ -12,7 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_oracle.so")
-HIST_WORDS = 23
+HIST_WORDS = 29
 
 _lib = None
 

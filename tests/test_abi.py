@@ -91,3 +91,13 @@ def test_stats_mirrors_match_the_header():
               for m in re.finditer(r"(long long|int|double)\s+(\w+);", body)]
     for mirror in (cpfft_gb300.Stats, pyoracle.Stats):
         assert [(n, t) for n, t in mirror._fields_] == fields
+
+
+def test_ctypes_signatures_match_the_header_arity(gpulib):
+    """Every ctypes signature takes as many arguments as the header's prototype."""
+    src = open(os.path.join(ROOT, "include", "cpfft_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    for m in re.finditer(r"\b(cpfft_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", src):
+        name, params = m.group(1), m.group(2).strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(gpulib.SIGNATURES[name][1]) == n, (name, n, gpulib.SIGNATURES[name][1])
