@@ -71,6 +71,63 @@ void fcc_geometry(double b[12][3], double n[12][3]) {
   memcpy(n, Nn, sizeof(Nn));
 }
 
+// BCC {110}, {112}, {123} <111>, 48 systems in the reference's order and signs
+// (slip_type 8, src/mod_crystals.f:812-1207): directions (+-1,+-1,+-1)/sqrt(3) and plane
+// normals as integer Miller triples, each normalised by its length as the reference's
+// constants are (1/sqrt(2), 1/sqrt(6), 2/sqrt(6), 1/sqrt(14), 2/sqrt(14), 3/sqrt(14)).
+void bcc48_geometry(double b[48][3], double n[48][3]) {
+  static const int B[48][3] = {
+      {-1, 1, 1}, {1, -1, 1}, {1, 1, 1}, {1, 1, -1},
+      {1, 1, -1}, {-1, 1, 1}, {1, 1, 1}, {1, -1, 1},
+      {1, 1, -1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1}};
+  static const int Nn[48][3] = {
+      {1, 1, 0}, {1, 1, 0}, {1, -1, 0}, {1, -1, 0},
+      {1, 0, 1}, {1, 0, 1}, {1, 0, -1}, {1, 0, -1},
+      {0, 1, 1}, {0, 1, 1}, {0, 1, -1}, {0, 1, -1},
+      {1, 1, 2}, {-1, 1, 2}, {1, -1, 2}, {1, 1, -2},
+      {1, 2, 1}, {-1, 2, 1}, {1, -2, 1}, {1, 2, -1},
+      {2, 1, 1}, {-2, 1, 1}, {2, -1, 1}, {2, 1, -1},
+      {1, 2, 3}, {-1, 2, 3}, {1, -2, 3}, {1, 2, -3},
+      {1, 3, 2}, {-1, 3, 2}, {1, -3, 2}, {1, 3, -2},
+      {2, 1, 3}, {-2, 1, 3}, {2, -1, 3}, {2, 1, -3},
+      {2, 3, 1}, {-2, 3, 1}, {2, -3, 1}, {2, 3, -1},
+      {3, 1, 2}, {-3, 1, 2}, {3, -1, 2}, {3, 1, -2},
+      {3, 2, 1}, {-3, 2, 1}, {3, -2, 1}, {3, 2, -1}};
+  const double f3 = 1.0 / std::sqrt(3.0);
+  for (int s = 0; s < 48; s++) {
+    const double len = std::sqrt((double)(Nn[s][0] * Nn[s][0] + Nn[s][1] * Nn[s][1] + Nn[s][2] * Nn[s][2]));
+    for (int i = 0; i < 3; i++) {
+      b[s][i] = B[s][i] * f3;
+      n[s][i] = (double)Nn[s][i] / len;
+    }
+  }
+}
+
+// slip systems of a slip_type: 12 (fcc) or 48 (bcc48), 0 when not supported
+int slip_geometry(int slip_type, double b[48][3], double n[48][3]) {
+  if (slip_type == 1) {
+    double bf[12][3], nf[12][3];
+    fcc_geometry(bf, nf);
+    memcpy(b, bf, sizeof(bf));
+    memcpy(n, nf, sizeof(nf));
+    return 12;
+  }
+  if (slip_type == 8) {
+    bcc48_geometry(b, n);
+    return 48;
+  }
+  return 0;
+}
+
 bool invert6(const double a[36], double out[36]) {
   double m[6][12];
   for (int i = 0; i < 6; i++)
@@ -127,13 +184,13 @@ void kocks_rotation(const double ang[3], double r[9]) {  // src/mm10_a.f:1287-13
   r[8] = cos(th);
 }
 
-void orientation_record(const double C0[36], const double bb[12][3], const double nn[12][3],
-                        const double ang[3], OriRec& o) {
+void orientation_record(const double C0[36], const double bb[48][3], const double nn[48][3],
+                        int nslip, const double ang[3], OriRec& o) {
   double g[9], tr[9];
   kocks_rotation(ang, g);
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) tr[3 * i + j] = g[3 * j + i];
-  for (int s = 0; s < 12; s++) {
+  for (int s = 0; s < nslip; s++) {
     double bs[3], ns[3];
     for (int i = 0; i < 3; i++) {
       bs[i] = tr[3 * i] * bb[s][0] + tr[3 * i + 1] * bb[s][1] + tr[3 * i + 2] * bb[s][2];
@@ -201,6 +258,7 @@ struct Ctx {
   long long N3 = 0;
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
+  int nslip = 12;  // slip systems of the grid's crystals (12 fcc, 48 bcc48)
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
   // voxel work queue of the implicit stress passes (cpfft_set_schedule)
   int sched = CPFFT_SCHED_BLOCKS;
@@ -934,7 +992,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   }
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
-  CK(launch_stress(a, warm, c->st));
+  CK(c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
   TRY(kt_stop(c));
   c->pass_step = step;
   c->pass_iter = iter;
@@ -1121,17 +1179,25 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   const long long N3 = (long long)N * N * N;
   std::vector<CrysRec> cr(ncrystals);
   std::vector<std::vector<double>> C0(ncrystals, std::vector<double>(36));
-  double bb[12][3], nn[12][3];
-  fcc_geometry(bb, nn);
+  double bb[48][3], nn[48][3];
+  int nslip = 0;
   for (int k = 0; k < ncrystals; k++) {
     const cpfft_crystal& p = props[k];
-    if (p.slip_type != 1 || p.h_type != 1 || !(p.tau_v != 0) || !(p.harden_n > 0) ||
+    const int ns = slip_geometry(p.slip_type, bb, nn);
+    if (!ns || p.h_type != 1 || !(p.tau_v != 0) || !(p.harden_n > 0) ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
-      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc + voce only, valid elasticity)", k + 1);
+      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip, voce hardening, "
+                      "valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
+    if (nslip && ns != nslip) {
+      cpfft_set_error("cpfft_init: the crystals of one grid must share the slip type");
+      return CPFFT_ERR_BAD_ARG;
+    }
+    nslip = ns;
     cr[k] = crystal_record(p);
   }
+  slip_geometry(props[0].slip_type, bb, nn);
   // distinct (crystal, orientation) records
   std::vector<int> ori(N3), crys(N3);
   std::map<std::tuple<int, double, double, double>, int> seen;
@@ -1149,7 +1215,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     if (it == seen.end()) {
       id = (int)oris.size();
       oris.emplace_back();
-      orientation_record(C0[m].data(), bb, nn, ang, oris.back());
+      orientation_record(C0[m].data(), bb, nn, nslip, ang, oris.back());
       seen.emplace(key, id);
     } else {
       id = it->second;
@@ -1158,6 +1224,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     crys[v] = m;
   }
   Ctx* c = new Ctx;
+  c->nslip = nslip;
   c->N = N;
   c->N3 = N3;
   c->dt = tstep;

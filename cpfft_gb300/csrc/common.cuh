@@ -32,8 +32,8 @@ extern thread_local long long g_kernel_launches;
 // recomputes on every call for every voxel.
 struct OriRec {
   double C[36];    // stiffness in the sample frame, row-major 6x6
-  double ms[72];   // 12 x 6 sym(b (x) n) Voigt, engineering shear
-  double qs[36];   // 12 x 3 skew(b (x) n) as (w23, w13, w12)
+  double ms[48 * 6];  // nslip x 6 sym(b (x) n) Voigt, engineering shear
+  double qs[48 * 3];  // nslip x 3 skew(b (x) n) as (w23, w13, w12)
   double g[9];     // lattice -> sample rotation applied to b and n, row-major
 };
 
@@ -103,8 +103,10 @@ struct StressArgs {
   int log_stride, log_phase;  // voxels v with v % stride == phase are logged
 };
 
-// warm = true: the learned initial guess starts the local Newton solve
+// warm = true: the learned initial guess starts the local Newton solve.  launch_stress
+// serves crystals with 12 slip systems (FCC), launch_stress48 those with 48 (BCC48).
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
+cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
 // Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost
 // bin, queue head zeroed.  scratch: 128 unsigned ints.
 cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,

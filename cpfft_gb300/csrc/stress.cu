@@ -12,9 +12,18 @@
 #include <algorithm>
 
 #include "common.cuh"
+
+// Slip systems of the crystals this translation unit serves: 12 (FCC {111}<110>) here;
+// stress48.cu compiles this file again with CPFFT_NSLIP 48 (BCC {110},{112},{123}<111>).
+#ifndef CPFFT_NSLIP
+#define CPFFT_NSLIP 12
+#define CPFFT_STRESS_LAUNCH launch_stress
+#endif
 #include "mlp.cuh"
 
 namespace {
+
+constexpr int NS = CPFFT_NSLIP;  // slip systems
 
 __device__ __forceinline__ double sgn1(double x) { return x < 0.0 ? -1.0 : 1.0; }
 
@@ -214,9 +223,9 @@ struct Crystal {
   // np1 / curr pieces
   double D[6];
   double tinc, dg;
-  double ms[12][6];
-  double qc[12][3];
-  double Cms[12][6];  // C ms_i, constant while ms is (the reference forms it per call)
+  double ms[NS][6];
+  double qc[NS][3];
+  double Cms[NS][6];  // C ms_i, constant while ms is (the reference forms it per call)
 };
 
 __device__ __forceinline__ double Cv(const double* C, int a, int b) { return __ldg(C + 6 * a + b); }
@@ -240,7 +249,7 @@ __device__ void setup_np1(Crystal& s, const OriRec* rec, const double* D, double
   rt2rve(tr, RE);
   mm3(R, tr, work);
   rt2rvw(work, RWC);
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     double m0[6], q0[3];
     for (int a = 0; a < 6; a++) m0[a] = __ldg(rec->ms + 6 * i + a);
     for (int a = 0; a < 3; a++) q0[a] = __ldg(rec->qs + 3 * i + a);
@@ -267,7 +276,7 @@ __device__ __forceinline__ void slips(const Crystal& s, const double* st, double
   const CrysRec& c = *s.cr;
   double itt = 1.0 / tt;
   double dgn = s.dg * (c.n_int >= 0 ? ipow(itt, c.n_int + 1) : pow(itt, c.rate_n));
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     double r = st[0] * s.ms[i][0] + st[1] * s.ms[i][1] + st[2] * s.ms[i][2] +
                st[3] * s.ms[i][3] + st[4] * s.ms[i][4] + st[5] * s.ms[i][5];
     rs[i] = r;
@@ -293,7 +302,7 @@ __device__ void formR1(const Crystal& s, const double* st, const double* rs, con
   const CrysRec& c = *s.cr;
   double dbar[6] = {0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0};
   double tid = s.tinc * c.iD_v;
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     double f = rs[i] * tid + si[i];
     for (int a = 0; a < 6; a++) dbar[a] += f * s.ms[i][a];
     for (int a = 0; a < 3; a++) w[a] += f * s.qc[i][a];
@@ -317,7 +326,7 @@ __device__ double formR(const Crystal& s, const double* x, double* R, double* rs
   double ht = hterm(c, x[6]);
   double hp = hpow(c, ht) * sgn1(ht);
   double h = 0.0;
-  for (int i = 0; i < 12; i++) h += hp * fabs(si[i]);
+  for (int i = 0; i < NS; i++) h += hp * fabs(si[i]);
   h = s.ntt + c.theta_0 * h;
   R[6] = x[6] - h;
   return (h - s.ntt) / s.tinc;
@@ -335,7 +344,7 @@ __device__ void formJ11(const Crystal& s, const double* st, double tt, const dou
   double fac = s.dg * c.rate_n / (c.n_int >= 0 ? ipow(tt, c.n_int + 1) : pow(tt, c.rate_n));
   double tid = s.tinc * c.iD_v;
   double w[3] = {0, 0, 0};
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     double dgdt = fac * pw[i] + tid;
     double sq[6], wv[6];
     symsw(st, s.qc[i], sq);
@@ -373,7 +382,7 @@ __device__ void formJ(const Crystal& s, const double* x, const double* rs, const
   double hp = hpow(c, ht);
   double sh = sgn1(ht);
   double etau = 0.0;
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     // mm10_estress_voche: |rs|^(n-2) rs = |rs|^(n-1) sign(rs)
     double r2 = c.n_int >= 0 ? (rs[i] < 0.0 ? -pw[i] : (rs[i] > 0.0 ? pw[i] : 0.0))
                              : pow(fabs(rs[i]), c.rate_n - 2.0) * rs[i];
@@ -427,7 +436,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
                       bool& haveJ, int& iters, int& piters, double& ttrate) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
-  double x[7], rs[12], si[12], pw[12];
+  double x[7], rs[NS], si[NS], pw[NS];
   for (int i = 0; i < 6; i++) x[i] = stress[i];
   x[6] = tt;
   double inR1;
@@ -490,7 +499,7 @@ __device__ bool solve(Crystal& cu, double dtinc, double* stress, double& tt, dou
 __device__ void pull_inside(const Crystal& cu, const double* nsig, double* x, double frac) {
   double smax = 1.0;
   const double lim = frac * x[6];
-  for (int i = 0; i < 12; i++) {
+  for (int i = 0; i < NS; i++) {
     double r0 = 0.0, dr = 0.0;
     for (int k = 0; k < 6; k++) {
       r0 += nsig[k] * cu.ms[i][k];
@@ -510,7 +519,7 @@ __device__ void pull_inside(const Crystal& cu, const double* nsig, double* x, do
 __device__ bool solve_from(Crystal& cu, double dtinc, const double* x0, double* stress,
                            double& tt, double* Jlast, bool& haveJ, int& iters, double& ttrate,
                            int cap) {
-  double x[7], R[7], rs[12], si[12], pw[12];
+  double x[7], R[7], rs[NS], si[NS], pw[NS];
   for (int i = 0; i < 6; i++) x[i] = stress[i];
   x[6] = tau_extrapolated(cu, tt, dtinc);
   formR(cu, x, R, rs, si, pw);
@@ -534,7 +543,7 @@ __device__ bool newton_update(Crystal& cu, double* x, double inR_alt, double* Jl
                               int& iters, double& ttrate, bool fixed_scale, int cap) {
   const CrysRec& c = *cu.cr;
   const double cls = 1.0e-4;
-  double rs[12], si[12], pw[12];
+  double rs[NS], si[NS], pw[NS];
   int it = 0;
   double R[7];
   ttrate = formR(cu, x, R, rs, si, pw);
@@ -806,6 +815,7 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
   }
 }
 
+#if CPFFT_NSLIP == 12
 // ---- the voxel work queue: voxels sorted by the cost of their previous pass -----------
 constexpr int QBINS = 64;  // costs 0 .. 62 and >= 63 (iterations of the local solve)
 
@@ -864,6 +874,8 @@ __global__ void __launch_bounds__(256) k_cost_scatter(const unsigned char* __res
     perm[start[b] + atomicAdd(&cnt[b], 1u)] = (int)v;
   }
 }
+
+#endif
 
 template <bool WARM>
 __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& iters,
@@ -979,7 +991,7 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   if (iter0 || no_load) {
     for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
     if (!no_load) {
-      double rs[12], si[12], pw[12], R1[6];
+      double rs[NS], si[NS], pw[NS], R1[6];
       slips(s, stress, tt, rs, si, pw);
       formR1(s, stress, rs, si, R1);
       for (int i = 0; i < 6; i++) stress[i] -= R1[i];
@@ -1112,10 +1124,10 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) tr[3 * i + j] = nRp[3 * j + i];
     rt2rvw(tr, RW);
-    double rs[12], si[12], pw[12], wb[3] = {0, 0, 0};
+    double rs[NS], si[NS], pw[NS], wb[3] = {0, 0, 0};
     slips(s, stress, tt, rs, si, pw);
     double tid = s.tinc * cr->iD_v;
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < NS; i++) {
       double q0[3], qs[3];
       for (int k = 0; k < 3; k++) q0[k] = __ldg(rec->qs + 3 * i + k);
       for (int k = 0; k < 3; k++) qs[k] = RW[3 * k] * q0[0] + RW[3 * k + 1] * q0[1] + RW[3 * k + 2] * q0[2];
@@ -1189,7 +1201,7 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
 
 }  // namespace
 
-cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s) {
+cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;
   static bool attr = false;
   if (warm && !attr) {
@@ -1222,6 +1234,7 @@ cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+#if CPFFT_NSLIP == 12
 cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,
                                int* perm, unsigned int* queue, cudaStream_t s) {
   unsigned int* hist = scratch;
@@ -1237,3 +1250,4 @@ cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned
   g_kernel_launches += 3;
   return cudaGetLastError();
 }
+#endif

@@ -22,6 +22,18 @@ FCC_VOCE = dict(
     exact_j22=1,
 )
 
+# The reference's example deck's crystal (examples/test_mm10.in): BCC with 48 slip
+# systems, isotropic elasticity, Voce hardening (the deck's `harden_n 5,48` read as 5.48),
+# the reference's own d(R2)/d(tau) (exact_j22 = 0).
+BCC48_DECK = dict(
+    slip_type=8, elastic_type=1, e=200000.0, nu=0.3, mu=0.0,
+    C11=0.0, C12=0.0, C13=0.0, C33=0.0, C44=0.0, C55=0.0,
+    h_type=1, harden_n=5.48, tau_y=205.0, tau_v=5000.0, theta_0=0.01, voce_m=1.0,
+    gamma_bar=4.0e-5, iD_v=0.0, alter_mode=1,
+    atol=1.0e-10, atol1=1.0e-10, rtol=1.0e-10, rtol1=1.0e-10, miter=30,
+    exact_j22=0,
+)
+
 # component order of 9-vectors: 11,12,13,21,22,23,31,32,33
 COMP = ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]
 
@@ -172,3 +184,12 @@ def uniaxial_strain(direction, total_strain, nstep):
     isNBC = np.zeros(9, dtype=np.int32)
     incr = (total_strain / nstep) * np.outer(n, n).ravel()
     return Loading(_accumulate(incr, isNBC, nstep), isNBC, "uniaxial_strain")
+
+
+def prescribed_stretch(diag_total, nstep):
+    """Every F component prescribed: F = I + diag(diag_total) s / nstep at step s (the
+    example deck's `strains F_xx .. F_yy .. F_zz ..` loading with zero shears)."""
+    isNBC = np.zeros(9, dtype=np.int32)
+    incr = np.zeros(9)
+    incr[[0, 4, 8]] = np.asarray(diag_total, dtype=np.float64) / nstep
+    return Loading(_accumulate(incr, isNBC, nstep), isNBC, "prescribed_stretch")

@@ -57,7 +57,9 @@ extern "C" {
  * keyword parser src/incrystal.f).  Units are the deck's (MPa, s).
  */
 typedef struct cpfft_crystal {
-    int    slip_type;      /* 1 = fcc {111}<110>, 12 systems (only value accepted)        */
+    int    slip_type;      /* 1 = fcc {111}<110>, 12 systems; 8 = bcc48 {110},{112},{123}
+                              <111>, 48 systems (src/mod_crystals.f:438-515, 812-1207); the
+                              crystals of one grid share the slip type                       */
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;

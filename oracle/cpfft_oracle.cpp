@@ -248,7 +248,8 @@ void polar_R(const M3 f, M3 r) {
 struct Crys {
   cpfft_crystal p;
   M6 C0;                 // stiffness in the crystal frame
-  double b[12][3], n[12][3];
+  int ns;                // slip systems
+  double b[48][3], n[48][3];
 };
 void fcc_systems(double b[12][3], double n[12][3]) {
   // FCC {111}<110>: slip directions and plane normals, in the reference's order.
@@ -262,9 +263,56 @@ void fcc_systems(double b[12][3], double n[12][3]) {
   for (int s = 0; s < 12; s++)
     for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
 }
+// BCC {110}, {112}, {123} <111> (slip_type 8, src/mod_crystals.f:812-1207), in the
+// reference's order and signs: directions (+-1,+-1,+-1)/sqrt(3), plane normals as integer
+// Miller triples normalised by their lengths.
+void bcc48_systems(double b[48][3], double n[48][3]) {
+  static const int B[48][3] = {
+      {-1, 1, 1}, {1, -1, 1}, {1, 1, 1}, {1, 1, -1},
+      {1, 1, -1}, {-1, 1, 1}, {1, 1, 1}, {1, -1, 1},
+      {1, 1, -1}, {1, -1, 1}, {1, 1, 1}, {-1, 1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {1, 1, -1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+      {1, -1, 1}, {1, 1, -1}, {1, 1, 1}, {-1, 1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1},
+      {-1, 1, 1}, {1, 1, 1}, {1, 1, -1}, {1, -1, 1}};
+  static const int Nn[48][3] = {
+      {1, 1, 0}, {1, 1, 0}, {1, -1, 0}, {1, -1, 0},
+      {1, 0, 1}, {1, 0, 1}, {1, 0, -1}, {1, 0, -1},
+      {0, 1, 1}, {0, 1, 1}, {0, 1, -1}, {0, 1, -1},
+      {1, 1, 2}, {-1, 1, 2}, {1, -1, 2}, {1, 1, -2},
+      {1, 2, 1}, {-1, 2, 1}, {1, -2, 1}, {1, 2, -1},
+      {2, 1, 1}, {-2, 1, 1}, {2, -1, 1}, {2, 1, -1},
+      {1, 2, 3}, {-1, 2, 3}, {1, -2, 3}, {1, 2, -3},
+      {1, 3, 2}, {-1, 3, 2}, {1, -3, 2}, {1, 3, -2},
+      {2, 1, 3}, {-2, 1, 3}, {2, -1, 3}, {2, 1, -3},
+      {2, 3, 1}, {-2, 3, 1}, {2, -3, 1}, {2, 3, -1},
+      {3, 1, 2}, {-3, 1, 2}, {3, -1, 2}, {3, 1, -2},
+      {3, 2, 1}, {-3, 2, 1}, {3, -2, 1}, {3, 2, -1}};
+  for (int s = 0; s < 48; s++) {
+    const double len = std::sqrt((double)(Nn[s][0] * Nn[s][0] + Nn[s][1] * Nn[s][1] + Nn[s][2] * Nn[s][2]));
+    for (int k = 0; k < 3; k++) {
+      b[s][k] = B[s][k] * (1.0 / std::sqrt(3.0));
+      n[s][k] = (double)Nn[s][k] / len;
+    }
+  }
+}
 void crystal_finalize(const cpfft_crystal& p, Crys& c) {
   c.p = p;
-  fcc_systems(c.b, c.n);
+  if (p.slip_type == 8) {
+    c.ns = 48;
+    bcc48_systems(c.b, c.n);
+  } else {
+    c.ns = 12;
+    double b[12][3], n[12][3];
+    fcc_systems(b, n);
+    std::memcpy(c.b, b, sizeof(b));
+    std::memcpy(c.n, n, sizeof(n));
+  }
   std::memset(c.C0, 0, sizeof(c.C0));
   if (p.elastic_type == 3) {
     double C22 = p.C11, C23 = p.C13, C66 = p.C55;
@@ -287,14 +335,16 @@ void crystal_finalize(const cpfft_crystal& p, Crys& c) {
 // Per-voxel orientation data: setup_mm10_rknstr (src/drive_eps_sig.f:537-1002)
 struct VoxProps {
   M6 C;            // stiffness rotated to the sample frame
-  double ms[12][6], qs[12][3];
+  int ns;          // slip systems
+  double ms[48][6], qs[48][3];
   M3 g;
 };
 void voxel_props(const Crys& cr, const double ang[3], VoxProps& vp) {
   kocks_g(ang, vp.g);
   M3 tr;
   tr33(vp.g, tr);  // trans_rot
-  for (int s = 0; s < 12; s++) {
+  vp.ns = cr.ns;
+  for (int s = 0; s < cr.ns; s++) {
     double bs[3], ns[3];
     for (int i = 0; i < 3; i++) {
       bs[i] = tr[i][0] * cr.b[s][0] + tr[i][1] * cr.b[s][1] + tr[i][2] * cr.b[s][2];
@@ -366,7 +416,7 @@ void state_unpack(const double* h, State& s) {
 struct Np1 {
   double D[6];
   double tinc, dg;
-  double ms[12][6], qs[12][3], qc[12][3];
+  double ms[48][6], qs[48][3], qc[48][3];
   double tt_rate;
 };
 
@@ -389,7 +439,7 @@ struct Mm10 {
     rt2rvw(tnRp, RW);
     mm33(R, tnRp, work);
     rt2rvw(work, RWC);
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < vp->ns; i++) {
       mv6(RE, vp->ms[i], s.ms[i]);
       for (int a = 0; a < 3; a++) {
         s.qs[i][a] = RW[a][0] * vp->qs[i][0] + RW[a][1] * vp->qs[i][1] + RW[a][2] * vp->qs[i][2];
@@ -421,7 +471,7 @@ struct Mm10 {
   }
   void form_wp(const Np1& s, const double* st, double tt, double w[3]) const {
     w[0] = w[1] = w[2] = 0.0;
-    for (int i = 0; i < 12; i++) {  // mm10_form_wp (src/mm10_b.f:1304-1381)
+    for (int i = 0; i < vp->ns; i++) {  // mm10_form_wp (src/mm10_b.f:1304-1381)
       double si = slipinc(s, st, tt, i);
       for (int a = 0; a < 3; a++) w[a] = w[a] + si * s.qc[i][a];
       double r = rs(s, st, i);
@@ -431,7 +481,7 @@ struct Mm10 {
   // mm10_formR1 (src/mm10_b.f:1061-1101)
   void formR1(const Np1& s, const double* st, double tt, double R1[6]) const {
     double dbar[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < 12; i++) {  // mm10_form_dbarp voce (:1161-1190)
+    for (int i = 0; i < vp->ns; i++) {  // mm10_form_dbarp voce (:1161-1190)
       double si = slipinc(s, st, tt, i);
       double r = rs(s, st, i);
       double f = r * s.tinc * p->iD_v + si;
@@ -447,7 +497,7 @@ struct Mm10 {
   // mm10_h_voche (src/mm10_b.f:1888-1912)
   double h_voce(const Np1& s, const double* st, double tt) const {
     double h = 0.0;
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < vp->ns; i++) {
       double si = slipinc(s, st, tt, i);
       double ht = hterm(tt);
       h = h + std::pow(std::fabs(ht), p->voce_m) * sgn1(ht) * std::fabs(si);
@@ -463,10 +513,10 @@ struct Mm10 {
   }
   // mm10_formJ11 (src/mm10_b.f:177-257)
   void formJ11(const Np1& s, const double* st, double tt, double J[6][6]) const {
-    double sq[12][6];
-    for (int i = 0; i < 12; i++) symsw(st, s.qc[i], sq[i]);
+    double sq[48][6];
+    for (int i = 0; i < vp->ns; i++) symsw(st, s.qc[i], sq[i]);
     std::memset(J, 0, 36 * sizeof(double));
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < vp->ns; i++) {
       double r = rs(s, st, i);
       double dgdt = std::pow(std::fabs(r), p->harden_n - 1.0);
       dgdt = s.dg * p->harden_n / std::pow(tt, p->harden_n) * dgdt;
@@ -500,10 +550,10 @@ struct Mm10 {
     double tt = x[6];
     double J11[6][6];
     formJ11(s, st, tt, J11);
-    double sq[12][6];
-    for (int i = 0; i < 12; i++) symsw(st, s.qc[i], sq[i]);
+    double sq[48][6];
+    for (int i = 0; i < vp->ns; i++) symsw(st, s.qc[i], sq[i]);
     double J12[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < 12; i++) {  // mm10_formJ12 + mm10_dgdh_voche (:271-353, 2012-2030)
+    for (int i = 0; i < vp->ns; i++) {  // mm10_formJ12 + mm10_dgdh_voche (:271-353, 2012-2030)
       double dgam = slipinc(s, st, tt, i);
       double dgdtt = -p->harden_n / tt * dgam;
       double tm[6];
@@ -513,7 +563,7 @@ struct Mm10 {
       for (int a = 0; a < 6; a++) J12[a] += tm[a] * dgdtt;
     }
     double et[6] = {0, 0, 0, 0, 0, 0};  // mm10_estress_voche (:1914-1940)
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < vp->ns; i++) {
       double r = rs(s, st, i);
       double ht = hterm(tt);
       double f = std::pow(std::fabs(ht), p->voce_m) * sgn1(ht) *
@@ -522,7 +572,7 @@ struct Mm10 {
     }
     double fac = p->theta_0 * s.dg * p->harden_n / std::pow(tt, p->harden_n);
     double etau = 0.0;  // mm10_ehard_voche (:1942-1968)
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < vp->ns; i++) {
       double si = slipinc(s, st, tt, i);
       double ht = hterm(tt);
       double a = p->voce_m * (-1.0 / p->tau_v - 0.0 / ((tt - p->tau_y) * (tt - p->tau_y))) *
@@ -783,7 +833,7 @@ struct Mm10 {
     // mm10_update_rotation (src/mm10_a.f:3310-3327) with np1 at the converged x
     {
       double wb[3] = {0, 0, 0};
-      for (int i = 0; i < 12; i++) {  // mm10_form_wbarp (src/mm10_b.f:1231-1290)
+      for (int i = 0; i < vp->ns; i++) {  // mm10_form_wbarp (src/mm10_b.f:1231-1290)
         double si = slipinc(np1, out.sig, out.tt, i);
         for (int a = 0; a < 3; a++) wb[a] = wb[a] + si * np1.qs[i][a];
         double r = rs(np1, out.sig, i);
@@ -1521,14 +1571,14 @@ void orc_polar(const double F[9], double R[9]) {
 }
 
 void orc_crystal_setup(const cpfft_crystal* props, const double kocks_deg[3], double C66[36],
-                       double ms[72], double qs[36]) {
+                       double* ms, double* qs) {
   Crys cr;
   crystal_finalize(*props, cr);
   VoxProps vp;
   voxel_props(cr, kocks_deg, vp);
   for (int a = 0; a < 6; a++)
     for (int b = 0; b < 6; b++) C66[a * 6 + b] = vp.C[a][b];
-  for (int s = 0; s < 12; s++) {
+  for (int s = 0; s < vp.ns; s++) {
     for (int a = 0; a < 6; a++) ms[s * 6 + a] = vp.ms[s][a];
     for (int a = 0; a < 3; a++) qs[s * 3 + a] = vp.qs[s][a];
   }

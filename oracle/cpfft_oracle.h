@@ -70,7 +70,7 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3],
 void orc_polar(const double F[9], double R[9]);
 /* crystal stiffness in the sample frame (row-major 6x6) and slip tensors (12x6) */
 void orc_crystal_setup(const cpfft_crystal* props, const double kocks_deg[3],
-                       double C66[36], double ms[72], double qs[36]);
+                       double C66[36], double* ms /*nslip x 6*/, double* qs /*nslip x 3*/);
 /* 3-D complex DFT of an N^3 array (split re/im), sign -1 forward, +1 backward
  * (backward scaled by 1/N^3), first index fastest. */
 void orc_fft3(int N, double* re, double* im, int sign);

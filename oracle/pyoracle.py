@@ -237,12 +237,13 @@ def polar(F):
 
 def crystal_setup(crystal, kocks):
     c = crystal_array([crystal])
+    ns = 48 if crystal.get("slip_type", 1) == 8 else 12
     C = np.zeros(36)
-    ms = np.zeros(72)
-    qs = np.zeros(36)
+    ms = np.zeros(6 * ns)
+    qs = np.zeros(3 * ns)
     lib().orc_crystal_setup(c, _p(np.ascontiguousarray(kocks, dtype=np.float64)), _p(C),
                             _p(ms), _p(qs))
-    return C.reshape(6, 6), ms.reshape(12, 6), qs.reshape(12, 3)
+    return C.reshape(6, 6), ms.reshape(ns, 6), qs.reshape(ns, 3)
 
 
 def fft3(x, sign=-1):
