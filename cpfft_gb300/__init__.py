@@ -109,6 +109,7 @@ SIGNATURES = {
     "cpfft_format_flat": (_I, [_I, ctypes.c_char_p, _LL, _P(_LL)]),
     "cpfft_write_flat": (_I, [_I, _I, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_format_e15": (_I, [_DP, _LL, ctypes.c_char_p]),
+    "cpfft_f2disp": (_I, [_D, _D, _D, _DP]),
     "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
@@ -373,6 +374,13 @@ class Solver:
         _check(load_library().cpfft_write_flat(int(quantity), int(step),
                                                structure_name.encode(), directory.encode()),
                "write_flat")
+
+    def f2disp(self, lengths=(100.0, 100.0, 100.0)):
+        """Nodal displacements (the reference's u array as ((N+1)^3, 3))."""
+        u = np.zeros(3 * (self.N + 1) ** 3)
+        _check(load_library().cpfft_f2disp(float(lengths[0]), float(lengths[1]),
+                                           float(lengths[2]), _dp(u)), "f2disp")
+        return u.reshape(-1, 3)
 
     def commit(self):
         _check(load_library().cpfft_commit_step(), "commit_step")

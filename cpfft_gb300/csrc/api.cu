@@ -27,6 +27,10 @@ cudaError_t launch_format_flat(const double* hist, long long N3, int word0, int 
 cudaError_t launch_format_values(const double* x, long long n, char* out, unsigned char* flags,
                                  cudaStream_t st);
 
+// nodal displacements (disp.cu)
+cudaError_t f2disp_device(const double* F, int N, double lx, double ly, double lz,
+                          const double* ctab, double* work, double* u, cudaStream_t st);
+
 // the learned initial guess's device weights and error check (mlp.cu)
 bool mlp_device_weights(mlp::Weights* w, int** err);
 int mlp_check_error();
@@ -1942,6 +1946,42 @@ int cpfft_write_flat(int quantity, int step, const char* structure_name, const c
     return CPFFT_ERR_BAD_ARG;
   }
   return 0;
+}
+
+// ---- nodal displacements (f2disp) -----------------------------------------------------
+int cpfft_f2disp(double lx, double ly, double lz, double* u) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (!u || !(lx > 0) || !(ly > 0) || !(lz > 0)) {
+    cpfft_set_error("cpfft_f2disp: invalid argument");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const int N = c->N;
+  const long long N1 = N + 1, nodes = N1 * N1 * N1;
+  // cos(pi k i / N) with the angle reduced to [0, 2 pi) in integers first
+  std::vector<double> ctab(N1 * N1);
+  for (long long k = 0; k < N1; k++)
+    for (long long i = 0; i < N1; i++) {
+      const long long m = (k * i) % (2LL * N);
+      ctab[k * N1 + i] = (double)cosl(3.14159265358979323846264338327950288L * m / N);
+    }
+  double *dtab = nullptr, *work = nullptr, *du = nullptr;
+  int rc = 0;
+  if ((rc = dalloc(dtab, ctab.size() * sizeof(double))) ||
+      (rc = dalloc(work, 6 * nodes * sizeof(double))) || (rc = dalloc(du, 3 * nodes * sizeof(double)))) {
+    cudaFree(dtab); cudaFree(work); cudaFree(du);
+    return rc;
+  }
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(dtab, ctab.data(), ctab.size() * sizeof(double), cudaMemcpyHostToDevice, c->st)) ||
+      (e = f2disp_device(c->Fn1, N, lx, ly, lz, dtab, work, du, c->st)) ||
+      (e = cudaMemcpyAsync(u, du, 3 * nodes * sizeof(double), cudaMemcpyDeviceToHost, c->st)) ||
+      (e = cudaStreamSynchronize(c->st)))
+    rc = cuda_check(e, "cpfft_f2disp");
+  cudaFree(dtab);
+  cudaFree(work);
+  cudaFree(du);
+  return rc;
 }
 
 }  // extern "C"

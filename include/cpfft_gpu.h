@@ -319,6 +319,15 @@ int cpfft_write_flat(int quantity, int step, const char* structure_name, const c
 /* E15.6 of n values (15 characters each, no separators) into out: the formatter above. */
 int cpfft_format_e15(const double* x, long long n, char* out);
 
+/* Nodal displacements of the current F field: replaces f2disp (src/f2disp.f:16-135) with
+ * form_BTB and its PARDISO solve.  The mesh is blkgen's (N+1)^3 nodes over the box lx x
+ * ly x lz (`sizes of x_direction ..`, src/oumodel.f:178-330), node n = i + (N+1) j +
+ * (N+1)^2 k, i along x; u (3 (N+1)^3) is the reference's u array: u[3 n + r], node 1 held
+ * at the origin.  The same least-squares system (B^T B with 2x2x2 Gauss points, B^T F with
+ * one point) is solved exactly by separable DCT-I transforms on the GPU: on the regular grid
+ * the operator is a tensor product of 1-D linear-element stiffness and mass matrices. */
+int cpfft_f2disp(double lx, double ly, double lz, double* u);
+
 /* State roll-over Fn <- Fn1, Pn <- Pn1, history n <- n+1: replaces update
  * (src/update.f:16-193) and FFT_nr3.f:173-179 in mirror mode. */
 int cpfft_commit_step(void);
