@@ -59,7 +59,8 @@ extern "C" {
 typedef struct cpfft_crystal {
     int    slip_type;      /* 1 = fcc {111}<110>, 12 systems; 8 = bcc48 {110},{112},{123}
                               <111>, 48 systems (src/mod_crystals.f:438-515, 812-1207); the
-                              crystals of one grid share the slip type                       */
+                              crystals of one grid share the slip type; CPFFT_NOT_A_CRYSTAL
+                              (0): another material model (cpfft_set_mises)                   */
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;
@@ -76,6 +77,25 @@ typedef struct cpfft_crystal {
                               converges only linearly once slip reverses on any system;
                               1: the exact derivative (no such factor). Not a deck keyword. */
 } cpfft_crystal;
+
+/* slip_type of a material that is not a crystal: its cpfft_crystal entry is not read, and
+ * cpfft_set_mises defines it before the first stress update. */
+#define CPFFT_NOT_A_CRYSTAL 0
+
+/*
+ * One bilinear Mises material: the `properties bilinear` keywords the mm01 path reads
+ * (src/inmat.f:96-126 into matprp(1:5), read by setup_mm01_rknstr,
+ * src/drive_eps_sig.f:486-520).  The reference stores them in single precision (matprp is
+ * `real`, src/mod_fft.f:20): pass those values widened to double for the same numbers.
+ */
+typedef struct cpfft_mises {
+    double e;        /* Young's modulus (matprp 1, default 30000)                      */
+    double nu;       /* Poisson's ratio (matprp 2, default 0.3)                        */
+    double yld_pt;   /* uniaxial yield stress (matprp 5)                               */
+    double tan_e;    /* tangent modulus of the bilinear curve (matprp 4)               */
+    double beta;     /* isotropic fraction of the hardening, 1 = isotropic (matprp 3,
+                        default 1)                                                     */
+} cpfft_mises;
 
 /* Per load-step statistics (mirrors the thyme buckets of src/thyme.f:15-47). */
 typedef struct cpfft_stats {
@@ -122,6 +142,14 @@ typedef struct cpfft_stats {
  */
 int cpfft_init(int N, const int* matList, const double* kocks_deg,
                const cpfft_crystal* props, int ncrystals, double tstep, int g_mapping);
+
+/* Make `material` (1-based, a matList value whose cpfft_init entry has slip_type
+ * CPFFT_NOT_A_CRYSTAL) an mm01 bilinear Mises material (src/mm01.f, model 1 of
+ * rknstr_set_up_materials, src/drive_eps_sig.f:355-420): its voxels are updated by mm01
+ * and its consistent tangent cnst1, then the same P and dP/dF pull-back as the crystals.
+ * Resets those voxels' state to mm01_set_history's.  Call before the first load step;
+ * stress updates fail with CPFFT_ERR_NOT_INIT while a declared material is undefined. */
+int cpfft_set_mises(int material, const cpfft_mises* props);
 
 /* Select the Krylov precision (CPFFT_PREC_*) and the start of the local mm10 solves
  * (warm_start: 0 = the reference's predictor from sigma_n, or an OR of the flags below).
@@ -327,6 +355,10 @@ int cpfft_format_e15(const double* x, long long n, char* out);
  * one point) is solved exactly by separable DCT-I transforms on the GPU: on the regular grid
  * the operator is a tensor product of 1-D linear-element stiffness and mass matrices. */
 int cpfft_f2disp(double lx, double ly, double lz, double* u);
+/* The nodal displacement file wndNNNNN_text of oudisp (src/ouresult.f:56-128): header,
+ * then one line of (3e15.6) per node, values below 1e-30 as zero, formatted on the GPU. */
+int cpfft_write_disp_flat(int step, double lx, double ly, double lz, const char* structure_name,
+                          const char* directory);
 
 /* State roll-over Fn <- Fn1, Pn <- Pn1, history n <- n+1: replaces update
  * (src/update.f:16-193) and FFT_nr3.f:173-179 in mirror mode. */

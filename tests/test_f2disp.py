@@ -50,3 +50,31 @@ def test_gpu_f2disp(gpulib, case):
         assert np.abs(u - uo).max() <= 1e-12 * max(L), np.abs(u - uo).max()
     finally:
         s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_disp_file(gpulib, tmp_path):
+    """oudisp's wnd file: the header and one (3e15.6) line per node of u."""
+    import os
+    from oracle import flat_ref
+    N = 5
+    r = rve.make_rve(N, 3, 72)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_REF_SHIFT)
+    try:
+        rng = np.random.default_rng(4)
+        F = np.zeros((9, N ** 3))
+        F[[0, 4, 8]] = 1.0
+        F = F + 0.01 * rng.standard_normal((9, N ** 3))
+        s.set_F(F, F)
+        u = s.f2disp((100.0, 100.0, 100.0))
+        s.write_disp_flat(3, (100.0, 100.0, 100.0), "rve5", str(tmp_path))
+        lines = open(os.path.join(tmp_path, "wnd00003_text")).read().split("\n")
+        assert lines[1] == "#  WARP3D nodal results: displacements  "
+        assert lines[3] == "#  Model nodes, elements: %8d%8d" % ((N + 1) ** 3, N ** 3)
+        body = lines[7:-1]
+        assert len(body) == (N + 1) ** 3
+        for n, line in enumerate(body):
+            vals = [0.0 if abs(x) < 1e-30 else x for x in u[n]]
+            assert line == "".join(flat_ref.e15_6(x) for x in vals)
+    finally:
+        s.close()
