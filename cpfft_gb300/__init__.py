@@ -15,6 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
 HIST_WORDS = 29
+NOT_A_CRYSTAL = 0  # slip_type of a material defined by Solver.set_mises
 
 G_REF_SHIFT, G_CENTERED = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
@@ -79,6 +80,13 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Mises(ctypes.Structure):
+    """``cpfft_mises`` of include/cpfft_gpu.h (bilinear Mises, mm01)."""
+
+    _fields_ = [("e", ctypes.c_double), ("nu", ctypes.c_double), ("yld_pt", ctypes.c_double),
+                ("tan_e", ctypes.c_double), ("beta", ctypes.c_double)]
+
+
 class Rve(ctypes.Structure):
     """``cpfft_rve`` of include/cpfft_gpu.h (one RVE of cpfft_batch_solve)."""
 
@@ -104,6 +112,7 @@ SIGNATURES = {
     "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
     "cpfft_set_mode": (_I, [_I, _I]),
     "cpfft_set_precond": (_I, [_I]),
+    "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
     "cpfft_format_flat": (_I, [_I, ctypes.c_char_p, _LL, _P(_LL)]),
@@ -275,6 +284,13 @@ class Solver:
         _check(load_library().cpfft_tuning(t.ctypes.data_as(_IP), _dp(ms)), "cpfft_tuning")
         return {"fp32_tiles": t[:2].tolist(), "double_float_tiles": t[2:].tolist(),
                 "fp32_ms": float(ms[0]), "double_float_ms": float(ms[1])}
+
+    def set_mises(self, material, e, nu, yld_pt, tan_e, beta=1.0):
+        """Make the 1-based ``material`` (declared with slip_type NOT_A_CRYSTAL) a bilinear
+        Mises material (mm01)."""
+        m = Mises(float(e), float(nu), float(yld_pt), float(tan_e), float(beta))
+        _check(load_library().cpfft_set_mises(int(material), ctypes.byref(m)),
+               "cpfft_set_mises")
 
     def set_precond(self, precond=PRECOND_REFERENCE):
         """Reference-medium preconditioner of the mixed-precision inner iterations."""

@@ -296,6 +296,14 @@ struct Ctx {
   int *ori = nullptr, *crys = nullptr;
   OriRec* oris = nullptr;
   CrysRec* cryss = nullptr;
+  // materials: 0-based material of every voxel; per material 0 = crystal, 1 = mm01
+  // (cpfft_set_mises), 2 = declared non-crystal and not yet defined
+  std::vector<int> mat;
+  std::vector<int> mat_kind;
+  long long n_crys_vox = 0, n_mises_vox = 0, n_undef_vox = 0;
+  std::vector<MisesRec> h_mises;  // per material (index = material)
+  int* mises = nullptr;           // (N3) material of an mm01 voxel, -1 for a crystal voxel
+  MisesRec* misess = nullptr;     // per material
   double2* S = nullptr;
   float2* Sf = nullptr;
   double2* tw = nullptr;
@@ -389,7 +397,8 @@ void free_ctx(Ctx* c) {
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
-                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq, c->pre_dev};
+                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq, c->pre_dev,
+                  c->mises, c->misess};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -949,7 +958,14 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.crys = c->crys;
   a.oris = c->oris;
   a.cryss = c->cryss;
+  a.mises = c->n_mises_vox ? c->mises : nullptr;
+  a.misess = c->misess;
   a.stats = c->stats;
+  if (c->n_undef_vox) {
+    cpfft_set_error("stress update: %lld voxels of a material declared CPFFT_NOT_A_CRYSTAL "
+                    "that cpfft_set_mises has not defined", c->n_undef_vox);
+    return CPFFT_ERR_NOT_INIT;
+  }
   a.N3 = c->N3;
   a.dt = c->dt;
   a.step = step;
@@ -988,7 +1004,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.perm = nullptr;
   a.queue = nullptr;
   a.cost = nullptr;
-  if (c->sched == CPFFT_SCHED_QUEUE && iter > 0) {
+  if (c->sched == CPFFT_SCHED_QUEUE && iter > 0 && c->n_crys_vox) {
     CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
     a.perm = c->vperm;
     a.queue = c->vq + 128;
@@ -996,7 +1012,9 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   }
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
-  CK(c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+  if (c->n_crys_vox)
+    CK(c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+  if (c->n_mises_vox) CK(launch_mises(a, c->st));
   TRY(kt_stop(c));
   c->pass_step = step;
   c->pass_iter = iter;
@@ -1185,8 +1203,11 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   std::vector<std::vector<double>> C0(ncrystals, std::vector<double>(36));
   double bb[48][3], nn[48][3];
   int nslip = 0;
+  int first_crystal = -1;
   for (int k = 0; k < ncrystals; k++) {
     const cpfft_crystal& p = props[k];
+    if (p.slip_type == CPFFT_NOT_A_CRYSTAL) continue;  // defined by cpfft_set_mises
+    if (first_crystal < 0) first_crystal = k;
     const int ns = slip_geometry(p.slip_type, bb, nn);
     if (!ns || p.h_type != 1 || !(p.tau_v != 0) || !(p.harden_n > 0) ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
@@ -1201,17 +1222,23 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     nslip = ns;
     cr[k] = crystal_record(p);
   }
-  slip_geometry(props[0].slip_type, bb, nn);
-  // distinct (crystal, orientation) records
-  std::vector<int> ori(N3), crys(N3);
+  if (first_crystal >= 0) slip_geometry(props[first_crystal].slip_type, bb, nn);
+  if (!nslip) nslip = 12;
+  // distinct (crystal, orientation) records; a voxel of another material points at the
+  // first crystal's first record (the crystal kernel reads but never stores it)
+  std::vector<int> ori(N3), crys(N3), mat(N3);
   std::map<std::tuple<int, double, double, double>, int> seen;
   std::vector<OriRec> oris;
+  long long n_crys_vox = 0;
   for (long long v = 0; v < N3; v++) {
     int m = matList[v] - 1;
     if (m < 0 || m >= ncrystals) {
       cpfft_set_error("cpfft_init: matList[%lld] = %d out of range", v, matList[v]);
       return CPFFT_ERR_BAD_ARG;
     }
+    mat[v] = m;
+    if (props[m].slip_type == CPFFT_NOT_A_CRYSTAL) continue;
+    n_crys_vox++;
     double ang[3] = {kocks_deg[v], kocks_deg[N3 + v], kocks_deg[2 * N3 + v]};
     auto key = std::make_tuple(m, ang[0], ang[1], ang[2]);
     auto it = seen.find(key);
@@ -1227,8 +1254,21 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     ori[v] = id;
     crys[v] = m;
   }
+  if (oris.empty()) oris.emplace_back(OriRec{});  // no crystal voxel: never read
+  for (long long v = 0; v < N3; v++)
+    if (props[mat[v]].slip_type == CPFFT_NOT_A_CRYSTAL) {
+      ori[v] = 0;
+      crys[v] = first_crystal >= 0 ? first_crystal : 0;
+    }
   Ctx* c = new Ctx;
   c->nslip = nslip;
+  c->mat = mat;
+  c->mat_kind.assign(ncrystals, 0);
+  for (int k = 0; k < ncrystals; k++)
+    if (props[k].slip_type == CPFFT_NOT_A_CRYSTAL) c->mat_kind[k] = 2;
+  c->h_mises.assign(ncrystals, MisesRec{});
+  c->n_crys_vox = n_crys_vox;
+  c->n_undef_vox = N3 - n_crys_vox;
   c->N = N;
   c->N3 = N3;
   c->dt = tstep;
@@ -1293,6 +1333,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   // history at n = the state of mm10_init_cc_hist0 (sigma 0, tau_y + 1e-5, Rp = I)
   std::vector<double> h(H_WORDS * N3, 0.0);
   for (long long v = 0; v < N3; v++) {
+    if (props[mat[v]].slip_type == CPFFT_NOT_A_CRYSTAL) continue;
     h[H_TT * N3 + v] = props[crys[v]].tau_y + 1.0e-5;
     for (int d : {0, 4, 8}) h[(H_RP + d) * N3 + v] = 1.0;
   }
@@ -1317,6 +1358,73 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   }
   for (int i = 0; i < 81; i++) c->C_homo[i] = 0.0;
   g_ctx = c;
+  return 0;
+}
+
+int cpfft_set_mises(int material, const cpfft_mises* props) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (material < 1 || material > (int)c->mat_kind.size() || !props) {
+    cpfft_set_error("cpfft_set_mises: material %d out of range", material);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const int m = material - 1;
+  const cpfft_mises& p = *props;
+  if (c->mat_kind[m] == 0) {
+    cpfft_set_error("cpfft_set_mises: material %d is a crystal (declare it with slip_type "
+                    "CPFFT_NOT_A_CRYSTAL in cpfft_init)", material);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (!(p.e > 0) || !(p.nu > -1.0 && p.nu < 0.5) || !(p.yld_pt > 0) || !(p.tan_e >= 0) ||
+      !(p.tan_e < p.e) || !(p.beta >= 0 && p.beta <= 1)) {
+    cpfft_set_error("cpfft_set_mises: material %d: need e > 0, -1 < nu < 0.5, yld_pt > 0, "
+                    "0 <= tan_e < e, 0 <= beta <= 1", material);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  // setup_mm01_rknstr (src/drive_eps_sig.f:486-520): h = tan_e e / (e - tan_e)
+  c->h_mises[m] = MisesRec{p.e, p.nu, p.yld_pt, p.tan_e * p.e / (p.e - p.tan_e), p.beta};
+  const long long N3 = c->N3;
+  if (!c->mises) {
+    TRY(dalloc(c->mises, N3 * sizeof(int)));
+    TRY(dalloc(c->misess, c->mat_kind.size() * sizeof(MisesRec)));
+  }
+  c->mat_kind[m] = 1;
+  std::vector<int> idx(N3);
+  long long nm = 0, nu = 0;
+  for (long long v = 0; v < N3; v++) {
+    const int k = c->mat_kind[c->mat[v]];
+    idx[v] = k == 1 ? c->mat[v] : -1;
+    nm += k == 1;
+    nu += k == 2;
+  }
+  // the voxels' state at n and n+1: mm01_set_history's (src/mm01.f:240-310)
+  std::vector<double> h(H_WORDS * N3);
+  cudaError_t e;
+  for (int t = 0; t < 2; t++) {
+    if ((e = cudaMemcpy(h.data(), c->hist[t], h.size() * sizeof(double), cudaMemcpyDeviceToHost))) {
+      cpfft_set_error("cpfft_set_mises: %s", cudaGetErrorString(e));
+      return CPFFT_ERR_CUDA;
+    }
+    for (long long v = 0; v < N3; v++) {
+      if (c->mat[v] != m) continue;
+      for (int w = 0; w < H_WORDS; w++) h[w * N3 + v] = 0.0;
+      h[M1_K * N3 + v] = p.yld_pt / 1.73205080756888;
+      h[M1_STATE * N3 + v] = 3.0;
+      h[M1_HP * N3 + v] = c->h_mises[m].h;
+    }
+    if ((e = cudaMemcpy(c->hist[t], h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice))) {
+      cpfft_set_error("cpfft_set_mises: %s", cudaGetErrorString(e));
+      return CPFFT_ERR_CUDA;
+    }
+  }
+  if ((e = cudaMemcpy(c->mises, idx.data(), N3 * sizeof(int), cudaMemcpyHostToDevice)) ||
+      (e = cudaMemcpy(c->misess, c->h_mises.data(), c->h_mises.size() * sizeof(MisesRec),
+                      cudaMemcpyHostToDevice))) {
+    cpfft_set_error("cpfft_set_mises: %s", cudaGetErrorString(e));
+    return CPFFT_ERR_CUDA;
+  }
+  c->n_mises_vox = nm;
+  c->n_undef_vox = nu;
   return 0;
 }
 
@@ -1982,6 +2090,48 @@ int cpfft_f2disp(double lx, double ly, double lz, double* u) {
   cudaFree(work);
   cudaFree(du);
   return rc;
+}
+
+int cpfft_write_disp_flat(int step, double lx, double ly, double lz, const char* structure_name,
+                          const char* directory) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  const long long N1 = c->N + 1, nodes = N1 * N1 * N1;
+  std::vector<double> u(3 * nodes);
+  TRY(cpfft_f2disp(lx, ly, lz, u.data()));
+  for (double& x : u)
+    if (std::fabs(x) < 1.0e-30) x = 0.0;  // oudisp's small_tol (src/ouresult.f:71,107)
+  std::vector<char> fields(15 * 3 * nodes);
+  TRY(cpfft_format_e15(u.data(), 3 * nodes, fields.data()));
+  // wnd + step (i5.5) + _text (ouocdd, src/ouresult.f:419-540); header of
+  // ouddpa_flat_header with type 1, quantity 1 (src/ouresult.f:335-396)
+  int stepno = step > 99999 ? step - 99999 : step;
+  char name[64];
+  snprintf(name, sizeof(name), "wnd%05d_text", stepno);
+  std::string path = directory && directory[0] ? std::string(directory) + "/" + name : name;
+  FILE* f = fopen(path.c_str(), "w");
+  if (!f) {
+    cpfft_set_error("cpfft_write_disp_flat: cannot open %s", path.c_str());
+    return CPFFT_ERR_BAD_ARG;
+  }
+  char sname[9];
+  snprintf(sname, sizeof(sname), "%-8.8s", structure_name ? structure_name : "");
+  time_t now = time(nullptr);
+  char date[32];
+  strftime(date, sizeof(date), "%a %b %e %H:%M:%S %Y", localtime(&now));
+  fprintf(f, "#\n#  WARP3D nodal results: %-15s\n#  Structure name: %s\n"
+             "#  Model nodes, elements: %8lld%8lld\n#  %-24s\n#  Load(time) step: %8d\n#\n",
+          "displacements", sname, nodes, c->N3, date, step);
+  bool ok = true;
+  for (long long n = 0; n < nodes && ok; n++) {  // format (3e15.6), one node a line
+    ok = fwrite(fields.data() + 45 * n, 1, 45, f) == 45 && fputc('\n', f) != EOF;
+  }
+  fclose(f);
+  if (!ok) {
+    cpfft_set_error("cpfft_write_disp_flat: short write to %s", path.c_str());
+    return CPFFT_ERR_BAD_ARG;
+  }
+  return 0;
 }
 
 }  // extern "C"

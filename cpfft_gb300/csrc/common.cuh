@@ -46,6 +46,13 @@ struct CrysRec {
   int m_is_one;    // voce_m == 1
 };
 
+// One bilinear Mises material (mm01, src/mm01.f; properties of setup_mm01_rknstr,
+// src/drive_eps_sig.f:486-520): e, nu, uniaxial yield stress, plastic modulus
+// h = tan_e e / (e - tan_e) and the isotropic fraction beta of the hardening.
+struct MisesRec {
+  double e, nu, yld, h, beta;
+};
+
 // Words of the compact per-voxel history (CPFFT_HIST_WORDS)
 enum {
   H_SIG = 0,      // 6  unrotated Cauchy stress
@@ -57,12 +64,27 @@ enum {
   H_WORDS = 29
 };
 
+// The same 29 words for an mm01 voxel: H_SIG and H_EPS as above, and in words 6..19 the
+// mm01 history vector (mm01_set_history, src/mm01.f:240-310) followed by the three extra
+// stress-vector words of oupestr's cgn(7:9) (src/mm01.f:95-100)
+enum {
+  M1_LDT = 6,     // 1  lambda * dt of the step (plastic multiplier)
+  M1_K = 7,       // 1  radius k of the yield surface (shear yield stress)
+  M1_EPSP = 8,    // 1  accumulated uniaxial plastic strain
+  M1_STATE = 9,   // 1  1 = actively yielding, 3 = not
+  M1_HP = 10,     // 1  plastic modulus at n+1
+  M1_ALPHA = 11,  // 6  back stress
+  M1_U = 17,      // 1  strain energy density
+  M1_WP = 18,     // 1  plastic work density
+  M1_EBP = 19     // 1  accumulated equivalent plastic strain (of the plastic work update)
+};
+
 // Stress kernel launch arguments
 struct StressArgs {
   const double* Fn;      // (9, N3)
   const double* Fn1;     // (9, N3)
-  const double* hist_n;  // (23, N3)
-  double* hist_np1;      // (23, N3): written; read as the previous iterate's local state
+  const double* hist_n;  // (H_WORDS, N3)
+  double* hist_np1;      // (H_WORDS, N3): written; read as the previous iterate's local state
   double* P;             // (9, N3)
   double* K4;            // (81, N3)
   float* K4f;            // (81, N3) optional FP32 copy (mixed precision), may be null
@@ -71,6 +93,9 @@ struct StressArgs {
   const int* crys;       // (N3) crystal id, 0-based
   const OriRec* oris;
   const CrysRec* cryss;
+  // mm01 voxels: mises[v] = index into misess, -1 for a crystal voxel (null: none)
+  const int* mises;
+  const MisesRec* misess;
   unsigned long long* stats;  // [0] local iters, [1] failures, [2] predict iters,
                               // [3] learned guesses the Newton solve rejected
   long long N3;
@@ -107,6 +132,8 @@ struct StressArgs {
 // serves crystals with 12 slip systems (FCC), launch_stress48 those with 48 (BCC48).
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
+// the mm01 voxels (a.mises[v] >= 0) of the grid; the crystal launches skip them
+cudaError_t launch_mises(const StressArgs& a, cudaStream_t s);
 // Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost
 // bin, queue head zeroed.  scratch: 128 unsigned ints.
 cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,

@@ -744,6 +744,11 @@ __device__ void guess_features(const double* g, const double* nRp, const double*
 template <bool WARM>
 __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& iters,
                              int& piters, bool& ok, int& rejected, GuessBlock* gb);
+__device__ void kinematics(const double* Fn, const double* Fn1, double* rnh, double* rn1,
+                           double* fnhinv, double* uddt);
+__device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, const double* Fn1,
+                           const double* stress, const double* cep, const double* rnh,
+                           const double* rn1, const double* fnhinv);
 
 // WARM: the learned initial guess starts each local Newton solve (launches with iter > 0
 // only); every thread of the block takes part in the block-level network evaluation, so
@@ -783,14 +788,16 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
     const bool valid = idx < a.N3;
     const long long last = a.N3 - 1;
     const long long v = a.perm ? (long long)a.perm[valid ? idx : last] : (valid ? idx : last);
+    // mm01 voxels belong to launch_mises: here they only fill the network's tile
+    const bool mine = valid && (!a.mises || __ldg(a.mises + v) < 0);
     int it = 0, pit = 0, rj = 0;
     bool ok = true;
     if (WARM) {
-      voxel_update<true>(a, v, valid, it, pit, ok, rj, &gb);
-    } else if (valid) {
+      voxel_update<true>(a, v, mine, it, pit, ok, rj, &gb);
+    } else if (mine) {
       voxel_update<false>(a, v, true, it, pit, ok, rj, nullptr);
     }
-    if (valid) {
+    if (mine) {
       iters += it;
       piters += pit;
       rej += rj;
@@ -904,29 +911,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int i = 0; i < 6; i++) nD[i] = a.hist_n[(H_D + i) * N3 + v];
     nttr = a.hist_n[H_TTR * N3 + v];
   }
-  // ---- kinematics (src/drive_eps_sig.f:227-265)
-  double fnh[9], dfn[9], rnh[9], rn1[9], fnhinv[9], fn1inv[9];
-  for (int i = 0; i < 9; i++) { fnh[i] = 0.5 * (Fn[i] + Fn1[i]); dfn[i] = Fn1[i] - Fn[i]; }
-  polar_R(fnh, rnh);
-  polar_R(Fn1, rn1);
-  inv3(fnh, fnhinv);
-  double ddt[6];
-  {
-    double L[9];
-    mm3(dfn, fnhinv, L);
-    ddt[0] = L[0]; ddt[1] = L[4]; ddt[2] = L[8];
-    ddt[3] = L[3] + L[1]; ddt[4] = L[7] + L[5]; ddt[5] = L[6] + L[2];
-  }
-  double uddt[6];
-  {  // getrm1 option 1 + qmply1: d = R^T D R in engineering-shear Voigt form
-    double Dm[9] = {ddt[0], 0.5 * ddt[3], 0.5 * ddt[5], 0.5 * ddt[3], ddt[1], 0.5 * ddt[4],
-                    0.5 * ddt[5], 0.5 * ddt[4], ddt[2]};
-    double t1[9], dm[9];
-    mtm3(rnh, Dm, t1);
-    mm3(t1, rnh, dm);
-    uddt[0] = dm[0]; uddt[1] = dm[4]; uddt[2] = dm[8];
-    uddt[3] = 2.0 * dm[1]; uddt[4] = 2.0 * dm[5]; uddt[5] = 2.0 * dm[2];
-  }
+  double rnh[9], rn1[9], fnhinv[9], uddt[6];
+  kinematics(Fn, Fn1, rnh, rn1, fnhinv, uddt);
   // ---- mm10 (src/mm10_a.f:2628-2845, 1080-1157)
   Crystal s;
   s.cr = cr;
@@ -1160,7 +1146,45 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   // src/drive_eps_sig.f:264-265, src/rstgp1.f:1378-1394); zero at n for step 1
   for (int i = 0; i < 6; i++)
     a.hist_np1[(H_EPS + i) * N3 + v] = (a.step == 1 ? 0.0 : a.hist_n[(H_EPS + i) * N3 + v]) + uddt[i];
-  // ---- Cauchy stress and P = J T F^-T (cs2p, src/drive_eps_sig.f:1182-1224)
+  store_P_K4(a, v, Fn, Fn1, stress, cep, rnh, rn1, fnhinv);
+}
+
+// kinematics of the material point (src/drive_eps_sig.f:227-265): the rotations of F at
+// the half step and at n+1, (F_n+1/2)^-1, and the unrotated strain increment uddt
+// (engineering shear)
+__device__ void kinematics(const double* Fn, const double* Fn1, double* rnh, double* rn1,
+                           double* fnhinv, double* uddt) {
+  double fnh[9], dfn[9];
+  for (int i = 0; i < 9; i++) { fnh[i] = 0.5 * (Fn[i] + Fn1[i]); dfn[i] = Fn1[i] - Fn[i]; }
+  polar_R(fnh, rnh);
+  polar_R(Fn1, rn1);
+  inv3(fnh, fnhinv);
+  double ddt[6];
+  {
+    double L[9];
+    mm3(dfn, fnhinv, L);
+    ddt[0] = L[0]; ddt[1] = L[4]; ddt[2] = L[8];
+    ddt[3] = L[3] + L[1]; ddt[4] = L[7] + L[5]; ddt[5] = L[6] + L[2];
+  }
+  {  // getrm1 option 1 + qmply1: d = R^T D R in engineering-shear Voigt form
+    double Dm[9] = {ddt[0], 0.5 * ddt[3], 0.5 * ddt[5], 0.5 * ddt[3], ddt[1], 0.5 * ddt[4],
+                    0.5 * ddt[5], 0.5 * ddt[4], ddt[2]};
+    double t1[9], dm[9];
+    mtm3(rnh, Dm, t1);
+    mm3(t1, rnh, dm);
+    uddt[0] = dm[0]; uddt[1] = dm[4]; uddt[2] = dm[8];
+    uddt[3] = 2.0 * dm[1]; uddt[4] = 2.0 * dm[5]; uddt[5] = 2.0 * dm[2];
+  }
+}
+
+// P = J T F^-T from the unrotated stress (getrm1 option 2 + cs2p, src/drive_eps_sig.f:
+// 285-296, 1182-1224) and dP/dF from the 6x6 tangent (cep2A, src/cep2A.f:86-284), into
+// P, K4 and the FP32 copies the mixed-precision operator reads
+__device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, const double* Fn1,
+                           const double* stress, const double* cep, const double* rnh,
+                           const double* rn1, const double* fnhinv) {
+  const long long N3 = a.N3;
+  double fn1inv[9];
   double tm[9] = {stress[0], stress[3], stress[5], stress[3], stress[1], stress[4],
                   stress[5], stress[4], stress[2]};
   double detF = inv3(Fn1, fn1inv);
@@ -1199,7 +1223,197 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     }
 }
 
+#if CPFFT_NSLIP == 12
+// ---- mm01: rate-independent Mises plasticity, bilinear uniaxial curve, mixed isotropic /
+// kinematic hardening (src/mm01.f), one voxel ---------------------------------------------
+// The isothermal update: mm01_init (:328-535), mm01_simple1 (:704-785), mm01_sig_final
+// (:626-690), mm01_plastic_work (:546-615), and the consistent tangent cnst1
+// (:1222-1374); the reference's decimal constants are kept as it writes them.  Inputs:
+// deps = uddt (engineering shear), the 29 history words at n (step 1: the state of
+// mm01_set_history, :240-310, with zero stresses).  Outputs: the 29 words at n+1 except
+// H_EPS, and the 6x6 tangent (row-major).
+__device__ void mises_update(const MisesRec& m, int step, const double* hn, const double* deps,
+                             double* hn1, double* cep) {
+  const double one = 1.0, two = 2.0, three = 3.0, half = 0.5;
+  const double root2 = 1.414213562373095, root3 = 1.7320508075688;
+  const double twthrd = 0.666666666666667, root23 = 0.816496580927;
+  const double yld_tol = 1.0e-7, htol = 1.0e-6;
+  double cgn[9], hist[12];  // stress vector at n (6 stresses, U, Wp, eps_p bar); hist[1..11]
+  if (step == 1) {
+    for (int i = 0; i < 9; i++) cgn[i] = 0.0;
+    for (int i = 0; i < 12; i++) hist[i] = 0.0;
+    hist[2] = m.yld / 1.73205080756888;
+    hist[4] = 3.0;
+    hist[5] = m.h;
+  } else {
+    for (int i = 0; i < 6; i++) cgn[i] = hn[H_SIG + i];
+    cgn[6] = hn[M1_U];
+    cgn[7] = hn[M1_WP];
+    cgn[8] = hn[M1_EBP];
+    hist[0] = 0.0;
+    for (int i = 1; i <= 11; i++) hist[i] = hn[M1_LDT + i - 1];
+  }
+  // ---- mm01_init: trial elastic state with the moduli at n and n+1 (both the deck's)
+  const double e = m.e, nu = m.nu, beta = m.beta, hp = m.h;
+  const double deps_vol = deps[0] + deps[1] + deps[2];
+  const double eps_mean = deps_vol / three;
+  const double g_n = e / two / (one + nu);
+  const double een1 = (cgn[0] - nu * (cgn[1] + cgn[2])) / e;
+  const double een2 = (cgn[1] - nu * (cgn[0] + cgn[2])) / e;
+  const double een3 = (cgn[2] - nu * (cgn[0] + cgn[1])) / e;
+  const double een4 = cgn[3] / g_n, een5 = cgn[4] / g_n, een6 = cgn[5] / g_n;
+  const double eps_vol_n1 = een1 + een2 + een3 + deps_vol;
+  const double eps_mean_n = (een1 + een2 + een3) / three;
+  const double ee[6] = {(een1 - eps_mean_n) + (deps[0] - eps_mean),
+                        (een2 - eps_mean_n) + (deps[1] - eps_mean),
+                        (een3 - eps_mean_n) + (deps[2] - eps_mean),
+                        een4 + deps[3], een5 + deps[4], een6 + deps[5]};
+  const double G = e / (two * (one + nu));
+  double dev_el[6], alpha[6], rtse[6];
+  for (int i = 0; i < 3; i++) dev_el[i] = two * G * ee[i];
+  for (int i = 3; i < 6; i++) dev_el[i] = G * ee[i];
+  for (int i = 0; i < 6; i++) alpha[i] = hist[6 + i];
+  const double hbari_np1 = beta * hp, hbark_np1 = (one - beta) * hp;
+  const double hbark_n = (one - beta) * hist[5];
+  const double kbar = (m.yld + hbari_np1 * hist[3]) / root3;
+  double lk = one;
+  if (fabs(hbark_n) > htol) lk = hbark_np1 / hbark_n;
+  for (int i = 0; i < 6; i++) rtse[i] = dev_el[i] - alpha[i] * lk;
+  double mrts = sqrt(rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
+                     two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]));
+  const double yf = mrts - root2 * kbar;
+  for (int i = 0; i < 6; i++) rtse[i] = dev_el[i] - alpha[i];
+  mrts = sqrt(rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
+              two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]));
+  const bool yield = yf >= yld_tol * root2 * kbar;
+  // ---- mm01_simple1 (yielding) or the elastic update of mm01
+  double h1[12], dev[6];
+  if (yield) {
+    const double ldt = (mrts - root2 * kbar) / (twthrd * (three * G + hp));
+    const double k_np1 = kbar + (root2 / three) * hbari_np1 * ldt;
+    h1[1] = ldt;
+    h1[2] = k_np1;
+    h1[3] = hist[3] + ldt * root23;
+    h1[5] = hp;
+    const double const1 = twthrd * hbark_np1 * ldt / mrts;
+    const double const2 = root2 * k_np1 / mrts;
+    for (int i = 0; i < 6; i++) {
+      h1[6 + i] = hist[6 + i] + const1 * rtse[i];
+      dev[i] = h1[6 + i] + const2 * rtse[i];
+    }
+  } else {
+    h1[1] = 0.0;
+    h1[2] = kbar;
+    h1[3] = hist[3];
+    h1[5] = hp;
+    for (int i = 0; i < 6; i++) {
+      h1[6 + i] = alpha[i] * lk;
+      dev[i] = rtse[i] + alpha[i];
+    }
+  }
+  h1[4] = yield ? 1.0 : 3.0;
+  // ---- mm01_sig_final: mean stress, energy density
+  double cgn1[9];
+  const double sig_mean =
+      eps_vol_n1 * (three * e * nu / ((one + nu) * (one - two * nu)) + two * G) / three;
+  for (int i = 0; i < 3; i++) cgn1[i] = dev[i] + sig_mean;
+  for (int i = 3; i < 6; i++) cgn1[i] = dev[i];
+  {
+    double w = 0.0;
+    for (int i = 0; i < 6; i++) w += deps[i] * (cgn1[i] + cgn[i]);
+    cgn1[6] = cgn[6] + half * w;
+  }
+  // ---- mm01_plastic_work
+  cgn1[7] = cgn[7];
+  cgn1[8] = cgn[8];
+  if (yield) {
+    double ds[6], dp[6];
+    for (int i = 0; i < 6; i++) ds[i] = cgn1[i] - cgn[i];
+    dp[0] = deps[0] - (ds[0] - nu * (ds[1] + ds[2])) / e;
+    dp[1] = deps[1] - (ds[1] - nu * (ds[0] + ds[2])) / e;
+    dp[2] = deps[2] - (ds[2] - nu * (ds[0] + ds[1])) / e;
+    for (int i = 3; i < 6; i++) dp[i] = deps[i] - ds[i] / G;
+    double w = 0.0;
+    for (int i = 0; i < 6; i++) w += dp[i] * (cgn1[i] + cgn[i]);
+    cgn1[7] = cgn[7] + half * w;
+    const double f1 = (dp[0] - dp[1]) * (dp[0] - dp[1]) + (dp[1] - dp[2]) * (dp[1] - dp[2]) +
+                      (dp[0] - dp[2]) * (dp[0] - dp[2]);
+    const double f2 = dp[3] * dp[3] + dp[4] * dp[4] + dp[5] * dp[5];
+    cgn1[8] = cgn[8] + (root2 / three) * sqrt(f1 + (three / two) * f2);
+  }
+  // ---- cnst1: consistent tangent (rtsg = rtse, kn1 = k_n+1, ldt = lambda dt)
+  for (int i = 0; i < 36; i++) cep[i] = 0.0;
+  if (!yield) {
+    const double c1 = e / ((one + nu) * (one - two * nu));
+    const double c2 = (one - nu) * c1, c3 = ((one - two * nu) / two) * c1, c4 = nu * c1;
+    for (int i = 0; i < 3; i++) {
+      for (int j = 0; j < 3; j++) cep[6 * i + j] = i == j ? c2 : c4;
+      cep[6 * (i + 3) + i + 3] = c3;
+    }
+  } else {
+    const double root2c = 1.414213562;  // cnst1's own sqrt(2)
+    const double g = e / (two * (one + nu));
+    const double l = (e * nu) / ((one + nu) * (one - two * nu));
+    const double k = (three * l + two * g) / three;
+    const double mrtsq = rtse[0] * rtse[0] + rtse[1] * rtse[1] + rtse[2] * rtse[2] +
+                         two * (rtse[3] * rtse[3] + rtse[4] * rtse[4] + rtse[5] * rtse[5]);
+    const double bb = (root2c * h1[2] + (two / three) * (one - beta) * h1[5] * h1[1]) / sqrt(mrtsq);
+    const double gamma = one / (one + h1[5] / (three * g));
+    const double gambar = gamma - one + bb;
+    const double gbar = g * bb;
+    const double albar = k - two * gbar / three;
+    const double thbar = two * g * gambar;
+    for (int i = 0; i < 6; i++)
+      for (int j = 0; j <= i; j++) {
+        double c = -(thbar * rtse[j] * rtse[i] / mrtsq);
+        if (i < 3 && j < 3) c += albar;
+        if (i == j) c += i < 3 ? two * gbar : gbar;
+        cep[6 * i + j] = c;
+        cep[6 * j + i] = c;
+      }
+  }
+  for (int i = 0; i < 6; i++) hn1[H_SIG + i] = cgn1[i];
+  for (int i = 1; i <= 11; i++) hn1[M1_LDT + i - 1] = h1[i];
+  hn1[M1_U] = cgn1[6];
+  hn1[M1_WP] = cgn1[7];
+  hn1[M1_EBP] = cgn1[8];
+  for (int w = M1_EBP + 1; w < H_EPS; w++) hn1[w] = 0.0;
+}
+
+__global__ void __launch_bounds__(128) mises_kernel(StressArgs a) {
+  const long long N3 = a.N3;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < N3;
+       v += (long long)gridDim.x * blockDim.x) {
+    const int mi = __ldg(a.mises + v);
+    if (mi < 0) continue;
+    const MisesRec m = a.misess[mi];
+    double Fn[9], Fn1[9], hn[H_WORDS], hn1[H_WORDS], cep[36];
+    for (int i = 0; i < 9; i++) {
+      Fn[i] = __ldg(a.Fn + i * N3 + v);
+      Fn1[i] = __ldg(a.Fn1 + i * N3 + v);
+    }
+    for (int w = 0; w < H_WORDS; w++) hn[w] = a.step == 1 ? 0.0 : a.hist_n[w * N3 + v];
+    double rnh[9], rn1[9], fnhinv[9], uddt[6];
+    kinematics(Fn, Fn1, rnh, rn1, fnhinv, uddt);
+    mises_update(m, a.step, hn, uddt, hn1, cep);
+    for (int i = 0; i < 6; i++) hn1[H_EPS + i] = hn[H_EPS + i] + uddt[i];
+    for (int w = 0; w < H_WORDS; w++) a.hist_np1[w * N3 + v] = hn1[w];
+    store_P_K4(a, v, Fn, Fn1, hn1 + H_SIG, cep, rnh, rn1, fnhinv);
+  }
+}
+#endif
+
 }  // namespace
+
+#if CPFFT_NSLIP == 12
+cudaError_t launch_mises(const StressArgs& a, cudaStream_t s) {
+  if (a.N3 <= 0 || !a.mises) return cudaSuccess;
+  const unsigned blocks = (unsigned)std::min<long long>((a.N3 + 127) / 128, 152LL * 16);
+  mises_kernel<<<blocks, 128, 0, s>>>(a);
+  g_kernel_launches += 1;
+  return cudaGetLastError();
+}
+#endif
 
 cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;

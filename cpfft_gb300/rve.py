@@ -34,6 +34,26 @@ BCC48_DECK = dict(
     exact_j22=0,
 )
 
+# The material entry of a non-crystal material: not read by the crystal path (the
+# bilinear Mises properties go through Solver.set_mises).
+NOT_A_CRYSTAL = dict(FCC_VOCE, slip_type=0)
+
+
+def single(x):
+    """A deck value as the reference holds material properties: single precision (matprp
+    is `real`, src/mod_fft.f:20), widened to double."""
+    return float(np.float32(x))
+
+
+# The two bilinear Mises materials of the reference's example deck (examples/test_mm01.in):
+# (e, nu, yld_pt, tan_e, beta), single-precision values.
+MM01_DECK = [
+    dict(e=single(12000.0), nu=single(0.3), yld_pt=single(100.0), tan_e=single(1000.0),
+         beta=single(0.5)),
+    dict(e=single(24000.0), nu=single(0.3), yld_pt=single(200.0), tan_e=single(1000.0),
+         beta=single(0.5)),
+]
+
 # component order of 9-vectors: 11,12,13,21,22,23,31,32,33
 COMP = ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]
 

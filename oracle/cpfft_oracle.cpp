@@ -387,6 +387,11 @@ struct State {          // compact history (CPFFT_HIST_WORDS order)
   double D[6];
   double tt_rate;
   double eps[6];        // unrotated strain (rstgp1_update_strains, src/rstgp1.f:1378-1394)
+  // mm01 voxels (m01 set): the history vector (1-based as the reference's, [1..11]) and
+  // the extra stress-vector words cgn(7:9); tt, Rp, D and tt_rate are not used
+  bool m01;
+  double h01[12];
+  double cgx[3];
 };
 void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f:473-571)
   std::memset(&s, 0, sizeof(s));
@@ -394,6 +399,14 @@ void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f
   s.tt = cr.p.tau_y + 1.0e-5;                // mm10_init_voche (:2046-2056)
 }
 void state_pack(const State& s, double* h) {
+  if (s.m01) {  // words 6..16 history, 17..19 cgn(7:9), 20..22 zero
+    for (int i = 0; i < ORC_HIST; i++) h[i] = 0.0;
+    for (int i = 0; i < 6; i++) h[i] = s.sig[i];
+    for (int k = 1; k <= 11; k++) h[5 + k] = s.h01[k];
+    for (int k = 0; k < 3; k++) h[17 + k] = s.cgx[k];
+    for (int i = 0; i < 6; i++) h[23 + i] = s.eps[i];
+    return;
+  }
   for (int i = 0; i < 6; i++) h[i] = s.sig[i];
   h[6] = s.tt;
   for (int j = 0; j < 3; j++)
@@ -403,6 +416,14 @@ void state_pack(const State& s, double* h) {
   for (int i = 0; i < 6; i++) h[23 + i] = s.eps[i];
 }
 void state_unpack(const double* h, State& s) {
+  if (s.m01) {
+    for (int i = 0; i < 6; i++) s.sig[i] = h[i];
+    s.h01[0] = 0.0;
+    for (int k = 1; k <= 11; k++) s.h01[k] = h[5 + k];
+    for (int k = 0; k < 3; k++) s.cgx[k] = h[17 + k];
+    for (int i = 0; i < 6; i++) s.eps[i] = h[23 + i];
+    return;
+  }
   for (int i = 0; i < 6; i++) s.sig[i] = h[i];
   s.tt = h[6];
   for (int j = 0; j < 3; j++)
@@ -956,11 +977,16 @@ struct PointOut {
   int iters;
   bool ok;
 };
-void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int iter,
-                    const M3 Fn, const M3 Fn1, const State& n_in, State& np1, PointOut& o) {
-  State n = n_in;
-  if (step == 1) state_init(cr, n);  // mm10 re-initialises history at step 1 (:78-83)
-  M3 fnh, dfn, rnh, rn1, fnhinv, fn1inv;
+struct Kin {
+  M3 rnh, rn1, fnhinv;
+  double uddt[6];
+};
+void kinematics(const M3 Fn, const M3 Fn1, Kin& k) {
+  M3 fnh, dfn;
+  M3& rnh = k.rnh;
+  M3& rn1 = k.rn1;
+  M3& fnhinv = k.fnhinv;
+  double* uddt = k.uddt;
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) {
       fnh[i][j] = 0.5 * (Fn[i][j] + Fn1[i][j]);
@@ -986,16 +1012,34 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
   }
   M6 qnh;
   getrm1_opt1(rnh, qnh);
-  double uddt[6];
   for (int j = 0; j < 6; j++)  // qmply1 (src/qmply1.f:15-49)
     uddt[j] = qnh[j][0] * ddt[0] + qnh[j][1] * ddt[1] + qnh[j][2] * ddt[2] +
               qnh[j][3] * ddt[3] + qnh[j][4] * ddt[4] + qnh[j][5] * ddt[5];
+}
+
+void pull_back(const M3 Fn, const M3 Fn1, const Kin& k, const State& np1, PointOut& o);
+
+void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int iter,
+                    const M3 Fn, const M3 Fn1, const State& n_in, State& np1, PointOut& o) {
+  State n = n_in;
+  if (step == 1) state_init(cr, n);  // mm10 re-initialises history at step 1 (:78-83)
+  Kin k;
+  kinematics(Fn, Fn1, k);
   Mm10 mm{&cr.p, &vp, &n};
   int it = 0;
-  o.ok = mm.update(uddt, dt, rn1, iter == 0, np1, o.cep, &it);
+  o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);
+  np1.m01 = false;
   o.iters = it;
   // strains at n+1 = strains at n + uddt (src/drive_eps_sig.f:264-265)
-  for (int i = 0; i < 6; i++) np1.eps[i] = n.eps[i] + uddt[i];
+  for (int i = 0; i < 6; i++) np1.eps[i] = n.eps[i] + k.uddt[i];
+  pull_back(Fn, Fn1, k, np1, o);
+}
+
+void pull_back(const M3 Fn, const M3 Fn1, const Kin& k, const State& np1, PointOut& o) {
+  const M3& rnh = k.rnh;
+  const M3& rn1 = k.rn1;
+  const M3& fnhinv = k.fnhinv;
+  M3 fn1inv;
   for (int i = 0; i < 6; i++) o.sig[i] = np1.sig[i];
   // Cauchy stress T = R t R^T (getrm1 opt 2 + qmply1), P = J T F^-T (cs2p :1182-1224)
   M6 qt;
@@ -1019,6 +1063,173 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
             {np1.sig[3], np1.sig[1], np1.sig[4]},
             {np1.sig[5], np1.sig[4], np1.sig[2]}};
   cep2A(Fn, t33, o.cep, rnh, fnhinv, rn1, Fn1, fn1inv, detF, o.A);
+}
+
+// ---- mm01: bilinear Mises, mixed hardening (src/mm01.f) -------------------------------
+// One material point of the isothermal path, in the reference's own sequence and with
+// 1-based vectors: cgn/cgn1 are the 9-word stress vectors (6 stresses, energy density,
+// plastic work, equivalent plastic strain), history/history1 the 11-word history.
+struct MisesP {
+  double e, nu, beta, yld, h;  // setup_mm01_rknstr (src/drive_eps_sig.f:486-520)
+};
+MisesP mises_props(const cpfft_mises& p) {
+  return MisesP{p.e, p.nu, p.beta, p.yld_pt, p.tan_e * p.e / (p.e - p.tan_e)};
+}
+void mises_state_init(const MisesP& m, State& s) {  // mm01_set_history (src/mm01.f:240-310)
+  std::memset(&s, 0, sizeof(s));
+  s.m01 = true;
+  s.h01[2] = m.yld / 1.73205080756888;
+  s.h01[4] = 3.0;  // state: not yielding
+  s.h01[5] = m.h;
+}
+// mm01 + cnst1 for one point; deps = uddt.  Returns the 6x6 tangent in cep.
+void mm01_point(const MisesP& m, const double deps1[6], const State& n, State& np1,
+                double cep[6][6]) {
+  const double root2 = 1.414213562373095, root3 = 1.7320508075688;
+  double deps[7], cgn[10], cgn1[10], history[12], history1[12];
+  for (int i = 1; i <= 6; i++) deps[i] = deps1[i - 1];
+  for (int i = 1; i <= 6; i++) cgn[i] = n.sig[i - 1];
+  for (int i = 7; i <= 9; i++) cgn[i] = n.cgx[i - 7];
+  for (int i = 1; i <= 11; i++) history[i] = n.h01[i];
+  for (int i = 1; i <= 11; i++) history1[i] = 0.0;
+  const double ym = m.e, nu = m.nu;
+  // mm01_init (src/mm01.f:328-535)
+  double deps_vol = deps[1] + deps[2] + deps[3];
+  double eps_mean = deps_vol / 3.0;
+  double de[7];
+  for (int i = 1; i <= 3; i++) de[i] = deps[i] - eps_mean;
+  for (int i = 4; i <= 6; i++) de[i] = deps[i];
+  double g_n = ym / 2.0 / (1.0 + nu);
+  double een[7];
+  een[1] = (cgn[1] - nu * (cgn[2] + cgn[3])) / ym;
+  een[2] = (cgn[2] - nu * (cgn[1] + cgn[3])) / ym;
+  een[3] = (cgn[3] - nu * (cgn[1] + cgn[2])) / ym;
+  for (int i = 4; i <= 6; i++) een[i] = cgn[i] / g_n;
+  double eps_vol_n1 = een[1] + een[2] + een[3] + deps_vol;
+  double eps_mean_n = (een[1] + een[2] + een[3]) / 3.0;
+  double ev[7];
+  for (int i = 1; i <= 3; i++) ev[i] = (een[i] - eps_mean_n) + de[i];
+  for (int i = 4; i <= 6; i++) ev[i] = een[i] + de[i];
+  double shear_mod = ym / (2.0 * (1.0 + nu));
+  double devel[7], alpha_n[7], rtse[7];
+  for (int i = 1; i <= 3; i++) devel[i] = 2.0 * shear_mod * ev[i];
+  for (int i = 4; i <= 6; i++) devel[i] = shear_mod * ev[i];
+  for (int i = 1; i <= 6; i++) alpha_n[i] = history[5 + i];
+  double hbari_np1 = m.beta * m.h, hbark_np1 = (1.0 - m.beta) * m.h;
+  double hbark_n = (1.0 - m.beta) * history[5];
+  double kbar = (m.yld + hbari_np1 * history[3]) / root3;
+  double lk = 1.0;
+  if (std::fabs(hbark_n) > 0.000001) lk = hbark_np1 / hbark_n;
+  auto norm = [&](const double* r) {
+    return std::sqrt(r[1] * r[1] + r[2] * r[2] + r[3] * r[3] +
+                     2.0 * (r[4] * r[4] + r[5] * r[5] + r[6] * r[6]));
+  };
+  for (int i = 1; i <= 6; i++) rtse[i] = devel[i] - alpha_n[i] * lk;
+  double yf = norm(rtse) - root2 * kbar;
+  for (int i = 1; i <= 6; i++) rtse[i] = devel[i] - alpha_n[i];
+  double mrts = norm(rtse);
+  int instat = 3;
+  bool yield = false;
+  if (yf >= 0.0000001 * root2 * kbar) { yield = true; instat = 1; }
+  // mm01_simple1 (src/mm01.f:704-785) or the elastic branch of mm01 (:190-199)
+  double devstr[7];
+  if (yield) {
+    const double twthrd = 0.666666666666667, root23 = 0.816496580927;
+    double ldt = (mrts - root2 * kbar) / (twthrd * (3.0 * shear_mod + m.h));
+    double k_np1 = kbar + (root2 / 3.0) * hbari_np1 * ldt;
+    history1[1] = ldt;
+    history1[2] = k_np1;
+    history1[3] = history[3] + ldt * root23;
+    history1[5] = m.h;
+    double const1 = twthrd * hbark_np1 * ldt / mrts;
+    double const2 = root2 * k_np1 / mrts;
+    for (int i = 1; i <= 6; i++) history1[5 + i] = history[5 + i] + const1 * rtse[i];
+    for (int i = 1; i <= 6; i++) devstr[i] = history1[5 + i] + const2 * rtse[i];
+  } else {
+    history1[1] = 0.0;
+    history1[2] = kbar;
+    history1[3] = history[3];
+    history1[5] = m.h;
+    for (int i = 1; i <= 6; i++) history1[5 + i] = alpha_n[i] * lk;
+    for (int i = 1; i <= 6; i++) devstr[i] = rtse[i] + alpha_n[i];
+  }
+  // mm01_sig_final (src/mm01.f:626-690)
+  double sig_mean = eps_vol_n1 * (3.0 * ym * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)) +
+                                  2.0 * shear_mod) / 3.0;
+  for (int i = 1; i <= 3; i++) cgn1[i] = devstr[i] + sig_mean;
+  for (int i = 4; i <= 6; i++) cgn1[i] = devstr[i];
+  double w = 0.0;
+  for (int i = 1; i <= 6; i++) w += deps[i] * (cgn1[i] + cgn[i]);
+  cgn1[7] = cgn[7] + 0.5 * w;
+  history1[4] = instat;
+  // mm01_plastic_work (src/mm01.f:546-615)
+  cgn1[8] = cgn[8];
+  cgn1[9] = cgn[9];
+  if (yield) {
+    double dsig[7], dp[7];
+    for (int i = 1; i <= 6; i++) dsig[i] = cgn1[i] - cgn[i];
+    dp[1] = deps[1] - (dsig[1] - nu * (dsig[2] + dsig[3])) / ym;
+    dp[2] = deps[2] - (dsig[2] - nu * (dsig[1] + dsig[3])) / ym;
+    dp[3] = deps[3] - (dsig[3] - nu * (dsig[1] + dsig[2])) / ym;
+    for (int i = 4; i <= 6; i++) dp[i] = deps[i] - dsig[i] / shear_mod;
+    double wp = 0.0;
+    for (int i = 1; i <= 6; i++) wp += dp[i] * (cgn1[i] + cgn[i]);
+    cgn1[8] = cgn[8] + 0.5 * wp;
+    double f1 = std::pow(dp[1] - dp[2], 2) + std::pow(dp[2] - dp[3], 2) + std::pow(dp[1] - dp[3], 2);
+    double f2 = dp[4] * dp[4] + dp[5] * dp[5] + dp[6] * dp[6];
+    cgn1[9] = cgn[9] + (root2 / 3.0) * std::sqrt(f1 + 1.5 * f2);
+  }
+  // cnst1 (src/mm01.f:1222-1374), with the reference's 10-digit sqrt(2)
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) cep[a][b] = 0.0;
+  if (!yield) {
+    double c1 = ym / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    double c2 = (1.0 - nu) * c1, c3 = ((1.0 - 2.0 * nu) / 2.0) * c1, c4 = nu * c1;
+    for (int a = 0; a < 3; a++) {
+      for (int b = 0; b < 3; b++) cep[a][b] = a == b ? c2 : c4;
+      cep[a + 3][a + 3] = c3;
+    }
+  } else {
+    const double r2 = 1.414213562;
+    const double* r = rtse;
+    double g = ym / (2.0 * (1.0 + nu));
+    double l = (ym * nu) / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    double k = (3.0 * l + 2.0 * g) / 3.0;
+    double mrtsq = r[1] * r[1] + r[2] * r[2] + r[3] * r[3] + 2.0 * (r[4] * r[4] + r[5] * r[5] + r[6] * r[6]);
+    double bb = (r2 * history1[2] + (2.0 / 3.0) * (1.0 - m.beta) * history1[5] * history1[1]) /
+                std::sqrt(mrtsq);
+    double gamma = 1.0 / (1.0 + history1[5] / (3.0 * g));
+    double gambar = gamma - 1.0 + bb;
+    double gbar = g * bb;
+    double albar = k - 2.0 * gbar / 3.0;
+    double thbar = 2.0 * g * gambar;
+    for (int a = 1; a <= 6; a++)
+      for (int b = 1; b <= 6; b++) {
+        double t = -(thbar * r[a] * r[b] / mrtsq);
+        if (a <= 3 && b <= 3) t += albar;
+        if (a == b) t += (a <= 3) ? 2.0 * gbar : gbar;
+        cep[a - 1][b - 1] = t;
+      }
+  }
+  np1 = n;
+  np1.m01 = true;
+  for (int i = 1; i <= 6; i++) np1.sig[i - 1] = cgn1[i];
+  for (int i = 7; i <= 9; i++) np1.cgx[i - 7] = cgn1[i];
+  np1.h01[0] = 0.0;
+  for (int i = 1; i <= 11; i++) np1.h01[i] = history1[i];
+}
+
+void mises_point(const MisesP& m, int step, const M3 Fn, const M3 Fn1, const State& n_in,
+                 State& np1, PointOut& o) {
+  State n = n_in;
+  if (step == 1) mises_state_init(m, n);  // mm01 calls mm01_set_history at step 1 (:160)
+  Kin k;
+  kinematics(Fn, Fn1, k);
+  mm01_point(m, k.uddt, n, np1, o.cep);
+  for (int i = 0; i < 6; i++) np1.eps[i] = n.eps[i] + k.uddt[i];
+  o.ok = true;
+  o.iters = 0;
+  pull_back(Fn, Fn1, k, np1, o);
 }
 
 // ---- FFT (restated DFTI role: exact complex DFT) --------------------------------------
@@ -1104,7 +1315,9 @@ struct orc_ctx {
   double dt;
   int gmap, nthreads;
   std::vector<Crys> crys;
-  std::vector<int> mat;            // 0-based crystal per voxel
+  std::vector<int> kind;           // per material: 0 crystal, 1 mm01, 2 not yet defined
+  std::vector<MisesP> mp;          // per material (mm01)
+  std::vector<int> mat;            // 0-based material per voxel
   std::vector<VoxProps> vprops;
   std::vector<State> hn, hn1;
   std::vector<double> Fn, Fn1, Pn, Pn1, K4, b, dFm;
@@ -1143,18 +1356,28 @@ orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
   c->gmap = g_mapping;
   c->nthreads = nthreads > 0 ? nthreads : 1;
   c->crys.resize(ncrystals);
-  for (int i = 0; i < ncrystals; i++) crystal_finalize(props[i], c->crys[i]);
+  c->kind.assign(ncrystals, 0);
+  c->mp.resize(ncrystals);
+  for (int i = 0; i < ncrystals; i++) {
+    if (props[i].slip_type == CPFFT_NOT_A_CRYSTAL) { c->kind[i] = 2; continue; }
+    crystal_finalize(props[i], c->crys[i]);
+  }
   long N3 = c->N3;
   c->mat.resize(N3);
   c->vprops.resize(N3);
   for (long v = 0; v < N3; v++) {
     c->mat[v] = matList[v] - 1;
+    if (c->kind[c->mat[v]] != 0) continue;
     double ang[3] = {kocks_deg[v], kocks_deg[N3 + v], kocks_deg[2 * N3 + v]};
     voxel_props(c->crys[c->mat[v]], ang, c->vprops[v]);
   }
   c->hn.resize(N3);
   c->hn1.resize(N3);
-  for (long v = 0; v < N3; v++) { state_init(c->crys[c->mat[v]], c->hn[v]); c->hn1[v] = c->hn[v]; }
+  for (long v = 0; v < N3; v++) {
+    if (c->kind[c->mat[v]] == 0) state_init(c->crys[c->mat[v]], c->hn[v]);
+    else std::memset(&c->hn[v], 0, sizeof(State));
+    c->hn1[v] = c->hn[v];
+  }
   c->Fn.assign(9 * N3, 0.0);
   for (int d : {0, 4, 8})
     for (long v = 0; v < N3; v++) c->Fn[d * N3 + v] = 1.0;
@@ -1207,6 +1430,31 @@ static void load33(const double* f, long N3, long v, M3 m) {
     for (int j = 0; j < 3; j++) m[i][j] = f[(3 * i + j) * N3 + v];
 }
 
+// the material point of voxel v with its material's model
+static void voxel_point(orc_ctx* c, long v, int step, int iter, const M3 fn, const M3 fn1,
+                        PointOut& o) {
+  const int m = c->mat[v];
+  if (c->kind[m] == 0) {
+    material_point(c->crys[m], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v], c->hn1[v], o);
+  } else if (c->kind[m] == 1) {
+    mises_point(c->mp[m], step, fn, fn1, c->hn[v], c->hn1[v], o);
+  } else {  // undefined material
+    std::memset(&o, 0, sizeof(o));
+    o.ok = false;
+  }
+}
+
+void orc_set_mises(orc_ctx* c, int material, const cpfft_mises* props) {
+  const int m = material - 1;
+  c->kind[m] = 1;
+  c->mp[m] = mises_props(*props);
+  for (long v = 0; v < c->N3; v++)
+    if (c->mat[v] == m) {
+      mises_state_init(c->mp[m], c->hn[v]);
+      c->hn1[v] = c->hn[v];
+    }
+}
+
 int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn, const double* Fn1,
                       double* Pn1, double* K4, long long* local_iters) {
   long N3 = c->N3;
@@ -1220,8 +1468,7 @@ int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn, const do
     load33(c->Fn.data(), N3, v, fn);
     load33(c->Fn1.data(), N3, v, fn1);
     PointOut o;
-    material_point(c->crys[c->mat[v]], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v],
-                   c->hn1[v], o);
+    voxel_point(c, v, step, iter, fn, fn1, o);
     if (!o.ok) fails++;
     its += o.iters;
     for (int i = 0; i < 9; i++) c->Pn1[i * N3 + v] = o.P[i];
@@ -1243,8 +1490,7 @@ int orc_stress_sample(orc_ctx* c, int step, int iter, long v0, long v1) {
     load33(c->Fn.data(), N3, v, fn);
     load33(c->Fn1.data(), N3, v, fn1);
     PointOut o;
-    material_point(c->crys[c->mat[v]], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v],
-                   c->hn1[v], o);
+    voxel_point(c, v, step, iter, fn, fn1, o);
     if (!o.ok) fails++;
     for (int i = 0; i < 9; i++) c->Pn1[i * N3 + v] = o.P[i];
     for (int m = 0; m < 81; m++) c->K4[m * N3 + v] = o.A[m];
@@ -1533,6 +1779,8 @@ void orc_set_history_n(orc_ctx* c, const double* hist_n) {
   double h[ORC_HIST];
   for (long v = 0; v < N3; v++) {
     for (int w = 0; w < ORC_HIST; w++) h[w] = hist_n[w * N3 + v];
+    std::memset(&c->hn[v], 0, sizeof(State));
+    c->hn[v].m01 = c->kind[c->mat[v]] == 1;
     state_unpack(h, c->hn[v]);
   }
 }
@@ -1546,6 +1794,8 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3], doub
   VoxProps vp;
   voxel_props(cr, kocks_deg, vp);
   State n, np1;
+  std::memset(&n, 0, sizeof(n));
+  std::memset(&np1, 0, sizeof(np1));
   if (hist_n) state_unpack(hist_n, n);
   else state_init(cr, n);
   M3 fn, fn1;
@@ -1559,6 +1809,28 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3], doub
   if (out_sig6) for (int i = 0; i < 6; i++) out_sig6[i] = o.sig[i];
   if (out_cep36) for (int a = 0; a < 6; a++) for (int b = 0; b < 6; b++) out_cep36[a * 6 + b] = o.cep[a][b];
   return o.ok ? o.iters : -1;
+}
+
+int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9], const double Fn1[9],
+                     const double* hist_n, double* hist_np1, double P[9], double A[81],
+                     double out_sig6[6], double out_cep36[36]) {
+  const MisesP m = mises_props(*props);
+  State n, np1;
+  std::memset(&n, 0, sizeof(n));
+  n.m01 = true;
+  if (hist_n) state_unpack(hist_n, n);
+  else mises_state_init(m, n);
+  M3 fn, fn1;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { fn[i][j] = Fn[3 * i + j]; fn1[i][j] = Fn1[3 * i + j]; }
+  PointOut o;
+  mises_point(m, step, fn, fn1, n, np1, o);
+  if (hist_np1) state_pack(np1, hist_np1);
+  if (P) for (int i = 0; i < 9; i++) P[i] = o.P[i];
+  if (A) for (int i = 0; i < 81; i++) A[i] = o.A[i];
+  if (out_sig6) for (int i = 0; i < 6; i++) out_sig6[i] = o.sig[i];
+  if (out_cep36) for (int a = 0; a < 6; a++) for (int b = 0; b < 6; b++) out_cep36[a * 6 + b] = o.cep[a][b];
+  return 0;
 }
 
 void orc_polar(const double F[9], double R[9]) {

@@ -25,6 +25,10 @@ orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
                     int g_mapping, int nthreads);
 void     orc_destroy(orc_ctx* c);
 
+/* make a material declared with slip_type CPFFT_NOT_A_CRYSTAL an mm01 bilinear Mises
+ * material (resets its voxels' state) */
+void orc_set_mises(orc_ctx* c, int material, const cpfft_mises* props);
+
 /* drive_eps_sig on every voxel; Fn/Fn1 NULL -> use the context's fields.
  * Pn1/K4 NULL -> keep in the context.  Returns number of local failures. */
 int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn,
@@ -66,6 +70,11 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3],
                      const double Fn1[9], const double* hist_n, double* hist_np1,
                      double P[9], double A[81], double out_sig6[6],
                      double out_cep36[36]);
+/* The same for an mm01 voxel (kinematics + mm01 + cnst1 + cep2A); hist_n NULL or
+ * step 1: mm01_set_history's state. */
+int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9],
+                     const double Fn1[9], const double* hist_n, double* hist_np1,
+                     double P[9], double A[81], double out_sig6[6], double out_cep36[36]);
 /* polar decomposition F = R U (rtcmp1), F and R row-major 3x3 */
 void orc_polar(const double F[9], double R[9]);
 /* crystal stiffness in the sample frame (row-major 6x6) and slip tensors (12x6) */

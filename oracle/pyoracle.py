@@ -40,6 +40,17 @@ class Crystal(ctypes.Structure):
     ]
 
 
+class Mises(ctypes.Structure):
+    """cpfft_mises of include/cpfft_gpu.h."""
+
+    _fields_ = [("e", ctypes.c_double), ("nu", ctypes.c_double), ("yld_pt", ctypes.c_double),
+                ("tan_e", ctypes.c_double), ("beta", ctypes.c_double)]
+
+
+def _mises(m):
+    return Mises(m["e"], m["nu"], m["yld_pt"], m["tan_e"], m.get("beta", 1.0))
+
+
 class Stats(ctypes.Structure):
     """Mirror of ``cpfft_stats``."""
 
@@ -102,6 +113,9 @@ def lib():
         L.orc_voxel_update.restype = i
         L.orc_voxel_update.argtypes = [P(Crystal), dp, d, i, i, dp, dp, dp, dp, dp, dp,
                                        dp, dp]
+        L.orc_set_mises.argtypes = [vp, i, P(Mises)]
+        L.orc_mises_update.restype = i
+        L.orc_mises_update.argtypes = [P(Mises), i, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_polar.argtypes = [dp, dp]
         L.orc_crystal_setup.argtypes = [P(Crystal), dp, dp, dp, dp]
         L.orc_fft3.argtypes = [i, dp, dp, i]
@@ -209,6 +223,27 @@ class Oracle:
 
     def set_history_n(self, hn):
         lib().orc_set_history_n(self.h, _p(np.ascontiguousarray(hn)))
+
+    def set_mises(self, material, props):
+        """props: dict e, nu, yld_pt, tan_e, beta (a bilinear Mises material, mm01)."""
+        m = _mises(props)
+        lib().orc_set_mises(self.h, int(material), ctypes.byref(m))
+
+
+def mises_update(props, step, Fn, Fn1, hist_n=None):
+    """One mm01 material point (kinematics + mm01 + cnst1 + cep2A); F 3x3 row-major."""
+    m = _mises(props)
+    P = np.zeros(9)
+    A = np.zeros(81)
+    sig = np.zeros(6)
+    cep = np.zeros(36)
+    h1 = np.zeros(HIST_WORDS)
+    fn = np.ascontiguousarray(Fn, dtype=np.float64).reshape(9)
+    fn1 = np.ascontiguousarray(Fn1, dtype=np.float64).reshape(9)
+    hn = None if hist_n is None else np.ascontiguousarray(hist_n, dtype=np.float64)
+    lib().orc_mises_update(ctypes.byref(m), step, _p(fn), _p(fn1), _p(hn), _p(h1), _p(P),
+                           _p(A), _p(sig), _p(cep))
+    return dict(P=P, A=A.reshape(9, 9), sig=sig, cep=cep.reshape(6, 6), hist=h1)
 
 
 def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
