@@ -14,7 +14,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
-HIST_WORDS = 29
+HIST_WORDS = 31
 NOT_A_CRYSTAL = 0  # slip_type of a material defined by Solver.set_mises
 
 G_REF_SHIFT, G_CENTERED = 0, 1
@@ -54,6 +54,14 @@ class Crystal(ctypes.Structure):
         ("atol", ctypes.c_double), ("atol1", ctypes.c_double),
         ("rtol", ctypes.c_double), ("rtol1", ctypes.c_double),
         ("miter", ctypes.c_int), ("exact_j22", ctypes.c_int),
+        ("tau_a", ctypes.c_double),
+        ("tau_hat_y", ctypes.c_double), ("G_0_y", ctypes.c_double),
+        ("p_y", ctypes.c_double), ("q_y", ctypes.c_double),
+        ("tau_hat_v", ctypes.c_double), ("G_0_v", ctypes.c_double),
+        ("p_v", ctypes.c_double), ("q_v", ctypes.c_double),
+        ("eps_dot_0_v", ctypes.c_double),
+        ("burgers", ctypes.c_double), ("boltzman", ctypes.c_double),
+        ("mu_0", ctypes.c_double), ("D_0", ctypes.c_double), ("T_0", ctypes.c_double),
     ]
 
 

@@ -242,11 +242,27 @@ CrysRec crystal_record(const cpfft_crystal& p) {
   c.theta_0 = p.theta_0;
   c.voce_m = p.voce_m;
   c.gamma_bar = p.gamma_bar;
-  c.iD_v = p.iD_v;
+  c.iD_v = p.h_type == 2 ? 0.0 : p.iD_v;  // MTS has no diffusion slip term (src/mm10_b.f:1191-1197)
   c.atol = p.atol;
   c.atol1 = p.atol1;
   c.rtol = p.rtol;
   c.rtol1 = p.rtol1;
+  c.tau_a = p.tau_a;
+  c.tau_hat_y = p.tau_hat_y;
+  c.G_0_y = p.G_0_y;
+  c.p_y = p.p_y;
+  c.q_y = p.q_y;
+  c.tau_hat_v = p.tau_hat_v;
+  c.G_0_v = p.G_0_v;
+  c.p_v = p.p_v;
+  c.q_v = p.q_v;
+  c.eps_dot_0_v = p.eps_dot_0_v;
+  c.burgers = p.burgers;
+  c.boltzman = p.boltzman;
+  c.mu_0 = p.mu_0;
+  c.D_0 = p.D_0;
+  c.T_0 = p.T_0;
+  c.h_type = p.h_type;
   c.miter = p.miter;
   c.alter_mode = p.alter_mode;
   c.exact_j22 = p.exact_j22;
@@ -263,6 +279,7 @@ struct Ctx {
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
   int nslip = 12;  // slip systems of the grid's crystals (12 fcc, 48 bcc48)
+  int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts)
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
   // voxel work queue of the implicit stress passes (cpfft_set_schedule)
   int sched = CPFFT_SCHED_BLOCKS;
@@ -1013,7 +1030,8 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
   if (c->n_crys_vox)
-    CK(c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+    CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
+                      : c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
   if (c->n_mises_vox) CK(launch_mises(a, c->st));
   TRY(kt_stop(c));
   c->pass_step = step;
@@ -1202,24 +1220,32 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   std::vector<CrysRec> cr(ncrystals);
   std::vector<std::vector<double>> C0(ncrystals, std::vector<double>(36));
   double bb[48][3], nn[48][3];
-  int nslip = 0;
+  int nslip = 0, h_type = 0;
   int first_crystal = -1;
   for (int k = 0; k < ncrystals; k++) {
     const cpfft_crystal& p = props[k];
     if (p.slip_type == CPFFT_NOT_A_CRYSTAL) continue;  // defined by cpfft_set_mises
     if (first_crystal < 0) first_crystal = k;
     const int ns = slip_geometry(p.slip_type, bb, nn);
-    if (!ns || p.h_type != 1 || !(p.tau_v != 0) || !(p.harden_n > 0) ||
+    // Voce needs tau_v != 0; MTS (fcc only) positive thermal-barrier parameters
+    const bool voce_ok = p.h_type == 1 && p.tau_v != 0;
+    const bool mts_ok = p.h_type == 2 && ns == 12 && p.mu_0 > 0 && p.burgers > 0 &&
+                        p.boltzman > 0 && p.G_0_y > 0 && p.G_0_v > 0 && p.p_y > 0 &&
+                        p.q_y > 0 && p.p_v > 0 && p.q_v > 0 && p.gamma_bar > 0 &&
+                        p.eps_dot_0_v > 0;
+    if (!ns || !(voce_ok || mts_ok) || !(p.harden_n > 0) ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
-      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip, voce hardening, "
-                      "valid elasticity)", k + 1);
+      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip with voce hardening, "
+                      "fcc with mts hardening, valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
-    if (nslip && ns != nslip) {
-      cpfft_set_error("cpfft_init: the crystals of one grid must share the slip type");
+    if ((nslip && ns != nslip) || (h_type && p.h_type != h_type)) {
+      cpfft_set_error("cpfft_init: the crystals of one grid must share the slip type and the "
+                      "hardening law");
       return CPFFT_ERR_BAD_ARG;
     }
     nslip = ns;
+    h_type = p.h_type;
     cr[k] = crystal_record(p);
   }
   if (first_crystal >= 0) slip_geometry(props[first_crystal].slip_type, bb, nn);
@@ -1262,6 +1288,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     }
   Ctx* c = new Ctx;
   c->nslip = nslip;
+  c->h_type = h_type;
   c->mat = mat;
   c->mat_kind.assign(ncrystals, 0);
   for (int k = 0; k < ncrystals; k++)
@@ -1334,7 +1361,13 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   std::vector<double> h(H_WORDS * N3, 0.0);
   for (long long v = 0; v < N3; v++) {
     if (props[mat[v]].slip_type == CPFFT_NOT_A_CRYSTAL) continue;
-    h[H_TT * N3 + v] = props[crys[v]].tau_y + 1.0e-5;
+    if (props[crys[v]].h_type == 2) {  // mm10_init_mts: flags, set by the first update
+      h[H_TT * N3 + v] = -1.0;
+      h[H_U * N3 + v] = -1.0;
+      h[(H_U + 1) * N3 + v] = -1.0;
+    } else {
+      h[H_TT * N3 + v] = props[crys[v]].tau_y + 1.0e-5;
+    }
     for (int d : {0, 4, 8}) h[(H_RP + d) * N3 + v] = 1.0;
   }
   cudaError_t e;

@@ -41,6 +41,10 @@ struct OriRec {
 struct CrysRec {
   double rate_n, tau_y, tau_v, inv_tau_v, theta_0, voce_m, gamma_bar, iD_v;
   double atol, atol1, rtol, rtol1;
+  // MTS (h_type 2)
+  double tau_a, tau_hat_y, G_0_y, p_y, q_y, tau_hat_v, G_0_v, p_v, q_v, eps_dot_0_v;
+  double burgers, boltzman, mu_0, D_0, T_0;
+  int h_type;
   int miter, alter_mode, exact_j22;
   int n_int;       // rate_n - 1 when rate_n is integer-valued in [2, 64], else -1
   int m_is_one;    // voce_m == 1
@@ -61,10 +65,11 @@ enum {
   H_D = 16,       // 6  unrotated strain increment of the step
   H_TTR = 22,     // 1  tau_tilde rate
   H_EPS = 23,     // 6  unrotated strain (sum of the step increments, rstgp1_update_strains)
-  H_WORDS = 29
+  H_U = 29,       // 2  MTS: tau_y and mu of the step (mm10's u(1:2)); -1 = not yet set
+  H_WORDS = 31
 };
 
-// The same 29 words for an mm01 voxel: H_SIG and H_EPS as above, and in words 6..19 the
+// The same words for an mm01 voxel: H_SIG and H_EPS as above, and in words 6..19 the
 // mm01 history vector (mm01_set_history, src/mm01.f:240-310) followed by the three extra
 // stress-vector words of oupestr's cgn(7:9) (src/mm01.f:95-100)
 enum {
@@ -132,6 +137,8 @@ struct StressArgs {
 // serves crystals with 12 slip systems (FCC), launch_stress48 those with 48 (BCC48).
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
+// MTS-hardened FCC crystals (stress_mts.cu)
+cudaError_t launch_stress_mts(const StressArgs& a, bool warm, cudaStream_t s);
 // the mm01 voxels (a.mises[v] >= 0) of the grid; the crystal launches skip them
 cudaError_t launch_mises(const StressArgs& a, cudaStream_t s);
 // Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost

@@ -19,11 +19,20 @@
 #define CPFFT_NSLIP 12
 #define CPFFT_STRESS_LAUNCH launch_stress
 #endif
+// Hardening law: Voce (1) here; stress_mts.cu compiles this file again with CPFFT_LAW 2
+// (MTS).  The kernels that serve every grid (mm01, the voxel queue) live in the first unit.
+#ifndef CPFFT_LAW
+#define CPFFT_LAW 1
+#endif
+#define CPFFT_FIRST_UNIT (CPFFT_NSLIP == 12 && CPFFT_LAW == 1)
 #include "mlp.cuh"
 
 namespace {
 
 constexpr int NS = CPFFT_NSLIP;  // slip systems
+constexpr bool MTS = CPFFT_LAW == 2;
+// the temperature of the reference's FFT path (drive_10_update, src/rstgp1.f:832)
+constexpr double TEMP = 297.0;
 
 __device__ __forceinline__ double sgn1(double x) { return x < 0.0 ? -1.0 : 1.0; }
 
@@ -226,6 +235,9 @@ struct Crystal {
   double ms[NS][6];
   double qc[NS][3];
   double Cms[NS][6];  // C ms_i, constant while ms is (the reference forms it per call)
+  // MTS: shear modulus and thresholds of this (sub)step, the n-state values of the history's
+  // u words (nu1, nu2 < 0: first step), and the temperature of the (sub)step
+  double mu, tau_y, tau_v, ntau_y, nmu, nu1, nu2, temp;
 };
 
 __device__ __forceinline__ double Cv(const double* C, int a, int b) { return __ldg(C + 6 * a + b); }
@@ -236,7 +248,7 @@ __device__ void setup_np1(Crystal& s, const OriRec* rec, const double* D, double
                           const double* R, const double* nRp) {
   for (int i = 0; i < 6; i++) s.D[i] = D[i];
   s.tinc = tinc;
-  if (s.cr->alter_mode) {
+  if (s.cr->alter_mode && !MTS) {  // mm10_setup_voche only (src/mm10_a.f:2073)
     s.dg = s.cr->gamma_bar * tinc;
   } else {
     double t1 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
@@ -286,6 +298,37 @@ __device__ __forceinline__ void slips(const Crystal& s, const double* st, double
   }
 }
 
+// mm10_setup_mts (src/mm10_a.f:2109-2166): mu(T), the thermal thresholds from the
+// continuum rate dg / tinc, and tau_y, mu at n (the history's u, or this step's values)
+__device__ void mts_setup(Crystal& s, double T) {
+  const CrysRec& c = *s.cr;
+  s.temp = T;
+  s.mu = T == 0.0 ? c.mu_0 : c.mu_0 - c.D_0 / (exp(c.T_0 / T) - 1.0);
+  const double dgc = s.dg / s.tinc;
+  if (dgc == 0.0) {
+    s.tau_v = c.tau_hat_v;
+    s.tau_y = c.tau_hat_y;
+  } else {
+    const double b3 = pow(c.burgers, 3.0);
+    s.tau_v = c.tau_hat_v * pow(1.0 - pow(c.boltzman * T / (s.mu * b3 * c.G_0_v) *
+                                              log(c.eps_dot_0_v / dgc), 1.0 / c.q_v), 1.0 / c.p_v);
+    s.tau_y = c.tau_hat_y * pow(1.0 - pow(c.boltzman * T / (s.mu * b3 * c.G_0_y) *
+                                              log(c.gamma_bar / dgc), 1.0 / c.q_y), 1.0 / c.p_y);
+  }
+  s.ntau_y = s.nu1 < 0.0 ? s.tau_y : s.nu1;
+  s.nmu = s.nu2 < 0.0 ? s.mu : s.nu2;
+}
+
+// MTS's (ct + tau_l / cta)^m with tau_l = 0, cta = (mu_0/mu)(tt - tau_a) - tau_y
+// (mm10_h_mts, src/mm10_b.f:2093-2100); 0/cta keeps the reference's NaN at cta = 0
+__device__ __forceinline__ double mts_cta(const Crystal& s, double tt) {
+  const CrysRec& c = *s.cr;
+  return (c.mu_0 / s.mu) * tt - (c.mu_0 / s.mu) * c.tau_a - s.tau_y;
+}
+__device__ __forceinline__ double mts_base(const Crystal& s, double cta) {
+  return 1.0 - cta / s.tau_v + 0.0 / cta;
+}
+
 __device__ __forceinline__ double hterm(const CrysRec& c, double tt) {
   // tau_l = 0 (the lattice-curvature gradients are zeroed by the reference)
   double h = 1.0 - (tt - c.tau_y) * c.inv_tau_v;
@@ -323,11 +366,18 @@ __device__ double formR(const Crystal& s, const double* x, double* R, double* rs
   const CrysRec& c = *s.cr;
   slips(s, x, x[6], rs, si, pw);
   formR1(s, x, rs, si, R);
-  double ht = hterm(c, x[6]);
-  double hp = hpow(c, ht) * sgn1(ht);
   double h = 0.0;
-  for (int i = 0; i < NS; i++) h += hp * fabs(si[i]);
-  h = s.ntt + c.theta_0 * h;
+  if constexpr (MTS) {  // mm10_h_mts (src/mm10_b.f:2080-2108)
+    const double hp = pow(mts_base(s, mts_cta(s, x[6])), c.voce_m);
+    for (int i = 0; i < NS; i++) h += hp * fabs(si[i]);
+    h = c.tau_a * (1.0 - s.mu / s.nmu) + (s.mu / c.mu_0) * (s.tau_y - s.ntau_y) +
+        (s.mu / s.nmu) * s.ntt + c.theta_0 * (s.mu / c.mu_0) * h;
+  } else {
+    double ht = hterm(c, x[6]);
+    double hp = hpow(c, ht) * sgn1(ht);
+    for (int i = 0; i < NS; i++) h += hp * fabs(si[i]);
+    h = s.ntt + c.theta_0 * h;
+  }
   R[6] = x[6] - h;
   return (h - s.ntt) / s.tinc;
 }
@@ -378,6 +428,29 @@ __device__ void formJ(const Crystal& s, const double* x, const double* rs, const
   double itt = 1.0 / tt;
   double J12[6] = {0, 0, 0, 0, 0, 0}, et[6] = {0, 0, 0, 0, 0, 0};
   formJ11<7, true>(s, x, tt, rs, si, pw, J, J12, itt);
+  if constexpr (MTS) {
+    // mm10_estress_mts / mm10_ehard_mts (src/mm10_b.f:2110-2187)
+    const double cta = mts_cta(s, tt);
+    const double b = mts_base(s, cta);
+    const double bm = pow(b, c.voce_m);
+    const double ur = s.mu / c.mu_0;
+    double sum = 0.0;
+    for (int i = 0; i < NS; i++) {
+      double r2 = c.n_int >= 0 ? (rs[i] < 0.0 ? -pw[i] : (rs[i] > 0.0 ? pw[i] : 0.0))
+                               : pow(fabs(rs[i]), c.rate_n - 2.0) * rs[i];
+      for (int a = 0; a < 6; a++) et[a] += bm * r2 * s.ms[i][a];
+      sum += (c.voce_m * (1.0 / s.tau_v + 0.0 / (cta * cta)) * pow(b, -1.0) +
+              ur * c.rate_n / tt) * bm * fabs(si[i]);
+    }
+    const double fac = c.theta_0 * ur * c.rate_n * s.dg /
+                       (c.n_int >= 0 ? ipow(tt, c.n_int + 1) : pow(tt, c.rate_n));
+    for (int a = 0; a < 6; a++) {
+      J[7 * a + 6] = J12[a];
+      J[7 * 6 + a] = -(fac * et[a]);
+    }
+    J[48] = 1.0 + c.theta_0 * sum;
+    return;
+  }
   double ht = hterm(c, tt);
   double hp = hpow(c, ht);
   double sh = sgn1(ht);
@@ -400,6 +473,59 @@ __device__ void formJ(const Crystal& s, const double* x, const double* rs, const
     J[7 * 6 + a] = -(fac * et[a]);
   }
   J[48] = 1.0 - c.theta_0 * etau;
+}
+
+// mm10_tangent's JA and JB for MTS (src/mm10_a.f:658-815 with mm10_ed_mts and
+// mm10_dgdd_mts, src/mm10_b.f:2189-2378) at the converged (sigma, tau) of the full step:
+// JR -= JA + JB, JA = sum_i (C ms_i + 2 symtq) (x) dgamma_i/dD, JB = J12 (x) ed / J22.
+// The reference passes the whole symtqmat where a column is meant, so every system's JA
+// term takes system 1's column (mm10_a_mult_type_4 reads its first six words).
+__device__ void mts_tangent_rhs(const Crystal& s, const double* st, double tt, const double* J,
+                                double* JR) {
+  const CrysRec& c = *s.cr;
+  double rs[NS], si[NS], pw[NS];
+  slips(s, st, tt, rs, si, pw);
+  const double dm[6] = {s.D[0], s.D[1], s.D[2], 0.5 * s.D[3], 0.5 * s.D[4], 0.5 * s.D[5]};
+  const double alpha = 2.0 / (3.0 * s.dg * s.dg);
+  double sq1[6];
+  symsw(st, s.qc[0], sq1);
+  // JA: sum_i wv_i (x) (alpha si_i d_mod)
+  for (int i = 0; i < NS; i++) {
+    double wv[6];
+    for (int a = 0; a < 6; a++) wv[a] = s.Cms[i][a] + 2.0 * sq1[a];
+    const double g = alpha * si[i];
+    for (int a = 0; a < 6; a++)
+      for (int b = 0; b < 6; b++) JR[6 * a + b] -= wv[a] * (g * dm[b]);
+  }
+  // ed (mm10_ed_mts)
+  const double dgc = s.dg / s.tinc;
+  const double b3 = pow(c.burgers, 3.0);
+  const double lny = log(c.gamma_bar / dgc);
+  const double ty = c.boltzman * s.temp / (s.mu * b3 * c.G_0_y) * lny;
+  const double fy = 2.0 * c.tau_hat_y / (3.0 * s.dg * s.dg * c.q_y * c.p_y * lny) *
+                    pow(1.0 - pow(ty, 1.0 / c.q_y), 1.0 / c.p_y - 1.0) * pow(ty, 1.0 / c.q_y);
+  const double lnv = log(c.eps_dot_0_v / dgc);
+  const double tv = c.boltzman * s.temp / (s.mu * b3 * c.G_0_v) * lnv;
+  const double fv = 2.0 * c.tau_hat_v / (3.0 * s.dg * s.dg * c.q_v * c.p_v * lnv) *
+                    pow(1.0 - pow(tv, 1.0 / c.q_v), 1.0 / c.p_v - 1.0) * pow(tv, 1.0 / c.q_v);
+  const double mnp0 = s.mu / c.mu_0;
+  const double sc = tt / mnp0 - c.tau_a / mnp0 - s.tau_y;
+  const double base = 1.0 - sc / s.tau_v + 0.0 / sc;
+  const double bm1 = pow(base, c.voce_m - 1.0), bm = pow(base, c.voce_m);
+  double ky = 0.0, kv = 0.0, kd = 0.0;
+  for (int i = 0; i < NS; i++) {
+    const double asi = fabs(si[i]);
+    ky += c.voce_m * (1.0 / s.tau_v + 0.0 / (sc * sc)) * bm1 * asi;
+    kv += c.voce_m / (s.tau_v * s.tau_v) * sc * bm1 * asi;
+    kd += 2.0 / (3.0 * s.dg * s.dg) * bm * asi;
+  }
+  double ed[6];
+  for (int b = 0; b < 6; b++)
+    ed[b] = c.theta_0 * mnp0 * (ky * fy * dm[b] + kv * fv * dm[b] + kd * dm[b]) + mnp0 * fy * dm[b];
+  // JB = J12 (J22^-1 ed)
+  const double i22 = 1.0 / J[48];
+  for (int a = 0; a < 6; a++)
+    for (int b = 0; b < 6; b++) JR[6 * a + b] -= J[7 * a + 6] * (ed[b] * i22);
 }
 
 __device__ __forceinline__ bool anynan(const double* x, int n) {
@@ -822,7 +948,7 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
   }
 }
 
-#if CPFFT_NSLIP == 12
+#if CPFFT_FIRST_UNIT
 // ---- the voxel work queue: voxels sorted by the cost of their previous pass -----------
 constexpr int QBINS = 64;  // costs 0 .. 62 and >= 63 (iterations of the local solve)
 
@@ -895,14 +1021,19 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   }
   const OriRec* rec = a.oris + __ldg(a.ori + v);
   const CrysRec* cr = a.cryss + __ldg(a.crys + v);
-  // history at n (step 1 re-initialises it, src/mm10_a.f:78-83 and :473-571)
-  double nsig[6], ntt, nttr, nRp[9], nD[6];
+  // history at n (step 1 re-initialises it, src/mm10_a.f:78-83 and :473-571; MTS:
+  // mm10_init_mts's -1 flags, src/mm10_a.f:2090-2107)
+  double nsig[6], ntt, nttr, nRp[9], nD[6], nu1 = -1.0, nu2 = -1.0;
   if (a.step == 1) {
     for (int i = 0; i < 6; i++) { nsig[i] = 0.0; nD[i] = 0.0; }
-    ntt = cr->tau_y + 1.0e-5;
+    ntt = MTS ? -1.0 : cr->tau_y + 1.0e-5;
     nttr = 0.0;
     for (int i = 0; i < 9; i++) nRp[i] = (i % 4 == 0) ? 1.0 : 0.0;
   } else {
+    if constexpr (MTS) {
+      nu1 = a.hist_n[H_U * N3 + v];
+      nu2 = a.hist_n[(H_U + 1) * N3 + v];
+    }
     for (int i = 0; i < 6; i++) nsig[i] = a.hist_n[(H_SIG + i) * N3 + v];
     ntt = a.hist_n[H_TT * N3 + v];
     // stored column-major; keep row-major locally
@@ -918,10 +1049,16 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
   s.cr = cr;
   s.C = rec->C;
   s.nsig = nsig;
-  s.ntt = ntt;
   s.nttr = nttr;
+  s.nu1 = nu1;
+  s.nu2 = nu2;
   for (int i = 0; i < 6; i++) s.nD[i] = nD[i];
   setup_np1(s, rec, uddt, a.dt, rn1, nRp);
+  if constexpr (MTS) {  // the full step's setup sets tau_tilde at n on the first step
+    mts_setup(s, TEMP);
+    if (ntt < 0.0) ntt = cr->tau_a + (s.mu / cr->mu_0) * s.tau_y + 0.1;
+  }
+  s.ntt = ntt;
   double stress[6], tt = ntt, ttrate = 0.0;
   for (int i = 0; i < 6; i++) stress[i] = nsig[i];
   double t1 = 0, t2 = 0;
@@ -1011,13 +1148,16 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
       // the sub-step state differs from np1 only in D, tinc and dg
       s.tinc = a.dt * (stp + frac);
       for (int i = 0; i < 6; i++) s.D[i] = Dw[i];
-      if (cr->alter_mode) {
+      if (cr->alter_mode && !MTS) {
         s.dg = cr->gamma_bar * s.tinc;
       } else {
         double q1 = Dw[0] * Dw[0] + Dw[1] * Dw[1] + Dw[2] * Dw[2];
         double q2 = Dw[3] * Dw[3] + Dw[4] * Dw[4] + Dw[5] * Dw[5];
         s.dg = sqrt((2.0 / 3.0) * (q1 + 0.5 * q2));
       }
+      // the sub-step's temperature: n's is zero, so it scales with the sub-step
+      // (mm10_solve_strup_iterate, src/mm10_a.f:2769)
+      if constexpr (MTS) mts_setup(s, TEMP * (stp + frac));
       tt = ntt;
       double tr_sub = 0.0;
       fail = !solve(s, a.dt * stp, stress, tt, Jl, haveJ, iters, piters, tr_sub);
@@ -1037,13 +1177,14 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     // restore the full-step np1 (used by the rotation update below)
     s.tinc = a.dt;
     for (int i = 0; i < 6; i++) s.D[i] = uddt[i];
-    if (cr->alter_mode) {
+    if (cr->alter_mode && !MTS) {
       s.dg = cr->gamma_bar * a.dt;
     } else {
       double q1 = uddt[0] * uddt[0] + uddt[1] * uddt[1] + uddt[2] * uddt[2];
       double q2 = uddt[3] * uddt[3] + uddt[4] * uddt[4] + uddt[5] * uddt[5];
       s.dg = sqrt((2.0 / 3.0) * (q1 + 0.5 * q2));
     }
+    if constexpr (MTS) mts_setup(s, TEMP);
     ok = !(fail || isnan(tt) || anynan(stress, 6));
     if (ok) {
       // mm10_tangent for Voce (JA = JB = 0): T = (J11 - J12 J21 / J22)^-1 C, symmetrised
@@ -1067,10 +1208,14 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
           for (int j = k + 1; j < 6; j++) JJ[6 * i + j] -= l * JJ[6 * k + j];
         }
       }
+      // right-hand side C - JA - JB (JA = JB = 0 for Voce)
+      double JR[36];
+      for (int i = 0; i < 36; i++) JR[i] = __ldg(rec->C + i);
+      if constexpr (MTS) mts_tangent_rhs(s, stress, tt, Jl, JR);
       double T[36];
       for (int c = 0; c < 6; c++) {
         double b[6];
-        for (int i = 0; i < 6; i++) b[i] = __ldg(rec->C + 6 * i + c);
+        for (int i = 0; i < 6; i++) b[i] = JR[6 * i + c];
         for (int k = 0; k < 6; k++)
           if (piv[k] != k) { double t = b[k]; b[k] = b[piv[k]]; b[piv[k]] = t; }
         for (int i = 1; i < 6; i++)
@@ -1142,6 +1287,8 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
     for (int j = 0; j < 3; j++) a.hist_np1[(H_RP + 3 * j + i) * N3 + v] = Rp[3 * i + j];
   for (int i = 0; i < 6; i++) a.hist_np1[(H_D + i) * N3 + v] = uddt[i];
   a.hist_np1[H_TTR * N3 + v] = ttrate;
+  a.hist_np1[H_U * N3 + v] = MTS ? s.tau_y : 0.0;  // mm10_setup_mts's u(1:2)
+  a.hist_np1[(H_U + 1) * N3 + v] = MTS ? s.mu : 0.0;
   // strains at n+1 = strains at n + the unrotated increment (rstgp1_update_strains,
   // src/drive_eps_sig.f:264-265, src/rstgp1.f:1378-1394); zero at n for step 1
   for (int i = 0; i < 6; i++)
@@ -1223,14 +1370,14 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
     }
 }
 
-#if CPFFT_NSLIP == 12
+#if CPFFT_FIRST_UNIT
 // ---- mm01: rate-independent Mises plasticity, bilinear uniaxial curve, mixed isotropic /
 // kinematic hardening (src/mm01.f), one voxel ---------------------------------------------
 // The isothermal update: mm01_init (:328-535), mm01_simple1 (:704-785), mm01_sig_final
 // (:626-690), mm01_plastic_work (:546-615), and the consistent tangent cnst1
 // (:1222-1374); the reference's decimal constants are kept as it writes them.  Inputs:
-// deps = uddt (engineering shear), the 29 history words at n (step 1: the state of
-// mm01_set_history, :240-310, with zero stresses).  Outputs: the 29 words at n+1 except
+// deps = uddt (engineering shear), the H_WORDS history words at n (step 1: the state of
+// mm01_set_history, :240-310, with zero stresses).  Outputs: those words at n+1 except
 // H_EPS, and the 6x6 tangent (row-major).
 __device__ void mises_update(const MisesRec& m, int step, const double* hn, const double* deps,
                              double* hn1, double* cep) {
@@ -1378,6 +1525,7 @@ __device__ void mises_update(const MisesRec& m, int step, const double* hn, cons
   hn1[M1_WP] = cgn1[7];
   hn1[M1_EBP] = cgn1[8];
   for (int w = M1_EBP + 1; w < H_EPS; w++) hn1[w] = 0.0;
+  for (int w = H_U; w < H_WORDS; w++) hn1[w] = 0.0;
 }
 
 __global__ void __launch_bounds__(128) mises_kernel(StressArgs a) {
@@ -1405,7 +1553,7 @@ __global__ void __launch_bounds__(128) mises_kernel(StressArgs a) {
 
 }  // namespace
 
-#if CPFFT_NSLIP == 12
+#if CPFFT_FIRST_UNIT
 cudaError_t launch_mises(const StressArgs& a, cudaStream_t s) {
   if (a.N3 <= 0 || !a.mises) return cudaSuccess;
   const unsigned blocks = (unsigned)std::min<long long>((a.N3 + 127) / 128, 152LL * 16);
@@ -1448,7 +1596,7 @@ cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm, cudaStream_t s) 
   return cudaGetLastError();
 }
 
-#if CPFFT_NSLIP == 12
+#if CPFFT_FIRST_UNIT
 cudaError_t launch_voxel_queue(const unsigned char* cost, long long N3, unsigned int* scratch,
                                int* perm, unsigned int* queue, cudaStream_t s) {
   unsigned int* hist = scratch;

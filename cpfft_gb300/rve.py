@@ -11,6 +11,14 @@ from dataclasses import dataclass
 
 import numpy as np
 
+# MTS parameters (h_type 2) at the reference's crystal defaults (initialize_new_crystal,
+# src/mod_crystals.f:257-276); Voce crystals carry them unread.
+MTS_DEFAULTS = dict(
+    tau_a=0.0, tau_hat_y=-1.0, G_0_y=-1.0, p_y=0.5, q_y=2.0, tau_hat_v=-1.0, G_0_v=-1.0,
+    p_v=0.5, q_v=2.0, eps_dot_0_v=1.0e10, burgers=2.87e-7, boltzman=1.3806e-20,
+    mu_0=69000.0 / 2.0 / 1.33, D_0=0.0, T_0=294.0,
+)
+
 # Material of the named workloads (MPa, s): FCC {111}<110>, anisotropic type-3
 # elasticity C11=C33=168.4, C12=C13=121.4, C44=C55=75.4 GPa, Voce hardening.
 FCC_VOCE = dict(
@@ -19,7 +27,7 @@ FCC_VOCE = dict(
     h_type=1, harden_n=20.0, tau_y=50.0, tau_v=100.0, theta_0=400.0, voce_m=1.0,
     gamma_bar=1.0e-3, iD_v=0.0, alter_mode=1,
     atol=1.0e-10, atol1=1.0e-10, rtol=1.0e-10, rtol1=1.0e-10, miter=30,
-    exact_j22=1,
+    exact_j22=1, **MTS_DEFAULTS,
 )
 
 # The reference's example deck's crystal (examples/test_mm10.in): BCC with 48 slip
@@ -31,7 +39,7 @@ BCC48_DECK = dict(
     h_type=1, harden_n=5.48, tau_y=205.0, tau_v=5000.0, theta_0=0.01, voce_m=1.0,
     gamma_bar=4.0e-5, iD_v=0.0, alter_mode=1,
     atol=1.0e-10, atol1=1.0e-10, rtol=1.0e-10, rtol1=1.0e-10, miter=30,
-    exact_j22=0,
+    exact_j22=0, **MTS_DEFAULTS,
 )
 
 # The material entry of a non-crystal material: not read by the crystal path (the
@@ -53,6 +61,15 @@ MM01_DECK = [
     dict(e=single(24000.0), nu=single(0.3), yld_pt=single(200.0), tan_e=single(1000.0),
          beta=single(0.5)),
 ]
+
+# An FCC crystal with MTS hardening (h_type 2): the workloads' elasticity, thermally
+# activated thresholds tau_y(rate, T) and tau_v(rate, T) (MPa, mm, mJ/K), rate exponent 20.
+MTS_FCC = dict(
+    FCC_VOCE, h_type=2, harden_n=20.0, theta_0=2000.0, voce_m=1.0, alter_mode=0,
+    tau_a=20.0, tau_hat_y=200.0, G_0_y=0.5, p_y=0.5, q_y=2.0,
+    tau_hat_v=300.0, G_0_v=0.5, p_v=0.5, q_v=2.0, eps_dot_0_v=1.0e7, gamma_bar=1.0e7,
+    burgers=2.5e-7, boltzman=1.3806e-20, mu_0=75400.0, D_0=0.0, T_0=294.0,
+)
 
 # component order of 9-vectors: 11,12,13,21,22,23,31,32,33
 COMP = ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]

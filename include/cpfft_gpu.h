@@ -64,7 +64,8 @@ typedef struct cpfft_crystal {
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;
-    int    h_type;         /* 1 = voce (only value accepted)                              */
+    int    h_type;         /* 1 = voce, 2 = mts (fcc crystals); the crystals of one grid
+                              share the hardening law                                       */
     double harden_n;       /* rate exponent                                               */
     double tau_y, tau_v, theta_0, voce_m;
     double gamma_bar;      /* eps_dot_0_y                                                 */
@@ -76,6 +77,16 @@ typedef struct cpfft_crystal {
                               which carries an extra sign(1,slip increment) factor and so
                               converges only linearly once slip reverses on any system;
                               1: the exact derivative (no such factor). Not a deck keyword. */
+    /* MTS hardening (h_type 2: mm10_h_mts .. mm10_dgdd_mts, src/mm10_b.f:2080-2380; setup
+       and initial state mm10_setup_mts / mm10_init_mts, src/mm10_a.f:2090-2173), at the
+       297 K of the reference's FFT path (src/rstgp1.f:832).  Not read by Voce.           */
+    double tau_a;                       /* athermal slip resistance                       */
+    double tau_hat_y, G_0_y, p_y, q_y;  /* thermal barrier of the yield part              */
+    double tau_hat_v, G_0_v, p_v, q_v;  /* thermal barrier of the saturation part         */
+    double eps_dot_0_v;                 /* reference rate of the saturation part (the yield
+                                           part's is gamma_bar, eps_dot_0_y)               */
+    double burgers, boltzman;
+    double mu_0, D_0, T_0;              /* mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1)       */
 } cpfft_crystal;
 
 /* slip_type of a material that is not a crystal: its cpfft_crystal entry is not read, and
@@ -328,7 +339,8 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
 
 /* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
  * compact history at n (N3, CPFFT_HIST_WORDS) used by the result writers. */
-#define CPFFT_HIST_WORDS 29   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6) */
+#define CPFFT_HIST_WORDS 31   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6)
+                                 u(2): MTS tau_y and mu at the step's end (mm10's u(1:2)) */
 int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history);
 
 /* ---- element result files (ouelestr, src/ouresult.f:140-300) --------------------------

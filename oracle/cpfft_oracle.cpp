@@ -392,11 +392,16 @@ struct State {          // compact history (CPFFT_HIST_WORDS order)
   bool m01;
   double h01[12];
   double cgx[3];
+  double u[2];          // MTS: tau_y and mu of the step (mm10's u(1:2)); -1 = not yet set
 };
 void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f:473-571)
   std::memset(&s, 0, sizeof(s));
   for (int i = 0; i < 3; i++) s.Rp[i][i] = 1.0;
   s.tt = cr.p.tau_y + 1.0e-5;                // mm10_init_voche (:2046-2056)
+  if (cr.p.h_type == 2) {                    // mm10_init_mts (:2090-2107): flags
+    s.tt = -1.0;
+    s.u[0] = s.u[1] = -1.0;
+  }
 }
 void state_pack(const State& s, double* h) {
   if (s.m01) {  // words 6..16 history, 17..19 cgn(7:9), 20..22 zero
@@ -414,6 +419,8 @@ void state_pack(const State& s, double* h) {
   for (int i = 0; i < 6; i++) h[16 + i] = s.D[i];
   h[22] = s.tt_rate;
   for (int i = 0; i < 6; i++) h[23 + i] = s.eps[i];
+  h[29] = s.u[0];
+  h[30] = s.u[1];
 }
 void state_unpack(const double* h, State& s) {
   if (s.m01) {
@@ -431,6 +438,8 @@ void state_unpack(const double* h, State& s) {
   for (int i = 0; i < 6; i++) s.D[i] = h[16 + i];
   s.tt_rate = h[22];
   for (int i = 0; i < 6; i++) s.eps[i] = h[23 + i];
+  s.u[0] = h[29];
+  s.u[1] = h[30];
 }
 
 // the np1 / curr "crystal_state" pieces the Voce routines read
@@ -439,7 +448,25 @@ struct Np1 {
   double tinc, dg;
   double ms[48][6], qs[48][3], qc[48][3];
   double tt_rate;
+  double temp, mu, tau_y, tau_v, ntau_y, nmu;  // MTS
 };
+
+// mm10_setup_mts's shear modulus and thresholds (src/mm10_a.f:2109-2150) at rate dgc, T
+void mts_thresholds(const cpfft_crystal& p, double dgc, double T, double& mu, double& tau_v,
+                    double& tau_y) {
+  if (T == 0.0) mu = p.mu_0;
+  else mu = p.mu_0 - p.D_0 / (std::exp(p.T_0 / T) - 1.0);
+  if (dgc == 0.0) {
+    tau_v = p.tau_hat_v;
+    tau_y = p.tau_hat_y;
+  } else {
+    tau_v = p.tau_hat_v * std::pow(1.0 - std::pow(p.boltzman * T / (mu * std::pow(p.burgers, 3.0) *
+                                   p.G_0_v) * std::log(p.eps_dot_0_v / dgc), 1.0 / p.q_v), 1.0 / p.p_v);
+    tau_y = p.tau_hat_y * std::pow(1.0 - std::pow(p.boltzman * T / (mu * std::pow(p.burgers, 3.0) *
+                                   p.G_0_y) * std::log(p.gamma_bar / dgc), 1.0 / p.q_y), 1.0 / p.p_y);
+  }
+}
+const double TEMP = 297.0;  // gp_temps of drive_10_update (src/rstgp1.f:832)
 
 struct Mm10 {
   const cpfft_crystal* p;
@@ -447,7 +474,9 @@ struct Mm10 {
   const State* n;
 
   // mm10_setup (src/mm10_a.f:830-975) + mm10_setup_voche (:2058-2080)
-  void setup(Np1& s, const double D[6], double tinc, const M3 R) const {
+  bool mts() const { return p->h_type == 2; }
+  double iDv() const { return mts() ? 0.0 : p->iD_v; }  // MTS has no diffusion term
+  void setup(Np1& s, const double D[6], double tinc, const M3 R, double T = TEMP) const {
     for (int i = 0; i < 6; i++) s.D[i] = D[i];
     s.tinc = tinc;
     double t1 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
@@ -467,8 +496,14 @@ struct Mm10 {
         s.qc[i][a] = RWC[a][0] * vp->qs[i][0] + RWC[a][1] * vp->qs[i][1] + RWC[a][2] * vp->qs[i][2];
       }
     }
-    if (p->alter_mode) s.dg = p->gamma_bar * s.tinc;
+    if (p->alter_mode && !mts()) s.dg = p->gamma_bar * s.tinc;  // mm10_setup_voche only
     s.tt_rate = 0.0;
+    s.temp = T;
+    if (mts()) {  // mm10_setup_mts: n's tau_y and mu from the history's u, else this step's
+      mts_thresholds(*p, s.dg / s.tinc, T, s.mu, s.tau_v, s.tau_y);
+      s.ntau_y = n->u[0] < 0.0 ? s.tau_y : n->u[0];
+      s.nmu = n->u[1] < 0.0 ? s.mu : n->u[1];
+    }
   }
   double rs(const Np1& s, const double* st, int i) const {  // mm10_rs (src/mm10_b.f:1831)
     return st[0] * s.ms[i][0] + st[1] * s.ms[i][1] + st[2] * s.ms[i][2] +
@@ -496,7 +531,7 @@ struct Mm10 {
       double si = slipinc(s, st, tt, i);
       for (int a = 0; a < 3; a++) w[a] = w[a] + si * s.qc[i][a];
       double r = rs(s, st, i);
-      for (int a = 0; a < 3; a++) w[a] = w[a] + r * s.tinc * p->iD_v * s.qc[i][a];
+      for (int a = 0; a < 3; a++) w[a] = w[a] + r * s.tinc * iDv() * s.qc[i][a];
     }
   }
   // mm10_formR1 (src/mm10_b.f:1061-1101)
@@ -505,7 +540,7 @@ struct Mm10 {
     for (int i = 0; i < vp->ns; i++) {  // mm10_form_dbarp voce (:1161-1190)
       double si = slipinc(s, st, tt, i);
       double r = rs(s, st, i);
-      double f = r * s.tinc * p->iD_v + si;
+      double f = r * s.tinc * iDv() + si;
       for (int a = 0; a < 6; a++) dbar[a] = dbar[a] + f * s.ms[i][a];
     }
     double w[3], sw[6], wv1[6], wv2[6];
@@ -525,10 +560,20 @@ struct Mm10 {
     }
     return n->tt + p->theta_0 * h;
   }
+  // mm10_h_mts (src/mm10_b.f:2080-2108), tau_l = 0
+  double h_mts(const Np1& s, const double* st, double tt) const {
+    double cta = (p->mu_0 / s.mu) * tt - (p->mu_0 / s.mu) * p->tau_a - s.tau_y;
+    double ct = 1.0 - cta / s.tau_v;
+    double h = 0.0;
+    for (int i = 0; i < vp->ns; i++)
+      h = h + std::pow(ct + 0.0 / cta, p->voce_m) * std::fabs(slipinc(s, st, tt, i));
+    return p->tau_a * (1.0 - s.mu / s.nmu) + (s.mu / p->mu_0) * (s.tau_y - s.ntau_y) +
+           (s.mu / s.nmu) * n->tt + p->theta_0 * (s.mu / p->mu_0) * h;
+  }
   // mm10_formR (src/mm10_b.f:1029-1047) with mm10_formR2 (:63-113)
   void formR(Np1& s, const double* x, double R[7]) const {
     formR1(s, x, x[6], R);
-    double h = h_voce(s, x, x[6]);
+    double h = mts() ? h_mts(s, x, x[6]) : h_voce(s, x, x[6]);
     R[6] = x[6] - h;
     s.tt_rate = (h - n->tt) / s.tinc;
   }
@@ -541,7 +586,7 @@ struct Mm10 {
       double r = rs(s, st, i);
       double dgdt = std::pow(std::fabs(r), p->harden_n - 1.0);
       dgdt = s.dg * p->harden_n / std::pow(tt, p->harden_n) * dgdt;
-      dgdt = dgdt + s.tinc * p->iD_v;
+      dgdt = dgdt + s.tinc * iDv();
       double wv[6];
       for (int a = 0; a < 6; a++) wv[a] = 2.0 * sq[i][a];
       for (int j = 0; j < 6; j++)
@@ -583,6 +628,34 @@ struct Mm10 {
         for (int a = 0; a < 6; a++) tm[a] = tm[a] + vp->C[a][j] * s.ms[i][j];
       for (int a = 0; a < 6; a++) J12[a] += tm[a] * dgdtt;
     }
+    if (mts()) {  // mm10_estress_mts / mm10_ehard_mts (:2110-2187)
+      double cta = (p->mu_0 / s.mu) * tt - (p->mu_0 / s.mu) * p->tau_a - s.tau_y;
+      double ct = 1.0 - cta / s.tau_v;
+      double et[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = 0; i < vp->ns; i++) {
+        double r = rs(s, st, i);
+        double f = std::pow(ct + 0.0 / cta, p->voce_m) * std::pow(std::fabs(r), p->harden_n - 2.0) * r;
+        for (int a = 0; a < 6; a++) et[a] = et[a] + f * s.ms[i][a];
+      }
+      for (int a = 0; a < 6; a++)
+        et[a] = p->theta_0 * (s.mu / p->mu_0) * et[a] * p->harden_n * s.dg / std::pow(tt, p->harden_n);
+      double ur = s.mu / p->mu_0, etau = 0.0;
+      for (int i = 0; i < vp->ns; i++) {
+        double si = slipinc(s, st, tt, i);
+        etau = etau + (p->voce_m * (1.0 / s.tau_v + 0.0 / (cta * cta)) *
+                       std::pow(ct + 0.0 / cta, -1.0) + ur * p->harden_n / tt) *
+                      std::pow(ct + 0.0 / cta, p->voce_m) * std::fabs(si);
+      }
+      etau = -p->theta_0 * etau;
+      etau = 1.0 - etau;
+      for (int a = 0; a < 6; a++) {
+        for (int c = 0; c < 6; c++) J[a][c] = J11[a][c];
+        J[a][6] = J12[a];
+        J[6][a] = -et[a];
+      }
+      J[6][6] = etau;
+      return;
+    }
     double et[6] = {0, 0, 0, 0, 0, 0};  // mm10_estress_voche (:1914-1940)
     for (int i = 0; i < vp->ns; i++) {
       double r = rs(s, st, i);
@@ -610,6 +683,60 @@ struct Mm10 {
       J[6][a] = -(fac * et[a]);
     }
     J[6][6] = etau;
+  }
+
+  // mm10_tangent's JA + JB for MTS (src/mm10_a.f:711-800; mm10_ed_mts, mm10_dgdd_mts,
+  // src/mm10_b.f:2189-2378), subtracted from JR = C.  mm10_a_mult_type_4 is handed the
+  // whole symtqmat array, so every system's term reads system 1's column.
+  void mts_tangent_rhs(const Np1& s, const double* st, double tt, const double J[7][7],
+                       double* JR) const {
+    double d_mod[6] = {s.D[0], s.D[1], s.D[2], 0.5 * s.D[3], 0.5 * s.D[4], 0.5 * s.D[5]};
+    double symtq1[6];
+    symsw(st, s.qc[0], symtq1);
+    double alpha = 2.0 / (3.0 * s.dg * s.dg);
+    double JA[6][6];
+    std::memset(JA, 0, sizeof(JA));
+    for (int i = 0; i < vp->ns; i++) {
+      double dgam = slipinc(s, st, tt, i);
+      double work[6];
+      for (int a = 0; a < 6; a++) {
+        work[a] = 2.0 * symtq1[a];
+        for (int j = 0; j < 6; j++) work[a] = work[a] + vp->C[a][j] * s.ms[i][j];
+      }
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) JA[a][b] = JA[a][b] + work[a] * (alpha * dgam * d_mod[b]);
+    }
+    // mm10_ed_mts
+    double dgc = s.dg / s.tinc;
+    double lny = std::log(p->gamma_bar / dgc);
+    double ty = p->boltzman * s.temp / (s.mu * std::pow(p->burgers, 3.0) * p->G_0_y) * lny;
+    double dydd[6], dvdd[6];
+    double fy = 2.0 * p->tau_hat_y / (3.0 * s.dg * s.dg * p->q_y * p->p_y * lny) *
+                std::pow(1.0 - std::pow(ty, 1.0 / p->q_y), 1.0 / p->p_y - 1.0) *
+                std::pow(ty, 1.0 / p->q_y);
+    double lnv = std::log(p->eps_dot_0_v / dgc);
+    double tv = p->boltzman * s.temp / (s.mu * std::pow(p->burgers, 3.0) * p->G_0_v) * lnv;
+    double fv = 2.0 * p->tau_hat_v / (3.0 * s.dg * s.dg * p->q_v * p->p_v * lnv) *
+                std::pow(1.0 - std::pow(tv, 1.0 / p->q_v), 1.0 / p->p_v - 1.0) *
+                std::pow(tv, 1.0 / p->q_v);
+    for (int a = 0; a < 6; a++) { dydd[a] = fy * d_mod[a]; dvdd[a] = fv * d_mod[a]; }
+    double mnp0 = s.mu / p->mu_0;
+    double sc = tt / mnp0 - p->tau_a / mnp0 - s.tau_y;
+    double ed[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < vp->ns; i++) {
+      double asi = std::fabs(slipinc(s, st, tt, i));
+      double base = 1.0 - sc / s.tau_v + 0.0 / sc;
+      for (int a = 0; a < 6; a++)
+        ed[a] = ed[a] + (p->voce_m * (1.0 / s.tau_v + 0.0 / (sc * sc)) *
+                             std::pow(base, p->voce_m - 1.0) * dydd[a] +
+                         p->voce_m / (s.tau_v * s.tau_v) * sc * std::pow(base, p->voce_m - 1.0) * dvdd[a] +
+                         2.0 / (3.0 * s.dg * s.dg) * std::pow(base, p->voce_m) * d_mod[a]) * asi;
+    }
+    for (int a = 0; a < 6; a++) ed[a] = p->theta_0 * mnp0 * ed[a] + mnp0 * dydd[a];
+    // JB = J12 (J22^-1 ed)
+    for (int a = 0; a < 6; a++)
+      for (int b = 0; b < 6; b++)
+        JR[a * 6 + b] = JR[a * 6 + b] - JA[a][b] - J[a][6] * (ed[b] / J[6][6]);
   }
 
   struct Result {
@@ -766,6 +893,8 @@ struct Mm10 {
               double cep[6][6], int* local_iters) const {
     Np1 np1;
     setup(np1, D, dt, R);
+    out.u[0] = mts() ? np1.tau_y : 0.0;  // the history's u(1:2) (mm10_setup_mts)
+    out.u[1] = mts() ? np1.mu : 0.0;
     double stress[6], ostress[6], tt = n->tt, ott = n->tt;
     for (int i = 0; i < 6; i++) stress[i] = ostress[i] = n->sig[i];
     double temp1 = 0, temp2 = 0;
@@ -794,7 +923,8 @@ struct Mm10 {
       while (frac < 1.0) {
         double Dw[6];
         for (int i = 0; i < 6; i++) Dw[i] = np1.D[i] * (step + frac);
-        setup(curr, Dw, np1.tinc * (step + frac), R);
+        // n's temperature is zero: the sub-step's scales with it (:2769)
+        setup(curr, Dw, np1.tinc * (step + frac), R, TEMP * (step + frac));
         tt = n->tt;
         fail = !solve(curr, np1.tinc * step, stress, tt, res);
         if (fail) {
@@ -847,6 +977,7 @@ struct Mm10 {
           JJ[a * 6 + b] = res.J[a][b] - res.J[a][6] * beta;
           JR[a * 6 + b] = vp->C[a][b];
         }
+      if (mts()) mts_tangent_rhs(np1, out.sig, out.tt, res.J, JR);
       lu_solve(6, JJ, 6, JR);
       for (int a = 0; a < 6; a++)  // mm10_a_make_symm_1
         for (int b = 0; b < 6; b++) cep[a][b] = (JR[a * 6 + b] + JR[b * 6 + a]) * 0.5;
@@ -1025,6 +1156,15 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
   if (step == 1) state_init(cr, n);  // mm10 re-initialises history at step 1 (:78-83)
   Kin k;
   kinematics(Fn, Fn1, k);
+  if (cr.p.h_type == 2 && n.tt < 0.0) {
+    // mm10_setup_mts with the full step sets tau_tilde at n on the first step (:2167-2171)
+    const double* d = k.uddt;
+    double dg = std::sqrt((2.0 / 3.0) * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2] +
+                                         0.5 * (d[3] * d[3] + d[4] * d[4] + d[5] * d[5])));
+    double mu, tv, ty;
+    mts_thresholds(cr.p, dg / dt, TEMP, mu, tv, ty);
+    n.tt = cr.p.tau_a + (mu / cr.p.mu_0) * ty + 0.1;
+  }
   Mm10 mm{&cr.p, &vp, &n};
   int it = 0;
   o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);

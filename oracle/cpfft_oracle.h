@@ -18,7 +18,7 @@ extern "C" {
 typedef struct orc_ctx orc_ctx;
 
 /* Per-voxel compact state, same words and order as CPFFT_HIST_WORDS. */
-#define ORC_HIST 29
+#define ORC_HIST 31
 
 orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
                     const cpfft_crystal* props, int ncrystals, double tstep,
