@@ -109,6 +109,7 @@ class Rve(ctypes.Structure):
         ("steps_done", ctypes.c_int), ("voxel_updates", ctypes.c_longlong),
         ("cg_iters", ctypes.c_longlong), ("seconds", ctypes.c_double),
         ("error", ctypes.c_char * 160),
+        ("mises", ctypes.POINTER(Mises)),
     ]
 
 
@@ -425,9 +426,10 @@ def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE
                 schedule=SCHED_QUEUE, tolNR=1e-5, tolPCG=1e-10, maxIter=20, nthreads=4,
                 want_fields=False):
     """Solve many RVEs at once (cpfft_batch_solve).  rves: dicts with N, mat_list, kocks,
-    crystals, tstep, g_mapping and a loading (rve.Loading: BC_all, isNBC, nsteps used).
-    Returns one dict per RVE: Pbar (nsteps, 9), status, voxel_updates, cg_iters, seconds,
-    and (want_fields) F, P (9, N3)."""
+    crystals, tstep, g_mapping and a loading (rve.Loading: BC_all, isNBC, nsteps used), and
+    optionally mises: {material (1-based): dict(e, nu, yld_pt, tan_e, beta)} for materials
+    declared NOT_A_CRYSTAL.  Returns one dict per RVE: Pbar (nsteps, 9), status,
+    voxel_updates, cg_iters, seconds, and (want_fields) F, P (9, N3)."""
     L = load_library()
     arr = (Rve * len(rves))()
     keep, out = [], []
@@ -451,6 +453,12 @@ def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE
         r.props = ctypes.cast(cr, ctypes.POINTER(Crystal))
         r.isNBC = nb.ctypes.data_as(_IP)
         r.Fn1, r.Pn1 = _dp(F), _dp(P)
+        if d.get("mises"):
+            ms = (Mises * len(d["crystals"]))()
+            for m, p in d["mises"].items():
+                ms[m - 1] = Mises(p["e"], p["nu"], p["yld_pt"], p["tan_e"], p.get("beta", 1.0))
+            keep.append(ms)
+            r.mises = ctypes.cast(ms, ctypes.POINTER(Mises))
         out.append({"Pbar": pb, "F": F, "P": P})
     rc = L.cpfft_batch_solve(arr, len(rves), precision, options, precond, schedule, tolNR,
                              tolPCG, maxIter, nthreads)

@@ -1903,6 +1903,8 @@ static void batch_one(cpfft_rve& r, int precision, int options, int precond, int
     snprintf(r.error, sizeof(r.error), "%s", cpfft_last_error());
   };
   int rc = cpfft_init(r.N, r.matList, r.kocks_deg, r.props, r.ncrystals, r.tstep, r.g_mapping);
+  for (int m = 0; rc >= 0 && r.mises && m < r.ncrystals; m++)
+    if (r.props[m].slip_type == CPFFT_NOT_A_CRYSTAL) rc = cpfft_set_mises(m + 1, &r.mises[m]);
   if (rc < 0) { fail(rc); r.seconds = std::chrono::duration<double>(clk::now() - t0).count(); return; }
   if ((rc = cpfft_set_mode(precision, options)) < 0 ||
       (precision == CPFFT_PREC_MIXED && (rc = cpfft_set_precond(precond)) < 0) ||

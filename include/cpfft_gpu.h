@@ -329,6 +329,10 @@ typedef struct cpfft_rve {
     long long cg_iters;
     double seconds;               /* host wall time of this RVE                            */
     char error[160];              /* cpfft_last_error() of the failing call                */
+    /* in, optional */
+    const cpfft_mises* mises;     /* (ncrystals) or NULL: entry m defines material m+1 as a
+                                     bilinear Mises material when props[m].slip_type is
+                                     CPFFT_NOT_A_CRYSTAL (cpfft_set_mises)                 */
 } cpfft_rve;
 
 /* precision / options / precond / schedule as cpfft_set_mode, cpfft_set_precond and

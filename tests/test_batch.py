@@ -25,6 +25,8 @@ def solo(gpulib, d, precision, options, precond, schedule):
     s = gpulib.Solver(d["N"], d["mat_list"], d["kocks"], d["crystals"], 1.0, d["g_mapping"],
                       precision)
     try:
+        for m, p in (d.get("mises") or {}).items():
+            s.set_mises(m, **p)
         s.set_mode(precision, options)
         if precision == gpulib.PREC_MIXED:
             s.set_precond(precond)
@@ -68,3 +70,28 @@ def test_batch_reports_errors(gpulib):
     d[0]["crystals"] = [dict(d[0]["crystals"][0], slip_type=2)]  # not FCC: cpfft_init refuses
     with pytest.raises(gpulib.CpfftError):
         gpulib.batch_solve(d, precision=gpulib.PREC_FP64, nthreads=1)
+
+
+def test_batch_other_material_models(gpulib):
+    """A batch mixing an MTS-hardened grid and a grid of bilinear Mises (mm01) materials
+    with a crystal: each equals its solo solve."""
+    batch = []
+    r = rve.make_rve(9, 4, 47, rve.MTS_FCC)
+    load = rve.uniaxial_tension(0.02, 20)
+    batch.append(dict(N=9, mat_list=r.mat_list, kocks=r.kocks, crystals=r.crystals, tstep=1.0,
+                      g_mapping=gpulib.G_REF_SHIFT, BC_all=load.BC_all, isNBC=load.isNBC,
+                      nsteps=2))
+    r = rve.make_rve(8, 3, 48)
+    mat = np.random.default_rng(48).integers(1, 4, 8 ** 3).astype(np.int32)
+    batch.append(dict(N=8, mat_list=mat, kocks=r.kocks,
+                      crystals=[r.crystals[0], rve.NOT_A_CRYSTAL, rve.NOT_A_CRYSTAL], tstep=1.0,
+                      g_mapping=gpulib.G_CENTERED, BC_all=load.BC_all, isNBC=load.isNBC,
+                      nsteps=2, mises={2: rve.MM01_DECK[0], 3: rve.MM01_DECK[1]}))
+    res = gpulib.batch_solve(batch, precision=gpulib.PREC_FP64, tolNR=1e-6, nthreads=2,
+                             want_fields=True)
+    for d, r in zip(batch, res):
+        assert r["status"] >= 0 and r["steps_done"] == 2, r["error"]
+        pb, F, P = solo(gpulib, d, gpulib.PREC_FP64, 0, gpulib.PRECOND_REFERENCE,
+                        gpulib.SCHED_QUEUE)
+        assert np.array_equal(r["Pbar"], pb), (d["N"], np.abs(r["Pbar"] - pb).max())
+        assert np.array_equal(r["P"], P), d["N"]
