@@ -192,7 +192,7 @@ def test_green_fp32_warp_path(gpulib, N):
         s.close()
 
 
-@pytest.mark.parametrize("N", [32, 64])
+@pytest.mark.parametrize("N", [32, 64, 128])
 def test_precond_cg_warp_path(gpulib, N):
     """Reference-medium preconditioned mixed CG on the warp-FFT sizes: the solution of the
     plain FP64 CG (itself checked against the oracle above) to the CG tolerance, the
