@@ -752,16 +752,6 @@ int cg_pre_body(Ctx* c, bool use_handle, bool timed) {
   g.pre = 1;
   int np = 0;
   CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
-  if (!timed && green_cg_fused_supported(c->N)) {
-    // pass E fused with the x / r update: G0(K4f : p) is never stored
-    CK(green_cg_front(c->pf, c->K4f, c->Sf, c->twf, g, c->st, c->part, &np));
-    CK(dev_final(c->part, np, c->sc, SC_PAP, OP_ALPHA, c->st));
-    CK(green_cg_back(c->Sf, c->twf, g, c->xf, c->rf, c->pf, c->pre_dev + 36, c->sc + SC_ALPHA,
-                     c->part, c->st, &np));
-    CK(dev_final(c->part, np, c->sc, SC_RRNEW, OP_BETA, c->st));
-    CK(dev_cg_cond(c->sc, c->cg_handle, use_handle, c->st));
-    return 0;
-  }
   if (timed) kt_start(c, KT_G32);
   CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np));
   if (timed) TRY(kt_stop(c));

@@ -109,37 +109,6 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
   return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr);
 }
 
-bool green_cg_fused_supported(int N) { return N == 32 || N == 64 || N == 128; }
-
-cudaError_t green_cg_front(const float* p, const float* K4f, float2* S, const float2* tw,
-                           const GridDesc& g, cudaStream_t st, double* part, int* nparts) {
-  switch (g.N) {
-    case 32: wgreen_cg_front<1>(p, K4f, S, tw, g, st, part); break;
-    case 64: wgreen_cg_front<2>(p, K4f, S, tw, g, st, part); break;
-    case 128: wgreen_cg_front<4>(p, K4f, S, tw, g, st, part); break;
-    case 256: wgreen_cg_front<8>(p, K4f, S, tw, g, st, part); break;
-    default: return cudaErrorInvalidValue;
-  }
-  *nparts = (g.N / 2) * g.N;
-  g_kernel_launches += 4;
-  return cudaGetLastError();
-}
-
-cudaError_t green_cg_back(const float2* S, const float2* tw, const GridDesc& g, float* x,
-                          float* r, const float* p, const float* k0, const double* alpha,
-                          double* part, cudaStream_t st, int* nparts) {
-  switch (g.N) {
-    case 32: wgreen_cg_back<1>(S, tw, g, x, r, p, k0, alpha, part, st); break;
-    case 64: wgreen_cg_back<2>(S, tw, g, x, r, p, k0, alpha, part, st); break;
-    case 128: wgreen_cg_back<4>(S, tw, g, x, r, p, k0, alpha, part, st); break;
-    case 256: wgreen_cg_back<8>(S, tw, g, x, r, p, k0, alpha, part, st); break;
-    default: return cudaErrorInvalidValue;
-  }
-  *nparts = (g.N / 2) * g.N;
-  g_kernel_launches += 1;
-  return cudaGetLastError();
-}
-
 cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2* S,
                                const float2* tw, GridDesc* g, cudaStream_t st, float* best_ms) {
   if (!green_df_supported(g->N)) return cudaSuccess;

@@ -69,18 +69,6 @@ cudaError_t green_setup_df(int N);
 cudaError_t green_apply_df(const double* x, const float* K4hi, const float* K4lo, int flgK,
                            double* y, dfl2* S, const dfl2* tw, GridDesc g, cudaStream_t st);
 
-// The preconditioned FP32 CG iteration's operator split around its step length (N in
-// {32, 64, 128}): green_cg_front runs passes A-D of G0(K4f : p) with pass A's partial
-// sums of <K4f : p, p> in part[0, *nparts); green_cg_back runs pass E fused with
-// x += alpha p, r -= alpha G0(K4f : p) (alpha read from device memory) and the partial sums
-// of <r, r>_K0 (k0: the reference medium's 9x9, FP32) in part[0, *nparts).
-bool green_cg_fused_supported(int N);
-cudaError_t green_cg_front(const float* p, const float* K4f, float2* S, const float2* tw,
-                           const GridDesc& g, cudaStream_t st, double* part, int* nparts);
-cudaError_t green_cg_back(const float2* S, const float2* tw, const GridDesc& g, float* x,
-                          float* r, const float* p, const float* k0, const double* alpha,
-                          double* part, cudaStream_t st, int* nparts);
-
 // Autotuner of the warp passes' tile shapes: times every candidate (columns per block of
 // passes B/D in {8, 16, 32} x of pass C in {2, 4}) on the given buffers with CUDA events
 // and stores the fastest in g->wtb / g->wtc (best_ms: its time per apply).  The buffers'

@@ -764,105 +764,6 @@ __global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __rest
   }
 }
 
-// Pass E of the preconditioned FP32 CG iteration fused with the vector update after the
-// apply: with alpha = *alpha_p (from pass A's product, set before this launch),
-// x += alpha p and r -= alpha G0(K4f : p), and one partial sum per block of <r, r>_K0 over
-// the block's voxels into part[blockIdx.x].  The apply's result itself is never stored.
-template <int M>
-__global__ void __launch_bounds__(288) wpass_e_cg(const float2* __restrict__ S, GridDesc g,
-                                                  const float2* __restrict__ twg,
-                                                  float* __restrict__ x, float* __restrict__ r,
-                                                  const float* __restrict__ p,
-                                                  const float* __restrict__ k0,
-                                                  const double* __restrict__ alpha_p,
-                                                  double* __restrict__ part) {
-  constexpr int N = 32 * M, H = N / 2 + 1;
-  const int Lp = padlen(N);
-  const long long N3 = g.N3;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* tw = reinterpret_cast<float2*>(smem_raw);
-  float2* col = tw + N;
-  __shared__ float s_k0[81];
-  for (int i = threadIdx.x; i < 81; i += blockDim.x) s_k0[i] = k0[i];
-  load_tw(tw, twg, N);
-  const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
-  const int bl0 = 2 * bp;
-  constexpr int NT = 288, E = 9 * N / NT;
-  static_assert(E * NT == 9 * N, "lines must divide evenly over the block");
-  {
-    float2 X0[E], X1[E];
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
-      const long long base = ((long long)i * N + c) * N;
-      const int kk = k < H ? k : N - k;
-      X0[e] = S[(base + bl0) * H + kk];
-      X1[e] = S[(base + bl0 + 1) * H + kk];
-    }
-#pragma unroll
-    for (int e = 0; e < E; e++) {
-      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
-      const int kk = k < H ? k : N - k;
-      float2 a = X0[e], b = X1[e];
-      if (kk == 0 || kk == N / 2) { a.y = 0; b.y = 0; }
-      if (k >= H) { a.y = -a.y; b.y = -b.y; }
-      float2 z;  // Z = X0 + i X1, as in wpass_e
-      z.x = a.x - b.y;
-      z.y = a.y + b.x;
-      col[i * Lp + pidx(k)] = z;
-    }
-  }
-  __syncthreads();
-  block_columns<N, float, true>(col, ncols9<N>(), Lp, tw);
-  __syncthreads();
-  // p, x and r are loaded after the transform: holding them across it would cost the
-  // registers of a resident block per SM
-  constexpr int EO = 2 * 9 * N / NT;
-  const float alpha = (float)*alpha_p;
-  float rv[EO];
-#pragma unroll
-  for (int e = 0; e < EO; e++) {
-    const int t = threadIdx.x + e * NT, l = t / (9 * N), rem = t - l * 9 * N;
-    const int i = rem / N, a = rem - i * N;
-    const float2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
-    const float yv = l ? z.y : z.x;
-    const long long k = i * N3 + a + (long long)N * (bl0 + l) + (long long)N * N * c;
-    x[k] = x[k] + alpha * p[k];
-    rv[e] = r[k] - alpha * yv;
-    r[k] = rv[e];
-  }
-  __syncthreads();  // every column read: the tile becomes the voxels' 9-vectors of r
-  float* rs = reinterpret_cast<float*>(col);
-#pragma unroll
-  for (int e = 0; e < EO; e++) {
-    const int t = threadIdx.x + e * NT, l = t / (9 * N), rem = t - l * 9 * N;
-    const int i = rem / N, a = rem - i * N;
-    rs[(l * N + a) * 9 + i] = rv[e];
-  }
-  __syncthreads();
-  float sum = 0.f;
-  for (int vv = threadIdx.x; vv < 2 * N; vv += NT) {
-    const float* q = rs + vv * 9;
-#pragma unroll
-    for (int i = 0; i < 9; i++) {
-      float t = 0.f;
-#pragma unroll
-      for (int j = 0; j < 9; j++) t += s_k0[9 * i + j] * q[j];
-      sum += q[i] * t;
-    }
-  }
-  __shared__ double wsum[9];  // block sum (9 warps), fixed order
-  double d = (double)sum;
-  for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
-  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = d;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double b = 0.0;
-    for (int k = 0; k < 9; k++) b += wsum[k];
-    part[blockIdx.x] = b;
-  }
-}
-
 template <typename T>
 size_t smem_w(int N, int ncols) { return sizeof(typename Vec2<T>::t) * (size_t)(N + ncols * padlen(N)); }
 template <typename T>
@@ -902,9 +803,6 @@ cudaError_t wgreen_setup() {
     if ((e = wsetup_b<M, T, 8>()) || (e = wsetup_c<M, T, 4>())) return e;
   if ((e = cudaFuncSetAttribute(wpass_e<M, T, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
-  if constexpr (small_code<T>())
-    if ((e = cudaFuncSetAttribute(wpass_e_cg<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem_w<T>(N, ncols9<N>())))) return e;
   return cudaSuccess;
 }
 
@@ -954,29 +852,6 @@ void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* 
   wlaunch_b_any<M, T>(g.wtb, S, g, tw, 1, st);
   wpass_e<M, T, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw,
                                                                  part_e ? x : nullptr, part_e);
-}
-
-// The preconditioned FP32 CG's operator in two halves around the step length: passes A-D
-// of G0(K4f : p) with pass A's partial sums of <K4f : p, p> in part, then (after alpha is
-// formed from them) pass E fused with the x / r update and the partials of <r, r>_K0.
-template <int M>
-void wgreen_cg_front(const float* p, const float* K4f, float2* S, const float2* tw,
-                     const GridDesc& g, cudaStream_t st, double* part) {
-  constexpr int N = 32 * M;
-  wpass_a<M, float, float, float><<<(N / 2) * N, 288, smem_w<float>(N, ncols9<N>()), st>>>(
-      p, K4f, nullptr, 1, S, g, tw, part);
-  wlaunch_b_any<M, float>(g.wtb, S, g, tw, 0, st);
-  if ((g.wtc ? g.wtc : wtile_c<float>()) == 4) wlaunch_c<M, float, 4>(S, g, tw, st);
-  else wlaunch_c<M, float, 2>(S, g, tw, st);
-  wlaunch_b_any<M, float>(g.wtb, S, g, tw, 1, st);
-}
-template <int M>
-void wgreen_cg_back(const float2* S, const float2* tw, const GridDesc& g, float* x, float* r,
-                    const float* p, const float* k0, const double* alpha, double* part,
-                    cudaStream_t st) {
-  constexpr int N = 32 * M;
-  wpass_e_cg<M><<<(N / 2) * N, 288, smem_w<float>(N, ncols9<N>()), st>>>(S, g, tw, x, r, p, k0,
-                                                                        alpha, part);
 }
 
 template <typename T>
