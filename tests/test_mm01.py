@@ -1,17 +1,12 @@
 """Bilinear Mises material (mm01, src/mm01.f): the oracle's restatement against the
-model's own identities, and the GPU path (launch_mises) against the oracle -- one
-stress update on a grid mixing mm01 and crystal voxels, and load steps of the
-reference's example deck (examples/test_mm01.in, extracted to tests/golden/mm01_deck.npz
-by tests/golden/make_mm01_deck.py)."""
-import os
-
+model's own identities, and the GPU path (launch_mises) against the oracle on a grid
+mixing mm01 and crystal voxels.  The reference's mm01 example deck runs in
+tests/test_example_decks.py."""
 import numpy as np
 import pytest
 
 from cpfft_gb300 import rve
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-DECK = np.load(os.path.join(HERE, "golden", "mm01_deck.npz"))
 MAT1, MAT2 = rve.MM01_DECK
 SQ2, ROOT3 = 1.414213562373095, 1.7320508075688  # mm01_init's constants
 
@@ -182,61 +177,6 @@ def test_gpu_mixed_grid_stress_update(gpulib, oracle):
         Po, Ko, fails, _ = o.stress_update(2, 1, Fn1, Fn2)
         assert per_voxel_rel(P[:, m01], Po[:, m01]) < 1e-12
         assert per_voxel_rel(K[:, m01], Ko[:, m01]) < 1e-11
-    finally:
-        s.close()
-        o.close()
-
-
-def deck_rve():
-    N = int(DECK["N"])
-    mat = DECK["mat_list"].astype(np.int32)
-    keys = [str(k) for k in DECK["prop_keys"]]
-    props = [dict(zip(keys, map(float, row))) for row in DECK["props"]]
-    return N, mat, props
-
-
-def deck_loading():
-    F_max = DECK["F_max"]
-    nstep = int(DECK["step_last"])
-    diag = F_max[[0, 4, 8]] * float(DECK["step_mult"]) * nstep
-    return rve.prescribed_stretch(diag, nstep)
-
-
-def test_deck_fixture_matches_the_material_table():
-    """The extracted deck: 7^3 grid, mat1 / mat2 as the material table MM01_DECK."""
-    N, mat, props = deck_rve()
-    assert N == 7 and mat.shape == (343,) and set(np.unique(mat)) == {1, 2}
-    for p, q in zip(props, rve.MM01_DECK):
-        assert p == q
-
-
-@pytest.mark.gpu
-def test_gpu_example_deck_load_steps(gpulib, oracle):
-    """The reference's mm01 example deck (7^3, two bilinear materials, F_xx 0.3,
-    F_yy = F_zz = -0.1 in 10 steps of 10 s, NR 1e-5, CG 1e-10): P_bar, Newton counts and
-    per-voxel P of the first load steps against the oracle."""
-    N, mat, props = deck_rve()
-    load = deck_loading()
-    kocks = np.zeros((3, N ** 3))
-    crystals = [rve.NOT_A_CRYSTAL, rve.NOT_A_CRYSTAL]
-    dt = float(DECK["time_step"])
-    s = gpulib.Solver(N, mat, kocks, crystals, dt, gpulib.G_REF_SHIFT)
-    o = oracle.Oracle(N, mat, kocks, crystals, dt, 0, nthreads=8)
-    try:
-        for k, p in enumerate(props, start=1):
-            s.set_mises(k, **p)
-            o.set_mises(k, p)
-        tol_nr, tol_cg, maxit = float(DECK["tol_nr"]), float(DECK["tol_cg"]), int(DECK["max_iter"])
-        s.nr3_begin(tol_cg)
-        o.nr3_begin(tol_cg)
-        for step in (1, 2, 3, 4):
-            rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, tol_nr, tol_cg, maxit)
-            rco, Pbo, sto = o.nr3_step(step, load.BC_all[step - 1], load.isNBC, tol_nr, tol_cg, maxit)
-            assert rc >= 0 and rco >= 0 and rc == rco
-            assert np.abs(Pbar - Pbo).max() < 1e-9 * np.abs(Pbo).max(), step
-            assert st["newton_iters"] == sto["newton_iters"]
-        F, P = s.fields()
-        assert per_voxel_rel(P, o.fields()["Pn1"]) < 1e-8
     finally:
         s.close()
         o.close()
