@@ -129,6 +129,7 @@ SIGNATURES = {
     "cpfft_format_e15": (_I, [_DP, _LL, ctypes.c_char_p]),
     "cpfft_f2disp": (_I, [_D, _D, _D, _DP]),
     "cpfft_write_disp_flat": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
+    "cpfft_ouresult": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
@@ -414,6 +415,13 @@ class Solver:
                                                     float(lengths[1]), float(lengths[2]),
                                                     structure_name.encode(),
                                                     directory.encode()), "write_disp_flat")
+
+    def ouresult(self, step, lengths=(100.0, 100.0, 100.0), structure_name="cpfft",
+                 directory=""):
+        """ouresult(step): the wnd, wee and wes flat files of the step."""
+        _check(load_library().cpfft_ouresult(int(step), float(lengths[0]), float(lengths[1]),
+                                             float(lengths[2]), structure_name.encode(),
+                                             directory.encode()), "ouresult")
 
     def commit(self):
         _check(load_library().cpfft_commit_step(), "commit_step")

@@ -2169,4 +2169,14 @@ int cpfft_write_disp_flat(int step, double lx, double ly, double lz, const char*
   return 0;
 }
 
+// ouresult (src/ouresult.f:12-42, called from src/FFT_nr3.f:183): the nodal displacement
+// file, then the element strain and stress files of the step (oustates writes nothing)
+int cpfft_ouresult(int step, double lx, double ly, double lz, const char* structure_name,
+                   const char* directory) {
+  TRY(cpfft_write_disp_flat(step, lx, ly, lz, structure_name, directory));
+  TRY(cpfft_write_flat(1, step, structure_name, directory));
+  TRY(cpfft_write_flat(2, step, structure_name, directory));
+  return 0;
+}
+
 }  // extern "C"

@@ -375,6 +375,11 @@ int cpfft_f2disp(double lx, double ly, double lz, double* u);
  * then one line of (3e15.6) per node, values below 1e-30 as zero, formatted on the GPU. */
 int cpfft_write_disp_flat(int step, double lx, double ly, double lz, const char* structure_name,
                           const char* directory);
+/* ouresult(step) (src/ouresult.f:12-42; called from src/FFT_nr3.f:183 on output steps): the
+ * three flat text files of the step -- wndNNNNN_text, weeNNNNN_text, wesNNNNN_text -- from
+ * the device state (the committed step: call after the step's commit). */
+int cpfft_ouresult(int step, double lx, double ly, double lz, const char* structure_name,
+                   const char* directory);
 
 /* State roll-over Fn <- Fn1, Pn <- Pn1, history n <- n+1: replaces update
  * (src/update.f:16-193) and FFT_nr3.f:173-179 in mirror mode. */

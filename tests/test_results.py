@@ -59,5 +59,18 @@ def test_gpu_flat_files(gpulib, tmp_path):
             assert lines[3] == "#  Model nodes, elements: %8d%8d" % ((N + 1) ** 3, N ** 3)
             assert lines[5] == "#  Load(time) step: %8d" % 2
             assert "\n".join(lines[7:]) == text
+        # ouresult writes the same two element files and the nodal file
+        sub = tmp_path / "ouresult"
+        sub.mkdir()
+        s.ouresult(2, (100.0, 100.0, 100.0), "rve9", str(sub))
+        assert sorted(os.listdir(sub)) == ["wee00002_text", "wes00002_text", "wnd00002_text"]
+        for name in ("wee00002_text", "wes00002_text"):
+            a = open(os.path.join(tmp_path, name)).read().split("\n")
+            b = open(os.path.join(sub, name)).read().split("\n")
+            assert a[:4] + a[5:] == b[:4] + b[5:]  # all but the date line
+        u = s.f2disp((100.0, 100.0, 100.0))
+        body = open(os.path.join(sub, "wnd00002_text")).read().split("\n")[7:-1]
+        assert len(body) == (N + 1) ** 3
+        assert body[5] == "".join(flat_ref.e15_6(0.0 if abs(x) < 1e-30 else x) for x in u[5])
     finally:
         s.close()
