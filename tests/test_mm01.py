@@ -202,3 +202,39 @@ def test_gpu_undefined_material_fails_loudly(gpulib):
             s.set_mises(1, e=100.0, nu=0.3, yld_pt=1.0, tan_e=200.0)  # tan_e >= e
     finally:
         s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_grid_fast_form(gpulib):
+    """Crystal and mm01 voxels on one grid in the fast form (FP32 inner CG with the
+    reference-medium preconditioner, iterate + trial starts, FP32 tangent, the voxel
+    queue, whose ordering mixes the mm01 voxels the crystal kernel skips) against the plain
+    FP64 form: P_bar within 1e-6, the same Newton counts."""
+    N = 16
+    mat, kocks, crystals = mixed_grid(N, 83)
+    load = rve.uniaxial_tension(0.02, 20)
+    out = []
+    for fast in (False, True):
+        s = gpulib.Solver(N, mat, kocks, crystals, 1.0, gpulib.G_CENTERED,
+                          gpulib.PREC_MIXED if fast else gpulib.PREC_FP64)
+        try:
+            for k, m in ((2, MAT1), (3, MAT2)):
+                s.set_mises(k, **m)
+            if fast:
+                s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL |
+                           gpulib.TANGENT_F32)
+                s.set_precond(gpulib.PRECOND_REFERENCE)
+                s.set_schedule(gpulib.SCHED_QUEUE)
+            s.nr3_begin(1e-10)
+            pb, its = [], []
+            for step in (1, 2, 3):
+                rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
+                assert rc == 0
+                pb.append(Pbar)
+                its.append(st["newton_iters"])
+            out.append((np.array(pb), its))
+        finally:
+            s.close()
+    (pb0, it0), (pb1, it1) = out
+    assert np.abs(pb1 - pb0).max() < 1e-6 * np.abs(pb0).max()
+    assert it1 == it0

@@ -152,3 +152,31 @@ def test_gpu_refuses_mixed_laws(gpulib):
     mat = np.array([1, 2] * 13 + [1], np.int32)
     with pytest.raises(RuntimeError, match="hardening law"):
         gpulib.Solver(N, mat, np.zeros((3, N ** 3)), [rve.FCC_VOCE, MTS], 1.0)
+
+
+@pytest.mark.gpu
+def test_gpu_mts_sub_stepping(gpulib, oracle):
+    """Local solves that fail at the full step and succeed in halves (miter 6: the first
+    load step of 2e-3 takes 564 local iterations against 399 with miter 30, same P_bar):
+    the sub-steps run with their own temperature and rate setup on both sides.  P_bar,
+    the Newton count and the summed local iterations against the oracle."""
+    N = 5
+    crystal = dict(MTS, miter=6)
+    r = rve.make_rve(N, 3, 93, crystal)
+    load = rve.prescribed_stretch([0.004, -0.002, -0.002], 2)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_REF_SHIFT)
+    o = oracle.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 0, nthreads=4)
+    try:
+        s.nr3_begin(1e-10)
+        o.nr3_begin(1e-10)
+        rc, Pbar, st = s.nr3_step(1, load.BC_all[0], load.isNBC, 1e-5, 1e-10, 10)
+        rco, Pbo, sto = o.nr3_step(1, load.BC_all[0], load.isNBC, 1e-5, 1e-10, 10)
+        assert rc == rco == 0
+        assert st["newton_iters"] == sto["newton_iters"]
+        assert st["local_fallbacks"] == sto["local_fallbacks"] == 0
+        assert np.abs(Pbar - Pbo).max() < 1e-9 * np.abs(Pbo).max()
+        assert sto["local_iters"] > 500  # halves taken
+        assert abs(st["local_iters"] - sto["local_iters"]) <= 0.01 * sto["local_iters"]
+    finally:
+        s.close()
+        o.close()
