@@ -480,12 +480,6 @@ int matvec_acc(Ctx* c, const double* x, double* y, int flgK) {
                  "green_apply double-float"));
   return kt_stop(c);
 }
-int matvec32(Ctx* c, const float* x, float* y) {
-  c->f32_matvecs++;
-  kt_start(c, KT_G32);
-  TRY(cuda_check(green_apply<float>(x, c->K4f, 1, y, c->Sf, c->twf, c->g, c->st), "green_apply fp32"));
-  return kt_stop(c);
-}
 // y = G(K4f : x) and sc[SC_PAP] = x . y with alpha = rr / (x . y): the product is summed
 // inside the last FFT pass where that pass supports it, else by a separate reduction
 int matvec32_alpha(Ctx* c, const float* x, float* y) {
@@ -1739,7 +1733,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   }
   if (existNBC) TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));
   for (int i = 0; i < 9; i++) barF[i] = c->barF_t[i] + DbarF[i];
-  int iiter_NBC = 0, rc = 0;
+  int iiter_NBC = 0;
   double tp = 0, ts = 0;
   for (;;) {
     CK(dev_fill9(c->dFm, N3, DbarF, c->st));
@@ -1863,7 +1857,6 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   S.kernel_launches = g_kernel_launches - launches0;
   S.t_total = sec(t0);
   if (st) *st = S;
-  (void)rc;
   return S.local_fallbacks ? CPFFT_WARN_LOCAL_FALLBACK : 0;
 }
 
