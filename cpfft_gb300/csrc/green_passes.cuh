@@ -504,10 +504,18 @@ __device__ __forceinline__ void block_columns(typename Vec2<T>::t* base, int nco
 }
 
 // part != nullptr (with flgK): one partial sum per block of <K : x, x> over its voxels.
+// Resident blocks per SM the FP32 passes A and E are compiled for at N = 128: four
+// 288-thread blocks (at most 56 registers a thread) keep more loads in flight than the
+// three the default register count allows -- 5 % off the FP32 apply at 128^3, measured.
+// 0 (no hint) elsewhere: the double-float passes, N = 256 (the cap would spill) and the
+// small grids (whose default counts already fit more blocks).
+template <int M, typename T>
+constexpr int minblocks_ae() { return (sizeof(T) == 4 && M == 4) ? 4 : 0; }
+
 // TIO: the field type of x (float, or double for the double-float transform T = dfl,
 // whose tangent is the pair K4, K4lo)
 template <int M, typename T, typename TK, typename TIO>
-__global__ void __launch_bounds__(288) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
+__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
                                                const float* __restrict__ K4lo,
                                                int flgK, typename Vec2<T>::t* __restrict__ S,
                                                GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
@@ -685,7 +693,7 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
 // dotx != nullptr: also one partial sum per block of dotx . y over the voxels the block
 // writes (the CG product p . Ap without re-reading Ap), into part[blockIdx.x]
 template <int M, typename T, typename TIO>
-__global__ void __launch_bounds__(288) wpass_e(const typename Vec2<T>::t* __restrict__ S,
+__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_e(const typename Vec2<T>::t* __restrict__ S,
                                                TIO* __restrict__ y, GridDesc g,
                                                const typename Vec2<T>::t* __restrict__ twg,
                                                const TIO* __restrict__ dotx,
