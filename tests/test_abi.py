@@ -101,3 +101,41 @@ def test_ctypes_signatures_match_the_header_arity(gpulib):
         name, params = m.group(1), m.group(2).strip()
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(gpulib.SIGNATURES[name][1]) == n, (name, n, gpulib.SIGNATURES[name][1])
+
+
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """Every struct of the boundary has, in the ctypes mirrors, the size and field offsets
+    gcc gives it from include/cpfft_gpu.h (a probe program compiled here), and the history
+    width constant agrees."""
+    import cpfft_gb300
+    from oracle import pyoracle
+    mirrors = {"cpfft_crystal": [cpfft_gb300.Crystal, pyoracle.Crystal],
+               "cpfft_mises": [cpfft_gb300.Mises, pyoracle.Mises],
+               "cpfft_stats": [cpfft_gb300.Stats, pyoracle.Stats],
+               "cpfft_rve": [cpfft_gb300.Rve]}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cpfft_gpu.h"',
+             'int main(void) {', 'printf("HIST %d\\n", CPFFT_HIST_WORDS);']
+    for name, ms in mirrors.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (name, name))
+        for f, _ in ms[0]._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (name, f, name, f))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        parts = ln.split()
+        if len(parts) == 2:
+            got[parts[0]] = int(parts[1])
+        elif len(parts) == 3:
+            got[(parts[0], parts[1])] = int(parts[2])
+    assert got["HIST"] == cpfft_gb300.HIST_WORDS == pyoracle.HIST_WORDS
+    for name, ms in mirrors.items():
+        for m in ms:
+            assert ctypes.sizeof(m) == got[(name, "size")], (name, m)
+            for f, _ in m._fields_:
+                assert getattr(m, f).offset == got[(name, f)], (name, f)
