@@ -377,7 +377,8 @@ int cpfft_write_disp_flat(int step, double lx, double ly, double lz, const char*
                           const char* directory);
 /* ouresult(step) (src/ouresult.f:12-42; called from src/FFT_nr3.f:183 on output steps): the
  * three flat text files of the step -- wndNNNNN_text, weeNNNNN_text, wesNNNNN_text -- from
- * the device state (the committed step: call after the step's commit). */
+ * the device state of the committed step: after cpfft_nr3_step, which ends with the
+ * update, or after cpfft_commit_step in mirror mode. */
 int cpfft_ouresult(int step, double lx, double ly, double lz, const char* structure_name,
                    const char* directory);
 
