@@ -304,9 +304,11 @@ def gb300_arm(args):
     tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
     solver.nr3_begin(tolPCG)
     step = 0
+    pbars = []  # P_bar of every step (the stress-strain curve), for --compare-fp64
     for _ in range(args.warmup):
         step += 1
-        rc, _, _ = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
+        rc, Pb, _ = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
+        pbars.append(Pb)
     # pinned host buffers for the e2e copies of each step's result fields
     Fh = torch.empty((9, N3), dtype=torch.float64).pin_memory()
     Ph = torch.empty((9, N3), dtype=torch.float64).pin_memory()
@@ -331,6 +333,7 @@ def gb300_arm(args):
             raise RuntimeError("sync_to_host failed")
         t_e2e += time.perf_counter() - t0
         stats.append(st)
+        pbars.append(Pbar)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     if world > 1:
@@ -435,9 +438,34 @@ def gb300_arm(args):
         "clocks": clk,
         "cpu_baseline": cpu,
     }
-    print(json.dumps(line), flush=True)
     solver.close()
+    if args.compare_fp64 and args.mode != "fp64" and world == 1:
+        line["error_vs_fp64"] = compare_fp64(cp, r, load, pbars, Ph.numpy(), tolNR, tolPCG,
+                                             maxIter)
+    print(json.dumps(line), flush=True)
     return 0
+
+
+def compare_fp64(cp, r, load, pbars, P_last, tolNR, tolPCG, maxIter):
+    """The plain FP64 form (FP64 CG, the reference's local starts) over the same load
+    steps, after the timed run: the fast form's error on the stress-strain curve (P_bar of
+    every step) and on the last step's per-voxel P.  Untimed."""
+    N = r.N
+    s = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, cp.PREC_FP64)
+    try:
+        s.set_mode(cp.PREC_FP64, cp.START_PLAIN)
+        s.nr3_begin(tolPCG)
+        rel = []
+        for step, pb in enumerate(pbars, start=1):
+            _, ref, _ = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
+            rel.append(float(np.abs(pb - ref).max() / np.abs(ref).max()))
+        _, P = s.fields()
+    finally:
+        s.close()
+    scale = np.maximum(np.abs(P).max(axis=0), 1e-6 * np.abs(P).max())
+    return {"pbar_rel_per_step": rel, "pbar_rel_max": max(rel),
+            "p_last_step_rel_max_per_voxel": float((np.abs(P_last - P).max(axis=0) / scale).max()),
+            "reference_form": "plain FP64: FP64 CG, the reference's local starts, FP64 tangent"}
 
 
 def config4_rves(cp, nsteps):
@@ -528,6 +556,9 @@ def main():
     # the benchmark uses the reference example deck's value 1e-5; the equilibrium
     # residual ||G(P)||/||P_bar|| is reported per step.
     ap.add_argument("--tol-nr", type=float, default=1e-5)
+    ap.add_argument("--compare-fp64", action="store_true",
+                    help="after the timed steps, run the plain FP64 form over the same steps "
+                         "and report the fast form's error on P_bar and on the last P")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
