@@ -1372,6 +1372,43 @@ void mises_point(const MisesP& m, int step, const M3 Fn, const M3 Fn1, const Sta
   pull_back(Fn, Fn1, k, np1, o);
 }
 
+// ---- mm00: the FFT program's original St-Venant-Kirchhoff material ------------------
+// constitutive (src/mm00.f:13-60): E = (F^T F - I) / 2, S = K tr(E) I + 2 mu dev(E),
+// P = F S and A_iJkL = dP_iJ / dF_kL = delta_ik S_LJ + F_iM C_MJNL F_kN with the isotropic
+// C of bulk modulus K and shear modulus mu.  A known-answer material for the global loop:
+// homogeneous grids and laminates have closed-form solutions.
+void svk_point(double K, double mu, const M3 F, double P[9], double A[81]) {
+  M3 E, S;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double c = 0.0;
+      for (int k = 0; k < 3; k++) c += F[k][i] * F[k][j];
+      E[i][j] = 0.5 * (c - (i == j ? 1.0 : 0.0));
+    }
+  const double tr = E[0][0] + E[1][1] + E[2][2];
+  const double lam = K - 2.0 * mu / 3.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) S[i][j] = 2.0 * mu * E[i][j] + (i == j ? lam * tr : 0.0);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double c = 0.0;
+      for (int k = 0; k < 3; k++) c += F[i][k] * S[k][j];
+      P[3 * i + j] = c;
+    }
+  auto C = [&](int a, int b, int c, int d) {
+    return lam * (a == b) * (c == d) + mu * ((a == c) * (b == d) + (a == d) * (b == c));
+  };
+  for (int i = 0; i < 3; i++)
+    for (int J = 0; J < 3; J++)
+      for (int k = 0; k < 3; k++)
+        for (int L = 0; L < 3; L++) {
+          double a = (i == k) ? S[L][J] : 0.0;
+          for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) a += F[i][m] * C(m, J, n, L) * F[k][n];
+          A[I4(i, J, k, L)] = a;
+        }
+}
+
 // ---- FFT (restated DFTI role: exact complex DFT) --------------------------------------
 struct FFT1 {
   int n;
@@ -1457,6 +1494,7 @@ struct orc_ctx {
   std::vector<Crys> crys;
   std::vector<int> kind;           // per material: 0 crystal, 1 mm01, 2 not yet defined
   std::vector<MisesP> mp;          // per material (mm01)
+  std::vector<double> svk;         // per material (mm00, kind 3): K, mu
   std::vector<int> mat;            // 0-based material per voxel
   std::vector<VoxProps> vprops;
   std::vector<State> hn, hn1;
@@ -1498,6 +1536,7 @@ orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
   c->crys.resize(ncrystals);
   c->kind.assign(ncrystals, 0);
   c->mp.resize(ncrystals);
+  c->svk.assign(2 * ncrystals, 0.0);
   for (int i = 0; i < ncrystals; i++) {
     if (props[i].slip_type == CPFFT_NOT_A_CRYSTAL) { c->kind[i] = 2; continue; }
     crystal_finalize(props[i], c->crys[i]);
@@ -1578,6 +1617,12 @@ static void voxel_point(orc_ctx* c, long v, int step, int iter, const M3 fn, con
     material_point(c->crys[m], c->vprops[v], c->dt, step, iter, fn, fn1, c->hn[v], c->hn1[v], o);
   } else if (c->kind[m] == 1) {
     mises_point(c->mp[m], step, fn, fn1, c->hn[v], c->hn1[v], o);
+  } else if (c->kind[m] == 3) {  // hyperelastic: no history
+    (void)fn;
+    svk_point(c->svk[2 * m], c->svk[2 * m + 1], fn1, o.P, o.A);
+    c->hn1[v] = c->hn[v];
+    o.ok = true;
+    o.iters = 0;
   } else {  // undefined material
     std::memset(&o, 0, sizeof(o));
     o.ok = false;
@@ -1593,6 +1638,25 @@ void orc_set_mises(orc_ctx* c, int material, const cpfft_mises* props) {
       mises_state_init(c->mp[m], c->hn[v]);
       c->hn1[v] = c->hn[v];
     }
+}
+
+void orc_set_svk(orc_ctx* c, int material, double K, double mu) {
+  const int m = material - 1;
+  c->kind[m] = 3;
+  c->svk[2 * m] = K;
+  c->svk[2 * m + 1] = mu;
+  for (long v = 0; v < c->N3; v++)
+    if (c->mat[v] == m) {
+      std::memset(&c->hn[v], 0, sizeof(State));
+      c->hn1[v] = c->hn[v];
+    }
+}
+
+void orc_svk_point(double K, double mu, const double F[9], double P[9], double A[81]) {
+  M3 f;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) f[i][j] = F[3 * i + j];
+  svk_point(K, mu, f, P, A);
 }
 
 int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn, const double* Fn1,

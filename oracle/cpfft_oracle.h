@@ -29,6 +29,13 @@ void     orc_destroy(orc_ctx* c);
  * material (resets its voxels' state) */
 void orc_set_mises(orc_ctx* c, int material, const cpfft_mises* props);
 
+/* make a material declared with slip_type CPFFT_NOT_A_CRYSTAL the FFT program's original
+ * St-Venant-Kirchhoff material (constitutive, src/mm00.f:13-60) of bulk modulus K and shear
+ * modulus mu: a known-answer material for the global loop (not a product model) */
+void orc_set_svk(orc_ctx* c, int material, double K, double mu);
+/* P and dP/dF (row-major, (ij)(kl)) of that material at F (row-major) */
+void orc_svk_point(double K, double mu, const double F[9], double P[9], double A[81]);
+
 /* drive_eps_sig on every voxel; Fn/Fn1 NULL -> use the context's fields.
  * Pn1/K4 NULL -> keep in the context.  Returns number of local failures. */
 int orc_stress_update(orc_ctx* c, int step, int iter, const double* Fn,

@@ -122,6 +122,8 @@ def lib():
         L.orc_voxel_update.argtypes = [P(Crystal), dp, d, i, i, dp, dp, dp, dp, dp, dp,
                                        dp, dp]
         L.orc_set_mises.argtypes = [vp, i, P(Mises)]
+        L.orc_set_svk.argtypes = [vp, i, d, d]
+        L.orc_svk_point.argtypes = [d, d, dp, dp, dp]
         L.orc_mises_update.restype = i
         L.orc_mises_update.argtypes = [P(Mises), i, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_polar.argtypes = [dp, dp]
@@ -232,10 +234,23 @@ class Oracle:
     def set_history_n(self, hn):
         lib().orc_set_history_n(self.h, _p(np.ascontiguousarray(hn)))
 
+    def set_svk(self, material, K, mu):
+        """A St-Venant-Kirchhoff material (the FFT program's original mm00)."""
+        lib().orc_set_svk(self.h, int(material), float(K), float(mu))
+
     def set_mises(self, material, props):
         """props: dict e, nu, yld_pt, tan_e, beta (a bilinear Mises material, mm01)."""
         m = _mises(props)
         lib().orc_set_mises(self.h, int(material), ctypes.byref(m))
+
+
+def svk_point(K, mu, F):
+    """P (3x3) and dP/dF (9x9, (ij)(kl)) of the St-Venant-Kirchhoff material."""
+    P = np.zeros(9)
+    A = np.zeros(81)
+    lib().orc_svk_point(K, mu, _p(np.ascontiguousarray(F, dtype=np.float64).reshape(9)),
+                        _p(P), _p(A))
+    return P.reshape(3, 3), A.reshape(9, 9)
 
 
 def mises_update(props, step, Fn, Fn1, hist_n=None):
