@@ -1408,13 +1408,13 @@ int cpfft_set_mises(int material, const cpfft_mises* props) {
                     "0 <= tan_e < e, 0 <= beta <= 1", material);
     return CPFFT_ERR_BAD_ARG;
   }
+  // the copies below use the default stream: the context's (non-blocking) stream drains first
+  TRY(sync(c));
   // setup_mm01_rknstr (src/drive_eps_sig.f:486-520): h = tan_e e / (e - tan_e)
   c->h_mises[m] = MisesRec{p.e, p.nu, p.yld_pt, p.tan_e * p.e / (p.e - p.tan_e), p.beta};
   const long long N3 = c->N3;
-  if (!c->mises) {
-    TRY(dalloc(c->mises, N3 * sizeof(int)));
-    TRY(dalloc(c->misess, c->mat_kind.size() * sizeof(MisesRec)));
-  }
+  if (!c->mises) TRY(dalloc(c->mises, N3 * sizeof(int)));
+  if (!c->misess) TRY(dalloc(c->misess, c->mat_kind.size() * sizeof(MisesRec)));
   c->mat_kind[m] = 1;
   std::vector<int> idx(N3);
   long long nm = 0, nu = 0;
