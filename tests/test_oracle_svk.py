@@ -120,3 +120,52 @@ def test_two_phase_laminate(oracle):
             assert np.abs(Pbar - Pref.ravel()).max() < 1e-8 * np.abs(Pref).max()
     finally:
         o.close()
+
+
+def test_laminate_under_uniaxial_stress(oracle):
+    """The laminate with mixed boundary conditions (F_xx, F_xy, F_xz, F_yz prescribed, the
+    other five P_bar components zero): the closed form now solves for the free components
+    of F_bar together with the layers' first columns, which exercises tangent_homo and
+    NBC_update on a heterogeneous grid."""
+    import scipy.optimize
+    N = 5
+    c = np.arange(N ** 3) // (N * N)
+    mat = np.where(c < 2, 1, 2).astype(np.int32)
+    fa = 2 / N
+    load = rve.uniaxial_tension(0.02, 20)
+    free = np.nonzero(load.isNBC)[0]  # the components with P_bar prescribed (zero)
+    o = grid(oracle, N, mat)
+    try:
+        o.nr3_begin(1e-10)
+        for step in (1, 2, 3):
+            bc = load.BC_all[step - 1]
+
+            def unpack(x):
+                Fbar = bc.copy()
+                Fbar[free] = x[3:]
+                Fbar = Fbar.reshape(3, 3)
+                FA, FB = Fbar.copy(), Fbar.copy()
+                FA[:, 0] = x[:3]
+                FB[:, 0] = (Fbar[:, 0] - fa * x[:3]) / (1 - fa)
+                return FA, FB
+
+            def res(x):
+                FA, FB = unpack(x)
+                PA, PB = oracle_svk(STIFF, FA), oracle_svk(SOFT, FB)
+                Pbar = (fa * PA + (1 - fa) * PB).ravel()
+                return np.concatenate([PA[:, 0] - PB[:, 0], Pbar[free]])
+
+            x0 = np.concatenate([bc.reshape(3, 3)[:, 0], np.eye(3).ravel()[free]])
+            x = scipy.optimize.fsolve(res, x0, xtol=1e-13)
+            assert np.abs(res(x)).max() < 1e-12
+            FA, FB = unpack(x)
+            PA, PB = oracle_svk(STIFF, FA), oracle_svk(SOFT, FB)
+            rc, Pbar, _ = o.nr3_step(step, bc, load.isNBC, 1e-8, 1e-10, 20)
+            assert rc == 0
+            Pref = (fa * PA + (1 - fa) * PB).ravel()
+            assert np.abs(Pbar - Pref).max() < 1e-8 * np.abs(Pref).max(), step
+            F = o.fields()["Fn1"]
+            for ph, Fx in ((1, FA), (2, FB)):
+                assert np.abs(F[:, mat == ph] - Fx.ravel()[:, None]).max() < 1e-9, (step, ph)
+    finally:
+        o.close()
