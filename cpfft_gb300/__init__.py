@@ -121,6 +121,7 @@ SIGNATURES = {
     "cpfft_init": (_I, [_I, _IP, _DP, _P(Crystal), _I, _D, _I]),
     "cpfft_set_mode": (_I, [_I, _I]),
     "cpfft_set_precond": (_I, [_I]),
+    "cpfft_set_equilibrium_tol": (_I, [_D]),
     "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
@@ -136,6 +137,7 @@ SIGNATURES = {
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
     "cpfft_green_apply_df": (_I, [_DP, _DP, _I]),
     "cpfft_set_K4": (_I, [_DP]),
+    "cpfft_pass_counts": (_I, [_P(_LL)]),
     "cpfft_cg": (_I, [_DP, _DP, _D, _IP]),
     "cpfft_tangent_homo": (_I, [_D, _DP]),
     "cpfft_nr3_step": (_I, [_I, _DP, _IP, _D, _D, _I, _DP, _P(Stats)]),
@@ -306,6 +308,11 @@ class Solver:
         """Reference-medium preconditioner of the mixed-precision inner iterations."""
         _check(load_library().cpfft_set_precond(int(precond)), "cpfft_set_precond")
 
+    def set_equilibrium_tol(self, tol):
+        """Also require ||G(P)|| / (sqrt(N3) ||P_bar||) <= tol to end a Newton loop of
+        nr3_step (0: the reference's ||dF|| / ||F|| test alone)."""
+        _check(load_library().cpfft_set_equilibrium_tol(float(tol)), "cpfft_set_equilibrium_tol")
+
     # --- learned initial guess of the local solve --------------------------------------
     def learn_log(self, capacity, stride=1, phase=0):
         """Log (features, converged increments) of the plain local solves of every
@@ -330,6 +337,14 @@ class Solver:
         rc = _check(load_library().cpfft_stress_update(step, it, _dp(Fn), _dp(Fn1), _dp(P),
                                                        _dp(K)), "drive_eps_sig")
         return P, K, rc
+
+    def pass_counts(self):
+        """Counters of the last stress pass: local iterations (summed over voxels),
+        failed local solves, predictor iterations, dropped starts, sub-stepped solves."""
+        c = (ctypes.c_longlong * 5)()
+        _check(load_library().cpfft_pass_counts(c), "cpfft_pass_counts")
+        return {"local_iters": c[0], "fallbacks": c[1], "predict_iters": c[2],
+                "starts_dropped": c[3], "substepped": c[4]}
 
     def G_K_dF(self, x, flgK=True):
         y = np.zeros((9, self.N3))

@@ -46,11 +46,16 @@ void cpfft_set_error(const char* fmt, ...) {
   va_end(ap);
 }
 
+// cudaFuncSetAttribute acts on the current device, so the raised limit is kept per
+// (device, kernel)
 cudaError_t raise_max_dynamic_smem(const void* func, size_t bytes) {
   static std::mutex mu;
-  static std::map<const void*, size_t> set;
+  static std::map<std::pair<int, const void*>, size_t> set;
+  int dev = 0;
+  cudaError_t ge = cudaGetDevice(&dev);
+  if (ge != cudaSuccess) return ge;
   std::lock_guard<std::mutex> lock(mu);
-  size_t& cur = set[func];
+  size_t& cur = set[std::make_pair(dev, func)];
   if (bytes <= cur) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
   if (e == cudaSuccess) cur = bytes;
@@ -345,6 +350,11 @@ struct Ctx {
   float* pre_dev = nullptr;  // the same on the device (read by the preconditioned kernels)
   // FFT_nr3 locals that persist across steps (Fortran DATA => SAVE, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
+  // equilibrium stop test of the Newton loop (cpfft_set_equilibrium_tol; 0 = the reference's)
+  double eq_tol = 0.0;
+  // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
+  // starts dropped, sub-stepped solves (cpfft_pass_counts)
+  long long last_pass[5] = {0, 0, 0, 0, 0};
   // counters of the current step
   long long cg_iters = 0, cg_solves = 0, f64_matvecs = 0, f32_matvecs = 0;
   // CUDA-event timing of every stress / Green launch on the library stream
@@ -456,6 +466,23 @@ int dnrm2(Ctx* c, const double* x, double* out) {
   double v;
   TRY(read_scalar(c, SC_TMP, &v));
   *out = std::sqrt(v);
+  return 0;
+}
+
+// ||g|| / (sqrt(N3) ||mean of P||) with g = G(P): the equilibrium residual of the current
+// state (one synchronisation)
+int equil_residual(Ctx* c, const double* g, double* out) {
+  CK(dev_dot(g, g, 9 * c->N3, c->part, c->sc, SC_TMP, OP_STORE, c->st));
+  CK(dev_sum9(c->P, c->N3, c->part, c->sc, SC_SUM9, c->st));
+  CK(cudaMemcpyAsync(c->h_sc + SC_TMP, c->sc + SC_TMP, (SC_SUM9 + 9 - SC_TMP) * sizeof(double),
+                     cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  double pb = 0;
+  for (int i = 0; i < 9; i++) {
+    const double m = c->h_sc[SC_SUM9 + i] / (double)c->N3;
+    pb += m * m;
+  }
+  *out = std::sqrt(c->h_sc[SC_TMP]) / (std::sqrt((double)c->N3) * std::sqrt(pb));
   return 0;
 }
 
@@ -989,7 +1016,9 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   // coupled Newton from that pass's converged state.  On the other implicit passes,
   // CPFFT_START_LEARNED starts it from the network's guess and CPFFT_START_TRIAL from the
   // elastic trial, both returned inside the rate surface.
-  const bool have_iterate = c->pass_step == step && c->pass_iter >= 1 && iter == c->pass_iter + 1;
+  // (iter == pass_iter: the same Newton iteration re-evaluated at a shortened increment)
+  const bool have_iterate = c->pass_step == step && c->pass_iter >= 1 &&
+                            (iter == c->pass_iter + 1 || iter == c->pass_iter);
   a.start_iterate = (c->warm & CPFFT_START_ITERATE) && iter >= 2 && have_iterate;
   a.start_trial = (c->warm & CPFFT_START_TRIAL) && !(c->warm & CPFFT_START_LEARNED) &&
                   !a.start_iterate;
@@ -1021,7 +1050,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
     a.queue = c->vq + 128;
     a.cost = c->vcost;
   }
-  CK(cudaMemsetAsync(c->stats, 0, 4 * sizeof(unsigned long long), c->st));
+  CK(cudaMemsetAsync(c->stats, 0, 5 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
   if (c->n_crys_vox)
     CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
@@ -1033,20 +1062,21 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   c->K4f_valid = a.K4f != nullptr;
   const bool reduce = c->K4f_valid && pre_applies(c);
   if (reduce) TRY(reference_reduce(c));
-  CK(cudaMemcpyAsync(c->h_stats, c->stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->h_stats, c->stats, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
   TRY(sync(c));
   if (reduce) TRY(reference_build(c));
+  for (int k = 0; k < 5; k++) c->last_pass[k] = (long long)c->h_stats[k];
   if (local_iters) *local_iters = (long long)c->h_stats[0];
   if (fails) *fails = (int)c->h_stats[1];
   if (predict_iters) *predict_iters = (long long)c->h_stats[2];
   if (rejected) *rejected = (long long)c->h_stats[3];
   if (c->log)  // per-pass local work (CPFFT_LOG=1)
     fprintf(stderr, "       stress pass step %d iter %d: update %.4f predictor %.4f per voxel%s, "
-            "%.4f starts dropped\n", step, iter, (double)c->h_stats[0] / (double)c->N3,
-            (double)c->h_stats[2] / (double)c->N3,
+            "%.4f starts dropped, %llu sub-stepped\n", step, iter,
+            (double)c->h_stats[0] / (double)c->N3, (double)c->h_stats[2] / (double)c->N3,
             warm ? " (learned start)" : a.start_iterate ? " (iterate start)" :
             a.start_trial && iter > 0 ? " (trial start)" : "",
-            (double)c->h_stats[3] / (double)c->N3);
+            (double)c->h_stats[3] / (double)c->N3, c->h_stats[4]);
   if (warm) TRY(mlp_check_error());
   return 0;
 }
@@ -1336,10 +1366,10 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
       (rc = dalloc(c->S, (size_t)9 * N * N * c->g.H * sizeof(double2))) ||
       (rc = dalloc(c->tw, N * sizeof(double2))) || (rc = dalloc(c->part, (size_t)std::max<long long>(9 * NPART, (long long)N * N) * sizeof(double))) ||
       (rc = dalloc(c->sc, SC_COUNT * sizeof(double))) ||
-      (rc = dalloc(c->stats, 4 * sizeof(unsigned long long))))
+      (rc = dalloc(c->stats, 8 * sizeof(unsigned long long))))
     return fail(rc);
   if (cudaMallocHost((void**)&c->h_sc, SC_COUNT * sizeof(double)) != cudaSuccess ||
-      cudaMallocHost((void**)&c->h_stats, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaMallocHost((void**)&c->h_stats, 8 * sizeof(unsigned long long)) != cudaSuccess) {
     cpfft_set_error("cudaMallocHost failed");
     return fail(CPFFT_ERR_NO_MEMORY);
   }
@@ -1501,6 +1531,16 @@ int cpfft_set_precond(int precond) {
   return 0;
 }
 
+int cpfft_set_equilibrium_tol(double tol) {
+  TRY(need_ctx());
+  if (!(tol >= 0.0) || !std::isfinite(tol)) {
+    cpfft_set_error("cpfft_set_equilibrium_tol: tolerance must be finite and >= 0");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  g_ctx->eq_tol = tol;
+  return 0;
+}
+
 int cpfft_tuning(int* tiles, double* ms) {
   TRY(need_ctx());
   Ctx* c = g_ctx;
@@ -1602,6 +1642,16 @@ int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1,
   if (K4) CK(cudaMemcpyAsync(K4, c->K4, 81 * c->N3 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
   TRY(sync(c));
   return fails ? CPFFT_WARN_LOCAL_FALLBACK : 0;
+}
+
+int cpfft_pass_counts(long long* counts) {
+  TRY(need_ctx());
+  if (!counts) {
+    cpfft_set_error("cpfft_pass_counts: null pointer");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  for (int k = 0; k < 5; k++) counts[k] = g_ctx->last_pass[k];
+  return 0;
 }
 
 int cpfft_set_K4(const double* K4) {
@@ -1749,7 +1799,16 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
     double resfft = 1.0;
     int iiter_EBC = 0;
-    while (resfft > tolNR) {
+    // With the equilibrium test the loop body starts with the stress update, so the
+    // update that follows the last accepted increment (the reference's closing
+    // drive_eps_sig) also evaluates the test: the loop ends there when both tests pass.
+    bool closed = false;  // the state's P is current (the closing update has run)
+    const bool eq_mode = c->eq_tol > 0.0;
+    // backtracking on the equilibrium residual (equilibrium test only): an increment
+    // after which the residual has grown is halved, at most 4 times, before the next solve
+    double eq_prev = HUGE_VAL, frac = 1.0;
+    int halvings = 0;
+    while (eq_mode || resfft > tolNR) {
       a = clk::now();
       long long li;
       int fails;
@@ -1762,6 +1821,28 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       S.local_fallbacks += fails;
       S.stress_updates++;
       TRY(matvec_acc(c, c->P, c->b, 0));
+      if (eq_mode || c->log) {
+        double eq;
+        TRY(equil_residual(c, c->b, &eq));
+        S.res_equil = eq;
+        if (c->log)
+          fprintf(stderr, "       equilibrium residual %10.3e (iteration %d)\n", eq, iiter_EBC);
+        if (eq_mode && resfft <= tolNR && eq <= c->eq_tol) {
+          closed = true;
+          break;
+        }
+        if (eq_mode && iiter_EBC >= 2 && eq > eq_prev && halvings < 4) {
+          frac *= 0.5;
+          CK(dev_axpy(c->Fn1, c->dFm, -frac, n, c->st));
+          halvings++;
+          resfft *= 0.5;
+          if (c->log) fprintf(stderr, "       increment halved (%d)\n", halvings);
+          continue;
+        }
+        eq_prev = eq;
+        halvings = 0;
+        frac = 1.0;
+      }
       CK(dev_scale(c->b, -1.0, n, c->st));
       a = clk::now();
       TRY(cg(c, c->b, c->dFm, tolPCG, &its));
@@ -1782,17 +1863,19 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
       }
       iiter_EBC++;
     }
-    a = clk::now();
-    long long li;
-    int fails;
-    long long pi = 0, rj = 0;
-    TRY(stress(c, step, iiter_EBC, &li, &fails, &pi, &rj));
-    ts += sec(a);
-    S.predict_iters += pi;
-    S.guess_rejected += rj;
-    S.local_iters += li;
-    S.local_fallbacks += fails;
-    S.stress_updates++;
+    if (!closed) {
+      a = clk::now();
+      long long li;
+      int fails;
+      long long pi = 0, rj = 0;
+      TRY(stress(c, step, iiter_EBC, &li, &fails, &pi, &rj));
+      ts += sec(a);
+      S.predict_iters += pi;
+      S.guess_rejected += rj;
+      S.local_iters += li;
+      S.local_fallbacks += fails;
+      S.stress_updates++;
+    }
     CK(dev_sum9(c->P, N3, c->part, c->sc, SC_SUM9, c->st));
     CK(cudaMemcpyAsync(c->h_sc + SC_SUM9, c->sc + SC_SUM9, 9 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
     TRY(sync(c));
@@ -1828,13 +1911,12 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   c->pass_step = 0;
   if (Pbar)
     for (int i = 0; i < 9; i++) Pbar[i] = c->P_bar[i];
-  // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||)
-  TRY(matvec_acc(c, c->P, c->b, 0));
-  double gp;
-  TRY(dnrm2(c, c->b, &gp));
-  double pb = 0;
-  for (int i = 0; i < 9; i++) pb += c->P_bar[i] * c->P_bar[i];
-  S.res_equil = gp / (std::sqrt((double)N3) * std::sqrt(pb));
+  // equilibrium residual ||G(P)|| / (sqrt(N3) ||P_bar||) of the committed state (the
+  // equilibrium test has evaluated it on that state already)
+  if (!c->eq_tol) {
+    TRY(matvec_acc(c, c->P, c->b, 0));
+    TRY(equil_residual(c, c->b, &S.res_equil));
+  }
   S.cg_solves = (int)c->cg_solves;
   S.cg_iters = (int)c->cg_iters;
   S.t_pcg = tp;

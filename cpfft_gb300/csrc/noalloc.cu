@@ -18,6 +18,8 @@
 //    streams, or different host threads on the same device) race; serialise them;
 //  * nothing in the array has to start at zero: each call rewrites the twiddles for its
 //    N and writes every spectral entry before reading it.
+#include <atomic>
+
 #include "fft_green.cuh"
 
 namespace {
@@ -30,8 +32,10 @@ constexpr size_t NOALLOC_WORDS = NOALLOC_SPEC + NOALLOC_MAX_N;  // spectrum + tw
 // cudaGetSymbolAddress in scratch_for_current_device().
 static __device__ __align__(256) double2 g_noalloc_scratch[NOALLOC_WORDS];
 
+// the array's device address per device, looked up once; host threads may race on the
+// first lookup, and each stores the same value
 constexpr int MAX_DEVICES = 64;
-double2* g_scratch_addr[MAX_DEVICES] = {nullptr};
+std::atomic<double2*> g_scratch_addr[MAX_DEVICES];
 
 __global__ void k_twiddles(double2* tw, int N) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -50,7 +54,8 @@ int scratch_for_current_device(double2** out) {
                     e != cudaSuccess ? cudaGetErrorString(e) : "device index out of range");
     return CPFFT_ERR_CUDA;
   }
-  if (!g_scratch_addr[dev]) {
+  double2* addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -58,9 +63,10 @@ int scratch_for_current_device(double2** out) {
                       cudaGetErrorString(e));
       return CPFFT_ERR_CUDA;
     }
-    g_scratch_addr[dev] = static_cast<double2*>(p);
+    addr = static_cast<double2*>(p);
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  *out = g_scratch_addr[dev];
+  *out = addr;
   return 0;
 }
 

@@ -1174,6 +1174,7 @@ __device__ void voxel_update(const StressArgs& a, long long v, bool valid, int& 
         ttrate = tr_sub;
       }
     }
+    if (cuts && a.stats) atomicAdd(a.stats + 4, 1ull);  // a sub-stepped solve (rare)
     // restore the full-step np1 (used by the rotation update below)
     s.tinc = a.dt;
     for (int i = 0; i < 6; i++) s.D[i] = uddt[i];

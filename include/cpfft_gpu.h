@@ -230,6 +230,12 @@ int cpfft_tuning(int* tiles, double* ms);
 int cpfft_stress_update(int step, int iter, const double* Fn, const double* Fn1,
                         double* Pn1, double* K4);
 
+/* Counters of the last stress pass (diagnostic, no counterpart in the reference):
+ * counts[0] local Newton iterations summed over the voxels, [1] voxels whose local solve
+ * failed, [2] predictor iterations summed, [3] starts the solve dropped, [4] voxels whose
+ * solve was sub-stepped (mm10_solve_strup's cuts, src/mm10_a.f:2765-2802). */
+int cpfft_pass_counts(long long* counts);
+
 /*
  * y = G(K4 : x) (flgK = 1) or y = G(x) (flgK = 0): replaces G_K_dF (src/G_K_dF.f:11-87).
  * K4 is the device copy written by the last cpfft_stress_update (or cpfft_set_K4).
@@ -292,6 +298,24 @@ int cpfft_tangent_homo(double tolPCG, double* C_homo);
  */
 int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR,
                    double tolPCG, int maxIter, double* Pbar, cpfft_stats* st);
+
+/*
+ * Equilibrium stop test of the global Newton loop (extension; the reference stops on
+ * ||dF|| / ||F|| <= tolNR alone, src/FFT_nr3.f:107-122).  With tol > 0, cpfft_nr3_step
+ * ends a Newton loop only when that test holds AND the equilibrium residual of the state
+ * reached, ||G(P)|| / (sqrt(N3) ||P_bar||) with G(P) evaluated by the FP64-accurate
+ * operator, is <= tol; while it is not, the loop continues with further Newton iterations
+ * (counted against maxIter).  The stress update that evaluates the test is the
+ * reference's closing drive_eps_sig (src/FFT_nr3.f:123), so a step whose first test
+ * passes costs what the reference's does.  The loop is globalised by backtracking on the
+ * same residual: from the third Newton iteration on, an increment after which the
+ * residual has grown is halved (at most 4 times in a row, each costing one stress update)
+ * before the next Krylov solve.  Without it the reference's undamped iteration can
+ * settle into a cycle (128^3 plane-strain compression, load step 2: ||dF||/||F|| stays
+ * at 6.7e-6, the equilibrium residual near 6e-4).  tol = 0 (the default) restores the
+ * reference's loop.  cpfft_stats.res_equil reports the value of the last test.
+ */
+int cpfft_set_equilibrium_tol(double tol);
 
 /*
  * Start of FFT_nr3 (src/FFT_nr3.f:36-47): the initial drive_eps_sig(1,0) of the

@@ -55,6 +55,8 @@ int  orc_cg(orc_ctx* c, const double* b, double* x, double tol, int* iters);
 int  orc_tangent_homo(orc_ctx* c, double tolPCG, double* C_homo);
 /* FFT_nr3 start (drive_eps_sig(1,0) + tangent_homo) */
 int  orc_nr3_begin(orc_ctx* c, double tolPCG);
+/* the library's equilibrium stop test of the Newton loop (cpfft_set_equilibrium_tol) */
+void orc_set_equilibrium_tol(orc_ctx* c, double tol);
 /* one load step of FFT_nr3 */
 int  orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC,
                   double tolNR, double tolPCG, int maxIter, double* Pbar,

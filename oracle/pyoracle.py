@@ -112,6 +112,7 @@ def lib():
         L.orc_tangent_homo.argtypes = [vp, d, dp]
         L.orc_nr3_begin.restype = i
         L.orc_nr3_begin.argtypes = [vp, d]
+        L.orc_set_equilibrium_tol.argtypes = [vp, d]
         L.orc_nr3_step.restype = i
         L.orc_nr3_step.argtypes = [vp, i, dp, ip, d, d, i, dp, P(Stats)]
         L.orc_get_fields.argtypes = [vp, dp, dp, dp, dp, dp]
@@ -204,6 +205,9 @@ class Oracle:
         C = np.zeros(81)
         rc = lib().orc_tangent_homo(self.h, tol, _p(C))
         return C.reshape(9, 9).T.copy(), rc  # C[i, j] = C_homo(i, j) (Fortran)
+
+    def set_equilibrium_tol(self, tol):
+        lib().orc_set_equilibrium_tol(self.h, float(tol))
 
     def nr3_begin(self, tolPCG):
         return lib().orc_nr3_begin(self.h, tolPCG)

@@ -13,7 +13,8 @@ Runs where the reference tree is mounted; the .npz files are committed so the te
 no reference files.  Material values are stored as the reference holds them: single
 precision (matprp is `real`, src/mod_fft.f:20), widened to double.
 
-    python tests/golden/make_example_decks.py [path/to/examples]
+    python tests/golden/make_example_decks.py path/to/reference/examples
+    (or with the directory in the environment variable CPFFT_REFERENCE_EXAMPLES)
 """
 import os
 import re
@@ -24,7 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-EXAMPLES = "/root/reference/examples"
+EXAMPLES = os.environ.get("CPFFT_REFERENCE_EXAMPLES")
 KEYS = ("e", "nu", "yld_pt", "tan_e", "beta")
 
 
@@ -170,5 +171,8 @@ def mm10_deck(examples):
 
 if __name__ == "__main__":
     ex = sys.argv[1] if len(sys.argv) > 1 else EXAMPLES
+    if not ex:
+        sys.exit("usage: make_example_decks.py <reference examples directory> "
+                 "(or set CPFFT_REFERENCE_EXAMPLES)")
     mm01_deck(ex)
     mm10_deck(ex)

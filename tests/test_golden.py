@@ -3,7 +3,7 @@ CPU oracle on small seeded cases).
 
 CPU tests: the oracle still reproduces its frozen outputs.  GPU tests: the C-ABI library
 matches them with the parity tolerances (1e-8 per voxel for the stress update and the
-load step's fields, 1e-11 for the Green operator, 1e-9 for P_bar), reading nothing but
+load step's fields, 1e-11 for the Green operator, 1e-10 for P_bar), reading nothing but
 the fixtures."""
 import os
 
@@ -128,7 +128,7 @@ def test_gpu_load_golden(gpulib):
         for step in (1, 2, 3):
             rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 20)
             assert rc == 0
-            assert rel(Pbar, d["Pbar"][step - 1]) < 1e-9
+            assert rel(Pbar, d["Pbar"][step - 1]) < 1e-10
             assert st["newton_iters"] == d["newton"][step - 1]
         F, P = s.fields()
         assert per_voxel_rel(P, d["Pn1"]) < 1e-8
