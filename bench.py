@@ -1,13 +1,16 @@
 #!/usr/bin/env python
 """Headline benchmark: voxel stress-updates/s and s/load-step of the finite-strain FFT
-crystal-plasticity hot path at 128^3 (the workload the metric is quoted on).
+crystal-plasticity hot path at 128^3 (the workload the metric is quoted on), fast form
+against the plain FP64 form on the GPU.
 
 Workload: 128^3 voxels, 256 periodic-Voronoi grains (seed 3) with Haar-random
 orientations, FCC mm10 Voce material, plane-strain compression at 1e-3 per load step
 (F_zz prescribed, F_yy = 1, shear F held at zero, other P zero), local Newton 1e-10,
-global NR 1e-5 (--tol-nr), CG 1e-10.  Synthetic inputs (no dataset).  A "step" is one whole load
-step of FFT_nr3 (Newton-Krylov to convergence, the P_bar loop with its homogenised
-tangents, and the state roll-over) through the C-ABI's resident entry point.
+global NR 1e-6, CG 1e-10, and the equilibrium residual ||G(P)|| / (sqrt(N^3) ||P_bar||)
+<= 1e-6 at the end of every Newton loop (cpfft_set_equilibrium_tol, both forms).
+Synthetic inputs (no dataset).  A "step" is one whole load step of FFT_nr3 (Newton-Krylov
+to convergence, the P_bar loop with its homogenised tangents, and the state roll-over)
+through the C-ABI's resident entry point.
 
 value  = N^3 x (stress-update passes in the timed steps) / device time of those steps
          (CUDA events on the library's stream), whole job over ranks (replicas).
@@ -15,10 +18,15 @@ e2e    = the same units over host wall time of each step plus copying the step's
          result fields Fn1, Pn1 back to pinned host buffers.
 Inputs larger than L2: every field is >= 150 MB (9 x 128^3 FP64), K4 is 1.4 GB.
 
-Modes (--mode): learned (default; the workload's configuration) = FP32 Krylov under the
-FP64 residual plus the learned initial guess of the local solves, whose network is
-trained before the timed steps on pairs logged from a 64^3 RVE of another seed
-(train_guess); mixed = the same without the learned guess; fp64 = the plain form.
+Forms (--mode): mixed (default) = FP32 Krylov inner iterations (reference-medium
+preconditioned) under FP64-accurate outer residuals, local solves started at the previous
+global iterate or the return-mapped elastic trial, FP32 consistent tangent; learned = the
+same with the learned initial guess in place of the trial start (its network trained
+before the timed steps on pairs logged from 64^3 RVEs of other seeds); fp64 = the plain
+form.  Unless --no-fp64, the plain FP64 form then runs the same warm-up and the first
+--fp64-steps timed steps: its s/step, the speed-up over it and the fast form's error
+against it (P_bar of every step, P per voxel) go into the line under "vs_fp64".
+--workload config5 runs the 256^3 cyclic workload the same way.
 
 `--impl reference` times the CPU stand-in of the reference (the C++ oracle, OpenMP on
 all host cores) on bounded samples of the same workload (see cpu_sample()).
@@ -110,129 +118,370 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def load_traffic():
-    """Per-launch DRAM traffic from the committed ncu summaries (bytes per voxel)."""
-    try:
-        with open(os.path.join(HERE, "profiles", "traffic_per_voxel.json")) as f:
-            return json.load(f)
-    except OSError:
-        return {}
+# DRAM traffic per launch of the kernels the roofline can name, per voxel, from ncu
+# captures on a GB300 (not measurable inside this run; each figure names its capture)
+TRAFFIC = {
+    "green32": (577.6, "profiles/traffic_plane_strain_128.md: ncu dram bytes of the 5 FP32 "
+                       "passes at 128^3"),
+    "green64": (1259.0, "profiles/traffic_plane_strain_128.md: ncu dram bytes of the 5 FP64 "
+                        "passes at 128^3"),
+    "stress": (21400.0, "profiles/stress_kernel_64.md: ncu dram bytes per voxel of an "
+                        "implicit stress_kernel launch at 64^3 (register spills included)"),
+}
 
 
-def train_guess(cp, N=64, grains=64, seed=100, steps=5, stride=3, epochs=4):
+def train_guess(cp, seeds=(100, 101, 102), N=64, grains=64, steps=8, stride=2, epochs=4):
     """The learned initial guess: log (features, converged increments) of the plain local
-    solves on a 64^3 RVE with another seed (every `stride`-th voxel, `steps` load steps of
-    the same loading, mixed precision), then train the network with the tcgen05 kernels.
-    Outside the timed region."""
+    solves on 64^3 RVEs of other seeds (every `stride`-th voxel, the first `steps` load
+    steps of the same loading, mixed precision), then train the network with the tcgen05
+    kernels.  Outside the timed region."""
     from cpfft_gb300 import rve
     t0 = time.perf_counter()
-    r = rve.make_rve(N, grains, seed)
     load = rve.plane_strain_compression(0.10, 100)
-    s = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, cp.PREC_MIXED)
-    try:
-        s.learn_log(N ** 3 * 10 * steps // stride, stride)
-        s.nr3_begin(1e-10)
-        done = 0
-        for step in range(1, steps + 1):
-            try:
-                # every local solve of every pass is a valid pair; a looser global
-                # tolerance only shortens the run
-                s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-4, 1e-10, 20)
-            except cp.CpfftError:
-                break  # a global Newton limit cycle ends the logging run; keep its pairs
-            done = step
-        X, T = s.learn_fetch()
-    finally:
-        s.close()
+    Xs, Ts, runs = [], [], []
+    for seed in seeds:
+        r = rve.make_rve(N, grains, seed)
+        s = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, cp.PREC_MIXED)
+        try:
+            s.learn_log(N ** 3 * 12 * steps // stride, stride, seed % stride)
+            s.nr3_begin(1e-10)
+            done = 0
+            for step in range(1, steps + 1):
+                try:
+                    # every local solve of every pass is a valid pair; a looser global
+                    # tolerance only shortens the run
+                    s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-4, 1e-10, 20)
+                except cp.CpfftError:
+                    break  # a global Newton limit cycle ends the logging run; keep its pairs
+                done = step
+            X, T = s.learn_fetch()
+        finally:
+            s.close()
+        Xs.append(X)
+        Ts.append(T)
+        runs.append(f"seed {seed}: {done} steps, {X.shape[0]} pairs")
+    X = np.concatenate(Xs)
+    T = np.concatenate(Ts)
     t1 = time.perf_counter()
-    m = cp.Mlp(seed)
-    loss = m.train(X, T, epochs=epochs, batch_tiles=32, lr=2e-3, seed=seed)
-    return {"pairs": int(X.shape[0]), "rve": f"{N}^3, {grains} grains, seed {seed}, {done} steps",
+    m = cp.Mlp(seeds[0])
+    loss = m.train(X, T, epochs=epochs, batch_tiles=32, lr=2e-3, seed=seeds[0])
+    return {"pairs": int(X.shape[0]), "rves": f"{N}^3, {grains} grains", "runs": runs,
             "epochs": epochs, "loss": loss, "t_log_s": t1 - t0,
             "t_train_s": time.perf_counter() - t1}
 
 
-def start_flags(cp, args):
+def start_flags(cp, form, args):
     """Start of the local solves: the reference's predictor in the plain FP64 form; the
     previous global iterate where there is one, else the learned guess (learned) or the
     return-mapped elastic trial (mixed), in the fast forms."""
-    if args.mode == "fp64":
+    if form == "fp64":
         return cp.START_PLAIN
-    first = cp.START_LEARNED if args.mode == "learned" else cp.START_TRIAL
+    first = cp.START_LEARNED if form == "learned" else cp.START_TRIAL
     return (first | (cp.START_ITERATE if args.start_iterate else 0) |
             (cp.TANGENT_F32 if args.tangent == "f32" else 0))
 
 
-def workload(N, grains, seed):
+def workload(args):
+    """The RVE and loading of --workload: the 128^3 plane-strain workload (N, grains and
+    seed from the arguments), or the 256^3 cyclic workload."""
     from cpfft_gb300 import rve
-    r = rve.make_rve(N, grains, seed)
-    load = rve.plane_strain_compression(0.10, 100)
+    if args.workload == "config5":
+        r = rve.make_rve(256, 2048, 4)
+        load = rve.cyclic_uniaxial(0.02, 2, 160)
+    else:
+        r = rve.make_rve(args.N, args.grains, args.seed)
+        load = rve.plane_strain_compression(0.10, 100)
     return r, load
 
 
-def cpu_sample(r, load, steps_hint, nthreads, n_stress_sample, n_green):
-    """CPU stand-in of the reference on a bounded sample of the same workload: the oracle
-    stress update on `n_stress_sample` voxels of the 128^3 RVE (after the first load
-    increment, Newton iteration 1) and `n_green` full-grid FP64 G(K:x) applies; a load
-    step is extrapolated with the per-step pass counts `steps_hint`
-    (stress-update passes, matvecs)."""
+def make_solver(cp, r, form, args):
+    prec = cp.PREC_FP64 if form == "fp64" else cp.PREC_MIXED
+    s = cp.Solver(r.N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
+    s.set_mode(prec, start_flags(cp, form, args))
+    if form != "fp64":
+        if args.schedule == "queue":
+            s.set_schedule(cp.SCHED_QUEUE)
+        if args.precond == "reference":
+            s.set_precond(cp.PRECOND_REFERENCE)
+    if args.tol_equil > 0:
+        s.set_equilibrium_tol(args.tol_equil)
+    return s
+
+
+def device_bytes_in_use(torch):
+    free, total = torch.cuda.mem_get_info()
+    return total - free
+
+
+def run_form(cp, r, load, form, args, world, local, steps=None, keep_step=None):
+    """`warmup` untimed and `steps` (default args.steps) timed load steps of one form.
+    Device time: CUDA events on the library's stream around each step
+    (cpfft_stats.t_device); e2e: host wall clock of each step plus the copy of its result
+    fields Fn1, Pn1 to pinned host buffers.  Returns the statistics, P_bar of every step,
+    the last step's F and P, the P field after load step `keep_step`, and the device
+    memory the context holds."""
+    import torch
+    steps = args.steps if steps is None else steps
+    N3 = r.N ** 3
+    torch.cuda.synchronize()
+    mem0 = device_bytes_in_use(torch)
+    solver = make_solver(cp, r, form, args)
+    tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, args.max_iter
+    solver.nr3_begin(tolPCG)
+    step = 0
+    pbars, warm_stats = [], []
+    for _ in range(args.warmup):
+        step += 1
+        rc, Pb, st = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG,
+                                     maxIter)
+        pbars.append(Pb)
+        warm_stats.append(st)
+    mem = device_bytes_in_use(torch) - mem0
+    Fh = torch.empty((9, N3), dtype=torch.float64).pin_memory()
+    Ph = torch.empty((9, N3), dtype=torch.float64).pin_memory()
+    Fp = ctypes.cast(Fh.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    Pp = ctypes.cast(Ph.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    L = cp.load_library()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.profiler.start()  # marks the timed region for `ncu --profile-from-start off`
+    stats, t_e2e, P_keep = [], 0.0, None
+    for _ in range(steps):
+        step += 1
+        t0 = time.perf_counter()
+        rc, Pbar, st = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG,
+                                       maxIter)
+        if L.cpfft_sync_to_host(Fp, Pp, None) != 0:
+            raise RuntimeError("sync_to_host failed")
+        t_e2e += time.perf_counter() - t0
+        stats.append(st)
+        pbars.append(Pbar)
+        if step == keep_step:
+            P_keep = Ph.numpy().copy()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    return {"form": form, "solver": solver, "N3": N3, "stats": stats, "warm_stats": warm_stats,
+            "pbars": pbars, "P_last": Ph.numpy().copy(), "F_last": Fh.numpy().copy(),
+            "P_keep": P_keep, "t_e2e": t_e2e, "t_dev": sum(s["t_device"] for s in stats),
+            "clocks": clk, "last_step": step, "device_bytes": mem}
+
+
+def counts(run):
+    st = run["stats"]
+    n = len(st)
+    su = sum(s["stress_updates"] for s in st)
+    N3 = run["N3"]
+    return {"stress_passes_per_step": su / n,
+            "matvecs_per_step": sum(s["n_green32"] + s["n_green64"] for s in st) / n,
+            "newton": [s["newton_iters"] for s in st], "nbc": [s["nbc_iters"] for s in st],
+            "cg_iters": [s["cg_iters"] for s in st],
+            "res_equil": [s["res_equil"] for s in st], "res_fft": [s["res_fft"] for s in st],
+            "local_iters_per_voxel_pass": sum(s["local_iters"] for s in st) / (N3 * su),
+            "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in st) / (N3 * su),
+            "local_fallbacks": sum(s["local_fallbacks"] for s in st)}
+
+
+def roofline(run, N, peaks, peak_kind, fp64_peak):
+    """The dominant kernel of the timed steps by summed CUDA-event time, and its average
+    launch time against its roofline."""
+    st = run["stats"]
+    N3 = N ** 3
+    su = sum(s["stress_updates"] for s in st)
+    ng32_all = sum(s["n_green32"] for s in st)
+    ng32 = sum(s["n_green32_timed"] for s in st)
+    tg32_timed = sum(s["t_green32"] for s in st)
+    # FP32 applies: the timed ones (first iteration of each CG segment, restarts) give the
+    # per-launch time; the rest run inside the iteration graph (t_cg_graph)
+    tg32 = tg32_timed / max(ng32, 1) * ng32_all
+    tg64 = sum(s["t_green64"] for s in st)
+    tsk = sum(s["t_stress_kernel"] for s in st)
+    ng64 = sum(s["n_green64"] for s in st)
+    kern = max([("green32", tg32), ("green64", tg64), ("stress", tsk)], key=lambda kv: kv[1])[0]
+    if kern == "green32":
+        per = tg32_timed / ng32
+        ach = BYTES_GREEN32 * N3 / per / 1e9
+        roof = {"kernel": "fp32 G(K:x) (5 passes)", "bound": "hbm", "achieved": ach,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+                "peak_source": f"{peak_kind} hbm_gbs",
+                "algorithmic_bytes_per_launch": BYTES_GREEN32 * N3, "avg_launch_ms": per * 1e3}
+    elif kern == "green64":
+        per = tg64 / ng64
+        ach = fft_flops_per_voxel(N) * N3 / per / 1e12
+        roof = {"kernel": "FP64-accurate G(K:x) (5 passes)", "bound": "fp64", "achieved": ach,
+                "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "peak_source": "measured DFMA rate on this GPU (cpfft_measure_fp64_peak)",
+                "algorithmic_flops_per_launch": fft_flops_per_voxel(N) * N3,
+                "avg_launch_ms": per * 1e3}
+    else:
+        per = tsk / su
+        ach = BYTES_STRESS * N3 / per / 1e9
+        roof = {"kernel": "stress update (mm10 + cep2A)", "bound": "hbm", "achieved": ach,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
+                "peak_source": f"{peak_kind} hbm_gbs; the kernel is FP64-pipe bound",
+                "algorithmic_bytes_per_launch": BYTES_STRESS * N3, "avg_launch_ms": per * 1e3}
+    tv, tsrc = TRAFFIC[kern]
+    roof["traffic"] = tv * N3
+    roof["traffic_source"] = tsrc
+    split = {"stress_s": tsk, "green64_s": tg64, "green32_s_estimated": tg32,
+             "n_green64": ng64, "n_green32": ng32_all, "n_green32_timed": ng32,
+             "green32_timed_s": tg32_timed, "cg_graph_s": sum(s["t_cg_graph"] for s in st),
+             "stress_passes": su,
+             "note": "green64 = FP64-accurate applies (double-float in the fast forms); "
+                     "green32_s_estimated = timed per-apply time x all FP32 applies (most "
+                     "run inside the CG iteration graph, whose whole time is cg_graph_s)"}
+    return roof, split
+
+
+def start_comparison(cp, run, load, args):
+    """Local Newton iterations per voxel of the first implicit stress pass of the next load
+    step (initial guess F_n+1 = F_n + the step's prescribed increment), from the state the
+    timed steps left, with each start of the local solves: the reference's predictor, the
+    return-mapped elastic trial and (when trained) the learned guess.  Same state, one
+    stress pass each, untimed."""
+    s = run["solver"]
+    step = run["last_step"] + 1
+    F, _ = s.fields()
+    d = load.BC_all[step - 1] - load.BC_all[step - 2]
+    F1 = F + d[:, None]
+    out = {}
+    starts = [("reference", cp.START_PLAIN), ("trial", cp.START_TRIAL)]
+    if args.learned_trained:
+        starts.append(("learned", cp.START_LEARNED))
+    for name, flag in starts:
+        s.set_mode(cp.PREC_MIXED, flag)
+        s.drive_eps_sig(step, 1, F, F1, want_P=False)
+        c = s.pass_counts()
+        out[name] = {"local_iters_per_voxel": c["local_iters"] / s.N3,
+                     "predictor_iters_per_voxel": c["predict_iters"] / s.N3,
+                     "total_per_voxel": (c["local_iters"] + c["predict_iters"]) / s.N3,
+                     "fallbacks": c["fallbacks"], "starts_dropped": c["starts_dropped"]}
+    out["state"] = f"after load step {step - 1}, first implicit pass of step {step}"
+    return out
+
+
+def cpu_sample(r, load, nthreads, n_sample, state=None, step=None, green=True):
+    """The CPU port of the reference (the C++ oracle, OpenMP) on a bounded sample of the
+    workload: the stress update of `n_sample` voxels and one full-grid FP64 G(K:x).
+
+    state = (F, history) of a committed load step from the GPU run: the sample updates
+    that plastic state to F + the next step's prescribed increment (the next step's first
+    implicit pass).  Without it (the reference arm, no GPU run) the sample voxels are driven
+    along the workload's homogeneous path (F_zz, F_yy prescribed, F_xx = 1/F_zz, no shear)
+    for `step - 1` steps and the timed pass is that of step `step`."""
     from oracle import pyoracle as po
     N = r.N
     N3 = N ** 3
+    v0 = N3 // 2
+    v1 = min(N3, v0 + n_sample)
     o = po.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 1, nthreads=nthreads)
     try:
-        # homogeneous first increment of the loading as the sample's F field
-        Fn = np.zeros((9, N3))
-        Fn[[0, 4, 8]] = 1.0
-        Fn1 = np.repeat(load.BC_all[0][:, None], N3, axis=1)
-        o.set_fields(Fn, Fn1)
+        if state is not None:
+            F, H = state
+            o.set_history_n(np.ascontiguousarray(H))
+            d = load.BC_all[step - 1] - load.BC_all[step - 2]
+            o.set_fields(np.ascontiguousarray(F), np.ascontiguousarray(F + d[:, None]))
+        else:
+            Fh = np.zeros(9)
+            Fh[[0, 4, 8]] = 1.0
+            for s in range(1, step + 1):
+                bc = load.BC_all[s - 1]
+                Fn1 = np.array([1.0 / bc[8], 0, 0, 0, bc[4], 0, 0, 0, bc[8]])
+                Fa = np.repeat(Fh[:, None], N3, axis=1)
+                Fb = np.repeat(Fn1[:, None], N3, axis=1)
+                o.set_fields(Fa, Fb)
+                if s < step:
+                    o.stress_sample(s, 1, v0, v1)
+                    o.stress_sample(s, 2, v0, v1)
+                    o.commit()
+                Fh = Fn1
         t0 = time.perf_counter()
-        o.stress_sample(1, 1, 0, n_stress_sample)
-        t_su = (time.perf_counter() - t0) * N3 / n_stress_sample
-        x = np.random.default_rng(0).standard_normal((9, N3))
-        t0 = time.perf_counter()
-        for _ in range(n_green):
+        o.stress_sample(step, 1, v0, v1)
+        t_su = (time.perf_counter() - t0) * N3 / (v1 - v0)
+        t_mv = None
+        if green:
+            x = np.random.default_rng(0).standard_normal((9, N3))
+            t0 = time.perf_counter()
             o.green(x, True)
-        t_mv = (time.perf_counter() - t0) / n_green
+            t_mv = time.perf_counter() - t0
     finally:
         o.close()
-    su, mv = steps_hint
-    t_step = su * t_su + mv * t_mv
-    return {"t_stress_full_grid": t_su, "t_matvec": t_mv, "t_load_step": t_step,
-            "value": N3 * su / t_step}
+    return {"t_stress_full_grid": t_su, "t_matvec": t_mv, "voxels": v1 - v0}
+
+
+def cpu_whole_steps(nthreads, nsteps=3):
+    """Whole load steps of the CPU port, timed (not extrapolated): the 16^3 uniaxial-tension
+    workload (8 grains, seed 1, 2 % in 20 steps; global NR 1e-6, CG 1e-10), its first
+    `nsteps` steps."""
+    from cpfft_gb300 import rve
+    from oracle import pyoracle as po
+    r = rve.make_rve(16, 8, 1)
+    load = rve.uniaxial_tension(0.02, 20)
+    o = po.Oracle(16, r.mat_list, r.kocks, r.crystals, 1.0, 1, nthreads=nthreads)
+    try:
+        t0 = time.perf_counter()
+        o.nr3_begin(1e-10)
+        su = 0
+        for s in range(1, nsteps + 1):
+            rc, _, st = o.nr3_step(s, load.BC_all[s - 1], load.isNBC, 1e-6, 1e-10, 20)
+            su += st["stress_updates"]
+        t = time.perf_counter() - t0
+    finally:
+        o.close()
+    return {"workload": "16^3, 8 grains (seed 1), uniaxial tension, NR 1e-6, CG 1e-10",
+            "steps": nsteps, "s_per_load_step": t / nsteps,
+            "voxel_updates_per_s": 4096 * su / t, "cores": nthreads}
 
 
 def reference_arm(args):
+    """The CPU port of the reference (the oracle with OpenMP on all host cores) on the
+    workload's metric.  A 128^3 load step of the port takes about an hour, so each timed
+    step is a bounded sample, extrapolated to a load step (labelled as such), next to whole
+    load steps of the 16^3 workload timed in full."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    N = args.N
-    r, load = workload(N, args.grains, args.seed)
-    hint = workload_counts()
+    r, load = workload(args)
+    N = r.N
     nthreads = os.cpu_count()
+    su_step, mv_step = REF_COUNTS
     vals = []
     t_total = 0.0
+    t_mv = None
     for s in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        res = cpu_sample(r, load, hint, nthreads, n_stress_sample=max(4096, N ** 3 // 64),
-                         n_green=1)
+        res = cpu_sample(r, load, nthreads, max(4096, N ** 3 // 256), step=6,
+                         green=(s == 0))
+        if s == 0:
+            t_mv = res["t_matvec"]
         t_total += time.perf_counter() - t0
         if s >= args.warmup:
-            vals.append(res)
-    v = statistics.median([x["value"] for x in vals])
-    tstep = statistics.median([x["t_load_step"] for x in vals])
+            vals.append(su_step * res["t_stress_full_grid"] + mv_step * t_mv)
+    tstep = statistics.median(vals)
+    v = N ** 3 * su_step / tstep
+    small = cpu_whole_steps(nthreads)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "voxel stress-updates/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tstep, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_dict(args, "reference"),
+        "extrapolated": True,
         "cpu_baseline": {"value": v, "unit": "voxel stress-updates/s", "cores": nthreads,
                          "kind": "port",
                          "sample": (f"C++ oracle (restatement of the Fortran+MKL path, OpenMP "
-                                    f"{nthreads} threads): stress update on N^3/64 voxels and one "
-                                    f"full-grid FP64 G(K:x) at {N}^3, extrapolated to a load step "
-                                    f"with {hint[0]} stress passes and {hint[1]} matvecs per step")},
+                                    f"{nthreads} threads) at {N}^3: each step times the stress "
+                                    f"update of N^3/256 voxels in a plastic state (load step 6 "
+                                    f"of the workload's homogeneous path); with one full-grid "
+                                    f"FP64 G(K:x) ({t_mv:.2f} s) the load step is EXTRAPOLATED "
+                                    f"with the plain form's counts ({su_step} stress passes, "
+                                    f"{mv_step} matvecs per step)")},
+        "timed_small_workload": small,
         "e2e": {"value": v, "unit": "voxel stress-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "s_per_load_step": tstep,
@@ -243,37 +492,36 @@ def reference_arm(args):
 
 
 METRIC = "voxel stress-updates/s and s/load-step at 128^3: learned+mixed vs plain FP64 on GPU"
-
-
-def workload_counts():
-    """Stress-update passes and FP64-equivalent matvecs of one load step of this
-    workload, as measured by the GPU run (profiles/workload_counts.json), else the
-    values of the first measurement."""
-    try:
-        with open(os.path.join(HERE, "profiles", "workload_counts.json")) as f:
-            d = json.load(f)
-            return d["stress_updates_per_step"], d["matvecs_per_step"]
-    except OSError:
-        return 17, 5700
+# stress passes and FP64 G(K:x) applies per load step of the plain FP64 form on the 128^3
+# workload (NR 1e-6 and the equilibrium test at 1e-6), from its GPU runs; the gb300 arm
+# measures them in the run itself, the reference arm (no GPU) uses these
+REF_COUNTS = (15, 4290)
 
 
 def config_dict(args, impl):
-    return {"workload": f"plane-strain compression 10%/100 steps, {args.N}^3 voxels, "
-                        f"{args.grains} Voronoi grains (seed {args.seed}), FCC mm10 Voce",
-            "N": args.N, "grains": args.grains, "seed": args.seed,
-            "mode": args.mode if impl != "reference" else "fp64",
-            "precond": (args.precond if impl != "reference" and args.mode != "fp64"
-                        else "none (the reference's fftPcg)"),
-            "local_start": ({"fp64": "reference predictor", "mixed": "return-mapped elastic trial",
-                             "learned": "return-mapped learned guess"}[args.mode if impl != "reference" else "fp64"]
+    fast = impl != "reference"
+    r_desc = ("cyclic uniaxial tension/compression +-2 % (2 cycles in 160 steps), 256^3 "
+              "voxels, 2048 Voronoi grains (seed 4), FCC mm10 Voce"
+              if args.workload == "config5" else
+              f"plane-strain compression 10%/100 steps, {args.N}^3 voxels, "
+              f"{args.grains} Voronoi grains (seed {args.seed}), FCC mm10 Voce")
+    return {"workload": r_desc,
+            "N": 256 if args.workload == "config5" else args.N,
+            "grains": 2048 if args.workload == "config5" else args.grains,
+            "seed": 4 if args.workload == "config5" else args.seed,
+            "mode": args.mode if fast else "fp64",
+            "precond": (args.precond if fast else "none (the reference's fftPcg)"),
+            "local_start": ({"mixed": "return-mapped elastic trial",
+                             "learned": "return-mapped learned guess"}[args.mode]
                             + (", previous global iterate where available"
-                               if impl != "reference" and args.mode != "fp64" and args.start_iterate
-                               else "")),
+                               if args.start_iterate else ""))
+                           if fast and args.mode != "fp64" else "reference predictor",
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
-            "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10},
+            "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10,
+                           "equilibrium": args.tol_equil},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
-            "stress_schedule": args.schedule if impl != "reference" and args.mode != "fp64" else "blocks",
-            "tangent": args.tangent if impl != "reference" and args.mode != "fp64" else "f64",
+            "stress_schedule": args.schedule if fast else "blocks",
+            "tangent": args.tangent if fast else "f64",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -290,122 +538,92 @@ def gb300_arm(args):
     cp.load_library()
     fp64_peak = cp.measure_fp64_peak()
     peaks, peak_kind = load_peaks()
-    N = args.N
+    r, load = workload(args)
+    N = r.N
     N3 = N ** 3
-    r, load = workload(N, args.grains, args.seed)
-    learned = train_guess(cp) if args.mode == "learned" else None
-    prec = cp.PREC_FP64 if args.mode == "fp64" else cp.PREC_MIXED
-    solver = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, prec)
-    solver.set_mode(prec, start_flags(cp, args))
-    if args.schedule == "queue" and args.mode != "fp64":
-        solver.set_schedule(cp.SCHED_QUEUE)
-    if prec == cp.PREC_MIXED and args.precond == "reference":
-        solver.set_precond(cp.PRECOND_REFERENCE)
-    tolNR, tolPCG, maxIter = args.tol_nr, 1e-10, 20
-    solver.nr3_begin(tolPCG)
-    step = 0
-    pbars = []  # P_bar of every step (the stress-strain curve), for --compare-fp64
-    for _ in range(args.warmup):
-        step += 1
-        rc, Pb, _ = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
-        pbars.append(Pb)
-    # pinned host buffers for the e2e copies of each step's result fields
-    Fh = torch.empty((9, N3), dtype=torch.float64).pin_memory()
-    Ph = torch.empty((9, N3), dtype=torch.float64).pin_memory()
-    Fp = ctypes.cast(Fh.data_ptr(), ctypes.POINTER(ctypes.c_double))
-    Pp = ctypes.cast(Ph.data_ptr(), ctypes.POINTER(ctypes.c_double))
-    L = cp.load_library()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    # marks the timed region for `ncu --profile-from-start off`; no effect otherwise
-    torch.cuda.profiler.start()
-    stats = []
-    t_e2e = 0.0
-    for _ in range(args.steps):
-        step += 1
-        t0 = time.perf_counter()
-        rc, Pbar, st = solver.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG,
-                                       maxIter)
-        if L.cpfft_sync_to_host(Fp, Pp, None) != 0:
-            raise RuntimeError("sync_to_host failed")
-        t_e2e += time.perf_counter() - t0
-        stats.append(st)
-        pbars.append(Pbar)
-    torch.cuda.synchronize()
-    torch.cuda.profiler.stop()
-    if world > 1:
-        torch.distributed.barrier()
-    clk = clocks.stop()
-    t_dev = sum(s["t_device"] for s in stats)
-    su = sum(s["stress_updates"] for s in stats)
-    units = float(N3 * su)
+    learned = None
+    args.learned_trained = False
+    if args.mode == "learned" or args.compare_starts:
+        learned = train_guess(cp)
+        args.learned_trained = True
+    # the plain FP64 form runs the same warm-up and the first `fp64_steps` of the timed steps
+    n64 = min(args.steps, args.fp64_steps)
+    fast = run_form(cp, r, load, args.mode, args, world, local, keep_step=args.warmup + n64)
+    su = sum(s["stress_updates"] for s in fast["stats"])
     from cpfft_gb300 import replicas
-    tmax, temax, units_all = replicas.reduce_timings(t_dev, t_e2e, units, device="cuda")
+    tmax, temax, units_all = replicas.reduce_timings(fast["t_dev"], fast["t_e2e"],
+                                                     float(N3 * su), device="cuda")
+    roof, split = roofline(fast, N, peaks, peak_kind, fp64_peak)
+    starts = start_comparison(cp, fast, load, args) if args.compare_starts else None
+    tuned = fast["solver"].tuning()
+    qchunk = fast["solver"].queue_chunk()
+    _, _, H = fast["solver"].fields(history=True)
+    fast_state = (fast["F_last"], H)
+    fast_step = fast["last_step"]
+    fast["solver"].close()
+    fast["solver"] = None
+    plain = None
+    comparison = None
+    if world == 1 and not args.no_fp64 and args.mode != "fp64" and n64 > 0:
+        plain = run_form(cp, r, load, "fp64", args, world, local, steps=n64)
+        plain_t = plain["t_dev"] / n64
+        fast_t = sum(s["t_device"] for s in fast["stats"][:n64]) / n64
+        rel = [float(np.abs(a - b).max() / np.abs(b).max())
+               for a, b in zip(fast["pbars"], plain["pbars"])]
+        P, Pf = plain["P_last"], fast["P_keep"]
+        scale = np.maximum(np.abs(P).max(axis=0), 1e-6 * np.abs(P).max())
+        eq_fast = [s["res_equil"] for s in fast["stats"]]
+        eq_plain = [s["res_equil"] for s in plain["stats"]]
+        pc = counts(plain)
+        proof, _ = roofline(plain, N, peaks, peak_kind, fp64_peak)
+        plain["solver"].close()
+        comparison = {
+            "steps_compared": f"timed steps {args.warmup + 1}-{args.warmup + n64}",
+            "fp64_s_per_load_step": plain_t,
+            "fast_s_per_load_step": fast_t,
+            "speedup_vs_fp64": plain_t / fast_t,
+            "target_speedup": 2.0,
+            "fp64_value": N3 * sum(s["stress_updates"] for s in plain["stats"]) / plain["t_dev"],
+            "fp64_e2e_s_per_load_step": plain["t_e2e"] / n64,
+            "error_vs_fp64": {
+                "pbar_rel_per_step": rel, "pbar_rel_max": max(rel),
+                "p_rel_max_per_voxel": float((np.abs(Pf - P).max(axis=0) / scale).max()),
+                "p_field_step": args.warmup + n64,
+                "target": 1e-6,
+                "steps": f"P_bar: load steps 1-{len(rel)} (warm-up and timed)"},
+            "res_equil": {"fast": eq_fast, "fp64": eq_plain,
+                          "max": max(eq_fast + eq_plain), "target": 1e-6},
+            "fp64_counts": pc, "fp64_roofline": proof, "fp64_clocks": plain["clocks"],
+            "fp64_device_bytes_per_voxel": plain["device_bytes"] / N3,
+            "fp64_form": "plain FP64: FP64 CG (the reference's fftPcg), FP64 Green passes, the "
+                         "reference's local starts, FP64 tangent"}
     if rank != 0:
-        solver.close()
         return 0
-    # roofline of the dominant kernel (largest summed event time in the timed steps)
-    # FP32 applies: the timed ones (first iteration of each CG segment, restarts) give the
-    # per-launch time; the rest run inside the iteration graph, whose time is t_cg_graph
-    ng32_all = sum(s["n_green32"] for s in stats)
-    ng32 = sum(s["n_green32_timed"] for s in stats)
-    tg32_timed = sum(s["t_green32"] for s in stats)
-    tg32 = tg32_timed / max(ng32, 1) * ng32_all
-    tcg = sum(s["t_cg_graph"] for s in stats)
-    tg64 = sum(s["t_green64"] for s in stats)
-    tsk = sum(s["t_stress_kernel"] for s in stats)
-    ng64 = sum(s["n_green64"] for s in stats)
-    traffic = load_traffic()
-    kern = max([("green32", tg32), ("green64", tg64), ("stress", tsk)], key=lambda kv: kv[1])[0]
-    if kern == "green32":
-        per = tg32_timed / ng32
-        ach = BYTES_GREEN32 * N3 / per / 1e9
-        roof = {"kernel": "fp32 G(K:x) (5 passes)", "bound": "hbm", "achieved": ach,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-                "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": traffic.get("green32", None) and traffic["green32"] * N3,
-                "algorithmic_bytes_per_launch": BYTES_GREEN32 * N3, "avg_launch_ms": per * 1e3}
-    elif kern == "green64":
-        per = tg64 / ng64
-        ach = fft_flops_per_voxel(N) * N3 / per / 1e12
-        roof = {"kernel": "fp64 G(K:x) (5 passes)", "bound": "fp64", "achieved": ach,
-                "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
-                "peak_source": "measured DFMA rate on this GPU (cpfft_measure_fp64_peak)",
-                "traffic": traffic.get("green64", None) and traffic["green64"] * N3,
-                "algorithmic_flops_per_launch": fft_flops_per_voxel(N) * N3,
-                "avg_launch_ms": per * 1e3}
-    else:
-        per = tsk / su
-        ach = BYTES_STRESS * N3 / per / 1e9
-        roof = {"kernel": "stress update (mm10 + cep2A)", "bound": "hbm", "achieved": ach,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-                "peak_source": f"{peak_kind} hbm_gbs; the kernel is FP64-pipe bound",
-                "traffic": traffic.get("stress", None) and traffic["stress"] * N3,
-                "algorithmic_bytes_per_launch": BYTES_STRESS * N3, "avg_launch_ms": per * 1e3}
-    kernel_split = {"stress_s": tsk, "green64_s": tg64,
-                    "green32_s_estimated": tg32, "n_green64": ng64, "n_green32": ng32_all,
-                    "n_green32_timed": ng32, "green32_timed_s": tg32_timed,
-                    "cg_graph_s": tcg, "stress_passes": su,
-                    "note": "green64 = FP64-accurate applies (double-float in the fast forms); "
-                            "green32_s_estimated = timed per-apply time x all FP32 applies "
-                            "(most run inside the CG iteration graph, whose whole time is "
-                            "cg_graph_s)"}
-    # G(K:x) applies per step, FP32 and FP64 together (each FP32 CG iteration is one)
-    hint = (su / len(stats), (ng32_all + ng64) / len(stats))
     cpu = None
     if world == 1 and not args.no_cpu:
-        res = cpu_sample(r, load, workload_counts(), os.cpu_count(),
-                         n_stress_sample=max(4096, N3 // 64), n_green=1)
-        cpu = {"value": res["value"], "unit": "voxel stress-updates/s", "cores": os.cpu_count(),
-               "kind": "port",
-               "sample": (f"C++ oracle, OpenMP {os.cpu_count()} threads: stress update of "
-                          f"N^3/64 voxels + one full-grid FP64 G(K:x) at {N}^3, extrapolated "
-                          f"to a load step ({workload_counts()[0]} passes, "
-                          f"{workload_counts()[1]} matvecs)"),
-               "s_per_load_step": res["t_load_step"]}
+        # counts per load step of the plain form (the reference's algorithm) in this run
+        if plain is not None:
+            su_step = comparison["fp64_counts"]["stress_passes_per_step"]
+            mv_step = comparison["fp64_counts"]["matvecs_per_step"]
+            src = "the plain FP64 form's timed steps in this run"
+        else:
+            su_step, mv_step = REF_COUNTS
+            src = "earlier runs of the plain FP64 form"
+        res = cpu_sample(r, load, os.cpu_count(), max(4096, N3 // 256), state=fast_state,
+                         step=fast_step + 1)
+        t_step = su_step * res["t_stress_full_grid"] + mv_step * res["t_matvec"]
+        small = cpu_whole_steps(os.cpu_count())
+        cpu = {"value": N3 * su_step / t_step, "unit": "voxel stress-updates/s",
+               "cores": os.cpu_count(), "kind": "port", "extrapolated": True,
+               "s_per_load_step": t_step,
+               "sample": (f"C++ oracle, OpenMP {os.cpu_count()} threads, at {N}^3: stress update "
+                          f"of {res['voxels']} voxels from the GPU run's committed plastic state "
+                          f"(load step {fast_step}) to the next step's first implicit pass, and "
+                          f"one full-grid FP64 G(K:x) ({res['t_matvec']:.2f} s); load step "
+                          f"EXTRAPOLATED with {su_step:.1f} stress passes and {mv_step:.0f} "
+                          f"matvecs per step ({src})"),
+               "timed_small_workload": small}
+    fc = counts(fast)
     line = {
         "metric": METRIC,
         "value": units_all / tmax,
@@ -420,52 +638,22 @@ def gb300_arm(args):
         "e2e": {"value": units_all / temax, "unit": "voxel stress-updates/s",
                 "h2d_bytes_per_step": 9 * 8 + 9 * 4,
                 "d2h_bytes_per_step": 2 * 9 * N3 * 8 + 9 * 8},
-        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "gpu_launches": int(sum(s["kernel_launches"] for s in fast["stats"])),
         "roofline": roof,
-        "kernel_time_split": kernel_split,
-        "per_step_counts": {"stress_passes": hint[0], "matvecs": hint[1],
-                            "newton": [s["newton_iters"] for s in stats],
-                            "nbc": [s["nbc_iters"] for s in stats],
-                            "cg_iters": [s["cg_iters"] for s in stats],
-                            "res_equil": [s["res_equil"] for s in stats],
-                            "res_fft": [s["res_fft"] for s in stats],
-                            "local_iters_per_voxel_pass": sum(s["local_iters"] for s in stats) / (N3 * su),
-                            "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in stats) / (N3 * su),
-                            "guess_rejected": [s["guess_rejected"] for s in stats]},
+        "kernel_time_split": split,
+        "per_step_counts": fc,
+        "device_bytes_per_voxel": fast["device_bytes"] / N3,
+        "vs_fp64": comparison,
+        "local_starts": starts,
         "learned": learned,
-        "autotuned_tiles": solver.tuning() if prec == cp.PREC_MIXED else None,
+        "autotuned_tiles": tuned,
+        "queue_chunk": qchunk,
         "fp64_peak_tflops": fp64_peak,
-        "clocks": clk,
+        "clocks": fast["clocks"],
         "cpu_baseline": cpu,
     }
-    solver.close()
-    if args.compare_fp64 and args.mode != "fp64" and world == 1:
-        line["error_vs_fp64"] = compare_fp64(cp, r, load, pbars, Ph.numpy(), tolNR, tolPCG,
-                                             maxIter)
     print(json.dumps(line), flush=True)
     return 0
-
-
-def compare_fp64(cp, r, load, pbars, P_last, tolNR, tolPCG, maxIter):
-    """The plain FP64 form (FP64 CG, the reference's local starts) over the same load
-    steps, after the timed run: the fast form's error on the stress-strain curve (P_bar of
-    every step) and on the last step's per-voxel P.  Untimed."""
-    N = r.N
-    s = cp.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, cp.G_CENTERED, cp.PREC_FP64)
-    try:
-        s.set_mode(cp.PREC_FP64, cp.START_PLAIN)
-        s.nr3_begin(tolPCG)
-        rel = []
-        for step, pb in enumerate(pbars, start=1):
-            _, ref, _ = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, tolNR, tolPCG, maxIter)
-            rel.append(float(np.abs(pb - ref).max() / np.abs(ref).max()))
-        _, P = s.fields()
-    finally:
-        s.close()
-    scale = np.maximum(np.abs(P).max(axis=0), 1e-6 * np.abs(P).max())
-    return {"pbar_rel_per_step": rel, "pbar_rel_max": max(rel),
-            "p_last_step_rel_max_per_voxel": float((np.abs(P_last - P).max(axis=0) / scale).max()),
-            "reference_form": "plain FP64: FP64 CG, the reference's local starts, FP64 tangent"}
 
 
 def config4_rves(cp, nsteps):
@@ -493,7 +681,7 @@ def config4_arm(args):
     import cpfft_gb300 as cp
     cp.load_library()
     prec = cp.PREC_FP64 if args.mode == "fp64" else cp.PREC_MIXED
-    opts = start_flags(cp, args) if args.mode != "learned" else (
+    opts = start_flags(cp, args.mode, args) if args.mode != "learned" else (
         cp.START_ITERATE | cp.START_TRIAL | cp.TANGENT_F32)
     res = {}
     for nthreads in sorted({1, args.batch_threads}):
@@ -536,7 +724,7 @@ def main():
     ap.add_argument("--seed", type=int, default=3)
     # mixed: FP32 Krylov under the FP64 residual; learned: the same with the learned
     # initial guess of the local solves (trained before the timed steps); fp64: plain
-    ap.add_argument("--mode", default="learned", choices=["learned", "mixed", "fp64"])
+    ap.add_argument("--mode", default="mixed", choices=["learned", "mixed", "fp64"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     # preconditioner of the FP32 inner Krylov iterations (mixed / learned): the Green
     # operator of the mean-tangent reference medium, or none (the reference's plain CG)
@@ -548,17 +736,24 @@ def main():
     ap.add_argument("--schedule", default="queue", choices=["blocks", "queue"])
     # fast forms: the consistent tangent (it steers Newton only) in FP32 or FP64
     ap.add_argument("--tangent", default="f32", choices=["f32", "f64"])
-    # config4: the 48-RVE batch (cpfft_batch_solve) in place of the 128^3 workload
-    ap.add_argument("--workload", default="128", choices=["128", "config4"])
+    # config4: the 48-RVE batch (cpfft_batch_solve); config5: the 256^3 cyclic workload
+    ap.add_argument("--workload", default="128", choices=["128", "config4", "config5"])
     ap.add_argument("--batch-threads", type=int, default=8)
-    # ||dF||/||F|| of FFT_nr3.  At 128^3 the reference algorithm's Newton loop enters a
-    # period-4 cycle at 6.7e-6 in load step 2 (symmetrised, lagged local tangent), so
-    # the benchmark uses the reference example deck's value 1e-5; the equilibrium
-    # residual ||G(P)||/||P_bar|| is reported per step.
-    ap.add_argument("--tol-nr", type=float, default=1e-5)
-    ap.add_argument("--compare-fp64", action="store_true",
-                    help="after the timed steps, run the plain FP64 form over the same steps "
-                         "and report the fast form's error on P_bar and on the last P")
+    # ||dF||/||F|| of FFT_nr3, and the equilibrium residual ||G(P)||/(sqrt(N^3)||P_bar||)
+    # both forms must also reach before a Newton loop ends (cpfft_set_equilibrium_tol)
+    ap.add_argument("--tol-nr", type=float, default=1e-6)
+    ap.add_argument("--tol-equil", type=float, default=1e-6)
+    ap.add_argument("--max-iter", type=int, default=30)
+    ap.add_argument("--fp64-steps", type=int, default=5,
+                    help="timed steps of the plain FP64 form (after the same warm-up), at "
+                         "most --steps")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain FP64 form (run by default after the fast form: its "
+                         "s/step on the first timed steps, the speed-up and the fast form's "
+                         "error against it)")
+    ap.add_argument("--no-compare-starts", dest="compare_starts", action="store_false",
+                    help="skip the local-start comparison (reference / trial / learned) on "
+                         "the state the timed steps leave")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")

@@ -125,6 +125,8 @@ SIGNATURES = {
     "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
+    "cpfft_set_tiles": (_I, [_IP]),
+    "cpfft_queue_chunk": (_I, [_IP, _DP]),
     "cpfft_format_flat": (_I, [_I, ctypes.c_char_p, _LL, _P(_LL)]),
     "cpfft_write_flat": (_I, [_I, _I, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_format_e15": (_I, [_DP, _LL, ctypes.c_char_p]),
@@ -296,6 +298,19 @@ class Solver:
         _check(load_library().cpfft_tuning(t.ctypes.data_as(_IP), _dp(ms)), "cpfft_tuning")
         return {"fp32_tiles": t[:2].tolist(), "double_float_tiles": t[2:].tolist(),
                 "fp32_ms": float(ms[0]), "double_float_ms": float(ms[1])}
+
+    def queue_chunk(self):
+        """The autotuned voxel-queue chunk and the candidates' pass times (ms)."""
+        v = ctypes.c_int(0)
+        ms = np.zeros(3)
+        _check(load_library().cpfft_queue_chunk(ctypes.byref(v), _dp(ms)), "cpfft_queue_chunk")
+        return {"chunk": v.value, "ms_128_256_512": ms.tolist()}
+
+    def set_tiles(self, fp32_bd, fp32_c, df_bd=16, df_c=2):
+        """Pin the register passes' tile shapes (fp32_c < 0: the register-resident
+        slowest-axis pass with -fp32_c columns per block)."""
+        t = np.array([fp32_bd, fp32_c, df_bd, df_c], np.int32)
+        _check(load_library().cpfft_set_tiles(t.ctypes.data_as(_IP)), "cpfft_set_tiles")
 
     def set_mises(self, material, e, nu, yld_pt, tan_e, beta=1.0):
         """Make the 1-based ``material`` (declared with slip_type NOT_A_CRYSTAL) a bilinear

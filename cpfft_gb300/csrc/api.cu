@@ -292,6 +292,9 @@ struct Ctx {
   unsigned char* vcost = nullptr;  // (N3) local iterations of each voxel's last implicit pass
   int* vperm = nullptr;            // (N3) queue order
   unsigned int* vq = nullptr;      // 2 x 64 bin counters / offsets + the queue head
+  int qchunk = 128;                // voxels a block takes from the queue at a time
+  bool qtuned = false;             // the chunk has been autotuned (first implicit queue pass)
+  float qchunk_ms[3] = {0.f, 0.f, 0.f};  // tuning times for 128 / 256 / 512
   cudaStream_t st = nullptr;
   GridDesc g;
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
@@ -980,6 +983,44 @@ int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
                                      : cg64(c, b, x, tol, iters);
 }
 
+// Queue chunk autotuner: on the context's first implicit queue pass, the pass runs once
+// per candidate chunk (voxels a block takes from the work queue at a time), timed with
+// CUDA events, and the fastest is kept.  The runs give identical results (no local solve
+// of this pass starts from an earlier pass's state); their statistics and logged pairs
+// are not kept.
+int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
+  c->qtuned = true;
+  a.log_X = nullptr;
+  a.log_cap = 0;
+  const long long l0 = g_kernel_launches;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bestq = 128;
+  for (int q : {128, 256, 512}) {
+    a.qchunk = q;
+    CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
+    CK(cudaEventRecord(e0, c->st));
+    CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
+                      : c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    c->qchunk_ms[q == 128 ? 0 : q == 256 ? 1 : 2] = ms;
+    if (ms < best) { best = ms; bestq = q; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  g_kernel_launches = l0;  // tuning launches are not the caller's work
+  c->qchunk = bestq;
+  if (c->log)
+    fprintf(stderr, "       queue chunk: %d voxels (%.2f / %.2f / %.2f ms for 128 / 256 / 512)\n",
+            bestq, c->qchunk_ms[0], c->qchunk_ms[1], c->qchunk_ms[2]);
+  return 0;
+}
+
 int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
            long long* predict_iters = nullptr, long long* rejected = nullptr) {
   StressArgs a;
@@ -1044,11 +1085,13 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.perm = nullptr;
   a.queue = nullptr;
   a.cost = nullptr;
+  a.qchunk = c->qchunk;
   if (c->sched == CPFFT_SCHED_QUEUE && iter > 0 && c->n_crys_vox) {
-    CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
     a.perm = c->vperm;
     a.queue = c->vq + 128;
     a.cost = c->vcost;
+    if (!c->qtuned && !a.start_iterate) TRY(tune_queue_chunk(c, a, warm));
+    CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
   }
   CK(cudaMemsetAsync(c->stats, 0, 5 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
@@ -1209,6 +1252,7 @@ int alloc_mixed(Ctx* c) {
     CK(green_autotune_f32(c->xf, c->K4f, c->Apf, c->Sf, c->twf, &c->g, c->st, &c->tune_ms[0]));
     c->gdf = c->g;
     c->gdf.wtc = 0;
+    c->gdf.wc2 = 0;
     CK(green_autotune_df(c->io, c->K4f, c->K4lo, c->b, reinterpret_cast<dfl2*>(c->S), c->twdf,
                          &c->gdf, c->st, &c->tune_ms[1]));
     g_kernel_launches = launches0;  // tuning launches are not the caller's work
@@ -1546,7 +1590,7 @@ int cpfft_tuning(int* tiles, double* ms) {
   Ctx* c = g_ctx;
   if (tiles) {
     tiles[0] = c->g.wtb;
-    tiles[1] = c->g.wtc;
+    tiles[1] = c->g.wc2 ? -c->g.wc2 : c->g.wtc;
     tiles[2] = c->gdf.wtb;
     tiles[3] = c->gdf.wtc;
   }
@@ -1554,6 +1598,51 @@ int cpfft_tuning(int* tiles, double* ms) {
     ms[0] = c->tune_ms[0];
     ms[1] = c->tune_ms[1];
   }
+  return 0;
+}
+
+int cpfft_queue_chunk(int* voxels, double* ms) {
+  TRY(need_ctx());
+  if (voxels) *voxels = g_ctx->qtuned ? g_ctx->qchunk : 0;
+  if (ms)
+    for (int k = 0; k < 3; k++) ms[k] = g_ctx->qchunk_ms[k];
+  return 0;
+}
+
+int cpfft_set_tiles(const int* tiles) {
+  TRY(need_ctx());
+  Ctx* c = g_ctx;
+  if (!tiles) {
+    cpfft_set_error("cpfft_set_tiles: null pointer");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  if (!c->df_ok) {
+    cpfft_set_error("cpfft_set_tiles: no register-FFT passes for this grid (or the mixed "
+                    "form was not selected)");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  const int tb = tiles[0], tc = tiles[1], db = tiles[2], dc = tiles[3];
+  const bool ok = (tb == 8 || tb == 16 || tb == 32) && (tc == 2 || tc == 4 || tc == -2 || tc == -4) &&
+                  (db == 16 || db == 32) && dc == 2;
+  if (!ok) {
+    cpfft_set_error("cpfft_set_tiles: unsupported tile shapes {%d, %d, %d, %d}", tb, tc, db, dc);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  c->g.wtb = tb;
+  c->g.wtc = tc > 0 ? tc : 2;
+  c->g.wc2 = tc < 0 ? -tc : 0;
+  c->gdf.wtb = db;
+  c->gdf.wtc = dc;
+  c->gdf.wc2 = 0;
+  if (c->cg_exec) {  // the captured CG iteration bakes in the launch shapes
+    cudaGraphExecDestroy(c->cg_exec);
+    c->cg_exec = nullptr;
+  }
+  if (c->cg_graph) {
+    cudaGraphDestroy(c->cg_graph);
+    c->cg_graph = nullptr;
+  }
+  c->cg_graph_state = 0;
   return 0;
 }
 

@@ -116,7 +116,7 @@ cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2
   cudaError_t e = tune_tiles(t, [&](const GridDesc& gg) {
     green_apply_dot<float>(x, K4, 1, y, S, tw, gg, st, nullptr, nullptr);
   }, st, best_ms, true);
-  if (e == cudaSuccess) { g->wtb = t.wtb; g->wtc = t.wtc; }
+  if (e == cudaSuccess) { g->wtb = t.wtb; g->wtc = t.wtc; g->wc2 = t.wc2; }
   return e;
 }
 

@@ -25,6 +25,8 @@ struct GridDesc {
   const float* acoef = nullptr;  // (36, device) acoustic-tensor coefficients of the medium
   int wtb = 16, wtc = 0;  // warp passes: columns per block of passes B/D and of pass C (0: 4 for
                           // FP32, 2 for double-float)
+  int wc2 = 0;            // FP32 warp passes: pass C in registers (wpass_c2) with this many
+                          // columns per block (0: the shared-memory pass C)
   FftPlan plan;
 };
 

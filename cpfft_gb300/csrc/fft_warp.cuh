@@ -147,4 +147,119 @@ __device__ __forceinline__ void column(T2* col, const T2* tw, int t) {
   __syncwarp();
 }
 
+// ---- column transforms with the data in registers at both ends ----------------------
+// A team of P consecutive lanes transforms one column; thread t of the team holds the
+// column in "space order" v[j] = x[t + P j] (j < R) or in "frequency order":
+//   P == R:  v[k2] = X[t + R k2]                        (k2 < P)
+//   P == 2R: v[i]  = X[k1 + R (hh R + i)], k1 = t / 2, hh = t % 2   (i < R)
+// The forward transform takes space order to frequency order, the inverse (unscaled,
+// sum_k X[k] W_N^{-nk}) frequency order back to space order, the inverse being the
+// forward's steps transposed (its inverse P-point step runs on the data each thread
+// holds).  Each direction exchanges the column once through the team's buffer `xb`
+// (xlen<N>() elements, index xidx<N>: rows of P padded so that a half-warp's accesses
+// of both the row and the column pattern fall in distinct banks).
+
+template <int N>
+constexpr int xpad() { return Shape<N>::P == Shape<N>::R ? 1 : 2; }
+template <int N>
+__device__ __forceinline__ int xidx(int k) { return k + (k / Shape<N>::P) * xpad<N>(); }
+template <int N>
+constexpr int xlen() { return N + Shape<N>::R * xpad<N>(); }
+
+// frequency of element e of thread t in frequency order
+template <int N>
+__device__ __forceinline__ int freq_of(int t, int e) {
+  constexpr int P = Shape<N>::P, R = Shape<N>::R;
+  if (P == R) return t + R * e;
+  return (t >> 1) + R * ((t & 1) * R + e);
+}
+
+template <int R, typename T2, typename T>
+__device__ __forceinline__ void idft(T2* v) {
+#pragma unroll
+  for (int k = 0; k < R; k++) v[k].y = -v[k].y;
+  dft<R, T2, T>(v);
+#pragma unroll
+  for (int k = 0; k < R; k++) v[k].y = -v[k].y;
+}
+
+template <int N, typename T2, typename T>
+__device__ __forceinline__ void fwd_regs(T2* v, T2* xb, const T2* tw, int t) {
+  constexpr int P = Shape<N>::P, R = Shape<N>::R;
+  dft<R, T2, T>(v);
+#pragma unroll
+  for (int k1 = 1; k1 < R; k1++) v[k1] = cmul(v[k1], tw[t * k1]);
+#pragma unroll
+  for (int k1 = 0; k1 < R; k1++) xb[xidx<N>(k1 * P + t)] = v[k1];
+  __syncwarp();
+  if (P == R) {
+#pragma unroll
+    for (int m = 0; m < P; m++) v[m] = xb[xidx<N>(t * P + m)];
+    __syncwarp();
+    dft<P, T2, T>(v);
+  } else {
+    const int k1 = t >> 1, hh = t & 1;
+#pragma unroll
+    for (int m = 0; m < R; m++) v[m] = xb[xidx<N>(k1 * P + 2 * m + hh)];
+    __syncwarp();
+    dft<R, T2, T>(v);
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+      T2 p = shfl_xor2(v[i], 1);
+      T2 e = hh ? p : v[i], od = hh ? v[i] : p;
+      T2 w = cmul(od, tw[i * R]);  // W_P^i = W_N^{i R}
+      v[i].x = hh ? e.x - w.x : e.x + w.x;
+      v[i].y = hh ? e.y - w.y : e.y + w.y;
+    }
+  }
+}
+
+template <int N, typename T2, typename T>
+__device__ __forceinline__ void inv_regs(T2* v, T2* xb, const T2* tw, int t) {
+  constexpr int P = Shape<N>::P, R = Shape<N>::R;
+  if (P == R) {
+    const int k1 = t;
+    idft<P, T2, T>(v);  // over k2: Z[k1][t'] in v[t']
+#pragma unroll
+    for (int tp = 0; tp < P; tp++) {
+      T2 w = tw[tp * k1];
+      w.y = -w.y;
+      xb[xidx<N>(k1 * P + tp)] = cmul(v[tp], w);
+    }
+  } else {
+    const int k1 = t >> 1, hh = t & 1;
+#pragma unroll
+    for (int i = 0; i < R; i++) {  // radix-2 across the thread pair, W_P^{-i} on the odd half
+      T2 p = shfl_xor2(v[i], 1);
+      T2 x0 = hh ? p : v[i], x1 = hh ? v[i] : p;
+      T2 u;
+      if (hh) {
+        T2 d;
+        d.x = x0.x - x1.x;
+        d.y = x0.y - x1.y;
+        T2 w = tw[i * R];
+        w.y = -w.y;
+        u = cmul(d, w);
+      } else {
+        u.x = x0.x + x1.x;
+        u.y = x0.y + x1.y;
+      }
+      v[i] = u;
+    }
+    idft<R, T2, T>(v);  // Z[k1][2m + hh] in v[m]
+#pragma unroll
+    for (int m = 0; m < R; m++) {
+      const int tp = 2 * m + hh;
+      T2 w = tw[tp * k1];
+      w.y = -w.y;
+      xb[xidx<N>(k1 * P + tp)] = cmul(v[m], w);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k1 = 0; k1 < R; k1++) v[k1] = xb[xidx<N>(k1 * P + t)];
+  __syncwarp();
+  idft<R, T2, T>(v);
+}
+
 }  // namespace regfft

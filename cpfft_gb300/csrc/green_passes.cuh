@@ -690,6 +690,178 @@ __global__ void __launch_bounds__(288) wpass_c(typename Vec2<T>::t* __restrict__
   }
 }
 
+// ---- pass C, register-resident form ---------------------------------------------------
+// The Green contraction acts row by row: (Ghat : A)_ij = q_j (sum_l A_il q_l) / |q|^2 needs
+// only row i of A at the same frequency.  A team of P lanes therefore holds the 3
+// components of one row (i = 3 row + l) of one (kb, ka) column along c in registers:
+// loaded straight from the half spectrum in space order, transformed forward (one
+// exchange through the team's buffer), contracted in registers, transformed back (one
+// exchange) and stored straight back -- four shared-memory accesses per element instead of
+// twelve in wpass_c.  The reference-medium operator couples the rows only through the
+// 3-vector d_i = sum_l A_il q_l: the teams of one column trade it through shared memory.
+// Block: 3 rows x TK columns of teams (3 TK P threads); grid ((H + TK - 1) / TK, N).
+template <typename T2, typename T>
+__device__ __forceinline__ void green_row_plain(const T2* A, int q0, int q1, int q2, T w,
+                                                T2* out) {
+  const int qq = q0 * q0 + q1 * q1 + q2 * q2;
+  if (qq == 0) return;
+  const T s = w / (T)qq;
+  const T q[3] = {(T)q0, (T)q1, (T)q2};
+  T2 d;
+  d.x = (A[0].x * q[0] + A[1].x * q[1] + A[2].x * q[2]) * s;
+  d.y = (A[0].y * q[0] + A[1].y * q[1] + A[2].y * q[2]) * s;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    out[j].x += q[j] * d.x;
+    out[j].y += q[j] * d.y;
+  }
+}
+
+// row `row` of Ghat0(q) : A from the three rows' d = A q (dq[3]), accumulated with weight w
+template <typename T2, typename T>
+__device__ __forceinline__ void green_row_pre(const float* coef, const T2* dq, int row, int q0,
+                                              int q1, int q2, T w, T2* out) {
+  if (q0 == 0 && q1 == 0 && q2 == 0) return;
+  const T q[3] = {(T)q0, (T)q1, (T)q2};
+  const T pr[6] = {q[0] * q[0], q[1] * q[1], q[2] * q[2], q[0] * q[1], q[1] * q[2], q[0] * q[2]};
+  T a[6];
+#pragma unroll
+  for (int r = 0; r < 6; r++) {
+    T s = 0;
+#pragma unroll
+    for (int m = 0; m < 6; m++) s += (T)coef[6 * r + m] * pr[m];
+    a[r] = s;
+  }
+  // a = (a00, a11, a22, a01, a12, a02); cofactors of the symmetric A0(q)
+  const T c00 = a[1] * a[2] - a[4] * a[4], c01 = a[5] * a[4] - a[3] * a[2];
+  const T c02 = a[3] * a[4] - a[5] * a[1], c11 = a[0] * a[2] - a[5] * a[5];
+  const T c12 = a[3] * a[5] - a[0] * a[4], c22 = a[0] * a[1] - a[3] * a[3];
+  const T det = a[0] * c00 + a[3] * c01 + a[5] * c02;
+  if (!(det > (T)0)) return;
+  const T cr0 = row == 0 ? c00 : row == 1 ? c01 : c02;
+  const T cr1 = row == 0 ? c01 : row == 1 ? c11 : c12;
+  const T cr2 = row == 0 ? c02 : row == 1 ? c12 : c22;
+  const T s = w / det;
+  T2 e;
+  e.x = (cr0 * dq[0].x + cr1 * dq[1].x + cr2 * dq[2].x) * s;
+  e.y = (cr0 * dq[0].y + cr1 * dq[1].y + cr2 * dq[2].y) * s;
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    out[j].x += e.x * q[j];
+    out[j].y += e.y * q[j];
+  }
+}
+
+template <typename T2, typename T>
+__device__ __forceinline__ T2 dot_q(const T2* A, int q0, int q1, int q2) {
+  const T a = (T)q0, b = (T)q1, c = (T)q2;
+  T2 d;
+  d.x = A[0].x * a + A[1].x * b + A[2].x * c;
+  d.y = A[0].y * a + A[1].y * b + A[2].y * c;
+  return d;
+}
+
+template <int N, int TK>
+constexpr int c2_threads() { return 3 * TK * regfft::Shape<N>::P; }
+template <typename T, int N, int TK>
+constexpr size_t smem_c2() {
+  // twiddles, one exchange buffer per team, and the d exchange of the reference medium
+  // (per column of the tile: N frequencies x {+q, -q} x 3 rows)
+  return sizeof(typename Vec2<T>::t) *
+         ((size_t)N + (size_t)3 * TK * regfft::xlen<N>() + (size_t)TK * N * 6);
+}
+
+template <int M, typename T, int TK>
+__global__ void __launch_bounds__(c2_threads<32 * M, TK>()) wpass_c2(
+    typename Vec2<T>::t* __restrict__ S, GridDesc g, const typename Vec2<T>::t* __restrict__ twg) {
+  using T2 = typename Vec2<T>::t;
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  constexpr int P = regfft::Shape<N>::P, R = regfft::Shape<N>::R;
+  constexpr int XL = regfft::xlen<N>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* xbuf = tw + N;
+  T2* dbuf = xbuf + 3 * TK * XL;
+  __shared__ float s_coef[36];
+  load_acoef(g, s_coef);
+  load_tw(tw, twg, N);
+  const int team = threadIdx.x / P, t = threadIdx.x % P;
+  const int row = team / TK, kk = team % TK;
+  const int ka = blockIdx.x * TK + kk, kb = blockIdx.y;
+  const bool valid = ka < H;
+  const long long cstr = (long long)N * H;
+  T2 v[3][R];
+#pragma unroll
+  for (int l = 0; l < 3; l++) {
+    const T2* src = S + (long long)(3 * row + l) * N * cstr + (long long)kb * H + ka;
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+      v[l][j].x = 0;
+      v[l][j].y = 0;
+      if (valid) v[l][j] = src[(long long)(t + P * j) * cstr];
+    }
+  }
+  __syncthreads();  // twiddles and coefficients
+  T2* xb = xbuf + team * XL;
+#pragma unroll
+  for (int l = 0; l < 3; l++) regfft::fwd_regs<N, T2, T>(v[l], xb, tw, t);
+  const int Nh = g.Nhalf, gm = g.gmap;
+  const T scale = (T)g.inv_n3;
+  const bool cen_even = gm == CPFFT_G_CENTERED && (N & 1) == 0;
+  const bool nyq_ab = cen_even && (2 * kb == N || 2 * ka == N);
+  const int p1 = qmap(kb, N, Nh, gm), p2 = qmap(ka, N, Nh, gm);
+  const int m1 = qmap((N - kb) & (N - 1), N, Nh, gm), m2 = qmap((N - ka) & (N - 1), N, Nh, gm);
+  bool pre = false;
+  if constexpr (sizeof(T) == 4) pre = g.pre != 0;
+  if (pre) {
+    // d = A q of this row at +q and -q, traded with the other rows of the column
+#pragma unroll
+    for (int e = 0; e < R; e++) {
+      const int kc = regfft::freq_of<N>(t, e);
+      const int p0 = qmap(kc, N, Nh, gm), m0 = qmap((N - kc) & (N - 1), N, Nh, gm);
+      const T2 A[3] = {v[0][e], v[1][e], v[2][e]};
+      T2* d = dbuf + ((size_t)kk * N + kc) * 6;
+      d[row] = dot_q<T2, T>(A, p0, p1, p2);
+      d[3 + row] = dot_q<T2, T>(A, m0, m1, m2);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int e = 0; e < R; e++) {
+    const int kc = regfft::freq_of<N>(t, e);
+    T2 out[3];
+#pragma unroll
+    for (int l = 0; l < 3; l++) { out[l].x = 0; out[l].y = 0; }
+    const bool nyq = nyq_ab || (cen_even && 2 * kc == N);
+    if (valid && !nyq) {
+      const int p0 = qmap(kc, N, Nh, gm), m0 = qmap((N - kc) & (N - 1), N, Nh, gm);
+      const bool sym = m0 == -p0 && m1 == -p1 && m2 == -p2;
+      const T w = sym ? scale : (T)0.5 * scale;
+      if (pre) {
+        const T2* d = dbuf + ((size_t)kk * N + kc) * 6;
+        green_row_pre<T2, T>(s_coef, d, row, p0, p1, p2, w, out);
+        if (!sym) green_row_pre<T2, T>(s_coef, d + 3, row, m0, m1, m2, w, out);
+      } else {
+        const T2 A[3] = {v[0][e], v[1][e], v[2][e]};
+        green_row_plain<T2, T>(A, p0, p1, p2, w, out);
+        if (!sym) green_row_plain<T2, T>(A, m0, m1, m2, w, out);
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < 3; l++) v[l][e] = out[l];
+  }
+#pragma unroll
+  for (int l = 0; l < 3; l++) regfft::inv_regs<N, T2, T>(v[l], xb, tw, t);
+  if (valid) {
+#pragma unroll
+    for (int l = 0; l < 3; l++) {
+      T2* dst = S + (long long)(3 * row + l) * N * cstr + (long long)kb * H + ka;
+#pragma unroll
+      for (int j = 0; j < R; j++) dst[(long long)(t + P * j) * cstr] = v[l][j];
+    }
+  }
+}
+
 // dotx != nullptr: also one partial sum per block of dotx . y over the voxels the block
 // writes (the CG product p . Ap without re-reading Ap), into part[blockIdx.x]
 template <int M, typename T, typename TIO>
@@ -783,6 +955,8 @@ constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
 // B/D tiles 16 and 32 and the C tile 2 only)
 constexpr int TB_CAND[3] = {8, 16, 32};
 constexpr int TC_CAND[2] = {2, 4};
+// pass C in registers (wpass_c2, FP32 only): 0 = the shared-memory pass C, else its TK
+constexpr int C2_CAND[3] = {0, 2, 4};
 
 template <int M, typename T, int TB>
 cudaError_t wsetup_b() {
@@ -800,6 +974,19 @@ cudaError_t wsetup_c() {
 template <typename T>
 constexpr bool small_code() { return sizeof(T) == 4; }
 
+template <int M, typename T, int TK>
+cudaError_t wsetup_c2() {
+  return cudaFuncSetAttribute(wpass_c2<M, T, TK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem_c2<T, 32 * M, TK>());
+}
+template <int M, typename T, int TK>
+void wlaunch_c2(typename Vec2<T>::t* S, const GridDesc& g, const typename Vec2<T>::t* tw,
+                cudaStream_t st) {
+  constexpr int N = 32 * M, H = N / 2 + 1;
+  dim3 gc((H + TK - 1) / TK, N);
+  wpass_c2<M, T, TK><<<gc, c2_threads<N, TK>(), smem_c2<T, N, TK>(), st>>>(S, g, tw);
+}
+
 template <int M, typename T, typename TK = T, typename TIO = T>
 cudaError_t wgreen_setup() {
   constexpr int N = 32 * M;
@@ -808,7 +995,9 @@ cudaError_t wgreen_setup() {
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   if ((e = wsetup_b<M, T, 16>()) || (e = wsetup_b<M, T, 32>()) || (e = wsetup_c<M, T, 2>())) return e;
   if constexpr (small_code<T>())
-    if ((e = wsetup_b<M, T, 8>()) || (e = wsetup_c<M, T, 4>())) return e;
+    if ((e = wsetup_b<M, T, 8>()) || (e = wsetup_c<M, T, 4>()) || (e = wsetup_c2<M, T, 2>()) ||
+        (e = wsetup_c2<M, T, 4>()))
+      return e;
   if ((e = cudaFuncSetAttribute(wpass_e<M, T, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   return cudaSuccess;
@@ -852,7 +1041,9 @@ void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* 
                                                                     part_a);
   wlaunch_b_any<M, T>(g.wtb, S, g, tw, 0, st);
   if constexpr (small_code<T>()) {
-    if ((g.wtc ? g.wtc : wtile_c<T>()) == 4) { wlaunch_c<M, T, 4>(S, g, tw, st); }
+    if (g.wc2 == 4) wlaunch_c2<M, T, 4>(S, g, tw, st);
+    else if (g.wc2 == 2) wlaunch_c2<M, T, 2>(S, g, tw, st);
+    else if ((g.wtc ? g.wtc : wtile_c<T>()) == 4) { wlaunch_c<M, T, 4>(S, g, tw, st); }
     else wlaunch_c<M, T, 2>(S, g, tw, st);
   } else {
     wlaunch_c<M, T, 2>(S, g, tw, st);
@@ -899,19 +1090,23 @@ template <typename C>
 cudaError_t tune_tiles(GridDesc& g, C&& one_apply, cudaStream_t st, float* best_ms,
                        bool all_shapes) {
   float best = 1e30f;
-  int btb = 16, btc = 2;
+  int btb = 16, btc = 2, bc2 = 0;
   for (int tb : TB_CAND)
-    for (int tc : TC_CAND) {
-      if (!all_shapes && (tb == 8 || tc == 4)) continue;
-      g.wtb = tb;
-      g.wtc = tc;
-      float ms = 0.f;
-      cudaError_t e = time_applies([&] { one_apply(g); }, 5, st, &ms);
-      if (e != cudaSuccess) return e;
-      if (ms < best) { best = ms; btb = tb; btc = tc; }
-    }
+    for (int tc : TC_CAND)
+      for (int c2 : C2_CAND) {
+        if (!all_shapes && (tb == 8 || tc == 4 || c2)) continue;
+        if (c2 && tc != TC_CAND[0]) continue;  // the register pass C has its own tile
+        g.wtb = tb;
+        g.wtc = tc;
+        g.wc2 = c2;
+        float ms = 0.f;
+        cudaError_t e = time_applies([&] { one_apply(g); }, 5, st, &ms);
+        if (e != cudaSuccess) return e;
+        if (ms < best) { best = ms; btb = tb; btc = tc; bc2 = c2; }
+      }
   g.wtb = btb;
   g.wtc = btc;
+  g.wc2 = bc2;
   if (best_ms) *best_ms = best;
   return cudaSuccess;
 }

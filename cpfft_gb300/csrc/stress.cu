@@ -899,13 +899,20 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
     gb = GuessBlock{guess_smem, mlp::tmem_block_alloc(&tslot, 256), &bar, 0u};
   }
   __shared__ long long chunk;
-  for (long long round = 0;; round++) {
+  // queue: a block takes a.qchunk voxels at a time and works through them 128 at a time
+  const int sub_n = a.perm ? a.qchunk / 128 : 1;
+  for (long long round = 0, sub = 0;; round++) {
     long long base;
     if (a.perm) {
-      if (threadIdx.x == 0) chunk = (long long)atomicAdd(a.queue, 128u);
-      __syncthreads();
-      base = chunk;
-      __syncthreads();
+      if (sub == 0) {
+        if (threadIdx.x == 0) chunk = (long long)atomicAdd(a.queue, (unsigned)a.qchunk);
+        __syncthreads();
+      }
+      base = chunk + 128 * sub;
+      if (++sub == sub_n) {
+        sub = 0;
+        __syncthreads();  // every thread has read `chunk` before the next take
+      }
     } else {
       base = (long long)blockIdx.x * 128;
     }

@@ -204,6 +204,24 @@ def uniaxial_tension(total_strain, nstep):
     return Loading(_accumulate(incr, isNBC, nstep), isNBC, "uniaxial_tension")
 
 
+def cyclic_uniaxial(amplitude, cycles, nstep):
+    """Uniaxial tension/compression cycles between +-amplitude in F_xx (boundary
+    conditions of uniaxial_tension): each cycle climbs to +amplitude, falls to -amplitude
+    and returns to zero in nstep / cycles equal increments."""
+    isNBC = np.array([0, 0, 0, 1, 1, 0, 1, 1, 1], dtype=np.int32)
+    per = nstep // cycles
+    q = per // 4
+    de = amplitude / q
+    signs = np.concatenate([np.full(q, 1.0), np.full(2 * q, -1.0), np.full(per - 3 * q, 1.0)])
+    incr = np.zeros((nstep, 9))
+    incr[:, 0] = de * np.tile(signs, cycles)[:nstep]
+    bc = np.cumsum(incr, axis=0)
+    for d in (0, 4, 8):
+        if not isNBC[d]:
+            bc[:, d] += 1.0
+    return Loading(bc, isNBC, "cyclic_uniaxial")
+
+
 def plane_strain_compression(total_strain, nstep):
     """F_zz decreasing, F_yy = 1, F_xy = F_xz = F_yz = 0 prescribed; P_xx, P_yx, P_zx,
     P_zy held at zero."""

@@ -209,14 +209,25 @@ int cpfft_set_precond(int precond);
 #define CPFFT_SCHED_BLOCKS  0
 #define CPFFT_SCHED_QUEUE   1
 int cpfft_set_schedule(int schedule);
+/* The work-queue chunk the autotuner chose (extension): on a context's first implicit
+ * CPFFT_SCHED_QUEUE pass the pass runs once per candidate -- 128, 256 or 512 voxels taken
+ * from the queue by a block at a time -- timed with CUDA events, and the fastest is kept
+ * (identical results).  *voxels = the chosen chunk (0 before that pass); ms (3, may be
+ * NULL) = the measured pass times of the candidates. */
+int cpfft_queue_chunk(int* voxels, double* ms);
 
 /* Tile shapes the autotuner chose for this grid when CPFFT_PREC_MIXED was first selected
  * (extension): columns per block of the transform passes along the middle axis (both
  * directions) and along the slowest axis (with the Green contraction), for the FP32
- * operator (tiles[0], tiles[1]) and the double-float operator (tiles[2], tiles[3]); ms:
- * the measured time per apply of each.  Zeros before the mixed form is selected or for
+ * operator (tiles[0], tiles[1]) and the double-float operator (tiles[2], tiles[3]); a
+ * negative tiles[1] means the FP32 slowest-axis pass holding each column's rows in
+ * registers, with -tiles[1] columns per block; ms: the measured time per apply of each.  Zeros before the mixed form is selected or for
  * grids the register passes do not cover (N other than 32, 64, 128, 256). */
 int cpfft_tuning(int* tiles, double* ms);
+/* Override the autotuner's choice (same encoding as cpfft_tuning: FP32 {8,16,32},
+ * {2,4,-2,-4}; double-float {16,32}, 2).  For callers that pin launch shapes, and for
+ * tests of every shape. */
+int cpfft_set_tiles(const int* tiles);
 
 /*
  * Stress update of every voxel: replaces drive_eps_sig(step, iter)

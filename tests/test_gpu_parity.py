@@ -227,6 +227,78 @@ def test_precond_cg_warp_path(gpulib, N):
         s.close()
 
 
+@pytest.mark.parametrize("N", [32, 64, 128, 256])
+@pytest.mark.parametrize("tc", [2, 4, -2, -4])
+def test_green_fp32_tile_shapes(gpulib, N, tc):
+    """Every tile shape of the FP32 register passes the autotuner chooses from, pinned with
+    cpfft_set_tiles: the shared-memory slowest-axis pass (tc > 0) and the one holding each
+    column's rows in registers (tc < 0), against the FP64 operator on the same tangent."""
+    r = rve.make_rve(N, 8, 13)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                      gpulib.PREC_MIXED)
+    try:
+        Fn, Fn1 = random_F(N, 1e-3, 4)
+        s.drive_eps_sig(1, 0, Fn, Fn1, want_P=False)
+        s.set_tiles(16, tc)
+        assert s.tuning()["fp32_tiles"] == [16, tc]
+        x = np.random.default_rng(N).standard_normal((9, N ** 3))
+        for flgK in (True, False):
+            y64 = s.G_K_dF(x, flgK)
+            y32 = s.G_K_dF_f32(x.astype(np.float32), flgK)
+            assert rel(y32, y64) < 1e-5, (flgK, rel(y32, y64))
+    finally:
+        s.close()
+
+
+@pytest.mark.parametrize("tc", [4, -2, -4])
+@pytest.mark.parametrize("N", [32, 64, 128])
+def test_precond_cg_tile_shapes(gpulib, N, tc):
+    """The reference-medium operator (it couples a column's rows) through each slowest-axis
+    pass: the preconditioned mixed CG reaches the plain FP64 CG's solution."""
+    r = rve.make_rve(N, 8, 17)
+    s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED)
+    try:
+        Fn, Fn1 = random_F(N, 2e-3, 5)
+        s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False)
+        b = -s.G_K_dF(np.ones((9, N ** 3)) * 1e-3, True)
+        x64, _ = s.fftPcg(b, 1e-10)
+        s.set_mode(gpulib.PREC_MIXED)
+        s.set_tiles(16, tc)
+        s.drive_eps_sig(1, 1, Fn, Fn1, want_P=False)
+        s.set_precond(gpulib.PRECOND_REFERENCE)
+        xp, _ = s.fftPcg(b, 1e-10)
+        assert rel(xp, x64) < 1e-7, rel(xp, x64)
+        res = s.G_K_dF(xp, True) - b
+        assert np.linalg.norm(res) <= 1.5e-10 * np.linalg.norm(b)
+    finally:
+        s.close()
+
+
+def test_queue_chunk_autotuned(gpulib):
+    """The voxel-queue chunk is chosen on the first implicit queue pass from timed runs of
+    that pass, and the results equal those of the one-block-per-128-voxels schedule."""
+    N = 16
+    r = rve.make_rve(N, 4, 29)
+    Fn, Fn1 = random_F(N, 1e-3, 6)
+    out = []
+    for sched in (gpulib.SCHED_BLOCKS, gpulib.SCHED_QUEUE):
+        s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                          gpulib.PREC_MIXED)
+        try:
+            s.set_mode(gpulib.PREC_MIXED, gpulib.START_TRIAL)
+            s.set_schedule(sched)
+            assert s.queue_chunk()["chunk"] == 0
+            P, K, _ = s.drive_eps_sig(1, 1, Fn, Fn1, want_K4=True)
+            q = s.queue_chunk()
+            if sched == gpulib.SCHED_QUEUE:
+                assert q["chunk"] in (128, 256, 512)
+                assert all(t > 0 for t in q["ms_128_256_512"])
+            out.append((P, K))
+        finally:
+            s.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 @pytest.mark.parametrize("N", [32, 64, 128])
 def test_green_double_float(gpulib, N):
     """The double-float operator of mixed precision against the native FP64 operator on the
