@@ -230,6 +230,13 @@ __device__ __forceinline__ T kval(const TK* __restrict__ K, const float* __restr
                                   long long i) {
   return (T)K[i];
 }
+// the double-float pair of an FP64 tangent entry, split in registers: (float)K and the
+// float of the remainder
+template <>
+__device__ __forceinline__ dfl kval<dfl, double>(const double* __restrict__ K,
+                                                 const float* __restrict__ Klo, long long i) {
+  return from_io<dfl, double>(K[i]);
+}
 template <>
 __device__ __forceinline__ dfl kval<dfl, float>(const float* __restrict__ K,
                                                 const float* __restrict__ Klo, long long i) {
@@ -513,7 +520,7 @@ template <int M, typename T>
 constexpr int minblocks_ae() { return (sizeof(T) == 4 && M == 4) ? 4 : 0; }
 
 // TIO: the field type of x (float, or double for the double-float transform T = dfl,
-// whose tangent is the pair K4, K4lo)
+// whose tangent is the FP64 K4, split into a float pair on load)
 template <int M, typename T, typename TK, typename TIO>
 __global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
                                                const float* __restrict__ K4lo,
