@@ -300,7 +300,8 @@ struct Ctx {
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
   double *r = nullptr, *p = nullptr, *Ap = nullptr, *w = nullptr, *io = nullptr;
   double* w2 = nullptr;  // mixed precision: FP64 copy of an inner correction
-  double* th_x = nullptr;  // mixed precision: tangent_homo's 9 solutions of the last call
+  float* th_x = nullptr;  // mixed precision: tangent_homo's 9 solutions of the last call
+                          // (FP32: they only start the next call's solves)
   bool th_valid = false;
   // logging of (features, converged increments) pairs for the learned initial guess
   float *log_X = nullptr, *log_T = nullptr;
@@ -1124,14 +1125,14 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
 
 // tangent_homo (src/tangent_homo.f:11-73): 9 CG solves, C_homo(i,j) stored at 9*j+i.
 // In mixed precision each solve starts from the fluctuation field the same column
-// converged to in the previous call (the tangent changes little between calls); the
-// stop test, ||r|| <= tol ||b||, is unchanged.  The plain FP64 path starts from zero as
+// converged to in the previous call (the tangent changes little between calls), kept in
+// FP32; the stop test, ||r|| <= tol ||b||, is unchanged.  The plain FP64 path starts from zero as
 // the reference does.
 int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
   const long long N3 = c->N3, n = 9 * N3;
   *its_total = 0;
   const bool warm = c->prec == CPFFT_PREC_MIXED;
-  if (warm && !c->th_x) TRY(dalloc(c->th_x, 9 * n * sizeof(double)));
+  if (warm && !c->th_x) TRY(dalloc(c->th_x, 9 * n * sizeof(float)));
   for (int i = 0; i < 9; i++) {
     for (int j = 0; j < 9; j++)
       CK(cudaMemcpyAsync(c->io + j * N3, c->K4 + (9 * j + i) * N3, N3 * sizeof(double),
@@ -1140,10 +1141,12 @@ int tangent_homo(Ctx* c, double tolPCG, double* C_homo, int* its_total) {
     CK(dev_scale(c->b, -1.0, n, c->st));
     int its = 0;
     if (warm) {
-      if (c->th_valid)
-        CK(cudaMemcpyAsync(c->io, c->th_x + i * n, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+      if (c->th_valid) {
+        CK(cudaMemsetAsync(c->io, 0, n * sizeof(double), c->st));
+        CK(dev_add_f32(c->io, c->th_x + i * n, 1.0, n, c->st));
+      }
       TRY(cg_mixed_any(c, c->b, c->io, tolPCG, &its, c->th_valid));
-      CK(cudaMemcpyAsync(c->th_x + i * n, c->io, n * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+      CK(dev_to_f32(c->th_x + i * n, c->io, 1.0, n, c->st));
     } else {
       TRY(cg(c, c->b, c->io, tolPCG, &its));
     }
