@@ -775,9 +775,12 @@ int cg_pre_body(Ctx* c, bool use_handle, bool timed) {
   GridDesc g = c->g;
   g.pre = 1;
   int np = 0;
-  CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+  // the register-FFT sizes update p = r + beta p inside the first pass of the apply
+  const bool fuse_p = green_df_supported(c->N);
+  if (!fuse_p) CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
   if (timed) kt_start(c, KT_G32);
-  CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np));
+  CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np,
+                            fuse_p ? c->rf : nullptr, fuse_p ? c->sc : nullptr));
   if (timed) TRY(kt_stop(c));
   if (!np) {
     cpfft_set_error("internal: the preconditioned product was not fused");

@@ -66,20 +66,22 @@ cudaError_t green_setup(int N) {
 template <typename T>
 cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                             const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st,
-                            double* part, int* nparts) {
+                            double* part, int* nparts, const T* rfuse, double* scf) {
   const int N = g.N, H = g.H;
   bool warp_path = false;
   if (nparts) *nparts = 0;
+  if (rfuse && !flgK) return cudaErrorInvalidValue;  // the fused update serves G(K : p) only
   if constexpr (sizeof(T) == 4) {
     warp_path = true;
     switch (N) {
-      case 32: wgreen_apply<1, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
-      case 64: wgreen_apply<2, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
-      case 128: wgreen_apply<4, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
-      case 256: wgreen_apply<8, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part); break;
+      case 32: wgreen_apply<1, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part, rfuse, scf); break;
+      case 64: wgreen_apply<2, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part, rfuse, scf); break;
+      case 128: wgreen_apply<4, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part, rfuse, scf); break;
+      case 256: wgreen_apply<8, T>(x, K4, nullptr, flgK, y, S, tw, g, st, part, rfuse, scf); break;
       default: warp_path = false;
     }
   }
+  if (rfuse && !warp_path) return cudaErrorNotSupported;  // the fused update needs the warp passes
   if (warp_path) {
     if (part && nparts) *nparts = (N / 2) * N;
     g_kernel_launches += 5;
@@ -106,7 +108,7 @@ cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Ve
 template <typename T>
 cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st) {
-  return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr);
+  return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr, nullptr, nullptr);
 }
 
 cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2* S,
@@ -114,7 +116,7 @@ cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2
   if (!green_df_supported(g->N)) return cudaSuccess;
   GridDesc t = *g;
   cudaError_t e = tune_tiles(t, [&](const GridDesc& gg) {
-    green_apply_dot<float>(x, K4, 1, y, S, tw, gg, st, nullptr, nullptr);
+    green_apply_dot<float>(x, K4, 1, y, S, tw, gg, st, nullptr, nullptr, nullptr, nullptr);
   }, st, best_ms, true);
   if (e == cudaSuccess) { g->wtb = t.wtb; g->wtc = t.wtc; g->wc2 = t.wc2; }
   return e;
@@ -128,4 +130,5 @@ template cudaError_t green_apply<double>(const double*, const double*, int, doub
 template cudaError_t green_apply<float>(const float*, const float*, int, float*, float2*,
                                         const float2*, GridDesc, cudaStream_t);
 template cudaError_t green_apply_dot<float>(const float*, const float*, int, float*, float2*,
-                                            const float2*, GridDesc, cudaStream_t, double*, int*);
+                                            const float2*, GridDesc, cudaStream_t, double*, int*,
+                                            const float*, double*);

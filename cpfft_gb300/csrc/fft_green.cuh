@@ -45,11 +45,14 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
                         const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st);
 // the same, and with part != nullptr also the partial sums of x . y: *nparts partials
 // in part (the warp-FFT sizes), or *nparts = 0 when this size does not fuse the product
-// (the caller then reduces x . y itself)
+// (the caller then reduces x . y itself).  rfuse != nullptr (FP32 warp-FFT sizes only,
+// else cudaErrorNotSupported): x is the CG direction p, first updated in place to
+// r + beta p (r = rfuse, beta = scf[SC_BETA]; scf[SC_RR] takes scf[SC_RRNEW])
 template <typename T>
 cudaError_t green_apply_dot(const T* x, const T* K4, int flgK, T* y, typename Vec2<T>::t* S,
                             const typename Vec2<T>::t* tw, GridDesc g, cudaStream_t st,
-                            double* part, int* nparts);
+                            double* part, int* nparts, const T* rfuse = nullptr,
+                            double* scf = nullptr);
 template <typename T>
 cudaError_t green_setup(int N);
 

@@ -5,6 +5,7 @@
 #pragma once
 #include "fft_green.cuh"
 #include "fft_warp.cuh"
+#include "krylov.cuh"
 
 namespace {
 
@@ -521,12 +522,17 @@ constexpr int minblocks_ae() { return (sizeof(T) == 4 && M == 4) ? 4 : 0; }
 
 // TIO: the field type of x (float, or double for the double-float transform T = dfl,
 // whose tangent is the FP64 K4, split into a float pair on load)
-template <int M, typename T, typename TK, typename TIO>
-__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
+// FUSEP (FP32 CG iteration): the operand is the CG direction updated in place on load,
+// p = r + beta p with beta = sc[SC_BETA] (x is p, rfuse is r), and sc[SC_RR] takes
+// sc[SC_RRNEW] -- the work of k_cg_p fused into this pass.
+template <int M, typename T, typename TK, typename TIO, bool FUSEP = false>
+__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* x, const TK* __restrict__ K4,
                                                const float* __restrict__ K4lo,
                                                int flgK, typename Vec2<T>::t* __restrict__ S,
                                                GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
-                                               double* __restrict__ part) {
+                                               double* __restrict__ part,
+                                               const TIO* __restrict__ rfuse = nullptr,
+                                               double* scf = nullptr) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
   const int Lp = padlen(N);
@@ -538,14 +544,29 @@ __global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* 
   const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
   const int bl0 = 2 * bp;
   T dsum = 0;
+  T beta = 0;
+  if constexpr (FUSEP) {
+    beta = (T)scf[SC_BETA];
+    if (blockIdx.x == 0 && threadIdx.x == 0) scf[SC_RR] = scf[SC_RRNEW];
+  }
   for (int t = threadIdx.x; t < 2 * N; t += blockDim.x) {
     int l = t / N, a = t - l * N;
     long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
     T y[9];
     if (flgK) {
       T xv[9];
+      if constexpr (FUSEP) {
+        TIO* p = const_cast<TIO*>(x);
 #pragma unroll
-      for (int j = 0; j < 9; j++) xv[j] = from_io<T, TIO>(x[j * N3 + v]);
+        for (int j = 0; j < 9; j++) {
+          const T pv = rfuse[j * N3 + v] + beta * p[j * N3 + v];
+          p[j * N3 + v] = pv;
+          xv[j] = pv;
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 9; j++) xv[j] = from_io<T, TIO>(x[j * N3 + v]);
+      }
 #pragma unroll
       for (int i = 0; i < 9; i++) {
         T s = 0;
@@ -1001,10 +1022,15 @@ cudaError_t wgreen_setup() {
   if ((e = cudaFuncSetAttribute(wpass_a<M, T, TK, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   if ((e = wsetup_b<M, T, 16>()) || (e = wsetup_b<M, T, 32>()) || (e = wsetup_c<M, T, 2>())) return e;
-  if constexpr (small_code<T>())
+  if constexpr (small_code<T>()) {
     if ((e = wsetup_b<M, T, 8>()) || (e = wsetup_c<M, T, 4>()) || (e = wsetup_c2<M, T, 2>()) ||
         (e = wsetup_c2<M, T, 4>()))
       return e;
+    if ((e = cudaFuncSetAttribute(wpass_a<M, T, TK, TIO, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_w<T>(N, ncols9<N>()))))
+      return e;
+  }
   if ((e = cudaFuncSetAttribute(wpass_e<M, T, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem_w<T>(N, ncols9<N>())))) return e;
   return cudaSuccess;
@@ -1037,15 +1063,25 @@ void wlaunch_b_any(int tb, typename Vec2<T>::t* S, const GridDesc& g,
 template <int M, typename T, typename TK = T, typename TIO = T>
 void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* y,
                   typename Vec2<T>::t* S, const typename Vec2<T>::t* tw, const GridDesc& g,
-                  cudaStream_t st, double* part) {
+                  cudaStream_t st, double* part, const TIO* rfuse = nullptr,
+                  double* scf = nullptr) {
   constexpr int N = 32 * M;
   constexpr int NA = ncols9<N>();
   // the fused product: <K : x, x> in pass A for the reference-medium operator (where it
   // equals <x, y> in the K0 inner product), else <x, y> in pass E
   double* part_a = g.pre ? part : nullptr;
   double* part_e = g.pre ? nullptr : part;
-  wpass_a<M, T, TK, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, K4lo, flgK, S, g, tw,
-                                                                    part_a);
+  if constexpr (small_code<T>()) {
+    if (rfuse)
+      wpass_a<M, T, TK, TIO, true><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(
+          x, K4, K4lo, flgK, S, g, tw, part_a, rfuse, scf);
+    else
+      wpass_a<M, T, TK, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, K4lo, flgK, S, g,
+                                                                        tw, part_a);
+  } else {
+    wpass_a<M, T, TK, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, K4lo, flgK, S, g, tw,
+                                                                      part_a);
+  }
   wlaunch_b_any<M, T>(g.wtb, S, g, tw, 0, st);
   if constexpr (small_code<T>()) {
     if (g.wc2 == 4) wlaunch_c2<M, T, 4>(S, g, tw, st);
