@@ -775,12 +775,20 @@ int cg_pre_body(Ctx* c, bool use_handle, bool timed) {
   GridDesc g = c->g;
   g.pre = 1;
   int np = 0;
-  // the register-FFT sizes update p = r + beta p inside the first pass of the apply
-  const bool fuse_p = green_df_supported(c->N);
-  if (!fuse_p) CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
+  if (green_df_supported(c->N)) {
+    // the register-FFT grids run the whole iteration in the five transform passes: p is
+    // updated in the first, x, r and the partials of <r, r>_K0 in the last
+    if (timed) kt_start(c, KT_G32);
+    CK(green_cg_iteration(c->xf, c->rf, c->pf, c->K4f, c->Sf, c->twf, g, c->st, c->part,
+                          c->part, c->pre_dev + 36, c->sc));
+    if (timed) TRY(kt_stop(c));
+    CK(dev_final(c->part, (c->N / 2) * c->N, c->sc, SC_RRNEW, OP_BETA, c->st));
+    CK(dev_cg_cond(c->sc, c->cg_handle, use_handle, c->st));
+    return 0;
+  }
+  CK(dev_cg_p<float>(c->pf, c->rf, n, c->sc, c->st));
   if (timed) kt_start(c, KT_G32);
-  CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np,
-                            fuse_p ? c->rf : nullptr, fuse_p ? c->sc : nullptr));
+  CK(green_apply_dot<float>(c->pf, c->K4f, 1, c->Apf, c->Sf, c->twf, g, c->st, c->part, &np));
   if (timed) TRY(kt_stop(c));
   if (!np) {
     cpfft_set_error("internal: the preconditioned product was not fused");

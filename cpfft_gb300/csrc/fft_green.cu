@@ -111,6 +111,20 @@ cudaError_t green_apply(const T* x, const T* K4, int flgK, T* y, typename Vec2<T
   return green_apply_dot<T>(x, K4, flgK, y, S, tw, g, st, nullptr, nullptr, nullptr, nullptr);
 }
 
+cudaError_t green_cg_iteration(float* x, float* r, float* p, const float* K4, float2* S,
+                               const float2* tw, const GridDesc& g, cudaStream_t st,
+                               double* part_a, double* part_e, const float* k0, double* sc) {
+  switch (g.N) {
+    case 32: wcg_iteration<1>(x, r, p, K4, S, tw, g, st, part_a, part_e, k0, sc); break;
+    case 64: wcg_iteration<2>(x, r, p, K4, S, tw, g, st, part_a, part_e, k0, sc); break;
+    case 128: wcg_iteration<4>(x, r, p, K4, S, tw, g, st, part_a, part_e, k0, sc); break;
+    case 256: wcg_iteration<8>(x, r, p, K4, S, tw, g, st, part_a, part_e, k0, sc); break;
+    default: return cudaErrorNotSupported;
+  }
+  g_kernel_launches += 5;  // the transform passes (dev_final counts its own launch)
+  return cudaGetLastError();
+}
+
 cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2* S,
                                const float2* tw, GridDesc* g, cudaStream_t st, float* best_ms) {
   if (!green_df_supported(g->N)) return cudaSuccess;

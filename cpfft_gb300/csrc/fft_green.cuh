@@ -69,6 +69,14 @@ cudaError_t green_setup(int N);
 // is loaded); S is the FP64 spectral scratch (double-float complex values are 16 bytes too);
 // tw the double-float twiddle table.  Relative error about 1e-13 against the FP64
 // operator, from about a fifth of its time.
+// One preconditioned FP32 CG iteration on the register-FFT grids (32..256), g.pre set:
+// p = r + beta p, y = G0(K : p) with alpha = rr / <K : p, p>, x += alpha p,
+// r -= alpha y, part_e = the (N/2) N block partials of <r, r>_K0 (k0: the 9 x 9 weights);
+// y never reaches memory.  The caller finishes rr_new / beta and the stop test.
+cudaError_t green_cg_iteration(float* x, float* r, float* p, const float* K4, float2* S,
+                               const float2* tw, const GridDesc& g, cudaStream_t st,
+                               double* part_a, double* part_e, const float* k0, double* sc);
+
 bool green_df_supported(int N);
 cudaError_t green_setup_df(int N);
 cudaError_t green_apply_df(const double* x, const double* K4, int flgK,

@@ -972,6 +972,102 @@ __global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_e(const typen
   }
 }
 
+// Pass E fused with the rest of a preconditioned FP32 CG iteration: the inverse transform
+// gives Ap = G0(K : p) on the block's two lines, and x += alpha p, r -= alpha Ap and one
+// partial sum of <r, r>_K0 per block follow at once, so Ap never reaches memory.  x, r and
+// p of the block's voxels are loaded before the transform (their latency hides behind it);
+// each thread owns whole voxels (all 9 components, as the K0 form needs them).
+template <int M>
+__global__ void __launch_bounds__(288, minblocks_ae<M, float>()) wpass_e_xr(
+    const float2* __restrict__ S, GridDesc g, const float2* __restrict__ twg,
+    float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+    const float* __restrict__ k0, const double* __restrict__ sc, double* __restrict__ part) {
+  using T = float;
+  using T2 = float2;
+  constexpr int N = 32 * M, H = N / 2 + 1, NT = 288;
+  constexpr int NV = (2 * N + NT - 1) / NT;  // voxels per thread
+  const int Lp = padlen(N);
+  const long long N3 = g.N3;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* tw = reinterpret_cast<T2*>(smem_raw);
+  T2* col = tw + N;
+  __shared__ float s_k0[81];
+  for (int i = threadIdx.x; i < 81; i += blockDim.x) s_k0[i] = k0[i];
+  load_tw(tw, twg, N);
+  const int bp = blockIdx.x % (N / 2), c = blockIdx.x / (N / 2);
+  const int bl0 = 2 * bp;
+  constexpr int E = 9 * N / NT;
+  static_assert(E * NT == 9 * N, "lines must divide evenly over the block");
+  {
+    T2 X0[E], X1[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
+      const long long base = ((long long)i * N + c) * N;
+      const int kk = k < H ? k : N - k;
+      X0[e] = S[(base + bl0) * H + kk];
+      X1[e] = S[(base + bl0 + 1) * H + kk];
+    }
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const int t = threadIdx.x + e * NT, i = t / N, k = t - i * N;
+      const int kk = k < H ? k : N - k;
+      T2 a = X0[e], b = X1[e];
+      if (kk == 0 || kk == N / 2) { a.y = 0; b.y = 0; }
+      if (k >= H) { a.y = -a.y; b.y = -b.y; }
+      T2 z;  // Z = X0 + i X1 (the inverse is taken as conj(FFT(conj Z)))
+      z.x = a.x - b.y;
+      z.y = a.y + b.x;
+      col[i * Lp + pidx(k)] = z;
+    }
+  }
+  float xv[NV][9], rv[NV][9], pv[NV][9];
+#pragma unroll
+  for (int u = 0; u < NV; u++) {
+    const int vt = threadIdx.x + NT * u;
+    if (vt < 2 * N) {
+      const int l = vt / N, a = vt - l * N;
+      const long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        xv[u][i] = x[i * N3 + v];
+        rv[u][i] = r[i * N3 + v];
+        pv[u][i] = p[i * N3 + v];
+      }
+    }
+  }
+  __syncthreads();
+  block_columns<N, T, true>(col, ncols9<N>(), Lp, tw);
+  __syncthreads();
+  const float alpha = (float)sc[SC_ALPHA];
+  float s = 0.f;
+#pragma unroll
+  for (int u = 0; u < NV; u++) {
+    const int vt = threadIdx.x + NT * u;
+    if (vt < 2 * N) {
+      const int l = vt / N, a = vt - l * N;
+      const long long v = a + (long long)N * (bl0 + l) + (long long)N * N * c;
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        const T2 z = col[i * Lp + pidx(a)];  // unscaled inverse (scale applied in pass C)
+        const float ap = l ? z.y : z.x;
+        xv[u][i] += alpha * pv[u][i];
+        rv[u][i] -= alpha * ap;
+        x[i * N3 + v] = xv[u][i];
+        r[i * N3 + v] = rv[u][i];
+      }
+#pragma unroll
+      for (int i = 0; i < 9; i++) {
+        float t = 0.f;
+#pragma unroll
+        for (int j = 0; j < 9; j++) t += s_k0[9 * i + j] * rv[u][j];
+        s += rv[u][i] * t;
+      }
+    }
+  }
+  block_partial<NT>((double)s, part + blockIdx.x);
+}
+
 template <typename T>
 size_t smem_w(int N, int ncols) { return sizeof(typename Vec2<T>::t) * (size_t)(N + ncols * padlen(N)); }
 template <typename T>
@@ -983,8 +1079,11 @@ constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
 // B/D tiles 16 and 32 and the C tile 2 only)
 constexpr int TB_CAND[3] = {8, 16, 32};
 constexpr int TC_CAND[2] = {2, 4};
-// pass C in registers (wpass_c2, FP32 only): 0 = the shared-memory pass C, else its TK
-constexpr int C2_CAND[3] = {0, 2, 4};
+// pass C in registers (wpass_c2, FP32 only): 0 = the shared-memory pass C, else its TK.
+// The autotuner keeps to one algorithm per grid (the two round differently, and contexts
+// of one grid must give identical results whatever their timings); cpfft_set_tiles
+// selects wpass_c2.
+constexpr int C2_CAND[1] = {0};
 
 template <int M, typename T, int TB>
 cudaError_t wsetup_b() {
@@ -1028,6 +1127,9 @@ cudaError_t wgreen_setup() {
       return e;
     if ((e = cudaFuncSetAttribute(wpass_a<M, T, TK, TIO, true>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_w<T>(N, ncols9<N>()))))
+      return e;
+    if ((e = cudaFuncSetAttribute(wpass_e_xr<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem_w<T>(N, ncols9<N>()))))
       return e;
   }
@@ -1094,6 +1196,28 @@ void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* 
   wlaunch_b_any<M, T>(g.wtb, S, g, tw, 1, st);
   wpass_e<M, T, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(S, y, g, tw,
                                                                  part_e ? x : nullptr, part_e);
+}
+
+// One preconditioned FP32 CG iteration's operator and vector work on the register-FFT
+// grids: pass A with p = r + beta p fused (and the partials of <K : p, p>), alpha from
+// them, passes B-D, pass E fused with x += alpha p, r -= alpha G0(K : p) and the partials
+// of <r, r>_K0 (part_e, (N/2) N of them).  g.pre must be set.
+template <int M>
+void wcg_iteration(float* x, float* r, float* p, const float* K4, float2* S, const float2* tw,
+                   const GridDesc& g, cudaStream_t st, double* part_a, double* part_e,
+                   const float* k0, double* sc) {
+  constexpr int N = 32 * M;
+  constexpr int NA = ncols9<N>();
+  wpass_a<M, float, float, float, true><<<(N / 2) * N, 288, smem_w<float>(N, NA), st>>>(
+      p, K4, nullptr, 1, S, g, tw, part_a, r, sc);
+  dev_final(part_a, (N / 2) * N, sc, SC_PAP, OP_ALPHA, st);
+  wlaunch_b_any<M, float>(g.wtb, S, g, tw, 0, st);
+  if (g.wc2 == 4) wlaunch_c2<M, float, 4>(S, g, tw, st);
+  else if (g.wc2 == 2) wlaunch_c2<M, float, 2>(S, g, tw, st);
+  else if ((g.wtc ? g.wtc : wtile_c<float>()) == 4) wlaunch_c<M, float, 4>(S, g, tw, st);
+  else wlaunch_c<M, float, 2>(S, g, tw, st);
+  wlaunch_b_any<M, float>(g.wtb, S, g, tw, 1, st);
+  wpass_e_xr<M><<<(N / 2) * N, 288, smem_w<float>(N, NA), st>>>(S, g, tw, x, r, p, k0, sc, part_e);
 }
 
 template <typename T>
