@@ -313,7 +313,8 @@ struct Ctx {
   int hn = 0;  // index of the history at n
   float *K4f = nullptr, *xf = nullptr, *rf = nullptr, *pf = nullptr, *Apf = nullptr;
   // mixed precision: FP64-accurate operator in double-float (power-of-two N 32..256):
-  // double-float twiddles (the operator splits the FP64 K4 into float pairs as it loads it)
+  // K4 = K4f + K4lo to 48 bits, double-float twiddles
+  float* K4lo = nullptr;
   dfl2* twdf = nullptr;
   bool df_ok = false;
   GridDesc gdf;            // the double-float operator's tile shapes (autotuned)
@@ -427,7 +428,7 @@ void free_ctx(Ctx* c) {
                   c->Fn, c->Fn1, c->P, c->K4, c->b, c->dFm, c->r, c->p, c->Ap, c->w, c->io, c->w2, c->th_x,
                   c->hist[0], c->hist[1], c->K4f, c->xf, c->rf, c->pf, c->Apf, c->ori, c->crys,
                   c->oris, c->cryss, c->S, c->Sf, c->tw, c->twf, c->part, c->sc, c->stats,
-                  c->k0sum, c->twdf, c->vcost, c->vperm, c->vq, c->pre_dev,
+                  c->k0sum, c->K4lo, c->twdf, c->vcost, c->vperm, c->vq, c->pre_dev,
                   c->mises, c->misess};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -505,7 +506,7 @@ int matvec_acc(Ctx* c, const double* x, double* y, int flgK) {
     return matvec64(c, x, y, flgK);
   c->f64_matvecs++;
   kt_start(c, KT_G64);
-  TRY(cuda_check(green_apply_df(x, c->K4, flgK, y, reinterpret_cast<dfl2*>(c->S),
+  TRY(cuda_check(green_apply_df(x, c->K4f, c->K4lo, flgK, y, reinterpret_cast<dfl2*>(c->S),
                                 c->twdf, c->gdf, c->st),
                  "green_apply double-float"));
   return kt_stop(c);
@@ -1042,6 +1043,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.P = c->P;
   a.K4 = c->K4;
   a.K4f = c->prec == CPFFT_PREC_MIXED ? c->K4f : nullptr;
+  a.K4lo = c->prec == CPFFT_PREC_MIXED && c->df_ok ? c->K4lo : nullptr;
   a.tangent_f32 = c->prec == CPFFT_PREC_MIXED && c->tangent_f32;
   a.ori = c->ori;
   a.crys = c->crys;
@@ -1243,6 +1245,7 @@ int alloc_mixed(Ctx* c) {
   CK(cudaMemcpy(c->twf, twf.data(), c->N * sizeof(float2), cudaMemcpyHostToDevice));
   CK(green_setup<float>(c->N));
   if (green_df_supported(c->N)) {
+    TRY(dalloc(c->K4lo, 81 * c->N3 * sizeof(float)));
     TRY(dalloc(c->twdf, c->N * sizeof(dfl2)));
     std::vector<dfl2> tw(c->N);
     for (int k = 0; k < c->N; k++) {
@@ -1257,13 +1260,14 @@ int alloc_mixed(Ctx* c) {
     c->df_ok = true;
     // tile shapes of both operators, timed on this GPU with this grid's buffers
     CK(cudaMemsetAsync(c->K4f, 0, 81 * c->N3 * sizeof(float), c->st));
+    CK(cudaMemsetAsync(c->K4lo, 0, 81 * c->N3 * sizeof(float), c->st));
     CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
     CK(cudaMemsetAsync(c->io, 0, n * sizeof(double), c->st));
     CK(green_autotune_f32(c->xf, c->K4f, c->Apf, c->Sf, c->twf, &c->g, c->st, &c->tune_ms[0]));
     c->gdf = c->g;
     c->gdf.wtc = 0;
     c->gdf.wc2 = 0;
-    CK(green_autotune_df(c->io, c->K4, c->b, reinterpret_cast<dfl2*>(c->S), c->twdf,
+    CK(green_autotune_df(c->io, c->K4f, c->K4lo, c->b, reinterpret_cast<dfl2*>(c->S), c->twdf,
                          &c->gdf, c->st, &c->tune_ms[1]));
     g_kernel_launches = launches0;  // tuning launches are not the caller's work
     if (c->log)
@@ -1758,11 +1762,16 @@ int cpfft_set_K4(const double* K4) {
   Ctx* c = g_ctx;
   CK(cudaMemcpyAsync(c->K4, K4, 81 * c->N3 * sizeof(double), cudaMemcpyHostToDevice, c->st));
   if (c->prec == CPFFT_PREC_MIXED) {
-    // FP32 copy for the inner solves
+    // FP32 copy for the inner solves (and its FP32 remainder for the double-float operator)
     std::vector<float> kf(81 * c->N3);
     for (long long i = 0; i < 81 * c->N3; i++) kf[i] = (float)K4[i];
     CK(cudaMemcpyAsync(c->K4f, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
     TRY(sync(c));
+    if (c->df_ok) {
+      for (long long i = 0; i < 81 * c->N3; i++) kf[i] = (float)(K4[i] - (double)(float)K4[i]);
+      CK(cudaMemcpyAsync(c->K4lo, kf.data(), kf.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+      TRY(sync(c));
+    }
     c->K4f_valid = true;
     if (pre_applies(c)) {
       TRY(reference_reduce(c));

@@ -93,6 +93,7 @@ struct StressArgs {
   double* P;             // (9, N3)
   double* K4;            // (81, N3)
   float* K4f;            // (81, N3) optional FP32 copy (mixed precision), may be null
+  float* K4lo;           // (81, N3) optional FP32 remainder K4 - K4f (double-float operator)
   const int* ori;        // (N3) orientation record id
   const int* crys;       // (N3) crystal id, 0-based
   const OriRec* oris;

@@ -65,8 +65,8 @@ cudaError_t green_setup(int N);
 
 // FP64-accurate y = G(K : x) (flgK = 1) or G(x) in double-float arithmetic on the FP32
 // pipes, for the power-of-two grids 32..256 of the warp-FFT passes (green_df_supported).
-// x, y, K are FP64 fields (each tangent entry is split into a float pair, 48 bits, as it
-// is loaded); S is the FP64 spectral scratch (double-float complex values are 16 bytes too);
+// x, y are FP64 fields; K is given as the float pair K4hi + K4lo (the FP64 tangent to 48
+// bits); S is the FP64 spectral scratch (double-float complex values are 16 bytes too);
 // tw the double-float twiddle table.  Relative error about 1e-13 against the FP64
 // operator, from about a fifth of its time.
 // One preconditioned FP32 CG iteration on the register-FFT grids (32..256), g.pre set:
@@ -79,7 +79,7 @@ cudaError_t green_cg_iteration(float* x, float* r, float* p, const float* K4, fl
 
 bool green_df_supported(int N);
 cudaError_t green_setup_df(int N);
-cudaError_t green_apply_df(const double* x, const double* K4, int flgK,
+cudaError_t green_apply_df(const double* x, const float* K4hi, const float* K4lo, int flgK,
                            double* y, dfl2* S, const dfl2* tw, GridDesc g, cudaStream_t st);
 
 // Autotuner of the warp passes' tile shapes: times every candidate (columns per block of
@@ -88,5 +88,5 @@ cudaError_t green_apply_df(const double* x, const double* K4, int flgK,
 // contents are overwritten (y, S).  No-op for sizes without warp passes.
 cudaError_t green_autotune_f32(const float* x, const float* K4, float* y, float2* S,
                                const float2* tw, GridDesc* g, cudaStream_t st, float* best_ms);
-cudaError_t green_autotune_df(const double* x, const double* K4, double* y,
+cudaError_t green_autotune_df(const double* x, const float* K4hi, const float* K4lo, double* y,
                               dfl2* S, const dfl2* tw, GridDesc* g, cudaStream_t st, float* best_ms);

@@ -231,13 +231,6 @@ __device__ __forceinline__ T kval(const TK* __restrict__ K, const float* __restr
                                   long long i) {
   return (T)K[i];
 }
-// the double-float pair of an FP64 tangent entry, split in registers: (float)K and the
-// float of the remainder
-template <>
-__device__ __forceinline__ dfl kval<dfl, double>(const double* __restrict__ K,
-                                                 const float* __restrict__ Klo, long long i) {
-  return from_io<dfl, double>(K[i]);
-}
 template <>
 __device__ __forceinline__ dfl kval<dfl, float>(const float* __restrict__ K,
                                                 const float* __restrict__ Klo, long long i) {
@@ -521,7 +514,7 @@ template <int M, typename T>
 constexpr int minblocks_ae() { return (sizeof(T) == 4 && M == 4) ? 4 : 0; }
 
 // TIO: the field type of x (float, or double for the double-float transform T = dfl,
-// whose tangent is the FP64 K4, split into a float pair on load)
+// whose tangent is the pair K4, K4lo)
 // FUSEP (FP32 CG iteration): the operand is the CG direction updated in place on load,
 // p = r + beta p with beta = sc[SC_BETA] (x is p, rfuse is r), and sc[SC_RR] takes
 // sc[SC_RRNEW] -- the work of k_cg_p fused into this pass.

@@ -1351,7 +1351,7 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
     for (int i = 0; i < 9; i++) a.P[i * N3 + v] = detF * P[i];
   }
   if (a.tangent_f32) {
-    // the fast form's tangent in FP32 (K4 = K4f exactly)
+    // the fast form's tangent in FP32 (K4 = K4f exactly, K4lo = 0)
     float f[9], f1[9], tf[9], rh[9], r1[9], fhi[9], f1i[9], cf[36], Af[81];
     for (int i = 0; i < 9; i++) {
       f[i] = (float)Fn[i]; f1[i] = (float)Fn1[i]; tf[i] = (float)tm[i]; rh[i] = (float)rnh[i];
@@ -1362,6 +1362,8 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
     for (int m = 0; m < 81; m++) a.K4[m * N3 + v] = (double)Af[m];
     if (a.K4f)
       for (int m = 0; m < 81; m++) a.K4f[m * N3 + v] = Af[m];
+    if (a.K4lo)
+      for (int m = 0; m < 81; m++) a.K4lo[m * N3 + v] = 0.0f;
     return;
   }
   double A[81];
@@ -1369,6 +1371,11 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
   for (int m = 0; m < 81; m++) a.K4[m * N3 + v] = A[m];
   if (a.K4f)
     for (int m = 0; m < 81; m++) a.K4f[m * N3 + v] = (float)A[m];
+  if (a.K4lo)
+    for (int m = 0; m < 81; m++) {
+      const float h = (float)A[m];
+      a.K4lo[m * N3 + v] = (float)(A[m] - (double)h);
+    }
 }
 
 #if CPFFT_FIRST_UNIT
