@@ -1072,11 +1072,14 @@ constexpr int wtile_c() { return sizeof(T) == 4 ? 4 : 2; }
 // B/D tiles 16 and 32 and the C tile 2 only)
 constexpr int TB_CAND[3] = {8, 16, 32};
 constexpr int TC_CAND[2] = {2, 4};
-// pass C in registers (wpass_c2, FP32 only): 0 = the shared-memory pass C, else its TK.
-// The autotuner keeps to one algorithm per grid (the two round differently, and contexts
-// of one grid must give identical results whatever their timings); cpfft_set_tiles
-// selects wpass_c2.
-constexpr int C2_CAND[1] = {0};
+// pass C in registers (wpass_c2, FP32 only): its TK.  The slowest-axis algorithm is fixed
+// per grid, because the two round differently and contexts of one grid must give identical
+// results whatever their timings: in registers up to N = 64 (64^3: 12.9 against 19.4 us a
+// launch), in shared memory above (128^3: 120 against 103 us), measured with ncu on a
+// GB300; the autotuner then chooses the tiles within that algorithm.  cpfft_set_tiles
+// selects either.
+constexpr int C2_CAND[2] = {2, 4};
+constexpr int C2_MAX_N = 64;
 
 template <int M, typename T, int TB>
 cudaError_t wsetup_b() {
@@ -1251,18 +1254,20 @@ cudaError_t tune_tiles(GridDesc& g, C&& one_apply, cudaStream_t st, float* best_
                        bool all_shapes) {
   float best = 1e30f;
   int btb = 16, btc = 2, bc2 = 0;
+  const bool regs_c = all_shapes && g.N <= C2_MAX_N;  // FP32 only (all_shapes)
   for (int tb : TB_CAND)
     for (int tc : TC_CAND)
       for (int c2 : C2_CAND) {
-        if (!all_shapes && (tb == 8 || tc == 4 || c2)) continue;
-        if (c2 && tc != TC_CAND[0]) continue;  // the register pass C has its own tile
+        if (!all_shapes && (tb == 8 || tc == 4)) continue;
+        // one loop over the tiles of the grid's slowest-axis algorithm
+        if (regs_c ? tc != TC_CAND[0] : c2 != C2_CAND[0]) continue;
         g.wtb = tb;
         g.wtc = tc;
-        g.wc2 = c2;
+        g.wc2 = regs_c ? c2 : 0;
         float ms = 0.f;
         cudaError_t e = time_applies([&] { one_apply(g); }, 5, st, &ms);
         if (e != cudaSuccess) return e;
-        if (ms < best) { best = ms; btb = tb; btc = tc; bc2 = c2; }
+        if (ms < best) { best = ms; btb = tb; btc = tc; bc2 = g.wc2; }
       }
   g.wtb = btb;
   g.wtc = btc;
