@@ -210,6 +210,8 @@ def make_solver(cp, r, form, args):
             s.set_precond(cp.PRECOND_REFERENCE)
     if args.tol_equil > 0:
         s.set_equilibrium_tol(args.tol_equil)
+        if form != "fp64" and args.inexact > 0:
+            s.set_inexact_newton(args.inexact)
     return s
 
 
@@ -528,7 +530,9 @@ def config_dict(args, impl):
                            if fast and args.mode != "fp64" else "reference predictor",
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
             "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10,
-                           "equilibrium": args.tol_equil},
+                           "equilibrium": args.tol_equil,
+                           "inexact_newton_eta_max": (args.inexact if fast and args.mode != "fp64"
+                                                      and args.tol_equil > 0 else 0.0)},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
             "stress_schedule": args.schedule if fast else "blocks",
             "tangent": args.tangent if fast else "f64",
@@ -754,6 +758,9 @@ def main():
     ap.add_argument("--tol-nr", type=float, default=1e-6)
     ap.add_argument("--tol-equil", type=float, default=1e-6)
     ap.add_argument("--max-iter", type=int, default=30)
+    # fast forms: inexact Newton (each Newton system solved as far as the equilibrium
+    # residual needs, at most this relative tolerance; 0 = every solve to the CG tolerance)
+    ap.add_argument("--inexact", type=float, default=1e-2)
     ap.add_argument("--fp64-steps", type=int, default=5,
                     help="timed steps of the plain FP64 form (after the same warm-up), at "
                          "most --steps")

@@ -122,6 +122,7 @@ SIGNATURES = {
     "cpfft_set_mode": (_I, [_I, _I]),
     "cpfft_set_precond": (_I, [_I]),
     "cpfft_set_equilibrium_tol": (_I, [_D]),
+    "cpfft_set_inexact_newton": (_I, [_D]),
     "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
@@ -322,6 +323,11 @@ class Solver:
     def set_precond(self, precond=PRECOND_REFERENCE):
         """Reference-medium preconditioner of the mixed-precision inner iterations."""
         _check(load_library().cpfft_set_precond(int(precond)), "cpfft_set_precond")
+
+    def set_inexact_newton(self, eta_max):
+        """Solve each Newton system of nr3_step only as far as the equilibrium residual
+        needs (Eisenstat-Walker forcing, at most eta_max; needs set_equilibrium_tol)."""
+        _check(load_library().cpfft_set_inexact_newton(float(eta_max)), "cpfft_set_inexact_newton")
 
     def set_equilibrium_tol(self, tol):
         """Also require ||G(P)|| / (sqrt(N3) ||P_bar||) <= tol to end a Newton loop of

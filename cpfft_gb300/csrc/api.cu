@@ -356,6 +356,9 @@ struct Ctx {
   double barF_t[9], P_bar[9], C_homo[81];
   // equilibrium stop test of the Newton loop (cpfft_set_equilibrium_tol; 0 = the reference's)
   double eq_tol = 0.0;
+  // inexact Newton (cpfft_set_inexact_newton; 0 = every Krylov solve to tolPCG): the
+  // largest relative tolerance of a Newton system's solve
+  double eta_max = 0.0;
   // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
   // starts dropped, sub-stepped solves (cpfft_pass_counts)
   long long last_pass[5] = {0, 0, 0, 0, 0};
@@ -1589,6 +1592,16 @@ int cpfft_set_precond(int precond) {
   return 0;
 }
 
+int cpfft_set_inexact_newton(double eta_max) {
+  TRY(need_ctx());
+  if (!(eta_max >= 0.0 && eta_max < 1.0)) {
+    cpfft_set_error("cpfft_set_inexact_newton: eta_max must lie in [0, 1)");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  g_ctx->eta_max = eta_max;
+  return 0;
+}
+
 int cpfft_set_equilibrium_tol(double tol) {
   TRY(need_ctx());
   if (!(tol >= 0.0) || !std::isfinite(tol)) {
@@ -1897,10 +1910,13 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     CK(dev_scale(c->b, -1.0, n, c->st));
     int its;
     auto a = clk::now();
-    TRY(cg(c, c->b, c->dFm, tolPCG, &its));
+    // inexact Newton: the predictor's system only starts the iteration
+    const bool inexact = c->eta_max > 0.0 && c->eq_tol > 0.0;
+    TRY(cg(c, c->b, c->dFm, inexact ? std::max(tolPCG, c->eta_max) : tolPCG, &its));
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
     double resfft = 1.0;
+    double eta = c->eta_max, eq_last = HUGE_VAL;
     int iiter_EBC = 0;
     // With the equilibrium test the loop body starts with the stress update, so the
     // update that follows the last accepted increment (the reference's closing
@@ -1947,8 +1963,21 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
         frac = 1.0;
       }
       CK(dev_scale(c->b, -1.0, n, c->st));
+      double tol_k = tolPCG;
+      if (inexact) {
+        // Eisenstat-Walker forcing (choice 2, gamma 0.9, exponent 2) with its safeguard,
+        // no tighter than the equilibrium tolerance needs, never below tolPCG
+        const double e = S.res_equil;
+        double eta_k = eq_last < HUGE_VAL ? 0.9 * (e / eq_last) * (e / eq_last) : c->eta_max;
+        const double sg = 0.9 * eta * eta;
+        if (sg > 0.1) eta_k = std::max(eta_k, sg);
+        eta_k = std::max(eta_k, 0.5 * c->eq_tol / e);
+        eta = std::min(c->eta_max, eta_k);
+        eq_last = e;
+        tol_k = std::max(tolPCG, eta);
+      }
       a = clk::now();
-      TRY(cg(c, c->b, c->dFm, tolPCG, &its));
+      TRY(cg(c, c->b, c->dFm, tol_k, &its));
       tp += sec(a);
       CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
       double dn;
@@ -2000,7 +2029,8 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     }
     a = clk::now();
     int th;
-    TRY(tangent_homo(c, tolPCG, c->C_homo, &th));
+    // the homogenised tangent only steers the P_bar update (its loop tests P_bar itself)
+    TRY(tangent_homo(c, inexact ? std::max(tolPCG, 1e-6) : tolPCG, c->C_homo, &th));
     tp += sec(a);
     for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
     TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));

@@ -329,6 +329,20 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR,
 int cpfft_set_equilibrium_tol(double tol);
 
 /*
+ * Inexact Newton (extension; the reference solves every Newton system to the CG
+ * tolerance, src/FFT_nr3.f:95, 112).  With eta_max > 0 and the equilibrium test on
+ * (cpfft_set_equilibrium_tol), cpfft_nr3_step solves each Newton system to the relative
+ * tolerance eta_k = min(eta_max, 0.9 (e_k / e_{k-1})^2) (Eisenstat-Walker's second
+ * choice with its safeguard max(eta_k, 0.9 eta_{k-1}^2) when that exceeds 0.1, and no
+ * tighter than 0.5 tol / e_k), e_k the equilibrium residual of iterate k; the predictor's
+ * system to eta_max and the homogenised tangent's to 1e-6 (it only steers the P_bar
+ * update), never below tolPCG.  The loop still ends on the equilibrium test, so the
+ * converged state meets the same tolerance with fewer Krylov iterations.  eta_max = 0
+ * (the default) solves every system to tolPCG.
+ */
+int cpfft_set_inexact_newton(double eta_max);
+
+/*
  * Start of FFT_nr3 (src/FFT_nr3.f:36-47): the initial drive_eps_sig(1,0) of the
  * `compute` command (src/FFT_finite_3d.f:145) and the first tangent_homo.
  */

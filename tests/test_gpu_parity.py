@@ -318,6 +318,41 @@ def test_green_double_float(gpulib, N):
         s.close()
 
 
+def test_inexact_newton_vs_fp64_32(gpulib):
+    """Inexact Newton in the fast form (Eisenstat-Walker forcing, eta_max 1e-2) under the
+    equilibrium test, against the plain FP64 form with every system solved to 1e-10: both
+    meet the equilibrium tolerance, P_bar agrees to 1e-7, and the fast form needs fewer
+    Krylov iterations."""
+    N = 32
+    r = rve.make_rve(N, 8, 23)
+    load = rve.uniaxial_tension(0.02, 20)
+    out = []
+    for fast in (False, True):
+        s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
+                          gpulib.PREC_MIXED if fast else gpulib.PREC_FP64)
+        try:
+            s.set_equilibrium_tol(1e-7)
+            if fast:
+                s.set_mode(gpulib.PREC_MIXED, gpulib.START_ITERATE | gpulib.START_TRIAL |
+                           gpulib.TANGENT_F32)
+                s.set_precond(gpulib.PRECOND_REFERENCE)
+                s.set_inexact_newton(1e-2)
+            s.nr3_begin(1e-10)
+            pb, cg = [], 0
+            for step in (1, 2, 3):
+                rc, Pbar, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10,
+                                          30)
+                assert rc >= 0 and st["res_equil"] <= 1e-7
+                pb.append(Pbar)
+                cg += st["cg_iters"]
+            out.append((np.array(pb), cg))
+        finally:
+            s.close()
+    (p64, cg64), (pfast, cgfast) = out
+    assert rel(pfast, p64) < 1e-7, rel(pfast, p64)
+    assert cgfast < cg64
+
+
 def test_mixed_fast_vs_fp64_32(gpulib):
     """The fast form at a warp-FFT size (FP32 inner CG with the reference-medium
     preconditioner, double-float outer residuals, iterate + trial local starts, FP32
