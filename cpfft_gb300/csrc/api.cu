@@ -359,6 +359,7 @@ struct Ctx {
   // inexact Newton (cpfft_set_inexact_newton; 0 = every Krylov solve to tolPCG): the
   // largest relative tolerance of a Newton system's solve
   double eta_max = 0.0;
+  bool cg_rel_only = false;  // the current solve stops on ||r|| <= tol ||b|| alone
   // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
   // starts dropped, sub-stepped solves (cpfft_pass_counts)
   long long last_pass[5] = {0, 0, 0, 0, 0};
@@ -691,6 +692,8 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
     return CPFFT_ERR_BAD_ARG;
   }
   const double tolb = tol * n2b;
+  // the reference's absolute test ||r|| <= tol, off for the inexact Newton solves
+  const double tola = c->cg_rel_only ? 0.0 : tol;
   // FP32 CG on scaled vectors (rf = r / ||r_true||) with reliable updates: whenever the
   // recursive FP32 residual has dropped by `delta` since the last true residual, the
   // FP32 increment is projected and added to x in FP64, the true residual
@@ -706,7 +709,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
     if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    if (rn <= tolb || rn <= tol) {
+    if (rn <= tolb || rn <= tola) {
       c->cg_solves++;
       return 0;
     }
@@ -731,7 +734,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
     TRY(read_scalar(c, SC_RRNEW, &rr));
     if (!std::isfinite(rr)) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
     const double rest = std::sqrt(rr) / scale;
-    if (rest < delta * maxr || rest <= tolb || rest <= tol || it >= maxIter) {
+    if (rest < delta * maxr || rest <= tolb || rest <= tola || it >= maxIter) {
       // reliable update
       restarts++;
       CK(cudaMemsetAsync(c->w2, 0, n * sizeof(double), c->st));
@@ -742,7 +745,7 @@ int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool us
       CK(dev_sub(c->w, b, c->Ap, n, c->st));
       TRY(dnrm2(c, c->w, &rn));
       if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
-      if (rn <= tolb || rn <= tol) { converged = true; break; }
+      if (rn <= tolb || rn <= tola) { converged = true; break; }
       if (it >= maxIter) break;
       const double nscale = 1.0 / rn, k = nscale / scale;
       CK(dev_to_f32(c->rf, c->w, nscale, n, c->st));
@@ -919,13 +922,15 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
     return CPFFT_ERR_BAD_ARG;
   }
   const double tolb = tol * n2b;
+  // the reference's absolute test ||r|| <= tol, off for the inexact Newton solves
+  const double tola = c->cg_rel_only ? 0.0 : tol;
   double rn = n2b;
   if (use_x0) {
     TRY(matvec_acc(c, x, c->Ap, 1));
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
     if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    if (rn <= tolb || rn <= tol) {
+    if (rn <= tolb || rn <= tola) {
       c->cg_solves++;
       return 0;
     }
@@ -949,7 +954,7 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
     // true residual it predicts meets the stop test, or maxIter
     int stop = 0;
     double rr_prev = rr;
-    TRY(cg_segment(c, rr, rn, tolb, tol, delta, it, maxIter, beta, &rr, &rr_prev, &it, &stop));
+    TRY(cg_segment(c, rr, rn, tolb, tola, delta, it, maxIter, beta, &rr, &rr_prev, &it, &stop));
     if (stop == STOP_NONFINITE) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
     // reliable update: x += G(xf / scale) in FP64-accurate arithmetic, true residual
     restarts++;
@@ -961,7 +966,7 @@ int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, boo
     CK(dev_sub(c->w, b, c->Ap, n, c->st));
     TRY(dnrm2(c, c->w, &rn));
     if (!std::isfinite(rn)) { cpfft_set_error("FP64 residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    if (rn <= tolb || rn <= tol) { converged = true; break; }
+    if (rn <= tolb || rn <= tola) { converged = true; break; }
     if (it >= maxIter) break;
     // restart from G0 of the true residual, keeping the search direction (rescaled)
     const double nscale = 1.0 / rn, k = nscale / scale;
@@ -1840,6 +1845,7 @@ int cpfft_green_apply_df(const double* x, double* y, int flgK) {
 int cpfft_cg(const double* b, double* x, double tol, int* iters) {
   TRY(need_ctx());
   Ctx* c = g_ctx;
+  c->cg_rel_only = false;
   const size_t f9 = 9 * c->N3 * sizeof(double);
   int its = 0;
   CK(cudaMemcpyAsync(c->b, b, f9, cudaMemcpyHostToDevice, c->st));
@@ -1884,6 +1890,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
   cpfft_stats S;
   memset(&S, 0, sizeof(S));
   c->cg_iters = c->cg_solves = c->f64_matvecs = c->f32_matvecs = 0;
+  c->cg_rel_only = false;
   TRY(kt_drain(c));
   kt_reset(c);
   const long long launches0 = g_kernel_launches;
@@ -1912,7 +1919,9 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     auto a = clk::now();
     // inexact Newton: the predictor's system only starts the iteration
     const bool inexact = c->eta_max > 0.0 && c->eq_tol > 0.0;
+    c->cg_rel_only = inexact;
     TRY(cg(c, c->b, c->dFm, inexact ? std::max(tolPCG, c->eta_max) : tolPCG, &its));
+    c->cg_rel_only = false;
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
     double resfft = 1.0;
@@ -1977,7 +1986,9 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
         tol_k = std::max(tolPCG, eta);
       }
       a = clk::now();
+      c->cg_rel_only = inexact;
       TRY(cg(c, c->b, c->dFm, tol_k, &its));
+      c->cg_rel_only = false;
       tp += sec(a);
       CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
       double dn;
