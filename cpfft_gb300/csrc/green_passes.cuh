@@ -519,13 +519,14 @@ constexpr int minblocks_ae() { return (sizeof(T) == 4 && M == 4) ? 4 : 0; }
 // p = r + beta p with beta = sc[SC_BETA] (x is p, rfuse is r), and sc[SC_RR] takes
 // sc[SC_RRNEW] -- the work of k_cg_p fused into this pass.
 template <int M, typename T, typename TK, typename TIO, bool FUSEP = false>
-__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* x, const TK* __restrict__ K4,
+__global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* __restrict__ x, const TK* __restrict__ K4,
                                                const float* __restrict__ K4lo,
                                                int flgK, typename Vec2<T>::t* __restrict__ S,
                                                GridDesc g, const typename Vec2<T>::t* __restrict__ twg,
                                                double* __restrict__ part,
                                                const TIO* __restrict__ rfuse = nullptr,
-                                               double* scf = nullptr) {
+                                               double* scf = nullptr,
+                                               TIO* __restrict__ pout = nullptr) {
   using T2 = typename Vec2<T>::t;
   constexpr int N = 32 * M, H = N / 2 + 1;
   const int Lp = padlen(N);
@@ -549,13 +550,12 @@ __global__ void __launch_bounds__(288, minblocks_ae<M, T>()) wpass_a(const TIO* 
     if (flgK) {
       T xv[9];
       if constexpr (FUSEP) {
-        TIO* p = const_cast<TIO*>(x);
+        // x (read) and pout (write) are the same field: each element is read, then
+        // written, by this thread alone
 #pragma unroll
-        for (int j = 0; j < 9; j++) {
-          const T pv = rfuse[j * N3 + v] + beta * p[j * N3 + v];
-          p[j * N3 + v] = pv;
-          xv[j] = pv;
-        }
+        for (int j = 0; j < 9; j++) xv[j] = rfuse[j * N3 + v] + beta * x[j * N3 + v];
+#pragma unroll
+        for (int j = 0; j < 9; j++) pout[j * N3 + v] = xv[j];
       } else {
 #pragma unroll
         for (int j = 0; j < 9; j++) xv[j] = from_io<T, TIO>(x[j * N3 + v]);
@@ -1172,7 +1172,7 @@ void wgreen_apply(const TIO* x, const TK* K4, const float* K4lo, int flgK, TIO* 
   if constexpr (small_code<T>()) {
     if (rfuse)
       wpass_a<M, T, TK, TIO, true><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(
-          x, K4, K4lo, flgK, S, g, tw, part_a, rfuse, scf);
+          x, K4, K4lo, flgK, S, g, tw, part_a, rfuse, scf, const_cast<TIO*>(x));
     else
       wpass_a<M, T, TK, TIO><<<(N / 2) * N, 288, smem_w<T>(N, NA), st>>>(x, K4, K4lo, flgK, S, g,
                                                                         tw, part_a);
@@ -1205,7 +1205,7 @@ void wcg_iteration(float* x, float* r, float* p, const float* K4, float2* S, con
   constexpr int N = 32 * M;
   constexpr int NA = ncols9<N>();
   wpass_a<M, float, float, float, true><<<(N / 2) * N, 288, smem_w<float>(N, NA), st>>>(
-      p, K4, nullptr, 1, S, g, tw, part_a, r, sc);
+      p, K4, nullptr, 1, S, g, tw, part_a, r, sc, p);
   dev_final(part_a, (N / 2) * N, sc, SC_PAP, OP_ALPHA, st);
   wlaunch_b_any<M, float>(g.wtb, S, g, tw, 0, st);
   if (g.wc2 == 4) wlaunch_c2<M, float, 4>(S, g, tw, st);
