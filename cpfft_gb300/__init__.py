@@ -127,7 +127,7 @@ SIGNATURES = {
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
     "cpfft_set_tiles": (_I, [_IP]),
-    "cpfft_queue_chunk": (_I, [_IP, _DP]),
+    "cpfft_queue_chunk": (_I, [_IP, _IP, _DP]),
     "cpfft_format_flat": (_I, [_I, ctypes.c_char_p, _LL, _P(_LL)]),
     "cpfft_write_flat": (_I, [_I, _I, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_format_e15": (_I, [_DP, _LL, ctypes.c_char_p]),
@@ -302,10 +302,12 @@ class Solver:
 
     def queue_chunk(self):
         """The autotuned voxel-queue chunk and the candidates' pass times (ms)."""
-        v = ctypes.c_int(0)
-        ms = np.zeros(3)
-        _check(load_library().cpfft_queue_chunk(ctypes.byref(v), _dp(ms)), "cpfft_queue_chunk")
-        return {"chunk": v.value, "ms_128_256_512": ms.tolist()}
+        v, b = ctypes.c_int(0), ctypes.c_int(0)
+        ms = np.zeros(6)
+        _check(load_library().cpfft_queue_chunk(ctypes.byref(v), ctypes.byref(b), _dp(ms)),
+               "cpfft_queue_chunk")
+        return {"chunk": v.value, "blocks_per_sm": b.value or "all",
+                "ms_128_256_512": ms[:3].tolist(), "ms_one_block_per_sm": ms[3:].tolist()}
 
     def set_tiles(self, fp32_bd, fp32_c, df_bd=16, df_c=2):
         """Pin the register passes' tile shapes (fp32_c < 0: the register-resident

@@ -293,8 +293,10 @@ struct Ctx {
   int* vperm = nullptr;            // (N3) queue order
   unsigned int* vq = nullptr;      // 2 x 64 bin counters / offsets + the queue head
   int qchunk = 128;                // voxels a block takes from the queue at a time
+  int qbps = 0;                    // persistent blocks per SM (0: as many as fit)
   bool qtuned = false;             // the chunk has been autotuned (first implicit queue pass)
-  float qchunk_ms[3] = {0.f, 0.f, 0.f};  // tuning times for 128 / 256 / 512
+  // tuning times: chunks 128 / 256 / 512 with as many blocks per SM as fit, then with one
+  float qchunk_ms[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   cudaStream_t st = nullptr;
   GridDesc g;
   double *Fn = nullptr, *Fn1 = nullptr, *P = nullptr, *K4 = nullptr, *b = nullptr, *dFm = nullptr;
@@ -1003,8 +1005,10 @@ int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
                                      : cg64(c, b, x, tol, iters);
 }
 
-// Queue chunk autotuner: on the context's first implicit queue pass, the pass runs once
-// per candidate chunk (voxels a block takes from the work queue at a time), timed with
+// Queue autotuner: on the context's first implicit queue pass, the pass runs once per
+// candidate -- chunk (voxels a block takes from the work queue at a time) 128 / 256 / 512,
+// with as many persistent blocks per SM as fit or with one (half the threads in flight:
+// their local-memory spill working set then stays closer to the L2's size) -- timed with
 // CUDA events, and the fastest is kept.  The runs give identical results (no local solve
 // of this pass starts from an earlier pass's state); their statistics and logged pairs
 // are not kept.
@@ -1017,9 +1021,11 @@ int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   float best = 1e30f;
-  int bestq = 128;
+  int bestq = 128, bestb = 0, k = 0;
+  for (int bps : {0, 1})
   for (int q : {128, 256, 512}) {
     a.qchunk = q;
+    a.qbps = bps;
     CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
     CK(cudaEventRecord(e0, c->st));
     CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
@@ -1028,16 +1034,19 @@ int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
-    c->qchunk_ms[q == 128 ? 0 : q == 256 ? 1 : 2] = ms;
-    if (ms < best) { best = ms; bestq = q; }
+    c->qchunk_ms[k++] = ms;
+    if (ms < best) { best = ms; bestq = q; bestb = bps; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   g_kernel_launches = l0;  // tuning launches are not the caller's work
   c->qchunk = bestq;
+  c->qbps = bestb;
   if (c->log)
-    fprintf(stderr, "       queue chunk: %d voxels (%.2f / %.2f / %.2f ms for 128 / 256 / 512)\n",
-            bestq, c->qchunk_ms[0], c->qchunk_ms[1], c->qchunk_ms[2]);
+    fprintf(stderr, "       queue: chunk %d voxels, %s blocks per SM (%.2f / %.2f / %.2f ms for "
+            "128 / 256 / 512; %.2f / %.2f / %.2f ms with one block per SM)\n", bestq,
+            bestb ? "1" : "all", c->qchunk_ms[0], c->qchunk_ms[1], c->qchunk_ms[2],
+            c->qchunk_ms[3], c->qchunk_ms[4], c->qchunk_ms[5]);
   return 0;
 }
 
@@ -1106,6 +1115,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   a.queue = nullptr;
   a.cost = nullptr;
   a.qchunk = c->qchunk;
+  a.qbps = c->qbps;
   if (c->sched == CPFFT_SCHED_QUEUE && iter > 0 && c->n_crys_vox) {
     a.perm = c->vperm;
     a.queue = c->vq + 128;
@@ -1633,11 +1643,12 @@ int cpfft_tuning(int* tiles, double* ms) {
   return 0;
 }
 
-int cpfft_queue_chunk(int* voxels, double* ms) {
+int cpfft_queue_chunk(int* voxels, int* blocks_per_sm, double* ms) {
   TRY(need_ctx());
   if (voxels) *voxels = g_ctx->qtuned ? g_ctx->qchunk : 0;
+  if (blocks_per_sm) *blocks_per_sm = g_ctx->qbps;
   if (ms)
-    for (int k = 0; k < 3; k++) ms[k] = g_ctx->qchunk_ms[k];
+    for (int k = 0; k < 6; k++) ms[k] = g_ctx->qchunk_ms[k];
   return 0;
 }
 

@@ -125,6 +125,7 @@ struct StressArgs {
   unsigned int* queue;        // next queue slot (zeroed by launch_voxel_queue)
   unsigned char* cost;        // (N3) out: local iterations of this pass (null: not kept)
   int qchunk;                 // voxels a block takes from the queue at a time (multiple of 128)
+  int qbps;                   // persistent blocks per SM (0: as many as fit)
   int tangent_f32;            // 1: dP/dF (cep2A) in FP32 (the fast form; it steers Newton only)
   // logging of (features, converged increments) pairs from the plain solve
   float* log_X;               // [cap][20], null: no logging

@@ -1583,20 +1583,17 @@ cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm, cudaStream_t s) 
   }
   unsigned blocks = (unsigned)((a.N3 + 127) / 128);
   if (a.perm) {
-    // persistent: as many blocks as fit on the GPU at once
-    static int resident[2] = {0, 0};
-    int& r = resident[warm ? 1 : 0];
-    if (!r) {
-      int dev = 0, sms = 0, per = 0;
-      cudaError_t e;
-      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-      e = warm ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<true>, 128, mlp::FWD_SMEM)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<false>, 128, 0);
-      if (e != cudaSuccess) return e;
-      r = sms * (per > 0 ? per : 1);
-    }
-    blocks = (unsigned)std::min<long long>((long long)r, (long long)blocks);
+    // persistent: as many blocks as fit on the GPU at once, or a.qbps per SM
+    int dev = 0, sms = 0, per = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    e = warm ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<true>, 128, mlp::FWD_SMEM)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, stress_kernel<false>, 128, 0);
+    if (e != cudaSuccess) return e;
+    if (per < 1) per = 1;
+    if (a.qbps > 0 && a.qbps < per) per = a.qbps;
+    blocks = (unsigned)std::min<long long>((long long)sms * per, (long long)blocks);
   }
   if (warm) stress_kernel<true><<<blocks, 128, mlp::FWD_SMEM, s>>>(a);
   else stress_kernel<false><<<blocks, 128, 0, s>>>(a);

@@ -209,12 +209,14 @@ int cpfft_set_precond(int precond);
 #define CPFFT_SCHED_BLOCKS  0
 #define CPFFT_SCHED_QUEUE   1
 int cpfft_set_schedule(int schedule);
-/* The work-queue chunk the autotuner chose (extension): on a context's first implicit
+/* The work-queue shape the autotuner chose (extension): on a context's first implicit
  * CPFFT_SCHED_QUEUE pass the pass runs once per candidate -- 128, 256 or 512 voxels taken
- * from the queue by a block at a time -- timed with CUDA events, and the fastest is kept
- * (identical results).  *voxels = the chosen chunk (0 before that pass); ms (3, may be
- * NULL) = the measured pass times of the candidates. */
-int cpfft_queue_chunk(int* voxels, double* ms);
+ * from the queue by a block at a time, with as many persistent blocks per SM as fit or
+ * with one -- timed with CUDA events, and the fastest is kept (identical results).
+ * *voxels = the chosen chunk (0 before that pass); *blocks_per_sm = 0 (as many as fit) or
+ * 1; ms (6, may be NULL) = the pass times of the candidates, chunks 128 / 256 / 512 with
+ * all blocks, then with one block per SM. */
+int cpfft_queue_chunk(int* voxels, int* blocks_per_sm, double* ms);
 
 /* Tile shapes the autotuner chose for this grid when CPFFT_PREC_MIXED was first selected
  * (extension): columns per block of the transform passes along the middle axis (both

@@ -275,8 +275,9 @@ def test_precond_cg_tile_shapes(gpulib, N, tc):
 
 
 def test_queue_chunk_autotuned(gpulib):
-    """The voxel-queue chunk is chosen on the first implicit queue pass from timed runs of
-    that pass, and the results equal those of the one-block-per-128-voxels schedule."""
+    """The voxel-queue chunk and persistent blocks per SM are chosen on the first implicit
+    queue pass from timed runs of that pass, and the results equal those of the
+    one-block-per-128-voxels schedule."""
     N = 16
     r = rve.make_rve(N, 4, 29)
     Fn, Fn1 = random_F(N, 1e-3, 6)
@@ -291,8 +292,8 @@ def test_queue_chunk_autotuned(gpulib):
             P, K, _ = s.drive_eps_sig(1, 1, Fn, Fn1, want_K4=True)
             q = s.queue_chunk()
             if sched == gpulib.SCHED_QUEUE:
-                assert q["chunk"] in (128, 256, 512)
-                assert all(t > 0 for t in q["ms_128_256_512"])
+                assert q["chunk"] in (128, 256, 512) and q["blocks_per_sm"] in ("all", 1)
+                assert all(t > 0 for t in q["ms_128_256_512"] + q["ms_one_block_per_sm"])
             out.append((P, K))
         finally:
             s.close()
