@@ -53,6 +53,12 @@ BYTES_STRESS = 1264.0          # stress update: F, F1, state n, P, A, state n+1
 # grids): pass A reads r, p, K4f and writes p (432), two half-spectrum round trips (144),
 # pass E reads x, r, p and writes x, r (180)
 BYTES_CG32_FUSED = 756.0
+# FP64 flops of a stress pass per voxel (2 DFMA + DADD + DMUL of active lanes, ncu at 64^3):
+# explicit passes (iteration 0), and implicit passes as a base plus a cost per local Newton
+# iteration (predictor iterations included), fitted over one timed load step's passes
+STRESS_FLOPS = {"explicit": 3933.0, "implicit_base": 6433.0, "per_iteration": 3909.0,
+                "source": "profiles/stress_kernel_64.md (ncu FP64 instruction counts of 8 "
+                          "passes at 64^3, fitted to their local iterations)"}
 FUSED_GRIDS = (32, 64, 128, 256)
 
 
@@ -330,12 +336,20 @@ def roofline(run, N, peaks, peak_kind, fp64_peak):
                 "algorithmic_flops_per_launch": fft_flops_per_voxel(N) * N3,
                 "avg_launch_ms": per * 1e3}
     else:
+        # FP64-pipe bound: FP64 flops of the timed passes from the flop model (explicit
+        # passes, one per P_bar pass; implicit passes by their local iterations)
         per = tsk / su
-        ach = BYTES_STRESS * N3 / per / 1e9
-        roof = {"kernel": "stress update (mm10 + cep2A)", "bound": "hbm", "achieved": ach,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": ach / peaks["hbm_gbs"],
-                "peak_source": f"{peak_kind} hbm_gbs; the kernel is FP64-pipe bound",
-                "algorithmic_bytes_per_launch": BYTES_STRESS * N3, "avg_launch_ms": per * 1e3}
+        nexp = sum(s["nbc_iters"] for s in st)
+        iters = sum(s["local_iters"] + s["predict_iters"] for s in st)
+        flops = N3 * (STRESS_FLOPS["explicit"] * nexp + STRESS_FLOPS["implicit_base"] * (su - nexp)) \
+            + STRESS_FLOPS["per_iteration"] * iters
+        ach = flops / tsk / 1e12
+        roof = {"kernel": "stress update (mm10 local solves + tangent + cep2A)", "bound": "fp64",
+                "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                "peak_source": "measured DFMA rate on this GPU (cpfft_measure_fp64_peak)",
+                "algorithmic_flops_per_launch": flops / su, "avg_launch_ms": per * 1e3,
+                "flop_model": STRESS_FLOPS["source"],
+                "hbm_algorithmic_bytes_per_launch": BYTES_STRESS * N3}
     key = "cg32_fused" if roof["kernel"].startswith("FP32 CG iteration") else kern
     tv, tsrc = TRAFFIC.get(key, (None, "not captured"))
     roof["traffic"] = tv * N3 if tv is not None else None
