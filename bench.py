@@ -136,6 +136,8 @@ TRAFFIC = {
                        "passes at 128^3"),
     "green64": (1259.0, "profiles/traffic_plane_strain_128.md: ncu dram bytes of the 5 FP64 "
                         "passes at 128^3"),
+    "cg32_fused": (801.2, "profiles/cg_iteration_fused_128.md: ncu dram bytes of the 5 fused "
+                          "passes of one FP32 CG iteration at 128^3"),
     "stress": (21400.0, "profiles/stress_kernel_64.md: ncu dram bytes per voxel of an "
                         "implicit stress_kernel launch at 64^3 (register spills included)"),
 }
