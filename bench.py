@@ -220,6 +220,7 @@ def make_solver(cp, r, form, args):
         s.set_equilibrium_tol(args.tol_equil)
         if form != "fp64" and args.inexact > 0:
             s.set_inexact_newton(args.inexact)
+            s.set_tangent_tol(args.tangent_tol)
     return s
 
 
@@ -528,6 +529,7 @@ REF_COUNTS = (15, 4290)
 
 def config_dict(args, impl):
     fast = impl != "reference"
+    inexact = fast and args.mode != "fp64" and args.tol_equil > 0 and args.inexact > 0
     r_desc = ("cyclic uniaxial tension/compression +-2 % (2 cycles in 160 steps), 256^3 "
               "voxels, 2048 Voronoi grains (seed 4), FCC mm10 Voce"
               if args.workload == "config5" else
@@ -547,8 +549,9 @@ def config_dict(args, impl):
             "g_mapping": "centered (Nyquist-filtered)", "exact_j22": 1,
             "tolerances": {"local": 1e-10, "NR": args.tol_nr, "CG": 1e-10,
                            "equilibrium": args.tol_equil,
-                           "inexact_newton_eta_max": (args.inexact if fast and args.mode != "fp64"
-                                                      and args.tol_equil > 0 else 0.0)},
+                           "inexact_newton_eta_max": (args.inexact if inexact else 0.0),
+                           "tangent_homo": (max(args.tangent_tol, 1e-10) if inexact
+                                            else 1e-10)},
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
             "stress_schedule": args.schedule if fast else "blocks",
             "tangent": args.tangent if fast else "f64",
@@ -619,7 +622,7 @@ def gb300_arm(args):
                 "pbar_rel_per_step": rel, "pbar_rel_max": max(rel),
                 "p_rel_max_per_voxel": float((np.abs(Pf - P).max(axis=0) / scale).max()),
                 "p_field_step": args.warmup + n64,
-                "target": 1e-6,
+                "target_pbar_rel": 1e-6,
                 "steps": f"P_bar: load steps 1-{len(rel)} (warm-up and timed)"},
             "res_equil": {"fast": eq_fast, "fp64": eq_plain,
                           "max": max(eq_fast + eq_plain), "target": 1e-6},
@@ -682,6 +685,13 @@ def gb300_arm(args):
         "clocks": fast["clocks"],
         "cpu_baseline": cpu,
     }
+    if args.curve:
+        # the volume-averaged P of every load step (row-major 3x3), both forms
+        with open(args.curve, "w") as f:
+            json.dump({"workload": line["config"]["workload"],
+                       "fast": [list(map(float, p)) for p in fast["pbars"]],
+                       "fp64": ([list(map(float, p)) for p in plain["pbars"]]
+                                if plain is not None else None)}, f)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -777,6 +787,10 @@ def main():
     # fast forms: inexact Newton (each Newton system solved as far as the equilibrium
     # residual needs, at most this relative tolerance; 0 = every solve to the CG tolerance)
     ap.add_argument("--inexact", type=float, default=1e-2)
+    ap.add_argument("--tangent-tol", type=float, default=1e-3,
+                    help="relative tolerance of tangent_homo's solves in the fast form")
+    ap.add_argument("--curve", default=None,
+                    help="write P_bar of every load step of both forms to this JSON file")
     ap.add_argument("--fp64-steps", type=int, default=5,
                     help="timed steps of the plain FP64 form (after the same warm-up), at "
                          "most --steps")

@@ -123,6 +123,7 @@ SIGNATURES = {
     "cpfft_set_precond": (_I, [_I]),
     "cpfft_set_equilibrium_tol": (_I, [_D]),
     "cpfft_set_inexact_newton": (_I, [_D]),
+    "cpfft_set_tangent_tol": (_I, [_D]),
     "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
@@ -330,6 +331,10 @@ class Solver:
         """Solve each Newton system of nr3_step only as far as the equilibrium residual
         needs (Eisenstat-Walker forcing, at most eta_max; needs set_equilibrium_tol)."""
         _check(load_library().cpfft_set_inexact_newton(float(eta_max)), "cpfft_set_inexact_newton")
+
+    def set_tangent_tol(self, tol):
+        """Relative tolerance of tangent_homo's solves under inexact Newton (default 1e-3)."""
+        _check(load_library().cpfft_set_tangent_tol(float(tol)), "cpfft_set_tangent_tol")
 
     def set_equilibrium_tol(self, tol):
         """Also require ||G(P)|| / (sqrt(N3) ||P_bar||) <= tol to end a Newton loop of

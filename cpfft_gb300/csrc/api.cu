@@ -361,6 +361,8 @@ struct Ctx {
   // inexact Newton (cpfft_set_inexact_newton; 0 = every Krylov solve to tolPCG): the
   // largest relative tolerance of a Newton system's solve
   double eta_max = 0.0;
+  // relative tolerance of tangent_homo's solves under inexact Newton (cpfft_set_tangent_tol)
+  double th_tol = 1.0e-3;
   bool cg_rel_only = false;  // the current solve stops on ||r|| <= tol ||b|| alone
   // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
   // starts dropped, sub-stepped solves (cpfft_pass_counts)
@@ -1617,6 +1619,16 @@ int cpfft_set_inexact_newton(double eta_max) {
   return 0;
 }
 
+int cpfft_set_tangent_tol(double tol) {
+  TRY(need_ctx());
+  if (!(tol > 0.0 && tol < 1.0)) {
+    cpfft_set_error("cpfft_set_tangent_tol: tolerance must lie in (0, 1)");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  g_ctx->th_tol = tol;
+  return 0;
+}
+
 int cpfft_set_equilibrium_tol(double tol) {
   TRY(need_ctx());
   if (!(tol >= 0.0) || !std::isfinite(tol)) {
@@ -2052,7 +2064,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     a = clk::now();
     int th;
     // the homogenised tangent only steers the P_bar update (its loop tests P_bar itself)
-    TRY(tangent_homo(c, inexact ? std::max(tolPCG, 1e-6) : tolPCG, c->C_homo, &th));
+    TRY(tangent_homo(c, inexact ? std::max(tolPCG, c->th_tol) : tolPCG, c->C_homo, &th));
     tp += sec(a);
     for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
     TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));
