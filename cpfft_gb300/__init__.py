@@ -15,6 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
 HIST_WORDS = 31
+HIST_WORDS_MRR = 55  # grids of Ma-Roters-Raabe crystals (h_type 7)
 NOT_A_CRYSTAL = 0  # slip_type of a material defined by Solver.set_mises
 
 G_REF_SHIFT, G_CENTERED = 0, 1
@@ -62,6 +63,8 @@ class Crystal(ctypes.Structure):
         ("eps_dot_0_v", ctypes.c_double),
         ("burgers", ctypes.c_double), ("boltzman", ctypes.c_double),
         ("mu_0", ctypes.c_double), ("D_0", ctypes.c_double), ("T_0", ctypes.c_double),
+        ("u1", ctypes.c_double), ("u2", ctypes.c_double), ("u3", ctypes.c_double),
+        ("u4", ctypes.c_double), ("u5", ctypes.c_double), ("u6", ctypes.c_double),
     ]
 
 
@@ -147,6 +150,7 @@ SIGNATURES = {
     "cpfft_nr3_step": (_I, [_I, _DP, _IP, _D, _D, _I, _DP, _P(Stats)]),
     "cpfft_nr3_begin": (_I, [_D]),
     "cpfft_sync_to_host": (_I, [_DP, _DP, _DP]),
+    "cpfft_hist_words": (_I, []),
     "cpfft_commit_step": (_I, []),
     "cpfft_set_F": (_I, [_DP, _DP]),
     "cpfft_finalize": (None, []),
@@ -426,7 +430,8 @@ class Solver:
     def fields(self, history=False):
         F = np.zeros((9, self.N3))
         P = np.zeros((9, self.N3))
-        H = np.zeros((HIST_WORDS, self.N3)) if history else None
+        H = np.zeros((_check(load_library().cpfft_hist_words(), "cpfft_hist_words"), self.N3)) \
+            if history else None
         _check(load_library().cpfft_sync_to_host(_dp(F), _dp(P), _dp(H)), "sync_to_host")
         return (F, P, H) if history else (F, P)
 

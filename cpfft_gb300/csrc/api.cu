@@ -238,8 +238,28 @@ void orientation_record(const double C0[36], const double bb[48][3], const doubl
     }
 }
 
+// Ma-Roters-Raabe interaction matrices of the FCC systems (mm10_mrr_GHfcc, src/mm10_e.f:
+// 55-340, formed here from the geometry): Gm(a,q) = |n_a . t_q| (forest projection),
+// Hm(a,q) = |n_a x t_q| (parallel), t_q = n_q x b_q the edge dislocation line of system q
+void mrr_interaction(double Gm[144], double Hm[144]) {
+  double b[12][3], n[12][3];
+  fcc_geometry(b, n);
+  for (int a = 0; a < 12; a++)
+    for (int q = 0; q < 12; q++) {
+      double t[3] = {n[q][1] * b[q][2] - n[q][2] * b[q][1], n[q][2] * b[q][0] - n[q][0] * b[q][2],
+                     n[q][0] * b[q][1] - n[q][1] * b[q][0]};
+      const double tl = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+      for (int k = 0; k < 3; k++) t[k] /= tl;
+      const double x[3] = {n[a][1] * t[2] - n[a][2] * t[1], n[a][2] * t[0] - n[a][0] * t[2],
+                           n[a][0] * t[1] - n[a][1] * t[0]};
+      Gm[12 * a + q] = std::fabs(n[a][0] * t[0] + n[a][1] * t[1] + n[a][2] * t[2]);
+      Hm[12 * a + q] = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    }
+}
+
 CrysRec crystal_record(const cpfft_crystal& p) {
   CrysRec c;
+  std::memset(&c, 0, sizeof(c));
   c.rate_n = p.harden_n;
   c.tau_y = p.tau_y;
   c.tau_v = p.tau_v;
@@ -267,6 +287,13 @@ CrysRec crystal_record(const cpfft_crystal& p) {
   c.mu_0 = p.mu_0;
   c.D_0 = p.D_0;
   c.T_0 = p.T_0;
+  c.u1 = p.u1;
+  c.u2 = p.u2;
+  c.u3 = p.u3;
+  c.u4 = p.u4;
+  c.u5 = p.u5;
+  c.u6 = p.u6;
+  if (p.h_type == 7) mrr_interaction(c.Gm, c.Hm);
   c.h_type = p.h_type;
   c.miter = p.miter;
   c.alter_mode = p.alter_mode;
@@ -284,7 +311,8 @@ struct Ctx {
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
   int nslip = 12;  // slip systems of the grid's crystals (12 fcc, 48 bcc48)
-  int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts)
+  int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts, 7 mrr)
+  int hist_words = H_WORDS;  // H_WORDS_MRR on Ma-Roters-Raabe grids
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
   // voxel work queue of the implicit stress passes (cpfft_set_schedule)
   int sched = CPFFT_SCHED_BLOCKS;
@@ -1014,6 +1042,13 @@ int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
 // CUDA events, and the fastest is kept.  The runs give identical results (no local solve
 // of this pass starts from an earlier pass's state); their statistics and logged pairs
 // are not kept.
+// the stress kernel compiled for the grid's slip systems and hardening law
+cudaError_t launch_crystals(Ctx* c, const StressArgs& a, bool warm) {
+  if (c->h_type == 2) return launch_stress_mts(a, warm, c->st);
+  if (c->h_type == 7) return launch_stress_mrr(a, false, c->st);
+  return c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st);
+}
+
 int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
   c->qtuned = true;
   a.log_X = nullptr;
@@ -1030,8 +1065,7 @@ int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
     a.qbps = bps;
     CK(launch_voxel_queue(c->vcost, c->N3, c->vq, c->vperm, c->vq + 128, c->st));
     CK(cudaEventRecord(e0, c->st));
-    CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
-                      : c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+    CK(launch_crystals(c, a, warm));
     CK(cudaEventRecord(e1, c->st));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -1127,9 +1161,7 @@ int stress(Ctx* c, int step, int iter, long long* local_iters, int* fails,
   }
   CK(cudaMemsetAsync(c->stats, 0, 5 * sizeof(unsigned long long), c->st));
   kt_start(c, KT_STRESS);
-  if (c->n_crys_vox)
-    CK(c->h_type == 2 ? launch_stress_mts(a, warm, c->st)
-                      : c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st));
+  if (c->n_crys_vox) CK(launch_crystals(c, a, warm));
   if (c->n_mises_vox) CK(launch_mises(a, c->st));
   TRY(kt_stop(c));
   c->pass_step = step;
@@ -1335,10 +1367,16 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
                         p.boltzman > 0 && p.G_0_y > 0 && p.G_0_v > 0 && p.p_y > 0 &&
                         p.q_y > 0 && p.p_v > 0 && p.q_v > 0 && p.gamma_bar > 0 &&
                         p.eps_dot_0_v > 0;
-    if (!ns || !(voce_ok || mts_ok) || !(p.harden_n > 0) ||
+    // MRR: positive constants (mm10_h_mrr stops on a non-positive temperature; the
+    // densities enter square roots and the rates divide by c1 c2 c3)
+    const bool mrr_ok = p.h_type == 7 && ns == 12 && p.mu_0 > 0 && p.burgers > 0 &&
+                        p.boltzman > 0 && p.G_0_y > 0 && p.G_0_v > 0 && p.p_v > 0 &&
+                        p.q_v > 0 && p.u1 > 0 && p.u2 > 0 && p.u3 > 0 && p.theta_0 >= 0;
+    const bool n_ok = p.h_type == 7 || p.harden_n > 0;
+    if (!ns || !(voce_ok || mts_ok || mrr_ok) || !n_ok ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
       cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip with voce hardening, "
-                      "fcc with mts hardening, valid elasticity)", k + 1);
+                      "fcc with mts or roters hardening, valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
     if ((nslip && ns != nslip) || (h_type && p.h_type != h_type)) {
@@ -1391,6 +1429,8 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   Ctx* c = new Ctx;
   c->nslip = nslip;
   c->h_type = h_type;
+  c->hist_words = h_type == 7 ? H_WORDS_MRR : H_WORDS;
+  const int HW = c->hist_words;
   c->mat = mat;
   c->mat_kind.assign(ncrystals, 0);
   for (int k = 0; k < ncrystals; k++)
@@ -1436,8 +1476,8 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
       (rc = dalloc(c->K4, 81 * N3 * sizeof(double))) || (rc = dalloc(c->b, f9)) ||
       (rc = dalloc(c->dFm, f9)) || (rc = dalloc(c->r, f9)) || (rc = dalloc(c->p, f9)) ||
       (rc = dalloc(c->Ap, f9)) || (rc = dalloc(c->w, f9)) || (rc = dalloc(c->io, f9)) ||
-      (rc = dalloc(c->hist[0], H_WORDS * N3 * sizeof(double))) ||
-      (rc = dalloc(c->hist[1], H_WORDS * N3 * sizeof(double))) ||
+      (rc = dalloc(c->hist[0], HW * N3 * sizeof(double))) ||
+      (rc = dalloc(c->hist[1], HW * N3 * sizeof(double))) ||
       (rc = dalloc(c->ori, N3 * sizeof(int))) || (rc = dalloc(c->crys, N3 * sizeof(int))) ||
       (rc = dalloc(c->oris, oris.size() * sizeof(OriRec))) ||
       (rc = dalloc(c->cryss, ncrystals * sizeof(CrysRec))) ||
@@ -1460,13 +1500,16 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   for (int d : {0, 4, 8})
     for (long long v = 0; v < N3; v++) F[d * N3 + v] = 1.0;
   // history at n = the state of mm10_init_cc_hist0 (sigma 0, tau_y + 1e-5, Rp = I)
-  std::vector<double> h(H_WORDS * N3, 0.0);
+  std::vector<double> h(HW * N3, 0.0);
   for (long long v = 0; v < N3; v++) {
     if (props[mat[v]].slip_type == CPFFT_NOT_A_CRYSTAL) continue;
     if (props[crys[v]].h_type == 2) {  // mm10_init_mts: flags, set by the first update
       h[H_TT * N3 + v] = -1.0;
       h[H_U * N3 + v] = -1.0;
       h[(H_U + 1) * N3 + v] = -1.0;
+    } else if (props[crys[v]].h_type == 7) {  // mm10_init_mrr (src/mm10_a.f:2205-2223)
+      const double r0 = props[crys[v]].theta_0 == 0.0 ? 1.0e8 : props[crys[v]].theta_0;
+      for (int i = 0; i < 12; i++) h[(H_RHO + i) * N3 + v] = r0;
     } else {
       h[H_TT * N3 + v] = props[crys[v]].tau_y + 1.0e-5;
     }
@@ -1533,7 +1576,7 @@ int cpfft_set_mises(int material, const cpfft_mises* props) {
     nu += k == 2;
   }
   // the voxels' state at n and n+1: mm01_set_history's (src/mm01.f:240-310)
-  std::vector<double> h(H_WORDS * N3);
+  std::vector<double> h((size_t)c->hist_words * N3);
   cudaError_t e;
   for (int t = 0; t < 2; t++) {
     if ((e = cudaMemcpy(h.data(), c->hist[t], h.size() * sizeof(double), cudaMemcpyDeviceToHost))) {
@@ -1542,7 +1585,7 @@ int cpfft_set_mises(int material, const cpfft_mises* props) {
     }
     for (long long v = 0; v < N3; v++) {
       if (c->mat[v] != m) continue;
-      for (int w = 0; w < H_WORDS; w++) h[w * N3 + v] = 0.0;
+      for (int w = 0; w < c->hist_words; w++) h[w * N3 + v] = 0.0;
       h[M1_K * N3 + v] = p.yld_pt / 1.73205080756888;
       h[M1_STATE * N3 + v] = 3.0;
       h[M1_HP * N3 + v] = c->h_mises[m].h;
@@ -2116,9 +2159,14 @@ int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history) {
   if (Fn1) CK(cudaMemcpyAsync(Fn1, c->Fn1, f9, cudaMemcpyDeviceToHost, c->st));
   if (Pn1) CK(cudaMemcpyAsync(Pn1, c->P, f9, cudaMemcpyDeviceToHost, c->st));
   if (history)
-    CK(cudaMemcpyAsync(history, c->hist[c->hn], H_WORDS * c->N3 * sizeof(double),
+    CK(cudaMemcpyAsync(history, c->hist[c->hn], c->hist_words * c->N3 * sizeof(double),
                        cudaMemcpyDeviceToHost, c->st));
   return sync(c);
+}
+
+int cpfft_hist_words(void) {
+  TRY(need_ctx());
+  return g_ctx->hist_words;
 }
 
 int cpfft_commit_step(void) {

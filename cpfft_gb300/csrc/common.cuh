@@ -44,6 +44,10 @@ struct CrysRec {
   // MTS (h_type 2)
   double tau_a, tau_hat_y, G_0_y, p_y, q_y, tau_hat_v, G_0_v, p_v, q_v, eps_dot_0_v;
   double burgers, boltzman, mu_0, D_0, T_0;
+  // Ma-Roters-Raabe (h_type 7): c1..c6 and the interaction matrices (row-major 12 x 12),
+  // rho_F = Gm rho, rho_P = Hm rho
+  double u1, u2, u3, u4, u5, u6;
+  double Gm[144], Hm[144];
   int h_type;
   int miter, alter_mode, exact_j22;
   int n_int;       // rate_n - 1 when rate_n is integer-valued in [2, 64], else -1
@@ -66,7 +70,11 @@ enum {
   H_TTR = 22,     // 1  tau_tilde rate
   H_EPS = 23,     // 6  unrotated strain (sum of the step increments, rstgp1_update_strains)
   H_U = 29,       // 2  MTS: tau_y and mu of the step (mm10's u(1:2)); -1 = not yet set
-  H_WORDS = 31
+  H_WORDS = 31,
+  // grids of Ma-Roters-Raabe crystals (CPFFT_HIST_WORDS_MRR): the twelve dislocation
+  // densities, then their rates; H_TT and H_TTR are zero there
+  H_RHO = 31,     // 12 + 12
+  H_WORDS_MRR = 55
 };
 
 // The same words for an mm01 voxel: H_SIG and H_EPS as above, and in words 6..19 the
@@ -141,6 +149,8 @@ cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
 // MTS-hardened FCC crystals (stress_mts.cu)
 cudaError_t launch_stress_mts(const StressArgs& a, bool warm, cudaStream_t s);
+// Ma-Roters-Raabe FCC crystals (stress_mrr.cu; warm is ignored: no learned guess)
+cudaError_t launch_stress_mrr(const StressArgs& a, bool warm, cudaStream_t s);
 // the mm01 voxels (a.mises[v] >= 0) of the grid; the crystal launches skip them
 cudaError_t launch_mises(const StressArgs& a, cudaStream_t s);
 // Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost

@@ -1,0 +1,566 @@
+// mrr.cuh -- Ma-Roters-Raabe hardening (h_type 7) for the stress kernel: twelve
+// dislocation densities, one per FCC slip system, as the slip resistance variables.
+// Included by stress.cu when it is compiled with CPFFT_LAW 7 (stress_mrr.cu).
+//
+// The slip law, hardening law and their derivatives follow mm10_slipinc_mrr ..
+// mm10_dgdd_mrr (src/mm10_b.f:2343-3325); the local solve is mm10_solve
+// (src/mm10_a.f:2860-3295) with 6 + 12 unknowns, the tangent mm10_tangent (:658-815) with
+// ed = dgammadd = 0.  exact_j22 = 0 forms the Jacobian with the reference's formulas
+// (sqrt(rho_F) in d h / d sigma and d h / d rho where mm10_h_mrr has sqrt(rho_P); no sign
+// of tau on estress's c8 term; the fract > 1 branch of dgdt / dgdh drops terms), which
+// slow the local Newton to linear convergence; exact_j22 = 1 differentiates the residual.
+// One thread per voxel: the 18 x 18 Jacobian and its LU live in local memory.
+
+constexpr int NH = 12;  // dislocation densities
+constexpr double MRR_PI = 3.141592653589793;
+constexpr double MRR_NU = 0.3;  // Poisson's ratio of the dipole distance (mm10_h_mrr)
+
+// the quantities of system a at (sigma, rho) every routine forms: resolved shear, forest
+// and parallel densities, rate prefactor, passing and cutting stresses, and the slip
+// increment (mm10_slipinc_mrr, src/mm10_b.f:2477-2546)
+struct MrrSys {
+  double rs, rhoF, rhoP, g0, tpass, tcut, fract, slip;
+};
+
+__device__ void mrr_sys(const Crystal& s, const double* st, const double* tt, int a, MrrSys& y) {
+  const CrysRec& c = *s.cr;
+  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  y.rs = st[0] * s.ms[a][0] + st[1] * s.ms[a][1] + st[2] * s.ms[a][2] + st[3] * s.ms[a][3] +
+         st[4] * s.ms[a][4] + st[5] * s.ms[a][5];
+  double f = 0.0, p = 0.0;
+  for (int q = 0; q < NH; q++) {
+    f += __ldg(c.Gm + NH * a + q) * tt[q];
+    p += __ldg(c.Hm + NH * a + q) * tt[q];
+  }
+  y.rhoF = f;
+  y.rhoP = p;
+  const double sp = sqrt(p);
+  y.g0 = c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) * sp;
+  y.tpass = c.u1 * G * b * sp;
+  y.tcut = c.G_0_v / (c.u2 * c.u3 * b * b) * sqrt(f);
+  y.fract = (fabs(y.rs) - y.tpass) / y.tcut;
+  const double Qk = c.G_0_v / k / th;
+  if (y.fract > 1.0) {  // linear extrapolation past fract = 1
+    const double m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
+    y.slip = s.tinc * (m * y.fract + y.g0);
+  } else if (fabs(y.rs) > 0.0) {
+    y.slip = s.tinc * y.g0 * sgn1(y.rs) * exp(-Qk * pow(1.0 - pow(y.fract, c.p_v), c.q_v));
+  } else {
+    y.slip = 0.0;
+  }
+}
+
+// d slip / d rs (mm10_dgdt_mrr, src/mm10_b.f:3111-3198)
+__device__ double mrr_dgdt(const Crystal& s, const MrrSys& y) {
+  const CrysRec& c = *s.cr;
+  const double Qk = c.G_0_v / c.boltzman / s.temp;
+  const double dfract = sgn1(y.rs) / y.tcut;
+  if (y.fract > 1.0) {
+    const double m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
+    return c.exact_j22 ? s.tinc * m * dfract : s.tinc * m;
+  }
+  if (fabs(y.rs) > 0.0) {
+    const double base = 1.0 - pow(y.fract, c.p_v);
+    const double slipexp = exp(-Qk * pow(base, c.q_v)) * sgn1(y.rs);
+    return s.tinc * (-y.g0 * slipexp * Qk * c.q_v * pow(base, c.q_v - 1.0) * (-1.0) * c.p_v *
+                     pow(y.fract, c.p_v - 1.0) * dfract);
+  }
+  return 0.0;
+}
+
+// d slip_a / d rho_q (mm10_dgdh_mrr, src/mm10_b.f:3201-3306)
+__device__ double mrr_dgdh(const Crystal& s, const MrrSys& y, int a, int q) {
+  const CrysRec& c = *s.cr;
+  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double Qk = c.G_0_v / k / th;
+  const double drhoF = __ldg(c.Gm + NH * a + q), drhoP = __ldg(c.Hm + NH * a + q);
+  const double dg0 = 0.5 * c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) / sqrt(y.rhoP) * drhoP;
+  const double dtpass = 0.5 * c.u1 * G * b / sqrt(y.rhoP) * drhoP;
+  const double dtcut = 0.5 * c.G_0_v / (c.u2 * c.u3 * b * b) / sqrt(y.rhoF) * drhoF;
+  const double dfract = ((-dtpass) * y.tcut - (fabs(y.rs) - y.tpass) * dtcut) / (y.tcut * y.tcut);
+  if (y.fract > 1.0) {
+    const double K = (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs);
+    const double dm = K * (dg0 / y.tcut - y.g0 * dtcut / (y.tcut * y.tcut));
+    if (!c.exact_j22) return s.tinc * dm;
+    const double m = y.g0 * K / y.tcut;
+    return s.tinc * (dm * y.fract + m * dfract + dg0);
+  }
+  if (fabs(y.rs) > 0.0) {
+    const double base = 1.0 - pow(y.fract, c.p_v);
+    const double slipexp = exp(-Qk * pow(base, c.q_v));
+    return s.tinc * (dg0 * slipexp * sgn1(y.rs) +
+                     y.g0 * sgn1(y.rs) * slipexp * (-1.0) * Qk * c.q_v * pow(base, c.q_v - 1.0) *
+                         (-1.0) * c.p_v * pow(y.fract, c.p_v - 1.0) * dfract);
+  }
+  return 0.0;
+}
+
+// R1 (mm10_formR1, src/mm10_b.f:1061-1101): dbarp and wp of the MRR slips
+__device__ void mrr_formR1(const Crystal& s, const double* st, const double* tt, double* R1) {
+  double dbar[6] = {0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0};
+  for (int i = 0; i < NS; i++) {
+    MrrSys y;
+    mrr_sys(s, st, tt, i, y);
+    for (int a = 0; a < 6; a++) dbar[a] += y.slip * s.ms[i][a];
+    for (int a = 0; a < 3; a++) w[a] += y.slip * s.qc[i][a];
+  }
+  double sw[6], wv1[6];
+  symsw(st, w, sw);
+  for (int a = 0; a < 6; a++) wv1[a] = s.D[a] - dbar[a];
+  for (int a = 0; a < 6; a++) {
+    double t = 0.0;
+    for (int j = 0; j < 6; j++) t += Cv(s.C, a, j) * wv1[j];
+    R1[a] = st[a] - s.nsig[a] - t + 2.0 * sw[a];
+  }
+}
+
+// R = (R1, tt - h) (mm10_formR, mm10_h_mrr, src/mm10_b.f:1029-1047, 2549-2646); the
+// densities' rates (h - rho_n) / tinc
+__device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x, double* R,
+                          double* rate) {
+  const CrysRec& c = *s.cr;
+  const double* st = x;
+  const double* tt = x + 6;
+  mrr_formR1(s, st, tt, R);
+  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double cdip = sqrt(3.0) * G * b / (16.0 * MRR_PI * (1.0 - MRR_NU));
+  const double cM = (2.0 * k / (c.u1 * c.u2 * c.u3 * G * b * b * b)) * th;
+  const double E = c.tau_hat_y * exp(-c.tau_a / k / th) / (k * th);
+  for (int a = 0; a < NH; a++) {
+    MrrSys y;
+    mrr_sys(s, st, tt, a, y);
+    const double rho = tt[a], ars = fabs(y.rs);
+    const double ddip = cdip / ars;
+    const double rhoM = cM * sqrt(y.rhoF * y.rhoP);
+    const double gd = fabs(y.slip / s.tinc);
+    const double tem1 = c.u4 / b * sqrt(y.rhoP) * gd;
+    const double tem2 = c.u6 * ddip / b * rhoM * gd;
+    const double tem3 = c.u5 * rho * gd;
+    const double tem4 = c.tau_hat_y * exp(-c.tau_a / k / th) * ars / (k * th) * rho * rho *
+                        pow(gd, c.tau_hat_v);
+    (void)E;
+    const double h = nrho[a] + s.tinc * (tem1 + tem2 - tem3 - tem4);
+    R[6 + a] = tt[a] - h;
+    rate[a] = (h - nrho[a]) / s.tinc;
+  }
+}
+
+// J11 (mm10_formJ11, src/mm10_b.f:177-257) with mm10_dgdt_mrr, ld = row stride of J
+template <int ld>
+__device__ void mrr_formJ11(const Crystal& s, const double* st, const double* tt, double* J) {
+  for (int a = 0; a < 6; a++)
+    for (int cc = 0; cc < 6; cc++) J[ld * a + cc] = 0.0;
+  double w[3] = {0, 0, 0};
+  for (int i = 0; i < NS; i++) {
+    MrrSys y;
+    mrr_sys(s, st, tt, i, y);
+    const double dg = mrr_dgdt(s, y);
+    double sq[6];
+    symsw(st, s.qc[i], sq);
+    for (int a = 0; a < 6; a++) {
+      const double wv = s.Cms[i][a] + 2.0 * sq[a];
+      for (int cc = 0; cc < 6; cc++) J[ld * a + cc] += wv * (dg * s.ms[i][cc]);
+    }
+    for (int a = 0; a < 3; a++) w[a] += y.slip * s.qc[i][a];
+  }
+  // mm10_iw (src/mm10_b.f:1590-1634) and the identity
+  J[ld * 0 + 3] += 2.0 * w[2];  J[ld * 0 + 5] += -2.0 * w[1];
+  J[ld * 1 + 3] += 2.0 * w[2];  J[ld * 1 + 4] += -2.0 * w[0];
+  J[ld * 2 + 4] += 2.0 * w[0];  J[ld * 2 + 5] += 2.0 * w[1];
+  J[ld * 3 + 0] += w[2];  J[ld * 3 + 1] += -w[2]; J[ld * 3 + 4] += -w[1]; J[ld * 3 + 5] += w[0];
+  J[ld * 4 + 1] += w[0];  J[ld * 4 + 2] += -w[0]; J[ld * 4 + 3] += w[1];  J[ld * 4 + 5] += w[2];
+  J[ld * 5 + 0] += w[1];  J[ld * 5 + 2] += -w[1]; J[ld * 5 + 3] += w[0];  J[ld * 5 + 4] += -w[2];
+  for (int a = 0; a < 6; a++) J[ld * a + a] += 1.0;
+}
+
+// the 18 x 18 Jacobian (mm10_formJ, src/mm10_b.f:901-954), row-major: J12 (mm10_formJ12
+// with mm10_dgdh_mrr), J21 = -estress (mm10_estress_mrr, :2859-2963), J22 = ehard
+// (mm10_ehard_mrr, :2966-3092)
+__device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
+  constexpr int L = 6 + NH;
+  const CrysRec& c = *s.cr;
+  const double* st = x;
+  const double* tt = x + 6;
+  mrr_formJ11<L>(s, st, tt, J);
+  for (int a = 0; a < 6; a++)
+    for (int q = 0; q < NH; q++) J[L * a + 6 + q] = 0.0;
+  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double dt = s.tinc;
+  const double cdip = sqrt(3.0) * G * b / (16.0 * MRR_PI * (1.0 - MRR_NU));
+  const double cM = 2.0 * k / (c.u1 * c.u2 * c.u3 * G * b * b * b) * th;
+  const double E = c.tau_hat_y * exp(-c.tau_a / k / th) / (k * th);
+  const double c8 = c.tau_hat_v;
+  for (int a = 0; a < NH; a++) {
+    MrrSys y;
+    mrr_sys(s, st, tt, a, y);
+    // J12 column block of system a's slip
+    {
+      double sq[6];
+      symsw(st, s.qc[a], sq);
+      for (int q = 0; q < NH; q++) {
+        const double d = mrr_dgdh(s, y, a, q);
+        for (int r = 0; r < 6; r++) J[L * r + 6 + q] += (s.Cms[a][r] + 2.0 * sq[r]) * d;
+      }
+    }
+    const double rho = tt[a], sg = sgn1(y.rs), ars = fabs(y.rs);
+    const double ddip = cdip / ars;
+    const double dddip = -cdip / (ars * ars) * sg;
+    const double rhoM = cM * sqrt(y.rhoF * y.rhoP);
+    const double gd = fabs(y.slip / dt);
+    const double dsl = mrr_dgdt(s, y) / dt;
+    double et;
+    if (!c.exact_j22) {
+      const double bad = gd == 0.0 ? 0.0 : c8 * ars * pow(gd, c8 - 1.0) * dsl;
+      et = dt * (c.u4 / b * sqrt(y.rhoF) * sg * dsl + c.u6 / b * rhoM * (ddip * sg * dsl + dddip * gd) -
+                 c.u5 * rho * sg * dsl - E * rho * rho * (bad + sg * pow(gd, c8)));
+    } else {
+      const double dgd = sgn1(y.slip) * dsl;
+      const double bad = gd == 0.0 ? 0.0 : c8 * ars * pow(gd, c8 - 1.0) * dgd;
+      et = dt * (c.u4 / b * sqrt(y.rhoP) * dgd + c.u6 / b * rhoM * (ddip * dgd + dddip * gd) -
+                 c.u5 * rho * dgd - E * rho * rho * (bad + sg * pow(gd, c8)));
+    }
+    for (int r = 0; r < 6; r++) J[L * (6 + a) + r] = -et * s.ms[a][r];
+    const double sqF = sqrt(y.rhoF), sqP = sqrt(y.rhoP), sqFP = sqrt(y.rhoF * y.rhoP);
+    for (int q = 0; q < NH; q++) {
+      const double drhoF = __ldg(c.Gm + NH * a + q), drhoP = __ldg(c.Hm + NH * a + q);
+      const double drhoM = 0.5 * cM / sqFP * (drhoF * y.rhoP + y.rhoF * drhoP);
+      const double d = a == q ? 1.0 : 0.0;
+      const double dsh = mrr_dgdh(s, y, a, q) / dt;
+      double e;
+      if (!c.exact_j22) {
+        const double bad = gd == 0.0 ? 0.0 : c8 * pow(gd, c8 - 1.0) * dsh;
+        e = d - dt * (c.u4 / b * (0.5 * drhoF / sqF * gd * sg + sqF * dsh) +
+                      c.u6 / b * (rhoM * ddip * dsh + drhoM * ddip * gd * sg) -
+                      c.u5 * (rho * dsh + d * gd * sg) -
+                      E * ars * (rho * rho * bad + 2.0 * rho * sg * d * pow(gd, c8))) * sg;
+      } else {
+        const double dgd = sgn1(y.slip) * dsh;
+        const double bad = gd == 0.0 ? 0.0 : c8 * pow(gd, c8 - 1.0) * dgd;
+        e = d - dt * (c.u4 / b * (0.5 * drhoP / sqP * gd + sqP * dgd) +
+                      c.u6 / b * ddip * (rhoM * dgd + drhoM * gd) - c.u5 * (rho * dgd + d * gd) -
+                      E * ars * (rho * rho * bad + 2.0 * rho * d * pow(gd, c8)));
+      }
+      J[L * (6 + a) + 6 + q] = e;
+    }
+  }
+}
+
+// mm10_solve (src/mm10_a.f:2860-3295) for 6 + 12 unknowns: the predictor's Newton on R1
+// with the densities extrapolated along the previous step's rates, then the coupled
+// Newton; Armijo line search c = 1e-4, halving, at most 11 trials.  Jl keeps the last
+// Jacobian (mm10_tangent's).
+__device__ bool mrr_solve(Crystal& cu, const double* nrho, const double* nrate, double dtinc,
+                          double* stress, double* tt, double* Jl, bool& haveJ, int& iters,
+                          int& piters, double* rate) {
+  constexpr int L = 6 + NH;
+  const CrysRec& c = *cu.cr;
+  const double cls = 1.0e-4;
+  double x[L];
+  for (int i = 0; i < 6; i++) x[i] = stress[i];
+  for (int i = 0; i < NH; i++) x[6 + i] = tt[i];
+  double inR1;
+  {  // ---- predict (:2975-3156)
+    double d1[6], d2[6];
+    for (int i = 0; i < 6; i++) { d1[i] = cu.D[i]; d2[i] = cu.nD[i]; }
+    for (int k = 0; k < 2; k++) {
+      double* d = k ? d2 : d1;
+      const double dtr = (d[0] + d[1] + d[2]) / 3.0;
+      d[0] -= dtr; d[1] -= dtr; d[2] -= dtr;
+      const double t1 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      const double t2 = d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
+      if (t1 + t2 == 0.0) {
+        for (int i = 0; i < 6; i++) d[i] = 0.0;
+      } else {
+        const double nn = sqrt(t1 + t2);
+        for (int i = 0; i < 6; i++) d[i] = d[i] / nn;
+      }
+    }
+    const double cos_ang = fmax(d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2] +
+                                    (d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5]), 0.0);
+    double x1[6], x2[NH], R1[6];
+    for (int i = 0; i < 6; i++) x1[i] = x[i];
+    for (int i = 0; i < NH; i++) x2[i] = x[6 + i] + cos_ang * nrate[i] * dtinc;
+    mrr_formR1(cu, x1, x2, R1);
+    double dot = 0;
+    for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
+    double nR1 = sqrt(dot);
+    inR1 = nR1;
+    int it = 0;
+    while (nR1 > c.atol1 && nR1 / inR1 > c.rtol1) {
+      double J[36], mJ[36], dx[6];
+      mrr_formJ11<6>(cu, x1, x2, J);
+      for (int a = 0; a < 36; a++) mJ[a] = -J[a];
+      for (int a = 0; a < 6; a++) dx[a] = R1[a];
+      lu_solve1<6>(mJ, dx);
+      double ls1 = 0.5 * dot, ls2 = 0.0;
+      for (int a = 0; a < 6; a++) {
+        double wv = 0.0;
+        for (int b = 0; b < 6; b++) wv += J[6 * b + a] * R1[b];
+        ls2 += dx[a] * wv;
+      }
+      ls2 *= cls;
+      double alpha = 1.0;
+      for (int ls = 0;; ls++) {
+        double xn[6];
+        for (int a = 0; a < 6; a++) xn[a] = x1[a] + alpha * dx[a];
+        mrr_formR1(cu, xn, x2, R1);
+        dot = 0;
+        for (int a = 0; a < 6; a++) dot += R1[a] * R1[a];
+        nR1 = sqrt(dot);
+        if (0.5 * dot <= ls1 + ls2 * alpha || ls > 10) {
+          for (int a = 0; a < 6; a++) x1[a] = xn[a];
+          break;
+        }
+        alpha *= 0.5;
+      }
+      it++;
+      if (it > c.miter || anynan(x1, 6)) { piters += it; return false; }
+    }
+    piters += it;
+    for (int i = 0; i < 6; i++) x[i] = x1[i];
+    for (int i = 0; i < NH; i++) x[6 + i] = x2[i];
+  }
+  // ---- update (:3162-3293)
+  double R[L];
+  mrr_formR(cu, nrho, x, R, rate);
+  double dot = 0;
+  for (int a = 0; a < L; a++) dot += R[a] * R[a];
+  double nR = sqrt(dot), inR = nR;
+  if (inR == 0.0) inR = inR1;
+  int it = 0;
+  while ((nR > c.atol && nR / inR > c.rtol) || it < 1) {
+    mrr_formJ(cu, x, Jl);
+    haveJ = true;
+    double mJ[L * L], dx[L];
+    for (int a = 0; a < L * L; a++) mJ[a] = -Jl[a];
+    for (int a = 0; a < L; a++) dx[a] = R[a];
+    lu_solve1<L>(mJ, dx);
+    double ls1 = 0.5 * dot, ls2 = 0.0;
+    for (int a = 0; a < L; a++) {
+      double wv = 0.0;
+      for (int b = 0; b < L; b++) wv += Jl[L * b + a] * R[b];
+      ls2 += dx[a] * wv;
+    }
+    ls2 *= cls;
+    double alpha = 1.0;
+    for (int ls = 0;; ls++) {
+      double xn[L];
+      for (int a = 0; a < L; a++) xn[a] = x[a] + alpha * dx[a];
+      mrr_formR(cu, nrho, xn, R, rate);
+      dot = 0;
+      for (int a = 0; a < L; a++) dot += R[a] * R[a];
+      nR = sqrt(dot);
+      if (0.5 * dot <= ls1 + ls2 * alpha || ls > 10) {
+        for (int a = 0; a < L; a++) x[a] = xn[a];
+        break;
+      }
+      alpha *= 0.5;
+    }
+    it++;
+    if (it > c.miter || anynan(x, L)) { iters += it; return false; }
+  }
+  iters += it;
+  for (int i = 0; i < 6; i++) stress[i] = x[i];
+  for (int i = 0; i < NH; i++) tt[i] = x[6 + i];
+  return true;
+}
+
+// One voxel of an MRR grid: the material-point sequence of voxel_update (kinematics,
+// mm10_solve_strup with sub-stepping, mm10_tangent, the rotation update, P and dP/dF)
+// with the densities in history words H_RHO .. H_RHO + 23 (rates after the densities).
+// The learned guess and the alternative starts do not apply: every implicit solve
+// starts from the reference's predictor.
+__device__ void voxel_update_mrr(const StressArgs& a, long long v, int& iters, int& piters,
+                                 bool& ok) {
+  constexpr int L = 6 + NH;
+  const long long N3 = a.N3;
+  double Fn[9], Fn1[9];
+  for (int i = 0; i < 9; i++) {
+    Fn[i] = __ldg(a.Fn + i * N3 + v);
+    Fn1[i] = __ldg(a.Fn1 + i * N3 + v);
+  }
+  const OriRec* rec = a.oris + __ldg(a.ori + v);
+  const CrysRec* cr = a.cryss + __ldg(a.crys + v);
+  // history at n (step 1: mm10_init_mrr, src/mm10_a.f:2205-2223)
+  double nsig[6], nRp[9], nD[6], nrho[NH], nrate[NH];
+  if (a.step == 1) {
+    for (int i = 0; i < 6; i++) { nsig[i] = 0.0; nD[i] = 0.0; }
+    const double r0 = cr->theta_0 == 0.0 ? 1.0e8 : cr->theta_0;
+    for (int i = 0; i < NH; i++) { nrho[i] = r0; nrate[i] = 0.0; }
+    for (int i = 0; i < 9; i++) nRp[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  } else {
+    for (int i = 0; i < 6; i++) nsig[i] = a.hist_n[(H_SIG + i) * N3 + v];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) nRp[3 * i + j] = a.hist_n[(H_RP + 3 * j + i) * N3 + v];
+    for (int i = 0; i < 6; i++) nD[i] = a.hist_n[(H_D + i) * N3 + v];
+    for (int i = 0; i < NH; i++) {
+      nrho[i] = a.hist_n[(H_RHO + i) * N3 + v];
+      nrate[i] = a.hist_n[(H_RHO + NH + i) * N3 + v];
+    }
+  }
+  double rnh[9], rn1[9], fnhinv[9], uddt[6];
+  kinematics(Fn, Fn1, rnh, rn1, fnhinv, uddt);
+  Crystal s;
+  s.cr = cr;
+  s.C = rec->C;
+  s.nsig = nsig;
+  for (int i = 0; i < 6; i++) s.nD[i] = nD[i];
+  setup_np1(s, rec, uddt, a.dt, rn1, nRp);
+  s.temp = TEMP;
+  double stress[6], tt[NH], rate[NH];
+  for (int i = 0; i < 6; i++) stress[i] = nsig[i];
+  for (int i = 0; i < NH; i++) { tt[i] = nrho[i]; rate[i] = 0.0; }
+  double t1 = 0, t2 = 0;
+  for (int i = 0; i < 6; i++) { t1 += uddt[i] * uddt[i]; t2 += stress[i] * stress[i]; }
+  const bool no_load = t1 == 0.0 && t2 == 0.0;
+  const bool iter0 = a.iter == 0;
+  double cep[36];
+  double Jl[L * L];
+  bool haveJ = false;
+  ok = true;
+  if (iter0 || no_load) {  // mm10_solve_strup_a (src/mm10_a.f:2721-2743)
+    for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
+    if (!no_load) {
+      double R1[6];
+      mrr_formR1(s, stress, tt, R1);
+      for (int i = 0; i < 6; i++) stress[i] -= R1[i];
+    }
+  } else {  // mm10_solve_strup_iterate (:2747-2843): at most 4 halvings
+    double ostress[6], ott[NH], frac = 0.0, stp = 1.0;
+    for (int i = 0; i < 6; i++) ostress[i] = stress[i];
+    for (int i = 0; i < NH; i++) ott[i] = tt[i];
+    int cuts = 0;
+    bool fail = false;
+    while (frac < 1.0) {
+      s.tinc = a.dt * (stp + frac);
+      for (int i = 0; i < 6; i++) s.D[i] = uddt[i] * (stp + frac);
+      s.temp = TEMP * (stp + frac);  // n's temperature is zero (:2769)
+      for (int i = 0; i < NH; i++) tt[i] = nrho[i];
+      double rsub[NH];
+      fail = !mrr_solve(s, nrho, nrate, a.dt * stp, stress, tt, Jl, haveJ, iters, piters, rsub);
+      if (fail) {
+        for (int i = 0; i < 6; i++) stress[i] = ostress[i];
+        for (int i = 0; i < NH; i++) tt[i] = ott[i];
+        stp *= 0.5;
+        if (++cuts > 4) break;
+        fail = false;
+      } else {
+        for (int i = 0; i < 6; i++) ostress[i] = stress[i];
+        for (int i = 0; i < NH; i++) { ott[i] = tt[i]; rate[i] = rsub[i]; }
+        frac += stp;
+      }
+    }
+    if (cuts && a.stats) atomicAdd(a.stats + 4, 1ull);
+    s.tinc = a.dt;
+    for (int i = 0; i < 6; i++) s.D[i] = uddt[i];
+    s.temp = TEMP;
+    ok = !(fail || anynan(stress, 6) || anynan(tt, NH));
+    if (ok) {
+      // mm10_tangent (:658-815), ed = dgammadd = 0: T = (J11 - J12 J22^-1 J21)^-1 C
+      double A22[NH * NH], B[NH * 6];
+      for (int r = 0; r < NH; r++)
+        for (int q = 0; q < NH; q++) A22[NH * r + q] = Jl[L * (6 + r) + 6 + q];
+      // LU of J22 once, then the six columns of J21
+      int piv[NH];
+      for (int k = 0; k < NH; k++) {
+        int p = k;
+        double best = fabs(A22[NH * k + k]);
+        for (int i = k + 1; i < NH; i++)
+          if (fabs(A22[NH * i + k]) > best) { best = fabs(A22[NH * i + k]); p = i; }
+        piv[k] = p;
+        if (p != k)
+          for (int j = 0; j < NH; j++) { double t = A22[NH * k + j]; A22[NH * k + j] = A22[NH * p + j]; A22[NH * p + j] = t; }
+        const double inv = 1.0 / A22[NH * k + k];
+        for (int i = k + 1; i < NH; i++) {
+          const double l = A22[NH * i + k] * inv;
+          A22[NH * i + k] = l;
+          for (int j = k + 1; j < NH; j++) A22[NH * i + j] -= l * A22[NH * k + j];
+        }
+      }
+      for (int col = 0; col < 6; col++) {
+        double bcol[NH];
+        for (int r = 0; r < NH; r++) bcol[r] = Jl[L * (6 + r) + col];
+        for (int k = 0; k < NH; k++)
+          if (piv[k] != k) { double t = bcol[k]; bcol[k] = bcol[piv[k]]; bcol[piv[k]] = t; }
+        for (int i = 1; i < NH; i++)
+          for (int k = 0; k < i; k++) bcol[i] -= A22[NH * i + k] * bcol[k];
+        for (int i = NH - 1; i >= 0; i--) {
+          double acc = bcol[i];
+          for (int k = i + 1; k < NH; k++) acc -= A22[NH * i + k] * bcol[k];
+          bcol[i] = acc / A22[NH * i + i];
+        }
+        for (int r = 0; r < NH; r++) B[6 * r + col] = bcol[r];
+      }
+      double JJ[36], T[36];
+      for (int r = 0; r < 6; r++)
+        for (int col = 0; col < 6; col++) {
+          double acc = Jl[L * r + col];
+          for (int q = 0; q < NH; q++) acc -= Jl[L * r + 6 + q] * B[6 * q + col];
+          JJ[6 * r + col] = acc;
+        }
+      for (int col = 0; col < 6; col++) {
+        double m[36], bb[6];
+        for (int i = 0; i < 36; i++) m[i] = JJ[i];
+        for (int i = 0; i < 6; i++) bb[i] = __ldg(rec->C + 6 * i + col);
+        lu_solve1<6>(m, bb);
+        for (int i = 0; i < 6; i++) T[6 * i + col] = bb[i];
+      }
+      for (int i = 0; i < 6; i++)
+        for (int j = 0; j < 6; j++) cep[6 * i + j] = (T[6 * i + j] + T[6 * j + i]) * 0.5;
+    } else {
+      for (int i = 0; i < 6; i++) stress[i] = nsig[i];
+      for (int i = 0; i < NH; i++) { tt[i] = nrho[i]; rate[i] = 0.0; }
+      for (int i = 0; i < 36; i++) cep[i] = __ldg(rec->C + i);
+    }
+  }
+  // ---- plastic rotation (mm10_update_rotation, src/mm10_a.f:3310-3327)
+  double Rp[9];
+  if (!ok) {
+    for (int i = 0; i < 9; i++) Rp[i] = nRp[i];
+  } else if (iter0 || no_load) {
+    for (int i = 0; i < 9; i++) Rp[i] = 0.0;
+  } else {
+    double tr[9], RW[9];
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) tr[3 * i + j] = nRp[3 * j + i];
+    rt2rvw(tr, RW);
+    double wb[3] = {0, 0, 0};
+    for (int i = 0; i < NS; i++) {
+      MrrSys y;
+      mrr_sys(s, stress, tt, i, y);
+      double q0[3], qs[3];
+      for (int k = 0; k < 3; k++) q0[k] = __ldg(rec->qs + 3 * i + k);
+      for (int k = 0; k < 3; k++) qs[k] = RW[3 * k] * q0[0] + RW[3 * k + 1] * q0[1] + RW[3 * k + 2] * q0[2];
+      for (int k = 0; k < 3; k++) wb[k] += y.slip * qs[k];
+    }
+    double W[9] = {0.0, wb[2], wb[1], -wb[2], 0.0, wb[0], -wb[1], -wb[0], 0.0};
+    const double al = sqrt(W[5] * W[5] + W[2] * W[2] + W[1] * W[1]);
+    double ex[9];
+    if (al < 1.0e-16) {
+      for (int i = 0; i < 9; i++) ex[i] = 0.0;
+    } else {
+      double WW[9];
+      mm3(W, W, WW);
+      const double ca = (1.0 - cos(al)) / (al * al), sa = sin(al) / al;
+      for (int i = 0; i < 9; i++) ex[i] = ca * WW[i] + sa * W[i];
+    }
+    ex[0] += 1.0; ex[4] += 1.0; ex[8] += 1.0;
+    mm3(ex, nRp, Rp);
+  }
+  // ---- history n+1
+  for (int i = 0; i < 6; i++) a.hist_np1[(H_SIG + i) * N3 + v] = stress[i];
+  a.hist_np1[H_TT * N3 + v] = 0.0;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) a.hist_np1[(H_RP + 3 * j + i) * N3 + v] = Rp[3 * i + j];
+  for (int i = 0; i < 6; i++) a.hist_np1[(H_D + i) * N3 + v] = uddt[i];
+  a.hist_np1[H_TTR * N3 + v] = 0.0;
+  a.hist_np1[H_U * N3 + v] = 0.0;
+  a.hist_np1[(H_U + 1) * N3 + v] = 0.0;
+  for (int i = 0; i < 6; i++)
+    a.hist_np1[(H_EPS + i) * N3 + v] = (a.step == 1 ? 0.0 : a.hist_n[(H_EPS + i) * N3 + v]) + uddt[i];
+  for (int i = 0; i < NH; i++) {
+    a.hist_np1[(H_RHO + i) * N3 + v] = tt[i];
+    a.hist_np1[(H_RHO + NH + i) * N3 + v] = rate[i];
+  }
+  store_P_K4(a, v, Fn, Fn1, stress, cep, rnh, rn1, fnhinv);
+}

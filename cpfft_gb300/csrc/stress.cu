@@ -20,7 +20,8 @@
 #define CPFFT_STRESS_LAUNCH launch_stress
 #endif
 // Hardening law: Voce (1) here; stress_mts.cu compiles this file again with CPFFT_LAW 2
-// (MTS).  The kernels that serve every grid (mm01, the voxel queue) live in the first unit.
+// (MTS) and stress_mrr.cu with CPFFT_LAW 7 (Ma-Roters-Raabe, mrr.cuh).  The kernels that
+// serve every grid (mm01, the voxel queue) live in the first unit.
 #ifndef CPFFT_LAW
 #define CPFFT_LAW 1
 #endif
@@ -31,6 +32,7 @@ namespace {
 
 constexpr int NS = CPFFT_NSLIP;  // slip systems
 constexpr bool MTS = CPFFT_LAW == 2;
+constexpr bool MRR = CPFFT_LAW == 7;
 // the temperature of the reference's FFT path (drive_10_update, src/rstgp1.f:832)
 constexpr double TEMP = 297.0;
 
@@ -876,6 +878,10 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
                            const double* stress, const double* cep, const double* rnh,
                            const double* rn1, const double* fnhinv);
 
+#if CPFFT_LAW == 7
+#include "mrr.cuh"
+#endif
+
 // WARM: the learned initial guess starts each local Newton solve (launches with iter > 0
 // only); every thread of the block takes part in the block-level network evaluation, so
 // the tail chunk's surplus threads evaluate a copy of the last voxel and store nothing.
@@ -925,11 +931,15 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
     const bool mine = valid && (!a.mises || __ldg(a.mises + v) < 0);
     int it = 0, pit = 0, rj = 0;
     bool ok = true;
+#if CPFFT_LAW == 7
+    if (mine) voxel_update_mrr(a, v, it, pit, ok);  // no learned guess for MRR grids
+#else
     if (WARM) {
       voxel_update<true>(a, v, mine, it, pit, ok, rj, &gb);
     } else if (mine) {
       voxel_update<false>(a, v, true, it, pit, ok, rj, nullptr);
     }
+#endif
     if (mine) {
       iters += it;
       piters += pit;
@@ -1571,15 +1581,14 @@ cudaError_t launch_mises(const StressArgs& a, cudaStream_t s) {
 }
 #endif
 
-cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm, cudaStream_t s) {
+cudaError_t CPFFT_STRESS_LAUNCH(const StressArgs& a, bool warm_in, cudaStream_t s) {
   if (a.N3 <= 0) return cudaSuccess;
-  static bool attr = false;
-  if (warm && !attr) {
+  const bool warm = warm_in && !MRR;  // the MRR solve has no learned guess
+  if (warm) {  // set on every call: the attribute belongs to the current device
     cudaError_t e = cudaFuncSetAttribute(stress_kernel<true>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          mlp::FWD_SMEM);
     if (e != cudaSuccess) return e;
-    attr = true;
   }
   unsigned blocks = (unsigned)((a.N3 + 127) / 128);
   if (a.perm) {

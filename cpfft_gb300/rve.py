@@ -11,12 +11,14 @@ from dataclasses import dataclass
 
 import numpy as np
 
-# MTS parameters (h_type 2) at the reference's crystal defaults (initialize_new_crystal,
-# src/mod_crystals.f:257-276); Voce crystals carry them unread.
+# MTS parameters (h_type 2) and the Ma-Roters-Raabe constants c1..c6 (h_type 7) at the
+# reference's crystal defaults (initialize_new_crystal, src/mod_crystals.f:257-285); Voce
+# crystals carry them unread.
 MTS_DEFAULTS = dict(
     tau_a=0.0, tau_hat_y=-1.0, G_0_y=-1.0, p_y=0.5, q_y=2.0, tau_hat_v=-1.0, G_0_v=-1.0,
     p_v=0.5, q_v=2.0, eps_dot_0_v=1.0e10, burgers=2.87e-7, boltzman=1.3806e-20,
     mu_0=69000.0 / 2.0 / 1.33, D_0=0.0, T_0=294.0,
+    u1=0.0, u2=0.0, u3=0.0, u4=0.0, u5=0.0, u6=0.0,
 )
 
 # Material of the named workloads (MPa, s): FCC {111}<110>, anisotropic type-3
@@ -69,6 +71,20 @@ MTS_FCC = dict(
     tau_a=20.0, tau_hat_y=200.0, G_0_y=0.5, p_y=0.5, q_y=2.0,
     tau_hat_v=300.0, G_0_v=0.5, p_v=0.5, q_v=2.0, eps_dot_0_v=1.0e7, gamma_bar=1.0e7,
     burgers=2.5e-7, boltzman=1.3806e-20, mu_0=75400.0, D_0=0.0, T_0=294.0,
+)
+
+# An FCC crystal with Ma-Roters-Raabe hardening (h_type 7; N, mm, s, MPa): the workloads'
+# elasticity, twelve dislocation densities starting at 1e6 / mm^2, thermally activated
+# glide over the passing stress (Q_slip = 3e-16 N mm, 73 kT at 297 K; attack frequency
+# 1e10 / s) with p = 1, q = 2 (with p < 1 the reference's fract**p is NaN wherever the
+# resolved shear is below the passing stress), storage c4 = 0.01, athermal annihilation
+# c5 = 5, dipole formation c6 = 1, thermal annihilation c7 = 0.01 (Q_bulk = 2.4e-16 N mm,
+# exponent c8 = 0.3); exact local Jacobian.
+MRR_FCC = dict(
+    FCC_VOCE, h_type=7, exact_j22=1, alter_mode=0,
+    tau_a=2.4e-16, G_0_v=3.0e-16, G_0_y=1.0e10, p_v=1.0, q_v=2.0,
+    tau_hat_y=0.01, tau_hat_v=0.3, burgers=2.5e-7, boltzman=1.3806e-20, mu_0=75400.0,
+    theta_0=1.0e6, u1=0.5, u2=0.1, u3=1.0, u4=0.01, u5=5.0, u6=1.0,
 )
 
 # component order of 9-vectors: 11,12,13,21,22,23,31,32,33

@@ -64,8 +64,9 @@ typedef struct cpfft_crystal {
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;
-    int    h_type;         /* 1 = voce, 2 = mts (fcc crystals); the crystals of one grid
-                              share the hardening law                                       */
+    int    h_type;         /* 1 = voce, 2 = mts, 7 = roters (Ma-Roters-Raabe dislocation
+                              densities, one per slip system); fcc crystals; the crystals of
+                              one grid share the hardening law                              */
     double harden_n;       /* rate exponent                                               */
     double tau_y, tau_v, theta_0, voce_m;
     double gamma_bar;      /* eps_dot_0_y                                                 */
@@ -87,6 +88,16 @@ typedef struct cpfft_crystal {
                                            part's is gamma_bar, eps_dot_0_y)               */
     double burgers, boltzman;
     double mu_0, D_0, T_0;              /* mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1)       */
+    /* Ma-Roters-Raabe hardening (h_type 7: mm10_slipinc_mrr .. mm10_dgdd_mrr,
+       src/mm10_b.f:2343-3325; initial densities mm10_init_mrr, src/mm10_a.f:2205-2223):
+       twelve dislocation densities, the slip resistance variables of the twelve systems.
+       It reads tau_a (Q_bulk), G_0_v (Q_slip), G_0_y (attack frequency), p_v, q_v,
+       tau_hat_y (c7), tau_hat_v (c8), burgers, boltzman, mu_0 (shear modulus),
+       theta_0 (initial density; 0 gives 1e8) and c1..c6 below.  exact_j22 = 1 takes
+       the exact derivatives of the residual in the local Jacobian (the reference's use
+       sqrt(rho_F) where the residual has sqrt(rho_P), src/mm10_b.f:2635 against :2952
+       and :3075).                                                                    */
+    double u1, u2, u3, u4, u5, u6;      /* c1 .. c6                                      */
 } cpfft_crystal;
 
 /* slip_type of a material that is not a crystal: its cpfft_crystal entry is not read, and
@@ -404,10 +415,17 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
                       int schedule, double tolNR, double tolPCG, int maxIter, int nthreads);
 
 /* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
- * compact history at n (N3, CPFFT_HIST_WORDS) used by the result writers. */
+ * compact history at n (N3, cpfft_hist_words()) used by the result writers. */
 #define CPFFT_HIST_WORDS 31   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6)
                                  u(2): MTS tau_y and mu at the step's end (mm10's u(1:2)) */
+#define CPFFT_HIST_WORDS_MRR 55  /* grids of Ma-Roters-Raabe crystals (h_type 7): the words
+                                    above (tau_tilde, its rate and u zero), then the twelve
+                                    dislocation densities (mm10's tau_tilde(1:12)) and their
+                                    rates (tt_rate(1:12))                                  */
 int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history);
+/* Words per voxel of the current context's history: CPFFT_HIST_WORDS, or
+ * CPFFT_HIST_WORDS_MRR on a grid of Ma-Roters-Raabe crystals; negative on error. */
+int cpfft_hist_words(void);
 
 /* ---- element result files (ouelestr, src/ouresult.f:140-300) --------------------------
  * The per-voxel lines of the flat text files wesNNNNN_text (quantity 2: the unrotated

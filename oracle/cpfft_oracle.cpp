@@ -250,6 +250,8 @@ struct Crys {
   M6 C0;                 // stiffness in the crystal frame
   int ns;                // slip systems
   double b[48][3], n[48][3];
+  // Ma-Roters-Raabe interaction matrices (h_type 7): rho_F = Gm rho, rho_P = Hm rho
+  double Gm[12][12], Hm[12][12];
 };
 void fcc_systems(double b[12][3], double n[12][3]) {
   // FCC {111}<110>: slip directions and plane normals, in the reference's order.
@@ -313,6 +315,21 @@ void crystal_finalize(const cpfft_crystal& p, Crys& c) {
     std::memcpy(c.b, b, sizeof(b));
     std::memcpy(c.n, n, sizeof(n));
   }
+  // the forest and parallel projections of mm10_mrr_GHfcc (src/mm10_e.f:55-340):
+  // Gm(a,b) = |n_a . t_b|, Hm(a,b) = |n_a x t_b|, t_b = n_b x b_b the edge line direction
+  for (int a = 0; a < 12; a++)
+    for (int q = 0; q < 12; q++) {
+      double t[3] = {c.n[q][1] * c.b[q][2] - c.n[q][2] * c.b[q][1],
+                     c.n[q][2] * c.b[q][0] - c.n[q][0] * c.b[q][2],
+                     c.n[q][0] * c.b[q][1] - c.n[q][1] * c.b[q][0]};
+      double tl = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+      for (int k = 0; k < 3; k++) t[k] /= tl;
+      const double* na = c.n[a];
+      double x[3] = {na[1] * t[2] - na[2] * t[1], na[2] * t[0] - na[0] * t[2],
+                     na[0] * t[1] - na[1] * t[0]};
+      c.Gm[a][q] = std::fabs(na[0] * t[0] + na[1] * t[1] + na[2] * t[2]);
+      c.Hm[a][q] = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    }
   std::memset(c.C0, 0, sizeof(c.C0));
   if (p.elastic_type == 3) {
     double C22 = p.C11, C23 = p.C13, C66 = p.C55;
@@ -393,6 +410,10 @@ struct State {          // compact history (CPFFT_HIST_WORDS order)
   double h01[12];
   double cgx[3];
   double u[2];          // MTS: tau_y and mu of the step (mm10's u(1:2)); -1 = not yet set
+  // Ma-Roters-Raabe crystals (mrr set): the twelve dislocation densities (tau_tilde(1:12))
+  // and their rates, history words 31..42 and 43..54; tt and tt_rate are not used
+  bool mrr;
+  double rho[12], rho_rate[12];
 };
 void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f:473-571)
   std::memset(&s, 0, sizeof(s));
@@ -401,6 +422,11 @@ void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f
   if (cr.p.h_type == 2) {                    // mm10_init_mts (:2090-2107): flags
     s.tt = -1.0;
     s.u[0] = s.u[1] = -1.0;
+  }
+  if (cr.p.h_type == 7) {                    // mm10_init_mrr (:2205-2223)
+    s.mrr = true;
+    s.tt = 0.0;
+    for (int i = 0; i < 12; i++) s.rho[i] = cr.p.theta_0 == 0.0 ? 1.0e8 : cr.p.theta_0;
   }
 }
 void state_pack(const State& s, double* h) {
@@ -421,6 +447,11 @@ void state_pack(const State& s, double* h) {
   for (int i = 0; i < 6; i++) h[23 + i] = s.eps[i];
   h[29] = s.u[0];
   h[30] = s.u[1];
+  if (s.mrr)
+    for (int i = 0; i < 12; i++) {
+      h[ORC_HIST + i] = s.rho[i];
+      h[ORC_HIST + 12 + i] = s.rho_rate[i];
+    }
 }
 void state_unpack(const double* h, State& s) {
   if (s.m01) {
@@ -440,6 +471,11 @@ void state_unpack(const double* h, State& s) {
   for (int i = 0; i < 6; i++) s.eps[i] = h[23 + i];
   s.u[0] = h[29];
   s.u[1] = h[30];
+  if (s.mrr)
+    for (int i = 0; i < 12; i++) {
+      s.rho[i] = h[ORC_HIST + i];
+      s.rho_rate[i] = h[ORC_HIST + 12 + i];
+    }
 }
 
 // the np1 / curr "crystal_state" pieces the Voce routines read
@@ -449,6 +485,7 @@ struct Np1 {
   double ms[48][6], qs[48][3], qc[48][3];
   double tt_rate;
   double temp, mu, tau_y, tau_v, ntau_y, nmu;  // MTS
+  double rho_rate[12];                          // MRR: rates of the twelve densities
 };
 
 // mm10_setup_mts's shear modulus and thresholds (src/mm10_a.f:2109-2150) at rate dgc, T
@@ -1010,6 +1047,519 @@ struct Mm10 {
   }
 };
 
+// ---- Ma-Roters-Raabe hardening (h_type 7), FCC, one density per slip system --------
+// mm10_slipinc_mrr .. mm10_dgdd_mrr (src/mm10_b.f:2343-3325), the (6 + 12)-unknown
+// mm10_solve (src/mm10_a.f:2860-3295) and mm10_tangent (:658-815) with ed = dgammadd = 0
+// (mm10_ed_mrr, mm10_dgdd_mrr).  exact_j22 = 0 forms the local Jacobian with the
+// reference's formulas, which do not all differentiate its residual: estress / ehard use
+// sqrt(rho_F) where mm10_h_mrr has sqrt(rho_P) (src/mm10_b.f:2635, 2952, 3075), the
+// estress "badterm" lacks the sign of tau, and the extrapolated branch of dgdt / dgdh
+// (fract > 1) drops terms.  exact_j22 = 1 differentiates the residual exactly.
+const int MRR_NH = 12;
+struct Mrr {
+  const cpfft_crystal* p;
+  const VoxProps* vp;
+  const State* n;
+  const double (*Gm)[12];   // rho_F = Gm rho  (mm10_mrr_GH)
+  const double (*Hm)[12];   // rho_P = Hm rho
+
+  // mm10_setup (src/mm10_a.f:830-975) with mm10_setup_mrr (:2225-2240: time only)
+  void setup(Np1& s, const double D[6], double tinc, const M3 R, double T) const {
+    for (int i = 0; i < 6; i++) s.D[i] = D[i];
+    s.tinc = tinc;
+    s.dg = 0.0;
+    M3 tnRp, RW, work, RWC;
+    tr33(n->Rp, tnRp);
+    M6 RE;
+    rt2rve(tnRp, RE);
+    rt2rvw(tnRp, RW);
+    mm33(R, tnRp, work);
+    rt2rvw(work, RWC);
+    for (int i = 0; i < vp->ns; i++) {
+      mv6(RE, vp->ms[i], s.ms[i]);
+      for (int a = 0; a < 3; a++) {
+        s.qs[i][a] = RW[a][0] * vp->qs[i][0] + RW[a][1] * vp->qs[i][1] + RW[a][2] * vp->qs[i][2];
+        s.qc[i][a] = RWC[a][0] * vp->qs[i][0] + RWC[a][1] * vp->qs[i][1] + RWC[a][2] * vp->qs[i][2];
+      }
+    }
+    s.temp = T;
+  }
+  double rs(const Np1& s, const double* st, int i) const {
+    return st[0] * s.ms[i][0] + st[1] * s.ms[i][1] + st[2] * s.ms[i][2] +
+           st[3] * s.ms[i][3] + st[4] * s.ms[i][4] + st[5] * s.ms[i][5];
+  }
+  // the quantities of system a at (st, tt) that every MRR routine forms
+  struct Sys {
+    double rs, rhoF, rhoP, g0, tpass, tcut, fract, slip;
+  };
+  void sys(const Np1& s, const double* st, const double* tt, int a, Sys& y) const {
+    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers;
+    y.rs = rs(s, st, a);
+    y.rhoF = 0.0;
+    y.rhoP = 0.0;
+    for (int q = 0; q < MRR_NH; q++) {
+      y.rhoF += Gm[a][q] * tt[q];
+      y.rhoP += Hm[a][q] * tt[q];
+    }
+    y.g0 = p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) * std::sqrt(y.rhoP);   // (15)
+    y.tpass = p->u1 * G * b * std::sqrt(y.rhoP);                                 // (16)
+    y.tcut = p->G_0_v / (p->u2 * p->u3 * b * b) * std::sqrt(y.rhoF);             // (17)
+    y.fract = (std::fabs(y.rs) - y.tpass) / y.tcut;
+    // mm10_slipinc_mrr (src/mm10_b.f:2477-2546)
+    const double Qk = p->G_0_v / k / th;
+    if (y.fract > 1.0) {  // linear extrapolation past fract = 1
+      double m = y.g0 * (-p->q_v * Qk) * (-p->p_v) * sgn1(y.rs) / y.tcut;
+      y.slip = s.tinc * (m * y.fract + y.g0);
+    } else if (std::fabs(y.rs) > 0.0) {
+      y.slip = s.tinc * y.g0 * sgn1(y.rs) *
+               std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v));  // (14)
+    } else {
+      y.slip = 0.0;
+    }
+  }
+  // d slip / d rs (mm10_dgdt_mrr, src/mm10_b.f:3111-3198)
+  double dgdt(const Np1& s, const Sys& y) const {
+    const double Qk = p->G_0_v / p->boltzman / s.temp;
+    const double dfract = sgn1(y.rs) / y.tcut;
+    if (y.fract > 1.0) {
+      double m = y.g0 * (-p->q_v * Qk) * (-p->p_v) * sgn1(y.rs) / y.tcut;
+      return p->exact_j22 ? s.tinc * m * dfract : s.tinc * m;
+    }
+    if (std::fabs(y.rs) > 0.0) {
+      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v)) * sgn1(y.rs);
+      return s.tinc * (-y.g0 * slipexp * Qk * p->q_v *
+                       std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v - 1.0) * (-1.0) * p->p_v *
+                       std::pow(y.fract, p->p_v - 1.0) * dfract);
+    }
+    return 0.0;
+  }
+  // d slip_a / d rho_c (mm10_dgdh_mrr, src/mm10_b.f:3201-3306)
+  double dgdh(const Np1& s, const Sys& y, int a, int c) const {
+    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers;
+    const double Qk = p->G_0_v / k / th;
+    const double drhoF = Gm[a][c], drhoP = Hm[a][c];
+    const double dg0 = 0.5 * p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) / std::sqrt(y.rhoP) * drhoP;
+    const double dtpass = 0.5 * p->u1 * G * b / std::sqrt(y.rhoP) * drhoP;
+    const double dtcut = 0.5 * p->G_0_v / (p->u2 * p->u3 * b * b) / std::sqrt(y.rhoF) * drhoF;
+    const double dfract = ((-dtpass) * y.tcut - (std::fabs(y.rs) - y.tpass) * dtcut) / (y.tcut * y.tcut);
+    if (y.fract > 1.0) {
+      double K = (-p->q_v * Qk) * (-p->p_v) * sgn1(y.rs);
+      double dm = K * (dg0 / y.tcut - y.g0 * dtcut / (y.tcut * y.tcut));
+      if (!p->exact_j22) return s.tinc * dm;
+      double m = y.g0 * K / y.tcut;
+      return s.tinc * (dm * y.fract + m * dfract + dg0);
+    }
+    if (std::fabs(y.rs) > 0.0) {
+      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v));
+      return s.tinc * (dg0 * slipexp * sgn1(y.rs) +
+                       y.g0 * sgn1(y.rs) * slipexp * (-1.0) * Qk * p->q_v *
+                           std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v - 1.0) * (-1.0) *
+                           p->p_v * std::pow(y.fract, p->p_v - 1.0) * dfract);
+    }
+    return 0.0;
+  }
+  // R1 (mm10_formR1, src/mm10_b.f:1061-1101) with dbarp / wp of the MRR slips
+  void formR1(const Np1& s, const double* st, const double* tt, double R1[6]) const {
+    double dbar[6] = {0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0};
+    for (int i = 0; i < vp->ns; i++) {
+      Sys y;
+      sys(s, st, tt, i, y);
+      for (int a = 0; a < 6; a++) dbar[a] = dbar[a] + y.slip * s.ms[i][a];
+      for (int a = 0; a < 3; a++) w[a] = w[a] + y.slip * s.qc[i][a];
+    }
+    double sw[6], wv1[6], wv2[6];
+    Mm10::symsw(st, w, sw);
+    for (int a = 0; a < 6; a++) wv1[a] = s.D[a] - dbar[a];
+    mv6(vp->C, wv1, wv2);
+    for (int a = 0; a < 6; a++) R1[a] = st[a] - n->sig[a] - wv2[a] + 2.0 * sw[a];
+  }
+  // mm10_h_mrr (src/mm10_b.f:2549-2646) and R2 = tt - h (mm10_formR2, :63-113)
+  void formR2(Np1& s, const double* st, const double* tt, double* R2) const {
+    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers, v = 0.3;
+    for (int a = 0; a < MRR_NH; a++) {
+      Sys y;
+      sys(s, st, tt, a, y);
+      const double rho = tt[a], rho_n = n->rho[a];
+      const double ddip = std::sqrt(3.0) * G * b / (16.0 * PI * (1.0 - v)) / std::fabs(y.rs);  // (42)
+      const double rhoM = (2.0 * k / (p->u1 * p->u2 * p->u3 * G * b * b * b)) * th *
+                          std::sqrt(y.rhoF * y.rhoP);                                       // (13)
+      const double gd = std::fabs(y.slip / s.tinc);
+      const double tem1 = p->u4 / b * std::sqrt(y.rhoP) * gd;
+      const double tem2 = p->u6 * ddip / b * rhoM * gd;
+      const double tem3 = p->u5 * rho * gd;
+      const double tem4 = p->tau_hat_y * std::exp(-p->tau_a / k / th) * std::fabs(y.rs) / (k * th) *
+                          rho * rho * std::pow(gd, p->tau_hat_v);
+      const double h = rho_n + s.tinc * (tem1 + tem2 - tem3 - tem4);                       // (18)
+      R2[a] = tt[a] - h;
+      s.rho_rate[a] = (h - rho_n) / s.tinc;
+    }
+  }
+  void formR(Np1& s, const double* x, double* R) const {
+    formR1(s, x, x + 6, R);
+    formR2(s, x, x + 6, R + 6);
+  }
+  // J11 (mm10_formJ11, src/mm10_b.f:177-257) with mm10_dgdt_mrr
+  void formJ11(const Np1& s, const double* st, const double* tt, double J[6][6]) const {
+    std::memset(J, 0, 36 * sizeof(double));
+    double w[3] = {0, 0, 0};
+    for (int i = 0; i < vp->ns; i++) {
+      Sys y;
+      sys(s, st, tt, i, y);
+      const double dg = dgdt(s, y);
+      double sq[6], wv[6];
+      Mm10::symsw(st, s.qc[i], sq);
+      for (int a = 0; a < 6; a++) wv[a] = 2.0 * sq[a];
+      for (int j = 0; j < 6; j++)
+        for (int a = 0; a < 6; a++) wv[a] = wv[a] + vp->C[a][j] * s.ms[i][j];
+      for (int c = 0; c < 6; c++) {
+        double t = dg * s.ms[i][c];
+        for (int a = 0; a < 6; a++) J[a][c] += wv[a] * t;
+      }
+      for (int a = 0; a < 3; a++) w[a] = w[a] + y.slip * s.qc[i][a];  // mm10_form_wp
+    }
+    double iw[6][6];
+    std::memset(iw, 0, sizeof(iw));  // mm10_iw (src/mm10_b.f:1590-1634)
+    iw[0][3] = 2.0 * w[2];  iw[0][5] = -2.0 * w[1];
+    iw[1][3] = 2.0 * w[2];  iw[1][4] = -2.0 * w[0];
+    iw[2][4] = 2.0 * w[0];  iw[2][5] = 2.0 * w[1];
+    iw[3][0] = w[2];  iw[3][1] = -w[2]; iw[3][4] = -w[1]; iw[3][5] = w[0];
+    iw[4][1] = w[0];  iw[4][2] = -w[0]; iw[4][3] = w[1];  iw[4][5] = w[2];
+    iw[5][0] = w[1];  iw[5][2] = -w[1]; iw[5][3] = w[0];  iw[5][4] = -w[2];
+    for (int a = 0; a < 6; a++)
+      for (int c = 0; c < 6; c++) J[a][c] = J[a][c] + iw[a][c];
+    for (int a = 0; a < 6; a++) J[a][a] = J[a][a] + 1.0;
+  }
+  // the (6 + 12)^2 Jacobian (mm10_formJ, src/mm10_b.f:901-954), row-major J[18*r + c]:
+  // J12 (mm10_formJ12 with mm10_dgdh_mrr), J21 = -estress (mm10_estress_mrr,
+  // src/mm10_b.f:2859-2963), J22 = ehard (mm10_ehard_mrr, :2966-3092)
+  void formJ(const Np1& s, const double* x, double* J) const {
+    const int L = 6 + MRR_NH;
+    const double* st = x;
+    const double* tt = x + 6;
+    double J11[6][6];
+    formJ11(s, st, tt, J11);
+    for (int a = 0; a < 6; a++)
+      for (int c = 0; c < 6; c++) J[L * a + c] = J11[a][c];
+    Sys ys[MRR_NH];
+    double dgt[MRR_NH];
+    for (int a = 0; a < MRR_NH; a++) {
+      sys(s, st, tt, a, ys[a]);
+      dgt[a] = dgdt(s, ys[a]);
+    }
+    // J12
+    for (int a = 0; a < 6; a++)
+      for (int c = 0; c < MRR_NH; c++) J[L * a + 6 + c] = 0.0;
+    for (int i = 0; i < vp->ns; i++) {
+      double sq[6], tm[6];
+      Mm10::symsw(st, s.qc[i], sq);
+      for (int a = 0; a < 6; a++) tm[a] = 2.0 * sq[a];
+      for (int j = 0; j < 6; j++)
+        for (int a = 0; a < 6; a++) tm[a] = tm[a] + vp->C[a][j] * s.ms[i][j];
+      for (int c = 0; c < MRR_NH; c++) {
+        double d = dgdh(s, ys[i], i, c);
+        for (int a = 0; a < 6; a++) J[L * a + 6 + c] += tm[a] * d;
+      }
+    }
+    // J21, J22
+    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers, v = 0.3;
+    const double dt = s.tinc;
+    const double cdip = std::sqrt(3.0) * G * b / (16.0 * PI * (1.0 - v));
+    const double cM = 2.0 * k / (p->u1 * p->u2 * p->u3 * G * b * b * b) * th;
+    const double E = p->tau_hat_y * std::exp(-p->tau_a / k / th) / (k * th);
+    const double c8 = p->tau_hat_v;
+    for (int a = 0; a < MRR_NH; a++) {
+      const Sys& y = ys[a];
+      const double rho = tt[a], sg = sgn1(y.rs), ars = std::fabs(y.rs);
+      const double ddip = cdip / ars;
+      const double dddip = -cdip / (ars * ars) * sg;
+      const double rhoM = cM * std::sqrt(y.rhoF * y.rhoP);
+      const double gd = std::fabs(y.slip / dt);
+      const double dsl = dgt[a] / dt;
+      double et;
+      if (!p->exact_j22) {
+        double bad = gd == 0.0 ? 0.0 : c8 * ars * std::pow(gd, c8 - 1.0) * dsl;
+        et = dt * (p->u4 / b * std::sqrt(y.rhoF) * sg * dsl +
+                   p->u6 / b * rhoM * (ddip * sg * dsl + dddip * gd) - p->u5 * rho * sg * dsl -
+                   E * rho * rho * (bad + sg * std::pow(gd, c8)));
+      } else {
+        const double sgd = sgn1(y.slip);  // d|slip| = sign(slip) d slip
+        const double dgd = sgd * dsl;     // d gd / d rs
+        double bad = gd == 0.0 ? 0.0 : c8 * ars * std::pow(gd, c8 - 1.0) * dgd;
+        et = dt * (p->u4 / b * std::sqrt(y.rhoP) * dgd +
+                   p->u6 / b * rhoM * (ddip * dgd + dddip * gd) - p->u5 * rho * dgd -
+                   E * rho * rho * (bad + sg * std::pow(gd, c8)));
+      }
+      for (int c = 0; c < 6; c++) J[L * (6 + a) + c] = -et * s.ms[a][c];
+      for (int c = 0; c < MRR_NH; c++) {
+        const double drhoF = Gm[a][c], drhoP = Hm[a][c];
+        const double drhoM = 0.5 * cM / std::sqrt(y.rhoF * y.rhoP) * (drhoF * y.rhoP + y.rhoF * drhoP);
+        const double d = a == c ? 1.0 : 0.0;
+        const double dsh = dgdh(s, y, a, c) / dt;
+        double e;
+        if (!p->exact_j22) {
+          double bad = gd == 0.0 ? 0.0 : c8 * std::pow(gd, c8 - 1.0) * dsh;
+          e = d - dt * (p->u4 / b * (0.5 * drhoF / std::sqrt(y.rhoF) * gd * sg + std::sqrt(y.rhoF) * dsh) +
+                        p->u6 / b * (rhoM * ddip * dsh + drhoM * ddip * gd * sg) -
+                        p->u5 * (rho * dsh + d * gd * sg) -
+                        E * ars * (rho * rho * bad + 2.0 * rho * sg * d * std::pow(gd, c8))) * sg;
+        } else {
+          const double dgd = sgn1(y.slip) * dsh;
+          double bad = gd == 0.0 ? 0.0 : c8 * std::pow(gd, c8 - 1.0) * dgd;
+          e = d - dt * (p->u4 / b * (0.5 * drhoP / std::sqrt(y.rhoP) * gd + std::sqrt(y.rhoP) * dgd) +
+                        p->u6 / b * ddip * (rhoM * dgd + drhoM * gd) - p->u5 * (rho * dgd + d * gd) -
+                        E * ars * (rho * rho * bad + 2.0 * rho * d * std::pow(gd, c8)));
+        }
+        J[L * (6 + a) + 6 + c] = e;
+      }
+    }
+  }
+
+  // mm10_solve (src/mm10_a.f:2860-3295) for 6 + 12 unknowns; Jl: the last Jacobian
+  bool solve(Np1& cu, double dtinc, double stress[6], double* tt, double* Jl, bool& haveJ,
+             int& iters) const {
+    const int L = 6 + MRR_NH;
+    const double c = 1.0e-4, red = 0.5;
+    const int mls = 10, mmin = 1;
+    double x[6 + MRR_NH];
+    for (int i = 0; i < 6; i++) x[i] = stress[i];
+    for (int i = 0; i < MRR_NH; i++) x[6 + i] = tt[i];
+    double inR1;
+    {  // predict (:2975-3156): R1 Newton with the densities extrapolated
+      int iter = 0;
+      double x1[6], x2[MRR_NH];
+      for (int i = 0; i < 6; i++) x1[i] = x[i];
+      double d1[6], d2[6];
+      for (int i = 0; i < 6; i++) { d1[i] = cu.D[i]; d2[i] = n->D[i]; }
+      for (double* d : {d1, d2}) {
+        double dtr = (d[0] + d[1] + d[2]) / 3.0;
+        d[0] -= dtr; d[1] -= dtr; d[2] -= dtr;
+        double t1 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double t2 = d[3] * d[3] + d[4] * d[4] + d[5] * d[5];
+        if (t1 + t2 == 0.0) for (int i = 0; i < 6; i++) d[i] = 0.0;
+        else { double nn = std::sqrt(t1 + t2); for (int i = 0; i < 6; i++) d[i] = d[i] / nn; }
+      }
+      double t1 = d1[0] * d2[0] + d1[1] * d2[1] + d1[2] * d2[2];
+      double t2 = d1[3] * d2[3] + d1[4] * d2[4] + d1[5] * d2[5];
+      double cos_ang = std::max(t1 + t2, 0.0);
+      for (int i = 0; i < MRR_NH; i++) x2[i] = x[6 + i] + cos_ang * n->rho_rate[i] * dtinc;
+      double R1[6];
+      formR1(cu, x1, x2, R1);
+      double nR1 = std::sqrt(R1[0] * R1[0] + R1[1] * R1[1] + R1[2] * R1[2] + R1[3] * R1[3] +
+                             R1[4] * R1[4] + R1[5] * R1[5]);
+      inR1 = nR1;
+      while (nR1 > p->atol1 && nR1 / inR1 > p->rtol1) {
+        double J11[6][6];
+        formJ11(cu, x1, x2, J11);
+        double mJ[36], dx1[6];
+        for (int a = 0; a < 6; a++)
+          for (int b = 0; b < 6; b++) mJ[a * 6 + b] = -J11[a][b];
+        for (int a = 0; a < 6; a++) dx1[a] = R1[a];
+        lu_solve(6, mJ, 1, dx1);
+        double alpha = 1.0;
+        double dotR1 = 0;
+        for (int a = 0; a < 6; a++) dotR1 += R1[a] * R1[a];
+        double ls1 = 0.5 * dotR1, wv[6], ls2 = 0;
+        for (int a = 0; a < 6; a++) {
+          wv[a] = 0.0;
+          for (int b = 0; b < 6; b++) wv[a] += J11[b][a] * R1[b];
+        }
+        for (int a = 0; a < 6; a++) ls2 += dx1[a] * wv[a];
+        ls2 = c * ls2;
+        int ls = 0;
+        for (;;) {
+          double nlsx = ls1 + ls2 * alpha;
+          double xn[6];
+          for (int a = 0; a < 6; a++) xn[a] = x1[a] + alpha * dx1[a];
+          formR1(cu, xn, x2, R1);
+          dotR1 = 0;
+          for (int a = 0; a < 6; a++) dotR1 += R1[a] * R1[a];
+          nR1 = std::sqrt(dotR1);
+          if (0.5 * dotR1 <= nlsx || ls > mls) {
+            for (int a = 0; a < 6; a++) x1[a] = xn[a];
+            break;
+          }
+          alpha = red * alpha;
+          ls++;
+        }
+        iter++;
+        bool nan = false;
+        for (int a = 0; a < 6; a++) nan |= std::isnan(x1[a]);
+        if (iter > p->miter || nan) return false;
+      }
+      for (int i = 0; i < 6; i++) x[i] = x1[i];
+      for (int i = 0; i < MRR_NH; i++) x[6 + i] = x2[i];
+    }
+    // update (:3162-3293)
+    int iter = 0;
+    double R[6 + MRR_NH];
+    formR(cu, x, R);
+    double dotR = 0;
+    for (int a = 0; a < L; a++) dotR += R[a] * R[a];
+    double nR = std::sqrt(dotR), inR = nR;
+    if (inR == 0.0) inR = inR1;
+    while ((nR > p->atol && nR / inR > p->rtol) || iter < mmin) {
+      formJ(cu, x, Jl);
+      haveJ = true;
+      double mJ[L * L], dx[L];
+      for (int a = 0; a < L * L; a++) mJ[a] = -Jl[a];
+      for (int a = 0; a < L; a++) dx[a] = R[a];
+      lu_solve(L, mJ, 1, dx);
+      double alpha = 1.0;
+      dotR = 0;
+      for (int a = 0; a < L; a++) dotR += R[a] * R[a];
+      double ls1 = 0.5 * dotR, ls2 = 0;
+      for (int a = 0; a < L; a++) {
+        double w = 0.0;
+        for (int b = 0; b < L; b++) w += Jl[L * b + a] * R[b];
+        ls2 += dx[a] * w;
+      }
+      ls2 = c * ls2;
+      int ls = 0;
+      for (;;) {
+        double nlsx = ls1 + ls2 * alpha;
+        double xn[L];
+        for (int a = 0; a < L; a++) xn[a] = x[a] + alpha * dx[a];
+        formR(cu, xn, R);
+        dotR = 0;
+        for (int a = 0; a < L; a++) dotR += R[a] * R[a];
+        nR = std::sqrt(dotR);
+        if (0.5 * dotR <= nlsx || ls > mls) {
+          for (int a = 0; a < L; a++) x[a] = xn[a];
+          break;
+        }
+        alpha = red * alpha;
+        ls++;
+      }
+      iter++;
+      bool nan = false;
+      for (int a = 0; a < L; a++) nan |= std::isnan(x[a]);
+      if (iter > p->miter || nan) { iters += iter; return false; }
+    }
+    iters += iter;
+    for (int i = 0; i < 6; i++) stress[i] = x[i];
+    for (int i = 0; i < MRR_NH; i++) tt[i] = x[6 + i];
+    return true;
+  }
+
+  // mm10_solve_strup + mm10_solve_crystal (src/mm10_a.f:2628-2845, 1080-1157)
+  bool update(const double D[6], double dt, const M3 R, bool iter0, State& out,
+              double cep[6][6], int* local_iters) const {
+    const int L = 6 + MRR_NH;
+    Np1 np1;
+    setup(np1, D, dt, R, TEMP);
+    double stress[6], ostress[6], tt[MRR_NH], ott[MRR_NH], rate[MRR_NH];
+    for (int i = 0; i < 6; i++) stress[i] = ostress[i] = n->sig[i];
+    for (int i = 0; i < MRR_NH; i++) { tt[i] = ott[i] = n->rho[i]; rate[i] = 0.0; }
+    double temp1 = 0, temp2 = 0;
+    for (int i = 0; i < 6; i++) { temp1 += D[i] * D[i]; temp2 += stress[i] * stress[i]; }
+    const bool no_load = temp2 == 0.0 && temp1 == 0.0;
+    double Jl[L * L];
+    bool haveJ = false;
+    int iters = 0;
+    bool ok = true;
+    if (iter0 || no_load) {  // mm10_solve_strup_a (:2721-2743)
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) cep[a][b] = vp->C[a][b];
+      if (!no_load) {
+        double R1[6];
+        formR1(np1, stress, tt, R1);
+        for (int a = 0; a < 6; a++) stress[a] = stress[a] - R1[a];
+      }
+    } else {  // mm10_solve_strup_iterate (:2747-2843)
+      double frac = 0.0, step = 1.0;
+      int cuts = 0;
+      Np1 curr;
+      bool fail = false;
+      while (frac < 1.0) {
+        double Dw[6];
+        for (int i = 0; i < 6; i++) Dw[i] = np1.D[i] * (step + frac);
+        setup(curr, Dw, np1.tinc * (step + frac), R, TEMP * (step + frac));
+        for (int i = 0; i < MRR_NH; i++) tt[i] = n->rho[i];
+        fail = !solve(curr, np1.tinc * step, stress, tt, Jl, haveJ, iters);
+        if (fail) {
+          for (int i = 0; i < 6; i++) stress[i] = ostress[i];
+          for (int i = 0; i < MRR_NH; i++) tt[i] = ott[i];
+          step = step * 0.5;
+          if (++cuts > 4) break;
+          fail = false;
+        } else {
+          for (int i = 0; i < 6; i++) ostress[i] = stress[i];
+          for (int i = 0; i < MRR_NH; i++) ott[i] = tt[i];
+          frac = frac + step;
+          for (int i = 0; i < MRR_NH; i++) rate[i] = curr.rho_rate[i];
+        }
+      }
+      bool nan = false;
+      for (int i = 0; i < 6; i++) nan |= std::isnan(stress[i]);
+      for (int i = 0; i < MRR_NH; i++) nan |= std::isnan(tt[i]);
+      if (fail || nan) ok = false;
+    }
+    if (local_iters) *local_iters = iters;
+    for (int i = 0; i < 6; i++) out.D[i] = D[i];
+    out.tt = 0.0;
+    out.tt_rate = 0.0;
+    out.u[0] = out.u[1] = 0.0;
+    if (!ok) {  // keep sigma_n / rho_n and the elastic tangent (see Mm10::update)
+      for (int i = 0; i < 6; i++) out.sig[i] = n->sig[i];
+      for (int i = 0; i < MRR_NH; i++) { out.rho[i] = n->rho[i]; out.rho_rate[i] = 0.0; }
+      std::memcpy(out.Rp, n->Rp, sizeof(M3));
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) cep[a][b] = vp->C[a][b];
+      return false;
+    }
+    for (int i = 0; i < 6; i++) out.sig[i] = stress[i];
+    for (int i = 0; i < MRR_NH; i++) { out.rho[i] = tt[i]; out.rho_rate[i] = rate[i]; }
+    if (iter0 || no_load) {
+      std::memset(out.Rp, 0, sizeof(M3));
+      return true;
+    }
+    // mm10_tangent (:658-815): T = (J11 - J12 J22^-1 J21)^-1 C (ed = dgammadd = 0)
+    {
+      double A22[MRR_NH * MRR_NH], B[MRR_NH * 6];
+      for (int a = 0; a < MRR_NH; a++) {
+        for (int c = 0; c < MRR_NH; c++) A22[MRR_NH * a + c] = Jl[L * (6 + a) + 6 + c];
+        for (int c = 0; c < 6; c++) B[6 * a + c] = Jl[L * (6 + a) + c];
+      }
+      lu_solve(MRR_NH, A22, 6, B);  // beta = J22^-1 J21
+      double JJ[36], JR[36];
+      for (int a = 0; a < 6; a++)
+        for (int c = 0; c < 6; c++) {
+          double s = Jl[L * a + c];
+          for (int q = 0; q < MRR_NH; q++) s -= Jl[L * a + 6 + q] * B[6 * q + c];
+          JJ[6 * a + c] = s;
+          JR[6 * a + c] = vp->C[a][c];
+        }
+      lu_solve(6, JJ, 6, JR);
+      for (int a = 0; a < 6; a++)
+        for (int b = 0; b < 6; b++) cep[a][b] = (JR[a * 6 + b] + JR[b * 6 + a]) * 0.5;
+    }
+    // mm10_update_rotation (:3310-3327): wbarp of the full step's slips at the solution
+    {
+      double wb[3] = {0, 0, 0};
+      for (int i = 0; i < vp->ns; i++) {
+        Sys y;
+        sys(np1, out.sig, out.rho, i, y);
+        for (int a = 0; a < 3; a++) wb[a] = wb[a] + y.slip * np1.qs[i][a];
+      }
+      M3 W = {{0.0, wb[2], wb[1]}, {-wb[2], 0.0, wb[0]}, {-wb[1], -wb[0], 0.0}};
+      M3 ex;
+      double al = std::sqrt(W[1][2] * W[1][2] + W[0][2] * W[0][2] + W[0][1] * W[0][1]);
+      if (al < 1.0e-16) {
+        std::memset(ex, 0, sizeof(ex));
+      } else {
+        M3 WW;
+        mm33(W, W, WW);
+        double ca = (1.0 - std::cos(al)) / (al * al), sa = std::sin(al) / al;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++) ex[i][j] = ca * WW[i][j] + sa * W[i][j];
+      }
+      for (int i = 0; i < 3; i++) ex[i][i] += 1.0;
+      mm33(ex, n->Rp, out.Rp);
+    }
+    return true;
+  }
+};
+
 // ---- cep2A (src/cep2A.f:86-284) ------------------------------------------------------
 inline int I4(int i, int j, int k, int l) { return i * 27 + j * 9 + k * 3 + l; }
 void cep2A(const M3 Fn, const M3 t, const double C[6][6], const M3 Rh, const M3 fnhinv,
@@ -1165,9 +1715,16 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
     mts_thresholds(cr.p, dg / dt, TEMP, mu, tv, ty);
     n.tt = cr.p.tau_a + (mu / cr.p.mu_0) * ty + 0.1;
   }
-  Mm10 mm{&cr.p, &vp, &n};
   int it = 0;
-  o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);
+  if (cr.p.h_type == 7) {
+    Mrr mm{&cr.p, &vp, &n, cr.Gm, cr.Hm};
+    o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);
+    np1.mrr = true;
+  } else {
+    Mm10 mm{&cr.p, &vp, &n};
+    o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);
+    np1.mrr = false;
+  }
   np1.m01 = false;
   o.iters = it;
   // strains at n+1 = strains at n + uddt (src/drive_eps_sig.f:264-265)
@@ -1507,6 +2064,7 @@ struct orc_ctx {
   // FFT_nr3 persistent locals (Fortran DATA => SAVE'd, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
   double eq_tol = 0.0;  // equilibrium stop test of the Newton loop (0: the reference's loop)
+  int hist_words = ORC_HIST;  // ORC_HIST_MRR on grids of Ma-Roters-Raabe crystals
 };
 
 static void ghat_apply(const orc_ctx* c, long v, const double* in9, double* out9,
@@ -1541,6 +2099,7 @@ orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
   for (int i = 0; i < ncrystals; i++) {
     if (props[i].slip_type == CPFFT_NOT_A_CRYSTAL) { c->kind[i] = 2; continue; }
     crystal_finalize(props[i], c->crys[i]);
+    if (props[i].h_type == 7) c->hist_words = ORC_HIST_MRR;
   }
   long N3 = c->N3;
   c->mat.resize(N3);
@@ -2010,21 +2569,28 @@ void orc_set_fields(orc_ctx* c, const double* Fn, const double* Fn1) {
   if (Fn) std::copy(Fn, Fn + 9 * c->N3, c->Fn.begin());
   if (Fn1) std::copy(Fn1, Fn1 + 9 * c->N3, c->Fn1.begin());
 }
+int orc_hist_words(orc_ctx* c) { return c->hist_words; }
 void orc_get_history(orc_ctx* c, double* hist_n, double* hist_np1) {
   long N3 = c->N3;
-  double h[ORC_HIST];
+  const int W = c->hist_words;
+  double h[ORC_HIST_MRR];
   for (long v = 0; v < N3; v++) {
-    if (hist_n) { state_pack(c->hn[v], h); for (int w = 0; w < ORC_HIST; w++) hist_n[w * N3 + v] = h[w]; }
-    if (hist_np1) { state_pack(c->hn1[v], h); for (int w = 0; w < ORC_HIST; w++) hist_np1[w * N3 + v] = h[w]; }
+    std::fill(h, h + ORC_HIST_MRR, 0.0);
+    if (hist_n) { state_pack(c->hn[v], h); for (int w = 0; w < W; w++) hist_n[w * N3 + v] = h[w]; }
+    std::fill(h, h + ORC_HIST_MRR, 0.0);
+    if (hist_np1) { state_pack(c->hn1[v], h); for (int w = 0; w < W; w++) hist_np1[w * N3 + v] = h[w]; }
   }
 }
 void orc_set_history_n(orc_ctx* c, const double* hist_n) {
   long N3 = c->N3;
-  double h[ORC_HIST];
+  const int W = c->hist_words;
+  double h[ORC_HIST_MRR];
   for (long v = 0; v < N3; v++) {
-    for (int w = 0; w < ORC_HIST; w++) h[w] = hist_n[w * N3 + v];
+    for (int w = 0; w < W; w++) h[w] = hist_n[w * N3 + v];
     std::memset(&c->hn[v], 0, sizeof(State));
-    c->hn[v].m01 = c->kind[c->mat[v]] == 1;
+    const int m = c->mat[v];
+    c->hn[v].m01 = c->kind[m] == 1;
+    c->hn[v].mrr = c->kind[m] == 0 && c->crys[m].p.h_type == 7;
     state_unpack(h, c->hn[v]);
   }
 }
@@ -2040,6 +2606,7 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3], doub
   State n, np1;
   std::memset(&n, 0, sizeof(n));
   std::memset(&np1, 0, sizeof(np1));
+  n.mrr = props->h_type == 7;
   if (hist_n) state_unpack(hist_n, n);
   else state_init(cr, n);
   M3 fn, fn1;
@@ -2074,6 +2641,28 @@ int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9], con
   if (A) for (int i = 0; i < 81; i++) A[i] = o.A[i];
   if (out_sig6) for (int i = 0; i < 6; i++) out_sig6[i] = o.sig[i];
   if (out_cep36) for (int a = 0; a < 6; a++) for (int b = 0; b < 6; b++) out_cep36[a * 6 + b] = o.cep[a][b];
+  return 0;
+}
+
+int orc_mrr_residual(const cpfft_crystal* props, const double kocks_deg[3], const double D[6],
+                     double tinc, const double* hist_n, const double x[18], double R[18],
+                     double J[324]) {
+  if (props->h_type != 7) return -1;
+  Crys cr;
+  crystal_finalize(*props, cr);
+  VoxProps vp;
+  voxel_props(cr, kocks_deg, vp);
+  State n;
+  std::memset(&n, 0, sizeof(n));
+  n.mrr = true;
+  if (hist_n) state_unpack(hist_n, n);
+  else state_init(cr, n);
+  Mrr mm{&cr.p, &vp, &n, cr.Gm, cr.Hm};
+  Np1 s;
+  M3 I = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  mm.setup(s, D, tinc, I, TEMP);
+  if (R) mm.formR(s, x, R);
+  if (J) mm.formJ(s, x, J);
   return 0;
 }
 

@@ -17,8 +17,10 @@ extern "C" {
 
 typedef struct orc_ctx orc_ctx;
 
-/* Per-voxel compact state, same words and order as CPFFT_HIST_WORDS. */
+/* Per-voxel compact state, same words and order as CPFFT_HIST_WORDS; grids of
+ * Ma-Roters-Raabe crystals (h_type 7) carry ORC_HIST_MRR words (CPFFT_HIST_WORDS_MRR). */
 #define ORC_HIST 31
+#define ORC_HIST_MRR 55
 
 orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
                     const cpfft_crystal* props, int ncrystals, double tstep,
@@ -66,12 +68,14 @@ int  orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC,
 void orc_get_fields(orc_ctx* c, double* Fn, double* Fn1, double* Pn, double* Pn1,
                     double* K4);
 void orc_set_fields(orc_ctx* c, const double* Fn, const double* Fn1);
+int  orc_hist_words(orc_ctx* c);   /* ORC_HIST or ORC_HIST_MRR */
 void orc_get_history(orc_ctx* c, double* hist_n, double* hist_np1);
 void orc_set_history_n(orc_ctx* c, const double* hist_n);
 
 /* ---- single-voxel entry points used by the unit tests ---------------------------- */
 /* Full material-point update of one voxel (kinematics + mm10 + cep2A).
- * hist_n (ORC_HIST) is read unless step == 1 (then initialised); hist_np1 written.
+ * hist_n (ORC_HIST words, ORC_HIST_MRR for h_type 7) is read unless step == 1 (then
+ * initialised); hist_np1 written.
  * out_sig6 = unrotated Cauchy stress, out_cep36 = 6x6 tangent (row-major).
  * Returns local Newton iterations (update phase), or -1 on failure. */
 int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3],
@@ -84,6 +88,12 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3],
 int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9],
                      const double Fn1[9], const double* hist_n, double* hist_np1,
                      double P[9], double A[81], double out_sig6[6], double out_cep36[36]);
+/* Ma-Roters-Raabe local residual R (18) and Jacobian J (18 x 18, row-major) at
+ * x = (sigma 6, densities 12) for the strain increment D over tinc at 297 K, the current
+ * rotation the identity; hist_n NULL: the initial state.  Returns -1 unless h_type 7. */
+int orc_mrr_residual(const cpfft_crystal* props, const double kocks_deg[3], const double D[6],
+                     double tinc, const double* hist_n, const double x[18], double R[18],
+                     double J[324]);
 /* polar decomposition F = R U (rtcmp1), F and R row-major 3x3 */
 void orc_polar(const double F[9], double R[9]);
 /* crystal stiffness in the sample frame (row-major 6x6) and slip tensors (12x6) */

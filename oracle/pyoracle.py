@@ -13,6 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_oracle.so")
 HIST_WORDS = 31
+HIST_WORDS_MRR = 55  # grids of Ma-Roters-Raabe crystals (h_type 7)
 
 _lib = None
 
@@ -45,6 +46,8 @@ class Crystal(ctypes.Structure):
         ("eps_dot_0_v", ctypes.c_double),
         ("burgers", ctypes.c_double), ("boltzman", ctypes.c_double),
         ("mu_0", ctypes.c_double), ("D_0", ctypes.c_double), ("T_0", ctypes.c_double),
+        ("u1", ctypes.c_double), ("u2", ctypes.c_double), ("u3", ctypes.c_double),
+        ("u4", ctypes.c_double), ("u5", ctypes.c_double), ("u6", ctypes.c_double),
     ]
 
 
@@ -118,6 +121,8 @@ def lib():
         L.orc_get_fields.argtypes = [vp, dp, dp, dp, dp, dp]
         L.orc_set_fields.argtypes = [vp, dp, dp]
         L.orc_get_history.argtypes = [vp, dp, dp]
+        L.orc_hist_words.restype = i
+        L.orc_hist_words.argtypes = [vp]
         L.orc_set_history_n.argtypes = [vp, dp]
         L.orc_voxel_update.restype = i
         L.orc_voxel_update.argtypes = [P(Crystal), dp, d, i, i, dp, dp, dp, dp, dp, dp,
@@ -128,6 +133,8 @@ def lib():
         L.orc_mises_update.restype = i
         L.orc_mises_update.argtypes = [P(Mises), i, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_polar.argtypes = [dp, dp]
+        L.orc_mrr_residual.restype = i
+        L.orc_mrr_residual.argtypes = [P(Crystal), dp, dp, d, dp, dp, dp, dp]
         L.orc_crystal_setup.argtypes = [P(Crystal), dp, dp, dp, dp]
         L.orc_fft3.argtypes = [i, dp, dp, i]
         _lib = L
@@ -230,8 +237,9 @@ class Oracle:
         lib().orc_set_fields(self.h, _p(Fn), _p(Fn1))
 
     def history(self):
-        hn = np.zeros((HIST_WORDS, self.N3))
-        hn1 = np.zeros((HIST_WORDS, self.N3))
+        W = lib().orc_hist_words(self.h)
+        hn = np.zeros((W, self.N3))
+        hn1 = np.zeros((W, self.N3))
         lib().orc_get_history(self.h, _p(hn), _p(hn1))
         return hn, hn1
 
@@ -280,7 +288,7 @@ def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
     A = np.zeros(81)
     sig = np.zeros(6)
     cep = np.zeros(36)
-    h1 = np.zeros(HIST_WORDS)
+    h1 = np.zeros(HIST_WORDS_MRR if crystal["h_type"] == 7 else HIST_WORDS)
     k = np.ascontiguousarray(kocks, dtype=np.float64)
     fn = np.ascontiguousarray(Fn, dtype=np.float64).reshape(9)
     fn1 = np.ascontiguousarray(Fn1, dtype=np.float64).reshape(9)
@@ -289,6 +297,20 @@ def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
                                  _p(h1), _p(P), _p(A), _p(sig), _p(cep))
     return dict(P=P, A=A.reshape(9, 9), sig=sig, cep=cep.reshape(6, 6), hist=h1,
                 iters=its)
+
+
+def mrr_residual(crystal, kocks, D, tinc, x, hist_n=None):
+    """Ma-Roters-Raabe local residual (18) and Jacobian (18 x 18) at x = (sigma, rho)."""
+    c = crystal_array([crystal])
+    R = np.zeros(18)
+    J = np.zeros(324)
+    hn = None if hist_n is None else np.ascontiguousarray(hist_n, dtype=np.float64)
+    rc = lib().orc_mrr_residual(c, _p(np.ascontiguousarray(kocks, dtype=np.float64)),
+                                _p(np.ascontiguousarray(D, dtype=np.float64)), float(tinc),
+                                _p(hn), _p(np.ascontiguousarray(x, dtype=np.float64)), _p(R),
+                                _p(J))
+    assert rc == 0
+    return R, J.reshape(18, 18)
 
 
 def polar(F):

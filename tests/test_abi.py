@@ -114,7 +114,8 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
                "cpfft_stats": [cpfft_gb300.Stats, pyoracle.Stats],
                "cpfft_rve": [cpfft_gb300.Rve]}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cpfft_gpu.h"',
-             'int main(void) {', 'printf("HIST %d\\n", CPFFT_HIST_WORDS);']
+             'int main(void) {', 'printf("HIST %d\\n", CPFFT_HIST_WORDS);',
+             'printf("HISTMRR %d\\n", CPFFT_HIST_WORDS_MRR);']
     for name, ms in mirrors.items():
         lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (name, name))
         for f, _ in ms[0]._fields_:
@@ -134,6 +135,7 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
         elif len(parts) == 3:
             got[(parts[0], parts[1])] = int(parts[2])
     assert got["HIST"] == cpfft_gb300.HIST_WORDS == pyoracle.HIST_WORDS
+    assert got["HISTMRR"] == cpfft_gb300.HIST_WORDS_MRR == pyoracle.HIST_WORDS_MRR
     for name, ms in mirrors.items():
         for m in ms:
             assert ctypes.sizeof(m) == got[(name, "size")], (name, m)
