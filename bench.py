@@ -221,6 +221,8 @@ def make_solver(cp, r, form, args):
         if form != "fp64" and args.inexact > 0:
             s.set_inexact_newton(args.inexact)
             s.set_tangent_tol(args.tangent_tol)
+            if args.coupled_bc:
+                s.set_coupled_bc(True)
     return s
 
 
@@ -789,6 +791,9 @@ def main():
     ap.add_argument("--inexact", type=float, default=1e-2)
     ap.add_argument("--tangent-tol", type=float, default=1e-3,
                     help="relative tolerance of tangent_homo's solves in the fast form")
+    ap.add_argument("--coupled-bc", action="store_true",
+                    help="update the prescribed-stress components of F_bar inside the Newton "
+                         "iteration (fast form)")
     ap.add_argument("--curve", default=None,
                     help="write P_bar of every load step of both forms to this JSON file")
     ap.add_argument("--fp64-steps", type=int, default=5,

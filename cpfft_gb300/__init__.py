@@ -127,6 +127,7 @@ SIGNATURES = {
     "cpfft_set_equilibrium_tol": (_I, [_D]),
     "cpfft_set_inexact_newton": (_I, [_D]),
     "cpfft_set_tangent_tol": (_I, [_D]),
+    "cpfft_set_coupled_bc": (_I, [_I]),
     "cpfft_set_mises": (_I, [_I, ctypes.POINTER(Mises)]),
     "cpfft_set_schedule": (_I, [_I]),
     "cpfft_tuning": (_I, [_IP, _DP]),
@@ -335,6 +336,11 @@ class Solver:
         """Solve each Newton system of nr3_step only as far as the equilibrium residual
         needs (Eisenstat-Walker forcing, at most eta_max; needs set_equilibrium_tol)."""
         _check(load_library().cpfft_set_inexact_newton(float(eta_max)), "cpfft_set_inexact_newton")
+
+    def set_coupled_bc(self, on=True):
+        """Update the prescribed-stress components of F_bar inside the Newton iteration
+        (needs set_equilibrium_tol and set_inexact_newton)."""
+        _check(load_library().cpfft_set_coupled_bc(int(bool(on))), "cpfft_set_coupled_bc")
 
     def set_tangent_tol(self, tol):
         """Relative tolerance of tangent_homo's solves under inexact Newton (default 1e-3)."""

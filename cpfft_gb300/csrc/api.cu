@@ -391,6 +391,8 @@ struct Ctx {
   double eta_max = 0.0;
   // relative tolerance of tangent_homo's solves under inexact Newton (cpfft_set_tangent_tol)
   double th_tol = 1.0e-3;
+  // the P_bar update inside the Newton iteration (cpfft_set_coupled_bc)
+  bool coupled_bc = false;
   bool cg_rel_only = false;  // the current solve stops on ||r|| <= tol ||b|| alone
   // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
   // starts dropped, sub-stepped solves (cpfft_pass_counts)
@@ -1662,6 +1664,12 @@ int cpfft_set_inexact_newton(double eta_max) {
   return 0;
 }
 
+int cpfft_set_coupled_bc(int on) {
+  TRY(need_ctx());
+  g_ctx->coupled_bc = on != 0;
+  return 0;
+}
+
 int cpfft_set_tangent_tol(double tol) {
   TRY(need_ctx());
   if (!(tol > 0.0 && tol < 1.0)) {
@@ -1942,6 +1950,105 @@ int cpfft_nr3_begin(double tolPCG) {
   return 0;
 }
 
+// One load step with the mixed boundary conditions inside the Newton iteration
+// (cpfft_set_coupled_bc; needs the equilibrium test and inexact Newton).  FFT_nr3 nests
+// a Newton loop at fixed macroscopic F inside a loop over P_bar updates
+// (src/FFT_nr3.f:75-171), and each P_bar pass starts again with an explicit stress pass.
+// Here each Newton iteration updates the prescribed-stress components of F_bar as well:
+// after the stress pass, DbarF solves C_homo DbarF = PBC - P_bar on those components
+// (NBC_update, src/FFT_nr3.f:375-433), and the fluctuation solves
+// G(K : dF) = -G(P) - G(K : DbarF), so that F_bar and the fluctuation take one
+// Newton step on the coupled system (C_homo is that system's Schur complement).  C_homo
+// is recomputed after the first two implicit stress passes.  The step ends when P_bar
+// meets tolNR, the equilibrium residual eq_tol and the last increment tolNR, the same
+// tests as the nested loops' last pass.  On entry barF holds F_bar with the step's
+// predicted DbarF applied and Fn1 the predictor's field.
+int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* barF,
+                 double Fnorm, double tolNR, double tolPCG, int maxIter, cpfft_stats& S,
+                 double& tp, double& ts) {
+  using clk = std::chrono::steady_clock;
+  auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+  const long long N3 = c->N3, n = 9 * N3;
+  double resfft = 1.0, eta = c->eta_max, eq_last = HUGE_VAL;
+  int tangents = 0;
+  for (int k = 0;; k++) {
+    auto a = clk::now();
+    long long li, pi = 0, rj = 0;
+    int fails;
+    TRY(stress(c, step, k, &li, &fails, &pi, &rj));
+    ts += sec(a);
+    S.predict_iters += pi;
+    S.guess_rejected += rj;
+    S.local_iters += li;
+    S.local_fallbacks += fails;
+    S.stress_updates++;
+    TRY(matvec_acc(c, c->P, c->b, 0));
+    double e;
+    TRY(equil_residual(c, c->b, &e));  // also leaves sum(P) in h_sc
+    S.res_equil = e;
+    double res1 = 0, res2 = 0;
+    for (int i = 0; i < 9; i++) {
+      c->P_bar[i] = c->h_sc[SC_SUM9 + i] / (double)N3;
+      res2 += c->P_bar[i] * c->P_bar[i];
+      if (isNBC[i]) res1 += (c->P_bar[i] - PBC[i]) * (c->P_bar[i] - PBC[i]);
+    }
+    const double res3 = res2 < 1.0e-8 ? std::sqrt(res1) : std::sqrt(res1 / res2);
+    S.res_pbar = res3;
+    if (c->log)
+      fprintf(stderr, "       coupled iteration %d: equilibrium %10.3e  P_bar %10.3e\n", k, e, res3);
+    if (res3 <= tolNR && e <= c->eq_tol && resfft <= tolNR) break;
+    if (k == maxIter) {
+      cpfft_set_error("coupled Newton loop does not converge (step %d)", step);
+      return CPFFT_ERR_NEWTON_MAXIT;
+    }
+    // the Schur complement at the first two implicit states
+    if (k >= 1 && tangents < 2) {
+      a = clk::now();
+      int th;
+      TRY(tangent_homo(c, std::max(tolPCG, c->th_tol), c->C_homo, &th));
+      tp += sec(a);
+      tangents++;
+    }
+    double DbarF[9];
+    for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
+    TRY(nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC));
+    // right-hand side -G(P) - G(K : DbarF)
+    CK(dev_fill9(c->dFm, N3, DbarF, c->st));
+    CK(dev_scale(c->b, -1.0, n, c->st));
+    TRY(matvec_acc(c, c->dFm, c->w, 1));
+    CK(dev_axpy(c->b, c->w, -1.0, n, c->st));
+    CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));  // F_bar += DbarF
+    for (int i = 0; i < 9; i++) barF[i] += DbarF[i];
+    // Eisenstat-Walker forcing as in the nested loops
+    double eta_k = eq_last < HUGE_VAL ? 0.9 * (e / eq_last) * (e / eq_last) : c->eta_max;
+    const double sg = 0.9 * eta * eta;
+    if (sg > 0.1) eta_k = std::max(eta_k, sg);
+    eta_k = std::max(eta_k, 0.5 * c->eq_tol / e);
+    eta = std::min(c->eta_max, eta_k);
+    eq_last = e;
+    a = clk::now();
+    int its;
+    c->cg_rel_only = true;
+    TRY(cg(c, c->b, c->dFm, std::max(tolPCG, eta), &its));
+    c->cg_rel_only = false;
+    tp += sec(a);
+    CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
+    double dn;
+    TRY(dnrm2(c, c->dFm, &dn));
+    double db = 0;
+    for (int i = 0; i < 9; i++) db += DbarF[i] * DbarF[i];
+    resfft = std::sqrt(dn * dn + (double)N3 * db) / Fnorm;
+    if (!std::isfinite(resfft)) { cpfft_set_error("Newton residual is not finite"); return CPFFT_ERR_NONFINITE; }
+    S.newton_iters++;
+    S.res_fft = resfft;
+    if (c->log)
+      fprintf(stderr, "       Iteration %5d  residual %10.3e  (cg %d, local fallbacks %d)\n", k,
+              resfft, its, fails);
+  }
+  S.nbc_iters = 1;
+  return 0;
+}
+
 int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, double tolPCG,
                    int maxIter, double* Pbar, cpfft_stats* st) {
   TRY(need_ctx());
@@ -1990,6 +2097,10 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     c->cg_rel_only = false;
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
+    if (inexact && existNBC && c->coupled_bc) {
+      TRY(coupled_step(c, step, PBC, isNBC, barF, Fnorm, tolNR, tolPCG, maxIter, S, tp, ts));
+      break;
+    }
     double resfft = 1.0;
     double eta = c->eta_max, eq_last = HUGE_VAL;
     int iiter_EBC = 0;

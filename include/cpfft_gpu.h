@@ -367,6 +367,19 @@ int cpfft_set_inexact_newton(double eta_max);
 int cpfft_set_tangent_tol(double tol);
 
 /*
+ * The P_bar update inside the Newton iteration (extension; on != 0; needs the equilibrium
+ * test and inexact Newton, and prescribed-stress components).  The reference nests a
+ * Newton loop at fixed macroscopic F inside a loop of P_bar updates, each pass opening
+ * with an explicit stress pass (src/FFT_nr3.f:75-171).  Here every Newton iteration also
+ * updates the prescribed-stress components of F_bar with NBC_update's system and solves
+ * the fluctuation for both changes, one Newton step on the coupled system (C_homo, its
+ * Schur complement, recomputed after the first two implicit stress passes).  The step ends
+ * on the nested loops' final tests: P_bar within tolNR, the equilibrium residual within
+ * its tolerance, the last increment within tolNR.  Default off.
+ */
+int cpfft_set_coupled_bc(int on);
+
+/*
  * Start of FFT_nr3 (src/FFT_nr3.f:36-47): the initial drive_eps_sig(1,0) of the
  * `compute` command (src/FFT_finite_3d.f:145) and the first tangent_homo.
  */

@@ -2644,6 +2644,22 @@ int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9], con
   return 0;
 }
 
+void orc_mrr_interaction(double G[144], double H[144]) {
+  cpfft_crystal p;
+  std::memset(&p, 0, sizeof(p));
+  p.slip_type = 1;
+  p.elastic_type = 1;
+  p.e = 1.0;
+  p.nu = 0.3;
+  Crys cr;
+  crystal_finalize(p, cr);
+  for (int a = 0; a < 12; a++)
+    for (int q = 0; q < 12; q++) {
+      G[12 * a + q] = cr.Gm[a][q];
+      H[12 * a + q] = cr.Hm[a][q];
+    }
+}
+
 int orc_mrr_residual(const cpfft_crystal* props, const double kocks_deg[3], const double D[6],
                      double tinc, const double* hist_n, const double x[18], double R[18],
                      double J[324]) {

@@ -133,6 +133,7 @@ def lib():
         L.orc_mises_update.restype = i
         L.orc_mises_update.argtypes = [P(Mises), i, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_polar.argtypes = [dp, dp]
+        L.orc_mrr_interaction.argtypes = [dp, dp]
         L.orc_mrr_residual.restype = i
         L.orc_mrr_residual.argtypes = [P(Crystal), dp, dp, d, dp, dp, dp, dp]
         L.orc_crystal_setup.argtypes = [P(Crystal), dp, dp, dp, dp]
@@ -297,6 +298,14 @@ def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
                                  _p(h1), _p(P), _p(A), _p(sig), _p(cep))
     return dict(P=P, A=A.reshape(9, 9), sig=sig, cep=cep.reshape(6, 6), hist=h1,
                 iters=its)
+
+
+def mrr_interaction():
+    """The Ma-Roters-Raabe forest and parallel interaction matrices (12 x 12 each)."""
+    G = np.zeros(144)
+    H = np.zeros(144)
+    lib().orc_mrr_interaction(_p(G), _p(H))
+    return G.reshape(12, 12), H.reshape(12, 12)
 
 
 def mrr_residual(crystal, kocks, D, tinc, x, hist_n=None):
