@@ -19,8 +19,10 @@ e2e    = the same units over host wall time of each step plus copying the step's
 Inputs larger than L2: every field is >= 150 MB (9 x 128^3 FP64), K4 is 1.4 GB.
 
 Forms (--mode): mixed (default) = FP32 Krylov inner iterations (reference-medium
-preconditioned) under FP64-accurate outer residuals, local solves started at the previous
-global iterate or the return-mapped elastic trial, FP32 consistent tangent; learned = the
+preconditioned) under FP64-accurate outer residuals, inexact Newton, the P_bar update
+inside the Newton iteration (--nested-bc: the reference's nested loop), local solves
+started at the previous global iterate or the return-mapped elastic trial, FP32
+consistent tangent; learned = the
 same with the learned initial guess in place of the trial start (its network trained
 before the timed steps on pairs logged from 64^3 RVEs of other seeds); fp64 = the plain
 form.  Unless --no-fp64, the plain FP64 form then runs the same warm-up and the first
@@ -218,9 +220,10 @@ def make_solver(cp, r, form, args):
             s.set_precond(cp.PRECOND_REFERENCE)
     if args.tol_equil > 0:
         s.set_equilibrium_tol(args.tol_equil)
-        if form != "fp64" and args.inexact > 0:
-            s.set_inexact_newton(args.inexact)
-            s.set_tangent_tol(args.tangent_tol)
+        if form != "fp64":
+            if args.inexact > 0:
+                s.set_inexact_newton(args.inexact)
+                s.set_tangent_tol(args.tangent_tol)
             if args.coupled_bc:
                 s.set_coupled_bc(True)
     return s
@@ -554,6 +557,9 @@ def config_dict(args, impl):
                            "inexact_newton_eta_max": (args.inexact if inexact else 0.0),
                            "tangent_homo": (max(args.tangent_tol, 1e-10) if inexact
                                             else 1e-10)},
+            "p_bar_update": ("inside the Newton iteration (coupled)"
+                             if fast and args.mode != "fp64" and args.coupled_bc
+                             and args.tol_equil > 0 else "nested loop (the reference's)"),
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
             "stress_schedule": args.schedule if fast else "blocks",
             "tangent": args.tangent if fast else "f64",
@@ -791,9 +797,9 @@ def main():
     ap.add_argument("--inexact", type=float, default=1e-2)
     ap.add_argument("--tangent-tol", type=float, default=1e-3,
                     help="relative tolerance of tangent_homo's solves in the fast form")
-    ap.add_argument("--coupled-bc", action="store_true",
-                    help="update the prescribed-stress components of F_bar inside the Newton "
-                         "iteration (fast form)")
+    ap.add_argument("--nested-bc", dest="coupled_bc", action="store_false",
+                    help="fast form: the reference's nested P_bar loop instead of the P_bar "
+                         "update inside the Newton iteration")
     ap.add_argument("--curve", default=None,
                     help="write P_bar of every load step of both forms to this JSON file")
     ap.add_argument("--fp64-steps", type=int, default=5,

@@ -339,7 +339,7 @@ class Solver:
 
     def set_coupled_bc(self, on=True):
         """Update the prescribed-stress components of F_bar inside the Newton iteration
-        (needs set_equilibrium_tol and set_inexact_newton)."""
+        (with set_equilibrium_tol)."""
         _check(load_library().cpfft_set_coupled_bc(int(bool(on))), "cpfft_set_coupled_bc")
 
     def set_tangent_tol(self, tol):

@@ -1951,7 +1951,7 @@ int cpfft_nr3_begin(double tolPCG) {
 }
 
 // One load step with the mixed boundary conditions inside the Newton iteration
-// (cpfft_set_coupled_bc; needs the equilibrium test and inexact Newton).  FFT_nr3 nests
+// (cpfft_set_coupled_bc; needs the equilibrium test).  FFT_nr3 nests
 // a Newton loop at fixed macroscopic F inside a loop over P_bar updates
 // (src/FFT_nr3.f:75-171), and each P_bar pass starts again with an explicit stress pass.
 // Here each Newton iteration updates the prescribed-stress components of F_bar as well:
@@ -1959,7 +1959,8 @@ int cpfft_nr3_begin(double tolPCG) {
 // (NBC_update, src/FFT_nr3.f:375-433), and the fluctuation solves
 // G(K : dF) = -G(P) - G(K : DbarF), so that F_bar and the fluctuation take one
 // Newton step on the coupled system (C_homo is that system's Schur complement).  C_homo
-// is recomputed after the first two implicit stress passes.  The step ends when P_bar
+// is recomputed after the first two implicit stress passes; increments that raise the
+// equilibrium residual are halved as in the nested loops.  The step ends when P_bar
 // meets tolNR, the equilibrium residual eq_tol and the last increment tolNR, the same
 // tests as the nested loops' last pass.  On entry barF holds F_bar with the step's
 // predicted DbarF applied and Fn1 the predictor's field.
@@ -1969,8 +1970,13 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
   using clk = std::chrono::steady_clock;
   auto sec = [](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
   const long long N3 = c->N3, n = 9 * N3;
+  const bool inexact = c->eta_max > 0.0;
   double resfft = 1.0, eta = c->eta_max, eq_last = HUGE_VAL;
   int tangents = 0;
+  // backtracking as in the nested loops: an increment after which the equilibrium
+  // residual has grown is halved, at most 4 times in a row (lastD: its F_bar part)
+  double eq_prev = HUGE_VAL, frac = 1.0, lastD[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int halvings = 0;
   for (int k = 0;; k++) {
     auto a = clk::now();
     long long li, pi = 0, rj = 0;
@@ -2001,13 +2007,33 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
       cpfft_set_error("coupled Newton loop does not converge (step %d)", step);
       return CPFFT_ERR_NEWTON_MAXIT;
     }
-    // the Schur complement at the first two implicit states
+    if (k >= 2 && e > eq_prev && halvings < 4) {
+      frac *= 0.5;
+      double h[9];
+      for (int i = 0; i < 9; i++) {
+        h[i] = -frac * lastD[i];
+        barF[i] += h[i];
+      }
+      CK(dev_axpy(c->Fn1, c->dFm, -frac, n, c->st));
+      CK(dev_fill9(c->w, N3, h, c->st));
+      CK(dev_axpy(c->Fn1, c->w, 1.0, n, c->st));
+      halvings++;
+      resfft *= 0.5;
+      if (c->log) fprintf(stderr, "       increment halved (%d)\n", halvings);
+      continue;
+    }
+    eq_prev = e;
+    halvings = 0;
+    frac = 1.0;
+    // the Schur complement at the first two implicit states (tangent_homo's solves use
+    // the b buffer: G(P) is formed again after it)
     if (k >= 1 && tangents < 2) {
       a = clk::now();
       int th;
-      TRY(tangent_homo(c, std::max(tolPCG, c->th_tol), c->C_homo, &th));
+      TRY(tangent_homo(c, inexact ? std::max(tolPCG, c->th_tol) : tolPCG, c->C_homo, &th));
       tp += sec(a);
       tangents++;
+      TRY(matvec_acc(c, c->P, c->b, 0));
     }
     double DbarF[9];
     for (int i = 0; i < 9; i++) DbarF[i] = 0.0;
@@ -2018,18 +2044,24 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
     TRY(matvec_acc(c, c->dFm, c->w, 1));
     CK(dev_axpy(c->b, c->w, -1.0, n, c->st));
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));  // F_bar += DbarF
-    for (int i = 0; i < 9; i++) barF[i] += DbarF[i];
-    // Eisenstat-Walker forcing as in the nested loops
-    double eta_k = eq_last < HUGE_VAL ? 0.9 * (e / eq_last) * (e / eq_last) : c->eta_max;
-    const double sg = 0.9 * eta * eta;
-    if (sg > 0.1) eta_k = std::max(eta_k, sg);
-    eta_k = std::max(eta_k, 0.5 * c->eq_tol / e);
-    eta = std::min(c->eta_max, eta_k);
-    eq_last = e;
+    for (int i = 0; i < 9; i++) {
+      barF[i] += DbarF[i];
+      lastD[i] = DbarF[i];
+    }
+    double tol_k = tolPCG;
+    if (inexact) {  // Eisenstat-Walker forcing as in the nested loops
+      double eta_k = eq_last < HUGE_VAL ? 0.9 * (e / eq_last) * (e / eq_last) : c->eta_max;
+      const double sg = 0.9 * eta * eta;
+      if (sg > 0.1) eta_k = std::max(eta_k, sg);
+      eta_k = std::max(eta_k, 0.5 * c->eq_tol / e);
+      eta = std::min(c->eta_max, eta_k);
+      eq_last = e;
+      tol_k = std::max(tolPCG, eta);
+    }
     a = clk::now();
     int its;
-    c->cg_rel_only = true;
-    TRY(cg(c, c->b, c->dFm, std::max(tolPCG, eta), &its));
+    c->cg_rel_only = inexact;
+    TRY(cg(c, c->b, c->dFm, tol_k, &its));
     c->cg_rel_only = false;
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
@@ -2097,7 +2129,7 @@ int cpfft_nr3_step(int step, const double* BC, const int* isNBC, double tolNR, d
     c->cg_rel_only = false;
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
-    if (inexact && existNBC && c->coupled_bc) {
+    if (c->eq_tol > 0.0 && existNBC && c->coupled_bc) {
       TRY(coupled_step(c, step, PBC, isNBC, barF, Fnorm, tolNR, tolPCG, maxIter, S, tp, ts));
       break;
     }

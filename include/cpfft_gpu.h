@@ -367,8 +367,8 @@ int cpfft_set_inexact_newton(double eta_max);
 int cpfft_set_tangent_tol(double tol);
 
 /*
- * The P_bar update inside the Newton iteration (extension; on != 0; needs the equilibrium
- * test and inexact Newton, and prescribed-stress components).  The reference nests a
+ * The P_bar update inside the Newton iteration (extension; on != 0; applies with the
+ * equilibrium test and prescribed-stress components).  The reference nests a
  * Newton loop at fixed macroscopic F inside a loop of P_bar updates, each pass opening
  * with an explicit stress pass (src/FFT_nr3.f:75-171).  Here every Newton iteration also
  * updates the prescribed-stress components of F_bar with NBC_update's system and solves

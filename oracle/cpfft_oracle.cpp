@@ -2064,6 +2064,7 @@ struct orc_ctx {
   // FFT_nr3 persistent locals (Fortran DATA => SAVE'd, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
   double eq_tol = 0.0;  // equilibrium stop test of the Newton loop (0: the reference's loop)
+  bool coupled_bc = false;  // the P_bar update inside the Newton iteration
   int hist_words = ORC_HIST;  // ORC_HIST_MRR on grids of Ma-Roters-Raabe crystals
 };
 
@@ -2420,6 +2421,89 @@ static double equil_residual(const orc_ctx* c, const double* g) {
 }
 
 void orc_set_equilibrium_tol(orc_ctx* c, double tol) { c->eq_tol = tol; }
+void orc_set_coupled_bc(orc_ctx* c, int on) { c->coupled_bc = on != 0; }
+
+// The library's coupled P_bar update (cpfft_set_coupled_bc, an extension restated here
+// for its parity tests): after each stress pass, DbarF from NBC_update's system with the
+// current C_homo (recomputed after the first two implicit passes), then the fluctuation
+// solves G(K : dF) = -G(P) - G(K : DbarF); increments that raise the equilibrium residual
+// are halved (at most 4 times in a row); the step ends when P_bar, the equilibrium
+// residual and the last increment all meet their tolerances.
+static int coupled_step(orc_ctx* c, int step, const double* PBC, const int* isNBC,
+                        double* barF, double Fnorm, double tolNR, double tolPCG, int maxIter,
+                        cpfft_stats& S) {
+  const long N3 = c->N3, n = 9 * N3;
+  double resfft = 1.0;
+  int tangents = 0, rc = 0;
+  std::vector<double> g(n), w(n);
+  double eq_prev = HUGE_VAL, frac = 1.0, lastD[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int halvings = 0;
+  for (int k = 0;; k++) {
+    long long li = 0;
+    S.local_fallbacks += orc_stress_update(c, step, k, nullptr, nullptr, nullptr, nullptr, &li);
+    S.local_iters += li;
+    S.stress_updates++;
+    orc_green_apply(c, c->Pn1.data(), g.data(), 0, nullptr);
+    const double e = equil_residual(c, g.data());
+    S.res_equil = e;
+    double res1 = 0, res2 = 0;
+    for (int i = 0; i < 9; i++) {
+      double s = 0;
+      for (long v = 0; v < N3; v++) s += c->Pn1[i * N3 + v];
+      c->P_bar[i] = s / (double)N3;
+      res2 += c->P_bar[i] * c->P_bar[i];
+      if (isNBC[i]) res1 += (c->P_bar[i] - PBC[i]) * (c->P_bar[i] - PBC[i]);
+    }
+    const double res3 = res2 < 1.0e-8 ? std::sqrt(res1) : std::sqrt(res1 / res2);
+    S.res_pbar = res3;
+    if (res3 <= tolNR && e <= c->eq_tol && resfft <= tolNR) break;
+    if (k == maxIter) return CPFFT_ERR_NEWTON_MAXIT;
+    if (k >= 2 && e > eq_prev && halvings < 4) {  // halve the last increment
+      frac *= 0.5;
+      for (int i = 0; i < 9; i++) barF[i] -= frac * lastD[i];
+      for (int i = 0; i < 9; i++)
+        for (long v = 0; v < N3; v++) c->Fn1[i * N3 + v] -= frac * (c->dFm[i * N3 + v] + lastD[i]);
+      halvings++;
+      resfft *= 0.5;
+      continue;
+    }
+    eq_prev = e;
+    halvings = 0;
+    frac = 1.0;
+    if (k >= 1 && tangents < 2) {
+      int th = orc_tangent_homo(c, tolPCG, c->C_homo);
+      if (th < 0) return th;
+      S.cg_solves += 9; S.cg_iters += th;
+      tangents++;
+    }
+    double DbarF[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if ((rc = nbc_update(c->C_homo, DbarF, c->P_bar, PBC, isNBC))) return rc;
+    for (int i = 0; i < 9; i++)
+      for (long v = 0; v < N3; v++) c->dFm[i * N3 + v] = DbarF[i];
+    orc_green_apply(c, c->dFm.data(), w.data(), 1, nullptr);
+    for (long q = 0; q < n; q++) {
+      c->b[q] = -g[q] - w[q];
+      c->Fn1[q] += c->dFm[q];
+    }
+    for (int i = 0; i < 9; i++) {
+      barF[i] += DbarF[i];
+      lastD[i] = DbarF[i];
+    }
+    int its = 0;
+    rc = orc_cg(c, c->b.data(), c->dFm.data(), tolPCG, &its);
+    S.cg_solves++; S.cg_iters += its;
+    if (rc) return rc;
+    for (long q = 0; q < n; q++) c->Fn1[q] += c->dFm[q];
+    double db = 0;
+    for (int i = 0; i < 9; i++) db += DbarF[i] * DbarF[i];
+    const double dn = nrm2(c->dFm.data(), n);
+    resfft = std::sqrt(dn * dn + (double)N3 * db) / Fnorm;
+    S.newton_iters++;
+    S.res_fft = resfft;
+  }
+  S.nbc_iters = 1;
+  return 0;
+}
 
 int orc_nr3_begin(orc_ctx* c, double tolPCG) {
   orc_stress_update(c, 1, 0, nullptr, nullptr, nullptr, nullptr, nullptr);
@@ -2464,6 +2548,11 @@ int orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC, doubl
     S.cg_solves++; S.cg_iters += its;
     if (rc) return rc;
     for (long k = 0; k < n; k++) c->Fn1[k] += c->dFm[k];
+    if (c->eq_tol > 0.0 && existNBC && c->coupled_bc) {
+      if ((rc = coupled_step(c, step, PBC, isNBC, barF, Fnorm, tolNR, tolPCG, maxIter, S)))
+        return rc;
+      break;
+    }
     double resfft = 1.0;
     int iiter_EBC = 0;
     // equilibrium test (an extension of the library, restated here for its parity tests):

@@ -116,6 +116,7 @@ def lib():
         L.orc_nr3_begin.restype = i
         L.orc_nr3_begin.argtypes = [vp, d]
         L.orc_set_equilibrium_tol.argtypes = [vp, d]
+        L.orc_set_coupled_bc.argtypes = [vp, i]
         L.orc_nr3_step.restype = i
         L.orc_nr3_step.argtypes = [vp, i, dp, ip, d, d, i, dp, P(Stats)]
         L.orc_get_fields.argtypes = [vp, dp, dp, dp, dp, dp]
@@ -216,6 +217,9 @@ class Oracle:
 
     def set_equilibrium_tol(self, tol):
         lib().orc_set_equilibrium_tol(self.h, float(tol))
+
+    def set_coupled_bc(self, on=True):
+        lib().orc_set_coupled_bc(self.h, int(bool(on)))
 
     def nr3_begin(self, tolPCG):
         return lib().orc_nr3_begin(self.h, tolPCG)
