@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_gb300.so")
 HIST_WORDS = 31
-HIST_WORDS_MRR = 55  # grids of Ma-Roters-Raabe crystals (h_type 7)
+HIST_WORDS_MRR = 55  # grids of dislocation-density crystals (h_type 7, 4)
 NOT_A_CRYSTAL = 0  # slip_type of a material defined by Solver.set_mises
 
 G_REF_SHIFT, G_CENTERED = 0, 1

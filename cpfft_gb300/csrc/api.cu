@@ -293,7 +293,7 @@ CrysRec crystal_record(const cpfft_crystal& p) {
   c.u4 = p.u4;
   c.u5 = p.u5;
   c.u6 = p.u6;
-  if (p.h_type == 7) mrr_interaction(c.Gm, c.Hm);
+  if (p.h_type == 7 || p.h_type == 4) mrr_interaction(c.Gm, c.Hm);
   c.h_type = p.h_type;
   c.miter = p.miter;
   c.alter_mode = p.alter_mode;
@@ -312,7 +312,7 @@ struct Ctx {
   int prec = CPFFT_PREC_FP64, warm = 0;
   int nslip = 12;  // slip systems of the grid's crystals (12 fcc, 48 bcc48)
   int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts, 7 mrr)
-  int hist_words = H_WORDS;  // H_WORDS_MRR on Ma-Roters-Raabe grids
+  int hist_words = H_WORDS;  // H_WORDS_MRR on dislocation-density grids (MRR, ORNL)
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
   // voxel work queue of the implicit stress passes (cpfft_set_schedule)
   int sched = CPFFT_SCHED_BLOCKS;
@@ -1048,6 +1048,7 @@ int cg(Ctx* c, const double* b, double* x, double tol, int* iters) {
 cudaError_t launch_crystals(Ctx* c, const StressArgs& a, bool warm) {
   if (c->h_type == 2) return launch_stress_mts(a, warm, c->st);
   if (c->h_type == 7) return launch_stress_mrr(a, false, c->st);
+  if (c->h_type == 4) return launch_stress_ornl(a, false, c->st);
   return c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st);
 }
 
@@ -1374,11 +1375,15 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     const bool mrr_ok = p.h_type == 7 && ns == 12 && p.mu_0 > 0 && p.burgers > 0 &&
                         p.boltzman > 0 && p.G_0_y > 0 && p.G_0_v > 0 && p.p_v > 0 &&
                         p.q_v > 0 && p.u1 > 0 && p.u2 > 0 && p.u3 > 0 && p.theta_0 >= 0;
-    const bool n_ok = p.h_type == 7 || p.harden_n > 0;
-    if (!ns || !(voce_ok || mts_ok || mrr_ok) || !n_ok ||
+    // ORNL: the same, with a negative G_0_y read as exp(-G_0_y) (mm10_slipinc_ornl)
+    const bool ornl_ok = p.h_type == 4 && ns == 12 && p.mu_0 > 0 && p.burgers > 0 &&
+                         p.boltzman > 0 && p.G_0_v > 0 && p.p_v > 0 && p.q_v > 0 &&
+                         p.u1 > 0 && p.u2 > 0 && p.u3 > 0 && p.theta_0 >= 0;
+    const bool n_ok = p.h_type == 7 || p.h_type == 4 || p.harden_n > 0;
+    if (!ns || !(voce_ok || mts_ok || mrr_ok || ornl_ok) || !n_ok ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
       cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip with voce hardening, "
-                      "fcc with mts or roters hardening, valid elasticity)", k + 1);
+                      "fcc with mts, roters or ornl hardening, valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
     if ((nslip && ns != nslip) || (h_type && p.h_type != h_type)) {
@@ -1431,7 +1436,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
   Ctx* c = new Ctx;
   c->nslip = nslip;
   c->h_type = h_type;
-  c->hist_words = h_type == 7 ? H_WORDS_MRR : H_WORDS;
+  c->hist_words = (h_type == 7 || h_type == 4) ? H_WORDS_MRR : H_WORDS;
   const int HW = c->hist_words;
   c->mat = mat;
   c->mat_kind.assign(ncrystals, 0);
@@ -1509,7 +1514,8 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
       h[H_TT * N3 + v] = -1.0;
       h[H_U * N3 + v] = -1.0;
       h[(H_U + 1) * N3 + v] = -1.0;
-    } else if (props[crys[v]].h_type == 7) {  // mm10_init_mrr (src/mm10_a.f:2205-2223)
+    } else if (props[crys[v]].h_type == 7 || props[crys[v]].h_type == 4) {
+      // mm10_init_mrr / mm10_init_ornl (src/mm10_a.f:2205-2223, 2286-2304)
       const double r0 = props[crys[v]].theta_0 == 0.0 ? 1.0e8 : props[crys[v]].theta_0;
       for (int i = 0; i < 12; i++) h[(H_RHO + i) * N3 + v] = r0;
     } else {

@@ -149,8 +149,10 @@ cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
 // MTS-hardened FCC crystals (stress_mts.cu)
 cudaError_t launch_stress_mts(const StressArgs& a, bool warm, cudaStream_t s);
-// Ma-Roters-Raabe FCC crystals (stress_mrr.cu; warm is ignored: no learned guess)
+// Ma-Roters-Raabe / ORNL FCC crystals (stress_mrr.cu / stress_ornl.cu; warm is ignored: no
+// learned guess)
 cudaError_t launch_stress_mrr(const StressArgs& a, bool warm, cudaStream_t s);
+cudaError_t launch_stress_ornl(const StressArgs& a, bool warm, cudaStream_t s);
 // the mm01 voxels (a.mises[v] >= 0) of the grid; the crystal launches skip them
 cudaError_t launch_mises(const StressArgs& a, cudaStream_t s);
 // Build the voxel work queue from the per-voxel costs: perm = voxel ids by descending cost

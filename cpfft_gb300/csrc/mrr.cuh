@@ -1,6 +1,9 @@
-// mrr.cuh -- Ma-Roters-Raabe hardening (h_type 7) for the stress kernel: twelve
-// dislocation densities, one per FCC slip system, as the slip resistance variables.
-// Included by stress.cu when it is compiled with CPFFT_LAW 7 (stress_mrr.cu).
+// mrr.cuh -- dislocation-density hardening for the stress kernel: twelve dislocation
+// densities, one per FCC slip system, as the slip resistance variables.  Ma-Roters-Raabe
+// (h_type 7, stress_mrr.cu) and ORNL (h_type 4, stress_ornl.cu: the same hardening law
+// with the temperature-dependent shear modulus mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1),
+// and its own slip law, mm10_slipinc_ornl .. mm10_dgdh_ornl, src/mm10_b.f:3457-4347).
+// Included by stress.cu when it is compiled with CPFFT_LAW 7 or 4.
 //
 // The slip law, hardening law and their derivatives follow mm10_slipinc_mrr ..
 // mm10_dgdd_mrr (src/mm10_b.f:2343-3325); the local solve is mm10_solve
@@ -12,6 +15,21 @@
 // One thread per voxel: the 18 x 18 Jacobian and its LU live in local memory.
 
 constexpr int NH = 12;  // dislocation densities
+constexpr bool ORNL = CPFFT_LAW == 4;
+
+// the law's shear modulus: MRR's constant mu_0, ORNL's mu(T)
+__device__ __forceinline__ double mrr_shear(const Crystal& s) {
+  const CrysRec& c = *s.cr;
+  return ORNL ? c.mu_0 - c.D_0 / (exp(c.T_0 / s.temp) - 1.0) : c.mu_0;
+}
+// ORNL: the attack frequency (exp(-G_0_y) when negative) and the slip exponent, 1 below
+// the passing stress (fract < 0)
+__device__ __forceinline__ double ornl_vs(const CrysRec& c) {
+  return c.G_0_y < 0.0 ? exp(-c.G_0_y) : c.G_0_y;
+}
+__device__ __forceinline__ double mrr_pexp(const CrysRec& c, double fract) {
+  return ORNL && fract < 0.0 ? 1.0 : c.p_v;
+}
 constexpr double MRR_PI = 3.141592653589793;
 constexpr double MRR_NU = 0.3;  // Poisson's ratio of the dipole distance (mm10_h_mrr)
 
@@ -24,7 +42,7 @@ struct MrrSys {
 
 __device__ void mrr_sys(const Crystal& s, const double* st, const double* tt, int a, MrrSys& y) {
   const CrysRec& c = *s.cr;
-  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
   y.rs = st[0] * s.ms[a][0] + st[1] * s.ms[a][1] + st[2] * s.ms[a][2] + st[3] * s.ms[a][3] +
          st[4] * s.ms[a][4] + st[5] * s.ms[a][5];
   double f = 0.0, p = 0.0;
@@ -35,16 +53,23 @@ __device__ void mrr_sys(const Crystal& s, const double* st, const double* tt, in
   y.rhoF = f;
   y.rhoP = p;
   const double sp = sqrt(p);
-  y.g0 = c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) * sp;
-  y.tpass = c.u1 * G * b * sp;
-  y.tcut = c.G_0_v / (c.u2 * c.u3 * b * b) * sqrt(f);
+  if (ORNL) {  // mobile density 0.1 rho_a, cutting stress tau_0 mu(T) / mu_0
+    y.g0 = 0.1 * tt[a] * b * ornl_vs(c) / b * (c.u2 * b);
+    y.tpass = c.u1 * G * b * sp;
+    y.tcut = c.u3 * G / c.mu_0;
+  } else {
+    y.g0 = c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) * sp;
+    y.tpass = c.u1 * G * b * sp;
+    y.tcut = c.G_0_v / (c.u2 * c.u3 * b * b) * sqrt(f);
+  }
   y.fract = (fabs(y.rs) - y.tpass) / y.tcut;
   const double Qk = c.G_0_v / k / th;
   if (y.fract > 1.0) {  // linear extrapolation past fract = 1
     const double m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
     y.slip = s.tinc * (m * y.fract + y.g0);
   } else if (fabs(y.rs) > 0.0) {
-    y.slip = s.tinc * y.g0 * sgn1(y.rs) * exp(-Qk * pow(1.0 - pow(y.fract, c.p_v), c.q_v));
+    y.slip = s.tinc * y.g0 * sgn1(y.rs) *
+             exp(-Qk * pow(1.0 - pow(y.fract, mrr_pexp(c, y.fract)), c.q_v));
   } else {
     y.slip = 0.0;
   }
@@ -60,23 +85,26 @@ __device__ double mrr_dgdt(const Crystal& s, const MrrSys& y) {
     return c.exact_j22 ? s.tinc * m * dfract : s.tinc * m;
   }
   if (fabs(y.rs) > 0.0) {
-    const double base = 1.0 - pow(y.fract, c.p_v);
+    const double pe = mrr_pexp(c, y.fract);
+    const double base = 1.0 - pow(y.fract, pe);
     const double slipexp = exp(-Qk * pow(base, c.q_v)) * sgn1(y.rs);
-    return s.tinc * (-y.g0 * slipexp * Qk * c.q_v * pow(base, c.q_v - 1.0) * (-1.0) * c.p_v *
-                     pow(y.fract, c.p_v - 1.0) * dfract);
+    return s.tinc * (-y.g0 * slipexp * Qk * c.q_v * pow(base, c.q_v - 1.0) * (-1.0) * pe *
+                     pow(y.fract, pe - 1.0) * dfract);
   }
   return 0.0;
 }
 
-// d slip_a / d rho_q (mm10_dgdh_mrr, src/mm10_b.f:3201-3306)
+// d slip_a / d rho_q (mm10_dgdh_mrr, src/mm10_b.f:3201-3306; ORNL: mm10_dgdh_ornl,
+// :4224-4347, the prefactor depends on rho_a alone and the cutting stress on no density)
 __device__ double mrr_dgdh(const Crystal& s, const MrrSys& y, int a, int q) {
   const CrysRec& c = *s.cr;
-  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
   const double Qk = c.G_0_v / k / th;
   const double drhoF = __ldg(c.Gm + NH * a + q), drhoP = __ldg(c.Hm + NH * a + q);
-  const double dg0 = 0.5 * c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) / sqrt(y.rhoP) * drhoP;
+  const double dg0 = ORNL ? (a == q ? 0.1 : 0.0) * b * ornl_vs(c) / b * (c.u2 * b)
+                          : 0.5 * c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) / sqrt(y.rhoP) * drhoP;
   const double dtpass = 0.5 * c.u1 * G * b / sqrt(y.rhoP) * drhoP;
-  const double dtcut = 0.5 * c.G_0_v / (c.u2 * c.u3 * b * b) / sqrt(y.rhoF) * drhoF;
+  const double dtcut = ORNL ? 0.0 : 0.5 * c.G_0_v / (c.u2 * c.u3 * b * b) / sqrt(y.rhoF) * drhoF;
   const double dfract = ((-dtpass) * y.tcut - (fabs(y.rs) - y.tpass) * dtcut) / (y.tcut * y.tcut);
   if (y.fract > 1.0) {
     const double K = (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs);
@@ -86,11 +114,12 @@ __device__ double mrr_dgdh(const Crystal& s, const MrrSys& y, int a, int q) {
     return s.tinc * (dm * y.fract + m * dfract + dg0);
   }
   if (fabs(y.rs) > 0.0) {
-    const double base = 1.0 - pow(y.fract, c.p_v);
+    const double pe = mrr_pexp(c, y.fract);
+    const double base = 1.0 - pow(y.fract, pe);
     const double slipexp = exp(-Qk * pow(base, c.q_v));
     return s.tinc * (dg0 * slipexp * sgn1(y.rs) +
                      y.g0 * sgn1(y.rs) * slipexp * (-1.0) * Qk * c.q_v * pow(base, c.q_v - 1.0) *
-                         (-1.0) * c.p_v * pow(y.fract, c.p_v - 1.0) * dfract);
+                         (-1.0) * pe * pow(y.fract, pe - 1.0) * dfract);
   }
   return 0.0;
 }
@@ -122,7 +151,7 @@ __device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x,
   const double* st = x;
   const double* tt = x + 6;
   mrr_formR1(s, st, tt, R);
-  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
   const double cdip = sqrt(3.0) * G * b / (16.0 * MRR_PI * (1.0 - MRR_NU));
   const double cM = (2.0 * k / (c.u1 * c.u2 * c.u3 * G * b * b * b)) * th;
   const double E = c.tau_hat_y * exp(-c.tau_a / k / th) / (k * th);
@@ -184,7 +213,7 @@ __device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
   mrr_formJ11<L>(s, st, tt, J);
   for (int a = 0; a < 6; a++)
     for (int q = 0; q < NH; q++) J[L * a + 6 + q] = 0.0;
-  const double k = c.boltzman, th = s.temp, G = c.mu_0, b = c.burgers;
+  const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
   const double dt = s.tinc;
   const double cdip = sqrt(3.0) * G * b / (16.0 * MRR_PI * (1.0 - MRR_NU));
   const double cM = 2.0 * k / (c.u1 * c.u2 * c.u3 * G * b * b * b) * th;

@@ -20,8 +20,9 @@
 #define CPFFT_STRESS_LAUNCH launch_stress
 #endif
 // Hardening law: Voce (1) here; stress_mts.cu compiles this file again with CPFFT_LAW 2
-// (MTS) and stress_mrr.cu with CPFFT_LAW 7 (Ma-Roters-Raabe, mrr.cuh).  The kernels that
-// serve every grid (mm01, the voxel queue) live in the first unit.
+// (MTS), stress_mrr.cu with CPFFT_LAW 7 (Ma-Roters-Raabe, mrr.cuh) and stress_ornl.cu with
+// CPFFT_LAW 4 (ORNL, mrr.cuh).  The kernels that serve every grid (mm01, the voxel queue)
+// live in the first unit.
 #ifndef CPFFT_LAW
 #define CPFFT_LAW 1
 #endif
@@ -32,7 +33,7 @@ namespace {
 
 constexpr int NS = CPFFT_NSLIP;  // slip systems
 constexpr bool MTS = CPFFT_LAW == 2;
-constexpr bool MRR = CPFFT_LAW == 7;
+constexpr bool MRR = CPFFT_LAW == 7 || CPFFT_LAW == 4;  // the dislocation-density laws
 // the temperature of the reference's FFT path (drive_10_update, src/rstgp1.f:832)
 constexpr double TEMP = 297.0;
 
@@ -878,7 +879,7 @@ __device__ void store_P_K4(const StressArgs& a, long long v, const double* Fn, c
                            const double* stress, const double* cep, const double* rnh,
                            const double* rn1, const double* fnhinv);
 
-#if CPFFT_LAW == 7
+#if CPFFT_LAW == 7 || CPFFT_LAW == 4
 #include "mrr.cuh"
 #endif
 
@@ -931,8 +932,8 @@ __global__ void __launch_bounds__(128) stress_kernel(StressArgs a) {
     const bool mine = valid && (!a.mises || __ldg(a.mises + v) < 0);
     int it = 0, pit = 0, rj = 0;
     bool ok = true;
-#if CPFFT_LAW == 7
-    if (mine) voxel_update_mrr(a, v, it, pit, ok);  // no learned guess for MRR grids
+#if CPFFT_LAW == 7 || CPFFT_LAW == 4
+    if (mine) voxel_update_mrr(a, v, it, pit, ok);  // no learned guess for these grids
 #else
     if (WARM) {
       voxel_update<true>(a, v, mine, it, pit, ok, rj, &gb);

@@ -87,6 +87,16 @@ MRR_FCC = dict(
     theta_0=1.0e6, u1=0.5, u2=0.1, u3=1.0, u4=0.01, u5=5.0, u6=1.0,
 )
 
+# An FCC crystal with ORNL hardening (h_type 4): MRR_FCC's densities and hardening
+# constants, the shear modulus softened at 297 K (D_0 = 3000 MPa, T_0 = 200 K), slip at
+# 0.1 rho_a v_s (c2 b) with v_s = 1e5 mm/s and c2 = 10, passing stress c1 mu b sqrt(rho_P),
+# cutting stress c3 mu / mu_0 with c3 = 150 MPa, p = 0.5 (1 below the passing stress),
+# q = 2.
+ORNL_FCC = dict(
+    MRR_FCC, h_type=4, G_0_y=1.0e5, p_v=0.5, q_v=2.0, D_0=3000.0, T_0=200.0,
+    u2=10.0, u3=150.0,
+)
+
 # component order of 9-vectors: 11,12,13,21,22,23,31,32,33
 COMP = ["xx", "xy", "xz", "yx", "yy", "yz", "zx", "zy", "zz"]
 

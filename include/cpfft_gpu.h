@@ -65,8 +65,9 @@ typedef struct cpfft_crystal {
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;
     int    h_type;         /* 1 = voce, 2 = mts, 7 = roters (Ma-Roters-Raabe dislocation
-                              densities, one per slip system); fcc crystals; the crystals of
-                              one grid share the hardening law                              */
+                              densities, one per slip system), 4 = ornl (the same densities,
+                              ORNL's slip law); fcc crystals; the crystals of one grid share
+                              the hardening law                                            */
     double harden_n;       /* rate exponent                                               */
     double tau_y, tau_v, theta_0, voce_m;
     double gamma_bar;      /* eps_dot_0_y                                                 */
@@ -97,6 +98,11 @@ typedef struct cpfft_crystal {
        the exact derivatives of the residual in the local Jacobian (the reference's use
        sqrt(rho_F) where the residual has sqrt(rho_P), src/mm10_b.f:2635 against :2952
        and :3075).                                                                    */
+    /* ORNL hardening (h_type 4: mm10_slipinc_ornl .. mm10_dgdd_ornl,
+       src/mm10_b.f:3330-4370): MRR's hardening law with mu(T) = mu_0 - D_0 /
+       (exp(T_0 / T) - 1); slip rate 0.1 rho_a v_s (c2 b) exp(-Q_slip / kT
+       (1 - fract^p)^q) with v_s = G_0_y (exp(-G_0_y) when negative), the cutting stress
+       c3 mu(T) / mu_0 and p = 1 below the passing stress.                          */
     double u1, u2, u3, u4, u5, u6;      /* c1 .. c6                                      */
 } cpfft_crystal;
 
@@ -431,7 +437,7 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
  * compact history at n (N3, cpfft_hist_words()) used by the result writers. */
 #define CPFFT_HIST_WORDS 31   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6)
                                  u(2): MTS tau_y and mu at the step's end (mm10's u(1:2)) */
-#define CPFFT_HIST_WORDS_MRR 55  /* grids of Ma-Roters-Raabe crystals (h_type 7): the words
+#define CPFFT_HIST_WORDS_MRR 55  /* grids of dislocation-density crystals (h_type 7, 4): the words
                                     above (tau_tilde, its rate and u zero), then the twelve
                                     dislocation densities (mm10's tau_tilde(1:12)) and their
                                     rates (tt_rate(1:12))                                  */

@@ -423,7 +423,7 @@ void state_init(const Crys& cr, State& s) {  // mm10_init_cc_hist0 (src/mm10_a.f
     s.tt = -1.0;
     s.u[0] = s.u[1] = -1.0;
   }
-  if (cr.p.h_type == 7) {                    // mm10_init_mrr (:2205-2223)
+  if (cr.p.h_type == 7 || cr.p.h_type == 4) {  // mm10_init_mrr / _ornl (:2205-2223, 2286-2304)
     s.mrr = true;
     s.tt = 0.0;
     for (int i = 0; i < 12; i++) s.rho[i] = cr.p.theta_0 == 0.0 ? 1.0e8 : cr.p.theta_0;
@@ -1092,8 +1092,17 @@ struct Mrr {
   struct Sys {
     double rs, rhoF, rhoP, g0, tpass, tcut, fract, slip;
   };
+  bool ornl() const { return p->h_type == 4; }
+  // shear modulus: MRR's constant mu_0; ORNL's mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1)
+  double shear(const Np1& s) const {
+    return ornl() ? p->mu_0 - p->D_0 / (std::exp(p->T_0 / s.temp) - 1.0) : p->mu_0;
+  }
+  // ORNL's attack frequency (G_0_y; exp(-G_0_y) when negative)
+  double vs() const { return p->G_0_y < 0.0 ? std::exp(-p->G_0_y) : p->G_0_y; }
+  // the slip-law exponent p: ORNL takes 1 below the passing stress (fract < 0)
+  double pexp(double fract) const { return ornl() && fract < 0.0 ? 1.0 : p->p_v; }
   void sys(const Np1& s, const double* st, const double* tt, int a, Sys& y) const {
-    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers;
+    const double k = p->boltzman, th = s.temp, G = shear(s), b = p->burgers;
     y.rs = rs(s, st, a);
     y.rhoF = 0.0;
     y.rhoP = 0.0;
@@ -1101,9 +1110,15 @@ struct Mrr {
       y.rhoF += Gm[a][q] * tt[q];
       y.rhoP += Hm[a][q] * tt[q];
     }
-    y.g0 = p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) * std::sqrt(y.rhoP);   // (15)
-    y.tpass = p->u1 * G * b * std::sqrt(y.rhoP);                                 // (16)
-    y.tcut = p->G_0_v / (p->u2 * p->u3 * b * b) * std::sqrt(y.rhoF);             // (17)
+    if (ornl()) {  // mm10_slipinc_ornl (src/mm10_b.f:3457-3540): mobile density 0.1 rho_a
+      y.g0 = 0.1 * tt[a] * b * vs() / b * (p->u2 * b);
+      y.tpass = p->u1 * G * b * std::sqrt(y.rhoP);
+      y.tcut = p->u3 * G / p->mu_0;
+    } else {
+      y.g0 = p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) * std::sqrt(y.rhoP);   // (15)
+      y.tpass = p->u1 * G * b * std::sqrt(y.rhoP);                                 // (16)
+      y.tcut = p->G_0_v / (p->u2 * p->u3 * b * b) * std::sqrt(y.rhoF);             // (17)
+    }
     y.fract = (std::fabs(y.rs) - y.tpass) / y.tcut;
     // mm10_slipinc_mrr (src/mm10_b.f:2477-2546)
     const double Qk = p->G_0_v / k / th;
@@ -1112,7 +1127,7 @@ struct Mrr {
       y.slip = s.tinc * (m * y.fract + y.g0);
     } else if (std::fabs(y.rs) > 0.0) {
       y.slip = s.tinc * y.g0 * sgn1(y.rs) *
-               std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v));  // (14)
+               std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, pexp(y.fract)), p->q_v));  // (14)
     } else {
       y.slip = 0.0;
     }
@@ -1126,21 +1141,26 @@ struct Mrr {
       return p->exact_j22 ? s.tinc * m * dfract : s.tinc * m;
     }
     if (std::fabs(y.rs) > 0.0) {
-      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v)) * sgn1(y.rs);
+      const double pe = pexp(y.fract);
+      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, pe), p->q_v)) * sgn1(y.rs);
       return s.tinc * (-y.g0 * slipexp * Qk * p->q_v *
-                       std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v - 1.0) * (-1.0) * p->p_v *
-                       std::pow(y.fract, p->p_v - 1.0) * dfract);
+                       std::pow(1.0 - std::pow(y.fract, pe), p->q_v - 1.0) * (-1.0) * pe *
+                       std::pow(y.fract, pe - 1.0) * dfract);
     }
     return 0.0;
   }
   // d slip_a / d rho_c (mm10_dgdh_mrr, src/mm10_b.f:3201-3306)
+  // (ORNL: mm10_dgdh_ornl, :4224-4347: the rate prefactor depends on rho_a alone, the
+  // cutting stress on no density)
   double dgdh(const Np1& s, const Sys& y, int a, int c) const {
-    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers;
+    const double k = p->boltzman, th = s.temp, G = shear(s), b = p->burgers;
     const double Qk = p->G_0_v / k / th;
     const double drhoF = Gm[a][c], drhoP = Hm[a][c];
-    const double dg0 = 0.5 * p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) / std::sqrt(y.rhoP) * drhoP;
+    const double dg0 = ornl() ? (a == c ? 0.1 : 0.0) * b * vs() / b * (p->u2 * b)
+                              : 0.5 * p->G_0_y * k * th / (p->u1 * p->u3 * G * b * b) /
+                                    std::sqrt(y.rhoP) * drhoP;
     const double dtpass = 0.5 * p->u1 * G * b / std::sqrt(y.rhoP) * drhoP;
-    const double dtcut = 0.5 * p->G_0_v / (p->u2 * p->u3 * b * b) / std::sqrt(y.rhoF) * drhoF;
+    const double dtcut = ornl() ? 0.0 : 0.5 * p->G_0_v / (p->u2 * p->u3 * b * b) / std::sqrt(y.rhoF) * drhoF;
     const double dfract = ((-dtpass) * y.tcut - (std::fabs(y.rs) - y.tpass) * dtcut) / (y.tcut * y.tcut);
     if (y.fract > 1.0) {
       double K = (-p->q_v * Qk) * (-p->p_v) * sgn1(y.rs);
@@ -1150,11 +1170,12 @@ struct Mrr {
       return s.tinc * (dm * y.fract + m * dfract + dg0);
     }
     if (std::fabs(y.rs) > 0.0) {
-      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v));
+      const double pe = pexp(y.fract);
+      double slipexp = std::exp(-Qk * std::pow(1.0 - std::pow(y.fract, pe), p->q_v));
       return s.tinc * (dg0 * slipexp * sgn1(y.rs) +
                        y.g0 * sgn1(y.rs) * slipexp * (-1.0) * Qk * p->q_v *
-                           std::pow(1.0 - std::pow(y.fract, p->p_v), p->q_v - 1.0) * (-1.0) *
-                           p->p_v * std::pow(y.fract, p->p_v - 1.0) * dfract);
+                           std::pow(1.0 - std::pow(y.fract, pe), p->q_v - 1.0) * (-1.0) *
+                           pe * std::pow(y.fract, pe - 1.0) * dfract);
     }
     return 0.0;
   }
@@ -1175,7 +1196,7 @@ struct Mrr {
   }
   // mm10_h_mrr (src/mm10_b.f:2549-2646) and R2 = tt - h (mm10_formR2, :63-113)
   void formR2(Np1& s, const double* st, const double* tt, double* R2) const {
-    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers, v = 0.3;
+    const double k = p->boltzman, th = s.temp, G = shear(s), b = p->burgers, v = 0.3;
     for (int a = 0; a < MRR_NH; a++) {
       Sys y;
       sys(s, st, tt, a, y);
@@ -1261,7 +1282,7 @@ struct Mrr {
       }
     }
     // J21, J22
-    const double k = p->boltzman, th = s.temp, G = p->mu_0, b = p->burgers, v = 0.3;
+    const double k = p->boltzman, th = s.temp, G = shear(s), b = p->burgers, v = 0.3;
     const double dt = s.tinc;
     const double cdip = std::sqrt(3.0) * G * b / (16.0 * PI * (1.0 - v));
     const double cM = 2.0 * k / (p->u1 * p->u2 * p->u3 * G * b * b * b) * th;
@@ -1716,7 +1737,7 @@ void material_point(const Crys& cr, const VoxProps& vp, double dt, int step, int
     n.tt = cr.p.tau_a + (mu / cr.p.mu_0) * ty + 0.1;
   }
   int it = 0;
-  if (cr.p.h_type == 7) {
+  if (cr.p.h_type == 7 || cr.p.h_type == 4) {
     Mrr mm{&cr.p, &vp, &n, cr.Gm, cr.Hm};
     o.ok = mm.update(k.uddt, dt, k.rn1, iter == 0, np1, o.cep, &it);
     np1.mrr = true;
@@ -2100,7 +2121,7 @@ orc_ctx* orc_create(int N, const int* matList, const double* kocks_deg,
   for (int i = 0; i < ncrystals; i++) {
     if (props[i].slip_type == CPFFT_NOT_A_CRYSTAL) { c->kind[i] = 2; continue; }
     crystal_finalize(props[i], c->crys[i]);
-    if (props[i].h_type == 7) c->hist_words = ORC_HIST_MRR;
+    if (props[i].h_type == 7 || props[i].h_type == 4) c->hist_words = ORC_HIST_MRR;
   }
   long N3 = c->N3;
   c->mat.resize(N3);
@@ -2679,7 +2700,7 @@ void orc_set_history_n(orc_ctx* c, const double* hist_n) {
     std::memset(&c->hn[v], 0, sizeof(State));
     const int m = c->mat[v];
     c->hn[v].m01 = c->kind[m] == 1;
-    c->hn[v].mrr = c->kind[m] == 0 && c->crys[m].p.h_type == 7;
+    c->hn[v].mrr = c->kind[m] == 0 && (c->crys[m].p.h_type == 7 || c->crys[m].p.h_type == 4);
     state_unpack(h, c->hn[v]);
   }
 }
@@ -2695,7 +2716,7 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3], doub
   State n, np1;
   std::memset(&n, 0, sizeof(n));
   std::memset(&np1, 0, sizeof(np1));
-  n.mrr = props->h_type == 7;
+  n.mrr = props->h_type == 7 || props->h_type == 4;
   if (hist_n) state_unpack(hist_n, n);
   else state_init(cr, n);
   M3 fn, fn1;
@@ -2752,7 +2773,7 @@ void orc_mrr_interaction(double G[144], double H[144]) {
 int orc_mrr_residual(const cpfft_crystal* props, const double kocks_deg[3], const double D[6],
                      double tinc, const double* hist_n, const double x[18], double R[18],
                      double J[324]) {
-  if (props->h_type != 7) return -1;
+  if (props->h_type != 7 && props->h_type != 4) return -1;
   Crys cr;
   crystal_finalize(*props, cr);
   VoxProps vp;

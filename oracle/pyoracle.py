@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libcpfft_oracle.so")
 HIST_WORDS = 31
-HIST_WORDS_MRR = 55  # grids of Ma-Roters-Raabe crystals (h_type 7)
+HIST_WORDS_MRR = 55  # grids of dislocation-density crystals (h_type 7, 4)
 
 _lib = None
 
@@ -293,7 +293,7 @@ def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
     A = np.zeros(81)
     sig = np.zeros(6)
     cep = np.zeros(36)
-    h1 = np.zeros(HIST_WORDS_MRR if crystal["h_type"] == 7 else HIST_WORDS)
+    h1 = np.zeros(HIST_WORDS_MRR if crystal["h_type"] in (4, 7) else HIST_WORDS)
     k = np.ascontiguousarray(kocks, dtype=np.float64)
     fn = np.ascontiguousarray(Fn, dtype=np.float64).reshape(9)
     fn1 = np.ascontiguousarray(Fn1, dtype=np.float64).reshape(9)

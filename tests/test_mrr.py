@@ -1,9 +1,11 @@
-"""Ma-Roters-Raabe hardening (h_type 7: mm10_slipinc_mrr .. mm10_dgdd_mrr,
-src/mm10_b.f:2343-3325; mm10_init_mrr, src/mm10_a.f:2205-2223): twelve dislocation
-densities as the slip resistance variables, a (6 + 12)-unknown local Newton.  The oracle
-against the reference's interaction tables, the Jacobian against central differences
-(exact derivatives) and the reference's formulas' known mismatch, the local solve's
-convergence, and the GPU kernel (stress_mrr.cu) against the oracle."""
+"""Dislocation-density hardening: Ma-Roters-Raabe (h_type 7: mm10_slipinc_mrr ..
+mm10_dgdd_mrr, src/mm10_b.f:2343-3325; mm10_init_mrr, src/mm10_a.f:2205-2223) and ORNL
+(h_type 4: mm10_slipinc_ornl .. mm10_dgdd_ornl, src/mm10_b.f:3330-4370): twelve
+dislocation densities as the slip resistance variables, a (6 + 12)-unknown local Newton.
+The oracle against the reference's interaction tables, the Jacobian against central
+differences (exact derivatives) and the reference's formulas' known mismatch, the local
+solve's convergence, and the GPU kernels (stress_mrr.cu, stress_ornl.cu) against the
+oracle."""
 import os
 
 import numpy as np
@@ -11,7 +13,8 @@ import pytest
 
 from cpfft_gb300 import rve
 
-MRR = rve.MRR_FCC
+LAWS = {"mrr": rve.MRR_FCC, "ornl": rve.ORNL_FCC}
+law = pytest.mark.parametrize("law", sorted(LAWS))
 KOCKS = np.array([20.0, 35.0, 50.0])
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "mrr_gh_fcc.npz")
 
@@ -53,13 +56,14 @@ def fd_jacobian(oracle, crystal, x, D, hs=1e-4):
     return J
 
 
-def test_exact_jacobian_against_finite_differences(oracle):
+@law
+def test_exact_jacobian_against_finite_differences(oracle, law):
     """exact_j22 = 1: the 18 x 18 Jacobian differentiates the residual (rows scaled by their
     largest entry; rows of systems that do not slip are at the differences' noise floor)."""
     D = np.array([1e-3, -4e-4, -6e-4, 2e-4, 1e-4, -1e-4])
     x = initial_x(np.random.default_rng(0))
-    R, J = oracle.mrr_residual(MRR, KOCKS, D, 1.0, x)
-    Jfd = fd_jacobian(oracle, MRR, x, D)
+    R, J = oracle.mrr_residual(LAWS[law], KOCKS, D, 1.0, x)
+    Jfd = fd_jacobian(oracle, LAWS[law], x, D)
     rowmax = np.maximum(np.abs(Jfd).max(axis=1), np.abs(J).max(axis=1))
     sig = rowmax > 1e-3
     err = np.abs(J - Jfd)[sig] / rowmax[sig][:, None]
@@ -68,27 +72,29 @@ def test_exact_jacobian_against_finite_differences(oracle):
     assert (np.abs(J[:6] - Jfd[:6]) / rowmax[:6, None]).max() < 1e-5
 
 
-def test_reference_jacobian_differs_where_the_reference_does(oracle):
+@law
+def test_reference_jacobian_differs_where_the_reference_does(oracle, law):
     """exact_j22 = 0 takes the reference's mm10_estress_mrr / mm10_ehard_mrr: sqrt(rho_F)
     where mm10_h_mrr has sqrt(rho_P) (src/mm10_b.f:2635 against :2952, :3075).  Its
     stress rows agree with the exact ones; its density rows do not."""
     D = np.array([1e-3, -4e-4, -6e-4, 2e-4, 1e-4, -1e-4])
     x = initial_x(np.random.default_rng(0))
-    _, Je = oracle.mrr_residual(MRR, KOCKS, D, 1.0, x)
-    _, Jr = oracle.mrr_residual(dict(MRR, exact_j22=0), KOCKS, D, 1.0, x)
+    _, Je = oracle.mrr_residual(LAWS[law], KOCKS, D, 1.0, x)
+    _, Jr = oracle.mrr_residual(dict(LAWS[law], exact_j22=0), KOCKS, D, 1.0, x)
     assert np.abs(Je[:6] - Jr[:6]).max() == 0.0
     scale = np.abs(Je[6:, :6]).max()
     assert np.abs(Je[6:, :6] - Jr[6:, :6]).max() > 1e-2 * scale
 
 
-def test_local_solve_converges_to_the_residual_root(oracle):
+@law
+def test_local_solve_converges_to_the_residual_root(oracle, law):
     """First implicit pass of step 1 (rotation-free stretch, Rp = I): the converged
     (sigma, rho) zeroes the residual; exact and reference Jacobians reach the same state,
     the exact one in fewer iterations."""
     F1 = stretch(np.eye(3), 2e-3)
     out = {}
     for ex in (1, 0):
-        cr = dict(MRR, exact_j22=ex)
+        cr = dict(LAWS[law], exact_j22=ex)
         r = oracle.voxel_update(cr, KOCKS, 1.0, 1, 1, np.eye(3), F1)
         assert r["iters"] > 0
         h = r["hist"]
@@ -102,7 +108,8 @@ def test_local_solve_converges_to_the_residual_root(oracle):
     assert out[1][1] < out[0][1]
 
 
-def test_densities_grow_under_monotonic_loading(oracle):
+@law
+def test_densities_grow_under_monotonic_loading(oracle, law):
     """Ten plastic steps: the local Newton converges in a few iterations each, the stress
     saturates below the elastic line and the densities of the active systems grow (those
     of systems that barely slip may lose a little to annihilation)."""
@@ -110,44 +117,46 @@ def test_densities_grow_under_monotonic_loading(oracle):
     rho0 = None
     for step in range(1, 11):
         F1 = stretch(F0)
-        r = oracle.voxel_update(MRR, KOCKS, 1.0, step, 1, F0, F1, hist)
+        r = oracle.voxel_update(LAWS[law], KOCKS, 1.0, step, 1, F0, F1, hist)
         assert 0 < r["iters"] <= 6, (step, r["iters"])
         if rho0 is None:
             rho0 = r["hist"][31:43].copy()
         hist, F0 = r["hist"], F1
     rho = hist[31:43]
-    assert rho.min() > (1 - 1e-6) * rho0.min() and rho.max() > 1.5 * MRR["theta_0"]
+    assert rho.min() > (1 - 1e-6) * rho0.min() and rho.max() > 1.5 * LAWS[law]["theta_0"]
     assert 100.0 < hist[0] < 400.0
 
 
-def test_tangent_against_finite_differences(oracle):
+@law
+def test_tangent_against_finite_differences(oracle, law):
     """dP/dF of a plastic step (exact local Jacobian: T = (J11 - J12 J22^-1 J21)^-1 C)
     against a central difference of P."""
     hist, Fs = None, [np.eye(3)]
     for step in (1, 2, 3):
         F1 = stretch(Fs[-1])
-        hist = oracle.voxel_update(MRR, KOCKS, 1.0, step, 1, Fs[-1], F1, hist)["hist"]
+        hist = oracle.voxel_update(LAWS[law], KOCKS, 1.0, step, 1, Fs[-1], F1, hist)["hist"]
         Fs.append(F1)
     rng = np.random.default_rng(1)
     Fa = Fs[-1]
     Fb = stretch(Fa) + 2e-4 * rng.standard_normal((3, 3))
-    r = oracle.voxel_update(MRR, KOCKS, 1.0, 4, 1, Fa, Fb, hist)
+    r = oracle.voxel_update(LAWS[law], KOCKS, 1.0, 4, 1, Fa, Fb, hist)
     d = 1e-7
     Afd = np.zeros((9, 9))
     for m in range(9):
         e = np.zeros(9)
         e[m] = d
-        Pp = oracle.voxel_update(MRR, KOCKS, 1.0, 4, 1, Fa, Fb + e.reshape(3, 3), hist)["P"]
-        Pm = oracle.voxel_update(MRR, KOCKS, 1.0, 4, 1, Fa, Fb - e.reshape(3, 3), hist)["P"]
+        Pp = oracle.voxel_update(LAWS[law], KOCKS, 1.0, 4, 1, Fa, Fb + e.reshape(3, 3), hist)["P"]
+        Pm = oracle.voxel_update(LAWS[law], KOCKS, 1.0, 4, 1, Fa, Fb - e.reshape(3, 3), hist)["P"]
         Afd[:, m] = (Pp - Pm) / (2 * d)
     # the tangent is symmetrised (mm10_a_make_symm_1) and neglects the rotation update
     assert np.abs(r["A"] - Afd).max() < 2e-2 * np.abs(Afd).max()
 
 
-def test_oracle_load_steps(oracle):
-    """Whole load steps of a 5^3 MRR grid in the oracle: the Newton loop converges."""
+@law
+def test_oracle_load_steps(oracle, law):
+    """Whole load steps of a 5^3 LAWS[law] grid in the oracle: the Newton loop converges."""
     N = 5
-    r = rve.make_rve(N, 3, 94, MRR)
+    r = rve.make_rve(N, 3, 94, LAWS[law])
     load = rve.prescribed_stretch([0.003, -0.0015, -0.0015], 3)
     o = oracle.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 0, nthreads=4)
     try:
@@ -166,12 +175,13 @@ def per_voxel_rel(a, b):
 
 
 @pytest.mark.gpu
+@law
 @pytest.mark.parametrize("exact", [1, 0])
-def test_gpu_mrr_stress_update_parity(gpulib, oracle, exact):
-    """P, dP/dF and the twelve densities and rates of the GPU MRR kernel against the oracle
+def test_gpu_mrr_stress_update_parity(gpulib, oracle, law, exact):
+    """P, dP/dF and the twelve densities and rates of the GPU LAWS[law] kernel against the oracle
     over the passes of two steps, with the exact and with the reference's Jacobian."""
     N = 5
-    crystal = dict(MRR, exact_j22=exact)
+    crystal = dict(LAWS[law], exact_j22=exact)
     r = rve.make_rve(N, 4, 95, crystal)
     s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_REF_SHIFT)
     o = oracle.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 0, nthreads=8)
@@ -201,11 +211,12 @@ def test_gpu_mrr_stress_update_parity(gpulib, oracle, exact):
 
 
 @pytest.mark.gpu
-def test_gpu_mrr_load_steps(gpulib, oracle):
+@law
+def test_gpu_mrr_load_steps(gpulib, oracle, law):
     """Whole load steps (7^3, uniaxial-strain stretch 1e-3 a step): P_bar and Newton
     counts against the oracle."""
     N = 7
-    r = rve.make_rve(N, 6, 96, MRR)
+    r = rve.make_rve(N, 6, 96, LAWS[law])
     load = rve.prescribed_stretch([0.004, -0.002, -0.002], 4)
     s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_REF_SHIFT)
     o = oracle.Oracle(N, r.mat_list, r.kocks, r.crystals, 1.0, 0, nthreads=8)
@@ -224,11 +235,12 @@ def test_gpu_mrr_load_steps(gpulib, oracle):
 
 
 @pytest.mark.gpu
-def test_gpu_mrr_mixed_form(gpulib, oracle):
+@law
+def test_gpu_mrr_mixed_form(gpulib, oracle, law):
     """The fast form (FP32 inner Krylov with the reference-medium preconditioner, FP32
-    tangent, voxel queue) on an MRR grid: P_bar within 1e-6 of the plain oracle."""
+    tangent, voxel queue) on an LAWS[law] grid: P_bar within 1e-6 of the plain oracle."""
     N = 8
-    r = rve.make_rve(N, 6, 97, MRR)
+    r = rve.make_rve(N, 6, 97, LAWS[law])
     load = rve.prescribed_stretch([0.004, -0.002, -0.002], 4)
     s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_CENTERED,
                       gpulib.PREC_MIXED)
