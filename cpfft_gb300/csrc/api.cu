@@ -710,10 +710,17 @@ int cg64(Ctx* c, const double* b, double* x, double tol, int* iters) {
 
 // Mixed precision: FP32 Green/FFT/CG inner solves corrected by an FP64 outer residual
 // (iterative refinement).  Same stop test on the FP64 residual as cg64.
+// Reduction of the residual norm per segment of FP32 iterations before a reliable
+// update.  Tight solves take 1e-2 (1e-3 lets the FP32 recursion drift until the solve
+// stagnates, measured at 128^3); a solve to tol >= 1e-4 runs in one segment to its
+// tolerance, where the recursion's drift (about 1e-7 of the starting residual) stays
+// far below what the solve asks.
+double reliable_delta(double tol) { return tol >= 1.0e-4 ? std::min(1.0e-2, 0.5 * tol) : 1.0e-2; }
+
 int cg_mixed(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
   const long long n = 9 * c->N3;
   const int maxIter = 2000;     // FP32 iterations (the FP64 path's cap is 1000)
-  const double delta = 1.0e-2;  // reliable-update threshold
+  const double delta = reliable_delta(tol);  // reliable-update threshold
   *iters = 0;
   if (!use_x0) CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
   double n2b;
@@ -941,9 +948,8 @@ int cg_segment(Ctx* c, double rr, double rn, double tolb, double tol, double del
 int cg_mixed_pre(Ctx* c, const double* b, double* x, double tol, int* iters, bool use_x0) {
   const long long n = 9 * c->N3;
   const int maxIter = 2000;
-  // reduction of <r,r>_K0 per segment before a reliable update; 1e-3 lets the FP32
-  // recursion drift until the solve stagnates (measured at 128^3)
-  const double delta = 1.0e-2;
+  // reduction of <r,r>_K0 per segment before a reliable update (reliable_delta)
+  const double delta = reliable_delta(tol);
   *iters = 0;
   if (!use_x0) CK(cudaMemsetAsync(x, 0, n * sizeof(double), c->st));
   double n2b;
