@@ -305,7 +305,8 @@ def counts(run):
             "res_equil": [s["res_equil"] for s in st], "res_fft": [s["res_fft"] for s in st],
             "local_iters_per_voxel_pass": sum(s["local_iters"] for s in st) / (N3 * su),
             "predict_iters_per_voxel_pass": sum(s["predict_iters"] for s in st) / (N3 * su),
-            "local_fallbacks": sum(s["local_fallbacks"] for s in st)}
+            "local_fallbacks": sum(s["local_fallbacks"] for s in st),
+            "s_device_per_step": [s["t_device"] for s in st]}
 
 
 def roofline(run, N, peaks, peak_kind, fp64_peak):

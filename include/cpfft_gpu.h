@@ -379,7 +379,7 @@ int cpfft_set_tangent_tol(double tol);
  * with an explicit stress pass (src/FFT_nr3.f:75-171).  Here every Newton iteration also
  * updates the prescribed-stress components of F_bar with NBC_update's system and solves
  * the fluctuation for both changes, one Newton step on the coupled system (C_homo, its
- * Schur complement, recomputed after the first two implicit stress passes).  The step ends
+ * Schur complement, recomputed after the first implicit stress pass).  The step ends
  * on the nested loops' final tests: P_bar within tolNR, the equilibrium residual within
  * its tolerance, the last increment within tolNR.  Default off.
  */

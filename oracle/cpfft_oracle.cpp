@@ -2446,7 +2446,7 @@ void orc_set_coupled_bc(orc_ctx* c, int on) { c->coupled_bc = on != 0; }
 
 // The library's coupled P_bar update (cpfft_set_coupled_bc, an extension restated here
 // for its parity tests): after each stress pass, DbarF from NBC_update's system with the
-// current C_homo (recomputed after the first two implicit passes), then the fluctuation
+// current C_homo (recomputed after the first implicit pass), then the fluctuation
 // solves G(K : dF) = -G(P) - G(K : DbarF); increments that raise the equilibrium residual
 // are halved (at most 4 times in a row); the step ends when P_bar, the equilibrium
 // residual and the last increment all meet their tolerances.
@@ -2491,7 +2491,7 @@ static int coupled_step(orc_ctx* c, int step, const double* PBC, const int* isNB
     eq_prev = e;
     halvings = 0;
     frac = 1.0;
-    if (k >= 1 && tangents < 2) {
+    if (k >= 1 && tangents < 1) {
       int th = orc_tangent_homo(c, tolPCG, c->C_homo);
       if (th < 0) return th;
       S.cg_solves += 9; S.cg_iters += th;
