@@ -864,14 +864,28 @@ void build_cg_graph(Ctx* c) {
   if (cudaGraphCreate(&g, 0) != cudaSuccess) { cudaGetLastError(); return; }
   cudaGraphConditionalHandle h;
   cudaGraphNodeParams prm = {};
-  cudaGraphNode_t node;
+  cudaGraphNode_t node, gate = nullptr;
   bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  // the gate kernel, then the WHILE node after it
+  if (ok) {
+    ok = cudaStreamBeginCaptureToGraph(c->st, g, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+      const cudaError_t e1 = dev_cg_gate(c->sc, h, c->st);
+      g_kernel_launches -= 1;
+      cudaGraph_t out = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(c->st, &out);
+      size_t nn = 1;
+      ok = e1 == cudaSuccess && e2 == cudaSuccess &&
+           cudaGraphGetNodes(g, &gate, &nn) == cudaSuccess && nn == 1;
+    }
+  }
   if (ok) {
     prm.type = cudaGraphNodeTypeConditional;
     prm.conditional.handle = h;
     prm.conditional.type = cudaGraphCondTypeWhile;
     prm.conditional.size = 1;
-    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &prm) == cudaSuccess;
+    ok = cudaGraphAddNode(&node, g, &gate, nullptr, 1, &prm) == cudaSuccess;
   }
   if (ok) {
     cudaGraph_t body = prm.conditional.phGraph_out[0];
@@ -921,15 +935,16 @@ int cg_segment(Ctx* c, double rr, double rn, double tolb, double tol, double del
   for (;;) {
     TRY(cg_pre_body(c, false, done == 0));
     done++;
-    double st;
-    TRY(read_scalar(c, SC_STOP, &st));
-    if (st != 0.0) break;
-    if (c->cg_graph_state == 1) {
+    if (c->cg_graph_state == 1) {  // the graph's gate skips its loop if already stopped
       kt_start(c, KT_CGGRAPH);
       CK(cudaGraphLaunch(c->cg_exec, c->st));
       TRY(kt_stop(c));
+      g_kernel_launches += 1;
       break;
     }
+    double st;
+    TRY(read_scalar(c, SC_STOP, &st));
+    if (st != 0.0) break;
   }
   CK(cudaMemcpyAsync(h + SC_CNT, c->sc + SC_CNT, (SC_STOP - SC_CNT + 1) * sizeof(double),
                      cudaMemcpyDeviceToHost, c->st));
@@ -1219,51 +1234,46 @@ int tangent_solve_f32(Ctx* c, int i, double tol, int* its) {
                                           nullptr, &np), "green_apply fp32"));
     return kt_stop(c);
   };
-  auto norm_f = [&](const float* v, double* out) -> int {
-    CK(dev_dot_f(v, v, n, c->part, c->sc, SC_TMP, OP_STORE, c->st));
-    double d;
-    TRY(read_scalar(c, SC_TMP, &d));
-    *out = std::sqrt(d);
-    return 0;
-  };
-  // ||b|| = ||G(K : E_i)||
+  // b = G(K : E_i), the start's residual w = -G(K : (E_i + x0)), their squared norms, the
+  // preconditioned residual rf = G0(w) and <rf, rf>_K0, read back in one transfer (the
+  // recursion needs no normalisation: its stop test uses ratios)
   CK(cudaMemsetAsync(c->io, 0, n * sizeof(double), c->st));
   CK(dev_add_const(c->io + i * N3, 1.0, N3, c->st));
   CK(dev_to_f32(c->pf, c->io, 1.0, n, c->st));
   TRY(apply(c->pf, c->rf));
-  double nb, rn;
-  TRY(norm_f(c->rf, &nb));
-  // residual of the start: w = -G(K : (E_i + x0))
+  CK(dev_dot_f(c->rf, c->rf, n, c->part, c->sc, SC_T1, OP_STORE, c->st));
   if (c->th_valid) {
     CK(dev_add_f32(c->io, x0, 1.0, n, c->st));
     CK(dev_to_f32(c->pf, c->io, 1.0, n, c->st));
     TRY(apply(c->pf, c->Apf));
-    TRY(norm_f(c->Apf, &rn));
   } else {
     CK(cudaMemcpyAsync(c->Apf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
-    rn = nb;
   }
+  CK(dev_scale_f(c->Apf, -1.0f, n, c->st));
+  CK(dev_dot_f(c->Apf, c->Apf, n, c->part, c->sc, SC_T2, OP_STORE, c->st));
+  TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
+  CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
+  CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+  CK(dev_dot_k0(c->rf, c->rf, c->N3, c->pre_dev + 36, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
+  CK(cudaMemcpyAsync(c->h_sc + SC_RRNEW, c->sc + SC_RRNEW, (SC_T2 - SC_RRNEW + 1) * sizeof(double),
+                     cudaMemcpyDeviceToHost, c->st));
+  TRY(sync(c));
+  const double nb = std::sqrt(c->h_sc[SC_T1]), rn = std::sqrt(c->h_sc[SC_T2]);
+  const double rr = c->h_sc[SC_RRNEW];
   *its = 0;
-  if (!std::isfinite(rn) || !std::isfinite(nb)) {
+  if (!std::isfinite(rn) || !std::isfinite(nb) || !std::isfinite(rr)) {
     cpfft_set_error("non-finite tangent right-hand side");
     return CPFFT_ERR_NONFINITE;
   }
-  if (rn > tol * nb && rn > 0.0) {
-    const double scale = 1.0 / rn;
-    CK(dev_scale_f(c->Apf, (float)(-scale), n, c->st));
-    TRY(matvec32_pre(c, c->Apf, c->rf, 0, false));
-    CK(cudaMemsetAsync(c->xf, 0, n * sizeof(float), c->st));
-    CK(cudaMemcpyAsync(c->pf, c->rf, n * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
-    CK(dev_dot_k0(c->rf, c->rf, c->N3, c->pre_dev + 36, c->part, c->sc, SC_RRNEW, OP_STORE, c->st));
-    double rr, rr_out, rr_prev;
-    TRY(read_scalar(c, SC_RRNEW, &rr));
+  if (rn > tol * nb && rr > 0.0) {
+    double rr_out, rr_prev;
     int it = 0, stop = 0;
     TRY(cg_segment(c, rr, rn, tol * nb, 0.0, 0.0, 0, 2000, 0.0, &rr_out, &rr_prev, &it, &stop));
     if (stop == STOP_NONFINITE) { cpfft_set_error("FP32 CG residual is not finite"); return CPFFT_ERR_NONFINITE; }
     if (stop == STOP_MAXIT) { cpfft_set_error("tangent_homo: FP32 CG did not converge"); return CPFFT_ERR_CG_MAXIT; }
     *its = it;
     c->cg_iters += it;
-    CK(dev_add_f32(c->io, c->xf, 1.0 / scale, n, c->st));  // io = E_i + x0 + correction
+    CK(dev_add_f32(c->io, c->xf, 1.0, n, c->st));  // io = E_i + x0 + correction
   }
   c->cg_solves++;
   // th_x = x = io - E_i
@@ -2085,6 +2095,11 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
   // residual has grown is halved, at most 4 times in a row (lastD: its F_bar part)
   double eq_prev = HUGE_VAL, frac = 1.0, lastD[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int halvings = 0;
+  // ||dF||^2 of the last solve is summed into SC_T1 on the device and read back with the
+  // next equilibrium residual (one host wait fewer per iteration)
+  bool pending_dn = false;
+  double pending_db = 0.0;
+  int pending_its = 0, pending_fails = 0;
   for (int k = 0;; k++) {
     auto a = clk::now();
     long long li, pi = 0, rj = 0;
@@ -2098,8 +2113,18 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
     S.stress_updates++;
     TRY(matvec_acc(c, c->P, c->b, 0));
     double e;
-    TRY(equil_residual(c, c->b, &e));  // also leaves sum(P) in h_sc
+    TRY(equil_residual(c, c->b, &e));  // also leaves sum(P) and SC_T1 in h_sc
     S.res_equil = e;
+    if (pending_dn) {
+      resfft = std::sqrt(c->h_sc[SC_T1] + (double)N3 * pending_db) / Fnorm;
+      pending_dn = false;
+      if (!std::isfinite(resfft)) { cpfft_set_error("Newton residual is not finite"); return CPFFT_ERR_NONFINITE; }
+      S.newton_iters++;
+      S.res_fft = resfft;
+      if (c->log)
+        fprintf(stderr, "       Iteration %5d  residual %10.3e  (cg %d, local fallbacks %d)\n", k - 1,
+                resfft, pending_its, pending_fails);
+    }
     double res1 = 0, res2 = 0;
     for (int i = 0; i < 9; i++) {
       c->P_bar[i] = c->h_sc[SC_SUM9 + i] / (double)N3;
@@ -2173,17 +2198,12 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
     c->cg_rel_only = false;
     tp += sec(a);
     CK(dev_axpy(c->Fn1, c->dFm, 1.0, n, c->st));
-    double dn;
-    TRY(dnrm2(c, c->dFm, &dn));
-    double db = 0;
-    for (int i = 0; i < 9; i++) db += DbarF[i] * DbarF[i];
-    resfft = std::sqrt(dn * dn + (double)N3 * db) / Fnorm;
-    if (!std::isfinite(resfft)) { cpfft_set_error("Newton residual is not finite"); return CPFFT_ERR_NONFINITE; }
-    S.newton_iters++;
-    S.res_fft = resfft;
-    if (c->log)
-      fprintf(stderr, "       Iteration %5d  residual %10.3e  (cg %d, local fallbacks %d)\n", k,
-              resfft, its, fails);
+    CK(dev_dot(c->dFm, c->dFm, n, c->part, c->sc, SC_T1, OP_STORE, c->st));
+    pending_db = 0.0;
+    for (int i = 0; i < 9; i++) pending_db += DbarF[i] * DbarF[i];
+    pending_dn = true;
+    pending_its = its;
+    pending_fails = fails;
   }
   S.nbc_iters = 1;
   return 0;

@@ -321,6 +321,13 @@ __global__ void k_cg_cond(double* __restrict__ sc, cudaGraphConditionalHandle h,
   if (use_handle) cudaGraphSetConditional(h, stop == STOP_NONE ? 1u : 0u);
 }
 
+// The iteration graph's first node: its WHILE loop runs only if the iterations are not
+// already stopped (an eager first iteration may have met the stop test), so the host
+// launches the graph without reading the stop flag first.
+__global__ void k_cg_gate(const double* __restrict__ sc, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, sc[SC_STOP] == (double)STOP_NONE ? 1u : 0u);
+}
+
 int grid_for(long long n, int bs) {
   long long b = (n + bs - 1) / bs;
   return (int)(b < 1 ? 1 : (b > 2048 ? 2048 : b));
@@ -437,5 +444,10 @@ cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81,
 cudaError_t dev_cg_cond(double* sc, cudaGraphConditionalHandle h, bool use_handle,
                         cudaStream_t st) {
   k_cg_cond<<<1, 1, 0, st>>>(sc, h, use_handle ? 1 : 0);
+  return counted(1);
+}
+
+cudaError_t dev_cg_gate(const double* sc, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_cg_gate<<<1, 1, 0, st>>>(sc, h);
   return counted(1);
 }

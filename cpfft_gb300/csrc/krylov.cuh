@@ -7,6 +7,7 @@ constexpr int NPART = 1024;  // partial sums per reduction (blocks of the first 
 // device scalar slots
 enum {
   SC_RR = 0, SC_PAP = 1, SC_RRNEW = 2, SC_ALPHA = 3, SC_BETA = 4, SC_TMP = 5,
+  SC_T1 = 6, SC_T2 = 7,  // scratch read back with others in one transfer
   SC_SUM9 = 8,     // 9 slots: component sums
   // stop test of a device-driven CG segment (k_cg_cond): <r,r> at the segment start,
   // the true residual norm there, the reference's absolute thresholds, the segment's
@@ -58,3 +59,5 @@ cudaError_t dev_mean81(const float* K, long long N3, double* part, double* sc81,
 // the captured iteration graph (cudaGraphSetConditional); the counter bounds that loop.
 cudaError_t dev_cg_cond(double* sc, cudaGraphConditionalHandle h, bool use_handle,
                         cudaStream_t st);
+// the graph's gate: its WHILE node runs while sc[SC_STOP] is STOP_NONE
+cudaError_t dev_cg_gate(const double* sc, cudaGraphConditionalHandle h, cudaStream_t st);
