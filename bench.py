@@ -796,7 +796,7 @@ def main():
     # fast forms: inexact Newton (each Newton system solved as far as the equilibrium
     # residual needs, at most this relative tolerance; 0 = every solve to the CG tolerance)
     ap.add_argument("--inexact", type=float, default=1e-2)
-    ap.add_argument("--tangent-tol", type=float, default=1e-3,
+    ap.add_argument("--tangent-tol", type=float, default=1e-2,
                     help="relative tolerance of tangent_homo's solves in the fast form")
     ap.add_argument("--nested-bc", dest="coupled_bc", action="store_false",
                     help="fast form: the reference's nested P_bar loop instead of the P_bar "

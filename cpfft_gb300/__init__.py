@@ -343,7 +343,7 @@ class Solver:
         _check(load_library().cpfft_set_coupled_bc(int(bool(on))), "cpfft_set_coupled_bc")
 
     def set_tangent_tol(self, tol):
-        """Relative tolerance of tangent_homo's solves under inexact Newton (default 1e-3)."""
+        """Relative tolerance of tangent_homo's solves under inexact Newton (default 1e-2)."""
         _check(load_library().cpfft_set_tangent_tol(float(tol)), "cpfft_set_tangent_tol")
 
     def set_equilibrium_tol(self, tol):

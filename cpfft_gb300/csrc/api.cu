@@ -390,7 +390,7 @@ struct Ctx {
   // largest relative tolerance of a Newton system's solve
   double eta_max = 0.0;
   // relative tolerance of tangent_homo's solves under inexact Newton (cpfft_set_tangent_tol)
-  double th_tol = 1.0e-3;
+  double th_tol = 1.0e-2;
   // the P_bar update inside the Newton iteration (cpfft_set_coupled_bc)
   bool coupled_bc = false;
   bool cg_rel_only = false;  // the current solve stops on ||r|| <= tol ||b|| alone

@@ -354,7 +354,7 @@ int cpfft_set_equilibrium_tol(double tol);
  * tolerance eta_k = min(eta_max, 0.9 (e_k / e_{k-1})^2) (Eisenstat-Walker's second
  * choice with its safeguard max(eta_k, 0.9 eta_{k-1}^2) when that exceeds 0.1, and no
  * tighter than 0.5 tol / e_k), e_k the equilibrium residual of iterate k; the predictor's
- * system to eta_max and the homogenised tangent's to 1e-3 (cpfft_set_tangent_tol; it
+ * system to eta_max and the homogenised tangent's to 1e-2 (cpfft_set_tangent_tol; it
  * only steers the P_bar update), never below tolPCG.  The loop still ends on the equilibrium test, so the
  * converged state meets the same tolerance with fewer Krylov iterations.  eta_max = 0
  * (the default) solves every system to tolPCG.
@@ -363,12 +363,12 @@ int cpfft_set_inexact_newton(double eta_max);
 
 /*
  * Relative tolerance of tangent_homo's 9 solves under inexact Newton (extension; default
- * 1e-3, never below tolPCG).  C_homo only steers the P_bar update of the mixed boundary
+ * 1e-2, never below tolPCG).  C_homo only steers the P_bar update of the mixed boundary
  * conditions (src/FFT_nr3.f:150-170), whose loop tests P_bar itself, so a looser
  * tangent can cost P_bar iterations but does not change what the step converges to
- * (128^3 plane-strain compression: the same 3 P_bar passes per step from 1e-6 to 1e-2,
- * P_bar within 3e-10 of the 1e-6 solves at 1e-3).  Without inexact Newton the solves use
- * tolPCG as the reference does.
+ * (128^3 plane-strain compression: the same P_bar and Newton counts from 1e-6 to 1e-2,
+ * P_bar within 5e-9 of the 1e-6 solves).  Without inexact Newton the solves use tolPCG
+ * as the reference does.
  */
 int cpfft_set_tangent_tol(double tol);
 
