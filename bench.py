@@ -225,7 +225,7 @@ def make_solver(cp, r, form, args):
                 s.set_inexact_newton(args.inexact)
                 s.set_tangent_tol(args.tangent_tol)
             if args.coupled_bc:
-                s.set_coupled_bc(True)
+                s.set_coupled_bc(2 if args.implicit_first else 1)
     return s
 
 
@@ -801,6 +801,9 @@ def main():
     ap.add_argument("--nested-bc", dest="coupled_bc", action="store_false",
                     help="fast form: the reference's nested P_bar loop instead of the P_bar "
                          "update inside the Newton iteration")
+    ap.add_argument("--implicit-first", action="store_true",
+                    help="fast form: the step's first stress pass implicit (no explicit "
+                         "elastic predictor pass)")
     ap.add_argument("--curve", default=None,
                     help="write P_bar of every load step of both forms to this JSON file")
     ap.add_argument("--fp64-steps", type=int, default=5,

@@ -339,8 +339,9 @@ class Solver:
 
     def set_coupled_bc(self, on=True):
         """Update the prescribed-stress components of F_bar inside the Newton iteration
-        (with set_equilibrium_tol)."""
-        _check(load_library().cpfft_set_coupled_bc(int(bool(on))), "cpfft_set_coupled_bc")
+        (with set_equilibrium_tol); on = 2 also makes the step's first stress pass
+        implicit."""
+        _check(load_library().cpfft_set_coupled_bc(int(on)), "cpfft_set_coupled_bc")
 
     def set_tangent_tol(self, tol):
         """Relative tolerance of tangent_homo's solves under inexact Newton (default 1e-2)."""

@@ -391,8 +391,9 @@ struct Ctx {
   double eta_max = 0.0;
   // relative tolerance of tangent_homo's solves under inexact Newton (cpfft_set_tangent_tol)
   double th_tol = 1.0e-2;
-  // the P_bar update inside the Newton iteration (cpfft_set_coupled_bc)
-  bool coupled_bc = false;
+  // the P_bar update inside the Newton iteration (cpfft_set_coupled_bc: 0 off, 1 on,
+  // 2 on with an implicit first stress pass)
+  int coupled_bc = 0;
   bool cg_rel_only = false;  // the current solve stops on ||r|| <= tol ||b|| alone
   // counters of the last stress pass: local iterations, fallbacks, predictor iterations,
   // starts dropped, sub-stepped solves (cpfft_pass_counts)
@@ -1783,7 +1784,11 @@ int cpfft_set_inexact_newton(double eta_max) {
 
 int cpfft_set_coupled_bc(int on) {
   TRY(need_ctx());
-  g_ctx->coupled_bc = on != 0;
+  if (on < 0 || on > 2) {
+    cpfft_set_error("cpfft_set_coupled_bc: mode must be 0, 1 or 2");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  g_ctx->coupled_bc = on;
   return 0;
 }
 
@@ -2104,7 +2109,8 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
     auto a = clk::now();
     long long li, pi = 0, rj = 0;
     int fails;
-    TRY(stress(c, step, k, &li, &fails, &pi, &rj));
+    // mode 2: no explicit opening pass (the stress kernel's iteration 0)
+    TRY(stress(c, step, c->coupled_bc == 2 ? k + 1 : k, &li, &fails, &pi, &rj));
     ts += sec(a);
     S.predict_iters += pi;
     S.guess_rejected += rj;
@@ -2160,7 +2166,7 @@ int coupled_step(Ctx* c, int step, const double* PBC, const int* isNBC, double* 
     frac = 1.0;
     // the Schur complement at the first implicit state (tangent_homo's solves use the b
     // buffer: G(P) is formed again after it)
-    if (k >= 1 && tangents < 1) {
+    if (k >= (c->coupled_bc == 2 ? 0 : 1) && tangents < 1) {
       a = clk::now();
       int th;
       TRY(tangent_homo(c, inexact ? std::max(tolPCG, c->th_tol) : tolPCG, c->C_homo, &th));

@@ -381,7 +381,9 @@ int cpfft_set_tangent_tol(double tol);
  * the fluctuation for both changes, one Newton step on the coupled system (C_homo, its
  * Schur complement, recomputed after the first implicit stress pass).  The step ends
  * on the nested loops' final tests: P_bar within tolNR, the equilibrium residual within
- * its tolerance, the last increment within tolNR.  Default off.
+ * its tolerance, the last increment within tolNR.  on = 2 also makes the step's first
+ * stress pass implicit (the reference's iteration 0 is an explicit elastic predictor).
+ * Default off.
  */
 int cpfft_set_coupled_bc(int on);
 
