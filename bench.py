@@ -558,7 +558,8 @@ def config_dict(args, impl):
                            "inexact_newton_eta_max": (args.inexact if inexact else 0.0),
                            "tangent_homo": (max(args.tangent_tol, 1e-10) if inexact
                                             else 1e-10)},
-            "p_bar_update": ("inside the Newton iteration (coupled)"
+            "p_bar_update": (("inside the Newton iteration (coupled), first stress pass "
+                              + ("implicit" if args.implicit_first else "explicit"))
                              if fast and args.mode != "fp64" and args.coupled_bc
                              and args.tol_equil > 0 else "nested loop (the reference's)"),
             "l2": "inputs larger than L2 (fields >= 150 MB, K4 1.4 GB)",
@@ -801,9 +802,9 @@ def main():
     ap.add_argument("--nested-bc", dest="coupled_bc", action="store_false",
                     help="fast form: the reference's nested P_bar loop instead of the P_bar "
                          "update inside the Newton iteration")
-    ap.add_argument("--implicit-first", action="store_true",
-                    help="fast form: the step's first stress pass implicit (no explicit "
-                         "elastic predictor pass)")
+    ap.add_argument("--explicit-first", dest="implicit_first", action="store_false",
+                    help="fast form: open each step with the reference's explicit elastic "
+                         "predictor pass (default: the first stress pass is implicit)")
     ap.add_argument("--curve", default=None,
                     help="write P_bar of every load step of both forms to this JSON file")
     ap.add_argument("--fp64-steps", type=int, default=5,

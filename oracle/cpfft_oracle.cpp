@@ -2085,7 +2085,7 @@ struct orc_ctx {
   // FFT_nr3 persistent locals (Fortran DATA => SAVE'd, src/FFT_nr3.f:29-34)
   double barF_t[9], P_bar[9], C_homo[81];
   double eq_tol = 0.0;  // equilibrium stop test of the Newton loop (0: the reference's loop)
-  bool coupled_bc = false;  // the P_bar update inside the Newton iteration
+  int coupled_bc = 0;  // the P_bar update inside the Newton iteration (2: implicit first pass)
   int hist_words = ORC_HIST;  // ORC_HIST_MRR on grids of Ma-Roters-Raabe crystals
 };
 
@@ -2442,11 +2442,12 @@ static double equil_residual(const orc_ctx* c, const double* g) {
 }
 
 void orc_set_equilibrium_tol(orc_ctx* c, double tol) { c->eq_tol = tol; }
-void orc_set_coupled_bc(orc_ctx* c, int on) { c->coupled_bc = on != 0; }
+void orc_set_coupled_bc(orc_ctx* c, int on) { c->coupled_bc = on; }
 
 // The library's coupled P_bar update (cpfft_set_coupled_bc, an extension restated here
-// for its parity tests): after each stress pass, DbarF from NBC_update's system with the
-// current C_homo (recomputed after the first implicit pass), then the fluctuation
+// for its parity tests; mode 2 makes the first stress pass implicit): after each stress
+// pass, DbarF from NBC_update's system with the current C_homo (recomputed after the
+// first implicit pass), then the fluctuation
 // solves G(K : dF) = -G(P) - G(K : DbarF); increments that raise the equilibrium residual
 // are halved (at most 4 times in a row); the step ends when P_bar, the equilibrium
 // residual and the last increment all meet their tolerances.
@@ -2461,7 +2462,8 @@ static int coupled_step(orc_ctx* c, int step, const double* PBC, const int* isNB
   int halvings = 0;
   for (int k = 0;; k++) {
     long long li = 0;
-    S.local_fallbacks += orc_stress_update(c, step, k, nullptr, nullptr, nullptr, nullptr, &li);
+    const int iter = c->coupled_bc == 2 ? k + 1 : k;  // mode 2: no explicit opening pass
+    S.local_fallbacks += orc_stress_update(c, step, iter, nullptr, nullptr, nullptr, nullptr, &li);
     S.local_iters += li;
     S.stress_updates++;
     orc_green_apply(c, c->Pn1.data(), g.data(), 0, nullptr);
@@ -2491,7 +2493,7 @@ static int coupled_step(orc_ctx* c, int step, const double* PBC, const int* isNB
     eq_prev = e;
     halvings = 0;
     frac = 1.0;
-    if (k >= 1 && tangents < 1) {
+    if (k >= (c->coupled_bc == 2 ? 0 : 1) && tangents < 1) {
       int th = orc_tangent_homo(c, tolPCG, c->C_homo);
       if (th < 0) return th;
       S.cg_solves += 9; S.cg_iters += th;

@@ -59,7 +59,8 @@ int  orc_tangent_homo(orc_ctx* c, double tolPCG, double* C_homo);
 int  orc_nr3_begin(orc_ctx* c, double tolPCG);
 /* the library's equilibrium stop test of the Newton loop (cpfft_set_equilibrium_tol) */
 void orc_set_equilibrium_tol(orc_ctx* c, double tol);
-/* the library's P_bar update inside the Newton iteration (cpfft_set_coupled_bc) */
+/* the library's P_bar update inside the Newton iteration (cpfft_set_coupled_bc: 0 off,
+ * 1 on, 2 on with an implicit first stress pass) */
 void orc_set_coupled_bc(orc_ctx* c, int on);
 /* one load step of FFT_nr3 */
 int  orc_nr3_step(orc_ctx* c, int step, const double* BC, const int* isNBC,

@@ -219,7 +219,7 @@ class Oracle:
         lib().orc_set_equilibrium_tol(self.h, float(tol))
 
     def set_coupled_bc(self, on=True):
-        lib().orc_set_coupled_bc(self.h, int(bool(on)))
+        lib().orc_set_coupled_bc(self.h, int(on))
 
     def nr3_begin(self, tolPCG):
         return lib().orc_nr3_begin(self.h, tolPCG)

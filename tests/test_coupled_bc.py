@@ -23,15 +23,17 @@ def run_oracle(oracle, r, load, coupled, steps, N):
         o.close()
 
 
-def test_oracle_coupled_against_nested(oracle):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_oracle_coupled_against_nested(oracle, mode):
     """9^3 plane-strain compression, 3 steps: both reach P_bar within tolNR of the
-    prescribed stresses and the equilibrium tolerance; the coupled iteration takes about a
-    third of the stress passes, and the two P_bar agree within the tolerance they share."""
+    prescribed stresses and the equilibrium tolerance; the coupled iteration (mode 2: its
+    first stress pass implicit) takes at most half the stress passes, and the two P_bar
+    agree within the tolerance they share."""
     N = 9
     r = rve.make_rve(N, 8, 3, rve.FCC_VOCE)
     load = rve.plane_strain_compression(0.10, 100)
-    nested = run_oracle(oracle, r, load, False, 3, N)
-    coupled = run_oracle(oracle, r, load, True, 3, N)
+    nested = run_oracle(oracle, r, load, 0, 3, N)
+    coupled = run_oracle(oracle, r, load, mode, 3, N)
     for (Pn, sn), (Pc, sc) in zip(nested, coupled):
         assert sc["res_equil"] <= 1e-6 and sc["res_pbar"] <= 1e-6
         assert sc["stress_updates"] * 2 <= sn["stress_updates"]
@@ -39,17 +41,18 @@ def test_oracle_coupled_against_nested(oracle):
 
 
 @pytest.mark.gpu
-def test_gpu_coupled_fp64_against_oracle(gpulib, oracle):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_gpu_coupled_fp64_against_oracle(gpulib, oracle, mode):
     """The GPU's coupled steps in the plain FP64 form (FP64 CG to 1e-10) against the
     oracle's: P_bar to 1e-10, the same Newton and stress-pass counts."""
     N = 9
     r = rve.make_rve(N, 8, 3, rve.FCC_VOCE)
     load = rve.plane_strain_compression(0.10, 100)
-    ref = run_oracle(oracle, r, load, True, 3, N)
+    ref = run_oracle(oracle, r, load, mode, 3, N)
     s = gpulib.Solver(N, r.mat_list, r.kocks, r.crystals, 1.0, gpulib.G_REF_SHIFT)
     try:
         s.set_equilibrium_tol(1e-6)
-        s.set_coupled_bc(True)
+        s.set_coupled_bc(mode)
         s.nr3_begin(1e-10)
         for step, (Po, so) in enumerate(ref, start=1):
             rc, Pb, st = s.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 30)
@@ -81,7 +84,7 @@ def test_gpu_coupled_fast_form(gpulib, oracle):
         s.set_schedule(gpulib.SCHED_QUEUE)
         s.set_equilibrium_tol(1e-6)
         s.set_inexact_newton(1e-2)
-        s.set_coupled_bc(True)
+        s.set_coupled_bc(2)
         s.nr3_begin(1e-10)
         for step in (1, 2, 3):
             rco, Po, so = o.nr3_step(step, load.BC_all[step - 1], load.isNBC, 1e-6, 1e-10, 30)
