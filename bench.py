@@ -196,15 +196,19 @@ def start_flags(cp, form, args):
             (cp.TANGENT_F32 if args.tangent == "f32" else 0))
 
 
+MATERIALS = {"voce": "FCC_VOCE", "mrr": "MRR_FCC", "ornl": "ORNL_FCC"}
+
+
 def workload(args):
     """The RVE and loading of --workload: the 128^3 plane-strain workload (N, grains and
-    seed from the arguments), or the 256^3 cyclic workload."""
+    seed from the arguments), or the 256^3 cyclic workload; crystals of --material."""
     from cpfft_gb300 import rve
+    crystal = getattr(rve, MATERIALS[getattr(args, "material", "voce")])
     if args.workload == "config5":
-        r = rve.make_rve(256, 2048, 4)
+        r = rve.make_rve(256, 2048, 4, crystal)
         load = rve.cyclic_uniaxial(0.02, 2, 160)
     else:
-        r = rve.make_rve(args.N, args.grains, args.seed)
+        r = rve.make_rve(args.N, args.grains, args.seed, crystal)
         load = rve.plane_strain_compression(0.10, 100)
     return r, load
 
@@ -536,11 +540,13 @@ REF_COUNTS = (15, 4290)
 def config_dict(args, impl):
     fast = impl != "reference"
     inexact = fast and args.mode != "fp64" and args.tol_equil > 0 and args.inexact > 0
+    mat = {"voce": "FCC mm10 Voce", "mrr": "FCC mm10 Ma-Roters-Raabe (12 densities)",
+           "ornl": "FCC mm10 ORNL (12 densities)"}[args.material]
     r_desc = ("cyclic uniaxial tension/compression +-2 % (2 cycles in 160 steps), 256^3 "
-              "voxels, 2048 Voronoi grains (seed 4), FCC mm10 Voce"
+              f"voxels, 2048 Voronoi grains (seed 4), {mat}"
               if args.workload == "config5" else
               f"plane-strain compression 10%/100 steps, {args.N}^3 voxels, "
-              f"{args.grains} Voronoi grains (seed {args.seed}), FCC mm10 Voce")
+              f"{args.grains} Voronoi grains (seed {args.seed}), {mat}")
     return {"workload": r_desc,
             "N": 256 if args.workload == "config5" else args.N,
             "grains": 2048 if args.workload == "config5" else args.grains,
@@ -788,6 +794,9 @@ def main():
     ap.add_argument("--tangent", default="f32", choices=["f32", "f64"])
     # config4: the 48-RVE batch (cpfft_batch_solve); config5: the 256^3 cyclic workload
     ap.add_argument("--workload", default="128", choices=["128", "config4", "config5"])
+    ap.add_argument("--material", default="voce", choices=sorted(MATERIALS),
+                    help="crystals of the workload: FCC Voce (the named workloads), or the "
+                         "dislocation-density laws (Ma-Roters-Raabe, ORNL)")
     ap.add_argument("--batch-threads", type=int, default=8)
     # ||dF||/||F|| of FFT_nr3, and the equilibrium residual ||G(P)||/(sqrt(N^3)||P_bar||)
     # both forms must also reach before a Newton loop ends (cpfft_set_equilibrium_tol)
@@ -822,6 +831,10 @@ def main():
     # (each costs minutes in the FP64 form); the headline workloads keep >= 3 warm-up steps
     if args.warmup < (1 if args.workload == "config5" else 3):
         ap.error("at least 3 warm-up steps")
+    if args.material != "voce" and (args.mode == "learned" or args.compare_starts):
+        if args.mode == "learned":
+            ap.error("the learned guess serves crystals with one slip resistance")
+        args.compare_starts = False  # the start comparison needs the learned guess
     if args.impl == "reference":
         return reference_arm(args)
     if args.workload == "config4":

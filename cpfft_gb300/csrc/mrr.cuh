@@ -34,10 +34,16 @@ constexpr double MRR_PI = 3.141592653589793;
 constexpr double MRR_NU = 0.3;  // Poisson's ratio of the dipole distance (mm10_h_mrr)
 
 // the quantities of system a at (sigma, rho) every routine forms: resolved shear, forest
-// and parallel densities, rate prefactor, passing and cutting stresses, and the slip
-// increment (mm10_slipinc_mrr, src/mm10_b.f:2477-2546)
+// and parallel densities, rate prefactor, passing and cutting stresses, the slip
+// increment (mm10_slipinc_mrr, src/mm10_b.f:2477-2546) and, once per system, the pieces
+// of its derivatives: slip / g0 and d slip / d fract (the reference's dgdt / dgdh
+// evaluate the same exponential and powers again for every entry they fill; here the
+// Jacobian's 288 d slip / d rho entries reuse each system's twelve values)
 struct MrrSys {
   double rs, rhoF, rhoP, g0, tpass, tcut, fract, slip;
+  double sg0;  // slip / g0 (exponential branch)
+  double dsf;  // d slip / d fract (exponential branch)
+  double m;    // slope of the linear extrapolation (fract > 1)
 };
 
 __device__ void mrr_sys(const Crystal& s, const double* st, const double* tt, int a, MrrSys& y) {
@@ -64,74 +70,71 @@ __device__ void mrr_sys(const Crystal& s, const double* st, const double* tt, in
   }
   y.fract = (fabs(y.rs) - y.tpass) / y.tcut;
   const double Qk = c.G_0_v / k / th;
+  y.sg0 = 0.0;
+  y.dsf = 0.0;
+  y.m = 0.0;
   if (y.fract > 1.0) {  // linear extrapolation past fract = 1
-    const double m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
-    y.slip = s.tinc * (m * y.fract + y.g0);
+    y.m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
+    y.slip = s.tinc * (y.m * y.fract + y.g0);
   } else if (fabs(y.rs) > 0.0) {
-    y.slip = s.tinc * y.g0 * sgn1(y.rs) *
-             exp(-Qk * pow(1.0 - pow(y.fract, mrr_pexp(c, y.fract)), c.q_v));
+    // exp(-Q / kT (1 - fract^p)^q) with the integral exponents of the usual parameters
+    // (p = 1, q = 2) formed without pow
+    const double pe = mrr_pexp(c, y.fract);
+    const double fp = pe == 1.0 ? y.fract : pow(y.fract, pe);
+    const double fp1 = pe == 1.0 ? 1.0 : pow(y.fract, pe - 1.0);
+    const double base = 1.0 - fp;
+    const double bq1 = c.q_v == 2.0 ? base : pow(base, c.q_v - 1.0);
+    const double bq = c.q_v == 2.0 ? base * base : pow(base, c.q_v);
+    y.sg0 = s.tinc * sgn1(y.rs) * exp(-Qk * bq);
+    y.slip = y.sg0 * y.g0;
+    y.dsf = y.slip * Qk * c.q_v * bq1 * pe * fp1;
   } else {
     y.slip = 0.0;
   }
 }
 
+// the twelve systems at one point
+__device__ __forceinline__ void mrr_systems(const Crystal& s, const double* st, const double* tt,
+                                            MrrSys* ys) {
+  for (int a = 0; a < NH; a++) mrr_sys(s, st, tt, a, ys[a]);
+}
+
 // d slip / d rs (mm10_dgdt_mrr, src/mm10_b.f:3111-3198)
-__device__ double mrr_dgdt(const Crystal& s, const MrrSys& y) {
-  const CrysRec& c = *s.cr;
-  const double Qk = c.G_0_v / c.boltzman / s.temp;
+__device__ __forceinline__ double mrr_dgdt(const Crystal& s, const MrrSys& y) {
   const double dfract = sgn1(y.rs) / y.tcut;
-  if (y.fract > 1.0) {
-    const double m = y.g0 * (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs) / y.tcut;
-    return c.exact_j22 ? s.tinc * m * dfract : s.tinc * m;
-  }
-  if (fabs(y.rs) > 0.0) {
-    const double pe = mrr_pexp(c, y.fract);
-    const double base = 1.0 - pow(y.fract, pe);
-    const double slipexp = exp(-Qk * pow(base, c.q_v)) * sgn1(y.rs);
-    return s.tinc * (-y.g0 * slipexp * Qk * c.q_v * pow(base, c.q_v - 1.0) * (-1.0) * pe *
-                     pow(y.fract, pe - 1.0) * dfract);
-  }
+  if (y.fract > 1.0) return s.cr->exact_j22 ? s.tinc * y.m * dfract : s.tinc * y.m;
+  if (fabs(y.rs) > 0.0) return y.dsf * dfract;
   return 0.0;
 }
 
 // d slip_a / d rho_q (mm10_dgdh_mrr, src/mm10_b.f:3201-3306; ORNL: mm10_dgdh_ornl,
-// :4224-4347, the prefactor depends on rho_a alone and the cutting stress on no density)
-__device__ double mrr_dgdh(const Crystal& s, const MrrSys& y, int a, int q) {
+// :4224-4347, the prefactor depends on rho_a alone and the cutting stress on no density):
+// g0, tau_pass and tau_cut scale with sqrt(rho_P) or sqrt(rho_F)
+__device__ __forceinline__ double mrr_dgdh(const Crystal& s, const MrrSys& y, int a, int q) {
   const CrysRec& c = *s.cr;
-  const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
-  const double Qk = c.G_0_v / k / th;
   const double drhoF = __ldg(c.Gm + NH * a + q), drhoP = __ldg(c.Hm + NH * a + q);
-  const double dg0 = ORNL ? (a == q ? 0.1 : 0.0) * b * ornl_vs(c) / b * (c.u2 * b)
-                          : 0.5 * c.G_0_y * k * th / (c.u1 * c.u3 * G * b * b) / sqrt(y.rhoP) * drhoP;
-  const double dtpass = 0.5 * c.u1 * G * b / sqrt(y.rhoP) * drhoP;
-  const double dtcut = ORNL ? 0.0 : 0.5 * c.G_0_v / (c.u2 * c.u3 * b * b) / sqrt(y.rhoF) * drhoF;
-  const double dfract = ((-dtpass) * y.tcut - (fabs(y.rs) - y.tpass) * dtcut) / (y.tcut * y.tcut);
+  const double dg0 = ORNL ? (a == q ? 0.1 : 0.0) * c.burgers * ornl_vs(c) / c.burgers * (c.u2 * c.burgers)
+                          : 0.5 * y.g0 * drhoP / y.rhoP;
+  const double dtpass = 0.5 * y.tpass * drhoP / y.rhoP;
+  const double dtcut = ORNL ? 0.0 : 0.5 * y.tcut * drhoF / y.rhoF;
+  const double dfract = -(dtpass + y.fract * dtcut) / y.tcut;
   if (y.fract > 1.0) {
+    const double Qk = c.G_0_v / c.boltzman / s.temp;
     const double K = (-c.q_v * Qk) * (-c.p_v) * sgn1(y.rs);
     const double dm = K * (dg0 / y.tcut - y.g0 * dtcut / (y.tcut * y.tcut));
     if (!c.exact_j22) return s.tinc * dm;
-    const double m = y.g0 * K / y.tcut;
-    return s.tinc * (dm * y.fract + m * dfract + dg0);
+    return s.tinc * (dm * y.fract + y.m * dfract + dg0);
   }
-  if (fabs(y.rs) > 0.0) {
-    const double pe = mrr_pexp(c, y.fract);
-    const double base = 1.0 - pow(y.fract, pe);
-    const double slipexp = exp(-Qk * pow(base, c.q_v));
-    return s.tinc * (dg0 * slipexp * sgn1(y.rs) +
-                     y.g0 * sgn1(y.rs) * slipexp * (-1.0) * Qk * c.q_v * pow(base, c.q_v - 1.0) *
-                         (-1.0) * pe * pow(y.fract, pe - 1.0) * dfract);
-  }
+  if (fabs(y.rs) > 0.0) return y.sg0 * dg0 + y.dsf * dfract;
   return 0.0;
 }
 
-// R1 (mm10_formR1, src/mm10_b.f:1061-1101): dbarp and wp of the MRR slips
-__device__ void mrr_formR1(const Crystal& s, const double* st, const double* tt, double* R1) {
+// R1 (mm10_formR1, src/mm10_b.f:1061-1101): dbarp and wp of the systems' slips
+__device__ void mrr_R1(const Crystal& s, const double* st, const MrrSys* ys, double* R1) {
   double dbar[6] = {0, 0, 0, 0, 0, 0}, w[3] = {0, 0, 0};
   for (int i = 0; i < NS; i++) {
-    MrrSys y;
-    mrr_sys(s, st, tt, i, y);
-    for (int a = 0; a < 6; a++) dbar[a] += y.slip * s.ms[i][a];
-    for (int a = 0; a < 3; a++) w[a] += y.slip * s.qc[i][a];
+    for (int a = 0; a < 6; a++) dbar[a] += ys[i].slip * s.ms[i][a];
+    for (int a = 0; a < 3; a++) w[a] += ys[i].slip * s.qc[i][a];
   }
   double sw[6], wv1[6];
   symsw(st, w, sw);
@@ -143,6 +146,12 @@ __device__ void mrr_formR1(const Crystal& s, const double* st, const double* tt,
   }
 }
 
+__device__ void mrr_formR1(const Crystal& s, const double* st, const double* tt, double* R1) {
+  MrrSys ys[NH];
+  mrr_systems(s, st, tt, ys);
+  mrr_R1(s, st, ys, R1);
+}
+
 // R = (R1, tt - h) (mm10_formR, mm10_h_mrr, src/mm10_b.f:1029-1047, 2549-2646); the
 // densities' rates (h - rho_n) / tinc
 __device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x, double* R,
@@ -150,14 +159,15 @@ __device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x,
   const CrysRec& c = *s.cr;
   const double* st = x;
   const double* tt = x + 6;
-  mrr_formR1(s, st, tt, R);
+  MrrSys ys[NH];
+  mrr_systems(s, st, tt, ys);
+  mrr_R1(s, st, ys, R);
   const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
   const double cdip = sqrt(3.0) * G * b / (16.0 * MRR_PI * (1.0 - MRR_NU));
   const double cM = (2.0 * k / (c.u1 * c.u2 * c.u3 * G * b * b * b)) * th;
   const double E = c.tau_hat_y * exp(-c.tau_a / k / th) / (k * th);
   for (int a = 0; a < NH; a++) {
-    MrrSys y;
-    mrr_sys(s, st, tt, a, y);
+    const MrrSys& y = ys[a];
     const double rho = tt[a], ars = fabs(y.rs);
     const double ddip = cdip / ars;
     const double rhoM = cM * sqrt(y.rhoF * y.rhoP);
@@ -165,9 +175,7 @@ __device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x,
     const double tem1 = c.u4 / b * sqrt(y.rhoP) * gd;
     const double tem2 = c.u6 * ddip / b * rhoM * gd;
     const double tem3 = c.u5 * rho * gd;
-    const double tem4 = c.tau_hat_y * exp(-c.tau_a / k / th) * ars / (k * th) * rho * rho *
-                        pow(gd, c.tau_hat_v);
-    (void)E;
+    const double tem4 = E * ars * rho * rho * pow(gd, c.tau_hat_v);
     const double h = nrho[a] + s.tinc * (tem1 + tem2 - tem3 - tem4);
     R[6 + a] = tt[a] - h;
     rate[a] = (h - nrho[a]) / s.tinc;
@@ -176,21 +184,19 @@ __device__ void mrr_formR(const Crystal& s, const double* nrho, const double* x,
 
 // J11 (mm10_formJ11, src/mm10_b.f:177-257) with mm10_dgdt_mrr, ld = row stride of J
 template <int ld>
-__device__ void mrr_formJ11(const Crystal& s, const double* st, const double* tt, double* J) {
+__device__ void mrr_J11(const Crystal& s, const double* st, const MrrSys* ys, double* J) {
   for (int a = 0; a < 6; a++)
     for (int cc = 0; cc < 6; cc++) J[ld * a + cc] = 0.0;
   double w[3] = {0, 0, 0};
   for (int i = 0; i < NS; i++) {
-    MrrSys y;
-    mrr_sys(s, st, tt, i, y);
-    const double dg = mrr_dgdt(s, y);
+    const double dg = mrr_dgdt(s, ys[i]);
     double sq[6];
     symsw(st, s.qc[i], sq);
     for (int a = 0; a < 6; a++) {
       const double wv = s.Cms[i][a] + 2.0 * sq[a];
       for (int cc = 0; cc < 6; cc++) J[ld * a + cc] += wv * (dg * s.ms[i][cc]);
     }
-    for (int a = 0; a < 3; a++) w[a] += y.slip * s.qc[i][a];
+    for (int a = 0; a < 3; a++) w[a] += ys[i].slip * s.qc[i][a];
   }
   // mm10_iw (src/mm10_b.f:1590-1634) and the identity
   J[ld * 0 + 3] += 2.0 * w[2];  J[ld * 0 + 5] += -2.0 * w[1];
@@ -210,7 +216,9 @@ __device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
   const CrysRec& c = *s.cr;
   const double* st = x;
   const double* tt = x + 6;
-  mrr_formJ11<L>(s, st, tt, J);
+  MrrSys ys[NH];
+  mrr_systems(s, st, tt, ys);
+  mrr_J11<L>(s, st, ys, J);
   for (int a = 0; a < 6; a++)
     for (int q = 0; q < NH; q++) J[L * a + 6 + q] = 0.0;
   const double k = c.boltzman, th = s.temp, G = mrr_shear(s), b = c.burgers;
@@ -220,16 +228,15 @@ __device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
   const double E = c.tau_hat_y * exp(-c.tau_a / k / th) / (k * th);
   const double c8 = c.tau_hat_v;
   for (int a = 0; a < NH; a++) {
-    MrrSys y;
-    mrr_sys(s, st, tt, a, y);
+    const MrrSys& y = ys[a];
+    double dsh[NH];  // d slip_a / d rho_q
+    for (int q = 0; q < NH; q++) dsh[q] = mrr_dgdh(s, y, a, q);
     // J12 column block of system a's slip
     {
       double sq[6];
       symsw(st, s.qc[a], sq);
-      for (int q = 0; q < NH; q++) {
-        const double d = mrr_dgdh(s, y, a, q);
-        for (int r = 0; r < 6; r++) J[L * r + 6 + q] += (s.Cms[a][r] + 2.0 * sq[r]) * d;
-      }
+      for (int q = 0; q < NH; q++)
+        for (int r = 0; r < 6; r++) J[L * r + 6 + q] += (s.Cms[a][r] + 2.0 * sq[r]) * dsh[q];
     }
     const double rho = tt[a], sg = sgn1(y.rs), ars = fabs(y.rs);
     const double ddip = cdip / ars;
@@ -237,16 +244,18 @@ __device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
     const double rhoM = cM * sqrt(y.rhoF * y.rhoP);
     const double gd = fabs(y.slip / dt);
     const double dsl = mrr_dgdt(s, y) / dt;
+    const double gdc8 = gd == 0.0 ? 0.0 : pow(gd, c8);   // gd^c8 (0 at gd = 0, c8 > 0)
+    const double gdc81 = gd == 0.0 ? 0.0 : gdc8 / gd;     // gd^(c8 - 1), only where gd != 0
     double et;
     if (!c.exact_j22) {
-      const double bad = gd == 0.0 ? 0.0 : c8 * ars * pow(gd, c8 - 1.0) * dsl;
+      const double bad = gd == 0.0 ? 0.0 : c8 * ars * gdc81 * dsl;
       et = dt * (c.u4 / b * sqrt(y.rhoF) * sg * dsl + c.u6 / b * rhoM * (ddip * sg * dsl + dddip * gd) -
-                 c.u5 * rho * sg * dsl - E * rho * rho * (bad + sg * pow(gd, c8)));
+                 c.u5 * rho * sg * dsl - E * rho * rho * (bad + sg * gdc8));
     } else {
       const double dgd = sgn1(y.slip) * dsl;
-      const double bad = gd == 0.0 ? 0.0 : c8 * ars * pow(gd, c8 - 1.0) * dgd;
+      const double bad = gd == 0.0 ? 0.0 : c8 * ars * gdc81 * dgd;
       et = dt * (c.u4 / b * sqrt(y.rhoP) * dgd + c.u6 / b * rhoM * (ddip * dgd + dddip * gd) -
-                 c.u5 * rho * dgd - E * rho * rho * (bad + sg * pow(gd, c8)));
+                 c.u5 * rho * dgd - E * rho * rho * (bad + sg * gdc8));
     }
     for (int r = 0; r < 6; r++) J[L * (6 + a) + r] = -et * s.ms[a][r];
     const double sqF = sqrt(y.rhoF), sqP = sqrt(y.rhoP), sqFP = sqrt(y.rhoF * y.rhoP);
@@ -254,20 +263,20 @@ __device__ void mrr_formJ(const Crystal& s, const double* x, double* J) {
       const double drhoF = __ldg(c.Gm + NH * a + q), drhoP = __ldg(c.Hm + NH * a + q);
       const double drhoM = 0.5 * cM / sqFP * (drhoF * y.rhoP + y.rhoF * drhoP);
       const double d = a == q ? 1.0 : 0.0;
-      const double dsh = mrr_dgdh(s, y, a, q) / dt;
+      const double dq = dsh[q] / dt;
       double e;
       if (!c.exact_j22) {
-        const double bad = gd == 0.0 ? 0.0 : c8 * pow(gd, c8 - 1.0) * dsh;
-        e = d - dt * (c.u4 / b * (0.5 * drhoF / sqF * gd * sg + sqF * dsh) +
-                      c.u6 / b * (rhoM * ddip * dsh + drhoM * ddip * gd * sg) -
-                      c.u5 * (rho * dsh + d * gd * sg) -
-                      E * ars * (rho * rho * bad + 2.0 * rho * sg * d * pow(gd, c8))) * sg;
+        const double bad = gd == 0.0 ? 0.0 : c8 * gdc81 * dq;
+        e = d - dt * (c.u4 / b * (0.5 * drhoF / sqF * gd * sg + sqF * dq) +
+                      c.u6 / b * (rhoM * ddip * dq + drhoM * ddip * gd * sg) -
+                      c.u5 * (rho * dq + d * gd * sg) -
+                      E * ars * (rho * rho * bad + 2.0 * rho * sg * d * gdc8)) * sg;
       } else {
-        const double dgd = sgn1(y.slip) * dsh;
-        const double bad = gd == 0.0 ? 0.0 : c8 * pow(gd, c8 - 1.0) * dgd;
+        const double dgd = sgn1(y.slip) * dq;
+        const double bad = gd == 0.0 ? 0.0 : c8 * gdc81 * dgd;
         e = d - dt * (c.u4 / b * (0.5 * drhoP / sqP * gd + sqP * dgd) +
                       c.u6 / b * ddip * (rhoM * dgd + drhoM * gd) - c.u5 * (rho * dgd + d * gd) -
-                      E * ars * (rho * rho * bad + 2.0 * rho * d * pow(gd, c8)));
+                      E * ars * (rho * rho * bad + 2.0 * rho * d * gdc8));
       }
       J[L * (6 + a) + 6 + q] = e;
     }
@@ -317,7 +326,11 @@ __device__ bool mrr_solve(Crystal& cu, const double* nrho, const double* nrate, 
     int it = 0;
     while (nR1 > c.atol1 && nR1 / inR1 > c.rtol1) {
       double J[36], mJ[36], dx[6];
-      mrr_formJ11<6>(cu, x1, x2, J);
+      {
+        MrrSys ys[NH];
+        mrr_systems(cu, x1, x2, ys);
+        mrr_J11<6>(cu, x1, ys, J);
+      }
       for (int a = 0; a < 36; a++) mJ[a] = -J[a];
       for (int a = 0; a < 6; a++) dx[a] = R1[a];
       lu_solve1<6>(mJ, dx);
