@@ -291,10 +291,16 @@ def run_form(cp, r, load, form, args, world, local, steps=None, keep_step=None):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
+    # explicit (iteration-0) stress passes per load step: one per P_bar pass in the nested
+    # loops, one per step in the coupled update, none with its implicit first pass
+    coupled = form != "fp64" and args.tol_equil > 0 and args.coupled_bc
+    explicit = [0 if (coupled and args.implicit_first) else 1 if coupled else s["nbc_iters"]
+                for s in stats]
     return {"form": form, "solver": solver, "N3": N3, "stats": stats, "warm_stats": warm_stats,
             "pbars": pbars, "P_last": Ph.numpy().copy(), "F_last": Fh.numpy().copy(),
             "P_keep": P_keep, "t_e2e": t_e2e, "t_dev": sum(s["t_device"] for s in stats),
-            "clocks": clk, "last_step": step, "device_bytes": mem}
+            "clocks": clk, "last_step": step, "device_bytes": mem, "explicit_passes": explicit,
+            "material": getattr(args, "material", "voce")}
 
 
 def counts(run):
@@ -352,7 +358,7 @@ def roofline(run, N, peaks, peak_kind, fp64_peak):
         # FP64-pipe bound: FP64 flops of the timed passes from the flop model (explicit
         # passes, one per P_bar pass; implicit passes by their local iterations)
         per = tsk / su
-        nexp = sum(s["nbc_iters"] for s in st)
+        nexp = sum(run.get("explicit_passes", [s["nbc_iters"] for s in st]))
         iters = sum(s["local_iters"] + s["predict_iters"] for s in st)
         flops = N3 * (STRESS_FLOPS["explicit"] * nexp + STRESS_FLOPS["implicit_base"] * (su - nexp)) \
             + STRESS_FLOPS["per_iteration"] * iters
@@ -363,8 +369,16 @@ def roofline(run, N, peaks, peak_kind, fp64_peak):
                 "algorithmic_flops_per_launch": flops / su, "avg_launch_ms": per * 1e3,
                 "flop_model": STRESS_FLOPS["source"],
                 "hbm_algorithmic_bytes_per_launch": BYTES_STRESS * N3}
+        if run.get("material", "voce") != "voce":
+            # the flop model is the Voce kernel's; the dislocation-density kernel's FP64 work
+            # is measured by ncu only (profiles/stress_kernel_mrr_32.md)
+            roof.update({"achieved": None, "frac": None, "algorithmic_flops_per_launch": None,
+                         "flop_model": "none for this material (the Voce kernel's fit does not "
+                                       "apply); ncu: profiles/stress_kernel_mrr_32.md"})
     key = "cg32_fused" if roof["kernel"].startswith("FP32 CG iteration") else kern
     tv, tsrc = TRAFFIC.get(key, (None, "not captured"))
+    if key == "stress" and run.get("material", "voce") != "voce":
+        tv, tsrc = None, "the Voce kernel's capture does not apply; profiles/stress_kernel_mrr_32.md"
     roof["traffic"] = tv * N3 if tv is not None else None
     roof["traffic_source"] = tsrc
     split = {"stress_s": tsk, "green64_s": tg64, "green32_s_estimated": tg32,
