@@ -783,7 +783,7 @@ def config4_arm(args):
     return 0
 
 
-def main():
+def make_parser():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
@@ -840,6 +840,11 @@ def main():
     ap.add_argument("--no-compare-starts", dest="compare_starts", action="store_false",
                     help="skip the local-start comparison (reference / trial / learned) on "
                          "the state the timed steps leave")
+    return ap
+
+
+def main():
+    ap = make_parser()
     args = ap.parse_args()
     # the 256^3 workload is reported for memory, s/step and accuracy at a few load steps
     # (each costs minutes in the FP64 form); the headline workloads keep >= 3 warm-up steps
