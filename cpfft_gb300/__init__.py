@@ -116,6 +116,13 @@ class Rve(ctypes.Structure):
     ]
 
 
+class Newton(ctypes.Structure):
+    """``cpfft_newton`` of include/cpfft_gpu.h (the fast form's Newton options of a batch)."""
+
+    _fields_ = [("equilibrium_tol", ctypes.c_double), ("eta_max", ctypes.c_double),
+                ("tangent_tol", ctypes.c_double), ("coupled_bc", ctypes.c_int)]
+
+
 # every exported symbol and its signature
 _D, _I, _P = ctypes.c_double, ctypes.c_int, ctypes.POINTER
 _DP, _IP = _P(_D), _P(_I)
@@ -140,6 +147,8 @@ SIGNATURES = {
     "cpfft_write_disp_flat": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_ouresult": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
+    "cpfft_batch_solve_newton": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I,
+                                      ctypes.POINTER(Newton), _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
     "cpfft_green_apply": (_I, [_DP, _DP, _I]),
     "cpfft_green_apply_f32": (_I, [_FP, _FP, _I]),
@@ -487,11 +496,13 @@ class Solver:
 
 def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE,
                 schedule=SCHED_QUEUE, tolNR=1e-5, tolPCG=1e-10, maxIter=20, nthreads=4,
-                want_fields=False):
+                want_fields=False, newton=None):
     """Solve many RVEs at once (cpfft_batch_solve).  rves: dicts with N, mat_list, kocks,
     crystals, tstep, g_mapping and a loading (rve.Loading: BC_all, isNBC, nsteps used), and
     optionally mises: {material (1-based): dict(e, nu, yld_pt, tan_e, beta)} for materials
-    declared NOT_A_CRYSTAL.  Returns one dict per RVE: Pbar (nsteps, 9), status,
+    declared NOT_A_CRYSTAL.  newton: None, or a dict of cpfft_newton's fields
+    (equilibrium_tol, eta_max, tangent_tol, coupled_bc; absent ones 0) applied to every RVE
+    (cpfft_batch_solve_newton).  Returns one dict per RVE: Pbar (nsteps, 9), status,
     voxel_updates, cg_iters, seconds, and (want_fields) F, P (9, N3)."""
     L = load_library()
     arr = (Rve * len(rves))()
@@ -523,8 +534,16 @@ def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE
             keep.append(ms)
             r.mises = ctypes.cast(ms, ctypes.POINTER(Mises))
         out.append({"Pbar": pb, "F": F, "P": P})
-    rc = L.cpfft_batch_solve(arr, len(rves), precision, options, precond, schedule, tolNR,
-                             tolPCG, maxIter, nthreads)
+    if newton is None:
+        rc = L.cpfft_batch_solve(arr, len(rves), precision, options, precond, schedule, tolNR,
+                                 tolPCG, maxIter, nthreads)
+    else:
+        unknown = set(newton) - {f for f, _ in Newton._fields_}
+        if unknown:
+            raise ValueError("batch_solve: unknown Newton options %s" % sorted(unknown))
+        nt = Newton(**newton)
+        rc = L.cpfft_batch_solve_newton(arr, len(rves), precision, options, precond, schedule,
+                                        ctypes.byref(nt), tolNR, tolPCG, maxIter, nthreads)
     for k, o in enumerate(out):
         r = arr[k]
         o.update(status=r.status, steps_done=r.steps_done, voxel_updates=r.voxel_updates,

@@ -2461,7 +2461,7 @@ int cpfft_commit_step(void) {
 
 // ---- many RVEs: one context per RVE, worker threads over a largest-first queue --------
 static void batch_one(cpfft_rve& r, int precision, int options, int precond, int schedule,
-                      double tolNR, double tolPCG, int maxIter) {
+                      const cpfft_newton* nt, double tolNR, double tolPCG, int maxIter) {
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
   r.status = 0;
@@ -2480,6 +2480,10 @@ static void batch_one(cpfft_rve& r, int precision, int options, int precond, int
   if ((rc = cpfft_set_mode(precision, options)) < 0 ||
       (precision == CPFFT_PREC_MIXED && (rc = cpfft_set_precond(precond)) < 0) ||
       (precision == CPFFT_PREC_MIXED && (rc = cpfft_set_schedule(schedule)) < 0) ||
+      (nt && ((rc = cpfft_set_equilibrium_tol(nt->equilibrium_tol)) < 0 ||
+              (rc = cpfft_set_inexact_newton(nt->eta_max)) < 0 ||
+              (nt->tangent_tol > 0.0 && (rc = cpfft_set_tangent_tol(nt->tangent_tol)) < 0) ||
+              (rc = cpfft_set_coupled_bc(nt->coupled_bc)) < 0)) ||
       (rc = cpfft_nr3_begin(tolPCG)) < 0) {
     fail(rc);
   } else {
@@ -2504,8 +2508,23 @@ static void batch_one(cpfft_rve& r, int precision, int options, int precond, int
 
 int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int precond,
                       int schedule, double tolNR, double tolPCG, int maxIter, int nthreads) {
+  return cpfft_batch_solve_newton(rves, nrve, precision, options, precond, schedule, nullptr,
+                                  tolNR, tolPCG, maxIter, nthreads);
+}
+
+int cpfft_batch_solve_newton(cpfft_rve* rves, int nrve, int precision, int options,
+                             int precond, int schedule, const cpfft_newton* nt,
+                             double tolNR, double tolPCG, int maxIter, int nthreads) {
   if (nrve < 0 || (nrve > 0 && !rves) || nthreads < 1) {
     cpfft_set_error("cpfft_batch_solve: invalid argument");
+    return CPFFT_ERR_BAD_ARG;
+  }
+  // the setters' own ranges, checked here so that no RVE starts with options it refuses
+  if (nt && (!(nt->equilibrium_tol >= 0.0) || !std::isfinite(nt->equilibrium_tol) ||
+             !(nt->eta_max >= 0.0 && nt->eta_max < 1.0) ||
+             !(nt->tangent_tol >= 0.0 && nt->tangent_tol < 1.0) || nt->coupled_bc < 0 ||
+             nt->coupled_bc > 2)) {
+    cpfft_set_error("cpfft_batch_solve_newton: Newton option out of range");
     return CPFFT_ERR_BAD_ARG;
   }
   for (int k = 0; k < nrve; k++)
@@ -2527,7 +2546,8 @@ int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int
     for (;;) {
       const int k = next.fetch_add(1);
       if (k >= nrve) break;
-      batch_one(rves[order[k]], precision, options, precond, schedule, tolNR, tolPCG, maxIter);
+      batch_one(rves[order[k]], precision, options, precond, schedule, nt, tolNR, tolPCG,
+                maxIter);
     }
   };
   std::vector<std::thread> pool;

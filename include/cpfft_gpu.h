@@ -435,6 +435,21 @@ typedef struct cpfft_rve {
 int cpfft_batch_solve(cpfft_rve* rves, int nrve, int precision, int options, int precond,
                       int schedule, double tolNR, double tolPCG, int maxIter, int nthreads);
 
+/* The Newton options of the fast form for every RVE of a batch (extension). */
+typedef struct cpfft_newton {
+    double equilibrium_tol;       /* cpfft_set_equilibrium_tol; 0: the reference's loop    */
+    double eta_max;               /* cpfft_set_inexact_newton; 0: every system to tolPCG   */
+    double tangent_tol;           /* cpfft_set_tangent_tol; 0 keeps its default (1e-2)     */
+    int coupled_bc;               /* cpfft_set_coupled_bc: 0, 1 or 2                       */
+} cpfft_newton;
+
+/* cpfft_batch_solve with `newton` applied in each RVE's context after its mode
+ * (newton == NULL: cpfft_batch_solve).  Options out of their setters' ranges return
+ * CPFFT_ERR_BAD_ARG before any RVE starts. */
+int cpfft_batch_solve_newton(cpfft_rve* rves, int nrve, int precision, int options,
+                             int precond, int schedule, const cpfft_newton* newton,
+                             double tolNR, double tolPCG, int maxIter, int nthreads);
+
 /* Copy device fields to the host (any pointer may be NULL): Fn1, Pn1 (N3,9) and the
  * compact history at n (N3, cpfft_hist_words()) used by the result writers. */
 #define CPFFT_HIST_WORDS 31   /* sigma(6) tau_tilde(1) Rp(9) D(6) tau_tilde_rate(1) eps(6)

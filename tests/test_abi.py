@@ -7,6 +7,7 @@ import re
 import subprocess
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -70,6 +71,22 @@ def test_init_rejects_bad_arguments(gpulib):
     assert L.cpfft_init(2, ml2.ctypes.data_as(P(ctypes.c_int)), kap, cr, 1, 1.0, 0) == -5
 
 
+@pytest.mark.parametrize("bad", [dict(eta_max=1.0), dict(coupled_bc=3),
+                                 dict(equilibrium_tol=-1e-6), dict(equilibrium_tol=np.inf),
+                                 dict(tangent_tol=1.5)])
+def test_batch_refuses_newton_options_out_of_range(gpulib, bad):
+    """cpfft_batch_solve_newton checks its options before any RVE starts (no GPU call)."""
+    L = gpulib.load_library()
+    nt = gpulib.Newton(**dict(dict(equilibrium_tol=1e-6, eta_max=1e-2, tangent_tol=1e-2,
+                                   coupled_bc=2), **bad))
+    rv = (gpulib.Rve * 1)()
+    assert L.cpfft_batch_solve_newton(rv, 1, 1, 0, 0, 0, ctypes.byref(nt), 1e-6, 1e-10, 20,
+                                      1) == -5
+    assert b"Newton option" in L.cpfft_last_error()
+    with pytest.raises(ValueError):
+        gpulib.batch_solve([], newton=dict(eta=1e-2))
+
+
 def test_product_path_does_not_reference_the_oracle():
     for dirpath, _, files in os.walk(os.path.join(ROOT, "cpfft_gb300")):
         for f in files:
@@ -112,7 +129,7 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
     mirrors = {"cpfft_crystal": [cpfft_gb300.Crystal, pyoracle.Crystal],
                "cpfft_mises": [cpfft_gb300.Mises, pyoracle.Mises],
                "cpfft_stats": [cpfft_gb300.Stats, pyoracle.Stats],
-               "cpfft_rve": [cpfft_gb300.Rve]}
+               "cpfft_rve": [cpfft_gb300.Rve], "cpfft_newton": [cpfft_gb300.Newton]}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "cpfft_gpu.h"',
              'int main(void) {', 'printf("HIST %d\\n", CPFFT_HIST_WORDS);',
              'printf("HISTMRR %d\\n", CPFFT_HIST_WORDS_MRR);']

@@ -21,7 +21,7 @@ def rves(specs, nsteps):
     return out
 
 
-def solo(gpulib, d, precision, options, precond, schedule):
+def solo(gpulib, d, precision, options, precond, schedule, newton=None):
     s = gpulib.Solver(d["N"], d["mat_list"], d["kocks"], d["crystals"], 1.0, d["g_mapping"],
                       precision)
     try:
@@ -31,6 +31,11 @@ def solo(gpulib, d, precision, options, precond, schedule):
         if precision == gpulib.PREC_MIXED:
             s.set_precond(precond)
             s.set_schedule(schedule)
+        if newton:
+            s.set_equilibrium_tol(newton["equilibrium_tol"])
+            s.set_inexact_newton(newton["eta_max"])
+            s.set_tangent_tol(newton["tangent_tol"])
+            s.set_coupled_bc(newton["coupled_bc"])
         s.nr3_begin(1e-10)
         pb = []
         for step in range(1, d["nsteps"] + 1):
@@ -43,11 +48,18 @@ def solo(gpulib, d, precision, options, precond, schedule):
         s.close()
 
 
-@pytest.mark.parametrize("form", ["fp64", "fast"])
+# the fast form's Newton options (cpfft_newton)
+FAST_NEWTON = dict(equilibrium_tol=1e-6, eta_max=1e-2, tangent_tol=1e-2, coupled_bc=2)
+
+
+@pytest.mark.parametrize("form", ["fp64", "fast", "fast_newton"])
 def test_batch_equals_solo(gpulib, form):
+    """fast_newton adds the equilibrium test, inexact Newton and the coupled P_bar update
+    (cpfft_batch_solve_newton) to the fast form."""
     specs = [(9, 4, 41, gpulib.G_REF_SHIFT), (8, 3, 42, gpulib.G_CENTERED),
              (16, 6, 43, gpulib.G_CENTERED), (32, 8, 44, gpulib.G_CENTERED),
              (7, 3, 45, gpulib.G_REF_SHIFT)]
+    newton = FAST_NEWTON if form == "fast_newton" else None
     if form == "fp64":
         prec, opts = gpulib.PREC_FP64, 0
     else:
@@ -56,11 +68,12 @@ def test_batch_equals_solo(gpulib, form):
     batch = rves(specs, 2)
     res = gpulib.batch_solve(batch, precision=prec, options=opts,
                              precond=gpulib.PRECOND_REFERENCE, schedule=gpulib.SCHED_QUEUE,
-                             tolNR=1e-6, nthreads=3, want_fields=True)
+                             tolNR=1e-6, nthreads=3, want_fields=True, newton=newton)
     for d, r in zip(batch, res):
         assert r["status"] >= 0 and r["steps_done"] == 2, r["error"]
         assert r["voxel_updates"] > 0
-        pb, F, P = solo(gpulib, d, prec, opts, gpulib.PRECOND_REFERENCE, gpulib.SCHED_QUEUE)
+        pb, F, P = solo(gpulib, d, prec, opts, gpulib.PRECOND_REFERENCE, gpulib.SCHED_QUEUE,
+                        newton)
         assert np.array_equal(r["Pbar"], pb), (d["N"], np.abs(r["Pbar"] - pb).max())
         assert np.array_equal(r["F"], F) and np.array_equal(r["P"], P), d["N"]
 
