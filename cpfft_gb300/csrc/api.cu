@@ -121,13 +121,63 @@ void bcc48_geometry(double b[48][3], double n[48][3]) {
   }
 }
 
-// slip systems of a slip_type: 12 (fcc) or 48 (bcc48), 0 when not supported
+// The other 12-system cubic sets, directions and plane normals as integer Miller triples
+// in the reference's order and signs, each normalised by its length (the reference's
+// constants are 1/sqrt(2) and 1/sqrt(3)):
+//   slip_type 2, bcc:     {110}<111> (src/mod_crystals.f:516-593)
+//   slip_type 6, roters:  {111}<110>, the FCC systems in Roters' order (:604-704)
+// slip_type 7 (bcc12, :705-811) is the first twelve systems of bcc48.
+void miller_systems(const int B[12][3], const int Nn[12][3], double b[][3], double n[][3]) {
+  for (int s = 0; s < 12; s++) {
+    const double lb = std::sqrt((double)(B[s][0] * B[s][0] + B[s][1] * B[s][1] + B[s][2] * B[s][2]));
+    const double ln = std::sqrt((double)(Nn[s][0] * Nn[s][0] + Nn[s][1] * Nn[s][1] + Nn[s][2] * Nn[s][2]));
+    for (int i = 0; i < 3; i++) {
+      b[s][i] = (double)B[s][i] / lb;
+      n[s][i] = (double)Nn[s][i] / ln;
+    }
+  }
+}
+
+void bcc_geometry(double b[][3], double n[][3]) {
+  static const int B[12][3] = {{1, 1, 1},   {1, 1, 1},   {1, 1, 1},   {-1, -1, 1},
+                               {-1, -1, 1}, {-1, -1, 1}, {-1, 1, 1},  {-1, 1, 1},
+                               {-1, 1, 1},  {1, -1, 1},  {1, -1, 1},  {1, -1, 1}};
+  static const int Nn[12][3] = {{0, -1, 1}, {1, 0, -1}, {-1, 1, 0}, {0, 1, 1},
+                                {1, 0, 1},  {1, -1, 0}, {0, -1, 1}, {-1, 0, -1},
+                                {1, 1, 0},  {0, 1, 1},  {1, 0, -1}, {-1, -1, 0}};
+  miller_systems(B, Nn, b, n);
+}
+
+void roters_geometry(double b[][3], double n[][3]) {
+  static const int B[12][3] = {{1, -1, 0}, {1, 0, -1}, {0, 1, -1}, {1, 1, 0},
+                               {1, 0, 1},  {0, 1, -1}, {1, 1, 0},  {1, 0, -1},
+                               {0, 1, 1},  {1, -1, 0}, {1, 0, 1},  {0, 1, 1}};
+  static const int Nn[12][3] = {{1, 1, 1},   {-1, -1, -1}, {1, 1, 1},   {1, -1, -1},
+                                {-1, 1, 1},  {1, -1, -1},  {1, -1, 1},  {1, -1, 1},
+                                {-1, 1, -1}, {-1, -1, 1},  {-1, -1, 1}, {1, 1, -1}};
+  miller_systems(B, Nn, b, n);
+}
+
+// slip systems of a slip_type: 12 (fcc, bcc, roters, bcc12) or 48 (bcc48), 0 when not
+// supported
 int slip_geometry(int slip_type, double b[48][3], double n[48][3]) {
   if (slip_type == 1) {
     double bf[12][3], nf[12][3];
     fcc_geometry(bf, nf);
     memcpy(b, bf, sizeof(bf));
     memcpy(n, nf, sizeof(nf));
+    return 12;
+  }
+  if (slip_type == 2) {
+    bcc_geometry(b, n);
+    return 12;
+  }
+  if (slip_type == 6) {
+    roters_geometry(b, n);
+    return 12;
+  }
+  if (slip_type == 7) {
+    bcc48_geometry(b, n);
     return 12;
   }
   if (slip_type == 8) {
@@ -238,12 +288,13 @@ void orientation_record(const double C0[36], const double bb[48][3], const doubl
     }
 }
 
-// Ma-Roters-Raabe interaction matrices of the FCC systems (mm10_mrr_GHfcc, src/mm10_e.f:
-// 55-340, formed here from the geometry): Gm(a,q) = |n_a . t_q| (forest projection),
-// Hm(a,q) = |n_a x t_q| (parallel), t_q = n_q x b_q the edge dislocation line of system q
-void mrr_interaction(double Gm[144], double Hm[144]) {
-  double b[12][3], n[12][3];
-  fcc_geometry(b, n);
+// Ma-Roters-Raabe interaction matrices of a 12-system slip type (mm10_mrr_GH's tables
+// mm10_mrr_GHfcc / GHbcc / GHfcc12 / GHbcc12, src/mm10_e.f:16-1424, formed here from the
+// geometry): Gm(a,q) = |n_a . t_q| (forest projection), Hm(a,q) = |n_a x t_q| (parallel),
+// t_q = n_q x b_q the edge dislocation line of system q
+void mrr_interaction(int slip_type, double Gm[144], double Hm[144]) {
+  double b[48][3], n[48][3];
+  slip_geometry(slip_type, b, n);
   for (int a = 0; a < 12; a++)
     for (int q = 0; q < 12; q++) {
       double t[3] = {n[q][1] * b[q][2] - n[q][2] * b[q][1], n[q][2] * b[q][0] - n[q][0] * b[q][2],
@@ -293,7 +344,7 @@ CrysRec crystal_record(const cpfft_crystal& p) {
   c.u4 = p.u4;
   c.u5 = p.u5;
   c.u6 = p.u6;
-  if (p.h_type == 7 || p.h_type == 4) mrr_interaction(c.Gm, c.Hm);
+  if (p.h_type == 7 || p.h_type == 4) mrr_interaction(p.slip_type, c.Gm, c.Hm);
   c.h_type = p.h_type;
   c.miter = p.miter;
   c.alter_mode = p.alter_mode;
@@ -310,7 +361,7 @@ struct Ctx {
   long long N3 = 0;
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
-  int nslip = 12;  // slip systems of the grid's crystals (12 fcc, 48 bcc48)
+  int nslip = 12;  // slip systems of the grid's crystals (12, or 48 for bcc48)
   int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts, 7 mrr)
   int hist_words = H_WORDS;  // H_WORDS_MRR on dislocation-density grids (MRR, ORNL)
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
@@ -1476,7 +1527,7 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     if (p.slip_type == CPFFT_NOT_A_CRYSTAL) continue;  // defined by cpfft_set_mises
     if (first_crystal < 0) first_crystal = k;
     const int ns = slip_geometry(p.slip_type, bb, nn);
-    // Voce needs tau_v != 0; MTS (fcc only) positive thermal-barrier parameters
+    // Voce needs tau_v != 0; MTS (12-system types) positive thermal-barrier parameters
     const bool voce_ok = p.h_type == 1 && p.tau_v != 0;
     const bool mts_ok = p.h_type == 2 && ns == 12 && p.mu_0 > 0 && p.burgers > 0 &&
                         p.boltzman > 0 && p.G_0_y > 0 && p.G_0_v > 0 && p.p_y > 0 &&
@@ -1494,11 +1545,13 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     const bool n_ok = p.h_type == 7 || p.h_type == 4 || p.harden_n > 0;
     if (!ns || !(voce_ok || mts_ok || mrr_ok || ornl_ok) || !n_ok ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
-      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc or bcc48 slip with voce hardening, "
-                      "fcc with mts, roters or ornl hardening, valid elasticity)", k + 1);
+      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc, bcc, roters, bcc12 or bcc48 "
+                      "slip with voce hardening, the 12-system types with mts, roters or ornl "
+                      "hardening, valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
-    if ((nslip && ns != nslip) || (h_type && p.h_type != h_type)) {
+    // one slip table per grid: the Schmid tensors are formed from the first crystal's
+    if ((nslip && p.slip_type != props[first_crystal].slip_type) || (h_type && p.h_type != h_type)) {
       cpfft_set_error("cpfft_init: the crystals of one grid must share the slip type and the "
                       "hardening law");
       return CPFFT_ERR_BAD_ARG;

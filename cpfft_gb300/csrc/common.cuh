@@ -144,12 +144,12 @@ struct StressArgs {
 };
 
 // warm = true: the learned initial guess starts the local Newton solve.  launch_stress
-// serves crystals with 12 slip systems (FCC), launch_stress48 those with 48 (BCC48).
+// serves crystals with 12 slip systems, launch_stress48 those with 48 (BCC48).
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
-// MTS-hardened FCC crystals (stress_mts.cu)
+// MTS-hardened 12-system crystals (stress_mts.cu)
 cudaError_t launch_stress_mts(const StressArgs& a, bool warm, cudaStream_t s);
-// Ma-Roters-Raabe / ORNL FCC crystals (stress_mrr.cu / stress_ornl.cu; warm is ignored: no
+// Ma-Roters-Raabe / ORNL 12-system crystals (stress_mrr.cu / stress_ornl.cu; warm is ignored: no
 // learned guess)
 cudaError_t launch_stress_mrr(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress_ornl(const StressArgs& a, bool warm, cudaStream_t s);

@@ -1,7 +1,8 @@
 // mrr.cuh -- dislocation-density hardening for the stress kernel: twelve dislocation
-// densities, one per FCC slip system, as the slip resistance variables.  Ma-Roters-Raabe
-// (h_type 7, stress_mrr.cu) and ORNL (h_type 4, stress_ornl.cu: the same hardening law
-// with the temperature-dependent shear modulus mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1),
+// densities, one per slip system of a 12-system crystal, as the slip resistance
+// variables.  Ma-Roters-Raabe (h_type 7, stress_mrr.cu) and ORNL (h_type 4,
+// stress_ornl.cu: the same hardening law with the temperature-dependent shear modulus
+// mu(T) = mu_0 - D_0 / (exp(T_0 / T) - 1),
 // and its own slip law, mm10_slipinc_ornl .. mm10_dgdh_ornl, src/mm10_b.f:3457-4347).
 // Included by stress.cu when it is compiled with CPFFT_LAW 7 or 4.
 //

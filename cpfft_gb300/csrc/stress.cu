@@ -13,7 +13,8 @@
 
 #include "common.cuh"
 
-// Slip systems of the crystals this translation unit serves: 12 (FCC {111}<110>) here;
+// Slip systems of the crystals this translation unit serves: 12 here (fcc, bcc, roters,
+// bcc12: the slip table is the grid's, in the crystal records);
 // stress48.cu compiles this file again with CPFFT_NSLIP 48 (BCC {110},{112},{123}<111>).
 #ifndef CPFFT_NSLIP
 #define CPFFT_NSLIP 12

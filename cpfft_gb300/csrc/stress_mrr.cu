@@ -1,4 +1,4 @@
-// stress_mrr.cu -- the stress kernel for FCC crystals with Ma-Roters-Raabe hardening
+// stress_mrr.cu -- the stress kernel for 12-system crystals with Ma-Roters-Raabe hardening
 // (h_type 7, twelve dislocation densities): the same translation unit as stress.cu,
 // compiled with the MRR law of mrr.cuh.
 #define CPFFT_NSLIP 12

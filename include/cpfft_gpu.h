@@ -53,12 +53,14 @@ extern "C" {
 
 /*
  * One crystal definition: the fields of the reference's `crystal` block that the
- * FCC + Voce path reads (src/mod_crystals.f:231-410 defaults, 1796-1880 elasticity;
+ * crystal path reads (src/mod_crystals.f:231-410 defaults, 1796-1880 elasticity;
  * keyword parser src/incrystal.f).  Units are the deck's (MPa, s).
  */
 typedef struct cpfft_crystal {
-    int    slip_type;      /* 1 = fcc {111}<110>, 12 systems; 8 = bcc48 {110},{112},{123}
-                              <111>, 48 systems (src/mod_crystals.f:438-515, 812-1207); the
+    int    slip_type;      /* 12 systems: 1 = fcc {111}<110>, 2 = bcc {110}<111>,
+                              6 = roters ({111}<110> in Roters' order), 7 = bcc12 ({110}<111>,
+                              bcc48's first twelve); 48 systems: 8 = bcc48 {110},{112},{123}
+                              <111> (src/mod_crystals.f:438-811, 812-1207), Voce only; the
                               crystals of one grid share the slip type; CPFFT_NOT_A_CRYSTAL
                               (0): another material model (cpfft_set_mises)                   */
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
@@ -66,8 +68,8 @@ typedef struct cpfft_crystal {
     double C11, C12, C13, C33, C44, C55;
     int    h_type;         /* 1 = voce, 2 = mts, 7 = roters (Ma-Roters-Raabe dislocation
                               densities, one per slip system), 4 = ornl (the same densities,
-                              ORNL's slip law); fcc crystals; the crystals of one grid share
-                              the hardening law                                            */
+                              ORNL's slip law); mts, roters and ornl with the 12-system slip
+                              types; the crystals of one grid share the hardening law      */
     double harden_n;       /* rate exponent                                               */
     double tau_y, tau_v, theta_0, voce_m;
     double gamma_bar;      /* eps_dot_0_y                                                 */

@@ -303,19 +303,49 @@ void bcc48_systems(double b[48][3], double n[48][3]) {
     }
   }
 }
+// BCC {110}<111> (slip_type 2, src/mod_crystals.f:516-593), in the reference's order and
+// signs: directions +-1/sqrt(3), normals 0 or +-1/sqrt(2) per component.
+void bcc_systems(double b[12][3], double n[12][3]) {
+  const double f = 1.0 / std::sqrt(2.0), g = 1.0 / std::sqrt(3.0);
+  const double B[12][3] = {{g, g, g},   {g, g, g},   {g, g, g},   {-g, -g, g},
+                           {-g, -g, g}, {-g, -g, g}, {-g, g, g},  {-g, g, g},
+                           {-g, g, g},  {g, -g, g},  {g, -g, g},  {g, -g, g}};
+  const double Nn[12][3] = {{0, -f, f}, {f, 0, -f}, {-f, f, 0}, {0, f, f},
+                            {f, 0, f},  {f, -f, 0}, {0, -f, f}, {-f, 0, -f},
+                            {f, f, 0},  {0, f, f},  {f, 0, -f}, {-f, -f, 0}};
+  for (int s = 0; s < 12; s++)
+    for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
+}
+// FCC {111}<110> in Roters' order (slip_type 6 "roters", src/mod_crystals.f:604-704):
+// directions 0 or +-1/sqrt(2), normals +-1/sqrt(3).
+void roters_systems(double b[12][3], double n[12][3]) {
+  const double f = 1.0 / std::sqrt(2.0), g = 1.0 / std::sqrt(3.0);
+  const double B[12][3] = {{f, -f, 0}, {f, 0, -f}, {0, f, -f}, {f, f, 0},
+                           {f, 0, f},  {0, f, -f}, {f, f, 0},  {f, 0, -f},
+                           {0, f, f},  {f, -f, 0}, {f, 0, f},  {0, f, f}};
+  const double Nn[12][3] = {{g, g, g},   {-g, -g, -g}, {g, g, g},   {g, -g, -g},
+                            {-g, g, g},  {g, -g, -g},  {g, -g, g},  {g, -g, g},
+                            {-g, g, -g}, {-g, -g, g},  {-g, -g, g}, {g, g, -g}};
+  for (int s = 0; s < 12; s++)
+    for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
+}
 void crystal_finalize(const cpfft_crystal& p, Crys& c) {
   c.p = p;
-  if (p.slip_type == 8) {
-    c.ns = 48;
-    bcc48_systems(c.b, c.n);
-  } else {
-    c.ns = 12;
-    double b[12][3], n[12][3];
-    fcc_systems(b, n);
+  double b[12][3], n[12][3];
+  c.ns = 12;
+  switch (p.slip_type) {
+    case 8: c.ns = 48; bcc48_systems(c.b, c.n); break;
+    case 7: bcc48_systems(c.b, c.n); break;  // bcc12: bcc48's first twelve (:705-811)
+    case 2: bcc_systems(b, n); break;
+    case 6: roters_systems(b, n); break;
+    default: fcc_systems(b, n); break;
+  }
+  if (p.slip_type != 8 && p.slip_type != 7) {
     std::memcpy(c.b, b, sizeof(b));
     std::memcpy(c.n, n, sizeof(n));
   }
-  // the forest and parallel projections of mm10_mrr_GHfcc (src/mm10_e.f:55-340):
+  // the forest and parallel projections of mm10_mrr_GH's tables (mm10_mrr_GHfcc, GHbcc,
+  // GHfcc12, GHbcc12, src/mm10_e.f:16-1424):
   // Gm(a,b) = |n_a . t_b|, Hm(a,b) = |n_a x t_b|, t_b = n_b x b_b the edge line direction
   for (int a = 0; a < 12; a++)
     for (int q = 0; q < 12; q++) {
@@ -2756,10 +2786,10 @@ int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9], con
   return 0;
 }
 
-void orc_mrr_interaction(double G[144], double H[144]) {
+void orc_mrr_interaction(int slip_type, double G[144], double H[144]) {
   cpfft_crystal p;
   std::memset(&p, 0, sizeof(p));
-  p.slip_type = 1;
+  p.slip_type = slip_type;
   p.elastic_type = 1;
   p.e = 1.0;
   p.nu = 0.3;

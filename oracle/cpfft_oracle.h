@@ -91,9 +91,9 @@ int orc_voxel_update(const cpfft_crystal* props, const double kocks_deg[3],
 int orc_mises_update(const cpfft_mises* props, int step, const double Fn[9],
                      const double Fn1[9], const double* hist_n, double* hist_np1,
                      double P[9], double A[81], double out_sig6[6], double out_cep36[36]);
-/* Ma-Roters-Raabe interaction matrices of the FCC systems (row-major 12 x 12):
- * rho_F = G rho, rho_P = H rho */
-void orc_mrr_interaction(double G[144], double H[144]);
+/* Ma-Roters-Raabe interaction matrices of a 12-system slip type (1 fcc, 2 bcc, 6 roters,
+ * 7 bcc12; row-major 12 x 12): rho_F = G rho, rho_P = H rho */
+void orc_mrr_interaction(int slip_type, double G[144], double H[144]);
 /* Ma-Roters-Raabe local residual R (18) and Jacobian J (18 x 18, row-major) at
  * x = (sigma 6, densities 12) for the strain increment D over tinc at 297 K, the current
  * rotation the identity; hist_n NULL: the initial state.  Returns -1 unless h_type 7. */

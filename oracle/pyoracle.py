@@ -134,7 +134,7 @@ def lib():
         L.orc_mises_update.restype = i
         L.orc_mises_update.argtypes = [P(Mises), i, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_polar.argtypes = [dp, dp]
-        L.orc_mrr_interaction.argtypes = [dp, dp]
+        L.orc_mrr_interaction.argtypes = [ctypes.c_int, dp, dp]
         L.orc_mrr_residual.restype = i
         L.orc_mrr_residual.argtypes = [P(Crystal), dp, dp, d, dp, dp, dp, dp]
         L.orc_crystal_setup.argtypes = [P(Crystal), dp, dp, dp, dp]
@@ -304,11 +304,12 @@ def voxel_update(crystal, kocks, tstep, step, it, Fn, Fn1, hist_n=None):
                 iters=its)
 
 
-def mrr_interaction():
-    """The Ma-Roters-Raabe forest and parallel interaction matrices (12 x 12 each)."""
+def mrr_interaction(slip_type=1):
+    """The Ma-Roters-Raabe forest and parallel interaction matrices (12 x 12 each) of a
+    12-system slip type (1 fcc, 2 bcc, 6 roters, 7 bcc12)."""
     G = np.zeros(144)
     H = np.zeros(144)
-    lib().orc_mrr_interaction(_p(G), _p(H))
+    lib().orc_mrr_interaction(int(slip_type), _p(G), _p(H))
     return G.reshape(12, 12), H.reshape(12, 12)
 
 
