@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcpfft_gb300.so")
-SOURCES = ["stress.cu", "stress48.cu", "stress_mts.cu", "stress_mrr.cu", "stress_ornl.cu", "fft_green.cu", "green_df.cu", "green_df_large.cu", "krylov.cu", "api.cu",
+SOURCES = ["stress.cu", "stress48.cu", "stress6.cu", "stress1.cu", "stress_mts.cu", "stress_mrr.cu", "stress_ornl.cu", "fft_green.cu", "green_df.cu", "green_df_large.cu", "krylov.cu", "api.cu",
            "diag.cu", "noalloc.cu", "mlp.cu", "results.cu", "disp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -158,9 +158,41 @@ void roters_geometry(double b[][3], double n[][3]) {
   miller_systems(B, Nn, b, n);
 }
 
-// slip systems of a slip_type: 12 (fcc, bcc, roters, bcc12) or 48 (bcc48), 0 when not
-// supported
+// One system, direction x on the plane normal to y (slip_type 3 "single",
+// src/mod_crystals.f:594-603).
+void single_geometry(double b[][3], double n[][3]) {
+  const double B[3] = {1.0, 0.0, 0.0}, Nn[3] = {0.0, 1.0, 0.0};
+  for (int i = 0; i < 3; i++) { b[0][i] = B[i]; n[0][i] = Nn[i]; }
+}
+
+// HCP basal {0001}<11-20> (systems 1-3) and prismatic {10-10}<11-20> (4-6) systems in
+// the reference's Cartesian frame, a1 along x and c along z (slip_type 9 "hcp6",
+// src/mod_crystals.f:1208-1476), written with h = sqrt(3)/2 as the reference does.
+// slip_type 10 "hcp18" declares 18 systems but assigns only these six (its pyramidal
+// <c+a> systems are commented out, :1477-1759), so its other twelve keep zero vectors:
+// they never slip and add exact zeros to every sum, and an hcp18 grid runs the same
+// arithmetic on these six.
+void hcp6_geometry(double b[][3], double n[][3]) {
+  const double h = std::sqrt(3.0) / 2.0;
+  const double B[6][3] = {{0.5, -h, 0.0}, {0.5, h, 0.0}, {-1.0, 0.0, 0.0},
+                          {1.0, 0.0, 0.0}, {0.5, h, 0.0}, {-0.5, h, 0.0}};
+  const double Nn[6][3] = {{0.0, 0.0, 1.0}, {0.0, 0.0, 1.0}, {0.0, 0.0, 1.0},
+                           {0.0, 1.0, 0.0}, {-h, 0.5, 0.0}, {-h, -0.5, 0.0}};
+  for (int s = 0; s < 6; s++)
+    for (int i = 0; i < 3; i++) { b[s][i] = B[s][i]; n[s][i] = Nn[s][i]; }
+}
+
+// slip systems of a slip_type as the stress kernels see them: 1 (single), 6 (hcp6,
+// hcp18), 12 (fcc, bcc, roters, bcc12) or 48 (bcc48); 0 when not supported
 int slip_geometry(int slip_type, double b[48][3], double n[48][3]) {
+  if (slip_type == 3) {
+    single_geometry(b, n);
+    return 1;
+  }
+  if (slip_type == 9 || slip_type == 10) {
+    hcp6_geometry(b, n);
+    return 6;
+  }
   if (slip_type == 1) {
     double bf[12][3], nf[12][3];
     fcc_geometry(bf, nf);
@@ -361,7 +393,7 @@ struct Ctx {
   long long N3 = 0;
   double dt = 0;
   int prec = CPFFT_PREC_FP64, warm = 0;
-  int nslip = 12;  // slip systems of the grid's crystals (12, or 48 for bcc48)
+  int nslip = 12;  // slip systems of the grid's stress kernel (1, 6, 12 or 48)
   int h_type = 1;  // hardening law of the grid's crystals (1 voce, 2 mts, 7 mrr)
   int hist_words = H_WORDS;  // H_WORDS_MRR on dislocation-density grids (MRR, ORNL)
   int pass_step = 0, pass_iter = -1;  // the last stress pass (its state is in history n+1)
@@ -1126,7 +1158,12 @@ cudaError_t launch_crystals(Ctx* c, const StressArgs& a, bool warm) {
   if (c->h_type == 2) return launch_stress_mts(a, warm, c->st);
   if (c->h_type == 7) return launch_stress_mrr(a, false, c->st);
   if (c->h_type == 4) return launch_stress_ornl(a, false, c->st);
-  return c->nslip == 48 ? launch_stress48(a, warm, c->st) : launch_stress(a, warm, c->st);
+  switch (c->nslip) {
+    case 48: return launch_stress48(a, warm, c->st);
+    case 6: return launch_stress6(a, warm, c->st);
+    case 1: return launch_stress1(a, warm, c->st);
+    default: return launch_stress(a, warm, c->st);
+  }
 }
 
 int tune_queue_chunk(Ctx* c, StressArgs a, bool warm) {
@@ -1545,9 +1582,9 @@ int cpfft_init(int N, const int* matList, const double* kocks_deg, const cpfft_c
     const bool n_ok = p.h_type == 7 || p.h_type == 4 || p.harden_n > 0;
     if (!ns || !(voce_ok || mts_ok || mrr_ok || ornl_ok) || !n_ok ||
         p.miter < 0 || p.miter > 1000 || !crystal_stiffness(p, C0[k].data())) {
-      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc, bcc, roters, bcc12 or bcc48 "
-                      "slip with voce hardening, the 12-system types with mts, roters or ornl "
-                      "hardening, valid elasticity)", k + 1);
+      cpfft_set_error("cpfft_init: crystal %d unsupported (fcc, bcc, roters, bcc12, bcc48, "
+                      "single, hcp6 or hcp18 slip with voce hardening, the 12-system types with "
+                      "mts, roters or ornl hardening, valid elasticity)", k + 1);
       return CPFFT_ERR_BAD_ARG;
     }
     // one slip table per grid: the Schmid tensors are formed from the first crystal's

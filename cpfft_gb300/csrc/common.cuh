@@ -147,6 +147,9 @@ struct StressArgs {
 // serves crystals with 12 slip systems, launch_stress48 those with 48 (BCC48).
 cudaError_t launch_stress(const StressArgs& a, bool warm, cudaStream_t s);
 cudaError_t launch_stress48(const StressArgs& a, bool warm, cudaStream_t s);
+// the 6-system (hcp6, hcp18) and 1-system (single) crystals (stress6.cu, stress1.cu)
+cudaError_t launch_stress6(const StressArgs& a, bool warm, cudaStream_t s);
+cudaError_t launch_stress1(const StressArgs& a, bool warm, cudaStream_t s);
 // MTS-hardened 12-system crystals (stress_mts.cu)
 cudaError_t launch_stress_mts(const StressArgs& a, bool warm, cudaStream_t s);
 // Ma-Roters-Raabe / ORNL 12-system crystals (stress_mrr.cu / stress_ornl.cu; warm is ignored: no

@@ -15,7 +15,8 @@
 
 // Slip systems of the crystals this translation unit serves: 12 here (fcc, bcc, roters,
 // bcc12: the slip table is the grid's, in the crystal records);
-// stress48.cu compiles this file again with CPFFT_NSLIP 48 (BCC {110},{112},{123}<111>).
+// stress48.cu compiles this file again with CPFFT_NSLIP 48 (BCC {110},{112},{123}<111>),
+// stress6.cu with 6 (hcp6, hcp18) and stress1.cu with 1 (single).
 #ifndef CPFFT_NSLIP
 #define CPFFT_NSLIP 12
 #define CPFFT_STRESS_LAUNCH launch_stress

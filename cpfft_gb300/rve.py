@@ -44,6 +44,15 @@ BCC48_DECK = dict(
     exact_j22=0, **MTS_DEFAULTS,
 )
 
+# An HCP crystal (slip_type 9, hcp6: basal and prismatic <a> systems) with anisotropic
+# type-3 elasticity of titanium's order (C11 = 162.4, C12 = 92.0, C13 = 69.0, C33 = 180.7,
+# C44 = C55 = 46.7 GPa; the reference's type 3 sets C66 = C55) and Voce hardening.
+HCP_VOCE = dict(
+    FCC_VOCE, slip_type=9,
+    C11=162400.0, C12=92000.0, C13=69000.0, C33=180700.0, C44=46700.0, C55=46700.0,
+    tau_y=120.0, tau_v=200.0, theta_0=800.0,
+)
+
 # The material entry of a non-crystal material: not read by the crystal path (the
 # bilinear Mises properties go through Solver.set_mises).
 NOT_A_CRYSTAL = dict(FCC_VOCE, slip_type=0)

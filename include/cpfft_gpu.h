@@ -59,10 +59,13 @@ extern "C" {
 typedef struct cpfft_crystal {
     int    slip_type;      /* 12 systems: 1 = fcc {111}<110>, 2 = bcc {110}<111>,
                               6 = roters ({111}<110> in Roters' order), 7 = bcc12 ({110}<111>,
-                              bcc48's first twelve); 48 systems: 8 = bcc48 {110},{112},{123}
-                              <111> (src/mod_crystals.f:438-811, 812-1207), Voce only; the
-                              crystals of one grid share the slip type; CPFFT_NOT_A_CRYSTAL
-                              (0): another material model (cpfft_set_mises)                   */
+                              bcc48's first twelve); with Voce only: 8 = bcc48 {110},{112},
+                              {123}<111> (48 systems), 3 = single (one system), 9 = hcp6
+                              (basal and prismatic <a>), 10 = hcp18 (the reference assigns
+                              hcp6's six systems and leaves twelve zero vectors, which never
+                              slip: run as hcp6) (src/mod_crystals.f:438-1759); the crystals
+                              of one grid share the slip type; CPFFT_NOT_A_CRYSTAL (0):
+                              another material model (cpfft_set_mises)                       */
     int    elastic_type;   /* 1 isotropic (e,nu), 2 cubic (e,nu,mu), 3 anisotropic (Cij)  */
     double e, nu, mu;
     double C11, C12, C13, C33, C44, C55;

@@ -329,20 +329,43 @@ void roters_systems(double b[12][3], double n[12][3]) {
   for (int s = 0; s < 12; s++)
     for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
 }
+// HCP (slip_type 9 "hcp6", src/mod_crystals.f:1208-1476): basal {0001}<11-20> systems 1-3
+// and prismatic {10-10}<11-20> systems 4-6 in the reference's Cartesian frame (a1 along x,
+// c along z), entries 0, +-0.5, +-1 and +-sqrt(3)/2.  slip_type 10 "hcp18" (:1477-1759)
+// assigns the same six and leaves systems 7-18 (its commented-out pyramidal ones) at the
+// zero of the crystal record: kept here as eighteen systems, twelve of them zero vectors.
+void hcp_systems(double b[][3], double n[][3]) {
+  const double r = std::sqrt(3.0) / 2.0;
+  const double B[6][3] = {{0.5, -r, 0.0}, {0.5, r, 0.0}, {-1.0, 0.0, 0.0},
+                          {1.0, 0.0, 0.0}, {0.5, r, 0.0}, {-0.5, r, 0.0}};
+  const double Nn[6][3] = {{0.0, 0.0, 1.0}, {0.0, 0.0, 1.0}, {0.0, 0.0, 1.0},
+                           {0.0, 1.0, 0.0}, {-r, 0.5, 0.0}, {-r, -0.5, 0.0}};
+  for (int s = 0; s < 6; s++)
+    for (int k = 0; k < 3; k++) { b[s][k] = B[s][k]; n[s][k] = Nn[s][k]; }
+}
 void crystal_finalize(const cpfft_crystal& p, Crys& c) {
   c.p = p;
   double b[12][3], n[12][3];
   c.ns = 12;
+  std::memset(c.b, 0, sizeof(c.b));
+  std::memset(c.n, 0, sizeof(c.n));
   switch (p.slip_type) {
     case 8: c.ns = 48; bcc48_systems(c.b, c.n); break;
     case 7: bcc48_systems(c.b, c.n); break;  // bcc12: bcc48's first twelve (:705-811)
-    case 2: bcc_systems(b, n); break;
-    case 6: roters_systems(b, n); break;
-    default: fcc_systems(b, n); break;
-  }
-  if (p.slip_type != 8 && p.slip_type != 7) {
-    std::memcpy(c.b, b, sizeof(b));
-    std::memcpy(c.n, n, sizeof(n));
+    case 3:  // single (:594-603): direction x on the plane normal to y
+      c.ns = 1;
+      c.b[0][0] = 1.0;
+      c.n[0][1] = 1.0;
+      break;
+    case 9: c.ns = 6; hcp_systems(c.b, c.n); break;
+    case 10: c.ns = 18; hcp_systems(c.b, c.n); break;
+    default:  // the 12-system tables
+      if (p.slip_type == 2) bcc_systems(b, n);
+      else if (p.slip_type == 6) roters_systems(b, n);
+      else fcc_systems(b, n);
+      std::memcpy(c.b, b, sizeof(b));
+      std::memcpy(c.n, n, sizeof(n));
+      break;
   }
   // the forest and parallel projections of mm10_mrr_GH's tables (mm10_mrr_GHfcc, GHbcc,
   // GHfcc12, GHbcc12, src/mm10_e.f:16-1424):

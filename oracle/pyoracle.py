@@ -335,7 +335,7 @@ def polar(F):
 
 def crystal_setup(crystal, kocks):
     c = crystal_array([crystal])
-    ns = 48 if crystal.get("slip_type", 1) == 8 else 12
+    ns = {8: 48, 3: 1, 9: 6, 10: 18}.get(crystal.get("slip_type", 1), 12)
     C = np.zeros(36)
     ms = np.zeros(6 * ns)
     qs = np.zeros(3 * ns)

@@ -64,7 +64,7 @@ def test_init_rejects_bad_arguments(gpulib):
     assert L.cpfft_init(2, mlp, kap, cr, 1, -1.0, 0) == -5      # tstep
     assert L.cpfft_init(2, mlp, kap, cr, 1, 1.0, 7) == -5       # mapping
     bad = dict(rve.FCC_VOCE)
-    bad["slip_type"] = 3  # single: not supported
+    bad["slip_type"] = 11  # halite: no slip table
     assert L.cpfft_init(2, mlp, kap, gpulib.crystal_struct([bad]), 1, 1.0, 0) == -5
     ml2 = ml.copy()
     ml2[3] = 5

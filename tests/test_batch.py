@@ -80,7 +80,7 @@ def test_batch_equals_solo(gpulib, form):
 
 def test_batch_reports_errors(gpulib):
     d = rves([(8, 3, 46, gpulib.G_CENTERED)], 1)
-    d[0]["crystals"] = [dict(d[0]["crystals"][0], slip_type=3)]  # single: cpfft_init refuses
+    d[0]["crystals"] = [dict(d[0]["crystals"][0], slip_type=11)]  # halite: cpfft_init refuses
     with pytest.raises(gpulib.CpfftError):
         gpulib.batch_solve(d, precision=gpulib.PREC_FP64, nthreads=1)
 

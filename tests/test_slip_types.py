@@ -1,6 +1,9 @@
-"""The cubic slip types besides fcc and bcc48 (src/incrystal.f:64-83): bcc (2, {110}<111>),
-roters (6, the FCC systems in Roters' order) and bcc12 (7, bcc48's first twelve), all with
-12 systems and so served by the 12-system stress kernels and every hardening law.
+"""The slip types besides fcc and bcc48 (src/incrystal.f:64-83): bcc (2, {110}<111>),
+roters (6, the FCC systems in Roters' order) and bcc12 (7, bcc48's first twelve), with 12
+systems and so served by the 12-system stress kernels and every hardening law; single
+(3, one system), hcp6 (9, basal and prismatic) and hcp18 (10: the reference assigns only
+hcp6's six systems and leaves twelve zero vectors), with Voce hardening (the reference's
+MRR / ORNL interaction tables exist for the cubic types only, src/mm10_e.f:16-38).
 
 The oracle's tables and interaction matrices against the reference's own
 (tests/golden/slip_tables.npz, read from src/mod_crystals.f and src/mm10_e.f by
@@ -32,7 +35,7 @@ def schmid(b, n, kocks):
     return ms, qs
 
 
-@pytest.mark.parametrize("slip_type", [1, 2, 6, 7, 8])
+@pytest.mark.parametrize("slip_type", [1, 2, 3, 6, 7, 8, 9, 10])
 def test_oracle_slip_tables_match_the_reference(oracle, slip_type):
     cr = dict(rve.BCC48_DECK if slip_type == 8 else rve.FCC_VOCE, slip_type=slip_type)
     _, ms, qs = oracle.crystal_setup(cr, KOCKS)
@@ -62,11 +65,31 @@ def test_library_refuses_mixed_and_unknown_slip_types(gpulib):
     mixed = gpulib.crystal_struct([dict(rve.FCC_VOCE), dict(rve.FCC_VOCE, slip_type=2)])
     assert L.cpfft_init(N, mlp, kap, mixed, 2, 1.0, 0) == -5
     assert b"share the slip type" in L.cpfft_last_error()
-    for bad in (3, 9, 10, 11):       # single, hcp6, hcp18, halite
+    for bad in (4, 5, 11, 12):       # no table (halite, 11, has a keyword but none)
         cr = gpulib.crystal_struct([dict(rve.FCC_VOCE, slip_type=bad)] * 2)
         assert L.cpfft_init(N, mlp, kap, cr, 2, 1.0, 0) == -5, bad
-    mrr48 = gpulib.crystal_struct([dict(rve.MRR_FCC, slip_type=8)] * 2)
-    assert L.cpfft_init(N, mlp, kap, mrr48, 2, 1.0, 0) == -5
+    # MTS and the dislocation-density laws need a 12-system type
+    for law, st in ((rve.MRR_FCC, 8), (rve.MRR_FCC, 9), (rve.ORNL_FCC, 3), (rve.MTS_FCC, 10)):
+        cr = gpulib.crystal_struct([dict(law, slip_type=st)] * 2)
+        assert L.cpfft_init(N, mlp, kap, cr, 2, 1.0, 0) == -5, (law["h_type"], st)
+
+
+def test_hcp18_is_hcp6_with_twelve_null_systems(oracle):
+    """The oracle restates hcp18 with its eighteen systems; the twelve zero vectors add
+    exact zeros, so every output equals hcp6's bit for bit (the library runs hcp18 grids
+    on the 6-system kernel)."""
+    I3 = np.eye(3)
+    F0 = I3
+    h6 = h18 = None
+    for step in (1, 2, 3):
+        F1 = F0 + 1.5e-3 * np.array([[1.0, 0.2, 0.0], [0.1, -0.5, 0.3], [0.0, 0.2, -0.5]])
+        a = oracle.voxel_update(rve.HCP_VOCE, KOCKS, 1.0, step, 1, F0, F1, h6)
+        b = oracle.voxel_update(dict(rve.HCP_VOCE, slip_type=10), KOCKS, 1.0, step, 1, F0, F1,
+                                h18)
+        assert a["iters"] > 0
+        for k in ("P", "A", "hist"):
+            assert np.array_equal(a[k], b[k]), (step, k)
+        h6, h18, F0 = a["hist"], b["hist"], F1
 
 
 def per_voxel_rel(a, b):
@@ -78,7 +101,10 @@ CASES = {"bcc_voce": dict(rve.FCC_VOCE, slip_type=2),
          "roters_voce": dict(rve.FCC_VOCE, slip_type=6),
          "bcc12_voce": dict(rve.FCC_VOCE, slip_type=7),
          "bcc_mrr": dict(rve.MRR_FCC, slip_type=2),
-         "bcc12_mts": dict(rve.MTS_FCC, slip_type=7)}
+         "bcc12_mts": dict(rve.MTS_FCC, slip_type=7),
+         "single_voce": dict(rve.FCC_VOCE, slip_type=3),
+         "hcp6_voce": rve.HCP_VOCE,
+         "hcp18_voce": dict(rve.HCP_VOCE, slip_type=10)}
 
 
 @pytest.mark.gpu
@@ -115,7 +141,7 @@ def test_gpu_stress_update_parity(gpulib, oracle, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["bcc_voce", "roters_voce"])
+@pytest.mark.parametrize("case", ["bcc_voce", "roters_voce", "hcp6_voce", "hcp18_voce"])
 def test_gpu_load_steps(gpulib, oracle, case):
     """Whole load steps (7^3, stretch 1e-3 a step): P_bar and Newton counts."""
     N = 7
