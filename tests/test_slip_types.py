@@ -92,6 +92,50 @@ def test_hcp18_is_hcp6_with_twelve_null_systems(oracle):
         h6, h18, F0 = a["hist"], b["hist"], F1
 
 
+def hexagonal_rotations():
+    """The 12 proper rotations of the hexagonal group about the crystal's c axis (z)."""
+    out = []
+    for k in range(6):
+        t = np.pi / 3 * k
+        S = np.array([[np.cos(t), -np.sin(t), 0.0], [np.sin(t), np.cos(t), 0.0], [0, 0, 1.0]])
+        out += [S, np.diag([1.0, -1.0, -1.0]) @ S]
+    return out
+
+
+def hex_departure(oracle, cr):
+    """Largest relative change of P and dP/dF over two plastic steps when the lattice
+    orientation g is replaced by S g, S a hexagonal rotation."""
+    g = rve.kocks_matrix(KOCKS)[0]
+    I3 = np.eye(3)
+    F = I3 + 2e-3 * np.array([[1.0, 0.3, -0.2], [0.1, -0.4, 0.25], [-0.15, 0.2, -0.5]])
+
+    def run(kocks):
+        a = oracle.voxel_update(cr, kocks, 1.0, 1, 1, I3, F)
+        b = oracle.voxel_update(cr, kocks, 1.0, 2, 1, F, F @ F, a["hist"])
+        assert a["iters"] > 0
+        return a, b
+
+    a1, a2 = run(KOCKS)
+    worst = 0.0
+    for S in hexagonal_rotations():
+        b1, b2 = run(rve.matrix_to_kocks((S @ g)[None])[0])
+        for x, y in ((b1["P"], a1["P"]), (b1["A"], a1["A"]), (b2["P"], a2["P"])):
+            worst = max(worst, np.abs(x - y).max() / np.abs(y).max())
+    return worst
+
+
+@pytest.mark.parametrize("slip_type", [9, 10])
+def test_hcp_is_hexagonally_symmetric(oracle, slip_type):
+    """With transversely isotropic elasticity (C44 = C55 = (C11 - C12) / 2, so that the
+    reference's C66 = C55 is the hexagonal value) the basal and prismatic systems make the
+    response invariant under the hexagonal rotations, to round-off.  With C55 away from
+    (C11 - C12) / 2 the reference's C66 = C55 breaks that symmetry."""
+    c11, c12 = rve.HCP_VOCE["C11"], rve.HCP_VOCE["C12"]
+    ti = dict(rve.HCP_VOCE, slip_type=slip_type, C44=(c11 - c12) / 2, C55=(c11 - c12) / 2)
+    assert hex_departure(oracle, ti) < 1e-13
+    assert hex_departure(oracle, dict(rve.HCP_VOCE, slip_type=slip_type)) > 1e-6
+
+
 def per_voxel_rel(a, b):
     scale = np.maximum(np.abs(b).max(axis=0), 1e-6 * np.abs(b).max())
     return (np.abs(a - b).max(axis=0) / scale).max()
