@@ -147,6 +147,7 @@ SIGNATURES = {
     "cpfft_write_disp_flat": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_ouresult": (_I, [_I, _D, _D, _D, ctypes.c_char_p, ctypes.c_char_p]),
     "cpfft_batch_solve": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I, _D, _D, _I, _I]),
+    "cpfft_slip_systems": (_I, [_I, _DP, _DP]),
     "cpfft_batch_solve_newton": (_I, [ctypes.POINTER(Rve), _I, _I, _I, _I, _I,
                                       ctypes.POINTER(Newton), _D, _D, _I, _I]),
     "cpfft_stress_update": (_I, [_I, _I, _DP, _DP, _DP, _DP]),
@@ -550,6 +551,16 @@ def batch_solve(rves, precision=PREC_MIXED, options=0, precond=PRECOND_REFERENCE
                  cg_iters=r.cg_iters, seconds=r.seconds, error=r.error.decode())
     _check(rc, "cpfft_batch_solve")
     return out
+
+
+def slip_systems(slip_type):
+    """The slip directions and plane normals (systems x 3, crystal frame) the stress
+    kernels use for a slip_type (cpfft_slip_systems; host only)."""
+    L = load_library()
+    ns = _check(L.cpfft_slip_systems(int(slip_type), None, None), "slip_systems")
+    b, n = np.zeros((ns, 3)), np.zeros((ns, 3))
+    _check(L.cpfft_slip_systems(int(slip_type), _dp(b), _dp(n)), "slip_systems")
+    return b, n
 
 
 def format_e15(values):

@@ -2540,6 +2540,21 @@ int cpfft_hist_words(void) {
   return g_ctx->hist_words;
 }
 
+int cpfft_slip_systems(int slip_type, double* b, double* n) {
+  double bb[48][3], nn[48][3];
+  const int ns = slip_geometry(slip_type, bb, nn);
+  if (!ns) {
+    cpfft_set_error("cpfft_slip_systems: slip_type %d has no slip table here", slip_type);
+    return CPFFT_ERR_BAD_ARG;
+  }
+  for (int s = 0; s < ns; s++)
+    for (int i = 0; i < 3; i++) {
+      if (b) b[3 * s + i] = bb[s][i];
+      if (n) n[3 * s + i] = nn[s][i];
+    }
+  return ns;
+}
+
 int cpfft_commit_step(void) {
   TRY(need_ctx());
   Ctx* c = g_ctx;

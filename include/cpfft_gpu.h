@@ -467,6 +467,12 @@ int cpfft_sync_to_host(double* Fn1, double* Pn1, double* history);
 /* Words per voxel of the current context's history: CPFFT_HIST_WORDS, or
  * CPFFT_HIST_WORDS_MRR on a grid of Ma-Roters-Raabe crystals; negative on error. */
 int cpfft_hist_words(void);
+/* The slip systems the stress kernels use for a slip_type (host only, no context):
+ * returns their number (1, 6, 12 or 48; hcp18 gives hcp6's six, its other twelve being
+ * zero vectors in the reference) and fills the unit directions b and plane normals n
+ * (systems x 3, row-major, crystal frame) when not NULL; CPFFT_ERR_BAD_ARG for a type
+ * without a table. */
+int cpfft_slip_systems(int slip_type, double* b, double* n);
 
 /* ---- element result files (ouelestr, src/ouresult.f:140-300) --------------------------
  * The per-voxel lines of the flat text files wesNNNNN_text (quantity 2: the unrotated

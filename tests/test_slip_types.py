@@ -44,6 +44,24 @@ def test_oracle_slip_tables_match_the_reference(oracle, slip_type):
     assert np.abs(ms - ms_ref).max() < 1e-15 and np.abs(qs - qs_ref).max() < 1e-15
 
 
+@pytest.mark.parametrize("slip_type", [1, 2, 3, 6, 7, 8, 9, 10])
+def test_library_slip_tables_match_the_reference(gpulib, slip_type):
+    """The tables the library hands its stress kernels (cpfft_slip_systems, host only)
+    equal the reference's bit for bit; hcp18 runs as its six assigned systems."""
+    b, n = gpulib.slip_systems(slip_type)
+    b_ref, n_ref = GOLDEN["b%d" % slip_type], GOLDEN["n%d" % slip_type]
+    if slip_type == 10:
+        assert not b_ref[6:].any() and not n_ref[6:].any()
+        b_ref, n_ref = b_ref[:6], n_ref[:6]
+    assert np.array_equal(b, b_ref) and np.array_equal(n, n_ref)
+
+
+def test_library_slip_tables_refuse_unknown_types(gpulib):
+    for bad in (0, 4, 11):
+        with pytest.raises(gpulib.CpfftError):
+            gpulib.slip_systems(bad)
+
+
 @pytest.mark.parametrize("slip_type", TYPES12)
 def test_oracle_interaction_matches_the_reference(oracle, slip_type):
     """mm10_mrr_GH's table for the slip type equals the geometric forest / parallel
