@@ -79,3 +79,55 @@ def test_two_rank_replicas(tmp_path, oracle):
     assert (int(res[0]["lo"]), int(res[0]["hi"]), int(res[1]["lo"]), int(res[1]["hi"])) == (0, 2, 2, 4)
     ref = _solve_replica(102)
     assert np.array_equal(res[1]["pbars"][0], ref)
+
+
+def _config4_rank(rank, world, port, outdir):
+    """bench.py's 48-RVE arm on one gloo rank, with the library's batch call replaced by a
+    stand-in that takes 10 ms per load step and reports N^3 x 4 stress updates per step
+    of each RVE (the arm's partition, barriers and reduction are what is under test)."""
+    import contextlib
+    import json
+    import sys
+    import time
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    import cpfft_gb300 as cp
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    seen = []
+
+    def batch_stub(rves, **kw):
+        time.sleep(0.01 * rves[0]["nsteps"])
+        seen.append([r["N"] for r in rves])
+        return [{"voxel_updates": r["N"] ** 3 * 4 * r["nsteps"]} for r in rves]
+
+    cp.load_library = lambda: None
+    cp.batch_solve = batch_stub
+    args = bench.make_parser().parse_args(["--workload", "config4", "--steps", "2",
+                                           "--warmup", "1", "--batch-threads", "1"])
+    out = os.path.join(outdir, f"c4_rank{rank}.txt")
+    try:
+        with open(out, "w") as f, contextlib.redirect_stdout(f):
+            assert bench.config4_arm(args) == 0
+        with open(os.path.join(outdir, f"c4_seen{rank}.json"), "w") as f:
+            json.dump(seen, f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_config4_partitioned_over_two_ranks(tmp_path):
+    """`bench.py --workload config4` under two ranks: each solves its own 24 RVEs, and
+    rank 0's line reports the units of all 48 over the slowest rank's time."""
+    import json
+    world = 2
+    mp.spawn(_config4_rank, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    seen = [json.load(open(tmp_path / f"c4_seen{r}.json")) for r in range(world)]
+    Ns = (24, 32, 48, 64)
+    for r, batches in enumerate(seen):
+        assert all(b == [Ns[k % 4] for k in range(24 * r, 24 * r + 24)] for b in batches)
+    assert open(tmp_path / "c4_rank1.txt").read() == ""
+    line = json.loads(open(tmp_path / "c4_rank0.txt").read())
+    all_units = sum(Ns[k % 4] ** 3 for k in range(48)) * 4 * 2    # 48 RVEs, 2 timed steps
+    assert line["n_gpus"] == 2 and line["by_threads"]["1"]["voxel_updates"] == all_units
+    assert 9.0 < line["ms_per_step"] < 500.0     # 10 ms a load step in the stand-in
